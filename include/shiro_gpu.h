@@ -1,0 +1,344 @@
+/*
+ * shiro_gpu.h - C ABI of the GB300 path-tracing backend for Shiro.
+ *
+ * This is the drop-in boundary that replaces Shiro's OptiX backend behind
+ * shiro::backend::RenderBackend (include/shiro/backend/RenderBackend.h:28-34 in
+ * ichin0se/Shiro).  The reference has no C ABI of its own: its backends are C++
+ * classes called through
+ *     virtual BackendStatus GetStatus() const;                    (RenderBackend.h:32)
+ *     virtual FrameBuffer RenderSampleBatch(const RenderRequest&); (RenderBackend.h:33)
+ *     bool SupportsScene(const Scene&) const;                      (OptixBackend.h:16)
+ * The entry points below are what a C++ adapter (shiro_gb300/backend/GpuBackend.cpp)
+ * binds to implement that class; every struct is plain data (pointers, sizes,
+ * floats), no C++ or torch types.
+ *
+ * Ownership: the caller owns every host array passed in; the context owns all
+ * device memory it allocates.  Calls on one context must be serialised by the
+ * caller (the reference serialises RenderSampleBatch with a mutex,
+ * OptixBackend.h:24-26).  Errors are reported as a negative status; the
+ * message is available from shiro_gpu_last_error().  The backend never falls
+ * back to a CPU path: a missing device or a failed launch is an error.
+ */
+#ifndef SHIRO_GPU_H_
+#define SHIRO_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SHIRO_GPU_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------- */
+#define SHIRO_OK 0
+#define SHIRO_ERR_INVALID_ARGUMENT (-1)
+#define SHIRO_ERR_NO_DEVICE (-2)
+#define SHIRO_ERR_CUDA (-3)
+#define SHIRO_ERR_OUT_OF_MEMORY (-4)
+#define SHIRO_ERR_UNSUPPORTED_SCENE (-5)
+#define SHIRO_ERR_CANCELLED (-6)
+#define SHIRO_ERR_NO_SCENE (-7)
+#define SHIRO_ERR_TIMEOUT (-8)
+#define SHIRO_ERR_DEVICE_CHECK (-9)
+
+/* ---- enums mirrored from shiro/render/Renderer.h ------------------------- */
+/* BackendKind, Renderer.h:23-27 */
+#define SHIRO_BACKEND_CPU 0
+#define SHIRO_BACKEND_GPU 1
+#define SHIRO_BACKEND_HYBRID 2
+/* EnvironmentMapLayout, Renderer.h:17-21 */
+#define SHIRO_ENV_LAYOUT_AUTOMATIC 0
+#define SHIRO_ENV_LAYOUT_LATLONG 1
+#define SHIRO_ENV_LAYOUT_ANGULAR 2
+
+/* Render flags (ShiroRenderDesc.flags). */
+/* Sample the dome light by binary search over the reference's row / column
+ * CDFs (EnvironmentMap.cpp:109-163) instead of the O(1) alias table.  Both
+ * give the same per-pixel probability; the CDF mode also maps a given 2-D
+ * sample to the same texel as the reference does, so paths match the CPU
+ * tracer sample for sample. */
+#define SHIRO_RENDER_ENV_CDF 0x1u
+/* Differentiable mode: the direct-sample (24) and throughput (12) clamps of
+ * the reference (CpuPathTracer.cpp:63-64) are disabled, in the forward and
+ * in the adjoint, so that the rendered estimate is smooth in the parameters. */
+#define SHIRO_RENDER_NO_CLAMP 0x2u
+
+/* ---- scene snapshot (shiro/render/Renderer.h:29-133) --------------------- */
+
+/* PbrMaterial, Renderer.h:56-102; same fields in the same order. Booleans are
+ * uint32 (0/1). */
+typedef struct ShiroMaterialDesc {
+    float base_color[3];
+    float emission_color[3];
+    float specular_color[3];
+    float transmission_color[3];
+    float transmission_scatter[3];
+    float coat_color[3];
+    float subsurface_color[3];
+    float subsurface_radius[3];
+    float sheen_color[3];
+    float normal_override[3];
+    float coat_normal_override[3];
+    float tangent_override[3];
+    float base_weight;
+    float emission_strength;
+    float specular_weight;
+    float metallic;
+    float roughness;
+    float diffuse_roughness;
+    float opacity;
+    float specular_anisotropy;
+    float specular_rotation;
+    float coat_weight;
+    float coat_roughness;
+    float coat_ior;
+    float coat_anisotropy;
+    float coat_rotation;
+    float sheen;
+    float sheen_roughness;
+    float subsurface;
+    float subsurface_scale;
+    float subsurface_anisotropy;
+    float transmission;
+    float transmission_depth;
+    float transmission_scatter_anisotropy;
+    float transmission_dispersion;
+    float transmission_extra_roughness;
+    float ior;
+    float coat_affect_color;
+    float coat_affect_roughness;
+    float thin_film_thickness;
+    float thin_film_ior;
+    uint32_t thin_walled;
+    uint32_t has_normal_override;
+    uint32_t has_coat_normal_override;
+    uint32_t has_tangent_override;
+} ShiroMaterialDesc;
+
+/* TriangleMesh, Renderer.h:104-109.  positions / normals are xyz float
+ * triples; normals may be absent (normal_count 0) and are only used when
+ * normal_count == vertex_count, as in TriangleShadingNormal
+ * (CpuPathTracer.cpp:156). */
+typedef struct ShiroMeshDesc {
+    const float* positions;
+    uint32_t vertex_count;
+    const float* normals;
+    uint32_t normal_count;
+    const uint32_t* indices;
+    uint32_t index_count;
+    uint32_t material_index;
+} ShiroMeshDesc;
+
+/* DirectionalLight, Renderer.h:111-114 */
+typedef struct ShiroDistantLightDesc {
+    float direction[3];
+    float radiance[3];
+} ShiroDistantLightDesc;
+
+/* DomeLight, Renderer.h:116-124.  The texture is passed as decoded RGB float
+ * pixels (row-major, env_width * env_height * 3), i.e. the contents of
+ * EnvironmentMap::Pixels() (EnvironmentMap.h:24); env_pixels NULL means a
+ * constant dome (DomeLight without environment). */
+typedef struct ShiroDomeLightDesc {
+    float radiance[3];
+    float right[3];
+    float up[3];
+    float forward[3];
+    uint32_t layout; /* SHIRO_ENV_LAYOUT_* */
+    uint32_t env_width;
+    uint32_t env_height;
+    const float* env_pixels;
+} ShiroDomeLightDesc;
+
+/* Scene, Renderer.h:126-133 */
+typedef struct ShiroSceneDesc {
+    const ShiroMaterialDesc* materials;
+    uint32_t material_count;
+    const ShiroMeshDesc* meshes;
+    uint32_t mesh_count;
+    const ShiroDistantLightDesc* distant_lights;
+    uint32_t distant_light_count;
+    const ShiroDomeLightDesc* dome_lights;
+    uint32_t dome_light_count;
+    float environment_top[3];
+    float environment_bottom[3];
+} ShiroSceneDesc;
+
+/* Camera, Renderer.h:47-54 */
+typedef struct ShiroCameraDesc {
+    float position[3];
+    float forward[3];
+    float right[3];
+    float up[3];
+    float vertical_fov_degrees;
+    float aspect_ratio;
+} ShiroCameraDesc;
+
+/* RenderSettings, Renderer.h:29-45 (booleans as uint32). */
+typedef struct ShiroSettingsDesc {
+    uint32_t width;
+    uint32_t height;
+    uint32_t samples_per_pixel;
+    uint32_t samples_per_update;
+    uint32_t dome_light_samples;
+    uint32_t max_depth;
+    uint32_t diffuse_depth;
+    uint32_t specular_depth;
+    uint32_t thread_limit;
+    uint32_t max_subdiv_level;
+    uint32_t backend;
+    uint32_t background_visible;
+    uint32_t enable_headlight;
+    uint32_t enable_caustics;
+    uint32_t enable_sss;
+} ShiroSettingsDesc;
+
+/* RenderRequest, RenderBackend.h:12-19 (scene is bound separately through
+ * shiro_gpu_upload_scene; the cancel flag is a call argument). */
+typedef struct ShiroRenderDesc {
+    ShiroCameraDesc camera;
+    ShiroSettingsDesc settings;
+    uint32_t sample_start;
+    uint32_t sample_count;
+    uint32_t flags; /* SHIRO_RENDER_* */
+    uint32_t reserved;
+} ShiroRenderDesc;
+
+/* FrameBuffer, FrameBuffer.h:10-37: beauty RGBA (alpha = hit fraction),
+ * albedo RGB, normal RGB (n * 0.5 + 0.5), depth (min hit distance, +inf on
+ * miss); row-major y * width + x.  on_device != 0 means the four pointers
+ * are device pointers (no host copy is made). */
+typedef struct ShiroAovs {
+    float* beauty;
+    float* albedo;
+    float* normal;
+    float* depth;
+    uint32_t on_device;
+    uint32_t reserved;
+} ShiroAovs;
+
+/* BackendStatus, RenderBackend.h:21-26 */
+typedef struct ShiroBackendStatus {
+    uint32_t kind; /* SHIRO_BACKEND_* */
+    uint32_t available;
+    uint32_t uses_gpu;
+    uint32_t device_count;
+    char name[32];
+    char device_name[96];
+    int32_t compute_major;
+    int32_t compute_minor;
+} ShiroBackendStatus;
+
+typedef struct ShiroGpuContext ShiroGpuContext;
+
+/* ---- entry points -------------------------------------------------------- */
+
+/* BackendStatus RenderBackend::GetStatus() (RenderBackend.h:32;
+ * OptixBackend.cpp:1036-1060): device present and an sm_103 part. */
+int shiro_gpu_status(ShiroBackendStatus* out);
+
+/* Creates a context on a device (OptixBackend::EnsureRuntime,
+ * OptixBackend.cpp:1071-1139, minus the NVRTC / OptiX pipeline). */
+int shiro_gpu_create(int device, ShiroGpuContext** out);
+void shiro_gpu_destroy(ShiroGpuContext* ctx);
+
+/* Last error message of this context (or of the last failed create when ctx
+ * is NULL). Never NULL. */
+const char* shiro_gpu_last_error(const ShiroGpuContext* ctx);
+
+/* Renders on this CUDA stream (cudaStream_t cast to void*; NULL = the
+ * context's own stream). */
+int shiro_gpu_set_stream(ShiroGpuContext* ctx, void* stream);
+
+/* bool SupportsScene(const Scene&) (OptixBackend.h:16, Renderer.cpp:20).
+ * Returns 1 when every material and light of the scene is handled by the GPU
+ * integrator, 0 otherwise (the renderer then falls back to the CPU tracer,
+ * Renderer.cpp:19-30).  reason (may be NULL) receives a short explanation. */
+int shiro_gpu_supports_scene(const ShiroSceneDesc* scene, char* reason, size_t reason_size);
+
+/* Uploads a scene snapshot: flattens meshes, builds the device BVH, the
+ * material table and the dome-light importance tables (CDF and alias).
+ * Counterpart of OptixBackend::UploadSceneData (OptixBackend.cpp:751-1026) and
+ * CpuPathTracer::BuildAccelerationScene (CpuPathTracer.cpp:477-598). */
+int shiro_gpu_upload_scene(ShiroGpuContext* ctx, const ShiroSceneDesc* scene);
+
+/* FrameBuffer RenderSampleBatch(const RenderRequest&)
+ * (RenderBackend.h:33; CpuPathTracer.cpp:2043-2170) with the plain
+ * one-thread-per-path megakernel.  cancel (may be NULL) is polled between
+ * launches; a set flag returns SHIRO_ERR_CANCELLED and leaves the AOVs
+ * cleared, as the reference discards a cancelled batch
+ * (RenderParam.cpp:791-798). */
+int shiro_gpu_render(ShiroGpuContext* ctx, const ShiroRenderDesc* request,
+                     const volatile int* cancel, ShiroAovs* out);
+
+/* Batched wavefront form: renders `count` requests (each with its own
+ * camera, resolution, spp and depth) against the uploaded scene with
+ * persistent stage kernels and per-stage queues.  Results equal those of
+ * shiro_gpu_render for each request. */
+int shiro_gpu_render_batch(ShiroGpuContext* ctx, const ShiroRenderDesc* requests, uint32_t count,
+                           const volatile int* cancel, ShiroAovs* outs);
+
+/* Wavefront tuning (tile of paths in flight per wave and block sizes). Zero
+ * fields leave the current value. The autotuner sets these itself when
+ * shiro_gpu_autotune is called. */
+typedef struct ShiroWavefrontConfig {
+    uint32_t paths_in_flight;
+    uint32_t extend_block;
+    uint32_t shade_block;
+    uint32_t shadow_block;
+    uint32_t use_graph;
+    uint32_t reserved[3];
+} ShiroWavefrontConfig;
+int shiro_gpu_get_wavefront_config(const ShiroGpuContext* ctx, ShiroWavefrontConfig* out);
+int shiro_gpu_set_wavefront_config(ShiroGpuContext* ctx, const ShiroWavefrontConfig* cfg);
+/* Times candidate configurations on `request` and keeps the fastest. */
+int shiro_gpu_autotune(ShiroGpuContext* ctx, const ShiroRenderDesc* request, ShiroWavefrontConfig* chosen);
+
+/* Differentiable form.  Parameters live on the device (float32):
+ *   base_color [material_count * 3], roughness [material_count],
+ *   metallic [material_count], env texels [env_height * env_width * 3] of
+ *   dome light 0.
+ * shiro_gpu_set_params overrides those material fields / texels of the
+ * uploaded scene (and rebuilds the dome importance table when env changes).
+ * shiro_gpu_adjoint replays every path of `request` from its QMC seed and
+ * accumulates d(sum over pixels of d_beauty . beauty)/d(param) into the
+ * gradient buffers (added, not overwritten).  All pointers are device
+ * pointers; any may be NULL to skip that parameter group. */
+int shiro_gpu_set_params(ShiroGpuContext* ctx, const float* base_color, const float* roughness,
+                         const float* metallic, const float* env_rgb);
+int shiro_gpu_adjoint(ShiroGpuContext* ctx, const ShiroRenderDesc* request, const float* d_beauty,
+                      float* d_base_color, float* d_roughness, float* d_metallic, float* d_env_rgb);
+
+/* Per-path debugging / parity probes (device or host arrays per on_device).
+ * Primary closest hit of every pixel's camera ray for sample sample_start:
+ * prim_out[i] = global triangle index (meshes in order, triangles in order)
+ * or 0xffffffff on a miss; t_out[i] = hit distance. */
+int shiro_gpu_primary_hits(ShiroGpuContext* ctx, const ShiroRenderDesc* request, uint32_t* prim_out,
+                           float* t_out, uint32_t on_device);
+/* Closest hit / occlusion for arbitrary rays: origins, directions [n*3];
+ * t_max [n] (FLT_MAX for unbounded).  prim_out, t_out as above;
+ * occluded_out[i] = 1 when any hit in [1e-4, t_max]. */
+int shiro_gpu_trace_rays(ShiroGpuContext* ctx, const float* origins, const float* directions,
+                         const float* t_max, uint32_t n, uint32_t* prim_out, float* t_out,
+                         uint32_t* occluded_out);
+
+/* Statistics of the last render (for the roofline and tests). */
+typedef struct ShiroRenderStats {
+    double kernel_ms;           /* device time of the render kernels */
+    uint64_t paths;             /* paths traced */
+    uint64_t kernel_launches;   /* kernels launched by the last call */
+    uint64_t bvh_nodes;         /* BVH nodes of the uploaded scene */
+    uint64_t triangles;         /* triangles of the uploaded scene */
+    uint32_t bvh_depth;
+    uint32_t bvh_max_leaf;
+    uint64_t device_bytes;      /* device memory held by the context */
+} ShiroRenderStats;
+int shiro_gpu_last_stats(const ShiroGpuContext* ctx, ShiroRenderStats* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SHIRO_GPU_H_ */

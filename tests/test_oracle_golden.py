@@ -1,0 +1,174 @@
+"""The CPU oracle (oracle/port) against golden vectors produced by the
+reference's own code (tests/golden/gen_golden.py).
+
+On x86-64 - where the fixtures were generated with the same libm - every
+value must be bit-identical.  Elsewhere transcendental functions may differ in
+the last ulp, so a tight tolerance is used instead.
+"""
+import platform
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import api
+from conftest import golden
+from scene_io import camera_from_array, scene_from_arrays, settings_from_array
+
+EXACT = platform.machine() in ("x86_64", "AMD64")
+
+
+@pytest.fixture(scope="module")
+def port():
+    oracle.build_port()
+    return oracle.port_checker()
+
+
+def assert_same(a, b, rtol=2e-5, atol=1e-6, what=""):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape, what
+    if EXACT:
+        same = (a == b) | (np.isnan(a) & np.isnan(b))
+        assert same.all(), f"{what}: {np.count_nonzero(~same)} of {a.size} values differ"
+    else:
+        np.testing.assert_allclose(a, b, rtol=rtol, atol=atol, err_msg=what)
+
+
+def test_sampler_kat(port):
+    g = golden("sampler_kat.npz")
+    out = api.sampler(port, g["px"], g["py"], g["index"], g["branch"])
+    # integer hash + IEEE float ops only: bit-exact on every platform
+    assert (out.view(np.uint32) == g["out"].view(np.uint32)).all()
+
+
+def test_sampler_properties(port):
+    n = 4096
+    z = np.zeros(n, np.uint32)
+    idx = np.arange(n, dtype=np.uint32)
+    out = api.sampler(port, z, z, idx, z)
+    assert ((out >= 0) & (out < 1)).all()
+    # dims 0/1 are the R2 sequence: frac(0.5 + a * i)
+    r2 = np.float32(0.5) + np.float32(0.7548776662466927) * idx.astype(np.float32)
+    assert np.array_equal(out[:, 0], r2 - np.floor(r2))
+
+
+def test_camera_rays(port):
+    g = golden("camera_rays.npz")
+    for k in range(int(g["count"])):
+        cam = camera_from_array(g[f"cam{k}"])
+        st = settings_from_array(g[f"settings{k}"])
+        o, d = api.camera_rays(port, cam, st, int(g[f"start{k}"]))
+        assert_same(o, g[f"origins{k}"], what=f"origins{k}")
+        assert_same(d, g[f"dirs{k}"], what=f"dirs{k}")
+
+
+def test_primary_hits(port):
+    g = golden("hits_sphere.npz")
+    scene = scene_from_arrays(g)
+    cam = camera_from_array(g["cam"])
+    st = settings_from_array(g["settings"])
+    for k in range(3):
+        prim, t = api.primary_hits(port, scene, cam, st, int(g[f"start{k}"]))
+        if EXACT:
+            assert np.array_equal(prim, g[f"prim{k}"])
+            assert np.array_equal(t, g[f"t{k}"])
+        else:
+            assert (prim == g[f"prim{k}"]).mean() > 0.999
+
+
+def test_random_rays_bvh_matches_bruteforce_semantics(port):
+    g = golden("hits_sphere.npz")
+    scene = scene_from_arrays(g)
+    prim, t, occ = api.trace_rays(port, scene, g["ray_o"], g["ray_d"], g["ray_tmax"])
+    assert np.array_equal(prim, g["ray_prim"])
+    assert np.array_equal(t, g["ray_t"])
+    assert np.array_equal(occ, g["ray_occ"])
+
+
+def test_bvh_equals_bruteforce_on_field(port):
+    from shiro_gb300 import scenes
+
+    scene = scenes.field_scene(instances=12, levels=3, materials=4, env_width=16, env_height=8, seed=21, plane=10.0)
+    rng = np.random.default_rng(5)
+    n = 20000
+    o = rng.uniform(-5, 5, (n, 3)).astype(np.float32)
+    o[:, 1] = rng.uniform(0.05, 3.0, n)
+    d = rng.normal(size=(n, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    tmax = rng.uniform(0.5, 20.0, n).astype(np.float32)
+    a = api.trace_rays(port, scene, o, d, tmax)
+    b = api.trace_rays(port, scene, o, d, tmax, bruteforce=True)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_bsdf_kat(port):
+    g = golden("bsdf_kat.npz")
+    sc = scene_from_arrays(g)
+    for i, name in enumerate(g["names"]):
+        f, pdf, w = api.bsdf(port, sc.materials[i], g[f"{name}_n"], g[f"{name}_v"], g[f"{name}_l"])
+        assert_same(f, g[f"{name}_f"], rtol=1e-4, atol=1e-6, what=f"{name} f")
+        assert_same(pdf, g[f"{name}_pdf"], rtol=1e-4, atol=1e-6, what=f"{name} pdf")
+        assert_same(w, g[f"{name}_w"], what=f"{name} weights")
+
+
+def test_env_tables_and_queries(port):
+    g = golden("env_kat.npz")
+    row, cond = api.env_tables(port, g["env"])
+    assert_same(row, g["row_cdf"], what="row cdf")
+    assert_same(cond, g["cond_cdf"], what="conditional cdf")
+    for layout, pre in ((1, "ll_"), (2, "ang_")):
+        q = api.env_query(port, g["env"], g["u2"], g["dirs"], layout)
+        for k, v in q.items():
+            assert_same(v, g[pre + k], rtol=1e-4, atol=1e-6, what=pre + k)
+
+
+RENDERS = ["sphere", "rich", "features_gradient_env", "angular_env", "field_small", "sphere_1spp_start5"]
+
+
+@pytest.mark.parametrize("name", RENDERS)
+def test_render_matches_reference(port, name):
+    g = golden(f"render_{name}.npz")
+    scene = scene_from_arrays(g)
+    cam = camera_from_array(g["cam"])
+    st = settings_from_array(g["settings"])
+    fb = api.render(port, scene, cam, st, int(g["start"]), int(g["count"]))
+    if EXACT:
+        for k in ("beauty", "albedo", "normal", "depth"):
+            assert_same(getattr(fb, k), g[k], what=k)
+    else:
+        # ulp-level libm differences can flip a path decision: compare the
+        # image statistically
+        close = np.isclose(fb.beauty, g["beauty"], rtol=1e-3, atol=1e-4).all(1)
+        assert close.mean() > 0.97
+        assert abs(fb.beauty[:, :3].mean() - g["beauty"][:, :3].mean()) < 0.02 * g["beauty"][:, :3].mean() + 1e-4
+
+
+def test_thread_count_invariance(port):
+    g = golden("render_sphere.npz")
+    scene = scene_from_arrays(g)
+    cam = camera_from_array(g["cam"])
+    st = settings_from_array(g["settings"])
+    port.lib.oracle_set_threads(1)
+    try:
+        a = api.render(port, scene, cam, st, 0, 2)
+    finally:
+        port.lib.oracle_set_threads(0)
+    b = api.render(port, scene, cam, st, 0, 2)
+    assert np.array_equal(a.beauty, b.beauty)
+
+
+def test_unsupported_scene_rejected(port):
+    from shiro_gb300 import scenes
+    from shiro_gb300.abi import MarshalledScene
+
+    sc = scenes.sphere_scene(16, 8)
+    sc.materials[0].transmission = 0.5
+    assert port.lib.oracle_supports_scene(MarshalledScene(sc).ref()) == 0
+    sc.materials[0].transmission = 0.0
+    sc.materials[1].emission_strength = 1.0
+    sc.materials[1].emission_color = (1.0, 1.0, 1.0)
+    assert port.lib.oracle_supports_scene(MarshalledScene(sc).ref()) == 0
+    sc.materials[1].emission_strength = 0.0
+    assert port.lib.oracle_supports_scene(MarshalledScene(sc).ref()) == 1
