@@ -1,0 +1,269 @@
+"""Python mirror of shiro::backend::RenderBackend over the GB300 C ABI.
+
+``GpuBackend`` follows the reference's backend interface
+(include/shiro/backend/RenderBackend.h:28-34 and OptixBackend.h:10-27):
+
+* ``get_status()``            -> BackendStatus          (RenderBackend.h:32)
+* ``supports_scene(scene)``   -> bool                   (OptixBackend.h:16)
+* ``render_sample_batch(req)``-> FrameBuffer            (RenderBackend.h:33)
+
+with the same error convention: a failed batch logs to stderr and returns a
+cleared, sized FrameBuffer (OptixBackend.cpp:1142-1155), and a failed
+runtime marks the backend unavailable.  ``render()`` is the strict variant
+that raises.  There is no CPU fallback inside the backend: without the
+native library or a device the backend is unavailable and rendering raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import abi
+from .abi import (Aovs, BackendStatus, Camera, FrameBuffer, MarshalledScene, RenderDesc, RenderSettings, RenderStats,
+                  Scene, WavefrontConfig, render_desc)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libshiro_gpu.so")
+
+_P = C.c_void_p
+_U = C.c_uint32
+
+
+class ShiroGpuError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads libshiro_gpu.so (built by shiro_gb300.build / __graft_entry__.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ShiroGpuError(abi.SHIRO_ERR_NO_DEVICE,
+                            f"native library missing: {path} (run __graft_entry__.build())")
+    lib = C.CDLL(path)
+    sig = {
+        "shiro_gpu_status": ([_P], C.c_int),
+        "shiro_gpu_create": ([C.c_int, _P], C.c_int),
+        "shiro_gpu_destroy": ([_P], None),
+        "shiro_gpu_last_error": ([_P], C.c_char_p),
+        "shiro_gpu_set_stream": ([_P, _P], C.c_int),
+        "shiro_gpu_supports_scene": ([_P, C.c_char_p, C.c_size_t], C.c_int),
+        "shiro_gpu_upload_scene": ([_P, _P], C.c_int),
+        "shiro_gpu_render": ([_P, _P, _P, _P], C.c_int),
+        "shiro_gpu_render_batch": ([_P, _P, _U, _P, _P], C.c_int),
+        "shiro_gpu_get_wavefront_config": ([_P, _P], C.c_int),
+        "shiro_gpu_set_wavefront_config": ([_P, _P], C.c_int),
+        "shiro_gpu_autotune": ([_P, _P, _P], C.c_int),
+        "shiro_gpu_set_params": ([_P, _P, _P, _P, _P], C.c_int),
+        "shiro_gpu_adjoint": ([_P, _P, _P, _P, _P, _P, _P], C.c_int),
+        "shiro_gpu_primary_hits": ([_P, _P, _P, _P, _U], C.c_int),
+        "shiro_gpu_trace_rays": ([_P, _P, _P, _P, _U, _P, _P, _P], C.c_int),
+        "shiro_gpu_last_stats": ([_P, _P], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+@dataclass
+class RenderRequest:
+    """shiro::backend::RenderRequest (RenderBackend.h:12-19)."""
+
+    scene: Scene
+    camera: Camera
+    settings: RenderSettings
+    sample_start: int = 0
+    sample_count: int = 1
+    cancel: Optional[C.c_int] = None  # set .value = 1 to cancel
+    flags: int = 0
+
+
+class GpuBackend:
+    """The GB300 backend.  One instance owns one device context; calls are
+    serialised by the caller (as the reference's mutex does)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        self._ctx = C.c_void_p()
+        rc = self.lib.shiro_gpu_create(int(device), C.byref(self._ctx))
+        if rc != 0:
+            raise ShiroGpuError(rc, self.lib.shiro_gpu_last_error(None).decode())
+        self._scene_key = None
+        self._marshalled: Optional[MarshalledScene] = None
+        self.last_error = ""
+
+    # -- lifetime ----------------------------------------------------------
+    def close(self):
+        if self._ctx:
+            self.lib.shiro_gpu_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- RenderBackend -----------------------------------------------------
+    @staticmethod
+    def get_status() -> dict:
+        lib = load_library()
+        st = BackendStatus()
+        lib.shiro_gpu_status(C.byref(st))
+        return dict(kind=st.kind, name=st.name.decode(), available=bool(st.available), uses_gpu=bool(st.uses_gpu),
+                    device_count=st.device_count, device_name=st.device_name.decode(),
+                    compute=(st.compute_major, st.compute_minor))
+
+    def supports_scene(self, scene: Scene) -> bool:
+        buf = C.create_string_buffer(256)
+        return bool(self.lib.shiro_gpu_supports_scene(MarshalledScene(scene).ref(), buf, 256))
+
+    def _err(self, rc: int) -> ShiroGpuError:
+        msg = self.lib.shiro_gpu_last_error(self._ctx).decode()
+        self.last_error = msg
+        return ShiroGpuError(rc, msg)
+
+    def upload_scene(self, scene: Scene, force: bool = False):
+        """Uploads (and caches by object identity, as CpuPathTracer caches by
+        Scene pointer, CpuPathTracer.cpp:2030-2041) the scene snapshot."""
+        key = id(scene)
+        if not force and self._scene_key == key:
+            return
+        ms = MarshalledScene(scene)
+        rc = self.lib.shiro_gpu_upload_scene(self._ctx, ms.ref())
+        if rc != 0:
+            self._scene_key = None
+            raise self._err(rc)
+        self._scene_key = key
+        self._marshalled = ms
+        self._scene_ref = scene
+
+    def render(self, scene: Scene, camera: Camera, settings: RenderSettings, sample_start: int = 0,
+               sample_count: Optional[int] = None, flags: int = 0, cancel: Optional[C.c_int] = None,
+               out: Optional[FrameBuffer] = None) -> FrameBuffer:
+        """Strict RenderSampleBatch: raises on failure."""
+        self.upload_scene(scene)
+        count = settings.samples_per_pixel if sample_count is None else sample_count
+        req = render_desc(camera, settings, sample_start, count, flags)
+        fb = out if out is not None else FrameBuffer(settings.width, settings.height)
+        aovs = fb.aovs()
+        rc = self.lib.shiro_gpu_render(self._ctx, C.byref(req), C.byref(cancel) if cancel is not None else None,
+                                       C.byref(aovs))
+        if rc != 0:
+            raise self._err(rc)
+        return fb
+
+    def render_sample_batch(self, request: RenderRequest) -> FrameBuffer:
+        """RenderBackend::RenderSampleBatch with the reference's error
+        convention (cleared FrameBuffer + stderr message on failure)."""
+        try:
+            return self.render(request.scene, request.camera, request.settings, request.sample_start,
+                               request.sample_count, request.flags, request.cancel)
+        except ShiroGpuError as e:
+            sys.stderr.write(f"shiro gb300 backend: {e}\n")
+            return FrameBuffer(request.settings.width, request.settings.height)
+
+    # -- wavefront ---------------------------------------------------------
+    def render_batch(self, scene: Scene, requests: Sequence[tuple], flags: int = 0,
+                     cancel: Optional[C.c_int] = None) -> List[FrameBuffer]:
+        """requests: (camera, settings[, sample_start[, sample_count]])."""
+        self.upload_scene(scene)
+        n = len(requests)
+        descs = (RenderDesc * max(1, n))()
+        fbs = []
+        outs = (Aovs * max(1, n))()
+        for i, r in enumerate(requests):
+            cam, st = r[0], r[1]
+            start = r[2] if len(r) > 2 else 0
+            count = r[3] if len(r) > 3 else st.samples_per_pixel
+            descs[i] = render_desc(cam, st, start, count, flags)
+            fb = FrameBuffer(st.width, st.height)
+            fbs.append(fb)
+            outs[i] = fb.aovs()
+        rc = self.lib.shiro_gpu_render_batch(self._ctx, descs, n, C.byref(cancel) if cancel is not None else None, outs)
+        if rc != 0:
+            raise self._err(rc)
+        return fbs
+
+    def wavefront_config(self) -> dict:
+        c = WavefrontConfig()
+        self.lib.shiro_gpu_get_wavefront_config(self._ctx, C.byref(c))
+        return dict(paths_in_flight=c.paths_in_flight, extend_block=c.extend_block, shade_block=c.shade_block,
+                    shadow_block=c.shadow_block, use_graph=c.use_graph)
+
+    def set_wavefront_config(self, **kw):
+        c = WavefrontConfig()
+        for k, v in kw.items():
+            setattr(c, k, int(v))
+        rc = self.lib.shiro_gpu_set_wavefront_config(self._ctx, C.byref(c))
+        if rc != 0:
+            raise self._err(rc)
+
+    def autotune(self, scene: Scene, camera: Camera, settings: RenderSettings, sample_count: Optional[int] = None) -> dict:
+        self.upload_scene(scene)
+        req = render_desc(camera, settings, 0, settings.samples_per_pixel if sample_count is None else sample_count)
+        c = WavefrontConfig()
+        rc = self.lib.shiro_gpu_autotune(self._ctx, C.byref(req), C.byref(c))
+        if rc != 0:
+            raise self._err(rc)
+        return self.wavefront_config()
+
+    # -- probes --------------------------------------------------------------
+    def primary_hits(self, scene: Scene, camera: Camera, settings: RenderSettings, sample_start: int = 0):
+        self.upload_scene(scene)
+        req = render_desc(camera, settings, sample_start, 1)
+        n = settings.width * settings.height
+        prim = np.zeros(n, np.uint32)
+        t = np.zeros(n, np.float32)
+        rc = self.lib.shiro_gpu_primary_hits(self._ctx, C.byref(req), _ptr(prim), _ptr(t), 0)
+        if rc != 0:
+            raise self._err(rc)
+        return prim, t
+
+    def trace_rays(self, scene: Scene, origins, dirs, tmax=None):
+        self.upload_scene(scene)
+        o = np.ascontiguousarray(origins, np.float32)
+        d = np.ascontiguousarray(dirs, np.float32)
+        n = o.shape[0]
+        tm = (np.full(n, np.finfo(np.float32).max, np.float32) if tmax is None
+              else np.ascontiguousarray(tmax, np.float32))
+        prim = np.zeros(n, np.uint32)
+        t = np.zeros(n, np.float32)
+        occ = np.zeros(n, np.uint32)
+        rc = self.lib.shiro_gpu_trace_rays(self._ctx, _ptr(o), _ptr(d), _ptr(tm), n, _ptr(prim), _ptr(t), _ptr(occ))
+        if rc != 0:
+            raise self._err(rc)
+        return prim, t, occ
+
+    def last_stats(self) -> dict:
+        s = RenderStats()
+        self.lib.shiro_gpu_last_stats(self._ctx, C.byref(s))
+        return {k: getattr(s, k) for k, _ in RenderStats._fields_}
+
+    @property
+    def handle(self):
+        return self._ctx

@@ -1,0 +1,276 @@
+// bsdf.cuh - layered BSDF of the reference CPU tracer.
+//
+// Restates src/backend/cpu/CpuPathTracer.cpp: SafeNormalized :836-839,
+// AdjustedRoughness :845-893, ProjectedTangent :852-860, DielectricF0Scalar
+// :895-899, DiffuseColor :901-909, BaseLayerRoughness :911-916, SpecularF0
+// :918-928, ThinFilmColor / ApplyThinFilm :934-968, ResolveShadingNormal
+// :970-986, GgxDistribution / GgxSmithVisibility / FresnelSchlick :988-1009,
+// layer transmittances :1035-1082, EvaluateSpecularLobe / Pdf :1096-1132,
+// PowerHeuristic :1218-1222, ClampMaxComponentValue :1224-1230,
+// EvaluateBsdfPdf :1232-1273, EvaluateBsdf :1275-1354, sample weights
+// :1376-1403, CosineSampleHemisphere :276-286, GgxSampleHalfVector :288-302.
+// Materials are the PbrMaterial fields verbatim (ShiroMaterialDesc); derived
+// quantities are recomputed per evaluation exactly as the reference does.
+#pragma once
+
+#include "common.cuh"
+#include "scene.cuh"
+
+namespace shiro_gpu {
+
+using Mat = ShiroMaterialDesc;
+
+__device__ __forceinline__ float sq(float v) { return v * v; }
+__device__ __forceinline__ V3 safe_normalized(const V3& v, const V3& fb) {
+    const float l = length(v);
+    return l > 0.0f ? v / l : fb;
+}
+__device__ __forceinline__ V3 ortho_x(const V3& n) {  // BuildOrthonormalX
+    const V3 axis = fabsf(n.z) < 0.999f ? V3{0.0f, 0.0f, 1.0f} : V3{0.0f, 1.0f, 0.0f};
+    return normalize(cross(axis, n));
+}
+__device__ __forceinline__ float f0_dielectric(float ior) {
+    const float s = smax(ior, 1.0f);
+    return sq((s - 1.0f) / (s + 1.0f));
+}
+__device__ __forceinline__ V3 diffuse_color(const Mat& m) {
+    const float metal = sclamp(m.metallic, 0.0f, 1.0f);
+    const float trans = sclamp(m.transmission, 0.0f, 1.0f);
+    const float sss = sclamp(m.subsurface, 0.0f, 1.0f);
+    const float blend = sclamp(maxc(ld3(m.subsurface_radius)) / 3.0f, 0.0f, 1.0f);
+    const V3 tint = lerp(ld3(m.base_color), ld3(m.subsurface_color), blend);
+    const V3 base = lerp(ld3(m.base_color), tint, sss);
+    return base * (sclamp(m.base_weight, 0.0f, 1.0f) * (1.0f - metal) * (1.0f - trans));
+}
+__device__ __forceinline__ float base_roughness(const Mat& m) {
+    return sclamp(m.roughness + m.coat_affect_roughness * m.coat_weight * m.coat_roughness, 0.0f, 1.0f);
+}
+__device__ __forceinline__ V3 spec_f0(const Mat& m) {
+    const float metal = sclamp(m.metallic, 0.0f, 1.0f);
+    const V3 d = ld3(m.specular_color) * (sclamp(m.specular_weight, 0.0f, 1.0f) * f0_dielectric(m.ior));
+    return lerp(d, ld3(m.base_color), metal);
+}
+__device__ __forceinline__ V3 coat_f0(const Mat& m) {
+    return ld3(m.coat_color) * (sclamp(m.coat_weight, 0.0f, 1.0f) * f0_dielectric(m.coat_ior));
+}
+__device__ __forceinline__ V3 one_minus_clamped(const V3& v) {
+    return {sclamp(1.0f - v.x, 0.0f, 1.0f), sclamp(1.0f - v.y, 0.0f, 1.0f), sclamp(1.0f - v.z, 0.0f, 1.0f)};
+}
+__device__ __forceinline__ V3 schlick(const V3& f0, float vDotH) {
+    const float c = sclamp(1.0f - vDotH, 0.0f, 1.0f);
+    const float f = c * c * c * c * c;
+    return f0 + (V3{1.0f, 1.0f, 1.0f} - f0) * f;
+}
+__device__ __forceinline__ V3 coat_tint(const Mat& m) {
+    const float a = sclamp(m.coat_affect_color * m.coat_weight, 0.0f, 1.0f);
+    return lerp(V3{1.0f, 1.0f, 1.0f}, sclamp3(ld3(m.coat_color), 0.0f, 1.0f), a);
+}
+__device__ __forceinline__ V3 layer_transmittance(const V3& f0, float nDotV, float nDotL) {
+    const V3 fv = schlick(f0, sclamp(nDotV, 0.0f, 1.0f));
+    const V3 fl = schlick(f0, sclamp(nDotL, 0.0f, 1.0f));
+    return one_minus_clamped((fv + fl) * 0.5f);
+}
+__device__ __forceinline__ float ggx_d(float nDotH, float r) {
+    const float a = smax(0.02f, r * r);
+    const float a2 = a * a;
+    const float den = smax(1.0e-6f, sq(nDotH * nDotH * (a2 - 1.0f) + 1.0f));
+    return a2 / (kPi * den);
+}
+__device__ __forceinline__ float ggx_lambda(float x, float a2) {
+    const float c = smax(x, 1.0e-6f);
+    return (-1.0f + sqrtf(1.0f + a2 * (1.0f - c * c) / (c * c))) * 0.5f;
+}
+__device__ __forceinline__ float ggx_vis(float nDotV, float nDotL, float r) {
+    const float a = smax(0.02f, r * r);
+    const float a2 = a * a;
+    return 1.0f / (1.0f + ggx_lambda(nDotV, a2) + ggx_lambda(nDotL, a2));
+}
+__device__ __forceinline__ V3 spec_lobe(const V3& n, const V3& v, const V3& l, const V3& f0, float r) {
+    const float nv = sclamp(dot(n, v), 0.0f, 1.0f);
+    const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
+    if (nv <= 0.0f || nl <= 0.0f) return {0.0f, 0.0f, 0.0f};
+    const V3 h = safe_normalized(v + l, n);
+    const float nh = sclamp(dot(n, h), 0.0f, 1.0f);
+    const float vh = sclamp(dot(v, h), 0.0f, 1.0f);
+    const float d = ggx_d(nh, r);
+    const float g = ggx_vis(nv, nl, r);
+    return schlick(f0, vh) * (d * g / smax(4.0f * nv * nl, 1.0e-6f));
+}
+__device__ __forceinline__ float spec_pdf(const V3& n, const V3& v, const V3& l, float r) {
+    const float nv = sclamp(dot(n, v), 0.0f, 1.0f);
+    const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
+    if (nv <= 0.0f || nl <= 0.0f) return 0.0f;
+    const V3 h = safe_normalized(v + l, n);
+    const float nh = sclamp(dot(n, h), 0.0f, 1.0f);
+    const float vh = sclamp(dot(v, h), 1.0e-6f, 1.0f);
+    return ggx_d(nh, r) * nh / smax(4.0f * vh, 1.0e-6f);
+}
+__device__ __forceinline__ V3 proj_tangent(const Mat& m, const V3& n) {
+    if (m.has_tangent_override) {
+        const V3 to = ld3(m.tangent_override);
+        const V3 t = to - n * dot(to, n);
+        if (length(t) > 0.0f) return normalize(t);
+    }
+    return ortho_x(n);
+}
+// AdjustedRoughness with the half-vector anisotropy phase; with zero
+// anisotropy the phase is multiplied by zero and skipped.
+__device__ __forceinline__ float roughness_for(float r, float aniso, float rot, const V3& n, const V3& tangent, const V3& v,
+                                               const V3& l) {
+    const float ca = sclamp(aniso, -0.95f, 0.95f);
+    float phase = 0.0f;
+    if (ca != 0.0f) {
+        const V3 td = safe_normalized(tangent - n * dot(tangent, n), ortho_x(n));
+        const V3 bt = normalize(cross(n, td));
+        const V3 h = safe_normalized(v + l, n);
+        const V3 hp = h - n * dot(n, h);
+        if (length(hp) <= 1.0e-6f) {
+            phase = cosf(rot * 2.0f * kPi);
+        } else {
+            const V3 hd = normalize(hp);
+            phase = cosf(atan2f(dot(hd, bt), dot(hd, td)) - rot * 2.0f * kPi);
+        }
+    }
+    return sclamp(r * (1.0f - 0.35f * ca * phase), 0.02f, 1.0f);
+}
+__device__ __forceinline__ float roughness_for(float r, float aniso, float rot) {
+    const float ca = sclamp(aniso, -0.95f, 0.95f);
+    const float phase = cosf(rot * 2.0f * kPi);
+    return sclamp(r * (1.0f - 0.35f * ca * phase), 0.02f, 1.0f);
+}
+__device__ __forceinline__ V3 film_color(float thickness, float ior, float vDotH) {
+    if (thickness <= 0.0f) return {1.0f, 1.0f, 1.0f};
+    const float si = smax(ior, 1.0f);
+    const float op = 2.0f * si * thickness * sclamp(vDotH, 0.05f, 1.0f);
+    const float p0 = 4.0f * kPi * op / smax(650.0f, 1.0f);
+    const float p1 = 4.0f * kPi * op / smax(510.0f, 1.0f);
+    const float p2 = 4.0f * kPi * op / smax(475.0f, 1.0f);
+    const V3 iri{0.5f + 0.5f * cosf(p0), 0.5f + 0.5f * cosf(p1), 0.5f + 0.5f * cosf(p2)};
+    const float strength = sclamp(thickness / 1200.0f, 0.0f, 1.0f);
+    return lerp(V3{1.0f, 1.0f, 1.0f}, (V3{1.0f, 1.0f, 1.0f} + iri) * 0.5f, strength);
+}
+__device__ __forceinline__ V3 thin_film(const V3& lobe, const Mat& m, const V3& n, const V3& v, const V3& l) {
+    if (m.thin_film_thickness <= 0.0f) return lobe;
+    const V3 h = safe_normalized(v + l, n);
+    const float vh = sclamp(dot(v, h), 0.0f, 1.0f);
+    return lobe * film_color(m.thin_film_thickness, m.thin_film_ior, vh);
+}
+__device__ __forceinline__ V3 resolve_normal(const Mat& m, const V3& fb, bool coat) {
+    const bool has = coat ? m.has_coat_normal_override != 0u : m.has_normal_override != 0u;
+    if (!has) return fb;
+    const V3 c = coat ? ld3(m.coat_normal_override) : ld3(m.normal_override);
+    if (length(c) <= 0.0f) return fb;
+    V3 n = normalize(c);
+    if (dot(n, fb) < 0.0f) n = n * -1.0f;
+    return n;
+}
+
+struct LobeWeights {
+    float diffuse, spec, coat;
+};
+__device__ __forceinline__ LobeWeights lobe_weights(const Mat& m) {
+    const V3 uc = coat_tint(m) * one_minus_clamped(coat_f0(m));
+    const V3 sf0 = spec_f0(m);
+    const V3 ub = one_minus_clamped(sf0);
+    LobeWeights w;
+    w.diffuse = smax(0.0f, maxc(diffuse_color(m) * uc * ub));
+    w.spec = smax(0.0f, maxc(uc * sf0));
+    w.coat = smax(0.0f, maxc(coat_f0(m)));
+    return w;
+}
+__device__ __forceinline__ float transmission_weight(const Mat& m) {
+    const float tr = sclamp(m.transmission, 0.0f, 1.0f);
+    const float metal = sclamp(m.metallic, 0.0f, 1.0f);
+    if (tr <= 0.0f || metal >= 0.999f) return 0.0f;
+    const V3 uc = coat_tint(m) * one_minus_clamped(coat_f0(m));
+    const V3 ub = one_minus_clamped(spec_f0(m));
+    return smax(0.0f, maxc(sclamp3(ld3(m.transmission_color), 0.0f, 1.0f) * uc * ub)) * tr * (1.0f - metal);
+}
+
+__device__ __noinline__ float bsdf_pdf(const Mat& m, const LobeWeights& w, const V3& n, const V3& cn, const V3& v,
+                                       const V3& l) {
+    const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
+    if (nl <= 0.0f) return 0.0f;
+    const float rw = w.diffuse + w.spec + w.coat;
+    if (rw <= 0.0f) return 0.0f;
+    const float dp = w.diffuse / rw, bp = w.spec / rw, cp = w.coat / rw;
+    const float sr = roughness_for(base_roughness(m), m.specular_anisotropy, m.specular_rotation, n, proj_tangent(m, n), v, l);
+    float coatTerm = 0.0f;
+    if (cp != 0.0f) {
+        const float cr = roughness_for(m.coat_roughness, m.coat_anisotropy, m.coat_rotation, cn, proj_tangent(m, cn), v, l);
+        coatTerm = cp * spec_pdf(cn, v, l, cr);
+    }
+    return dp * nl * kInvPi + bp * spec_pdf(n, v, l, sr) + coatTerm;
+}
+
+__device__ __noinline__ V3 bsdf_eval(const Mat& m, const V3& n, const V3& cn, const V3& v, const V3& l) {
+    const float nv = sclamp(dot(n, v), 0.0f, 1.0f);
+    const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
+    if (nv <= 0.0f || nl <= 0.0f) return {0.0f, 0.0f, 0.0f};
+    const V3 baseF0 = spec_f0(m);
+    const V3 cF0 = coat_f0(m);
+    const V3 underCoat = coat_tint(m) * layer_transmittance(cF0, dot(cn, v), dot(cn, l));
+    const V3 underBase = layer_transmittance(baseF0, nv, nl);
+    const V3 vp = normalize(v - n * nv);
+    const V3 lp = normalize(l - n * nl);
+    const float cosPhi = length(vp) > 0.0f && length(lp) > 0.0f ? sclamp(dot(vp, lp), -1.0f, 1.0f) : 0.0f;
+    const float sigma = sclamp(m.diffuse_roughness, 0.0f, 1.0f);
+    const float s2 = sigma * sigma;
+    const float orenA = 1.0f - (s2 / (2.0f * (s2 + 0.33f)));
+    const float orenB = 0.45f * s2 / (s2 + 0.09f);
+    const float sinV = sqrtf(smax(0.0f, 1.0f - nv * nv));
+    const float sinL = sqrtf(smax(0.0f, 1.0f - nl * nl));
+    const float sinAlpha = smax(sinV, sinL);
+    const float tanBeta = smin(sinV / smax(nv, 1.0e-6f), sinL / smax(nl, 1.0e-6f));
+    const float wrap = sclamp(m.subsurface * m.subsurface_scale *
+                                  (0.35f + 0.15f * sclamp(m.subsurface_anisotropy, -1.0f, 1.0f) +
+                                   0.1f * sclamp(maxc(ld3(m.subsurface_radius)) / 3.0f, 0.0f, 1.0f)),
+                              0.0f, 0.9f);
+    const float wrapped = sclamp((nl + wrap) / (1.0f + wrap), 0.0f, 1.0f);
+    const float term = (orenA + orenB * smax(0.0f, cosPhi) * sinAlpha * tanBeta) * (wrapped / smax(nl, 1.0e-6f));
+    const V3 diffuse = diffuse_color(m) * underCoat * underBase * (kInvPi * term);
+    const float sr = roughness_for(base_roughness(m), m.specular_anisotropy, m.specular_rotation, n, proj_tangent(m, n), v, l);
+    const V3 spec = underCoat * thin_film(spec_lobe(n, v, l, baseF0, sr), m, n, v, l);
+    const float cr = roughness_for(m.coat_roughness, m.coat_anisotropy, m.coat_rotation, cn, proj_tangent(m, cn), v, l);
+    const V3 coat = thin_film(spec_lobe(cn, v, l, cF0, cr), m, cn, v, l);
+    const V3 h = safe_normalized(v + l, n);
+    const float sw = sclamp(m.sheen, 0.0f, 1.0f);
+    const float lh = sclamp(dot(l, h), 0.0f, 1.0f);
+    const float sf = powf(1.0f - lh, 5.0f) * (1.0f - 0.5f * sclamp(m.sheen_roughness, 0.0f, 1.0f));
+    const V3 sheen = ld3(m.sheen_color) * sw * sf * underCoat * underBase;
+    return diffuse + spec + coat + sheen;
+}
+
+__device__ __forceinline__ V3 cosine_hemisphere(const V3& n, const V2& s) {
+    const float phi = 2.0f * kPi * s.x;
+    const float r = sqrtf(s.y);
+    const float x = r * cosf(phi);
+    const float y = r * sinf(phi);
+    const float z = sqrtf(smax(0.0f, 1.0f - s.y));
+    const V3 t = ortho_x(n);
+    const V3 b = cross(n, t);
+    return normalize(t * x + b * y + n * z);
+}
+__device__ __forceinline__ V3 ggx_half(const V3& n, const V2& s, float rough) {
+    const float a = smax(0.02f, rough * rough);
+    const float a2 = a * a;
+    const float phi = 2.0f * kPi * s.x;
+    const float ct = sqrtf(smax(0.0f, (1.0f - s.y) / smax(1.0e-6f, 1.0f + (a2 - 1.0f) * s.y)));
+    const float st = sqrtf(smax(0.0f, 1.0f - ct * ct));
+    const float x = st * cosf(phi);
+    const float y = st * sinf(phi);
+    const V3 t = ortho_x(n);
+    const V3 b = cross(n, t);
+    return normalize(t * x + b * y + n * ct);
+}
+__device__ __forceinline__ V3 clamp_max(const V3& v, float mx) {
+    const float c = maxc(v);
+    if (c <= mx || c <= 0.0f) return v;
+    return v * (mx / c);
+}
+__device__ __forceinline__ float power_heuristic(float a, float b) {
+    const float a2 = a * a, b2 = b * b;
+    return a2 / smax(a2 + b2, 1.0e-6f);
+}
+
+}  // namespace shiro_gpu

@@ -1,0 +1,473 @@
+// bvh_build.cu - device BVH construction.
+//
+// Counterpart of CpuPathTracer::BuildAccelerationScene's Embree build
+// (src/backend/cpu/CpuPathTracer.cpp:524-592, RTC_BUILD_QUALITY_LOW) and of
+// the OptiX GAS build (src/backend/optix/OptixBackend.cpp:974-1015).
+//
+// Pipeline (all on the device, one stream):
+//   1. centroid bounds            (block reduction + ordered-int atomics)
+//   2. 63-bit Morton codes        (21 bits per axis)
+//   3. radix sort of (code, prim) (CUB DeviceRadixSort - a library sort)
+//   4. Karras 2012 hierarchy      (one thread per internal node)
+//   5. bottom-up boxes + SAH      (atomic arrival counters; a subtree of <= 8
+//                                  triangles becomes a leaf when the SAH leaf
+//                                  cost does not exceed the split cost)
+//   6. compaction + emission      (surviving internal nodes renumbered by an
+//                                  exclusive scan, written in the traversal
+//                                  layout of scene.cuh)
+// Triangles whose box spans a large part of the scene (ground planes) would
+// inflate every Morton-neighbour box up to the root; up to 8 of them are kept
+// out of the Morton tree and placed in a leaf beside it under the root.
+#include <cub/cub.cuh>
+
+#include "bvh_build.h"
+#include "common.cuh"
+
+namespace shiro_gpu {
+
+namespace {
+
+constexpr float kCostNode = 1.2f;
+constexpr float kCostTri = 1.0f;
+constexpr uint32_t kMaxLeaf = 8;
+
+__device__ __forceinline__ uint32_t f2ord(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__global__ void k_centroid_bounds(const float4* __restrict__ cen, uint32_t n, uint32_t* __restrict__ out6) {
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 c = cen[i];
+        lo[0] = fminf(lo[0], c.x);
+        lo[1] = fminf(lo[1], c.y);
+        lo[2] = fminf(lo[2], c.z);
+        hi[0] = fmaxf(hi[0], c.x);
+        hi[1] = fmaxf(hi[1], c.y);
+        hi[2] = fmaxf(hi[2], c.z);
+    }
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(&out6[k], f2ord(lo[k]));
+            atomicMax(&out6[3 + k], f2ord(hi[k]));
+        }
+    }
+}
+
+__device__ __forceinline__ uint64_t spread21(uint64_t v) {
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+__global__ void k_morton(const float4* __restrict__ cen, uint32_t n, const uint32_t* __restrict__ b6,
+                         uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float lo[3] = {ord2f(b6[0]), ord2f(b6[1]), ord2f(b6[2])};
+    const float hi[3] = {ord2f(b6[3]), ord2f(b6[4]), ord2f(b6[5])};
+    const float4 c = cen[i];
+    const float cc[3] = {c.x, c.y, c.z};
+    uint64_t q[3];
+    for (int k = 0; k < 3; ++k) {
+        const float ext = hi[k] - lo[k];
+        float f = ext > 0.0f ? (cc[k] - lo[k]) / ext : 0.5f;
+        f = fminf(fmaxf(f, 0.0f), 1.0f);
+        q[k] = static_cast<uint64_t>(fminf(f * 2097152.0f, 2097151.0f));
+    }
+    keys[i] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
+    vals[i] = i;
+}
+
+__device__ __forceinline__ int delta(const uint64_t* keys, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const uint64_t a = keys[i], b = keys[j];
+    if (a != b) return __clzll(static_cast<long long>(a ^ b));
+    return 64 + __clz(i ^ j);
+}
+
+// Karras 2012, "Maximizing parallelism in the construction of BVHs, octrees
+// and k-d trees", algorithm 2.  Child encoding: >= 0 internal node index,
+// < 0 leaf ~(sorted position).
+__global__ void k_karras(const uint64_t* __restrict__ keys, int n, int2* __restrict__ child, int2* __restrict__ range,
+                         int* __restrict__ nodeParent, int* __restrict__ leafParent) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta(keys, n, i, i - d);
+    int lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = delta(keys, n, i, j);
+    int s = 0;
+    int div = 2;
+    int t;
+    do {
+        t = (l + div - 1) / div;
+        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+        div <<= 1;
+    } while (t > 1);
+    const int g = i + s * d + min(d, 0);
+    const int first = min(i, j), last = max(i, j);
+    const int left = (first == g) ? ~g : g;
+    const int right = (last == g + 1) ? ~(g + 1) : g + 1;
+    child[i] = make_int2(left, right);
+    range[i] = make_int2(first, last);
+    if (left < 0) leafParent[~left] = i; else nodeParent[left] = i;
+    if (right < 0) leafParent[~right] = i; else nodeParent[right] = i;
+    if (i == 0) nodeParent[0] = -1;
+}
+
+struct Box {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ float box_area(const Box& b) {
+    const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+    return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+__device__ __forceinline__ Box load_prim_box(const float4* pb, uint32_t prim) {
+    const float4 a = pb[2 * prim], b = pb[2 * prim + 1];
+    Box r;
+    r.lo[0] = a.x; r.lo[1] = a.y; r.lo[2] = a.z;
+    r.hi[0] = b.x; r.hi[1] = b.y; r.hi[2] = b.z;
+    return r;
+}
+
+// Bottom-up: the second thread to reach a node computes its box, triangle
+// count and SAH cost.
+__global__ void k_bottom_up(int n, const uint32_t* __restrict__ sortedPrim, const float4* __restrict__ primBox,
+                            const int2* __restrict__ child, const int* __restrict__ nodeParent,
+                            const int* __restrict__ leafParent, unsigned int* __restrict__ arrivals,
+                            float4* __restrict__ nodeBox, float* __restrict__ nodeCost, int* __restrict__ nodeCount,
+                            uint8_t* __restrict__ collapse) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    int node = leafParent[j];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(&arrivals[node], 1u) == 0u) return;
+        __threadfence();
+        const int2 c = child[node];
+        Box bb[2];
+        float cost[2];
+        int cnt[2];
+        const int cs[2] = {c.x, c.y};
+        for (int k = 0; k < 2; ++k) {
+            if (cs[k] < 0) {
+                bb[k] = load_prim_box(primBox, sortedPrim[~cs[k]]);
+                cnt[k] = 1;
+                cost[k] = kCostTri * box_area(bb[k]);
+            } else {
+                const float4 a = __ldcg(&nodeBox[2 * cs[k]]), b = __ldcg(&nodeBox[2 * cs[k] + 1]);
+                bb[k].lo[0] = a.x; bb[k].lo[1] = a.y; bb[k].lo[2] = a.z;
+                bb[k].hi[0] = b.x; bb[k].hi[1] = b.y; bb[k].hi[2] = b.z;
+                cnt[k] = __ldcg(&nodeCount[cs[k]]);
+                cost[k] = __ldcg(&nodeCost[cs[k]]);
+            }
+        }
+        Box u;
+        for (int k = 0; k < 3; ++k) {
+            u.lo[k] = fminf(bb[0].lo[k], bb[1].lo[k]);
+            u.hi[k] = fmaxf(bb[0].hi[k], bb[1].hi[k]);
+        }
+        const float area = box_area(u);
+        const int count = cnt[0] + cnt[1];
+        const float split = kCostNode * area + cost[0] + cost[1];
+        const float leaf = kCostTri * area * static_cast<float>(count);
+        const bool asLeaf = count <= static_cast<int>(kMaxLeaf) && leaf <= split;
+        nodeBox[2 * node] = make_float4(u.lo[0], u.lo[1], u.lo[2], 0.0f);
+        nodeBox[2 * node + 1] = make_float4(u.hi[0], u.hi[1], u.hi[2], 0.0f);
+        nodeCount[node] = count;
+        nodeCost[node] = asLeaf ? leaf : split;
+        collapse[node] = asLeaf ? 1 : 0;
+        node = nodeParent[node];
+    }
+}
+
+// A node is emitted when neither it nor any ancestor became a leaf.
+__global__ void k_emit_flags(int nInternal, const int* __restrict__ nodeParent, const uint8_t* __restrict__ collapse,
+                             uint32_t* __restrict__ flag, unsigned int* __restrict__ maxDepth) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nInternal) return;
+    bool emitted = collapse[k] == 0;
+    unsigned int depth = 0;
+    for (int p = nodeParent[k]; p >= 0; p = nodeParent[p]) {
+        if (collapse[p]) emitted = false;
+        ++depth;
+    }
+    flag[k] = emitted ? 1u : 0u;
+    if (emitted) atomicMax(maxDepth, depth + 1u);
+}
+
+__device__ __forceinline__ int leaf_link(int first, int count) { return ~((first << 3) | (count - 1)); }
+
+__global__ void k_emit_nodes(int nInternal, const uint32_t* __restrict__ flag, const uint32_t* __restrict__ newIndex,
+                             uint32_t offset, const int2* __restrict__ child, const int2* __restrict__ range,
+                             const uint8_t* __restrict__ collapse, const float4* __restrict__ nodeBox,
+                             const uint32_t* __restrict__ sortedPrim, const float4* __restrict__ primBox,
+                             float4* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nInternal || !flag[k]) return;
+    const int2 c = child[k];
+    const int cs[2] = {c.x, c.y};
+    Box bb[2];
+    int link[2];
+    for (int q = 0; q < 2; ++q) {
+        const int ch = cs[q];
+        if (ch < 0) {
+            bb[q] = load_prim_box(primBox, sortedPrim[~ch]);
+            link[q] = leaf_link(~ch, 1);
+        } else {
+            const float4 a = nodeBox[2 * ch], b = nodeBox[2 * ch + 1];
+            bb[q].lo[0] = a.x; bb[q].lo[1] = a.y; bb[q].lo[2] = a.z;
+            bb[q].hi[0] = b.x; bb[q].hi[1] = b.y; bb[q].hi[2] = b.z;
+            if (collapse[ch]) {
+                const int2 r = range[ch];
+                link[q] = leaf_link(r.x, r.y - r.x + 1);
+            } else {
+                link[q] = static_cast<int>(newIndex[ch] + offset);
+            }
+        }
+    }
+    float4* o = out + 4 * static_cast<size_t>(newIndex[k] + offset);
+    o[0] = make_float4(bb[0].lo[0], bb[0].hi[0], bb[0].lo[1], bb[0].hi[1]);
+    o[1] = make_float4(bb[1].lo[0], bb[1].hi[0], bb[1].lo[1], bb[1].hi[1]);
+    o[2] = make_float4(bb[0].lo[2], bb[0].hi[2], bb[1].lo[2], bb[1].hi[2]);
+    o[3] = make_float4(__int_as_float(link[0]), __int_as_float(link[1]), 0.0f, 0.0f);
+}
+
+__global__ void k_write_tris(uint32_t n, const uint32_t* __restrict__ sortedPrim, const float4* __restrict__ triIn,
+                             float4* __restrict__ triOut) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t p = sortedPrim[s];
+    triOut[3 * static_cast<size_t>(s)] = triIn[3 * static_cast<size_t>(p)];
+    triOut[3 * static_cast<size_t>(s) + 1] = triIn[3 * static_cast<size_t>(p) + 1];
+    triOut[3 * static_cast<size_t>(s) + 2] = triIn[3 * static_cast<size_t>(p) + 2];
+}
+
+// Root node for trees with fewer than two emitted Morton nodes and for the
+// top node that holds the large triangles: child 0 / child 1 given as
+// (box, link); an absent child gets an empty (inverted) box.
+__global__ void k_write_root(float4* out, float4 b0lo, float4 b0hi, int l0, float4 b1lo, float4 b1hi, int l1) {
+    out[0] = make_float4(b0lo.x, b0hi.x, b0lo.y, b0hi.y);
+    out[1] = make_float4(b1lo.x, b1hi.x, b1lo.y, b1hi.y);
+    out[2] = make_float4(b0lo.z, b0hi.z, b1lo.z, b1hi.z);
+    out[3] = make_float4(__int_as_float(l0), __int_as_float(l1), 0.0f, 0.0f);
+}
+
+__global__ void k_copy_box(const float4* __restrict__ nodeBox, float4* __restrict__ dst) {
+    dst[0] = nodeBox[0];
+    dst[1] = nodeBox[1];
+}
+
+#define BVH_CHECK(x)                                                       \
+    do {                                                                   \
+        cudaError_t e_ = (x);                                              \
+        if (e_ != cudaSuccess) {                                           \
+            err = std::string(#x) + ": " + cudaGetErrorString(e_);         \
+            return e_ == cudaErrorMemoryAllocation ? SHIRO_ERR_OUT_OF_MEMORY \
+                                                   : SHIRO_ERR_CUDA;       \
+        }                                                                  \
+    } while (0)
+
+struct Scratch {
+    std::vector<void*> ptrs;
+    ~Scratch() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+    template <typename T>
+    cudaError_t alloc(T** p, size_t count) {
+        void* v = nullptr;
+        const cudaError_t e = cudaMalloc(&v, count * sizeof(T) + 16);
+        if (e == cudaSuccess) ptrs.push_back(v);
+        *p = static_cast<T*>(v);
+        return e;
+    }
+};
+
+inline unsigned blocks(size_t n, unsigned b) { return static_cast<unsigned>((n + b - 1) / b); }
+
+}  // namespace
+
+int build_bvh(const BvhInput& in, cudaStream_t stream, BvhOutput* out, std::string& err) {
+    const uint32_t m = in.smallCount;
+    const uint32_t L = static_cast<uint32_t>(in.largeSlots.size());
+    const uint32_t total = m + L;
+    if (total == 0) {
+        err = "scene has no triangles";
+        return SHIRO_ERR_INVALID_ARGUMENT;
+    }
+    if (total >= (1u << 28)) {
+        err = "too many triangles for the leaf encoding (2^28)";
+        return SHIRO_ERR_INVALID_ARGUMENT;
+    }
+    Scratch sc;
+    float4* triOut = nullptr;
+    BVH_CHECK(cudaMalloc(&triOut, 3 * sizeof(float4) * static_cast<size_t>(total)));
+    out->tris = triOut;
+    out->triCount = total;
+
+    // Morton tree over the small triangles -------------------------------
+    uint32_t* sortedPrim = nullptr;  // sorted position -> small prim index
+    int2 *child = nullptr, *range = nullptr;
+    int *nodeParent = nullptr, *leafParent = nullptr;
+    float4* nodeBox = nullptr;
+    float* nodeCost = nullptr;
+    int* nodeCount = nullptr;
+    uint8_t* collapse = nullptr;
+    uint32_t emittedMorton = 0;
+    bool mortonRootIsNode = false;
+    float4 mortonLo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0), mortonHi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0);
+    unsigned int depthHost = 0;
+    uint32_t* flag = nullptr;
+    uint32_t* newIndex = nullptr;
+    const int nInternal = m >= 2 ? static_cast<int>(m) - 1 : 0;
+
+    if (m > 0) {
+        uint32_t* b6 = nullptr;
+        uint64_t *keys = nullptr, *keysOut = nullptr;
+        uint32_t* vals = nullptr;
+        BVH_CHECK(sc.alloc(&b6, 6));
+        BVH_CHECK(sc.alloc(&keys, m));
+        BVH_CHECK(sc.alloc(&keysOut, m));
+        BVH_CHECK(sc.alloc(&vals, m));
+        BVH_CHECK(sc.alloc(&sortedPrim, m));
+        const uint32_t init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+        BVH_CHECK(cudaMemcpyAsync(b6, init, sizeof(init), cudaMemcpyHostToDevice, stream));
+        k_centroid_bounds<<<std::min(blocks(m, 256), 1024u), 256, 0, stream>>>(in.centroids, m, b6);
+        k_morton<<<blocks(m, 256), 256, 0, stream>>>(in.centroids, m, b6, keys, vals);
+        BVH_CHECK(cudaGetLastError());
+        size_t tmpBytes = 0;
+        BVH_CHECK(cub::DeviceRadixSort::SortPairs(nullptr, tmpBytes, keys, keysOut, vals, sortedPrim, static_cast<int>(m), 0,
+                                                  63, stream));
+        void* tmp = nullptr;
+        BVH_CHECK(sc.alloc(reinterpret_cast<uint8_t**>(&tmp), tmpBytes));
+        BVH_CHECK(cub::DeviceRadixSort::SortPairs(tmp, tmpBytes, keys, keysOut, vals, sortedPrim, static_cast<int>(m), 0,
+                                                  63, stream));
+        if (nInternal > 0) {
+            BVH_CHECK(sc.alloc(&child, nInternal));
+            BVH_CHECK(sc.alloc(&range, nInternal));
+            BVH_CHECK(sc.alloc(&nodeParent, nInternal));
+            BVH_CHECK(sc.alloc(&leafParent, m));
+            BVH_CHECK(sc.alloc(&nodeBox, 2 * static_cast<size_t>(nInternal)));
+            BVH_CHECK(sc.alloc(&nodeCost, nInternal));
+            BVH_CHECK(sc.alloc(&nodeCount, nInternal));
+            BVH_CHECK(sc.alloc(&collapse, nInternal));
+            unsigned int* arrivals = nullptr;
+            unsigned int* maxDepth = nullptr;
+            BVH_CHECK(sc.alloc(&arrivals, nInternal));
+            BVH_CHECK(sc.alloc(&maxDepth, 1));
+            BVH_CHECK(sc.alloc(&flag, nInternal));
+            BVH_CHECK(sc.alloc(&newIndex, nInternal));
+            BVH_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(unsigned int) * nInternal, stream));
+            BVH_CHECK(cudaMemsetAsync(maxDepth, 0, sizeof(unsigned int), stream));
+            k_karras<<<blocks(nInternal, 256), 256, 0, stream>>>(keysOut, static_cast<int>(m), child, range, nodeParent,
+                                                                  leafParent);
+            k_bottom_up<<<blocks(m, 256), 256, 0, stream>>>(static_cast<int>(m), sortedPrim, in.primBoxes, child, nodeParent,
+                                                             leafParent, arrivals, nodeBox, nodeCost, nodeCount, collapse);
+            k_emit_flags<<<blocks(nInternal, 256), 256, 0, stream>>>(nInternal, nodeParent, collapse, flag, maxDepth);
+            BVH_CHECK(cudaGetLastError());
+            size_t scanBytes = 0;
+            BVH_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, flag, newIndex, nInternal, stream));
+            void* scanTmp = nullptr;
+            BVH_CHECK(sc.alloc(reinterpret_cast<uint8_t**>(&scanTmp), scanBytes));
+            BVH_CHECK(cub::DeviceScan::ExclusiveSum(scanTmp, scanBytes, flag, newIndex, nInternal, stream));
+            uint32_t lastIdx = 0, lastFlag = 0;
+            uint8_t rootCollapsed = 0;
+            BVH_CHECK(cudaMemcpyAsync(&lastIdx, newIndex + nInternal - 1, 4, cudaMemcpyDeviceToHost, stream));
+            BVH_CHECK(cudaMemcpyAsync(&lastFlag, flag + nInternal - 1, 4, cudaMemcpyDeviceToHost, stream));
+            BVH_CHECK(cudaMemcpyAsync(&rootCollapsed, collapse, 1, cudaMemcpyDeviceToHost, stream));
+            BVH_CHECK(cudaMemcpyAsync(&depthHost, maxDepth, 4, cudaMemcpyDeviceToHost, stream));
+            float4 rb[2];
+            BVH_CHECK(cudaMemcpyAsync(rb, nodeBox, sizeof(rb), cudaMemcpyDeviceToHost, stream));
+            BVH_CHECK(cudaStreamSynchronize(stream));
+            emittedMorton = lastIdx + lastFlag;
+            mortonRootIsNode = rootCollapsed == 0;
+            mortonLo = rb[0];
+            mortonHi = rb[1];
+        } else {
+            // a single small triangle
+            float4 pb[2];
+            uint32_t p0 = 0;
+            BVH_CHECK(cudaMemcpyAsync(&p0, sortedPrim, 4, cudaMemcpyDeviceToHost, stream));
+            BVH_CHECK(cudaStreamSynchronize(stream));
+            BVH_CHECK(cudaMemcpy(pb, in.primBoxes + 2 * p0, sizeof(pb), cudaMemcpyDeviceToHost));
+            mortonLo = pb[0];
+            mortonHi = pb[1];
+        }
+        k_write_tris<<<blocks(m, 256), 256, 0, stream>>>(m, sortedPrim, in.triData, triOut);
+        BVH_CHECK(cudaGetLastError());
+    }
+    // large triangles follow the Morton-ordered ones
+    float4 largeLo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0), largeHi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0);
+    for (uint32_t k = 0; k < L; ++k) {
+        const LargeTri& lt = in.largeSlots[k];
+        BVH_CHECK(cudaMemcpyAsync(triOut + 3 * static_cast<size_t>(m + k), lt.tri, 3 * sizeof(float4), cudaMemcpyHostToDevice,
+                                  stream));
+        largeLo.x = std::min(largeLo.x, lt.lo[0]);
+        largeLo.y = std::min(largeLo.y, lt.lo[1]);
+        largeLo.z = std::min(largeLo.z, lt.lo[2]);
+        largeHi.x = std::max(largeHi.x, lt.hi[0]);
+        largeHi.y = std::max(largeHi.y, lt.hi[1]);
+        largeHi.z = std::max(largeHi.z, lt.hi[2]);
+    }
+
+    // Node array: [top root if needed] + emitted Morton nodes -------------
+    const bool mortonTree = m >= 2 && mortonRootIsNode;
+    const bool needTop = !mortonTree || L > 0;
+    const uint32_t offset = needTop ? 1u : 0u;
+    const uint32_t nodeCountOut = offset + (mortonTree ? emittedMorton : 0u);
+    float4* nodes = nullptr;
+    BVH_CHECK(cudaMalloc(&nodes, 4 * sizeof(float4) * static_cast<size_t>(nodeCountOut)));
+    out->nodes = nodes;
+    out->nodeCount = nodeCountOut;
+    if (mortonTree) {
+        k_emit_nodes<<<blocks(nInternal, 256), 256, 0, stream>>>(nInternal, flag, newIndex, offset, child, range, collapse,
+                                                                  nodeBox, sortedPrim, in.primBoxes, nodes);
+        BVH_CHECK(cudaGetLastError());
+    }
+    const float4 emptyLo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0), emptyHi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0);
+    const int emptyLink = leaf_link_host(0, 1);
+    if (needTop) {
+        int l0 = emptyLink, l1 = emptyLink;
+        float4 b0lo = emptyLo, b0hi = emptyHi, b1lo = emptyLo, b1hi = emptyHi;
+        if (m > 0) {
+            b0lo = mortonLo;
+            b0hi = mortonHi;
+            l0 = mortonTree ? 1 : leaf_link_host(0, static_cast<int>(m));
+        }
+        if (L > 0) {
+            b1lo = largeLo;
+            b1hi = largeHi;
+            l1 = leaf_link_host(static_cast<int>(m), static_cast<int>(L));
+        }
+        k_write_root<<<1, 1, 0, stream>>>(nodes, b0lo, b0hi, l0, b1lo, b1hi, l1);
+        BVH_CHECK(cudaGetLastError());
+    }
+    BVH_CHECK(cudaStreamSynchronize(stream));
+    out->depth = depthHost + offset + 1u;
+    out->maxLeaf = kMaxLeaf;
+    return SHIRO_OK;
+}
+
+}  // namespace shiro_gpu

@@ -1,0 +1,124 @@
+// render_plain.cu - the plain GPU form: one thread per path.
+//
+// CpuPathTracer::RenderSampleBatch (src/backend/cpu/CpuPathTracer.cpp:
+// 2043-2170) loops pixels on host threads and samples inside each pixel; here
+// every (pixel, sample) path is one CUDA thread running the whole estimator
+// (camera ray, traversal, shading, next-event estimation, Russian roulette)
+// to completion, and writes a 48-byte record.  A second kernel sums each
+// pixel's records in sample order, so the batch average is formed with the
+// same additions, in the same order, as the reference.
+#include "integrator.cuh"
+#include "kernels.h"
+
+namespace shiro_gpu {
+
+namespace {
+
+__global__ void __launch_bounds__(128) k_plain_paths(const DevScene s, const DevRequest q, uint64_t pathBase,
+                                                     uint32_t count, float4* __restrict__ records) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const uint64_t path = pathBase + i;
+    const uint64_t pixel = path / q.sampleCount;
+    const uint32_t smp = static_cast<uint32_t>(path - pixel * q.sampleCount);
+    const uint32_t y = static_cast<uint32_t>(pixel / q.width);
+    const uint32_t x = static_cast<uint32_t>(pixel - static_cast<uint64_t>(y) * q.width);
+    const PathResult r = trace_path(s, q, x, y, q.sampleStart + smp);
+    float4* o = records + 3 * static_cast<size_t>(i);
+    o[0] = make_float4(r.radiance.x, r.radiance.y, r.radiance.z, r.depth);
+    o[1] = make_float4(r.albedo.x, r.albedo.y, r.albedo.z, 0.0f);
+    o[2] = make_float4(r.normal.x, r.normal.y, r.normal.z, 0.0f);
+}
+
+__global__ void k_resolve(const DevRequest q, uint64_t pixelBase, uint32_t count, const float4* __restrict__ records,
+                          AovPtrs aov) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const uint32_t n = q.sampleCount;
+    float b0 = 0.0f, b1 = 0.0f, b2 = 0.0f, b3 = 0.0f;
+    V3 alb{0.0f, 0.0f, 0.0f}, nrm{0.0f, 0.0f, 0.0f};
+    float depth = __int_as_float(0x7f800000);
+    const float4* r = records + 3 * static_cast<size_t>(i) * n;
+    for (uint32_t k = 0; k < n; ++k) {
+        const float4 a = r[3 * k], b = r[3 * k + 1], c = r[3 * k + 2];
+        b0 = b0 + a.x;
+        b1 = b1 + a.y;
+        b2 = b2 + a.z;
+        b3 = b3 + (a.w < __int_as_float(0x7f800000) ? 1.0f : 0.0f);
+        alb = alb + V3{b.x, b.y, b.z};
+        nrm = nrm + V3{c.x, c.y, c.z};
+        if (a.w < depth) depth = a.w;
+    }
+    const float cnt = static_cast<float>(n);
+    const float inv = 1.0f / cnt;
+    const size_t p = static_cast<size_t>(pixelBase + i);
+    aov.beauty[4 * p + 0] = b0 / cnt;
+    aov.beauty[4 * p + 1] = b1 / cnt;
+    aov.beauty[4 * p + 2] = b2 / cnt;
+    aov.beauty[4 * p + 3] = b3 / cnt;
+    const V3 a = alb * inv, nn = nrm * inv;
+    aov.albedo[3 * p + 0] = a.x;
+    aov.albedo[3 * p + 1] = a.y;
+    aov.albedo[3 * p + 2] = a.z;
+    aov.normal[3 * p + 0] = nn.x;
+    aov.normal[3 * p + 1] = nn.y;
+    aov.normal[3 * p + 2] = nn.z;
+    aov.depth[p] = depth;
+}
+
+__global__ void k_primary_hits(const DevScene s, const DevRequest q, uint32_t* __restrict__ prim, float* __restrict__ tout) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= q.width * q.height) return;
+    const uint32_t y = i / q.width, x = i - y * q.width;
+    const Sampler smp{x, y, q.sampleStart};
+    V3 o, d;
+    camera_ray(q, x, y, smp.next2d(0u), &o, &d);
+    HitRec h;
+    const bool hit = trace_closest(s, o, d, &h);
+    prim[i] = hit ? h.gid : 0xffffffffu;
+    tout[i] = hit ? h.t : FLT_MAX;
+}
+
+__global__ void k_trace_rays(const DevScene s, const float* __restrict__ o, const float* __restrict__ d,
+                             const float* __restrict__ tmax, uint32_t n, uint32_t* __restrict__ prim,
+                             float* __restrict__ tout, uint32_t* __restrict__ occ) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const V3 ro{o[3 * i], o[3 * i + 1], o[3 * i + 2]};
+    const V3 rd{d[3 * i], d[3 * i + 1], d[3 * i + 2]};
+    HitRec h;
+    const bool hit = trace_closest(s, ro, rd, &h);
+    prim[i] = hit ? h.gid : 0xffffffffu;
+    tout[i] = hit ? h.t : FLT_MAX;
+    occ[i] = trace_occluded(s, ro, rd, tmax[i]) ? 1u : 0u;
+}
+
+inline unsigned grid(uint64_t n, unsigned b) { return static_cast<unsigned>((n + b - 1) / b); }
+
+}  // namespace
+
+void launch_plain_paths(const DevScene& s, const DevRequest& q, uint64_t pathBase, uint32_t count, float4* records,
+                        cudaStream_t stream) {
+    if (count == 0) return;
+    k_plain_paths<<<grid(count, 128), 128, 0, stream>>>(s, q, pathBase, count, records);
+}
+
+void launch_resolve_pixels(const DevRequest& q, uint64_t pixelBase, uint32_t count, const float4* records, AovPtrs aov,
+                           cudaStream_t stream) {
+    if (count == 0) return;
+    k_resolve<<<grid(count, 128), 128, 0, stream>>>(q, pixelBase, count, records, aov);
+}
+
+void launch_primary_hits(const DevScene& s, const DevRequest& q, uint32_t* prim, float* t, cudaStream_t stream) {
+    const uint64_t n = static_cast<uint64_t>(q.width) * q.height;
+    if (n == 0) return;
+    k_primary_hits<<<grid(n, 128), 128, 0, stream>>>(s, q, prim, t);
+}
+
+void launch_trace_rays(const DevScene& s, const float* o, const float* d, const float* tmax, uint32_t n, uint32_t* prim,
+                       float* t, uint32_t* occ, cudaStream_t stream) {
+    if (n == 0) return;
+    k_trace_rays<<<grid(n, 128), 128, 0, stream>>>(s, o, d, tmax, n, prim, t, occ);
+}
+
+}  // namespace shiro_gpu

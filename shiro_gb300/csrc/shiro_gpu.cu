@@ -1,0 +1,880 @@
+// shiro_gpu.cu - C ABI of the GB300 path-tracing backend (include/shiro_gpu.h).
+//
+// Host side of the plain form: context management, scene upload (flattening
+// of the Scene snapshot, device BVH build, dome importance tables), the
+// RenderSampleBatch entry point and the parity probes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "bvh_build.h"
+#include "context.h"
+#include "kernels.h"
+
+using namespace shiro_gpu;
+
+namespace shiro_gpu {
+
+namespace {
+thread_local std::string gCreateError;
+constexpr float kHostPi = 3.14159265358979323846f;
+
+void free_block(DeviceBlock* b) {
+    if (b->ptr) cudaFree(b->ptr);
+    b->ptr = nullptr;
+    b->bytes = 0;
+}
+
+template <typename T>
+int upload(ContextImpl* ctx, const std::vector<T>& v, const T** out, const char* what) {
+    DeviceBlock b;
+    const size_t bytes = std::max<size_t>(v.size() * sizeof(T), 16);
+    cudaError_t e = cudaMalloc(&b.ptr, bytes);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, what);
+    b.bytes = bytes;
+    ctx->sceneBlocks.push_back(b);
+    if (!v.empty()) {
+        e = cudaMemcpyAsync(b.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, what);
+    }
+    *out = static_cast<const T*>(b.ptr);
+    return SHIRO_OK;
+}
+
+ShiroMaterialDesc default_material() {  // PbrMaterial defaults, Renderer.h:56-102
+    ShiroMaterialDesc m;
+    std::memset(&m, 0, sizeof(m));
+    for (int k = 0; k < 3; ++k) {
+        m.base_color[k] = 0.8f;
+        m.specular_color[k] = 1.0f;
+        m.transmission_color[k] = 1.0f;
+        m.coat_color[k] = 1.0f;
+        m.subsurface_color[k] = 1.0f;
+        m.subsurface_radius[k] = 1.0f;
+        m.sheen_color[k] = 1.0f;
+    }
+    m.base_weight = 1.0f;
+    m.specular_weight = 1.0f;
+    m.roughness = 0.5f;
+    m.opacity = 1.0f;
+    m.coat_roughness = 0.03f;
+    m.coat_ior = 1.5f;
+    m.sheen_roughness = 0.3f;
+    m.subsurface_scale = 1.0f;
+    m.ior = 1.5f;
+    m.thin_film_ior = 1.5f;
+    return m;
+}
+
+inline float hclamp(float v, float lo, float hi) { return v < lo ? lo : (hi < v ? hi : v); }
+inline float hmax(float a, float b) { return a < b ? b : a; }
+
+// TransmissionSampleWeight > 0 (CpuPathTracer.cpp:1391-1403), evaluated with
+// the reference's arithmetic.
+bool has_transmission(const ShiroMaterialDesc& m) {
+    const float tr = hclamp(m.transmission, 0.0f, 1.0f);
+    const float metal = hclamp(m.metallic, 0.0f, 1.0f);
+    if (tr <= 0.0f || metal >= 0.999f) return false;
+    auto f0d = [](float ior) {
+        const float s = hmax(ior, 1.0f);
+        const float r = (s - 1.0f) / (s + 1.0f);
+        return r * r;
+    };
+    const float ca = hclamp(m.coat_affect_color * m.coat_weight, 0.0f, 1.0f);
+    float best = 0.0f;
+    for (int k = 0; k < 3; ++k) {
+        const float tint = 1.0f * (1.0f - ca) + hclamp(m.coat_color[k], 0.0f, 1.0f) * ca;
+        const float cf0 = m.coat_color[k] * (hclamp(m.coat_weight, 0.0f, 1.0f) * f0d(m.coat_ior));
+        const float uc = tint * hclamp(1.0f - cf0, 0.0f, 1.0f);
+        const float d = m.specular_color[k] * (hclamp(m.specular_weight, 0.0f, 1.0f) * f0d(m.ior));
+        const float sf0 = d * (1.0f - metal) + m.base_color[k] * metal;
+        const float ub = hclamp(1.0f - sf0, 0.0f, 1.0f);
+        best = hmax(best, hclamp(m.transmission_color[k], 0.0f, 1.0f) * uc * ub);
+    }
+    return hmax(0.0f, best) * tr * (1.0f - metal) > 0.0f;
+}
+
+}  // namespace
+
+ContextImpl::~ContextImpl() {
+    wavefront_free(this);
+    adjoint_free(this);
+    freeScene();
+    free_block(&pathRecords);
+    free_block(&aovScratch);
+    free_block(&probeScratch);
+    if (errorWord) cudaFree(errorWord);
+    if (ownStream) cudaStreamDestroy(ownStream);
+}
+
+void ContextImpl::freeScene() {
+    for (auto& b : sceneBlocks) free_block(&b);
+    sceneBlocks.clear();
+    envDev.clear();
+    envHost.clear();
+    domeEnv.clear();
+    materialsHost.clear();
+    hasScene = false;
+    scene = DevScene{};
+}
+
+size_t ContextImpl::deviceBytes() const {
+    size_t n = pathRecords.bytes + aovScratch.bytes + probeScratch.bytes;
+    for (const auto& b : sceneBlocks) n += b.bytes;
+    return n;
+}
+
+bool ensure_block(ContextImpl* ctx, DeviceBlock* b, size_t bytes, const char* what) {
+    if (b->bytes >= bytes) return true;
+    free_block(b);
+    const cudaError_t e = cudaMalloc(&b->ptr, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        ctx->lastError = std::string(what) + ": cudaMalloc(" + std::to_string(bytes) + "): " + cudaGetErrorString(e);
+        b->ptr = nullptr;
+        return false;
+    }
+    b->bytes = bytes;
+    return true;
+}
+
+int fail(ContextImpl* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->lastError = msg;
+    return code;
+}
+
+int cuda_fail(ContextImpl* ctx, cudaError_t e, const char* what) {
+    cudaGetLastError();
+    return fail(ctx, e == cudaErrorMemoryAllocation ? SHIRO_ERR_OUT_OF_MEMORY : SHIRO_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+DevRequest make_request(const ShiroRenderDesc& r) {
+    DevRequest q{};
+    const ShiroCameraDesc& c = r.camera;
+    q.camPos = ld3(c.position);
+    q.camForward = ld3(c.forward);
+    q.camRight = ld3(c.right);
+    q.camUp = ld3(c.up);
+    q.tanHalfFov = std::tan(c.vertical_fov_degrees * 0.5f * kHostPi / 180.0f);
+    q.aspect = c.aspect_ratio;
+    q.width = r.settings.width;
+    q.height = r.settings.height;
+    q.sampleStart = r.sample_start;
+    q.sampleCount = r.sample_count;
+    q.maxDepth = r.settings.max_depth;
+    q.diffuseDepth = r.settings.diffuse_depth;
+    q.specularDepth = r.settings.specular_depth;
+    q.domeSamples = std::max(1u, r.settings.dome_light_samples);
+    q.backgroundVisible = r.settings.background_visible ? 1u : 0u;
+    q.flags = r.flags;
+    return q;
+}
+
+int validate_request(ContextImpl* ctx, const ShiroRenderDesc& r) {
+    if (!ctx->hasScene) return fail(ctx, SHIRO_ERR_NO_SCENE, "no scene uploaded");
+    const uint64_t px = static_cast<uint64_t>(r.settings.width) * r.settings.height;
+    if (px > (1ull << 31)) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "frame too large");
+    if (r.flags & ~(SHIRO_RENDER_ENV_CDF | SHIRO_RENDER_NO_CLAMP)) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "unknown flags");
+    return SHIRO_OK;
+}
+
+// EnvironmentMap::BuildImportanceTable (EnvironmentMap.cpp:185-236), float
+// arithmetic in the reference's order; also records each texel's probability
+// mass rowMass * columnMass (LatLongPdf, :302-313).
+void build_env_table(EnvHost& e) {
+    e.rowCdf.clear();
+    e.condCdf.clear();
+    e.mass.assign(static_cast<size_t>(e.w) * e.h, 0.0f);
+    if (e.w == 0 || e.h == 0 || !e.latlong) return;
+    const uint32_t w = e.w, h = e.h;
+    e.rowCdf.assign(h + 1u, 0.0f);
+    e.condCdf.assign(static_cast<size_t>(h) * (w + 1u), 0.0f);
+    float total = 0.0f;
+    for (uint32_t y = 0; y < h; ++y) {
+        const float theta = (static_cast<float>(y) + 0.5f) * kHostPi / static_cast<float>(h);
+        const float sinT = std::max(std::sin(theta), 1.0e-6f);
+        const size_t off = static_cast<size_t>(y) * (w + 1u);
+        float row = 0.0f;
+        for (uint32_t x = 0; x < w; ++x) {
+            const float* c = &e.rgb[3 * (static_cast<size_t>(y) * w + x)];
+            const float lum = c[0] * 0.2126f + c[1] * 0.7152f + c[2] * 0.0722f;
+            row += std::max(0.0f, lum) * sinT;
+            e.condCdf[off + x + 1u] = row;
+        }
+        if (row > 0.0f) {
+            for (uint32_t x = 1; x <= w; ++x) e.condCdf[off + x] /= row;
+        } else {
+            for (uint32_t x = 1; x <= w; ++x) e.condCdf[off + x] = static_cast<float>(x) / static_cast<float>(w);
+            row = 1.0f;
+        }
+        total += row;
+        e.rowCdf[y + 1u] = total;
+    }
+    if (total <= 0.0f) {
+        for (uint32_t y = 1; y <= h; ++y) e.rowCdf[y] = static_cast<float>(y) / static_cast<float>(h);
+    } else {
+        for (uint32_t y = 1; y <= h; ++y) e.rowCdf[y] /= total;
+    }
+    for (uint32_t y = 0; y < h; ++y) {
+        const float rowMass = e.rowCdf[y + 1u] - e.rowCdf[y];
+        const size_t off = static_cast<size_t>(y) * (w + 1u);
+        for (uint32_t x = 0; x < w; ++x) {
+            const float colMass = e.condCdf[off + x + 1u] - e.condCdf[off + x];
+            e.mass[static_cast<size_t>(y) * w + x] = rowMass * colMass;
+        }
+    }
+}
+
+namespace {
+
+// Walker / Vose alias table over the texel masses: entry i accepts itself
+// when u < threshold[i], else jumps to alias[i].
+std::vector<uint2> build_alias(const std::vector<float>& mass) {
+    const size_t n = mass.size();
+    std::vector<uint2> out(n);
+    double sum = 0.0;
+    for (float m : mass) sum += std::max(0.0f, m);
+    std::vector<double> scaled(n);
+    std::vector<uint32_t> small, large;
+    small.reserve(n);
+    large.reserve(n);
+    for (size_t i = 0; i < n; ++i) {
+        scaled[i] = sum > 0.0 ? std::max(0.0f, mass[i]) / sum * static_cast<double>(n) : 1.0;
+        (scaled[i] < 1.0 ? small : large).push_back(static_cast<uint32_t>(i));
+    }
+    std::vector<float> thr(n, 1.0f);
+    std::vector<uint32_t> alias(n);
+    std::iota(alias.begin(), alias.end(), 0u);
+    while (!small.empty() && !large.empty()) {
+        const uint32_t s = small.back();
+        small.pop_back();
+        const uint32_t l = large.back();
+        large.pop_back();
+        thr[s] = static_cast<float>(scaled[s]);
+        alias[s] = l;
+        scaled[l] = (scaled[l] + scaled[s]) - 1.0;
+        (scaled[l] < 1.0 ? small : large).push_back(l);
+    }
+    for (uint32_t i : large) thr[i] = 1.0f;
+    for (uint32_t i : small) thr[i] = 1.0f;  // rounding leftovers
+    for (size_t i = 0; i < n; ++i) {
+        uint32_t bits;
+        std::memcpy(&bits, &thr[i], 4);
+        out[i] = make_uint2(bits, alias[i]);
+    }
+    return out;
+}
+
+}  // namespace
+
+int upload_envs(ContextImpl* ctx) {
+    // env blocks are appended to sceneBlocks; the env table itself is
+    // rewritten in place.
+    for (size_t k = 0; k < ctx->envHost.size(); ++k) {
+        EnvHost& e = ctx->envHost[k];
+        build_env_table(e);
+        const size_t n = static_cast<size_t>(e.w) * e.h;
+        std::vector<float4> tex(n);
+        for (size_t i = 0; i < n; ++i) tex[i] = make_float4(e.rgb[3 * i], e.rgb[3 * i + 1], e.rgb[3 * i + 2], e.mass[i]);
+        DevEnv& d = ctx->envDev[k];
+        const bool fresh = d.texels == nullptr;
+        if (fresh) {
+            int rc;
+            if ((rc = upload(ctx, tex, &d.texels, "env texels")) != SHIRO_OK) return rc;
+            if ((rc = upload(ctx, e.rowCdf, &d.rowCdf, "env row cdf")) != SHIRO_OK) return rc;
+            if ((rc = upload(ctx, e.condCdf, &d.condCdf, "env conditional cdf")) != SHIRO_OK) return rc;
+            const std::vector<uint2> al = e.latlong ? build_alias(e.mass) : std::vector<uint2>();
+            if ((rc = upload(ctx, al, &d.alias, "env alias")) != SHIRO_OK) return rc;
+        } else {
+            cudaError_t err = cudaMemcpyAsync(const_cast<float4*>(d.texels), tex.data(), n * sizeof(float4),
+                                              cudaMemcpyHostToDevice, ctx->stream);
+            if (err == cudaSuccess && !e.rowCdf.empty())
+                err = cudaMemcpyAsync(const_cast<float*>(d.rowCdf), e.rowCdf.data(), e.rowCdf.size() * 4,
+                                      cudaMemcpyHostToDevice, ctx->stream);
+            if (err == cudaSuccess && !e.condCdf.empty())
+                err = cudaMemcpyAsync(const_cast<float*>(d.condCdf), e.condCdf.data(), e.condCdf.size() * 4,
+                                      cudaMemcpyHostToDevice, ctx->stream);
+            const std::vector<uint2> al = e.latlong ? build_alias(e.mass) : std::vector<uint2>();
+            if (err == cudaSuccess && !al.empty())
+                err = cudaMemcpyAsync(const_cast<uint2*>(d.alias), al.data(), al.size() * sizeof(uint2),
+                                      cudaMemcpyHostToDevice, ctx->stream);
+            if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
+            if (err != cudaSuccess) return cuda_fail(ctx, err, "env update");
+        }
+        d.w = e.w;
+        d.h = e.h;
+        d.latlong = e.latlong ? 1u : 0u;
+        d.hasTable = (e.latlong && !e.rowCdf.empty()) ? 1u : 0u;
+    }
+    return SHIRO_OK;
+}
+
+int check_device_error(ContextImpl* ctx) {
+    uint32_t word = 0;
+    cudaError_t e = cudaMemcpyAsync(&word, ctx->errorWord, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel execution");
+    if (word != 0) {
+        cudaMemsetAsync(ctx->errorWord, 0, 4, ctx->stream);
+        std::string msg = "device check failed:";
+        if (word & kErrTraversalLimit) msg += " traversal visit limit reached;";
+        if (word & kErrStackOverflow) msg += " traversal stack overflow;";
+        if (word & kErrBadIndex) msg += " index out of range;";
+        if (word & kErrQueueOverflow) msg += " queue overflow;";
+        return fail(ctx, SHIRO_ERR_DEVICE_CHECK, msg);
+    }
+    return SHIRO_OK;
+}
+
+}  // namespace shiro_gpu
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+namespace {
+
+int supports(const ShiroSceneDesc* scene, std::string* why) {
+    if (!scene) {
+        *why = "null scene";
+        return 0;
+    }
+    for (uint32_t i = 0; i < scene->material_count; ++i) {
+        const ShiroMaterialDesc& m = scene->materials[i];
+        if (has_transmission(m)) {
+            *why = "material " + std::to_string(i) + " uses transmission";
+            return 0;
+        }
+        if (hclamp(m.opacity, 0.0f, 1.0f) < 0.999f) {
+            *why = "material " + std::to_string(i) + " uses opacity";
+            return 0;
+        }
+        if (m.emission_strength > 0.0f) {
+            *why = "material " + std::to_string(i) + " is emissive";
+            return 0;
+        }
+    }
+    return 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int shiro_gpu_status(ShiroBackendStatus* out) {
+    if (!out) return SHIRO_ERR_INVALID_ARGUMENT;
+    std::memset(out, 0, sizeof(*out));
+    out->kind = SHIRO_BACKEND_GPU;
+    std::snprintf(out->name, sizeof(out->name), "gb300");
+    out->uses_gpu = 1;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        return SHIRO_OK;
+    }
+    out->device_count = static_cast<uint32_t>(count);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, 0) == cudaSuccess) {
+        std::snprintf(out->device_name, sizeof(out->device_name), "%s", prop.name);
+        out->compute_major = prop.major;
+        out->compute_minor = prop.minor;
+        // the kernels are built for sm_103a only
+        out->available = (prop.major == 10 && prop.minor == 3) ? 1u : 0u;
+    }
+    return SHIRO_OK;
+}
+
+int shiro_gpu_create(int device, ShiroGpuContext** out) {
+    if (!out) return SHIRO_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        gCreateError = "no CUDA device";
+        return SHIRO_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) {
+        gCreateError = "device index out of range";
+        return SHIRO_ERR_INVALID_ARGUMENT;
+    }
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        gCreateError = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+        return SHIRO_ERR_CUDA;
+    }
+    auto* ctx = new (std::nothrow) ShiroGpuContext();
+    if (!ctx) return SHIRO_ERR_OUT_OF_MEMORY;
+    ContextImpl& c = ctx->impl;
+    c.device = device;
+    e = cudaStreamCreateWithFlags(&c.ownStream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c.errorWord, 16);
+    if (e == cudaSuccess) e = cudaMemset(c.errorWord, 0, 16);
+    if (e != cudaSuccess) {
+        gCreateError = std::string("context setup: ") + cudaGetErrorString(e);
+        delete ctx;
+        return e == cudaErrorMemoryAllocation ? SHIRO_ERR_OUT_OF_MEMORY : SHIRO_ERR_CUDA;
+    }
+    c.stream = c.ownStream;
+    *out = ctx;
+    return SHIRO_OK;
+}
+
+void shiro_gpu_destroy(ShiroGpuContext* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->impl.device);
+    if (ctx->impl.stream) cudaStreamSynchronize(ctx->impl.stream);
+    delete ctx;
+}
+
+const char* shiro_gpu_last_error(const ShiroGpuContext* ctx) {
+    if (!ctx) return gCreateError.c_str();
+    return ctx->impl.lastError.c_str();
+}
+
+int shiro_gpu_set_stream(ShiroGpuContext* ctx, void* stream) {
+    if (!ctx) return SHIRO_ERR_INVALID_ARGUMENT;
+    ctx->impl.stream = stream ? static_cast<cudaStream_t>(stream) : ctx->impl.ownStream;
+    return SHIRO_OK;
+}
+
+int shiro_gpu_supports_scene(const ShiroSceneDesc* scene, char* reason, size_t reason_size) {
+    std::string why;
+    const int ok = supports(scene, &why);
+    if (reason && reason_size) std::snprintf(reason, reason_size, "%s", why.c_str());
+    return ok;
+}
+
+int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
+    if (!handle || !sd) return SHIRO_ERR_INVALID_ARGUMENT;
+    ContextImpl* ctx = &handle->impl;
+    cudaSetDevice(ctx->device);
+    std::string why;
+    if (!supports(sd, &why)) return fail(ctx, SHIRO_ERR_UNSUPPORTED_SCENE, "unsupported scene: " + why);
+    if (sd->mesh_count && !sd->meshes) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "null mesh array");
+    if (sd->material_count && !sd->materials) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "null material array");
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->freeScene();
+
+    // --- flatten ------------------------------------------------------------
+    std::vector<float4> positions, normals;
+    std::vector<uint4> triVerts;
+    std::vector<uint32_t> meshMaterial(sd->mesh_count), meshHasNormals(sd->mesh_count);
+    size_t vtotal = 0, ttotal = 0;
+    for (uint32_t i = 0; i < sd->mesh_count; ++i) {
+        const ShiroMeshDesc& m = sd->meshes[i];
+        if ((m.vertex_count && !m.positions) || (m.index_count && !m.indices))
+            return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "mesh " + std::to_string(i) + ": null array");
+        vtotal += m.vertex_count;
+        ttotal += m.index_count / 3u;
+    }
+    if (ttotal >= (1ull << 28) || vtotal >= (1ull << 32))
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene exceeds 2^28 triangles");
+    positions.reserve(vtotal);
+    normals.reserve(vtotal);
+    triVerts.reserve(ttotal);
+    std::vector<float4> triData;      // small triangles: 3 per
+    std::vector<float4> primBoxes;    // 2 per
+    std::vector<float4> centroids;
+    struct Cand {
+        float area;
+        uint32_t gid;
+    };
+    std::vector<float4> allTri(3 * ttotal);
+    std::vector<float> boxes(6 * ttotal);
+    float mag = 0.0f;
+    float slo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, shi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    uint32_t gid = 0;
+    for (uint32_t i = 0; i < sd->mesh_count; ++i) {
+        const ShiroMeshDesc& m = sd->meshes[i];
+        const uint32_t base = static_cast<uint32_t>(positions.size());
+        for (uint32_t v = 0; v < m.vertex_count; ++v) {
+            const float* p = m.positions + 3 * static_cast<size_t>(v);
+            positions.push_back(make_float4(p[0], p[1], p[2], 0.0f));
+            mag = std::max(mag, std::max(std::fabs(p[0]), std::max(std::fabs(p[1]), std::fabs(p[2]))));
+        }
+        const bool hasN = m.normals && m.normal_count == m.vertex_count;
+        for (uint32_t v = 0; v < m.vertex_count; ++v) {
+            if (hasN) {
+                const float* n = m.normals + 3 * static_cast<size_t>(v);
+                normals.push_back(make_float4(n[0], n[1], n[2], 0.0f));
+            } else {
+                normals.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+            }
+        }
+        meshHasNormals[i] = hasN ? 1u : 0u;
+        meshMaterial[i] = m.material_index < sd->material_count ? m.material_index : sd->material_count;
+        const uint32_t tris = m.index_count / 3u;
+        for (uint32_t t = 0; t < tris; ++t, ++gid) {
+            const uint32_t a = m.indices[3 * t], b = m.indices[3 * t + 1], c = m.indices[3 * t + 2];
+            if (a >= m.vertex_count || b >= m.vertex_count || c >= m.vertex_count)
+                return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT,
+                            "mesh " + std::to_string(i) + ": index out of range at triangle " + std::to_string(t));
+            triVerts.push_back(make_uint4(base + a, base + b, base + c, i));
+            const float* p0 = m.positions + 3 * static_cast<size_t>(a);
+            const float* p1 = m.positions + 3 * static_cast<size_t>(b);
+            const float* p2 = m.positions + 3 * static_cast<size_t>(c);
+            float gbits;
+            std::memcpy(&gbits, &gid, 4);
+            allTri[3 * gid] = make_float4(p0[0], p0[1], p0[2], gbits);
+            allTri[3 * gid + 1] = make_float4(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], 0.0f);
+            allTri[3 * gid + 2] = make_float4(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2], 0.0f);
+            for (int k = 0; k < 3; ++k) {
+                const float lo = std::min(p0[k], std::min(p1[k], p2[k]));
+                const float hi = std::max(p0[k], std::max(p1[k], p2[k]));
+                boxes[6 * gid + k] = lo;
+                boxes[6 * gid + 3 + k] = hi;
+                slo[k] = std::min(slo[k], lo);
+                shi[k] = std::max(shi[k], hi);
+            }
+        }
+    }
+    if (ttotal == 0) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene has no triangles");
+
+    // --- large triangles + inflated boxes -----------------------------------
+    auto area = [](const float* lo, const float* hi) {
+        const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        return 2.0f * (dx * dy + dy * dz + dz * dx);
+    };
+    const float sceneArea = area(slo, shi);
+    std::vector<Cand> cand;
+    for (uint32_t g = 0; g < ttotal; ++g) {
+        const float a = area(&boxes[6 * g], &boxes[6 * g + 3]);
+        if (ttotal > 16 && a > 0.05f * sceneArea) cand.push_back({a, g});
+    }
+    std::sort(cand.begin(), cand.end(), [](const Cand& x, const Cand& y) { return x.area > y.area || (x.area == y.area && x.gid < y.gid); });
+    if (cand.size() > 8) cand.resize(8);
+    std::vector<uint8_t> isLarge(ttotal, 0);
+    for (const Cand& c : cand) isLarge[c.gid] = 1;
+    const float pad = mag * 1.0e-5f + 1.0e-30f;
+    BvhInput bin;
+    triData.reserve(3 * ttotal);
+    primBoxes.reserve(2 * ttotal);
+    centroids.reserve(ttotal);
+    for (uint32_t g = 0; g < ttotal; ++g) {
+        float lo[3], hi[3];
+        for (int k = 0; k < 3; ++k) {
+            const float e = pad + (boxes[6 * g + 3 + k] - boxes[6 * g + k]) * 1.0e-5f;
+            lo[k] = boxes[6 * g + k] - e;
+            hi[k] = boxes[6 * g + 3 + k] + e;
+        }
+        if (isLarge[g]) {
+            LargeTri lt;
+            for (int k = 0; k < 3; ++k) {
+                lt.tri[k] = allTri[3 * g + k];
+                lt.lo[k] = lo[k];
+                lt.hi[k] = hi[k];
+            }
+            bin.largeSlots.push_back(lt);
+            continue;
+        }
+        triData.push_back(allTri[3 * g]);
+        triData.push_back(allTri[3 * g + 1]);
+        triData.push_back(allTri[3 * g + 2]);
+        primBoxes.push_back(make_float4(lo[0], lo[1], lo[2], 0.0f));
+        primBoxes.push_back(make_float4(hi[0], hi[1], hi[2], 0.0f));
+        centroids.push_back(make_float4(0.5f * (boxes[6 * g] + boxes[6 * g + 3]), 0.5f * (boxes[6 * g + 1] + boxes[6 * g + 4]),
+                                        0.5f * (boxes[6 * g + 2] + boxes[6 * g + 5]), 0.0f));
+    }
+    std::vector<float4>().swap(allTri);
+    std::vector<float>().swap(boxes);
+
+    int rc;
+    const float4 *dTri = nullptr, *dBox = nullptr, *dCen = nullptr;
+    if ((rc = upload(ctx, triData, &dTri, "triangle staging")) != SHIRO_OK) return rc;
+    if ((rc = upload(ctx, primBoxes, &dBox, "box staging")) != SHIRO_OK) return rc;
+    if ((rc = upload(ctx, centroids, &dCen, "centroid staging")) != SHIRO_OK) return rc;
+    bin.triData = dTri;
+    bin.primBoxes = dBox;
+    bin.centroids = dCen;
+    bin.smallCount = static_cast<uint32_t>(centroids.size());
+    BvhOutput bout;
+    std::string berr;
+    rc = build_bvh(bin, ctx->stream, &bout, berr);
+    // staging blocks are no longer needed
+    for (int k = 0; k < 3; ++k) {
+        free_block(&ctx->sceneBlocks.back());
+        ctx->sceneBlocks.pop_back();
+    }
+    if (rc != SHIRO_OK) {
+        if (bout.nodes) cudaFree(bout.nodes);
+        if (bout.tris) cudaFree(bout.tris);
+        return fail(ctx, rc, "BVH build: " + berr);
+    }
+    if (bout.depth + 4 > static_cast<uint32_t>(kStack)) {
+        cudaFree(bout.nodes);
+        cudaFree(bout.tris);
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "BVH deeper than the traversal stack");
+    }
+    ctx->sceneBlocks.push_back({bout.nodes, 4 * sizeof(float4) * bout.nodeCount});
+    ctx->sceneBlocks.push_back({bout.tris, 3 * sizeof(float4) * bout.triCount});
+    ctx->bvhDepth = bout.depth;
+    ctx->bvhMaxLeaf = bout.maxLeaf;
+    DevScene& s = ctx->scene;
+    s.nodes = bout.nodes;
+    s.tris = bout.tris;
+    s.nodeCount = bout.nodeCount;
+    s.triCount = bout.triCount;
+
+    // --- shading data ----------------------------------------------------------
+    ctx->materialsHost.assign(sd->materials, sd->materials + sd->material_count);
+    ctx->materialsHost.push_back(default_material());
+    ctx->materialCount = sd->material_count;
+    if ((rc = upload(ctx, triVerts, &s.triVerts, "triangle vertices")) != SHIRO_OK) return rc;
+    if ((rc = upload(ctx, normals, &s.normals, "normals")) != SHIRO_OK) return rc;
+    if ((rc = upload(ctx, positions, &s.positions, "positions")) != SHIRO_OK) return rc;
+    if ((rc = upload(ctx, meshMaterial, &s.meshMaterial, "mesh materials")) != SHIRO_OK) return rc;
+    if ((rc = upload(ctx, meshHasNormals, &s.meshHasNormals, "mesh normal flags")) != SHIRO_OK) return rc;
+    if ((rc = upload(ctx, ctx->materialsHost, &s.materials, "materials")) != SHIRO_OK) return rc;
+    std::vector<DevDistant> distant(sd->distant_light_count);
+    for (uint32_t i = 0; i < sd->distant_light_count; ++i)
+        distant[i] = DevDistant{ld3(sd->distant_lights[i].direction), ld3(sd->distant_lights[i].radiance)};
+    if ((rc = upload(ctx, distant, &s.distant, "distant lights")) != SHIRO_OK) return rc;
+    s.distantCount = sd->distant_light_count;
+
+    std::vector<DevDome> domes(sd->dome_light_count);
+    for (uint32_t i = 0; i < sd->dome_light_count; ++i) {
+        const ShiroDomeLightDesc& d = sd->dome_lights[i];
+        domes[i].radiance = ld3(d.radiance);
+        domes[i].right = ld3(d.right);
+        domes[i].up = ld3(d.up);
+        domes[i].forward = ld3(d.forward);
+        domes[i].env = -1;
+        if (d.env_pixels && d.env_width && d.env_height) {
+            EnvHost e;
+            e.w = d.env_width;
+            e.h = d.env_height;
+            e.latlong = d.layout != SHIRO_ENV_LAYOUT_ANGULAR;
+            e.rgb.assign(d.env_pixels, d.env_pixels + 3 * static_cast<size_t>(e.w) * e.h);
+            domes[i].env = static_cast<int32_t>(ctx->envHost.size());
+            ctx->envHost.push_back(std::move(e));
+        }
+        ctx->domeEnv.push_back(domes[i].env);
+    }
+    ctx->envDev.assign(ctx->envHost.size(), DevEnv{});
+    if ((rc = upload_envs(ctx)) != SHIRO_OK) return rc;
+    if ((rc = upload(ctx, ctx->envDev, &s.envs, "env table")) != SHIRO_OK) return rc;
+    if ((rc = upload(ctx, domes, &s.domes, "dome lights")) != SHIRO_OK) return rc;
+    s.domeCount = sd->dome_light_count;
+    s.envTop = ld3(sd->environment_top);
+    s.envBottom = ld3(sd->environment_bottom);
+    s.error = ctx->errorWord;
+    const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "scene upload");
+    ctx->hasScene = true;
+    ctx->stats = ShiroRenderStats{};
+    ctx->stats.bvh_nodes = s.nodeCount;
+    ctx->stats.triangles = s.triCount;
+    ctx->stats.bvh_depth = ctx->bvhDepth;
+    ctx->stats.bvh_max_leaf = ctx->bvhMaxLeaf;
+    ctx->stats.device_bytes = ctx->deviceBytes();
+    return SHIRO_OK;
+}
+
+int shiro_gpu_render(ShiroGpuContext* handle, const ShiroRenderDesc* req, const volatile int* cancel, ShiroAovs* out) {
+    if (!handle || !req || !out) return SHIRO_ERR_INVALID_ARGUMENT;
+    ContextImpl* ctx = &handle->impl;
+    cudaSetDevice(ctx->device);
+    int rc = validate_request(ctx, *req);
+    if (rc != SHIRO_OK) return rc;
+    if (!out->beauty || !out->albedo || !out->normal || !out->depth)
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "null AOV pointer");
+    const DevRequest q = make_request(*req);
+    const uint64_t pixels = static_cast<uint64_t>(q.width) * q.height;
+    ctx->stats.paths = 0;
+    ctx->stats.kernel_launches = 0;
+    ctx->stats.kernel_ms = 0.0;
+    // AOV destination: caller's device planes or the context's staging planes
+    AovPtrs aov;
+    if (out->on_device) {
+        aov = AovPtrs{out->beauty, out->albedo, out->normal, out->depth};
+    } else {
+        if (!ensure_block(ctx, &ctx->aovScratch, std::max<uint64_t>(pixels, 1) * 11 * sizeof(float), "AOV staging"))
+            return SHIRO_ERR_OUT_OF_MEMORY;
+        float* b = static_cast<float*>(ctx->aovScratch.ptr);
+        aov = AovPtrs{b, b + 4 * pixels, b + 7 * pixels, b + 10 * pixels};
+    }
+    auto clear_host = [&]() {
+        if (out->on_device) return;
+        for (uint64_t i = 0; i < pixels; ++i) {
+            for (int c = 0; c < 4; ++c) out->beauty[4 * i + c] = 0.0f;
+            for (int c = 0; c < 3; ++c) out->albedo[3 * i + c] = out->normal[3 * i + c] = 0.0f;
+            out->depth[i] = std::numeric_limits<float>::infinity();
+        }
+    };
+    if (req->sample_count == 0 || pixels == 0) {
+        // FrameBuffer::Clear semantics (FrameBuffer.cpp:19-24)
+        if (out->on_device) {
+            cudaMemsetAsync(out->beauty, 0, pixels * 16, ctx->stream);
+            cudaMemsetAsync(out->albedo, 0, pixels * 12, ctx->stream);
+            cudaMemsetAsync(out->normal, 0, pixels * 12, ctx->stream);
+            std::vector<float> inf(pixels, std::numeric_limits<float>::infinity());
+            if (pixels) cudaMemcpyAsync(out->depth, inf.data(), pixels * 4, cudaMemcpyHostToDevice, ctx->stream);
+            cudaStreamSynchronize(ctx->stream);
+        } else {
+            clear_host();
+        }
+        return SHIRO_OK;
+    }
+    // paths in flight per launch: whole pixels, at most 2^24 paths (805 MB of records)
+    const uint64_t maxPaths = 1ull << 24;
+    const uint64_t pixelsPerChunk = std::max<uint64_t>(1, maxPaths / q.sampleCount);
+    const uint64_t recBytes = std::min<uint64_t>(pixelsPerChunk, pixels) * q.sampleCount * kPathRecordBytes;
+    if (!ensure_block(ctx, &ctx->pathRecords, recBytes, "path records")) return SHIRO_ERR_OUT_OF_MEMORY;
+    float4* rec = static_cast<float4*>(ctx->pathRecords.ptr);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, ctx->stream);
+    for (uint64_t p0 = 0; p0 < pixels; p0 += pixelsPerChunk) {
+        if (cancel && *cancel) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            clear_host();
+            return fail(ctx, SHIRO_ERR_CANCELLED, "cancelled");
+        }
+        const uint32_t np = static_cast<uint32_t>(std::min(pixelsPerChunk, pixels - p0));
+        const uint64_t paths = static_cast<uint64_t>(np) * q.sampleCount;
+        launch_plain_paths(ctx->scene, q, p0 * q.sampleCount, static_cast<uint32_t>(paths), rec, ctx->stream);
+        launch_resolve_pixels(q, p0, np, rec, aov, ctx->stream);
+        ctx->stats.kernel_launches += 2;
+        ctx->stats.paths += paths;
+        const cudaError_t le = cudaGetLastError();
+        if (le != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return cuda_fail(ctx, le, "render launch");
+        }
+    }
+    cudaEventRecord(e1, ctx->stream);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "render");
+    ctx->stats.kernel_ms = ms;
+    if ((rc = check_device_error(ctx)) != SHIRO_OK) return rc;
+    if (!out->on_device) {
+        e = cudaMemcpyAsync(out->beauty, aov.beauty, pixels * 16, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out->albedo, aov.albedo, pixels * 12, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out->normal, aov.normal, pixels * 12, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out->depth, aov.depth, pixels * 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "AOV readback");
+    }
+    ctx->stats.device_bytes = ctx->deviceBytes();
+    return SHIRO_OK;
+}
+
+int shiro_gpu_render_batch(ShiroGpuContext* handle, const ShiroRenderDesc* reqs, uint32_t count, const volatile int* cancel,
+                           ShiroAovs* outs) {
+    if (!handle || (count && (!reqs || !outs))) return SHIRO_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(handle->impl.device);
+    return wavefront_render(&handle->impl, reqs, count, cancel, outs);
+}
+
+int shiro_gpu_get_wavefront_config(const ShiroGpuContext* ctx, ShiroWavefrontConfig* out) {
+    if (!ctx || !out) return SHIRO_ERR_INVALID_ARGUMENT;
+    return wavefront_get_config(&ctx->impl, out);
+}
+
+int shiro_gpu_set_wavefront_config(ShiroGpuContext* ctx, const ShiroWavefrontConfig* cfg) {
+    if (!ctx || !cfg) return SHIRO_ERR_INVALID_ARGUMENT;
+    return wavefront_set_config(&ctx->impl, cfg);
+}
+
+int shiro_gpu_autotune(ShiroGpuContext* ctx, const ShiroRenderDesc* req, ShiroWavefrontConfig* chosen) {
+    if (!ctx || !req) return SHIRO_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->impl.device);
+    return wavefront_autotune(&ctx->impl, req, chosen);
+}
+
+int shiro_gpu_set_params(ShiroGpuContext* ctx, const float* base, const float* rough, const float* metal, const float* env) {
+    if (!ctx) return SHIRO_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->impl.device);
+    return adjoint_set_params(&ctx->impl, base, rough, metal, env);
+}
+
+int shiro_gpu_adjoint(ShiroGpuContext* ctx, const ShiroRenderDesc* req, const float* dBeauty, float* dBase, float* dRough,
+                      float* dMetal, float* dEnv) {
+    if (!ctx || !req || !dBeauty) return SHIRO_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->impl.device);
+    return adjoint_run(&ctx->impl, req, dBeauty, dBase, dRough, dMetal, dEnv);
+}
+
+int shiro_gpu_primary_hits(ShiroGpuContext* handle, const ShiroRenderDesc* req, uint32_t* prim, float* t, uint32_t on_device) {
+    if (!handle || !req || !prim || !t) return SHIRO_ERR_INVALID_ARGUMENT;
+    ContextImpl* ctx = &handle->impl;
+    cudaSetDevice(ctx->device);
+    int rc = validate_request(ctx, *req);
+    if (rc != SHIRO_OK) return rc;
+    const DevRequest q = make_request(*req);
+    const uint64_t n = static_cast<uint64_t>(q.width) * q.height;
+    uint32_t* dp = prim;
+    float* dt = t;
+    if (!on_device) {
+        if (!ensure_block(ctx, &ctx->probeScratch, std::max<uint64_t>(n, 1) * 8, "probe")) return SHIRO_ERR_OUT_OF_MEMORY;
+        dp = static_cast<uint32_t*>(ctx->probeScratch.ptr);
+        dt = reinterpret_cast<float*>(dp + n);
+    }
+    launch_primary_hits(ctx->scene, q, dp, dt, ctx->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "primary hits launch");
+    if ((rc = check_device_error(ctx)) != SHIRO_OK) return rc;
+    if (!on_device) {
+        e = cudaMemcpyAsync(prim, dp, n * 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(t, dt, n * 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "primary hits readback");
+    }
+    return SHIRO_OK;
+}
+
+int shiro_gpu_trace_rays(ShiroGpuContext* handle, const float* origins, const float* dirs, const float* tmax, uint32_t n,
+                         uint32_t* prim, float* t, uint32_t* occ) {
+    if (!handle || (n && (!origins || !dirs || !tmax || !prim || !t || !occ))) return SHIRO_ERR_INVALID_ARGUMENT;
+    ContextImpl* ctx = &handle->impl;
+    cudaSetDevice(ctx->device);
+    if (!ctx->hasScene) return fail(ctx, SHIRO_ERR_NO_SCENE, "no scene uploaded");
+    if (n == 0) return SHIRO_OK;
+    // host arrays: 7 floats in, 3 words out per ray
+    if (!ensure_block(ctx, &ctx->probeScratch, static_cast<size_t>(n) * 10 * 4, "probe")) return SHIRO_ERR_OUT_OF_MEMORY;
+    float* base = static_cast<float*>(ctx->probeScratch.ptr);
+    float *dO = base, *dD = base + 3 * static_cast<size_t>(n), *dM = base + 6 * static_cast<size_t>(n);
+    uint32_t* dP = reinterpret_cast<uint32_t*>(base + 7 * static_cast<size_t>(n));
+    float* dT = base + 8 * static_cast<size_t>(n);
+    uint32_t* dOcc = reinterpret_cast<uint32_t*>(base + 9 * static_cast<size_t>(n));
+    cudaError_t e = cudaMemcpyAsync(dO, origins, 12ull * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dD, dirs, 12ull * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dM, tmax, 4ull * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "trace rays upload");
+    launch_trace_rays(ctx->scene, dO, dD, dM, n, dP, dT, dOcc, ctx->stream);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "trace rays launch");
+    int rc = check_device_error(ctx);
+    if (rc != SHIRO_OK) return rc;
+    e = cudaMemcpyAsync(prim, dP, 4ull * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t, dT, 4ull * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(occ, dOcc, 4ull * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "trace rays readback");
+    return SHIRO_OK;
+}
+
+int shiro_gpu_last_stats(const ShiroGpuContext* ctx, ShiroRenderStats* out) {
+    if (!ctx || !out) return SHIRO_ERR_INVALID_ARGUMENT;
+    *out = ctx->impl.stats;
+    return SHIRO_OK;
+}
+
+}  // extern "C"

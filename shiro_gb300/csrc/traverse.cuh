@@ -1,0 +1,222 @@
+// traverse.cuh - BVH traversal with the reference's hit semantics.
+//
+// The reference (without Embree) intersects every triangle with
+// Moller-Trumbore (CpuPathTracer.cpp:386-429) and keeps a new hit only when
+// strictly closer, so among equal distances the first (mesh, primitive) wins
+// (:431-466).  Here the triangles are reached through a BVH and a hit replaces
+// the best one when (t, global index) is lexicographically smaller, which
+// selects the same triangle.  The triangle test uses the same operations in
+// the same order (compiled without FMA contraction), so t, u, v are
+// bit-identical.  Child boxes are inflated at build time by a margin far above
+// the rounding error of the box test, so a box is never culled while it holds
+// a triangle the exhaustive test would report.
+//
+// Each traversal loop is bounded by kMaxVisits node visits; past that the
+// error word is set and the ray is reported as a miss (a corrupt BVH can never
+// hang the kernel).
+#pragma once
+
+#include "common.cuh"
+#include "scene.cuh"
+
+namespace shiro_gpu {
+
+
+constexpr uint32_t kMaxVisits = 1u << 22;
+
+struct HitRec {
+    float t, u, v;
+    uint32_t slot;  // leaf-order triangle index, 0xffffffff on a miss
+    uint32_t gid;   // global triangle index (meshes in order)
+};
+
+struct RayInv {
+    V3 inv, ood;
+};
+
+__device__ __forceinline__ RayInv ray_inv(const V3& o, const V3& d) {
+    RayInv r;
+    const float dx = fabsf(d.x) > 1.0e-20f ? d.x : copysignf(1.0e-20f, d.x);
+    const float dy = fabsf(d.y) > 1.0e-20f ? d.y : copysignf(1.0e-20f, d.y);
+    const float dz = fabsf(d.z) > 1.0e-20f ? d.z : copysignf(1.0e-20f, d.z);
+    r.inv = V3{1.0f / dx, 1.0f / dy, 1.0f / dz};
+    r.ood = V3{o.x * r.inv.x, o.y * r.inv.y, o.z * r.inv.z};
+    return r;
+}
+
+// Entry / exit of both child boxes of a node (slab test, fused form).
+__device__ __forceinline__ void node_boxes(const float4& n0, const float4& n1, const float4& n2, const RayInv& r,
+                                           float tmax, float* t0, float* t1, bool* h0, bool* h1) {
+    const float ax = __fmaf_rn(n0.x, r.inv.x, -r.ood.x), bx = __fmaf_rn(n0.y, r.inv.x, -r.ood.x);
+    const float ay = __fmaf_rn(n0.z, r.inv.y, -r.ood.y), by = __fmaf_rn(n0.w, r.inv.y, -r.ood.y);
+    const float az = __fmaf_rn(n2.x, r.inv.z, -r.ood.z), bz = __fmaf_rn(n2.y, r.inv.z, -r.ood.z);
+    const float cx = __fmaf_rn(n1.x, r.inv.x, -r.ood.x), dx = __fmaf_rn(n1.y, r.inv.x, -r.ood.x);
+    const float cy = __fmaf_rn(n1.z, r.inv.y, -r.ood.y), dy = __fmaf_rn(n1.w, r.inv.y, -r.ood.y);
+    const float cz = __fmaf_rn(n2.z, r.inv.z, -r.ood.z), dz = __fmaf_rn(n2.w, r.inv.z, -r.ood.z);
+    const float lo0 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fmaxf(fminf(az, bz), 0.0f));
+    const float hi0 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fminf(fmaxf(az, bz), tmax));
+    const float lo1 = fmaxf(fmaxf(fminf(cx, dx), fminf(cy, dy)), fmaxf(fminf(cz, dz), 0.0f));
+    const float hi1 = fminf(fminf(fmaxf(cx, dx), fmaxf(cy, dy)), fminf(fmaxf(cz, dz), tmax));
+    *t0 = lo0;
+    *t1 = lo1;
+    *h0 = lo0 <= hi0;
+    *h1 = lo1 <= hi1;
+}
+
+// Moller-Trumbore, IntersectTriangle (CpuPathTracer.cpp:386-429).
+__device__ __forceinline__ bool tri_test(const V3& o, const V3& d, float tMin, float tMax, const float4& a,
+                                         const float4& b, const float4& c, float* t, float* u, float* v) {
+    const V3 p0 = f4xyz(a), e1 = f4xyz(b), e2 = f4xyz(c);
+    const V3 pvec = cross(d, e2);
+    const float det = dot(e1, pvec);
+    if (fabsf(det) < 1.0e-8f) return false;
+    const float inv = 1.0f / det;
+    const V3 tvec = o - p0;
+    const float uu = dot(tvec, pvec) * inv;
+    if (uu < 0.0f || uu > 1.0f) return false;
+    const V3 qvec = cross(tvec, e1);
+    const float vv = dot(d, qvec) * inv;
+    if (vv < 0.0f || uu + vv > 1.0f) return false;
+    const float tt = dot(e2, qvec) * inv;
+    if (tt < tMin || tt > tMax) return false;
+    *t = tt;
+    *u = uu;
+    *v = vv;
+    return true;
+}
+
+__device__ __noinline__ bool trace_closest(const DevScene& s, const V3 o, const V3 d, HitRec* out) {
+    const RayInv r = ray_inv(o, d);
+    float bestT = FLT_MAX;
+    uint32_t bestGid = 0xffffffffu, bestSlot = 0xffffffffu;
+    float bu = 0.0f, bv = 0.0f;
+    int stackNode[kStack];
+    float stackT[kStack];
+    int sp = 0;
+    int node = 0;
+    uint32_t visits = 0;
+    for (;;) {
+        if (++visits > kMaxVisits) {
+            atomicOr(s.error, kErrTraversalLimit);
+            bestSlot = 0xffffffffu;
+            break;
+        }
+        if (node >= 0) {
+            const float4* np = s.nodes + 4 * static_cast<size_t>(node);
+            const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+            float t0, t1;
+            bool h0, h1;
+            node_boxes(n0, n1, n2, r, bestT, &t0, &t1, &h0, &h1);
+            const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+            if (h0 && h1) {
+                const bool swap = t1 < t0;
+                if (sp >= kStack) {
+                    atomicOr(s.error, kErrStackOverflow);
+                    bestSlot = 0xffffffffu;
+                    break;
+                }
+                stackNode[sp] = swap ? c0 : c1;
+                stackT[sp] = swap ? t0 : t1;
+                ++sp;
+                node = swap ? c1 : c0;
+                continue;
+            }
+            if (h0) {
+                node = c0;
+                continue;
+            }
+            if (h1) {
+                node = c1;
+                continue;
+            }
+        } else {
+            const uint32_t enc = ~static_cast<uint32_t>(node);
+            const uint32_t first = enc >> 3, cnt = (enc & 7u) + 1u;
+            for (uint32_t k = first; k < first + cnt; ++k) {
+                const float4* tp = s.tris + 3 * static_cast<size_t>(k);
+                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                float t, u, v;
+                if (!tri_test(o, d, kRayEpsilon, FLT_MAX, a, b, c, &t, &u, &v)) continue;
+                const uint32_t gid = __float_as_uint(a.w);
+                if (t < bestT || (t == bestT && gid < bestGid)) {
+                    bestT = t;
+                    bestGid = gid;
+                    bestSlot = k;
+                    bu = u;
+                    bv = v;
+                }
+            }
+        }
+        // pop the next entry still in range
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            if (stackT[sp] <= bestT) {
+                node = stackNode[sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    out->t = bestT;
+    out->u = bu;
+    out->v = bv;
+    out->slot = bestSlot;
+    out->gid = bestGid;
+    return bestSlot != 0xffffffffu;
+}
+
+// Any hit with t in [1e-4, maxDist] (Occluded, CpuPathTracer.cpp:468-475).
+__device__ __noinline__ bool trace_occluded(const DevScene& s, const V3 o, const V3 d, float maxDist) {
+    const RayInv r = ray_inv(o, d);
+    int stackNode[kStack];
+    int sp = 0;
+    int node = 0;
+    uint32_t visits = 0;
+    for (;;) {
+        if (++visits > kMaxVisits) {
+            atomicOr(s.error, kErrTraversalLimit);
+            return false;
+        }
+        if (node >= 0) {
+            const float4* np = s.nodes + 4 * static_cast<size_t>(node);
+            const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+            float t0, t1;
+            bool h0, h1;
+            node_boxes(n0, n1, n2, r, maxDist, &t0, &t1, &h0, &h1);
+            const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+            if (h0 && h1) {
+                if (sp >= kStack) {
+                    atomicOr(s.error, kErrStackOverflow);
+                    return false;
+                }
+                const bool swap = t1 < t0;
+                stackNode[sp++] = swap ? c0 : c1;
+                node = swap ? c1 : c0;
+                continue;
+            }
+            if (h0) {
+                node = c0;
+                continue;
+            }
+            if (h1) {
+                node = c1;
+                continue;
+            }
+        } else {
+            const uint32_t enc = ~static_cast<uint32_t>(node);
+            const uint32_t first = enc >> 3, cnt = (enc & 7u) + 1u;
+            for (uint32_t k = first; k < first + cnt; ++k) {
+                const float4* tp = s.tris + 3 * static_cast<size_t>(k);
+                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                float t, u, v;
+                if (tri_test(o, d, kRayEpsilon, maxDist, a, b, c, &t, &u, &v)) return true;
+            }
+        }
+        if (sp == 0) return false;
+        node = stackNode[--sp];
+    }
+}
+
+}  // namespace shiro_gpu
