@@ -1,0 +1,395 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 path-tracing backend.
+
+Workload (default): the 1M-triangle field scene at 1080p - 256 noise-displaced
+icospheres (1 310 720 triangles) + a 50x50 ground quad, 64 standard_surface
+materials, 2048x1024 HDRI dome + one directional light, 1920x1080, 64 spp,
+max depth 12.  One step renders the whole frame (132 710 400 paths).
+
+Metric: Mpaths/s (whole job).  ``value`` is timed with CUDA events on the
+render stream with the scene resident in HBM and the AOVs written to device
+memory; ``e2e`` goes through the public API (GpuBackend.render with host
+FrameBuffer planes), so the device->host copy of the four AOV planes is inside
+the timed region.  Between timed steps L2 is flushed (a 512 MiB memset).
+
+--impl reference times the reference's CPU path on the host cores: the CPU
+restatement of CpuPathTracer (oracle/port; the reference's own sources are not
+present on the GPU machine) with every host thread, on a bounded sample of rows of
+the same frame.
+
+Multi-GPU (torchrun): paths are independent, so every rank renders the full
+frame with its own sample range (sampleStart = rank * spp): replicas with no
+data-path collective, weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mpaths/s 1080p 1M-tri (plain vs wavefront) at equal RMSE; adjoint grads/s"
+UNIT = "Mpaths/s"
+
+# Bytes moved per unit of counted work in this backend's layout (the
+# algorithmic-bytes model of the roofline).
+BYTES = dict(node=64, tri=48, hit=16 + 3 * 16 + 4 + 4 + 276, env_eval=4 * 16, env_sample=16 + 8, record=2 * 48)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", choices=["field", "sphere"], default="field")
+    p.add_argument("--form", choices=["auto", "plain", "wavefront"], default="auto")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--width", type=int, default=0, help="override the frame width (profiling cases)")
+    p.add_argument("--height", type=int, default=0)
+    p.add_argument("--spp", type=int, default=0)
+    return p.parse_args()
+
+
+def workload(name: str, args=None):
+    from shiro_gb300 import scenes
+
+    if name == "field":
+        w = scenes.field_workload(1920, 1080, 64, 12)
+    else:
+        w = scenes.sphere_workload(256, 256, 16, 8)
+    if args is not None and (args.width or args.height or args.spp):
+        s = w.settings
+        s.width = args.width or s.width
+        s.height = args.height or s.height
+        s.samples_per_pixel = args.spp or s.samples_per_pixel
+        w.camera.aspect_ratio = s.width / s.height
+        w.name += f" (profiling case {s.width}x{s.height} {s.samples_per_pixel}spp)"
+    return w
+
+
+def workload_config(w, flush: str) -> dict:
+    s = w.settings
+    return {"workload": w.name, "triangles": int(w.scene.triangle_count), "width": s.width, "height": s.height,
+            "spp": s.samples_per_pixel, "max_depth": s.max_depth, "dome_light_samples": s.dome_light_samples,
+            "env": list(w.scene.dome_lights[0].env.shape[:2][::-1]), "distant_lights": len(w.scene.distant_lights),
+            "paths_per_step": w.paths, "l2": flush}
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def wait_first(self, timeout: float = 5.0):
+        """nvidia-smi's start-up takes driver locks; start timing only once it
+        is sampling."""
+        t0 = time.time()
+        while self.proc and not self.lines and time.time() - t0 < timeout:
+            time.sleep(0.05)
+        time.sleep(0.3)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.t:
+                self.t.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active") or v == "1":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic(kernel: str, workload_name: str):
+    """DRAM bytes per path of `kernel` from the committed ncu summary (a
+    smaller case of the same kernel, scaled per path)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload_name}.json")
+    if not os.path.exists(path):
+        return None
+    d = json.load(open(path))
+    return d.get("dram_bytes_per_path")
+
+
+def cpu_baseline(w, seconds: float, rank: int = 0) -> dict:
+    """The CPU path tracer (oracle restatement of CpuPathTracer) on every host
+    thread, over evenly spaced bands of rows of the same frame."""
+    import ctypes as C
+
+    import oracle
+    from shiro_gb300.abi import FrameBuffer, MarshalledScene, render_desc
+
+    lib = oracle.load_port()
+    lib.oracle_scene_create.argtypes = [C.c_void_p, C.c_void_p]
+    lib.oracle_scene_create.restype = C.c_int
+    lib.oracle_scene_render_rows.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
+    lib.oracle_scene_render_rows.restype = C.c_int64
+    lib.oracle_scene_destroy.argtypes = [C.c_void_p]
+    threads = os.cpu_count() or 1
+    lib.oracle_set_threads(threads)
+    ms = MarshalledScene(w.scene)
+    h = C.c_void_p()
+    t0 = time.perf_counter()
+    rc = lib.oracle_scene_create(ms.ref(), C.byref(h))
+    build_s = time.perf_counter() - t0
+    if rc != 0:
+        raise RuntimeError(f"oracle scene build failed: {rc}")
+    st = w.settings
+    req = render_desc(w.camera, st, 0, st.samples_per_pixel)
+    fb = FrameBuffer(st.width, st.height)
+    aovs = fb.aovs()
+    # calibrate on one band of 2 rows, then spread the budget over bands
+    paths = 0
+    t_render = 0.0
+    y = st.height // 2
+    t0 = time.perf_counter()
+    paths += lib.oracle_scene_render_rows(h, C.byref(req), y, y + 2, C.byref(aovs))
+    t_render += time.perf_counter() - t0
+    rate = paths / max(t_render, 1e-6)
+    rows_budget = max(2, int(seconds * rate / (st.width * st.samples_per_pixel)))
+    bands = 8
+    per = max(1, rows_budget // bands)
+    rows = 2
+    for b in range(bands):
+        y0 = int((b + 0.5) * st.height / bands) - per // 2
+        y0 = min(max(0, y0), st.height - per)
+        t0 = time.perf_counter()
+        n = lib.oracle_scene_render_rows(h, C.byref(req), y0, y0 + per, C.byref(aovs))
+        t_render += time.perf_counter() - t0
+        paths += n
+        rows += per
+    lib.oracle_scene_destroy(h)
+    value = paths / t_render / 1e6
+    cpu = ""
+    try:
+        cpu = [ln.split(":", 1)[1].strip() for ln in open("/proc/cpuinfo") if ln.lower().startswith(("model name", "cpu part"))][0]
+    except Exception:
+        pass
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{rows} rows x {st.width} px x {st.samples_per_pixel} spp ({paths} paths, "
+                      f"{rows / st.height:.1%} of the frame, 9 bands), {t_render:.1f} s render + {build_s:.1f} s BVH build",
+            "cpu": cpu, "seconds": t_render, "paths": int(paths)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    w = workload(args.workload, args)
+    vals = []
+    info = None
+    for _ in range(args.warmup + args.steps):
+        info = cpu_baseline(w, max(2.0, args.cpu_seconds / 2))
+        vals.append(info["value"])
+    timed = vals[args.warmup:]
+    value = statistics.mean(timed)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": info["seconds"] * 1000.0, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "impl": "reference", "config": workload_config(w, "n/a (CPU)"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["cores"], "kind": "port",
+                             "sample": info["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from shiro_gb300 import GpuBackend
+    from shiro_gb300.abi import FrameBuffer
+
+    w = workload(args.workload, args)
+    st = w.settings
+    spp = st.samples_per_pixel
+    gpu = GpuBackend(local)
+    stream = torch.cuda.current_stream()
+    gpu.lib.shiro_gpu_set_stream(gpu.handle, stream.cuda_stream)
+    t0 = time.perf_counter()
+    gpu.upload_scene(w.scene)
+    upload_s = time.perf_counter() - t0
+    form = "plain" if args.form in ("auto", "plain") else "wavefront"
+
+    npx = st.width * st.height
+    dev = {k: torch.empty(npx * c, dtype=torch.float32, device="cuda") for k, c in
+           (("beauty", 4), ("albedo", 3), ("normal", 3), ("depth", 1))}
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    import ctypes as C
+
+    from shiro_gb300.abi import Aovs, render_desc
+
+    aov = Aovs(*[C.cast(C.c_void_p(dev[k].data_ptr()), C.POINTER(C.c_float)) for k in ("beauty", "albedo", "normal", "depth")],
+               1, 0)
+    start = rank * spp
+
+    def step(k):
+        req = render_desc(w.camera, st, start, spp)
+        rc = gpu.lib.shiro_gpu_render(gpu.handle, C.byref(req), None, C.byref(aov))
+        if rc != 0:
+            raise RuntimeError(gpu.lib.shiro_gpu_last_error(gpu.handle).decode())
+        return gpu.last_stats()
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    path_ms, path_launches, launches = 0.0, 0, 0
+    with ClockSampler(local) as clocks:
+        clocks.wait_first()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(args.steps):
+            flush.zero_()
+            s = step(k)
+            path_ms += s["path_kernel_ms"]
+            path_launches += s["path_kernel_launches"]
+            launches += s["kernel_launches"]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    total_paths = w.paths * world * args.steps
+    value = total_paths / (ms / 1000.0) / 1e6
+    stats = gpu.last_stats()
+
+    # end to end through the public API with host FrameBuffer planes
+    e2e = None
+    if not args.no_e2e:
+        fb = FrameBuffer(st.width, st.height)
+        gpu.render(w.scene, w.camera, st, start, spp, out=fb)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()
+            gpu.render(w.scene, w.camera, st, start, spp, out=fb)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([el], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        req_bytes = C.sizeof(render_desc(w.camera, st, 0, 1))
+        e2e = {"value": total_paths / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": req_bytes,
+               "d2h_bytes_per_step": npx * 44, "note": "scene resident (uploaded once, "
+               f"{upload_s:.2f} s incl. BVH build); per step: request in, 4 AOV planes out"}
+
+    # roofline of the dominant kernel (the path megakernel)
+    wc = gpu.count_work(w.scene, w.camera, st, stride=64, sample_start=start)
+    per_path = (wc["node_visits"] * BYTES["node"] + wc["tri_tests"] * BYTES["tri"] + wc["hits"] * BYTES["hit"]
+                + wc["env_evals"] * BYTES["env_eval"] + wc["env_samples"] * BYTES["env_sample"]) / max(wc["paths"], 1)
+    per_path += BYTES["record"] / 2  # the megakernel writes its 48-byte record
+    paths_per_launch = w.paths / max(stats["path_kernel_launches"], 1)
+    avg_launch_ms = path_ms / max(path_launches, 1)
+    pk = peaks()
+    achieved = per_path * paths_per_launch / (avg_launch_ms / 1000.0) / 1e9
+    dram_per_path = ncu_traffic("plain_megakernel", args.workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "traffic": (dram_per_path * paths_per_launch) if dram_per_path else None,
+                "kernel": "k_plain_paths", "peak_source": pk["source"], "algorithmic_bytes_per_path": per_path,
+                "avg_launch_ms": avg_launch_ms, "paths_per_launch": paths_per_launch,
+                "work_per_path": {k: v / max(wc["paths"], 1) for k, v in wc.items() if k != "paths"}}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, args.cpu_seconds)
+    if rank == 0:
+        cfg = workload_config(w, "flushed (512 MiB memset between steps)")
+        cfg.update({"form": form, "parallelism": f"replicas x{world}", "scene_upload_s": upload_s,
+                    "bvh_nodes": int(stats["bvh_nodes"]), "bvh_depth": int(stats["bvh_depth"])})
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene, random-init HDRI)",
+                "config": cfg, "clocks": clocks.summary(), "gpu_launches": launches, "e2e": e2e,
+                "roofline": roofline, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    gpu.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

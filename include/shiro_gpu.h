@@ -326,7 +326,9 @@ int shiro_gpu_trace_rays(ShiroGpuContext* ctx, const float* origins, const float
 
 /* Statistics of the last render (for the roofline and tests). */
 typedef struct ShiroRenderStats {
-    double kernel_ms;           /* device time of the render kernels */
+    double kernel_ms;           /* device time of all kernels of the last call */
+    double path_kernel_ms;      /* device time of the path-tracing kernel(s) alone */
+    uint64_t path_kernel_launches;
     uint64_t paths;             /* paths traced */
     uint64_t kernel_launches;   /* kernels launched by the last call */
     uint64_t bvh_nodes;         /* BVH nodes of the uploaded scene */
@@ -336,6 +338,24 @@ typedef struct ShiroRenderStats {
     uint64_t device_bytes;      /* device memory held by the context */
 } ShiroRenderStats;
 int shiro_gpu_last_stats(const ShiroGpuContext* ctx, ShiroRenderStats* out);
+
+/* Work counts of the estimator, for the algorithmic-bytes roofline: traces
+ * every `stride`-th path of `request` with counting kernels (same paths, same
+ * decisions as the render) and returns the totals over the traced paths. */
+typedef struct ShiroWorkCounts {
+    uint64_t paths;
+    uint64_t closest_rays;
+    uint64_t occlusion_rays;
+    uint64_t node_visits;       /* BVH nodes fetched (both kinds of ray) */
+    uint64_t tri_tests;         /* triangles fetched and tested */
+    uint64_t hits;              /* surface hits shaded */
+    uint64_t env_evals;         /* bilinear environment lookups (4 texels) */
+    uint64_t env_samples;       /* importance-table lookups */
+    uint64_t bsdf_evals;
+    uint64_t bsdf_pdfs;
+} ShiroWorkCounts;
+int shiro_gpu_count_work(ShiroGpuContext* ctx, const ShiroRenderDesc* request, uint32_t stride,
+                         ShiroWorkCounts* out);
 
 #ifdef __cplusplus
 }

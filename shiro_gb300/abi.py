@@ -142,10 +142,16 @@ class WavefrontConfig(C.Structure):
 
 class RenderStats(C.Structure):
     _fields_ = [
-        ("kernel_ms", C.c_double), ("paths", C.c_uint64), ("kernel_launches", C.c_uint64),
+        ("kernel_ms", C.c_double), ("path_kernel_ms", C.c_double), ("path_kernel_launches", C.c_uint64),
+        ("paths", C.c_uint64), ("kernel_launches", C.c_uint64),
         ("bvh_nodes", C.c_uint64), ("triangles", C.c_uint64), ("bvh_depth", C.c_uint32),
         ("bvh_max_leaf", C.c_uint32), ("device_bytes", C.c_uint64),
     ]
+
+
+class WorkCounts(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("paths", "closest_rays", "occlusion_rays", "node_visits", "tri_tests", "hits",
+                                          "env_evals", "env_samples", "bsdf_evals", "bsdf_pdfs")]
 
 
 # ---------------------------------------------------------------------------

@@ -70,6 +70,7 @@ def load_library(path: str = LIB_PATH):
         "shiro_gpu_primary_hits": ([_P, _P, _P, _P, _U], C.c_int),
         "shiro_gpu_trace_rays": ([_P, _P, _P, _P, _U, _P, _P, _P], C.c_int),
         "shiro_gpu_last_stats": ([_P, _P], C.c_int),
+        "shiro_gpu_count_work": ([_P, _P, _U, _P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -258,6 +259,21 @@ class GpuBackend:
         if rc != 0:
             raise self._err(rc)
         return prim, t, occ
+
+    def count_work(self, scene: Scene, camera: Camera, settings: RenderSettings, stride: int = 64,
+                   sample_start: int = 0, sample_count: Optional[int] = None, flags: int = 0) -> dict:
+        """Work counts of every `stride`-th path (node visits, triangle
+        tests, environment lookups ...), for the algorithmic-bytes roofline."""
+        from .abi import WorkCounts
+
+        self.upload_scene(scene)
+        req = render_desc(camera, settings, sample_start,
+                          settings.samples_per_pixel if sample_count is None else sample_count, flags)
+        wc = WorkCounts()
+        rc = self.lib.shiro_gpu_count_work(self._ctx, C.byref(req), int(stride), C.byref(wc))
+        if rc != 0:
+            raise self._err(rc)
+        return {k: getattr(wc, k) for k, _ in WorkCounts._fields_}
 
     def last_stats(self) -> dict:
         s = RenderStats()

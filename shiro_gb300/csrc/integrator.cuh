@@ -69,16 +69,18 @@ __device__ __forceinline__ V3 clamp12(const DevRequest& q, const V3& v) {
 }
 
 // DirectLighting without the emissive-triangle term (:1511-1576).
+template <typename Ctr>
 __device__ __forceinline__ V3 direct_lighting(const DevScene& s, const DevRequest& q, const Surface& hit, const V3& n,
                                               const V3& cn, const Mat& m, const LobeWeights& w, const V3& view,
-                                              const Sampler& smp, uint32_t depth) {
+                                              const Sampler& smp, uint32_t depth, Ctr& ctr) {
     V3 out{0.0f, 0.0f, 0.0f};
     const V3 origin = hit.position + n * kRayEpsilon;
     for (uint32_t i = 0; i < s.distantCount; ++i) {
         const DevDistant l = s.distant[i];
         const V3 ld = normalize(l.direction * -1.0f);
         const float nl = sclamp(dot(n, ld), 0.0f, 1.0f);
-        if (nl <= 0.0f || trace_occluded(s, origin, ld, FLT_MAX)) continue;
+        if (nl <= 0.0f || trace_occluded(s, origin, ld, FLT_MAX, ctr)) continue;
+        ctr.bsdf_eval();
         out = out + clamp24(q, bsdf_eval(m, n, cn, view, ld) * l.radiance * nl);
     }
     const bool useCdf = (q.flags & SHIRO_RENDER_ENV_CDF) != 0u;
@@ -88,9 +90,15 @@ __device__ __forceinline__ V3 direct_lighting(const DevScene& s, const DevReques
             const uint32_t dim = kDirectDimBase + depth * kDirectDepthStride + li * kDirectLightStride + k * kDirectSampleStride;
             V3 ld, lr;
             float lp = 0.0f;
+            if (s.domes[li].env >= 0) {
+                ctr.env_sample();
+                ctr.env_eval();
+            }
             if (!sample_dome(s, s.domes[li], smp.next2d(dim), useCdf, &ld, &lr, &lp) || lp <= 0.0f) continue;
             const float nl = sclamp(dot(n, ld), 0.0f, 1.0f);
-            if (nl <= 0.0f || trace_occluded(s, origin, ld, FLT_MAX)) continue;
+            if (nl <= 0.0f || trace_occluded(s, origin, ld, FLT_MAX, ctr)) continue;
+            ctr.bsdf_pdf();
+            ctr.bsdf_eval();
             const float bp = bsdf_pdf(m, w, n, cn, view, ld);
             const float mis = power_heuristic(lp, bp);
             acc = acc + clamp24(q, bsdf_eval(m, n, cn, view, ld) * lr * (nl * mis / lp));
@@ -123,8 +131,9 @@ __device__ __forceinline__ void shading_frame(const Mat& m, const Surface& hit, 
     *cn = resolve_normal(m, nn, true);
 }
 
+template <typename Ctr>
 __device__ __forceinline__ PathResult trace_path(const DevScene& s, const DevRequest& q, uint32_t x, uint32_t y,
-                                                 uint32_t sampleIndex) {
+                                                 uint32_t sampleIndex, Ctr& ctr) {
     PathResult res;
     res.radiance = V3{0.0f, 0.0f, 0.0f};
     res.albedo = V3{0.0f, 0.0f, 0.0f};
@@ -140,17 +149,20 @@ __device__ __forceinline__ PathResult trace_path(const DevScene& s, const DevReq
     for (uint32_t depth = 0; depth < q.maxDepth; ++depth) {
         const uint32_t base = depth * kPathDimStride;
         HitRec h;
-        if (!trace_closest(s, ro, rd, &h)) {
+        if (!trace_closest(s, ro, rd, &h, ctr)) {
             if (depth > 0 || q.backgroundVisible) {
                 const V3 env = environment_radiance(s, rd);
+                ctr.env_eval(s.domeCount);
                 if (s.domeCount == 0 || depth == 0 || prevDelta) {
                     res.radiance = res.radiance + T * env;
                 } else {
+                    ctr.env_sample(s.domeCount);
                     res.radiance = res.radiance + T * env * env_miss_mis(s, prevPdf, rd);
                 }
             }
             break;
         }
+        ctr.hit();
         const Surface hit = make_surface(s, ro, rd, h);
         const Mat& m = s.materials[hit.material];
         V3 n, cn;
@@ -162,7 +174,7 @@ __device__ __forceinline__ PathResult trace_path(const DevScene& s, const DevReq
             res.depth = h.t;
         }
         const LobeWeights w = lobe_weights(m);
-        res.radiance = res.radiance + T * direct_lighting(s, q, hit, n, cn, m, w, view, smp, depth);
+        res.radiance = res.radiance + T * direct_lighting(s, q, hit, n, cn, m, w, view, smp, depth, ctr);
 
         const float rw = w.diffuse + w.spec + w.coat;
         const float tw = rw + 0.0f;
@@ -179,6 +191,7 @@ __device__ __forceinline__ PathResult trace_path(const DevScene& s, const DevReq
             next = cosine_hemisphere(n, ds);
             const float cpdf = sclamp(dot(n, next), 0.0f, 1.0f) * kInvPi;
             pdf = smax((rw / tw) * (1.0f * cpdf + 0.0f * 0.0f), 1.0e-6f);
+            ctr.bsdf_eval();
             f = bsdf_eval(m, n, cn, view, next);
         } else {
             const bool coat = !(rs < w.diffuse + w.spec);
@@ -191,6 +204,8 @@ __device__ __forceinline__ PathResult trace_path(const DevScene& s, const DevReq
             next = normalize(reflect(rd, hv));
             const float rc = sclamp(dot(sn, next), 0.0f, 1.0f);
             if (rc <= 0.0f) break;
+            ctr.bsdf_pdf();
+            ctr.bsdf_eval();
             pdf = smax((rw / tw) * bsdf_pdf(m, w, n, cn, view, next), 1.0e-6f);
             f = bsdf_eval(m, n, cn, view, next);
             delta = sr <= kDeltaRoughness;

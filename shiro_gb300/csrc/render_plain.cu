@@ -23,7 +23,8 @@ __global__ void __launch_bounds__(128) k_plain_paths(const DevScene s, const Dev
     const uint32_t smp = static_cast<uint32_t>(path - pixel * q.sampleCount);
     const uint32_t y = static_cast<uint32_t>(pixel / q.width);
     const uint32_t x = static_cast<uint32_t>(pixel - static_cast<uint64_t>(y) * q.width);
-    const PathResult r = trace_path(s, q, x, y, q.sampleStart + smp);
+    NullCounter ctr;
+    const PathResult r = trace_path(s, q, x, y, q.sampleStart + smp, ctr);
     float4* o = records + 3 * static_cast<size_t>(i);
     o[0] = make_float4(r.radiance.x, r.radiance.y, r.radiance.z, r.depth);
     o[1] = make_float4(r.albedo.x, r.albedo.y, r.albedo.z, 0.0f);
@@ -74,7 +75,8 @@ __global__ void k_primary_hits(const DevScene s, const DevRequest q, uint32_t* _
     V3 o, d;
     camera_ray(q, x, y, smp.next2d(0u), &o, &d);
     HitRec h;
-    const bool hit = trace_closest(s, o, d, &h);
+    NullCounter ctr;
+    const bool hit = trace_closest(s, o, d, &h, ctr);
     prim[i] = hit ? h.gid : 0xffffffffu;
     tout[i] = hit ? h.t : FLT_MAX;
 }
@@ -87,10 +89,37 @@ __global__ void k_trace_rays(const DevScene s, const float* __restrict__ o, cons
     const V3 ro{o[3 * i], o[3 * i + 1], o[3 * i + 2]};
     const V3 rd{d[3 * i], d[3 * i + 1], d[3 * i + 2]};
     HitRec h;
-    const bool hit = trace_closest(s, ro, rd, &h);
+    NullCounter ctr;
+    const bool hit = trace_closest(s, ro, rd, &h, ctr);
     prim[i] = hit ? h.gid : 0xffffffffu;
     tout[i] = hit ? h.t : FLT_MAX;
-    occ[i] = trace_occluded(s, ro, rd, tmax[i]) ? 1u : 0u;
+    occ[i] = trace_occluded(s, ro, rd, tmax[i], ctr) ? 1u : 0u;
+}
+
+// Work-counting variant: every `stride`-th path of the request, same
+// decisions as k_plain_paths; totals accumulated with one atomic per field
+// per warp.
+__global__ void __launch_bounds__(128) k_count_paths(const DevScene s, const DevRequest q, uint64_t totalPaths,
+                                                     uint32_t stride, unsigned long long* __restrict__ totals) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const uint64_t path = i * stride;
+    LocalCounter c;
+    uint32_t traced = 0;
+    if (path < totalPaths) {
+        const uint64_t pixel = path / q.sampleCount;
+        const uint32_t smp = static_cast<uint32_t>(path - pixel * q.sampleCount);
+        const uint32_t y = static_cast<uint32_t>(pixel / q.width);
+        const uint32_t x = static_cast<uint32_t>(pixel - static_cast<uint64_t>(y) * q.width);
+        trace_path(s, q, x, y, q.sampleStart + smp, c);
+        traced = 1;
+    }
+    const uint32_t v[10] = {traced, c.closestRays, c.occlusionRays, c.nodes, c.tris, c.hits, c.envEvals, c.envSamples,
+                            c.bsdfEvals, c.bsdfPdfs};
+    for (int k = 0; k < 10; ++k) {
+        unsigned long long x = v[k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0 && x) atomicAdd(&totals[k], x);
+    }
 }
 
 inline unsigned grid(uint64_t n, unsigned b) { return static_cast<unsigned>((n + b - 1) / b); }
@@ -113,6 +142,14 @@ void launch_primary_hits(const DevScene& s, const DevRequest& q, uint32_t* prim,
     const uint64_t n = static_cast<uint64_t>(q.width) * q.height;
     if (n == 0) return;
     k_primary_hits<<<grid(n, 128), 128, 0, stream>>>(s, q, prim, t);
+}
+
+void launch_count_paths(const DevScene& s, const DevRequest& q, uint32_t stride, unsigned long long* totals,
+                        cudaStream_t stream) {
+    const uint64_t total = static_cast<uint64_t>(q.width) * q.height * q.sampleCount;
+    const uint64_t n = (total + stride - 1) / stride;
+    if (n == 0) return;
+    k_count_paths<<<grid(n, 128), 128, 0, stream>>>(s, q, total, stride, totals);
 }
 
 void launch_trace_rays(const DevScene& s, const float* o, const float* d, const float* tmax, uint32_t n, uint32_t* prim,

@@ -692,6 +692,8 @@ int shiro_gpu_render(ShiroGpuContext* handle, const ShiroRenderDesc* req, const 
     ctx->stats.paths = 0;
     ctx->stats.kernel_launches = 0;
     ctx->stats.kernel_ms = 0.0;
+    ctx->stats.path_kernel_ms = 0.0;
+    ctx->stats.path_kernel_launches = 0;
     // AOV destination: caller's device planes or the context's staging planes
     AovPtrs aov;
     if (out->on_device) {
@@ -730,39 +732,61 @@ int shiro_gpu_render(ShiroGpuContext* handle, const ShiroRenderDesc* req, const 
     const uint64_t recBytes = std::min<uint64_t>(pixelsPerChunk, pixels) * q.sampleCount * kPathRecordBytes;
     if (!ensure_block(ctx, &ctx->pathRecords, recBytes, "path records")) return SHIRO_ERR_OUT_OF_MEMORY;
     float4* rec = static_cast<float4*>(ctx->pathRecords.ptr);
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    // events around the whole call and around every path-kernel launch
+    std::vector<cudaEvent_t> ev;
+    auto new_event = [&]() {
+        cudaEvent_t x;
+        cudaEventCreate(&x);
+        ev.push_back(x);
+        return x;
+    };
+    auto drop_events = [&]() {
+        for (cudaEvent_t x : ev) cudaEventDestroy(x);
+    };
+    cudaEvent_t e0 = new_event();
     cudaEventRecord(e0, ctx->stream);
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pathEv;
     for (uint64_t p0 = 0; p0 < pixels; p0 += pixelsPerChunk) {
         if (cancel && *cancel) {
             cudaStreamSynchronize(ctx->stream);
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
+            drop_events();
             clear_host();
             return fail(ctx, SHIRO_ERR_CANCELLED, "cancelled");
         }
         const uint32_t np = static_cast<uint32_t>(std::min(pixelsPerChunk, pixels - p0));
         const uint64_t paths = static_cast<uint64_t>(np) * q.sampleCount;
+        cudaEvent_t a = new_event(), b = new_event();
+        cudaEventRecord(a, ctx->stream);
         launch_plain_paths(ctx->scene, q, p0 * q.sampleCount, static_cast<uint32_t>(paths), rec, ctx->stream);
+        cudaEventRecord(b, ctx->stream);
+        pathEv.emplace_back(a, b);
         launch_resolve_pixels(q, p0, np, rec, aov, ctx->stream);
         ctx->stats.kernel_launches += 2;
         ctx->stats.paths += paths;
         const cudaError_t le = cudaGetLastError();
         if (le != cudaSuccess) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
+            drop_events();
             return cuda_fail(ctx, le, "render launch");
         }
     }
+    cudaEvent_t e1 = new_event();
     cudaEventRecord(e1, ctx->stream);
     cudaError_t e = cudaEventSynchronize(e1);
     float ms = 0.0f;
-    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    double pathMs = 0.0;
+    if (e == cudaSuccess) {
+        cudaEventElapsedTime(&ms, e0, e1);
+        for (auto& pe : pathEv) {
+            float x = 0.0f;
+            cudaEventElapsedTime(&x, pe.first, pe.second);
+            pathMs += x;
+        }
+    }
+    drop_events();
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render");
     ctx->stats.kernel_ms = ms;
+    ctx->stats.path_kernel_ms = pathMs;
+    ctx->stats.path_kernel_launches = pathEv.size();
     if ((rc = check_device_error(ctx)) != SHIRO_OK) return rc;
     if (!out->on_device) {
         e = cudaMemcpyAsync(out->beauty, aov.beauty, pixels * 16, cudaMemcpyDeviceToHost, ctx->stream);
@@ -868,6 +892,38 @@ int shiro_gpu_trace_rays(ShiroGpuContext* handle, const float* origins, const fl
     if (e == cudaSuccess) e = cudaMemcpyAsync(occ, dOcc, 4ull * n, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "trace rays readback");
+    return SHIRO_OK;
+}
+
+int shiro_gpu_count_work(ShiroGpuContext* handle, const ShiroRenderDesc* req, uint32_t stride, ShiroWorkCounts* out) {
+    if (!handle || !req || !out || stride == 0) return SHIRO_ERR_INVALID_ARGUMENT;
+    ContextImpl* ctx = &handle->impl;
+    cudaSetDevice(ctx->device);
+    int rc = validate_request(ctx, *req);
+    if (rc != SHIRO_OK) return rc;
+    const DevRequest q = make_request(*req);
+    if (!ensure_block(ctx, &ctx->probeScratch, 16 * sizeof(unsigned long long), "work counters")) return SHIRO_ERR_OUT_OF_MEMORY;
+    auto* totals = static_cast<unsigned long long*>(ctx->probeScratch.ptr);
+    cudaError_t e = cudaMemsetAsync(totals, 0, 10 * sizeof(unsigned long long), ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "work counters");
+    if (req->sample_count > 0) launch_count_paths(ctx->scene, q, stride, totals, ctx->stream);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "count launch");
+    if ((rc = check_device_error(ctx)) != SHIRO_OK) return rc;
+    unsigned long long h[10];
+    e = cudaMemcpyAsync(h, totals, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "work counters readback");
+    out->paths = h[0];
+    out->closest_rays = h[1];
+    out->occlusion_rays = h[2];
+    out->node_visits = h[3];
+    out->tri_tests = h[4];
+    out->hits = h[5];
+    out->env_evals = h[6];
+    out->env_samples = h[7];
+    out->bsdf_evals = h[8];
+    out->bsdf_pdfs = h[9];
     return SHIRO_OK;
 }
 

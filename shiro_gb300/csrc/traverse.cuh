@@ -24,6 +24,33 @@ namespace shiro_gpu {
 
 constexpr uint32_t kMaxVisits = 1u << 22;
 
+// Work counters of the roofline probe (shiro_gpu_count_work).  NullCounter
+// compiles every increment away in the render kernels.
+struct NullCounter {
+    __device__ __forceinline__ void node() {}
+    __device__ __forceinline__ void tri() {}
+    __device__ __forceinline__ void closest() {}
+    __device__ __forceinline__ void occlusion() {}
+    __device__ __forceinline__ void hit() {}
+    __device__ __forceinline__ void env_eval(uint32_t n = 1) {}
+    __device__ __forceinline__ void env_sample(uint32_t n = 1) {}
+    __device__ __forceinline__ void bsdf_eval() {}
+    __device__ __forceinline__ void bsdf_pdf() {}
+};
+struct LocalCounter {
+    uint32_t nodes = 0, tris = 0, closestRays = 0, occlusionRays = 0, hits = 0, envEvals = 0, envSamples = 0,
+             bsdfEvals = 0, bsdfPdfs = 0;
+    __device__ __forceinline__ void node() { ++nodes; }
+    __device__ __forceinline__ void tri() { ++tris; }
+    __device__ __forceinline__ void closest() { ++closestRays; }
+    __device__ __forceinline__ void occlusion() { ++occlusionRays; }
+    __device__ __forceinline__ void hit() { ++hits; }
+    __device__ __forceinline__ void env_eval(uint32_t n = 1) { envEvals += n; }
+    __device__ __forceinline__ void env_sample(uint32_t n = 1) { envSamples += n; }
+    __device__ __forceinline__ void bsdf_eval() { ++bsdfEvals; }
+    __device__ __forceinline__ void bsdf_pdf() { ++bsdfPdfs; }
+};
+
 struct HitRec {
     float t, u, v;
     uint32_t slot;  // leaf-order triangle index, 0xffffffff on a miss
@@ -85,7 +112,9 @@ __device__ __forceinline__ bool tri_test(const V3& o, const V3& d, float tMin, f
     return true;
 }
 
-__device__ __noinline__ bool trace_closest(const DevScene& s, const V3 o, const V3 d, HitRec* out) {
+template <typename Ctr>
+__device__ __noinline__ bool trace_closest(const DevScene& s, const V3 o, const V3 d, HitRec* out, Ctr& ctr) {
+    ctr.closest();
     const RayInv r = ray_inv(o, d);
     float bestT = FLT_MAX;
     uint32_t bestGid = 0xffffffffu, bestSlot = 0xffffffffu;
@@ -102,6 +131,7 @@ __device__ __noinline__ bool trace_closest(const DevScene& s, const V3 o, const 
             break;
         }
         if (node >= 0) {
+            ctr.node();
             const float4* np = s.nodes + 4 * static_cast<size_t>(node);
             const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
             float t0, t1;
@@ -133,6 +163,7 @@ __device__ __noinline__ bool trace_closest(const DevScene& s, const V3 o, const 
             const uint32_t enc = ~static_cast<uint32_t>(node);
             const uint32_t first = enc >> 3, cnt = (enc & 7u) + 1u;
             for (uint32_t k = first; k < first + cnt; ++k) {
+                ctr.tri();
                 const float4* tp = s.tris + 3 * static_cast<size_t>(k);
                 const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
                 float t, u, v;
@@ -168,7 +199,9 @@ __device__ __noinline__ bool trace_closest(const DevScene& s, const V3 o, const 
 }
 
 // Any hit with t in [1e-4, maxDist] (Occluded, CpuPathTracer.cpp:468-475).
-__device__ __noinline__ bool trace_occluded(const DevScene& s, const V3 o, const V3 d, float maxDist) {
+template <typename Ctr>
+__device__ __noinline__ bool trace_occluded(const DevScene& s, const V3 o, const V3 d, float maxDist, Ctr& ctr) {
+    ctr.occlusion();
     const RayInv r = ray_inv(o, d);
     int stackNode[kStack];
     int sp = 0;
@@ -180,6 +213,7 @@ __device__ __noinline__ bool trace_occluded(const DevScene& s, const V3 o, const
             return false;
         }
         if (node >= 0) {
+            ctr.node();
             const float4* np = s.nodes + 4 * static_cast<size_t>(node);
             const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
             float t0, t1;
@@ -208,6 +242,7 @@ __device__ __noinline__ bool trace_occluded(const DevScene& s, const V3 o, const
             const uint32_t enc = ~static_cast<uint32_t>(node);
             const uint32_t first = enc >> 3, cnt = (enc & 7u) + 1u;
             for (uint32_t k = first; k < first + cnt; ++k) {
+                ctr.tri();
                 const float4* tp = s.tris + 3 * static_cast<size_t>(k);
                 const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
                 float t, u, v;
