@@ -281,7 +281,7 @@ def main():
     t0 = time.perf_counter()
     gpu.upload_scene(w.scene)
     upload_s = time.perf_counter() - t0
-    form = "plain" if args.form in ("auto", "plain") else "wavefront"
+    forms = ["plain", "wavefront"] if args.form == "auto" else [args.form]
 
     npx = st.width * st.height
     dev = {k: torch.empty(npx * c, dtype=torch.float32, device="cuda") for k, c in
@@ -295,56 +295,81 @@ def main():
                1, 0)
     start = rank * spp
 
-    def step(k):
+    def render_dev(form):
         req = render_desc(w.camera, st, start, spp)
-        rc = gpu.lib.shiro_gpu_render(gpu.handle, C.byref(req), None, C.byref(aov))
+        if form == "plain":
+            rc = gpu.lib.shiro_gpu_render(gpu.handle, C.byref(req), None, C.byref(aov))
+        else:
+            rc = gpu.lib.shiro_gpu_render_batch(gpu.handle, C.byref(req), 1, None, C.byref(aov))
         if rc != 0:
             raise RuntimeError(gpu.lib.shiro_gpu_last_error(gpu.handle).decode())
         return gpu.last_stats()
 
-    for k in range(args.warmup):
-        step(k)
-    torch.cuda.synchronize()
-    path_ms, path_launches, launches = 0.0, 0, 0
-    with ClockSampler(local) as clocks:
-        clocks.wait_first()
+    tuned = None
+    if "wavefront" in forms:
+        tuned = gpu.autotune(w.scene, w.camera, st)
+
+    def timed(form):
+        for _ in range(args.warmup):
+            render_dev(form)
+        torch.cuda.synchronize()
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        launches, path_ms, path_launches = 0, 0.0, 0
         e0.record(stream)
-        for k in range(args.steps):
+        for _ in range(args.steps):
             flush.zero_()
-            s = step(k)
+            s = render_dev(form)
+            launches += s["kernel_launches"]
             path_ms += s["path_kernel_ms"]
             path_launches += s["path_kernel_launches"]
-            launches += s["kernel_launches"]
         e1.record(stream)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return {"ms": ms, "launches": launches, "path_ms": path_ms, "path_launches": path_launches}
+
+    results = {}
+    with ClockSampler(local) as clocks:
+        clocks.wait_first()
+        for f in forms:
+            results[f] = timed(f)
     total_paths = w.paths * world * args.steps
-    value = total_paths / (ms / 1000.0) / 1e6
+    for f in forms:
+        results[f]["value"] = total_paths / (results[f]["ms"] / 1000.0) / 1e6
+    head = max(forms, key=lambda f: results[f]["value"])
+    value = results[head]["value"]
+    ms = results[head]["ms"]
+    launches = results[head]["launches"]
     stats = gpu.last_stats()
 
     # end to end through the public API with host FrameBuffer planes
     e2e = None
     if not args.no_e2e:
         fb = FrameBuffer(st.width, st.height)
-        gpu.render(w.scene, w.camera, st, start, spp, out=fb)
+
+        def api_step():
+            if head == "plain":
+                gpu.render(w.scene, w.camera, st, start, spp, out=fb)
+            else:
+                gpu.render_batch(w.scene, [(w.camera, st, start, spp)])
+
+        api_step()
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for k in range(args.steps):
             flush.zero_()
-            gpu.render(w.scene, w.camera, st, start, spp, out=fb)
+            api_step()
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
         if dist:
@@ -353,32 +378,57 @@ def main():
             el = float(t.item())
         req_bytes = C.sizeof(render_desc(w.camera, st, 0, 1))
         e2e = {"value": total_paths / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": req_bytes,
-               "d2h_bytes_per_step": npx * 44, "note": "scene resident (uploaded once, "
+               "d2h_bytes_per_step": npx * 44, "form": head, "note": "scene resident (uploaded once, "
                f"{upload_s:.2f} s incl. BVH build); per step: request in, 4 AOV planes out"}
 
-    # roofline of the dominant kernel (the path megakernel)
+    # roofline of the headline form's dominant kernel
     wc = gpu.count_work(w.scene, w.camera, st, stride=64, sample_start=start)
-    per_path = (wc["node_visits"] * BYTES["node"] + wc["tri_tests"] * BYTES["tri"] + wc["hits"] * BYTES["hit"]
-                + wc["env_evals"] * BYTES["env_eval"] + wc["env_samples"] * BYTES["env_sample"]) / max(wc["paths"], 1)
-    per_path += BYTES["record"] / 2  # the megakernel writes its 48-byte record
-    paths_per_launch = w.paths / max(stats["path_kernel_launches"], 1)
-    avg_launch_ms = path_ms / max(path_launches, 1)
+    npth = max(wc["paths"], 1)
+    cn = wc["node_visits"] - wc["occlusion_node_visits"]
+    ct = wc["tri_tests"] - wc["occlusion_tri_tests"]
     pk = peaks()
+    if head == "plain":
+        per_path = (wc["node_visits"] * BYTES["node"] + wc["tri_tests"] * BYTES["tri"] + wc["hits"] * BYTES["hit"]
+                    + wc["env_evals"] * BYTES["env_eval"] + wc["env_samples"] * BYTES["env_sample"]) / npth
+        per_path += BYTES["record"] / 2  # the megakernel writes its 48-byte record
+        kernel, kms, kl = "k_plain_paths", results["plain"]["path_ms"], results["plain"]["path_launches"]
+        stage_share = None
+    else:
+        gpu.set_wavefront_config(use_graph=0)
+        diag = render_dev("wavefront")
+        gpu.set_wavefront_config(use_graph=1)
+        names = ["wf_generate", "wf_extend", "wf_shade", "wf_shadow", "wf_resolve", "wf_bookkeeping"]
+        dom = max(range(6), key=lambda k: diag["stage_ms"][k])
+        kernel, kms, kl = names[dom], diag["stage_ms"][dom], diag["stage_launches"][dom]
+        stage_share = {names[k]: diag["stage_ms"][k] / max(sum(diag["stage_ms"]), 1e-9) for k in range(6)}
+        rays = wc["closest_rays"] / npth
+        if dom == 1:     # closest hit: nodes, triangles, ray in (32 B), hit out (20 B), queue (4 B)
+            per_path = (cn * BYTES["node"] + ct * BYTES["tri"]) / npth + rays * (32 + 20 + 4)
+        elif dom == 3:   # occlusion: nodes, triangles, per path the shadow record
+            per_path = (wc["occlusion_node_visits"] * BYTES["node"] + wc["occlusion_tri_tests"] * BYTES["tri"]) / npth
+            per_path += wc["occlusion_rays"] / npth * 32 + wc["hits"] / npth * 64
+        else:            # shading
+            per_path = (wc["hits"] * BYTES["hit"] + wc["env_evals"] * BYTES["env_eval"]
+                        + wc["env_samples"] * BYTES["env_sample"]) / npth + rays * 160
+    paths_per_launch = w.paths / max(kl, 1)
+    avg_launch_ms = kms / max(kl, 1)
     achieved = per_path * paths_per_launch / (avg_launch_ms / 1000.0) / 1e9
-    dram_per_path = ncu_traffic("plain_megakernel", args.workload)
+    dram_per_path = ncu_traffic(kernel, args.workload)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"], "traffic": (dram_per_path * paths_per_launch) if dram_per_path else None,
-                "kernel": "k_plain_paths", "peak_source": pk["source"], "algorithmic_bytes_per_path": per_path,
-                "avg_launch_ms": avg_launch_ms, "paths_per_launch": paths_per_launch,
-                "work_per_path": {k: v / max(wc["paths"], 1) for k, v in wc.items() if k != "paths"}}
+                "kernel": kernel, "peak_source": pk["source"], "algorithmic_bytes_per_path": per_path,
+                "avg_launch_ms": avg_launch_ms, "paths_per_launch": paths_per_launch, "stage_share": stage_share,
+                "work_per_path": {k: v / npth for k, v in wc.items() if k != "paths"}}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(w, args.cpu_seconds)
     if rank == 0:
         cfg = workload_config(w, "flushed (512 MiB memset between steps)")
-        cfg.update({"form": form, "parallelism": f"replicas x{world}", "scene_upload_s": upload_s,
-                    "bvh_nodes": int(stats["bvh_nodes"]), "bvh_depth": int(stats["bvh_depth"])})
+        cfg.update({"form": head, "parallelism": f"replicas x{world}", "scene_upload_s": upload_s,
+                    "bvh_nodes": int(stats["bvh_nodes"]), "bvh_depth": int(stats["bvh_depth"]),
+                    "forms": {f: {"Mpaths_s": results[f]["value"], "ms_per_step": results[f]["ms"] / args.steps}
+                              for f in forms}, "wavefront_config": tuned})
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene, random-init HDRI)",

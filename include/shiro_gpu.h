@@ -336,6 +336,12 @@ typedef struct ShiroRenderStats {
     uint32_t bvh_depth;
     uint32_t bvh_max_leaf;
     uint64_t device_bytes;      /* device memory held by the context */
+    /* wavefront stages (filled by an event-timed run, use_graph = 0):
+     * 0 generate, 1 extend (closest hit), 2 shade, 3 shadow (occlusion),
+     * 4 resolve, 5 queue bookkeeping */
+    double stage_ms[6];
+    uint64_t stage_launches[6];
+    uint64_t waves;             /* waves of the last wavefront call */
 } ShiroRenderStats;
 int shiro_gpu_last_stats(const ShiroGpuContext* ctx, ShiroRenderStats* out);
 
@@ -353,6 +359,8 @@ typedef struct ShiroWorkCounts {
     uint64_t env_samples;       /* importance-table lookups */
     uint64_t bsdf_evals;
     uint64_t bsdf_pdfs;
+    uint64_t occlusion_node_visits;  /* part of node_visits spent on occlusion rays */
+    uint64_t occlusion_tri_tests;    /* part of tri_tests spent on occlusion rays */
 } ShiroWorkCounts;
 int shiro_gpu_count_work(ShiroGpuContext* ctx, const ShiroRenderDesc* request, uint32_t stride,
                          ShiroWorkCounts* out);

@@ -146,12 +146,14 @@ class RenderStats(C.Structure):
         ("paths", C.c_uint64), ("kernel_launches", C.c_uint64),
         ("bvh_nodes", C.c_uint64), ("triangles", C.c_uint64), ("bvh_depth", C.c_uint32),
         ("bvh_max_leaf", C.c_uint32), ("device_bytes", C.c_uint64),
+        ("stage_ms", C.c_double * 6), ("stage_launches", C.c_uint64 * 6), ("waves", C.c_uint64),
     ]
 
 
 class WorkCounts(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("paths", "closest_rays", "occlusion_rays", "node_visits", "tri_tests", "hits",
-                                          "env_evals", "env_samples", "bsdf_evals", "bsdf_pdfs")]
+                                          "env_evals", "env_samples", "bsdf_evals", "bsdf_pdfs",
+                                          "occlusion_node_visits", "occlusion_tri_tests")]
 
 
 # ---------------------------------------------------------------------------

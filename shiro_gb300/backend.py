@@ -278,7 +278,11 @@ class GpuBackend:
     def last_stats(self) -> dict:
         s = RenderStats()
         self.lib.shiro_gpu_last_stats(self._ctx, C.byref(s))
-        return {k: getattr(s, k) for k, _ in RenderStats._fields_}
+        out = {}
+        for k, _ in RenderStats._fields_:
+            v = getattr(s, k)
+            out[k] = list(v) if hasattr(v, "__len__") else v
+        return out
 
     @property
     def handle(self):

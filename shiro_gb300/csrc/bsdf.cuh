@@ -187,7 +187,7 @@ __device__ __forceinline__ float transmission_weight(const Mat& m) {
     return smax(0.0f, maxc(sclamp3(ld3(m.transmission_color), 0.0f, 1.0f) * uc * ub)) * tr * (1.0f - metal);
 }
 
-__device__ __noinline__ float bsdf_pdf(const Mat& m, const LobeWeights& w, const V3& n, const V3& cn, const V3& v,
+static __device__ __noinline__ float bsdf_pdf(const Mat& m, const LobeWeights& w, const V3& n, const V3& cn, const V3& v,
                                        const V3& l) {
     const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
     if (nl <= 0.0f) return 0.0f;
@@ -203,7 +203,7 @@ __device__ __noinline__ float bsdf_pdf(const Mat& m, const LobeWeights& w, const
     return dp * nl * kInvPi + bp * spec_pdf(n, v, l, sr) + coatTerm;
 }
 
-__device__ __noinline__ V3 bsdf_eval(const Mat& m, const V3& n, const V3& cn, const V3& v, const V3& l) {
+static __device__ __noinline__ V3 bsdf_eval(const Mat& m, const V3& n, const V3& cn, const V3& v, const V3& l) {
     const float nv = sclamp(dot(n, v), 0.0f, 1.0f);
     const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
     if (nv <= 0.0f || nl <= 0.0f) return {0.0f, 0.0f, 0.0f};

@@ -28,7 +28,7 @@ void launch_plain_paths(const DevScene& s, const DevRequest& q, uint64_t pathBas
 void launch_resolve_pixels(const DevRequest& q, uint64_t pixelBase, uint32_t count, const float4* records, AovPtrs aov,
                            cudaStream_t stream);
 void launch_primary_hits(const DevScene& s, const DevRequest& q, uint32_t* prim, float* t, cudaStream_t stream);
-// Work counts of every stride-th path (10 totals, see ShiroWorkCounts).
+// Work counts of every stride-th path (12 totals, see ShiroWorkCounts).
 void launch_count_paths(const DevScene& s, const DevRequest& q, uint32_t stride, unsigned long long* totals,
                         cudaStream_t stream);
 void launch_trace_rays(const DevScene& s, const float* o, const float* d, const float* tmax, uint32_t n, uint32_t* prim,

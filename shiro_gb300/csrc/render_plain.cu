@@ -113,9 +113,9 @@ __global__ void __launch_bounds__(128) k_count_paths(const DevScene s, const Dev
         trace_path(s, q, x, y, q.sampleStart + smp, c);
         traced = 1;
     }
-    const uint32_t v[10] = {traced, c.closestRays, c.occlusionRays, c.nodes, c.tris, c.hits, c.envEvals, c.envSamples,
-                            c.bsdfEvals, c.bsdfPdfs};
-    for (int k = 0; k < 10; ++k) {
+    const uint32_t v[12] = {traced,  c.closestRays, c.occlusionRays, c.nodes + c.onodes, c.tris + c.otris, c.hits,
+                            c.envEvals, c.envSamples, c.bsdfEvals, c.bsdfPdfs, c.onodes, c.otris};
+    for (int k = 0; k < 12; ++k) {
         unsigned long long x = v[k];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
         if ((threadIdx.x & 31) == 0 && x) atomicAdd(&totals[k], x);

@@ -39,7 +39,7 @@ __device__ __forceinline__ float qmc_radical(uint32_t i) {  // RadicalInverse, :
     return acc;
 }
 
-__device__ __noinline__ float qmc_radical_dim(uint32_t dim, uint32_t i) {
+static __device__ __noinline__ float qmc_radical_dim(uint32_t dim, uint32_t i) {
     switch (dim % 24u) {
         case 0: return qmc_radical<2>(i);
         case 1: return qmc_radical<3>(i);

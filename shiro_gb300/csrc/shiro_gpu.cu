@@ -904,13 +904,13 @@ int shiro_gpu_count_work(ShiroGpuContext* handle, const ShiroRenderDesc* req, ui
     const DevRequest q = make_request(*req);
     if (!ensure_block(ctx, &ctx->probeScratch, 16 * sizeof(unsigned long long), "work counters")) return SHIRO_ERR_OUT_OF_MEMORY;
     auto* totals = static_cast<unsigned long long*>(ctx->probeScratch.ptr);
-    cudaError_t e = cudaMemsetAsync(totals, 0, 10 * sizeof(unsigned long long), ctx->stream);
+    cudaError_t e = cudaMemsetAsync(totals, 0, 12 * sizeof(unsigned long long), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "work counters");
     if (req->sample_count > 0) launch_count_paths(ctx->scene, q, stride, totals, ctx->stream);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(ctx, e, "count launch");
     if ((rc = check_device_error(ctx)) != SHIRO_OK) return rc;
-    unsigned long long h[10];
+    unsigned long long h[12];
     e = cudaMemcpyAsync(h, totals, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "work counters readback");
@@ -924,6 +924,8 @@ int shiro_gpu_count_work(ShiroGpuContext* handle, const ShiroRenderDesc* req, ui
     out->env_samples = h[7];
     out->bsdf_evals = h[8];
     out->bsdf_pdfs = h[9];
+    out->occlusion_node_visits = h[10];
+    out->occlusion_tri_tests = h[11];
     return SHIRO_OK;
 }
 

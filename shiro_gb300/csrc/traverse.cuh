@@ -29,6 +29,8 @@ constexpr uint32_t kMaxVisits = 1u << 22;
 struct NullCounter {
     __device__ __forceinline__ void node() {}
     __device__ __forceinline__ void tri() {}
+    __device__ __forceinline__ void onode() {}
+    __device__ __forceinline__ void otri() {}
     __device__ __forceinline__ void closest() {}
     __device__ __forceinline__ void occlusion() {}
     __device__ __forceinline__ void hit() {}
@@ -38,10 +40,12 @@ struct NullCounter {
     __device__ __forceinline__ void bsdf_pdf() {}
 };
 struct LocalCounter {
-    uint32_t nodes = 0, tris = 0, closestRays = 0, occlusionRays = 0, hits = 0, envEvals = 0, envSamples = 0,
-             bsdfEvals = 0, bsdfPdfs = 0;
+    uint32_t nodes = 0, tris = 0, onodes = 0, otris = 0, closestRays = 0, occlusionRays = 0, hits = 0, envEvals = 0,
+             envSamples = 0, bsdfEvals = 0, bsdfPdfs = 0;
     __device__ __forceinline__ void node() { ++nodes; }
     __device__ __forceinline__ void tri() { ++tris; }
+    __device__ __forceinline__ void onode() { ++onodes; }
+    __device__ __forceinline__ void otri() { ++otris; }
     __device__ __forceinline__ void closest() { ++closestRays; }
     __device__ __forceinline__ void occlusion() { ++occlusionRays; }
     __device__ __forceinline__ void hit() { ++hits; }
@@ -213,7 +217,7 @@ __device__ __noinline__ bool trace_occluded(const DevScene& s, const V3 o, const
             return false;
         }
         if (node >= 0) {
-            ctr.node();
+            ctr.onode();
             const float4* np = s.nodes + 4 * static_cast<size_t>(node);
             const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
             float t0, t1;
@@ -242,7 +246,7 @@ __device__ __noinline__ bool trace_occluded(const DevScene& s, const V3 o, const
             const uint32_t enc = ~static_cast<uint32_t>(node);
             const uint32_t first = enc >> 3, cnt = (enc & 7u) + 1u;
             for (uint32_t k = first; k < first + cnt; ++k) {
-                ctr.tri();
+                ctr.otri();
                 const float4* tp = s.tris + 3 * static_cast<size_t>(k);
                 const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
                 float t, u, v;

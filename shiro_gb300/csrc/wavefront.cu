@@ -1,19 +1,782 @@
-// wavefront.cu - batched wavefront form (placeholder until implemented).
+// wavefront.cu - the batched wavefront form.
+//
+// The reference has no wavefront path (its README and docs list one only as
+// planned).  This form renders many requests (views / frames of uneven
+// resolution, spp and depth) in one call, against one resident scene, with
+// the estimator of integrator.cuh split into stages over a pool of paths:
+//
+//   generate : camera rays of the wave's paths                -> ray queue
+//   extend   : closest hit of every queued ray
+//   shade    : miss / hit shading, light samples (+ their
+//              contributions), continuation & Russian roulette -> next ray queue,
+//                                                               shadow queue
+//   shadow   : occlusion of each queued path's light samples,
+//              in-order sum of the visible contributions
+//   resolve  : per-pixel average of the wave's path records
+//
+// Paths are packed into waves of at most `paths_in_flight` paths (whole
+// pixels; a wave may span several requests).  One wave is one CUDA graph -
+// generate, max-depth x (extend, shade, shadow, bookkeeping), resolve - and
+// the graph is replayed for every wave; the stage kernels are persistent
+// (grid sized to the resident capacity) and read their queue lengths from
+// device memory, so nothing returns to the host between bounces.  Queue
+// slots are claimed with warp-aggregated atomics (one atomicAdd per warp).
+//
+// Every float of a path is produced by the same integrator.cuh functions as
+// the plain form, in the same order, so results are bit-identical to
+// shiro_gpu_render.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <vector>
+
 #include "context.h"
+#include "integrator.cuh"
 
 namespace shiro_gpu {
 
-int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc*, uint32_t, const volatile int*, ShiroAovs*) {
-    return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "wavefront form not built");
+namespace {
+
+struct WaveSeg {
+    uint32_t req;
+    uint32_t pixelStart;
+    uint32_t pixelCount;
+    uint32_t pathOffset;   // first path of the segment within the wave
+    uint32_t pixelOffset;  // first pixel of the segment within the wave
+    uint32_t pad[3];
+};
+
+struct WaveDesc {
+    uint32_t segBegin, segCount;
+    uint32_t paths, pixels;
+};
+
+struct WfRequest {
+    DevRequest q;
+    AovPtrs aov;
+};
+
+// State flag bits (T.w)
+constexpr uint32_t kFlagPrevDelta = 1u << 16;
+constexpr uint32_t kFlagDone = 1u << 17;
+
+struct WfView {
+    // path state, one entry per slot of the wave
+    float4* ro;      // ro.xyz, unused
+    float4* rd;      // rd.xyz, prevPdf
+    float4* T;       // T.xyz, bits: diffDepth | specDepth << 8 | flags
+    float4* rad;     // radiance.xyz, first-hit depth
+    uint4* ident;    // px, py, sample index, request
+    float4* hit;     // t, u, v, slot bits
+    uint32_t* hitGid;
+    // shadow records
+    float4* shOrigin;  // origin.xyz
+    float4* shT;       // throughput at the vertex
+    float4* shDir;     // [lightSamples][P]: dir.xyz, valid
+    float4* shC;       // [lightSamples][P]: contribution
+    uint32_t* rayQ0;
+    uint32_t* rayQ1;
+    uint32_t* shadowQ;
+    uint32_t* counters;  // 0: ray count A, 1: ray count B, 2: shadow count, 3: wave index
+    float4* records;     // 3 per slot
+    const WaveDesc* waves;
+    const WaveSeg* segs;
+    const WfRequest* reqs;
+    uint32_t P;
+    uint32_t lightSamples;
+};
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// Appends `item` to a queue when `pred`; one atomicAdd per warp.
+__device__ __forceinline__ void warp_push(uint32_t* counter, uint32_t* queue, bool pred, uint32_t item) {
+    const uint32_t active = __activemask();
+    const uint32_t ballot = __ballot_sync(active, pred);
+    if (ballot == 0u) return;
+    const uint32_t leader = __ffs(active) - 1u;
+    uint32_t base = 0;
+    if (lane_id() == leader) base = atomicAdd(counter, static_cast<uint32_t>(__popc(ballot)));
+    base = __shfl_sync(active, base, leader);
+    if (pred) queue[base + __popc(ballot & ((1u << lane_id()) - 1u))] = item;
 }
-void wavefront_free(ContextImpl*) {}
-int wavefront_get_config(const ContextImpl*, ShiroWavefrontConfig* out) {
-    *out = ShiroWavefrontConfig{};
+
+__device__ __forceinline__ const WaveDesc& cur_wave(const WfView& v) { return v.waves[v.counters[3]]; }
+
+__device__ __forceinline__ const WaveSeg& find_seg(const WfView& v, const WaveDesc& w, uint32_t j, bool byPixel) {
+    uint32_t lo = w.segBegin, hi = w.segBegin + w.segCount - 1u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1u) >> 1;
+        const uint32_t key = byPixel ? v.segs[mid].pixelOffset : v.segs[mid].pathOffset;
+        if (key <= j) lo = mid; else hi = mid - 1u;
+    }
+    return v.segs[lo];
+}
+
+__global__ void wf_begin(WfView v) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const uint32_t w = v.counters[3] + 1u;
+        v.counters[3] = w;
+        v.counters[0] = v.waves[w].paths;
+        v.counters[1] = 0u;
+        v.counters[2] = 0u;
+    }
+}
+
+__global__ void __launch_bounds__(128) wf_generate(WfView v) {
+    const WaveDesc w = cur_wave(v);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < w.paths; j += gridDim.x * blockDim.x) {
+        const WaveSeg& sg = find_seg(v, w, j, false);
+        const DevRequest& q = v.reqs[sg.req].q;
+        const uint32_t local = j - sg.pathOffset;
+        const uint32_t pix = sg.pixelStart + local / q.sampleCount;
+        const uint32_t smpIdx = q.sampleStart + (local - (local / q.sampleCount) * q.sampleCount);
+        const uint32_t y = pix / q.width, x = pix - y * q.width;
+        const Sampler smp{x, y, smpIdx};
+        PathState ps;
+        init_path(q, smp, ps);
+        v.ro[j] = make_float4(ps.ro.x, ps.ro.y, ps.ro.z, 0.0f);
+        v.rd[j] = make_float4(ps.rd.x, ps.rd.y, ps.rd.z, ps.prevPdf);
+        v.T[j] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(kFlagPrevDelta));
+        v.rad[j] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(0x7f800000));
+        v.ident[j] = make_uint4(x, y, smpIdx, sg.req);
+        v.records[3 * static_cast<size_t>(j) + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        v.records[3 * static_cast<size_t>(j) + 2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        v.rayQ0[j] = j;
+    }
+}
+
+__global__ void __launch_bounds__(256) wf_extend(WfView v, DevScene s, uint32_t cur) {
+    const uint32_t count = v.counters[cur];
+    const uint32_t* q = cur ? v.rayQ1 : v.rayQ0;
+    NullCounter ctr;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t j = q[i];
+        const float4 o = v.ro[j], d = v.rd[j];
+        HitRec h;
+        trace_closest(s, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, &h, ctr);
+        v.hit[j] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+        v.hitGid[j] = h.gid;
+    }
+}
+
+__device__ __forceinline__ void write_record(const WfView& v, uint32_t j, const V3& rad, float depth0) {
+    v.records[3 * static_cast<size_t>(j)] = make_float4(rad.x, rad.y, rad.z, depth0);
+}
+
+__global__ void __launch_bounds__(256) wf_shade(WfView v, DevScene s, uint32_t cur, uint32_t depth) {
+    const uint32_t count = v.counters[cur];
+    const uint32_t* qin = cur ? v.rayQ1 : v.rayQ0;
+    uint32_t* qout = cur ? v.rayQ0 : v.rayQ1;
+    uint32_t* cout = &v.counters[cur ^ 1u];
+    NullCounter ctr;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // every lane of a warp runs the same number of iterations so that the
+    // warp-aggregated pushes see the whole warp
+    const uint32_t iters = (count + stride - 1u) / stride;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (uint32_t it = 0; it < iters; ++it, i += stride) {
+        const bool valid = i < count;
+        bool pushRay = false, pushShadow = false;
+        uint32_t j = 0;
+        if (valid) {
+            j = qin[i];
+            const uint4 id = v.ident[j];
+            const DevRequest& q = v.reqs[id.w].q;
+            const float4 o = v.ro[j], d = v.rd[j], t4 = v.T[j], r4 = v.rad[j], h4 = v.hit[j];
+            const uint32_t bits = __float_as_uint(t4.w);
+            PathState ps;
+            ps.ro = V3{o.x, o.y, o.z};
+            ps.rd = V3{d.x, d.y, d.z};
+            ps.prevPdf = d.w;
+            ps.T = V3{t4.x, t4.y, t4.z};
+            ps.radiance = V3{r4.x, r4.y, r4.z};
+            ps.diffDepth = bits & 0xffu;
+            ps.specDepth = (bits >> 8) & 0xffu;
+            ps.prevDelta = (bits & kFlagPrevDelta) != 0u;
+            float depth0 = r4.w;
+            HitRec h;
+            h.t = h4.x;
+            h.u = h4.y;
+            h.v = h4.z;
+            h.slot = __float_as_uint(h4.w);
+            h.gid = v.hitGid[j];
+            if (h.slot == 0xffffffffu) {
+                add_miss(s, q, ps, depth, ctr);
+                write_record(v, j, ps.radiance, depth0);
+            } else {
+                const Vertex vx = make_vertex(s, ps.ro, ps.rd, h);
+                if (depth == 0) {
+                    const V3 alb = diffuse_color(s.materials[vx.hit.material]);
+                    const V3 nn = vx.n * 0.5f + V3{0.5f, 0.5f, 0.5f};
+                    v.records[3 * static_cast<size_t>(j) + 1] = make_float4(alb.x, alb.y, alb.z, 0.0f);
+                    v.records[3 * static_cast<size_t>(j) + 2] = make_float4(nn.x, nn.y, nn.z, 0.0f);
+                    depth0 = h.t;
+                }
+                const Sampler smp{id.x, id.y, id.z};
+                bool anyLight = false;
+                for (uint32_t k = 0; k < v.lightSamples; ++k) {
+                    V3 dir{0.0f, 0.0f, 0.0f}, c{0.0f, 0.0f, 0.0f};
+                    const bool ok = light_sample(s, q, vx, smp, depth, k, &dir, &c, ctr);
+                    anyLight |= ok;
+                    const size_t e = static_cast<size_t>(k) * v.P + j;
+                    v.shDir[e] = make_float4(dir.x, dir.y, dir.z, ok ? 1.0f : 0.0f);
+                    v.shC[e] = make_float4(c.x, c.y, c.z, 0.0f);
+                }
+                if (anyLight) {
+                    const V3 org = shadow_origin(vx);
+                    v.shOrigin[j] = make_float4(org.x, org.y, org.z, 0.0f);
+                    v.shT[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, 0.0f);
+                    pushShadow = true;
+                }
+                const bool cont = continue_path(s, q, vx, smp, depth, ps, ctr) && depth + 1u < q.maxDepth;
+                uint32_t nb = (ps.diffDepth & 0xffu) | ((ps.specDepth & 0xffu) << 8) | (ps.prevDelta ? kFlagPrevDelta : 0u);
+                if (!cont && anyLight) nb |= kFlagDone;
+                v.T[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, __uint_as_float(nb));
+                if (cont) {
+                    v.ro[j] = make_float4(ps.ro.x, ps.ro.y, ps.ro.z, 0.0f);
+                    v.rd[j] = make_float4(ps.rd.x, ps.rd.y, ps.rd.z, ps.prevPdf);
+                    pushRay = true;
+                }
+                v.rad[j] = make_float4(ps.radiance.x, ps.radiance.y, ps.radiance.z, depth0);
+                if (!cont && !anyLight) write_record(v, j, ps.radiance, depth0);
+            }
+        }
+        warp_push(cout, qout, pushRay, j);
+        warp_push(&v.counters[2], v.shadowQ, pushShadow, j);
+    }
+}
+
+__global__ void __launch_bounds__(256) wf_shadow(WfView v, DevScene s) {
+    const uint32_t count = v.counters[2];
+    NullCounter ctr;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t j = v.shadowQ[i];
+        const DevRequest& q = v.reqs[v.ident[j].w].q;
+        const float4 o4 = v.shOrigin[j], t4 = v.shT[j], r4 = v.rad[j];
+        const V3 org{o4.x, o4.y, o4.z};
+        const V3 direct = sum_direct(s, q, [&](uint32_t k, V3* c) {
+            const size_t e = static_cast<size_t>(k) * v.P + j;
+            const float4 d4 = v.shDir[e];
+            if (d4.w == 0.0f) return false;
+            if (trace_occluded(s, org, V3{d4.x, d4.y, d4.z}, FLT_MAX, ctr)) return false;
+            const float4 c4 = v.shC[e];
+            *c = V3{c4.x, c4.y, c4.z};
+            return true;
+        });
+        const V3 rad = V3{r4.x, r4.y, r4.z} + V3{t4.x, t4.y, t4.z} * direct;
+        v.rad[j] = make_float4(rad.x, rad.y, rad.z, r4.w);
+        if (__float_as_uint(v.T[j].w) & kFlagDone) write_record(v, j, rad, r4.w);
+    }
+}
+
+__global__ void wf_end_bounce(WfView v, uint32_t cur) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        v.counters[cur] = 0u;
+        v.counters[2] = 0u;
+    }
+}
+
+// Per-pixel average of the wave's records, same additions as k_resolve.
+__global__ void __launch_bounds__(128) wf_resolve(WfView v) {
+    const WaveDesc w = cur_wave(v);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < w.pixels; p += gridDim.x * blockDim.x) {
+        const WaveSeg& sg = find_seg(v, w, p, true);
+        const WfRequest& r = v.reqs[sg.req];
+        const uint32_t n = r.q.sampleCount;
+        const uint32_t lp = p - sg.pixelOffset;
+        const float4* rec = v.records + 3 * (static_cast<size_t>(sg.pathOffset) + static_cast<size_t>(lp) * n);
+        float b0 = 0.0f, b1 = 0.0f, b2 = 0.0f, b3 = 0.0f;
+        V3 alb{0.0f, 0.0f, 0.0f}, nrm{0.0f, 0.0f, 0.0f};
+        float depth = __int_as_float(0x7f800000);
+        for (uint32_t k = 0; k < n; ++k) {
+            const float4 a = rec[3 * k], b = rec[3 * k + 1], c = rec[3 * k + 2];
+            b0 = b0 + a.x;
+            b1 = b1 + a.y;
+            b2 = b2 + a.z;
+            b3 = b3 + (a.w < __int_as_float(0x7f800000) ? 1.0f : 0.0f);
+            alb = alb + V3{b.x, b.y, b.z};
+            nrm = nrm + V3{c.x, c.y, c.z};
+            if (a.w < depth) depth = a.w;
+        }
+        const float cnt = static_cast<float>(n);
+        const float inv = 1.0f / cnt;
+        const size_t px = static_cast<size_t>(sg.pixelStart) + lp;
+        r.aov.beauty[4 * px + 0] = b0 / cnt;
+        r.aov.beauty[4 * px + 1] = b1 / cnt;
+        r.aov.beauty[4 * px + 2] = b2 / cnt;
+        r.aov.beauty[4 * px + 3] = b3 / cnt;
+        const V3 a = alb * inv, nn = nrm * inv;
+        r.aov.albedo[3 * px + 0] = a.x;
+        r.aov.albedo[3 * px + 1] = a.y;
+        r.aov.albedo[3 * px + 2] = a.z;
+        r.aov.normal[3 * px + 0] = nn.x;
+        r.aov.normal[3 * px + 1] = nn.y;
+        r.aov.normal[3 * px + 2] = nn.z;
+        r.aov.depth[px] = depth;
+    }
+}
+
+}  // namespace
+
+// ===========================================================================
+// host side
+// ===========================================================================
+struct WavefrontState {
+    ShiroWavefrontConfig cfg{};
+    DeviceBlock state, shadow, queues, records, tables;
+    uint32_t P = 0, lightSamples = 0;
+    int smCount = 0;
+    bool tuned = false;
+};
+
+namespace {
+
+WavefrontState* wf_state(ContextImpl* ctx) {
+    if (!ctx->wavefront) {
+        ctx->wavefront = new WavefrontState();
+        ShiroWavefrontConfig& c = ctx->wavefront->cfg;
+        c.paths_in_flight = 1u << 22;
+        c.extend_block = 128;
+        c.shade_block = 128;
+        c.shadow_block = 128;
+        c.use_graph = 1;
+        cudaDeviceGetAttribute(&ctx->wavefront->smCount, cudaDevAttrMultiProcessorCount, ctx->device);
+    }
+    return ctx->wavefront;
+}
+
+bool ensure_pool(ContextImpl* ctx, WavefrontState* wf, uint32_t P, uint32_t lightSamples) {
+    const size_t p = P;
+    const size_t stateBytes = p * (6 * sizeof(float4) + sizeof(uint32_t));
+    const size_t shadowBytes = p * (2 + 2 * static_cast<size_t>(std::max(1u, lightSamples))) * sizeof(float4);
+    const size_t queueBytes = p * 3 * sizeof(uint32_t) + 64;
+    const size_t recordBytes = p * 3 * sizeof(float4);
+    if (!ensure_block(ctx, &wf->state, stateBytes, "wavefront state")) return false;
+    if (!ensure_block(ctx, &wf->shadow, shadowBytes, "wavefront shadow records")) return false;
+    if (!ensure_block(ctx, &wf->queues, queueBytes, "wavefront queues")) return false;
+    if (!ensure_block(ctx, &wf->records, recordBytes, "wavefront path records")) return false;
+    wf->P = P;
+    wf->lightSamples = lightSamples;
+    return true;
+}
+
+WfView make_view(WavefrontState* wf, uint32_t P, uint32_t lightSamples, const WaveDesc* waves, const WaveSeg* segs,
+                 const WfRequest* reqs) {
+    WfView v{};
+    const size_t p = P;
+    char* st = static_cast<char*>(wf->state.ptr);
+    v.ro = reinterpret_cast<float4*>(st);
+    v.rd = v.ro + p;
+    v.T = v.rd + p;
+    v.rad = v.T + p;
+    v.ident = reinterpret_cast<uint4*>(v.rad + p);
+    v.hit = reinterpret_cast<float4*>(v.ident + p);
+    v.hitGid = reinterpret_cast<uint32_t*>(v.hit + p);
+    float4* sh = static_cast<float4*>(wf->shadow.ptr);
+    v.shOrigin = sh;
+    v.shT = sh + p;
+    v.shDir = sh + 2 * p;
+    v.shC = sh + (2 + static_cast<size_t>(std::max(1u, lightSamples))) * p;
+    uint32_t* qb = static_cast<uint32_t*>(wf->queues.ptr);
+    v.counters = qb;
+    v.rayQ0 = qb + 16;
+    v.rayQ1 = v.rayQ0 + p;
+    v.shadowQ = v.rayQ1 + p;
+    v.records = static_cast<float4*>(wf->records.ptr);
+    v.waves = waves;
+    v.segs = segs;
+    v.reqs = reqs;
+    v.P = P;
+    v.lightSamples = lightSamples;
+    return v;
+}
+
+template <typename K>
+int grid_for(K kernel, int block, int smCount) {
+    int perSm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, block, 0);
+    return std::max(1, perSm) * smCount;
+}
+
+struct Plan {
+    std::vector<WaveDesc> waves;
+    std::vector<WaveSeg> segs;
+    uint32_t maxDepth = 0;
+    uint32_t maxWavePixels = 0;
+    uint64_t paths = 0;
+};
+
+// Packs whole pixels of the requests, in order, into waves of <= P paths.
+Plan plan_waves(const std::vector<DevRequest>& qs, uint32_t P) {
+    Plan pl;
+    WaveDesc cur{0, 0, 0, 0};
+    auto flush = [&]() {
+        if (cur.paths) {
+            pl.maxWavePixels = std::max(pl.maxWavePixels, cur.pixels);
+            pl.waves.push_back(cur);
+        }
+        cur = WaveDesc{static_cast<uint32_t>(pl.segs.size()), 0, 0, 0};
+    };
+    cur.segBegin = 0;
+    for (uint32_t r = 0; r < qs.size(); ++r) {
+        const DevRequest& q = qs[r];
+        const uint64_t pixels = static_cast<uint64_t>(q.width) * q.height;
+        if (q.sampleCount == 0 || pixels == 0 || q.maxDepth == 0) continue;
+        pl.maxDepth = std::max(pl.maxDepth, q.maxDepth);
+        pl.paths += pixels * q.sampleCount;
+        uint64_t done = 0;
+        while (done < pixels) {
+            const uint32_t room = (P - cur.paths) / q.sampleCount;
+            if (room == 0) {
+                flush();
+                continue;
+            }
+            const uint32_t take = static_cast<uint32_t>(std::min<uint64_t>(room, pixels - done));
+            WaveSeg sg{};
+            sg.req = r;
+            sg.pixelStart = static_cast<uint32_t>(done);
+            sg.pixelCount = take;
+            sg.pathOffset = cur.paths;
+            sg.pixelOffset = cur.pixels;
+            pl.segs.push_back(sg);
+            cur.segCount += 1;
+            cur.paths += take * q.sampleCount;
+            cur.pixels += take;
+            done += take;
+        }
+    }
+    flush();
+    return pl;
+}
+
+struct Launch {
+    WfView v;
+    DevScene s;
+    int gGen, gExt, gShade, gShadow, gRes;
+    int bExt, bShade, bShadow;
+    uint32_t depth;
+};
+
+void enqueue_wave(const Launch& L, cudaStream_t st) {
+    wf_begin<<<1, 32, 0, st>>>(L.v);
+    wf_generate<<<L.gGen, 128, 0, st>>>(L.v);
+    for (uint32_t d = 0; d < L.depth; ++d) {
+        const uint32_t cur = d & 1u;
+        wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur);
+        wf_shade<<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
+        wf_shadow<<<L.gShadow, L.bShadow, 0, st>>>(L.v, L.s);
+        wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur);
+    }
+    wf_resolve<<<L.gRes, 128, 0, st>>>(L.v);
+}
+
+// The same wave with events around every stage launch (diagnostic timing).
+void enqueue_wave_timed(const Launch& L, cudaStream_t st, std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>>& ev) {
+    auto timed = [&](int stage, auto&& launch) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, st);
+        launch();
+        cudaEventRecord(b, st);
+        ev.push_back({stage, {a, b}});
+    };
+    timed(5, [&] { wf_begin<<<1, 32, 0, st>>>(L.v); });
+    timed(0, [&] { wf_generate<<<L.gGen, 128, 0, st>>>(L.v); });
+    for (uint32_t d = 0; d < L.depth; ++d) {
+        const uint32_t cur = d & 1u;
+        timed(1, [&] { wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur); });
+        timed(2, [&] { wf_shade<<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d); });
+        timed(3, [&] { wf_shadow<<<L.gShadow, L.bShadow, 0, st>>>(L.v, L.s); });
+        timed(5, [&] { wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur); });
+    }
+    timed(4, [&] { wf_resolve<<<L.gRes, 128, 0, st>>>(L.v); });
+}
+
+// Renders the requests (device AOV planes in `aovs`) with configuration
+// `cfg`.  maxWaves limits the waves run (autotuning); returns paths traced.
+int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& cfg, const std::vector<DevRequest>& qs,
+              const std::vector<AovPtrs>& aovs, const volatile int* cancel, uint32_t maxWaves, uint64_t* pathsOut,
+              double* msOut) {
+    uint32_t lightSamples = ctx->scene.distantCount;
+    uint32_t domeSamplesMax = 1;
+    for (const DevRequest& q : qs) domeSamplesMax = std::max(domeSamplesMax, q.domeSamples);
+    lightSamples += ctx->scene.domeCount * domeSamplesMax;
+    if (lightSamples > kMaxLightSamples)
+        return fail(ctx, SHIRO_ERR_UNSUPPORTED_SCENE, "wavefront form: more than 8 light samples per shading point");
+    uint32_t maxSpp = 1;
+    for (const DevRequest& q : qs) maxSpp = std::max(maxSpp, q.sampleCount);
+    const uint32_t P = std::max(cfg.paths_in_flight, maxSpp);
+    Plan pl = plan_waves(qs, P);
+    if (pl.waves.empty()) {
+        *pathsOut = 0;
+        return SHIRO_OK;
+    }
+    uint32_t used = std::min<uint32_t>(static_cast<uint32_t>(pl.waves.size()), maxWaves);
+    uint32_t poolP = 0;
+    for (uint32_t w = 0; w < used; ++w) poolP = std::max(poolP, pl.waves[w].paths);
+    if (!ensure_pool(ctx, wf, poolP, lightSamples)) return SHIRO_ERR_OUT_OF_MEMORY;
+    // tables: waves, segments, requests
+    std::vector<WfRequest> rq(qs.size());
+    for (size_t r = 0; r < qs.size(); ++r) rq[r] = WfRequest{qs[r], aovs[r]};
+    const size_t tb = pl.waves.size() * sizeof(WaveDesc) + pl.segs.size() * sizeof(WaveSeg) + rq.size() * sizeof(WfRequest) + 256;
+    if (!ensure_block(ctx, &wf->tables, tb, "wavefront tables")) return SHIRO_ERR_OUT_OF_MEMORY;
+    char* t = static_cast<char*>(wf->tables.ptr);
+    WaveDesc* dWaves = reinterpret_cast<WaveDesc*>(t);
+    WaveSeg* dSegs = reinterpret_cast<WaveSeg*>(t + ((pl.waves.size() * sizeof(WaveDesc) + 63) & ~size_t(63)));
+    WfRequest* dReqs = reinterpret_cast<WfRequest*>(reinterpret_cast<char*>(dSegs) +
+                                                    ((pl.segs.size() * sizeof(WaveSeg) + 63) & ~size_t(63)));
+    cudaStream_t st = ctx->stream;
+    cudaError_t e = cudaMemcpyAsync(dWaves, pl.waves.data(), pl.waves.size() * sizeof(WaveDesc), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dSegs, pl.segs.data(), pl.segs.size() * sizeof(WaveSeg), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dReqs, rq.data(), rq.size() * sizeof(WfRequest), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "wavefront tables");
+    Launch L;
+    L.v = make_view(wf, poolP, lightSamples, dWaves, dSegs, dReqs);
+    L.s = ctx->scene;
+    L.bExt = static_cast<int>(cfg.extend_block);
+    L.bShade = static_cast<int>(cfg.shade_block);
+    L.bShadow = static_cast<int>(cfg.shadow_block);
+    L.gGen = grid_for(wf_generate, 128, wf->smCount);
+    L.gExt = grid_for(wf_extend, L.bExt, wf->smCount);
+    L.gShade = grid_for(wf_shade, L.bShade, wf->smCount);
+    L.gShadow = grid_for(wf_shadow, L.bShadow, wf->smCount);
+    L.gRes = grid_for(wf_resolve, 128, wf->smCount);
+    L.depth = pl.maxDepth;
+    const uint32_t minus1 = 0xffffffffu;
+    e = cudaMemsetAsync(L.v.counters, 0, 16 * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(L.v.counters + 3, &minus1, 4, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "wavefront counters");
+
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev;
+    cudaGraphExec_t exec = nullptr;
+    int rc = SHIRO_OK;
+    if (cfg.use_graph) {
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            enqueue_wave(L, st);
+            e = cudaStreamEndCapture(st, &graph);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront graph");
+    }
+    uint64_t launches = 0;
+    for (uint32_t w = 0; w < used && rc == SHIRO_OK; ++w) {
+        if (cancel && *cancel) {
+            rc = fail(ctx, SHIRO_ERR_CANCELLED, "cancelled");
+            break;
+        }
+        if (exec) {
+            e = cudaGraphLaunch(exec, st);
+        } else {
+            enqueue_wave_timed(L, st, ev);
+            e = cudaGetLastError();
+        }
+        launches += 3 + 4ull * L.depth;
+        if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront launch");
+    }
+    cudaEventRecord(e1, st);
+    e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess && rc == SHIRO_OK) rc = cuda_fail(ctx, e, "wavefront render");
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (exec) cudaGraphExecDestroy(exec);
+    double stageMs[6] = {0, 0, 0, 0, 0, 0};
+    uint64_t stageN[6] = {0, 0, 0, 0, 0, 0};
+    for (auto& x : ev) {
+        float v = 0.0f;
+        if (rc == SHIRO_OK) cudaEventElapsedTime(&v, x.second.first, x.second.second);
+        stageMs[x.first] += v;
+        stageN[x.first] += 1;
+        cudaEventDestroy(x.second.first);
+        cudaEventDestroy(x.second.second);
+    }
+    if (rc != SHIRO_OK) {
+        cudaStreamSynchronize(st);
+        return rc;
+    }
+    if ((rc = check_device_error(ctx)) != SHIRO_OK) return rc;
+    uint64_t paths = 0;
+    for (uint32_t w = 0; w < used; ++w) paths += pl.waves[w].paths;
+    *pathsOut = paths;
+    if (msOut) *msOut = ms;
+    ctx->stats.kernel_ms = ms;
+    ctx->stats.kernel_launches = launches;
+    ctx->stats.paths = paths;
+    ctx->stats.waves = used;
+    if (!ev.empty()) {
+        for (int k = 0; k < 6; ++k) {
+            ctx->stats.stage_ms[k] = stageMs[k];
+            ctx->stats.stage_launches[k] = stageN[k];
+        }
+        ctx->stats.path_kernel_ms = stageMs[1];
+        ctx->stats.path_kernel_launches = stageN[1];
+    }
     return SHIRO_OK;
 }
-int wavefront_set_config(ContextImpl*, const ShiroWavefrontConfig*) { return SHIRO_OK; }
-int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc*, ShiroWavefrontConfig*) {
-    return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "wavefront form not built");
+
+}  // namespace
+
+int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t count, const volatile int* cancel,
+                     ShiroAovs* outs) {
+    if (!ctx->hasScene) return fail(ctx, SHIRO_ERR_NO_SCENE, "no scene uploaded");
+    WavefrontState* wf = wf_state(ctx);
+    std::vector<DevRequest> qs(count);
+    std::vector<AovPtrs> aov(count);
+    uint64_t stagingFloats = 0;
+    for (uint32_t r = 0; r < count; ++r) {
+        int rc = validate_request(ctx, reqs[r]);
+        if (rc != SHIRO_OK) return rc;
+        if (!outs[r].beauty || !outs[r].albedo || !outs[r].normal || !outs[r].depth)
+            return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "null AOV pointer");
+        qs[r] = make_request(reqs[r]);
+        if (!outs[r].on_device) stagingFloats += 11ull * reqs[r].settings.width * reqs[r].settings.height;
+    }
+    if (stagingFloats && !ensure_block(ctx, &ctx->aovScratch, stagingFloats * sizeof(float), "AOV staging"))
+        return SHIRO_ERR_OUT_OF_MEMORY;
+    uint64_t off = 0;
+    for (uint32_t r = 0; r < count; ++r) {
+        const uint64_t px = static_cast<uint64_t>(reqs[r].settings.width) * reqs[r].settings.height;
+        if (outs[r].on_device) {
+            aov[r] = AovPtrs{outs[r].beauty, outs[r].albedo, outs[r].normal, outs[r].depth};
+        } else {
+            float* b = static_cast<float*>(ctx->aovScratch.ptr) + off;
+            aov[r] = AovPtrs{b, b + 4 * px, b + 7 * px, b + 10 * px};
+            off += 11 * px;
+        }
+        // requests without samples get cleared planes (FrameBuffer::Clear)
+        if (reqs[r].sample_count == 0 || px == 0) {
+            cudaMemsetAsync(aov[r].beauty, 0, px * 16, ctx->stream);
+            cudaMemsetAsync(aov[r].albedo, 0, px * 12, ctx->stream);
+            cudaMemsetAsync(aov[r].normal, 0, px * 12, ctx->stream);
+            std::vector<float> inf(px, __builtin_inff());
+            if (px) cudaMemcpyAsync(aov[r].depth, inf.data(), px * 4, cudaMemcpyHostToDevice, ctx->stream);
+            cudaStreamSynchronize(ctx->stream);
+        }
+    }
+    ctx->stats.path_kernel_ms = 0.0;
+    ctx->stats.path_kernel_launches = 0;
+    for (int k = 0; k < 6; ++k) {
+        ctx->stats.stage_ms[k] = 0.0;
+        ctx->stats.stage_launches[k] = 0;
+    }
+    uint64_t paths = 0;
+    int rc = run_waves(ctx, wf, wf->cfg, qs, aov, cancel, 0xffffffffu, &paths, nullptr);
+    if (rc != SHIRO_OK) return rc;
+    for (uint32_t r = 0; r < count; ++r) {
+        if (outs[r].on_device) continue;
+        const uint64_t px = static_cast<uint64_t>(reqs[r].settings.width) * reqs[r].settings.height;
+        cudaError_t e = cudaMemcpyAsync(outs[r].beauty, aov[r].beauty, px * 16, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(outs[r].albedo, aov[r].albedo, px * 12, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(outs[r].normal, aov[r].normal, px * 12, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(outs[r].depth, aov[r].depth, px * 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "AOV readback");
+    }
+    const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "AOV readback");
+    ctx->stats.device_bytes = ctx->deviceBytes();
+    return SHIRO_OK;
+}
+
+void wavefront_free(ContextImpl* ctx) {
+    if (!ctx->wavefront) return;
+    WavefrontState* wf = ctx->wavefront;
+    for (DeviceBlock* b : {&wf->state, &wf->shadow, &wf->queues, &wf->records, &wf->tables})
+        if (b->ptr) cudaFree(b->ptr);
+    delete wf;
+    ctx->wavefront = nullptr;
+}
+
+int wavefront_get_config(const ContextImpl* ctx, ShiroWavefrontConfig* out) {
+    WavefrontState* wf = wf_state(const_cast<ContextImpl*>(ctx));
+    *out = wf->cfg;
+    return SHIRO_OK;
+}
+
+int wavefront_set_config(ContextImpl* ctx, const ShiroWavefrontConfig* cfg) {
+    WavefrontState* wf = wf_state(ctx);
+    auto okBlock = [](uint32_t b) { return b == 0 || (b >= 32 && b <= 1024 && b % 32 == 0); };
+    if (!okBlock(cfg->extend_block) || !okBlock(cfg->shade_block) || !okBlock(cfg->shadow_block))
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "block sizes must be multiples of 32 in [32, 1024]");
+    if (cfg->paths_in_flight) {
+        if (cfg->paths_in_flight < 1024 || cfg->paths_in_flight > (1u << 27))
+            return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "paths_in_flight out of range [1024, 2^27]");
+        wf->cfg.paths_in_flight = cfg->paths_in_flight;
+    }
+    if (cfg->extend_block) wf->cfg.extend_block = cfg->extend_block;
+    if (cfg->shade_block) wf->cfg.shade_block = cfg->shade_block;
+    if (cfg->shadow_block) wf->cfg.shadow_block = cfg->shadow_block;
+    wf->cfg.use_graph = cfg->use_graph;
+    return SHIRO_OK;
+}
+
+// Coordinate descent over the pool size and the three stage block sizes,
+// each candidate timed on the first waves of `req` (scratch AOV planes).
+int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefrontConfig* chosen) {
+    int rc = validate_request(ctx, *req);
+    if (rc != SHIRO_OK) return rc;
+    WavefrontState* wf = wf_state(ctx);
+    std::vector<DevRequest> qs{make_request(*req)};
+    const uint64_t px = static_cast<uint64_t>(req->settings.width) * req->settings.height;
+    if (!ensure_block(ctx, &ctx->aovScratch, std::max<uint64_t>(px, 1) * 11 * sizeof(float), "AOV staging"))
+        return SHIRO_ERR_OUT_OF_MEMORY;
+    float* b = static_cast<float*>(ctx->aovScratch.ptr);
+    std::vector<AovPtrs> aov{AovPtrs{b, b + 4 * px, b + 7 * px, b + 10 * px}};
+    const uint64_t total = px * qs[0].sampleCount;
+    ShiroWavefrontConfig best = wf->cfg;
+    best.use_graph = 1;
+    double bestRate = 0.0;
+    auto trial = [&](ShiroWavefrontConfig c) -> int {
+        c.use_graph = 1;
+        // enough waves for ~1/8 of the frame, at least two
+        const uint32_t waves = static_cast<uint32_t>(std::max<uint64_t>(2, (total / 8) / std::max<uint32_t>(c.paths_in_flight, 1)));
+        uint64_t paths = 0;
+        double ms = 0.0;
+        int r = run_waves(ctx, wf, c, qs, aov, nullptr, waves, &paths, &ms);  // warm
+        if (r != SHIRO_OK) return r;
+        r = run_waves(ctx, wf, c, qs, aov, nullptr, waves, &paths, &ms);
+        if (r != SHIRO_OK) return r;
+        const double rate = static_cast<double>(paths) / std::max(ms, 1e-6);
+        if (rate > bestRate) {
+            bestRate = rate;
+            best = c;
+        }
+        return SHIRO_OK;
+    };
+    const uint32_t pools[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24};
+    for (uint32_t p : pools) {
+        if (p > total * 2 && p != pools[0]) break;
+        ShiroWavefrontConfig c = best;
+        c.paths_in_flight = p;
+        if ((rc = trial(c)) != SHIRO_OK) return rc;
+    }
+    for (uint32_t blk : {64u, 128u, 256u}) {
+        ShiroWavefrontConfig c = best;
+        c.extend_block = blk;
+        if ((rc = trial(c)) != SHIRO_OK) return rc;
+    }
+    for (uint32_t blk : {64u, 128u, 256u}) {
+        ShiroWavefrontConfig c = best;
+        c.shade_block = blk;
+        if ((rc = trial(c)) != SHIRO_OK) return rc;
+    }
+    for (uint32_t blk : {64u, 128u, 256u}) {
+        ShiroWavefrontConfig c = best;
+        c.shadow_block = blk;
+        if ((rc = trial(c)) != SHIRO_OK) return rc;
+    }
+    wf->cfg = best;
+    wf->tuned = true;
+    if (chosen) *chosen = best;
+    return SHIRO_OK;
 }
 
 }  // namespace shiro_gpu

@@ -1,0 +1,117 @@
+"""The batched wavefront form against the plain megakernel.
+
+Both forms evaluate every float of a path with the same integrator functions
+in the same order, so the wavefront frames must be bit-identical to the plain
+ones (and thereby carry the plain form's parity with the CPU oracle), for any
+pool size, block sizes, graph or direct launches, and any mix of requests.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from shiro_gb300 import GpuBackend
+
+    with GpuBackend(0) as g:
+        yield g
+
+
+def same(a, b):
+    for k in ("beauty", "albedo", "normal", "depth"):
+        x, y = getattr(a, k), getattr(b, k)
+        if not np.array_equal(x.view(np.uint32), y.view(np.uint32)):
+            return False, k, int(np.count_nonzero(x.view(np.uint32) != y.view(np.uint32)))
+    return True, None, 0
+
+
+def test_single_request_bit_identical(gpu):
+    from shiro_gb300 import scenes
+
+    w = scenes.sphere_workload(64, 48, 8, 8, env_width=128, env_height=64)
+    plain = gpu.render(w.scene, w.camera, w.settings)
+    (wave,) = gpu.render_batch(w.scene, [(w.camera, w.settings)])
+    ok, k, n = same(plain, wave)
+    assert ok, (k, n)
+
+
+@pytest.mark.parametrize("flags", [0, 1, 2])
+def test_field_scene_bit_identical(gpu, flags):
+    from shiro_gb300 import scenes
+
+    sc = scenes.field_scene(instances=16, levels=4, materials=8, env_width=256, env_height=128, seed=5, plane=14.0)
+    st = scenes.RenderSettings(width=80, height=45, samples_per_pixel=6, max_depth=12, diffuse_depth=12,
+                               specular_depth=12, backend=1)
+    cam = scenes.look_at((0.0, 4.0, 9.0), (0.0, 0.3, 0.0), 45.0, 80 / 45)
+    plain = gpu.render(sc, cam, st, 3, 6, flags=flags)
+    (wave,) = gpu.render_batch(sc, [(cam, st, 3, 6)], flags=flags)
+    ok, k, n = same(plain, wave)
+    assert ok, (k, n)
+
+
+def test_uneven_batch_small_pool(gpu):
+    """Many requests of uneven size / spp / depth, packed into waves much
+    smaller than a frame (pixels of one request straddle several waves)."""
+    from shiro_gb300 import scenes
+
+    scene = scenes.sphere_scene(env_width=128, env_height=64)
+    reqs = scenes.batch_requests(count=7, seed=11, lo=8, hi=40)
+    gpu.set_wavefront_config(paths_in_flight=4096, extend_block=64, shade_block=256, shadow_block=128, use_graph=1)
+    try:
+        outs = gpu.render_batch(scene, [(r.camera, r.settings) for r in reqs])
+        for r, fb in zip(reqs, outs):
+            ref = gpu.render(scene, r.camera, r.settings)
+            ok, k, n = same(ref, fb)
+            assert ok, (r.settings.width, r.settings.samples_per_pixel, k, n)
+    finally:
+        gpu.set_wavefront_config(paths_in_flight=1 << 22, extend_block=128, shade_block=128, shadow_block=128,
+                                 use_graph=1)
+
+
+def test_direct_launch_matches_graph_and_reports_stages(gpu):
+    from shiro_gb300 import scenes
+
+    w = scenes.sphere_workload(40, 40, 4, 6, env_width=64, env_height=32)
+    (a,) = gpu.render_batch(w.scene, [(w.camera, w.settings)])
+    gpu.set_wavefront_config(use_graph=0)
+    try:
+        (b,) = gpu.render_batch(w.scene, [(w.camera, w.settings)])
+        st = gpu.last_stats()
+    finally:
+        gpu.set_wavefront_config(use_graph=1)
+    assert same(a, b)[0]
+    assert st["stage_launches"][1] >= 6 and st["stage_ms"][1] > 0.0
+    assert st["paths"] == 40 * 40 * 4
+
+
+def test_zero_sample_request_in_batch(gpu):
+    from shiro_gb300 import scenes
+
+    w = scenes.sphere_workload(16, 16, 4, 4, env_width=32, env_height=16)
+    outs = gpu.render_batch(w.scene, [(w.camera, w.settings, 0, 0), (w.camera, w.settings, 0, 4)])
+    assert (outs[0].beauty == 0).all() and np.isinf(outs[0].depth).all()
+    assert same(outs[1], gpu.render(w.scene, w.camera, w.settings))[0]
+
+
+def test_autotune_picks_a_valid_config(gpu):
+    from shiro_gb300 import scenes
+
+    w = scenes.sphere_workload(128, 128, 16, 8, env_width=128, env_height=64)
+    cfg = gpu.autotune(w.scene, w.camera, w.settings)
+    assert cfg["paths_in_flight"] >= 1 << 20
+    assert cfg["extend_block"] in (64, 128, 256) and cfg["shade_block"] in (64, 128, 256)
+    (fb,) = gpu.render_batch(w.scene, [(w.camera, w.settings)])
+    assert same(fb, gpu.render(w.scene, w.camera, w.settings))[0]
+
+
+def test_cancel_batch(gpu):
+    from shiro_gb300 import ShiroGpuError, scenes
+
+    w = scenes.sphere_workload(16, 16, 4, 4, env_width=32, env_height=16)
+    with pytest.raises(ShiroGpuError) as ei:
+        gpu.render_batch(w.scene, [(w.camera, w.settings)], cancel=C.c_int(1))
+    assert ei.value.code == -6
