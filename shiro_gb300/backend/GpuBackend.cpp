@@ -1,0 +1,297 @@
+// GpuBackend.cpp - RenderBackend adapter over the GB300 C ABI.
+#include "GpuBackend.h"
+
+#include <cstdio>
+#include <cstring>
+#include <limits>
+
+#include "shiro/render/EnvironmentMap.h"
+#include "shiro_gpu.h"
+
+namespace shiro::backend::gb300 {
+
+namespace {
+
+using namespace shiro::render;
+
+void Put3(float* d, const Vec3f& v) {
+    d[0] = v.x;
+    d[1] = v.y;
+    d[2] = v.z;
+}
+
+ShiroMaterialDesc ToDesc(const PbrMaterial& m) {
+    ShiroMaterialDesc d;
+    std::memset(&d, 0, sizeof(d));
+    Put3(d.base_color, m.baseColor);
+    Put3(d.emission_color, m.emissionColor);
+    Put3(d.specular_color, m.specularColor);
+    Put3(d.transmission_color, m.transmissionColor);
+    Put3(d.transmission_scatter, m.transmissionScatter);
+    Put3(d.coat_color, m.coatColor);
+    Put3(d.subsurface_color, m.subsurfaceColor);
+    Put3(d.subsurface_radius, m.subsurfaceRadius);
+    Put3(d.sheen_color, m.sheenColor);
+    Put3(d.normal_override, m.normalOverride);
+    Put3(d.coat_normal_override, m.coatNormalOverride);
+    Put3(d.tangent_override, m.tangentOverride);
+    d.base_weight = m.baseWeight;
+    d.emission_strength = m.emissionStrength;
+    d.specular_weight = m.specularWeight;
+    d.metallic = m.metallic;
+    d.roughness = m.roughness;
+    d.diffuse_roughness = m.diffuseRoughness;
+    d.opacity = m.opacity;
+    d.specular_anisotropy = m.specularAnisotropy;
+    d.specular_rotation = m.specularRotation;
+    d.coat_weight = m.coatWeight;
+    d.coat_roughness = m.coatRoughness;
+    d.coat_ior = m.coatIor;
+    d.coat_anisotropy = m.coatAnisotropy;
+    d.coat_rotation = m.coatRotation;
+    d.sheen = m.sheen;
+    d.sheen_roughness = m.sheenRoughness;
+    d.subsurface = m.subsurface;
+    d.subsurface_scale = m.subsurfaceScale;
+    d.subsurface_anisotropy = m.subsurfaceAnisotropy;
+    d.transmission = m.transmission;
+    d.transmission_depth = m.transmissionDepth;
+    d.transmission_scatter_anisotropy = m.transmissionScatterAnisotropy;
+    d.transmission_dispersion = m.transmissionDispersion;
+    d.transmission_extra_roughness = m.transmissionExtraRoughness;
+    d.ior = m.ior;
+    d.coat_affect_color = m.coatAffectColor;
+    d.coat_affect_roughness = m.coatAffectRoughness;
+    d.thin_film_thickness = m.thinFilmThickness;
+    d.thin_film_ior = m.thinFilmIor;
+    d.thin_walled = m.thinWalled ? 1u : 0u;
+    d.has_normal_override = m.hasNormalOverride ? 1u : 0u;
+    d.has_coat_normal_override = m.hasCoatNormalOverride ? 1u : 0u;
+    d.has_tangent_override = m.hasTangentOverride ? 1u : 0u;
+    return d;
+}
+
+static_assert(sizeof(Vec3f) == 3 * sizeof(float), "Vec3f must be three packed floats");
+
+// Flat ABI view of a Scene; points into the Scene's own vectors.
+struct SceneView {
+    std::vector<ShiroMaterialDesc> materials;
+    std::vector<ShiroMeshDesc> meshes;
+    std::vector<ShiroDistantLightDesc> distant;
+    std::vector<ShiroDomeLightDesc> domes;
+    ShiroSceneDesc desc{};
+
+    explicit SceneView(const Scene& s) {
+        for (const PbrMaterial& m : s.materials) materials.push_back(ToDesc(m));
+        for (const TriangleMesh& m : s.meshes) {
+            ShiroMeshDesc d{};
+            d.positions = reinterpret_cast<const float*>(m.positions.data());
+            d.vertex_count = static_cast<uint32_t>(m.positions.size());
+            d.normals = m.normals.empty() ? nullptr : reinterpret_cast<const float*>(m.normals.data());
+            d.normal_count = static_cast<uint32_t>(m.normals.size());
+            d.indices = m.indices.data();
+            d.index_count = static_cast<uint32_t>(m.indices.size());
+            d.material_index = m.materialIndex;
+            meshes.push_back(d);
+        }
+        for (const DirectionalLight& l : s.distantLights) {
+            ShiroDistantLightDesc d{};
+            Put3(d.direction, l.direction);
+            Put3(d.radiance, l.radiance);
+            distant.push_back(d);
+        }
+        for (const DomeLight& l : s.domeLights) {
+            ShiroDomeLightDesc d{};
+            Put3(d.radiance, l.radiance);
+            Put3(d.right, l.right);
+            Put3(d.up, l.up);
+            Put3(d.forward, l.forward);
+            d.layout = SHIRO_ENV_LAYOUT_LATLONG;
+            if (l.environment && !l.environment->Pixels().empty()) {
+                d.layout = l.environment->Layout() == EnvironmentMapLayout::Angular ? SHIRO_ENV_LAYOUT_ANGULAR
+                                                                                      : SHIRO_ENV_LAYOUT_LATLONG;
+                d.env_width = l.environment->Width();
+                d.env_height = l.environment->Height();
+                d.env_pixels = reinterpret_cast<const float*>(l.environment->Pixels().data());
+            }
+            domes.push_back(d);
+        }
+        desc.materials = materials.data();
+        desc.material_count = static_cast<uint32_t>(materials.size());
+        desc.meshes = meshes.data();
+        desc.mesh_count = static_cast<uint32_t>(meshes.size());
+        desc.distant_lights = distant.data();
+        desc.distant_light_count = static_cast<uint32_t>(distant.size());
+        desc.dome_lights = domes.data();
+        desc.dome_light_count = static_cast<uint32_t>(domes.size());
+        Put3(desc.environment_top, s.environmentTop);
+        Put3(desc.environment_bottom, s.environmentBottom);
+    }
+};
+
+// FNV-1a over the scene's sizes and a few samples of its arrays: detects a
+// new snapshot placed at the same address.
+uint64_t Signature(const Scene& s) {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+    };
+    const size_t counts[4] = {s.materials.size(), s.meshes.size(), s.distantLights.size(), s.domeLights.size()};
+    mix(counts, sizeof(counts));
+    for (const TriangleMesh& m : s.meshes) {
+        const size_t c[3] = {m.positions.size(), m.normals.size(), m.indices.size()};
+        mix(c, sizeof(c));
+        if (!m.positions.empty()) {
+            mix(&m.positions.front(), sizeof(Vec3f));
+            mix(&m.positions.back(), sizeof(Vec3f));
+        }
+    }
+    for (const PbrMaterial& m : s.materials) mix(&m, sizeof(PbrMaterial) - 4);
+    for (const DomeLight& d : s.domeLights) {
+        const void* env = d.environment.get();
+        mix(&env, sizeof(env));
+        mix(&d.radiance, sizeof(Vec3f));
+    }
+    return h;
+}
+
+ShiroRenderDesc ToRequest(const RenderRequest& r) {
+    ShiroRenderDesc d{};
+    Put3(d.camera.position, r.camera.position);
+    Put3(d.camera.forward, r.camera.forward);
+    Put3(d.camera.right, r.camera.right);
+    Put3(d.camera.up, r.camera.up);
+    d.camera.vertical_fov_degrees = r.camera.verticalFovDegrees;
+    d.camera.aspect_ratio = r.camera.aspectRatio;
+    const RenderSettings& s = r.settings;
+    d.settings = ShiroSettingsDesc{s.width, s.height, s.samplesPerPixel, s.samplesPerUpdate, s.domeLightSamples,
+                                   s.maxDepth, s.diffuseDepth, s.specularDepth, s.threadLimit, s.maxSubdivLevel,
+                                   static_cast<uint32_t>(s.backend), s.backgroundVisible ? 1u : 0u,
+                                   s.enableHeadlight ? 1u : 0u, s.enableCaustics ? 1u : 0u, s.enableSss ? 1u : 0u};
+    d.sample_start = r.sampleStart;
+    d.sample_count = r.sampleCount;
+    return d;
+}
+
+struct Planes {
+    std::vector<float> beauty, albedo, normal, depth;
+    explicit Planes(size_t n) : beauty(4 * n), albedo(3 * n), normal(3 * n), depth(n) {}
+    ShiroAovs Aovs() { return ShiroAovs{beauty.data(), albedo.data(), normal.data(), depth.data(), 0, 0}; }
+    void CopyTo(FrameBuffer* fb) const {
+        const uint32_t w = fb->Width(), h = fb->Height();
+        for (uint32_t y = 0; y < h; ++y)
+            for (uint32_t x = 0; x < w; ++x) {
+                const size_t i = static_cast<size_t>(y) * w + x;
+                fb->SetBeauty(x, y, {beauty[4 * i], beauty[4 * i + 1], beauty[4 * i + 2], beauty[4 * i + 3]});
+                fb->SetAlbedo(x, y, {albedo[3 * i], albedo[3 * i + 1], albedo[3 * i + 2]});
+                fb->SetNormal(x, y, {normal[3 * i], normal[3 * i + 1], normal[3 * i + 2]});
+                fb->SetDepth(x, y, depth[i]);
+            }
+    }
+};
+
+bool Cancelled(const std::atomic<bool>* c) { return c && c->load(std::memory_order_relaxed); }
+
+}  // namespace
+
+GpuBackend::GpuBackend(int device) : device_(device) {}
+
+GpuBackend::~GpuBackend() {
+    if (ctx_) shiro_gpu_destroy(ctx_);
+}
+
+BackendStatus GpuBackend::GetStatus() const {
+    BackendStatus status;
+    status.kind = render::BackendKind::Gpu;
+    status.name = "gb300";
+    status.usesGpu = true;
+    ShiroBackendStatus s;
+    status.available = shiro_gpu_status(&s) == SHIRO_OK && s.available != 0;
+    std::scoped_lock lock(mutex_);
+    if (runtimeAttempted_ && runtimeFailed_) status.available = false;
+    return status;
+}
+
+bool GpuBackend::SupportsScene(const render::Scene& scene) const {
+    SceneView view(scene);
+    return shiro_gpu_supports_scene(&view.desc, nullptr, 0) != 0;
+}
+
+bool GpuBackend::EnsureRuntime(const render::Scene& scene) const {
+    runtimeAttempted_ = true;
+    if (!ctx_) {
+        if (shiro_gpu_create(device_, &ctx_) != SHIRO_OK) {
+            std::fprintf(stderr, "[shiro gb300] context creation failed: %s\n", shiro_gpu_last_error(nullptr));
+            runtimeFailed_ = true;
+            ctx_ = nullptr;
+            return false;
+        }
+    }
+    const uint64_t sig = Signature(scene);
+    if (cachedScene_ != &scene || cachedSignature_ != sig) {
+        SceneView view(scene);
+        if (shiro_gpu_upload_scene(ctx_, &view.desc) != SHIRO_OK) {
+            std::fprintf(stderr, "[shiro gb300] scene upload failed: %s\n", shiro_gpu_last_error(ctx_));
+            cachedScene_ = nullptr;
+            return false;
+        }
+        cachedScene_ = &scene;
+        cachedSignature_ = sig;
+    }
+    return true;
+}
+
+render::FrameBuffer GpuBackend::RenderSampleBatch(const RenderRequest& request) const {
+    render::FrameBuffer frame;
+    frame.Resize(request.settings.width, request.settings.height);
+    frame.Clear();
+    if (request.sampleCount == 0 || Cancelled(request.cancel)) return frame;
+    std::scoped_lock lock(mutex_);
+    if (!EnsureRuntime(request.scene)) return frame;
+    const ShiroRenderDesc desc = ToRequest(request);
+    Planes planes(static_cast<size_t>(request.settings.width) * request.settings.height);
+    ShiroAovs aovs = planes.Aovs();
+    const int rc = shiro_gpu_render(ctx_, &desc, nullptr, &aovs);
+    if (rc != SHIRO_OK) {
+        std::fprintf(stderr, "[shiro gb300] render failed (%d): %s\n", rc, shiro_gpu_last_error(ctx_));
+        return frame;
+    }
+    if (Cancelled(request.cancel)) return frame;
+    planes.CopyTo(&frame);
+    return frame;
+}
+
+std::vector<render::FrameBuffer> GpuBackend::RenderSampleBatches(const std::vector<RenderRequest>& requests) const {
+    std::vector<render::FrameBuffer> frames(requests.size());
+    for (size_t i = 0; i < requests.size(); ++i) {
+        frames[i].Resize(requests[i].settings.width, requests[i].settings.height);
+        frames[i].Clear();
+    }
+    if (requests.empty()) return frames;
+    for (const RenderRequest& r : requests)
+        if (&r.scene != &requests.front().scene) {
+            std::fprintf(stderr, "[shiro gb300] batched requests must share one scene\n");
+            return frames;
+        }
+    std::scoped_lock lock(mutex_);
+    if (!EnsureRuntime(requests.front().scene)) return frames;
+    std::vector<ShiroRenderDesc> descs;
+    std::vector<Planes> planes;
+    planes.reserve(requests.size());
+    std::vector<ShiroAovs> aovs;
+    for (const RenderRequest& r : requests) {
+        descs.push_back(ToRequest(r));
+        planes.emplace_back(static_cast<size_t>(r.settings.width) * r.settings.height);
+        aovs.push_back(planes.back().Aovs());
+    }
+    const int rc = shiro_gpu_render_batch(ctx_, descs.data(), static_cast<uint32_t>(descs.size()), nullptr, aovs.data());
+    if (rc != SHIRO_OK) {
+        std::fprintf(stderr, "[shiro gb300] batched render failed (%d): %s\n", rc, shiro_gpu_last_error(ctx_));
+        return frames;
+    }
+    for (size_t i = 0; i < requests.size(); ++i) planes[i].CopyTo(&frames[i]);
+    return frames;
+}
+
+}  // namespace shiro::backend::gb300

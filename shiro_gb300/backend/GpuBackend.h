@@ -1,0 +1,52 @@
+// GpuBackend - the GB300 path tracer as a shiro::backend::RenderBackend.
+//
+// Drop-in replacement of backend::optix::OptixBackend
+// (include/shiro/backend/optix/OptixBackend.h:10-27 of ichin0se/Shiro): same
+// public methods (GetStatus, SupportsScene, RenderSampleBatch), same error
+// convention (a failed batch logs to stderr and returns a cleared, sized
+// FrameBuffer; a failed runtime reports available = false, which makes
+// Renderer::Impl::ResolveBackend fall back to the CPU tracer,
+// Renderer.cpp:16-31).  All device work goes through the C ABI of
+// include/shiro_gpu.h.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "shiro/backend/RenderBackend.h"
+
+struct ShiroGpuContext;
+
+namespace shiro::backend::gb300 {
+
+class GpuBackend final : public RenderBackend {
+public:
+    explicit GpuBackend(int device = 0);
+    ~GpuBackend() override;
+
+    GpuBackend(const GpuBackend&) = delete;
+    GpuBackend& operator=(const GpuBackend&) = delete;
+
+    BackendStatus GetStatus() const override;
+    bool SupportsScene(const render::Scene& scene) const;
+    render::FrameBuffer RenderSampleBatch(const RenderRequest& request) const override;
+
+    // Batched wavefront form: several requests against the same scene in one
+    // call (all requests must reference the same Scene object).
+    std::vector<render::FrameBuffer> RenderSampleBatches(const std::vector<RenderRequest>& requests) const;
+
+private:
+    bool EnsureRuntime(const render::Scene& scene) const;
+
+    int device_;
+    mutable std::mutex mutex_;
+    mutable ShiroGpuContext* ctx_ = nullptr;
+    mutable bool runtimeAttempted_ = false;
+    mutable bool runtimeFailed_ = false;
+    mutable const render::Scene* cachedScene_ = nullptr;
+    mutable uint64_t cachedSignature_ = 0;
+};
+
+}  // namespace shiro::backend::gb300
