@@ -324,6 +324,23 @@ int shiro_gpu_trace_rays(ShiroGpuContext* ctx, const float* origins, const float
                          const float* t_max, uint32_t n, uint32_t* prim_out, float* t_out,
                          uint32_t* occluded_out);
 
+/* Render without allocating device memory.  No counterpart in the reference:
+ * this entry point exists for callers that must not allocate device memory
+ * while they render - e.g. a process that hands all device memory to its own
+ * allocator at start-up, or a render loop that must not stall on the
+ * allocator's implicit device synchronisation while other streams run.  It
+ * renders exactly like shiro_gpu_render (same kernels and results) but draws
+ * the per-path scratch from an array reserved in the library's device image
+ * (1 048 576 path records = 48 MiB, held by every device that loads the
+ * library until the process exits) and calls no cudaMalloc / cudaFree.
+ * Rules: the AOV planes must be device pointers (on_device = 1); a request
+ * with sample_count > 1 048 576 is refused (SHIRO_ERR_INVALID_ARGUMENT);
+ * all calls share the array, so calls that overlap on the GPU race and must be
+ * serialised by the caller; the first call on a device looks the array's
+ * address up - make it before any stream capture. */
+int shiro_gpu_render_static(ShiroGpuContext* ctx, const ShiroRenderDesc* request, const volatile int* cancel,
+                            ShiroAovs* out);
+
 /* Statistics of the last render (for the roofline and tests). */
 typedef struct ShiroRenderStats {
     double kernel_ms;           /* device time of all kernels of the last call */
