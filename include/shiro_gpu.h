@@ -311,6 +311,15 @@ int shiro_gpu_set_params(ShiroGpuContext* ctx, const float* base_color, const fl
 int shiro_gpu_adjoint(ShiroGpuContext* ctx, const ShiroRenderDesc* request, const float* d_beauty,
                       float* d_base_color, float* d_roughness, float* d_metallic, float* d_env_rgb);
 
+/* Frozen-sampling forward of the differentiable form: renders the beauty
+ * plane (device pointer, 4 floats per pixel) with every sampling decision,
+ * pdf and MIS weight taken from the uploaded scene's parameters and the BSDF
+ * values / dome-0 radiance taken from the given parameter arrays (device
+ * pointers, NULL = the scene's own).  Central finite differences of this
+ * render are exactly the derivative shiro_gpu_adjoint estimates. */
+int shiro_gpu_render_frozen(ShiroGpuContext* ctx, const ShiroRenderDesc* request, const float* base_color,
+                            const float* roughness, const float* metallic, const float* env_rgb, float* beauty);
+
 /* Per-path debugging / parity probes (device or host arrays per on_device).
  * Primary closest hit of every pixel's camera ray for sample sample_start:
  * prim_out[i] = global triangle index (meshes in order, triangles in order)

@@ -1,0 +1,48 @@
+"""torch.autograd binding of the differentiable form.
+
+``render(backend, camera, settings, base_color, roughness, metallic, env)``
+returns the beauty image [H, W, 4] as a differentiable function of the
+per-material base colour [M, 3], roughness [M], metalness [M] and the texels
+[H_env, W_env, 3] of dome light 0.  The forward renders with the plain GPU form
+after writing the parameters into the resident scene; the backward runs the
+adjoint path-replay kernel (shiro_gpu_adjoint), which recomputes every path
+from its QMC seed instead of storing it.
+"""
+from __future__ import annotations
+
+import torch
+
+from .abi import Camera, RenderSettings
+
+
+class _Render(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, base_color, roughness, metallic, env, backend, camera, settings, sample_start, flags):
+        tensors = [t.detach().contiguous().float() if t is not None else None
+                   for t in (base_color, roughness, metallic, env)]
+        backend.set_params(*tensors)
+        beauty = backend.render_device(camera, settings, sample_start, settings.samples_per_pixel, flags)
+        ctx.backend = backend
+        ctx.camera = camera
+        ctx.settings = settings
+        ctx.sample_start = sample_start
+        ctx.flags = flags
+        ctx.shapes = [None if t is None else t.shape for t in (base_color, roughness, metallic, env)]
+        return beauty
+
+    @staticmethod
+    def backward(ctx, d_beauty):
+        grads = {}
+        names = ("base_color", "roughness", "metallic", "env")
+        for name, shape, need in zip(names, ctx.shapes, ctx.needs_input_grad[:4]):
+            if shape is not None and need:
+                grads[name] = torch.zeros(shape, dtype=torch.float32, device="cuda")
+        ctx.backend.adjoint(ctx.camera, ctx.settings, d_beauty.contiguous().float(), grads, ctx.sample_start,
+                            ctx.settings.samples_per_pixel, ctx.flags)
+        return tuple(grads.get(n) for n in names) + (None, None, None, None, None)
+
+
+def render(backend, camera: Camera, settings: RenderSettings, base_color, roughness, metallic, env=None,
+           sample_start: int = 0, flags: int = 0):
+    """Differentiable render of the backend's uploaded scene (see module doc)."""
+    return _Render.apply(base_color, roughness, metallic, env, backend, camera, settings, sample_start, flags)

@@ -71,6 +71,7 @@ def load_library(path: str = LIB_PATH):
         "shiro_gpu_trace_rays": ([_P, _P, _P, _P, _U, _P, _P, _P], C.c_int),
         "shiro_gpu_last_stats": ([_P, _P], C.c_int),
         "shiro_gpu_count_work": ([_P, _P, _U, _P], C.c_int),
+        "shiro_gpu_render_frozen": ([_P, _P, _P, _P, _P, _P, _P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -274,6 +275,71 @@ class GpuBackend:
         if rc != 0:
             raise self._err(rc)
         return {k: getattr(wc, k) for k, _ in WorkCounts._fields_}
+
+    # -- differentiable form -------------------------------------------------
+    @staticmethod
+    def _dptr(t):
+        """Device pointer of a contiguous float32 CUDA tensor (None -> NULL)."""
+        if t is None:
+            return None
+        if not (t.is_cuda and t.dtype.is_floating_point and t.is_contiguous()):
+            raise ValueError("expected a contiguous float32 CUDA tensor")
+        return C.c_void_p(t.data_ptr())
+
+    def set_params(self, base_color=None, roughness=None, metallic=None, env=None):
+        """Overwrites the uploaded scene's base colour [M,3], roughness [M],
+        metalness [M] and dome-0 texels [H,W,3] (CUDA float32 tensors)."""
+        rc = self.lib.shiro_gpu_set_params(self._ctx, self._dptr(base_color), self._dptr(roughness),
+                                           self._dptr(metallic), self._dptr(env))
+        if rc != 0:
+            raise self._err(rc)
+
+    def render_device(self, camera: Camera, settings: RenderSettings, sample_start: int = 0,
+                      sample_count: Optional[int] = None, flags: int = 0, wavefront: bool = False):
+        """Renders the uploaded scene into CUDA tensors; returns beauty [H,W,4]."""
+        import torch
+
+        from .abi import Aovs
+
+        count = settings.samples_per_pixel if sample_count is None else sample_count
+        n = settings.width * settings.height
+        planes = [torch.empty(n * c, dtype=torch.float32, device="cuda") for c in (4, 3, 3, 1)]
+        aovs = Aovs(*[C.cast(C.c_void_p(p.data_ptr()), C.POINTER(C.c_float)) for p in planes], 1, 0)
+        req = render_desc(camera, settings, sample_start, count, flags)
+        if wavefront:
+            rc = self.lib.shiro_gpu_render_batch(self._ctx, C.byref(req), 1, None, C.byref(aovs))
+        else:
+            rc = self.lib.shiro_gpu_render(self._ctx, C.byref(req), None, C.byref(aovs))
+        if rc != 0:
+            raise self._err(rc)
+        return planes[0].view(settings.height, settings.width, 4)
+
+    def adjoint(self, camera: Camera, settings: RenderSettings, d_beauty, grads: dict, sample_start: int = 0,
+                sample_count: Optional[int] = None, flags: int = 0):
+        """Adds d(sum d_beauty . beauty)/d(params) into grads['base_color'],
+        ['roughness'], ['metallic'], ['env'] (CUDA float32 tensors)."""
+        count = settings.samples_per_pixel if sample_count is None else sample_count
+        req = render_desc(camera, settings, sample_start, count, flags)
+        rc = self.lib.shiro_gpu_adjoint(self._ctx, C.byref(req), self._dptr(d_beauty.contiguous()),
+                                        self._dptr(grads.get("base_color")), self._dptr(grads.get("roughness")),
+                                        self._dptr(grads.get("metallic")), self._dptr(grads.get("env")))
+        if rc != 0:
+            raise self._err(rc)
+
+    def render_frozen(self, camera: Camera, settings: RenderSettings, base_color=None, roughness=None, metallic=None,
+                      env=None, sample_start: int = 0, sample_count: Optional[int] = None, flags: int = 0):
+        """Beauty with sampling from the scene's parameters and values from the
+        given ones (the quantity whose finite differences the adjoint estimates)."""
+        import torch
+
+        count = settings.samples_per_pixel if sample_count is None else sample_count
+        out = torch.empty(settings.height * settings.width * 4, dtype=torch.float32, device="cuda")
+        req = render_desc(camera, settings, sample_start, count, flags)
+        rc = self.lib.shiro_gpu_render_frozen(self._ctx, C.byref(req), self._dptr(base_color), self._dptr(roughness),
+                                              self._dptr(metallic), self._dptr(env), C.c_void_p(out.data_ptr()))
+        if rc != 0:
+            raise self._err(rc)
+        return out.view(settings.height, settings.width, 4)
 
     def last_stats(self) -> dict:
         s = RenderStats()

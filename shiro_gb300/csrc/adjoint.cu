@@ -1,14 +1,538 @@
-// adjoint.cu - differentiable form (placeholder until implemented).
+// adjoint.cu - the differentiable form (no counterpart in the reference).
+//
+// Gradients of an image loss with respect to per-material base colour,
+// specular roughness and metalness and to the texels of dome light 0's
+// environment map, by path replay: every path is recomputed from its QMC
+// seed twice - once for its radiance L, once to push the adjoint radiance
+// dL/dL_path = d_beauty(pixel) / spp into the parameters - so no path
+// vertex is stored.
+//
+// Estimator: the one of integrator.cuh (same sample dimensions, lobe
+// choice, MIS, clamps, Russian roulette).  Sampling decisions, pdfs, MIS
+// weights, Russian-roulette probabilities and clamp scales are held constant
+// (detached); the parameters enter through the BSDF values (continuation and
+// light samples) and the environment radiance (light samples and misses):
+//   * a light sample's contribution c = s * f * L * w  contributes
+//     delta * T * s * (df * L * w + f * dL * w);
+//   * a continuation BSDF value f_k scales every later contribution, which
+//     is the radiance not yet accounted for, L_rem: delta * L_rem * df_k / f_k;
+//   * a miss adds delta * T * mis * dL_env.
+// BSDF derivatives come from bsdf_eval_d (forward-mode dual numbers).
+//
+// shiro_gpu_render_frozen evaluates the same estimator with the sampling
+// taken from the scene's parameters and the BSDF / environment values from a
+// second parameter set; its central finite differences are exactly the
+// quantity the adjoint computes, which is how the adjoint is checked.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "bsdf_diff.cuh"
 #include "context.h"
+#include "integrator.cuh"
 
 namespace shiro_gpu {
 
-int adjoint_run(ContextImpl* ctx, const ShiroRenderDesc*, const float*, float*, float*, float*, float*) {
-    return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "adjoint form not built");
+namespace {
+
+struct AdjView {
+    const Mat* evalMats;  // BSDF values (= scene materials except for frozen renders)
+    DevEnv evalEnv;       // dome 0's environment for radiance values
+    int32_t env0;         // env index of dome 0, -1 if it has none
+    uint32_t materialCount;
+    const float* dBeauty;  // 4 per pixel
+    float* dBase;          // 3 per material
+    float* dRough;
+    float* dMetal;
+    float* dEnv;  // 3 per texel of env0
+    uint32_t useShared;
+};
+
+__device__ __forceinline__ const DevEnv& env_for_eval(const DevScene& s, const AdjView& a, int32_t env) {
+    return env == a.env0 ? a.evalEnv : s.envs[env];
 }
-int adjoint_set_params(ContextImpl* ctx, const float*, const float*, const float*, const float*) {
-    return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "adjoint form not built");
+
+// Texels and weights of the bilinear lookup env_evaluate makes for `local`
+// (EvaluateLatLong / EvaluateAngular + BilinearSample).
+__device__ __forceinline__ int env_footprint(const DevEnv& e, const V3& local, uint32_t idx[4], float wgt[4]) {
+    if (e.w == 0 || e.h == 0) return 0;
+    const V3 d = normalize(local);
+    float u, v;
+    if (!e.latlong) {
+        const float rl = sqrtf(d.x * d.x + d.y * d.y);
+        if (rl <= 1.0e-6f) {
+            u = 0.5f;
+            v = 0.5f;
+        } else {
+            const float angle = acosf(sclamp(d.z, -1.0f, 1.0f));
+            const float radius = angle / kPi;
+            u = 0.5f + 0.5f * radius * (d.x / rl);
+            v = 0.5f + 0.5f * radius * (d.y / rl);
+            if (u < 0.0f || u > 1.0f || v < 0.0f || v > 1.0f) return 0;
+        }
+    } else {
+        const float phi = atan2f(d.x, d.z);
+        const float theta = acosf(sclamp(d.y, -1.0f, 1.0f));
+        u = env_wrap(phi / kTwoPi);
+        v = sclamp(theta / kPi, 0.0f, 1.0f);
+    }
+    u = env_wrap(u) * static_cast<float>(e.w) - 0.5f;
+    v = sclamp(v, 0.0f, 1.0f) * static_cast<float>(e.h) - 0.5f;
+    const int x0 = static_cast<int>(floorf(u));
+    const int y0 = static_cast<int>(floorf(v));
+    const int x1 = x0 + 1;
+    const int y1 = min(y0 + 1, static_cast<int>(e.h) - 1);
+    const float tx = u - static_cast<float>(x0);
+    const float ty = v - static_cast<float>(y0);
+    const int xs[4] = {x0, x1, x0, x1}, ys[4] = {y0, y0, y1, y1};
+    const float ws[4] = {(1.0f - tx) * (1.0f - ty), tx * (1.0f - ty), (1.0f - tx) * ty, tx * ty};
+    for (int k = 0; k < 4; ++k) {
+        int xx = xs[k] % static_cast<int>(e.w);
+        if (xx < 0) xx += static_cast<int>(e.w);
+        const int yy = ys[k] < 0 ? 0 : (ys[k] > static_cast<int>(e.h) - 1 ? static_cast<int>(e.h) - 1 : ys[k]);
+        idx[k] = static_cast<uint32_t>(yy) * e.w + static_cast<uint32_t>(xx);
+        wgt[k] = ws[k];
+    }
+    return 4;
 }
-void adjoint_free(ContextImpl*) {}
+
+__device__ __forceinline__ void add_env_grad(const AdjView& a, const DevEnv& e, const V3& local, const V3& coef) {
+    if (!a.dEnv || (coef.x == 0.0f && coef.y == 0.0f && coef.z == 0.0f)) return;
+    uint32_t idx[4];
+    float w[4];
+    const int n = env_footprint(e, local, idx, w);
+    for (int k = 0; k < n; ++k) {
+        if (w[k] == 0.0f) continue;
+        atomicAdd(&a.dEnv[3 * static_cast<size_t>(idx[k])], coef.x * w[k]);
+        atomicAdd(&a.dEnv[3 * static_cast<size_t>(idx[k]) + 1], coef.y * w[k]);
+        atomicAdd(&a.dEnv[3 * static_cast<size_t>(idx[k]) + 2], coef.z * w[k]);
+    }
+}
+
+// dL/dparams of material `mat` += sum_c coef_c * df_c (df from the duals).
+__device__ __forceinline__ void add_mat_grad(const AdjView& a, float* smem, uint32_t mat, const DV3& f, const V3& coef) {
+    if (mat >= a.materialCount) return;
+    float g[kDualN];
+#pragma unroll
+    for (int p = 0; p < kDualN; ++p) g[p] = coef.x * f.x.d[p] + coef.y * f.y.d[p] + coef.z * f.z.d[p];
+    if (a.useShared) {
+        float* m = smem + 5 * mat;
+#pragma unroll
+        for (int p = 0; p < kDualN; ++p)
+            if (g[p] != 0.0f) atomicAdd(&m[p], g[p]);
+    } else {
+        if (a.dBase) {
+            for (int c = 0; c < 3; ++c)
+                if (g[c] != 0.0f) atomicAdd(&a.dBase[3 * mat + c], g[c]);
+        }
+        if (a.dRough && g[kDRough] != 0.0f) atomicAdd(&a.dRough[mat], g[kDRough]);
+        if (a.dMetal && g[kDMetal] != 0.0f) atomicAdd(&a.dMetal[mat], g[kDMetal]);
+    }
+}
+
+__device__ __forceinline__ float clamp_scale(const DevRequest& q, const V3& v, float mx) {
+    if (q.flags & SHIRO_RENDER_NO_CLAMP) return 1.0f;
+    const float c = maxc(v);
+    if (c <= mx || c <= 0.0f) return 1.0f;
+    return mx / c;
+}
+
+// Environment radiance of a miss with dome 0 evaluated from the eval texels.
+__device__ __forceinline__ V3 env_radiance_eval(const DevScene& s, const AdjView& a, const V3& dir) {
+    if (s.domeCount > 0) {
+        V3 r{0.0f, 0.0f, 0.0f};
+        for (uint32_t i = 0; i < s.domeCount; ++i) {
+            const DevDome& d = s.domes[i];
+            r = r + (d.env >= 0 ? env_evaluate(env_for_eval(s, a, d.env), world_to_light(d, dir)) * d.radiance : d.radiance);
+        }
+        return r;
+    }
+    const float t = sclamp(dir.y * 0.5f + 0.5f, 0.0f, 1.0f);
+    return lerp(s.envBottom, s.envTop, t);
+}
+
+// One path of the estimator with sampling from the scene and values from
+// (a.evalMats, a.evalEnv).  kGrad = false returns the radiance; kGrad = true
+// replays it and accumulates the gradients of delta . radiance, given the
+// path's total radiance Ltot.
+template <bool kGrad>
+__device__ V3 adj_path(const DevScene& s, const DevRequest& q, const AdjView& a, float* smem, uint32_t x, uint32_t y,
+                       uint32_t sampleIndex, const V3& delta, const V3& Ltot, float* depthOut) {
+    NullCounter ctr;
+    const Sampler smp{x, y, sampleIndex};
+    PathState ps;
+    init_path(q, smp, ps);
+    V3 Lrem = Ltot;
+    float depth0 = __int_as_float(0x7f800000);
+    const bool useCdf = (q.flags & SHIRO_RENDER_ENV_CDF) != 0u;
+    for (uint32_t depth = 0; depth < q.maxDepth; ++depth) {
+        HitRec h;
+        if (!trace_closest(s, ps.ro, ps.rd, &h, ctr)) {
+            if (depth > 0 || q.backgroundVisible) {
+                const V3 env = env_radiance_eval(s, a, ps.rd);
+                float mis = 1.0f;
+                if (s.domeCount == 0 || depth == 0 || ps.prevDelta) {
+                    ps.radiance = ps.radiance + ps.T * env;
+                } else {
+                    mis = env_miss_mis(s, ps.prevPdf, ps.rd);
+                    ps.radiance = ps.radiance + ps.T * env * mis;
+                }
+                if (kGrad && a.env0 >= 0) {
+                    for (uint32_t i = 0; i < s.domeCount; ++i) {
+                        const DevDome& d = s.domes[i];
+                        if (d.env != a.env0) continue;
+                        const V3 coef = delta * ps.T * d.radiance * mis;
+                        add_env_grad(a, a.evalEnv, world_to_light(d, ps.rd), coef);
+                    }
+                }
+            }
+            break;
+        }
+        const Vertex v = make_vertex(s, ps.ro, ps.rd, h);
+        const Mat& me = a.evalMats[v.hit.material];
+        const Mat& ms = s.materials[v.hit.material];
+        if (depth == 0) depth0 = h.t;
+        const V3 origin = shadow_origin(v);
+        // light samples, in sum_direct's order
+        const V3 dT = delta * ps.T;
+        const V3 direct = sum_direct(s, q, [&](uint32_t k, V3* c) {
+            V3 ld, L;
+            float w;
+            int32_t envIdx = -1;
+            V3 local{0.0f, 0.0f, 0.0f};
+            V3 domeRad{0.0f, 0.0f, 0.0f};
+            if (k < s.distantCount) {
+                const DevDistant l = s.distant[k];
+                ld = normalize(l.direction * -1.0f);
+                const float nl = sclamp(dot(v.n, ld), 0.0f, 1.0f);
+                if (nl <= 0.0f) return false;
+                L = l.radiance;
+                w = nl;
+            } else {
+                const uint32_t r = k - s.distantCount;
+                const uint32_t li = r / q.domeSamples, j = r - li * q.domeSamples;
+                const DevDome& d = s.domes[li];
+                const uint32_t dim = kDirectDimBase + depth * kDirectDepthStride + li * kDirectLightStride + j * kDirectSampleStride;
+                const V2 u = smp.next2d(dim);
+                float lp;
+                if (d.env >= 0) {
+                    env_sample(s.envs[d.env], u, useCdf, &local, &lp);
+                    if (lp <= 0.0f) return false;
+                    L = env_evaluate(env_for_eval(s, a, d.env), local) * d.radiance;
+                    envIdx = d.env;
+                    domeRad = d.radiance;
+                } else {
+                    const float yy = 1.0f - 2.0f * u.y;
+                    const float rr = sqrtf(smax(0.0f, 1.0f - yy * yy));
+                    const float phi = 2.0f * kPi * u.x;
+                    local = V3{sinf(phi) * rr, yy, cosf(phi) * rr};
+                    lp = kInvFourPi;
+                    L = V3{1.0f, 1.0f, 1.0f} * d.radiance;
+                }
+                ld = light_to_world(d, local);
+                const float nl = sclamp(dot(v.n, ld), 0.0f, 1.0f);
+                if (nl <= 0.0f) return false;
+                const float bp = bsdf_pdf(ms, v.w, v.n, v.cn, v.view, ld);
+                const float mis = power_heuristic(lp, bp);
+                w = nl * mis / lp;
+            }
+            if (trace_occluded(s, origin, ld, FLT_MAX, ctr)) return false;
+            const V3 f = bsdf_eval(me, v.n, v.cn, v.view, ld);
+            const V3 raw = f * L * w;
+            *c = clamp24(q, raw);
+            if (kGrad) {
+                const float sc = clamp_scale(q, raw, kDirectSampleClamp);
+                const DV3 fd = bsdf_eval_d(me, v.n, v.cn, v.view, ld);
+                add_mat_grad(a, smem, v.hit.material, fd, dT * L * (w * sc));
+                if (envIdx >= 0 && envIdx == a.env0) add_env_grad(a, a.evalEnv, local, dT * f * domeRad * (w * sc));
+            }
+            return true;
+        });
+        ps.radiance = ps.radiance + ps.T * direct;
+        if (kGrad) Lrem = Lrem - ps.T * direct;
+        // continuation (continue_path with the BSDF value from the eval material)
+        const uint32_t base = depth * kPathDimStride;
+        const float rw = v.w.diffuse + v.w.spec + v.w.coat;
+        const float tw = rw + 0.0f;
+        if (tw <= 0.0f) break;
+        const float sel = smp.next1d(base + 1u) * tw;
+        const V2 ds = smp.next2d(base + 2u);
+        V3 next, f;
+        float pdf;
+        bool delta2 = false;
+        const float rs = sel - 0.0f;
+        if (rs < v.w.diffuse) {
+            if (ps.diffDepth >= q.diffuseDepth) break;
+            ++ps.diffDepth;
+            next = cosine_hemisphere(v.n, ds);
+            const float cpdf = sclamp(dot(v.n, next), 0.0f, 1.0f) * kInvPi;
+            pdf = smax((rw / tw) * (1.0f * cpdf + 0.0f * 0.0f), 1.0e-6f);
+            f = bsdf_eval(me, v.n, v.cn, v.view, next);
+        } else {
+            const bool coat = !(rs < v.w.diffuse + v.w.spec);
+            if (ps.specDepth >= q.specularDepth) break;
+            ++ps.specDepth;
+            const V3 sn = coat ? v.cn : v.n;
+            const float sr = coat ? roughness_for(ms.coat_roughness, ms.coat_anisotropy, ms.coat_rotation)
+                                  : roughness_for(base_roughness(ms), ms.specular_anisotropy, ms.specular_rotation);
+            const V3 hv = ggx_half(sn, ds, sr);
+            next = normalize(reflect(ps.rd, hv));
+            const float rc = sclamp(dot(sn, next), 0.0f, 1.0f);
+            if (rc <= 0.0f) break;
+            pdf = smax((rw / tw) * bsdf_pdf(ms, v.w, v.n, v.cn, v.view, next), 1.0e-6f);
+            f = bsdf_eval(me, v.n, v.cn, v.view, next);
+            delta2 = sr <= kDeltaRoughness;
+        }
+        const float cosT = sclamp(dot(v.n, next), 0.0f, 1.0f);
+        if (cosT <= 0.0f) break;
+        ps.T = clamp12(q, ps.T * f * (cosT / pdf));
+        const float off = dot(v.n, next) >= 0.0f ? 1.0f : -1.0f;
+        ps.ro = v.hit.position + v.n * (kRayEpsilon * off);
+        const V3 prevDir = ps.rd;
+        ps.rd = next;
+        ps.prevDelta = delta2;
+        ps.prevPdf = pdf;
+        bool alive = true;
+        if (depth >= 2) {
+            const float cp = sclamp(maxc(ps.T), 0.05f, 0.95f);
+            if (smp.next1d(base + 4u) > cp) alive = false;
+            else ps.T = ps.T / cp;
+        }
+        if (kGrad && alive && depth + 1u < q.maxDepth) {
+            // every later contribution scales with f (per channel)
+            const DV3 fd = bsdf_eval_d(me, v.n, v.cn, v.view, next);
+            const V3 coef{f.x > 0.0f ? delta.x * Lrem.x / f.x : 0.0f, f.y > 0.0f ? delta.y * Lrem.y / f.y : 0.0f,
+                          f.z > 0.0f ? delta.z * Lrem.z / f.z : 0.0f};
+            add_mat_grad(a, smem, v.hit.material, fd, coef);
+        }
+        (void)prevDir;
+        if (!alive) break;
+    }
+    if (depthOut) *depthOut = depth0;
+    return ps.radiance;
+}
+
+__global__ void __launch_bounds__(128) k_adjoint(const DevScene s, const DevRequest q, const AdjView a, uint64_t pathBase,
+                                                 uint32_t count) {
+    extern __shared__ float smem[];
+    if (a.useShared) {
+        for (uint32_t i = threadIdx.x; i < 5 * a.materialCount; i += blockDim.x) smem[i] = 0.0f;
+        __syncthreads();
+    }
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) {
+        const uint64_t path = pathBase + i;
+        const uint64_t pixel = path / q.sampleCount;
+        const uint32_t smp = static_cast<uint32_t>(path - pixel * q.sampleCount);
+        const uint32_t y = static_cast<uint32_t>(pixel / q.width);
+        const uint32_t x = static_cast<uint32_t>(pixel - static_cast<uint64_t>(y) * q.width);
+        const float cnt = static_cast<float>(q.sampleCount);
+        const float4 g = reinterpret_cast<const float4*>(a.dBeauty)[pixel];
+        const V3 delta{g.x / cnt, g.y / cnt, g.z / cnt};
+        if (delta.x != 0.0f || delta.y != 0.0f || delta.z != 0.0f) {
+            const V3 L = adj_path<false>(s, q, a, smem, x, y, q.sampleStart + smp, delta, V3{0, 0, 0}, nullptr);
+            adj_path<true>(s, q, a, smem, x, y, q.sampleStart + smp, delta, L, nullptr);
+        }
+    }
+    if (a.useShared) {
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < 5 * a.materialCount; k += blockDim.x) {
+            const float v = smem[k];
+            if (v == 0.0f) continue;
+            const uint32_t mat = k / 5, p = k - mat * 5;
+            if (p < 3) {
+                if (a.dBase) atomicAdd(&a.dBase[3 * mat + p], v);
+            } else if (p == 3) {
+                if (a.dRough) atomicAdd(&a.dRough[mat], v);
+            } else if (a.dMetal) {
+                atomicAdd(&a.dMetal[mat], v);
+            }
+        }
+    }
+}
+
+// Frozen-sampling forward: radiance + first-hit depth per path as a record.
+__global__ void __launch_bounds__(128) k_frozen(const DevScene s, const DevRequest q, const AdjView a, uint64_t pathBase,
+                                                uint32_t count, float4* __restrict__ records) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const uint64_t path = pathBase + i;
+    const uint64_t pixel = path / q.sampleCount;
+    const uint32_t smp = static_cast<uint32_t>(path - pixel * q.sampleCount);
+    const uint32_t y = static_cast<uint32_t>(pixel / q.width);
+    const uint32_t x = static_cast<uint32_t>(pixel - static_cast<uint64_t>(y) * q.width);
+    float depth0;
+    const V3 L = adj_path<false>(s, q, a, nullptr, x, y, q.sampleStart + smp, V3{0, 0, 0}, V3{0, 0, 0}, &depth0);
+    float4* o = records + 3 * static_cast<size_t>(i);
+    o[0] = make_float4(L.x, L.y, L.z, depth0);
+    o[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    o[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+__global__ void k_scatter_params(Mat* mats, uint32_t n, const float* base, const float* rough, const float* metal) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (base) {
+        mats[i].base_color[0] = base[3 * i];
+        mats[i].base_color[1] = base[3 * i + 1];
+        mats[i].base_color[2] = base[3 * i + 2];
+    }
+    if (rough) mats[i].roughness = rough[i];
+    if (metal) mats[i].metallic = metal[i];
+}
+
+__global__ void k_rgb_to_texels(const float* rgb, float4* tex, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    tex[i] = make_float4(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], 0.0f);
+}
+
+inline unsigned grid(uint64_t n, unsigned b) { return static_cast<unsigned>((n + b - 1) / b); }
+
+}  // namespace
+
+struct AdjointState {
+    DeviceBlock evalMats, evalTexels;
+};
+
+namespace {
+
+AdjointState* adj_state(ContextImpl* ctx) {
+    if (!ctx->adjoint) ctx->adjoint = new AdjointState();
+    return ctx->adjoint;
+}
+
+int32_t dome0_env(const ContextImpl* ctx) { return ctx->domeEnv.empty() ? -1 : ctx->domeEnv[0]; }
+
+AdjView base_view(ContextImpl* ctx) {
+    AdjView a{};
+    a.evalMats = ctx->scene.materials;
+    a.env0 = dome0_env(ctx);
+    if (a.env0 >= 0) a.evalEnv = ctx->envDev[a.env0];
+    a.materialCount = ctx->materialCount;
+    return a;
+}
+
+}  // namespace
+
+int adjoint_set_params(ContextImpl* ctx, const float* base, const float* rough, const float* metal, const float* env) {
+    if (!ctx->hasScene) return fail(ctx, SHIRO_ERR_NO_SCENE, "no scene uploaded");
+    if ((base || rough || metal) && ctx->materialCount) {
+        k_scatter_params<<<grid(ctx->materialCount, 128), 128, 0, ctx->stream>>>(
+            const_cast<Mat*>(ctx->scene.materials), ctx->materialCount, base, rough, metal);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "set material params");
+    }
+    if (env) {
+        const int32_t e0 = dome0_env(ctx);
+        if (e0 < 0) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "dome light 0 has no environment texture");
+        EnvHost& eh = ctx->envHost[e0];
+        cudaError_t e = cudaMemcpyAsync(eh.rgb.data(), env, eh.rgb.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "read env params");
+        const int rc = upload_envs(ctx);  // texels + rebuilt importance table
+        if (rc != SHIRO_OK) return rc;
+    }
+    const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? SHIRO_OK : cuda_fail(ctx, e, "set params");
+}
+
+int adjoint_run(ContextImpl* ctx, const ShiroRenderDesc* req, const float* dBeauty, float* dBase, float* dRough, float* dMetal,
+                float* dEnv) {
+    int rc = validate_request(ctx, *req);
+    if (rc != SHIRO_OK) return rc;
+    const DevRequest q = make_request(*req);
+    AdjView a = base_view(ctx);
+    a.dBeauty = dBeauty;
+    a.dBase = dBase;
+    a.dRough = dRough;
+    a.dMetal = dMetal;
+    a.dEnv = a.env0 >= 0 ? dEnv : nullptr;
+    const size_t shared = 5ull * a.materialCount * sizeof(float);
+    a.useShared = (shared > 0 && shared <= 32 * 1024) ? 1u : 0u;
+    const uint64_t total = static_cast<uint64_t>(q.width) * q.height * q.sampleCount;
+    const uint64_t chunk = 1ull << 24;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, ctx->stream);
+    uint64_t launches = 0;
+    for (uint64_t p0 = 0; p0 < total; p0 += chunk) {
+        const uint32_t n = static_cast<uint32_t>(std::min(chunk, total - p0));
+        k_adjoint<<<grid(n, 128), 128, a.useShared ? shared : 0, ctx->stream>>>(ctx->scene, q, a, p0, n);
+        ++launches;
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return cuda_fail(ctx, e, "adjoint launch");
+        }
+    }
+    cudaEventRecord(e1, ctx->stream);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "adjoint");
+    ctx->stats.kernel_ms = ms;
+    ctx->stats.path_kernel_ms = ms;
+    ctx->stats.path_kernel_launches = launches;
+    ctx->stats.kernel_launches = launches;
+    ctx->stats.paths = total;
+    return check_device_error(ctx);
+}
+
+void adjoint_free(ContextImpl* ctx) {
+    if (!ctx->adjoint) return;
+    for (DeviceBlock* b : {&ctx->adjoint->evalMats, &ctx->adjoint->evalTexels})
+        if (b->ptr) cudaFree(b->ptr);
+    delete ctx->adjoint;
+    ctx->adjoint = nullptr;
+}
+
+int adjoint_render_frozen(ContextImpl* ctx, const ShiroRenderDesc* req, const float* base, const float* rough,
+                          const float* metal, const float* env, float* beauty) {
+    int rc = validate_request(ctx, *req);
+    if (rc != SHIRO_OK) return rc;
+    AdjointState* st = adj_state(ctx);
+    const DevRequest q = make_request(*req);
+    AdjView a = base_view(ctx);
+    const uint32_t nm = ctx->materialCount + 1;
+    if (!ensure_block(ctx, &st->evalMats, nm * sizeof(Mat), "eval materials")) return SHIRO_ERR_OUT_OF_MEMORY;
+    Mat* em = static_cast<Mat*>(st->evalMats.ptr);
+    cudaError_t e = cudaMemcpyAsync(em, ctx->scene.materials, nm * sizeof(Mat), cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "eval materials");
+    if ((base || rough || metal) && ctx->materialCount)
+        k_scatter_params<<<grid(ctx->materialCount, 128), 128, 0, ctx->stream>>>(em, ctx->materialCount, base, rough, metal);
+    a.evalMats = em;
+    if (env && a.env0 >= 0) {
+        const uint32_t n = a.evalEnv.w * a.evalEnv.h;
+        if (!ensure_block(ctx, &st->evalTexels, std::max<size_t>(n, 1) * sizeof(float4), "eval texels"))
+            return SHIRO_ERR_OUT_OF_MEMORY;
+        k_rgb_to_texels<<<grid(n, 256), 256, 0, ctx->stream>>>(env, static_cast<float4*>(st->evalTexels.ptr), n);
+        a.evalEnv.texels = static_cast<const float4*>(st->evalTexels.ptr);
+    }
+    const uint64_t pixels = static_cast<uint64_t>(q.width) * q.height;
+    if (q.sampleCount == 0 || pixels == 0) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "empty request");
+    const uint64_t pixelsPerChunk = std::max<uint64_t>(1, (1ull << 24) / q.sampleCount);
+    const uint64_t recBytes = std::min<uint64_t>(pixelsPerChunk, pixels) * q.sampleCount * kPathRecordBytes;
+    if (!ensure_block(ctx, &ctx->pathRecords, recBytes, "path records")) return SHIRO_ERR_OUT_OF_MEMORY;
+    if (!ensure_block(ctx, &ctx->aovScratch, pixels * 11 * sizeof(float), "AOV staging")) return SHIRO_ERR_OUT_OF_MEMORY;
+    float* sc = static_cast<float*>(ctx->aovScratch.ptr);
+    const AovPtrs aov{beauty, sc + 4 * pixels, sc + 7 * pixels, sc + 10 * pixels};
+    float4* rec = static_cast<float4*>(ctx->pathRecords.ptr);
+    for (uint64_t p0 = 0; p0 < pixels; p0 += pixelsPerChunk) {
+        const uint32_t np = static_cast<uint32_t>(std::min(pixelsPerChunk, pixels - p0));
+        const uint32_t paths = np * q.sampleCount;
+        k_frozen<<<grid(paths, 128), 128, 0, ctx->stream>>>(ctx->scene, q, a, p0 * q.sampleCount, paths, rec);
+        launch_resolve_pixels(q, p0, np, rec, aov, ctx->stream);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "frozen render launch");
+    }
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "frozen render");
+    return check_device_error(ctx);
+}
 
 }  // namespace shiro_gpu

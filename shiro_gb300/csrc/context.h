@@ -92,6 +92,8 @@ int adjoint_run(ContextImpl* ctx, const ShiroRenderDesc* req, const float* dBeau
                 float* dMetal, float* dEnv);
 int adjoint_set_params(ContextImpl* ctx, const float* base, const float* rough, const float* metal, const float* env);
 void adjoint_free(ContextImpl* ctx);
+int adjoint_render_frozen(ContextImpl* ctx, const ShiroRenderDesc* req, const float* base, const float* rough,
+                          const float* metal, const float* env, float* beauty);
 
 }  // namespace shiro_gpu
 

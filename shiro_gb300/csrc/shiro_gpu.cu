@@ -836,6 +836,13 @@ int shiro_gpu_adjoint(ShiroGpuContext* ctx, const ShiroRenderDesc* req, const fl
     return adjoint_run(&ctx->impl, req, dBeauty, dBase, dRough, dMetal, dEnv);
 }
 
+int shiro_gpu_render_frozen(ShiroGpuContext* ctx, const ShiroRenderDesc* req, const float* base, const float* rough,
+                            const float* metal, const float* env, float* beauty) {
+    if (!ctx || !req || !beauty) return SHIRO_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->impl.device);
+    return adjoint_render_frozen(&ctx->impl, req, base, rough, metal, env, beauty);
+}
+
 int shiro_gpu_primary_hits(ShiroGpuContext* handle, const ShiroRenderDesc* req, uint32_t* prim, float* t, uint32_t on_device) {
     if (!handle || !req || !prim || !t) return SHIRO_ERR_INVALID_ARGUMENT;
     ContextImpl* ctx = &handle->impl;
