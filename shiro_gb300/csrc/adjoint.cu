@@ -46,6 +46,7 @@ struct AdjView {
     float* dMetal;
     float* dEnv;  // 3 per texel of env0
     uint32_t useShared;
+    uint32_t distinctEval;  // evalMats differ from the scene's: track the sampling throughput too
 };
 
 __device__ __forceinline__ const DevEnv& env_for_eval(const DevScene& s, const AdjView& a, int32_t env) {
@@ -162,6 +163,8 @@ __device__ V3 adj_path(const DevScene& s, const DevRequest& q, const AdjView& a,
     const Sampler smp{x, y, sampleIndex};
     PathState ps;
     init_path(q, smp, ps);
+    // throughput under the sampling parameters: Russian roulette decides on it
+    V3 Ts = ps.T;
     V3 Lrem = Ltot;
     float depth0 = __int_as_float(0x7f800000);
     const bool useCdf = (q.flags & SHIRO_RENDER_ENV_CDF) != 0u;
@@ -285,7 +288,9 @@ __device__ V3 adj_path(const DevScene& s, const DevRequest& q, const AdjView& a,
         }
         const float cosT = sclamp(dot(v.n, next), 0.0f, 1.0f);
         if (cosT <= 0.0f) break;
+        if (a.distinctEval) Ts = clamp12(q, Ts * bsdf_eval(ms, v.n, v.cn, v.view, next) * (cosT / pdf));
         ps.T = clamp12(q, ps.T * f * (cosT / pdf));
+        if (!a.distinctEval) Ts = ps.T;
         const float off = dot(v.n, next) >= 0.0f ? 1.0f : -1.0f;
         ps.ro = v.hit.position + v.n * (kRayEpsilon * off);
         const V3 prevDir = ps.rd;
@@ -294,9 +299,13 @@ __device__ V3 adj_path(const DevScene& s, const DevRequest& q, const AdjView& a,
         ps.prevPdf = pdf;
         bool alive = true;
         if (depth >= 2) {
-            const float cp = sclamp(maxc(ps.T), 0.05f, 0.95f);
-            if (smp.next1d(base + 4u) > cp) alive = false;
-            else ps.T = ps.T / cp;
+            const float cp = sclamp(maxc(Ts), 0.05f, 0.95f);
+            if (smp.next1d(base + 4u) > cp) {
+                alive = false;
+            } else {
+                ps.T = ps.T / cp;
+                Ts = Ts / cp;
+            }
         }
         if (kGrad && alive && depth + 1u < q.maxDepth) {
             // every later contribution scales with f (per channel)
@@ -506,6 +515,7 @@ int adjoint_render_frozen(ContextImpl* ctx, const ShiroRenderDesc* req, const fl
     if ((base || rough || metal) && ctx->materialCount)
         k_scatter_params<<<grid(ctx->materialCount, 128), 128, 0, ctx->stream>>>(em, ctx->materialCount, base, rough, metal);
     a.evalMats = em;
+    a.distinctEval = 1u;
     if (env && a.env0 >= 0) {
         const uint32_t n = a.evalEnv.w * a.evalEnv.h;
         if (!ensure_block(ctx, &st->evalTexels, std::max<size_t>(n, 1) * sizeof(float4), "eval texels"))

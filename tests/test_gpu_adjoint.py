@@ -116,8 +116,9 @@ def test_adjoint_matches_frozen_finite_differences(setup):
         fd = (lp - lm) / (2 * h)
         adj = float(grads[name].flatten()[i])
         errs.append((abs(adj - fd) / max(abs(fd), 1e-6), name, i, adj, fd))
-    worst = max(errs)
-    assert worst[0] <= 1e-2, worst
+    errs.sort(reverse=True)
+    print("worst relative errors:", errs[:5])
+    assert errs[0][0] <= 1e-2, errs[:5]
 
 
 def test_adjoint_agrees_with_plain_renderer_fd(setup):
