@@ -114,12 +114,14 @@ __device__ __forceinline__ V3 proj_tangent(const Mat& m, const V3& n) {
     return ortho_x(n);
 }
 // AdjustedRoughness with the half-vector anisotropy phase; with zero
-// anisotropy the phase is multiplied by zero and skipped.
-__device__ __forceinline__ float roughness_for(float r, float aniso, float rot, const V3& n, const V3& tangent, const V3& v,
+// anisotropy the phase is multiplied by zero, so neither it nor the tangent
+// (ProjectedTangent) is computed.
+__device__ __forceinline__ float roughness_for(float r, float aniso, float rot, const Mat& m, const V3& n, const V3& v,
                                                const V3& l) {
     const float ca = sclamp(aniso, -0.95f, 0.95f);
     float phase = 0.0f;
     if (ca != 0.0f) {
+        const V3 tangent = proj_tangent(m, n);
         const V3 td = safe_normalized(tangent - n * dot(tangent, n), ortho_x(n));
         const V3 bt = normalize(cross(n, td));
         const V3 h = safe_normalized(v + l, n);
@@ -194,10 +196,10 @@ static __device__ __noinline__ float bsdf_pdf(const Mat& m, const LobeWeights& w
     const float rw = w.diffuse + w.spec + w.coat;
     if (rw <= 0.0f) return 0.0f;
     const float dp = w.diffuse / rw, bp = w.spec / rw, cp = w.coat / rw;
-    const float sr = roughness_for(base_roughness(m), m.specular_anisotropy, m.specular_rotation, n, proj_tangent(m, n), v, l);
+    const float sr = roughness_for(base_roughness(m), m.specular_anisotropy, m.specular_rotation, m, n, v, l);
     float coatTerm = 0.0f;
     if (cp != 0.0f) {
-        const float cr = roughness_for(m.coat_roughness, m.coat_anisotropy, m.coat_rotation, cn, proj_tangent(m, cn), v, l);
+        const float cr = roughness_for(m.coat_roughness, m.coat_anisotropy, m.coat_rotation, m, cn, v, l);
         coatTerm = cp * spec_pdf(cn, v, l, cr);
     }
     return dp * nl * kInvPi + bp * spec_pdf(n, v, l, sr) + coatTerm;
@@ -211,32 +213,44 @@ static __device__ __noinline__ V3 bsdf_eval(const Mat& m, const V3& n, const V3&
     const V3 cF0 = coat_f0(m);
     const V3 underCoat = coat_tint(m) * layer_transmittance(cF0, dot(cn, v), dot(cn, l));
     const V3 underBase = layer_transmittance(baseF0, nv, nl);
-    const V3 vp = normalize(v - n * nv);
-    const V3 lp = normalize(l - n * nl);
-    const float cosPhi = length(vp) > 0.0f && length(lp) > 0.0f ? sclamp(dot(vp, lp), -1.0f, 1.0f) : 0.0f;
     const float sigma = sclamp(m.diffuse_roughness, 0.0f, 1.0f);
-    const float s2 = sigma * sigma;
-    const float orenA = 1.0f - (s2 / (2.0f * (s2 + 0.33f)));
-    const float orenB = 0.45f * s2 / (s2 + 0.09f);
-    const float sinV = sqrtf(smax(0.0f, 1.0f - nv * nv));
-    const float sinL = sqrtf(smax(0.0f, 1.0f - nl * nl));
-    const float sinAlpha = smax(sinV, sinL);
-    const float tanBeta = smin(sinV / smax(nv, 1.0e-6f), sinL / smax(nl, 1.0e-6f));
     const float wrap = sclamp(m.subsurface * m.subsurface_scale *
                                   (0.35f + 0.15f * sclamp(m.subsurface_anisotropy, -1.0f, 1.0f) +
                                    0.1f * sclamp(maxc(ld3(m.subsurface_radius)) / 3.0f, 0.0f, 1.0f)),
                               0.0f, 0.9f);
     const float wrapped = sclamp((nl + wrap) / (1.0f + wrap), 0.0f, 1.0f);
-    const float term = (orenA + orenB * smax(0.0f, cosPhi) * sinAlpha * tanBeta) * (wrapped / smax(nl, 1.0e-6f));
+    float term;
+    if (sigma == 0.0f) {
+        // Lambert: orenA = 1 and orenB = 0 exactly, so the Oren-Nayar factor
+        // (finite) multiplies zero and the sum is 1.
+        term = 1.0f * (wrapped / smax(nl, 1.0e-6f));
+    } else {
+        const V3 vp = normalize(v - n * nv);
+        const V3 lp = normalize(l - n * nl);
+        const float cosPhi = length(vp) > 0.0f && length(lp) > 0.0f ? sclamp(dot(vp, lp), -1.0f, 1.0f) : 0.0f;
+        const float s2 = sigma * sigma;
+        const float orenA = 1.0f - (s2 / (2.0f * (s2 + 0.33f)));
+        const float orenB = 0.45f * s2 / (s2 + 0.09f);
+        const float sinV = sqrtf(smax(0.0f, 1.0f - nv * nv));
+        const float sinL = sqrtf(smax(0.0f, 1.0f - nl * nl));
+        const float sinAlpha = smax(sinV, sinL);
+        const float tanBeta = smin(sinV / smax(nv, 1.0e-6f), sinL / smax(nl, 1.0e-6f));
+        term = (orenA + orenB * smax(0.0f, cosPhi) * sinAlpha * tanBeta) * (wrapped / smax(nl, 1.0e-6f));
+    }
     const V3 diffuse = diffuse_color(m) * underCoat * underBase * (kInvPi * term);
-    const float sr = roughness_for(base_roughness(m), m.specular_anisotropy, m.specular_rotation, n, proj_tangent(m, n), v, l);
+    const float sr = roughness_for(base_roughness(m), m.specular_anisotropy, m.specular_rotation, m, n, v, l);
     const V3 spec = underCoat * thin_film(spec_lobe(n, v, l, baseF0, sr), m, n, v, l);
-    const float cr = roughness_for(m.coat_roughness, m.coat_anisotropy, m.coat_rotation, cn, proj_tangent(m, cn), v, l);
+    const float cr = roughness_for(m.coat_roughness, m.coat_anisotropy, m.coat_rotation, m, cn, v, l);
     const V3 coat = thin_film(spec_lobe(cn, v, l, cF0, cr), m, cn, v, l);
-    const V3 h = safe_normalized(v + l, n);
     const float sw = sclamp(m.sheen, 0.0f, 1.0f);
-    const float lh = sclamp(dot(l, h), 0.0f, 1.0f);
-    const float sf = powf(1.0f - lh, 5.0f) * (1.0f - 0.5f * sclamp(m.sheen_roughness, 0.0f, 1.0f));
+    // With zero sheen weight the factor sf (finite, >= 0) only multiplies a
+    // signed zero; 1 gives the same signed zero without the powf.
+    float sf = 1.0f;
+    if (sw != 0.0f) {
+        const V3 h = safe_normalized(v + l, n);
+        const float lh = sclamp(dot(l, h), 0.0f, 1.0f);
+        sf = powf(1.0f - lh, 5.0f) * (1.0f - 0.5f * sclamp(m.sheen_roughness, 0.0f, 1.0f));
+    }
     const V3 sheen = ld3(m.sheen_color) * sw * sf * underCoat * underBase;
     return diffuse + spec + coat + sheen;
 }

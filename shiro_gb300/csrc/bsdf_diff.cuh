@@ -221,11 +221,12 @@ __device__ __forceinline__ DV3 spec_lobe_d(const V3& n, const V3& v, const V3& l
     return schlick_d(f0, vh) * (d * g / smax(4.0f * nv * nl, 1.0e-6f));
 }
 // AdjustedRoughness on a dual base roughness (the phase factor is geometry).
-__device__ __forceinline__ Dual roughness_for_d(const Dual& r, float aniso, float rot, const V3& n, const V3& tangent,
+__device__ __forceinline__ Dual roughness_for_d(const Dual& r, float aniso, float rot, const Mat& m, const V3& n,
                                                 const V3& v, const V3& l) {
     const float ca = sclamp(aniso, -0.95f, 0.95f);
     float phase = 0.0f;
     if (ca != 0.0f) {
+        const V3 tangent = proj_tangent(m, n);
         const V3 td = safe_normalized(tangent - n * dot(tangent, n), ortho_x(n));
         const V3 bt = normalize(cross(n, td));
         const V3 h = safe_normalized(v + l, n);
@@ -250,38 +251,46 @@ __device__ __noinline__ DV3 bsdf_eval_d(const Mat& m, const V3& n, const V3& cn,
     const V3 cF0 = coat_f0(m);
     const V3 underCoat = coat_tint(m) * layer_transmittance(cF0, dot(cn, v), dot(cn, l));
     const DV3 underBase = layer_transmittance_d(baseF0, nv, nl);
-    const V3 vp = normalize(v - n * nv);
-    const V3 lp = normalize(l - n * nl);
-    const float cosPhi = length(vp) > 0.0f && length(lp) > 0.0f ? sclamp(dot(vp, lp), -1.0f, 1.0f) : 0.0f;
     const float sigma = sclamp(m.diffuse_roughness, 0.0f, 1.0f);
-    const float s2 = sigma * sigma;
-    const float orenA = 1.0f - (s2 / (2.0f * (s2 + 0.33f)));
-    const float orenB = 0.45f * s2 / (s2 + 0.09f);
-    const float sinV = sqrtf(smax(0.0f, 1.0f - nv * nv));
-    const float sinL = sqrtf(smax(0.0f, 1.0f - nl * nl));
-    const float sinAlpha = smax(sinV, sinL);
-    const float tanBeta = smin(sinV / smax(nv, 1.0e-6f), sinL / smax(nl, 1.0e-6f));
     const float wrap = sclamp(m.subsurface * m.subsurface_scale *
                                   (0.35f + 0.15f * sclamp(m.subsurface_anisotropy, -1.0f, 1.0f) +
                                    0.1f * sclamp(maxc(ld3(m.subsurface_radius)) / 3.0f, 0.0f, 1.0f)),
                               0.0f, 0.9f);
     const float wrapped = sclamp((nl + wrap) / (1.0f + wrap), 0.0f, 1.0f);
-    const float term = (orenA + orenB * smax(0.0f, cosPhi) * sinAlpha * tanBeta) * (wrapped / smax(nl, 1.0e-6f));
+    float term;
+    if (sigma == 0.0f) {
+        term = 1.0f * (wrapped / smax(nl, 1.0e-6f));
+    } else {
+        const V3 vp = normalize(v - n * nv);
+        const V3 lp = normalize(l - n * nl);
+        const float cosPhi = length(vp) > 0.0f && length(lp) > 0.0f ? sclamp(dot(vp, lp), -1.0f, 1.0f) : 0.0f;
+        const float s2 = sigma * sigma;
+        const float orenA = 1.0f - (s2 / (2.0f * (s2 + 0.33f)));
+        const float orenB = 0.45f * s2 / (s2 + 0.09f);
+        const float sinV = sqrtf(smax(0.0f, 1.0f - nv * nv));
+        const float sinL = sqrtf(smax(0.0f, 1.0f - nl * nl));
+        const float sinAlpha = smax(sinV, sinL);
+        const float tanBeta = smin(sinV / smax(nv, 1.0e-6f), sinL / smax(nl, 1.0e-6f));
+        term = (orenA + orenB * smax(0.0f, cosPhi) * sinAlpha * tanBeta) * (wrapped / smax(nl, 1.0e-6f));
+    }
     const DV3 diffuse = diffuse_color_d(m, p) * underCoat * underBase * (kInvPi * term);
     const Dual baseRough = dclamp(p.rough + m.coat_affect_roughness * m.coat_weight * m.coat_roughness, 0.0f, 1.0f);
-    const Dual sr = roughness_for_d(baseRough, m.specular_anisotropy, m.specular_rotation, n, proj_tangent(m, n), v, l);
+    const Dual sr = roughness_for_d(baseRough, m.specular_anisotropy, m.specular_rotation, m, n, v, l);
     DV3 spec = underCoat * spec_lobe_d(n, v, l, baseF0, sr);
     if (m.thin_film_thickness > 0.0f) {
         const V3 h = safe_normalized(v + l, n);
         spec = underCoat * (spec_lobe_d(n, v, l, baseF0, sr) * film_color(m.thin_film_thickness, m.thin_film_ior,
                                                                           sclamp(dot(v, h), 0.0f, 1.0f)));
     }
-    const float cr = roughness_for(m.coat_roughness, m.coat_anisotropy, m.coat_rotation, cn, proj_tangent(m, cn), v, l);
+    const float cr = roughness_for(m.coat_roughness, m.coat_anisotropy, m.coat_rotation, m, cn, v, l);
     const V3 coat = thin_film(spec_lobe(cn, v, l, cF0, cr), m, cn, v, l);
-    const V3 h = safe_normalized(v + l, n);
     const float sw = sclamp(m.sheen, 0.0f, 1.0f);
-    const float lh = sclamp(dot(l, h), 0.0f, 1.0f);
-    const float sf = powf(1.0f - lh, 5.0f) * (1.0f - 0.5f * sclamp(m.sheen_roughness, 0.0f, 1.0f));
+    float sf = 1.0f;
+    if (sw != 0.0f) {
+        const V3 h = safe_normalized(v + l, n);
+        const float lh = sclamp(dot(l, h), 0.0f, 1.0f);
+        sf = powf(1.0f - lh, 5.0f) * (1.0f - 0.5f * sclamp(m.sheen_roughness, 0.0f, 1.0f));
+    }
     const DV3 sheen = (ld3(m.sheen_color) * sw * sf * underCoat) * underBase;
     return diffuse + spec + dv3(coat) + sheen;
 }
