@@ -59,6 +59,7 @@ def parse():
     p.add_argument("--width", type=int, default=0, help="override the frame width (profiling cases)")
     p.add_argument("--height", type=int, default=0)
     p.add_argument("--spp", type=int, default=0)
+    p.add_argument("--no-adjoint", action="store_true")
     return p.parse_args()
 
 
@@ -231,6 +232,60 @@ def cpu_baseline(w, seconds: float, rank: int = 0) -> dict:
             "cpu": cpu, "seconds": t_render, "paths": int(paths)}
 
 
+def adjoint_bench(local: int, iters: int = 5, warmup: int = 2) -> dict:
+    """Gradient throughput of the differentiable form on the 256-material
+    sphere scene: 512x512, 32 spp, depth 6, L2 loss against a seeded target,
+    gradients for 256 x (base colour, roughness, metalness) and the 512x256x3
+    environment texels.  One gradient = one forward render + one adjoint pass."""
+    import torch
+
+    from shiro_gb300 import GpuBackend, scenes
+    from shiro_gb300.abi import RenderSettings
+
+    scene = scenes.split_sphere_scene(parts=256, env_width=512, env_height=256, seed=4)
+    st = RenderSettings(width=512, height=512, samples_per_pixel=32, max_depth=6, diffuse_depth=6, specular_depth=6,
+                        backend=1)
+    cam = scenes.sphere_camera(1.0)
+    gpu = GpuBackend(local)
+    stream = torch.cuda.current_stream()
+    gpu.lib.shiro_gpu_set_stream(gpu.handle, stream.cuda_stream)
+    gpu.upload_scene(scene)
+    p = dict(base_color=torch.tensor([m.base_color for m in scene.materials], dtype=torch.float32, device="cuda"),
+             roughness=torch.tensor([m.roughness for m in scene.materials], dtype=torch.float32, device="cuda"),
+             metallic=torch.tensor([m.metallic for m in scene.materials], dtype=torch.float32, device="cuda"),
+             env=torch.tensor(scene.dome_lights[0].env, dtype=torch.float32, device="cuda"))
+    target = torch.rand((512, 512, 3), generator=torch.Generator().manual_seed(9)).cuda()
+    grads = {k: torch.zeros_like(v) for k, v in p.items()}
+
+    def step():
+        img = gpu.render_device(cam, st)
+        d = torch.zeros_like(img)
+        d[..., :3] = 2.0 * (img[..., :3] - target) / target.numel()
+        for g in grads.values():
+            g.zero_()
+        gpu.adjoint(cam, st, d, grads)
+        return gpu.last_stats()["kernel_ms"]
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    adj_ms = 0.0
+    e0.record(stream)
+    for _ in range(iters):
+        adj_ms += step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / iters
+    nparams = sum(v.numel() for v in p.values())
+    paths = 512 * 512 * 32
+    gpu.close()
+    return {"workload": "256-material sphere scene, 512x256 env, 512x512, 32 spp, depth 6, L2 loss",
+            "params": int(nparams), "ms_per_gradient": ms, "grads_per_s": 1000.0 / ms,
+            "adjoint_ms": adj_ms / iters, "adjoint_Mpaths_s": paths / (adj_ms / iters / 1000.0) / 1e6,
+            "param_gradients_per_s": nparams * 1000.0 / ms}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -397,7 +452,7 @@ def main():
         gpu.set_wavefront_config(use_graph=0)
         diag = render_dev("wavefront")
         gpu.set_wavefront_config(use_graph=1)
-        names = ["wf_generate", "wf_extend", "wf_shade", "wf_shadow", "wf_resolve", "wf_bookkeeping"]
+        names = ["wf_generate", "wf_extend", "wf_shade", "wf_occlude", "wf_resolve", "wf_shadow+bookkeeping"]
         dom = max(range(6), key=lambda k: diag["stage_ms"][k])
         kernel, kms, kl = names[dom], diag["stage_ms"][dom], diag["stage_launches"][dom]
         stage_share = {names[k]: diag["stage_ms"][k] / max(sum(diag["stage_ms"]), 1e-9) for k in range(6)}
@@ -420,6 +475,10 @@ def main():
                 "avg_launch_ms": avg_launch_ms, "paths_per_launch": paths_per_launch, "stage_share": stage_share,
                 "work_per_path": {k: v / npth for k, v in wc.items() if k != "paths"}}
 
+    adjoint = None
+    if rank == 0 and not args.no_adjoint and args.workload == "field" and not (args.width or args.height or args.spp):
+        adjoint = adjoint_bench(local)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(w, args.cpu_seconds)
@@ -433,7 +492,7 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene, random-init HDRI)",
                 "config": cfg, "clocks": clocks.summary(), "gpu_launches": launches, "e2e": e2e,
-                "roofline": roofline, "cpu_baseline": cpu}
+                "roofline": roofline, "cpu_baseline": cpu, "adjoint": adjoint}
         print(json.dumps(line), flush=True)
     gpu.close()
     if dist:

@@ -363,8 +363,8 @@ typedef struct ShiroRenderStats {
     uint32_t bvh_max_leaf;
     uint64_t device_bytes;      /* device memory held by the context */
     /* wavefront stages (filled by an event-timed run, use_graph = 0):
-     * 0 generate, 1 extend (closest hit), 2 shade, 3 shadow (occlusion),
-     * 4 resolve, 5 queue bookkeeping */
+     * 0 generate, 1 extend (closest hit), 2 shade, 3 occlusion rays,
+     * 4 resolve, 5 light-sample accumulation and queue bookkeeping */
     double stage_ms[6];
     uint64_t stage_launches[6];
     uint64_t waves;             /* waves of the last wavefront call */

@@ -76,8 +76,9 @@ struct WfView {
     float4* shC;       // [lightSamples][P]: contribution
     uint32_t* rayQ0;
     uint32_t* rayQ1;
-    uint32_t* shadowQ;
-    uint32_t* counters;  // 0: ray count A, 1: ray count B, 2: shadow count, 3: wave index
+    uint32_t* shadowQ;     // paths with light samples to accumulate
+    uint32_t* shadowRayQ;  // one item per light sample to test: slot << 3 | sample
+    uint32_t* counters;  // 0: ray count A, 1: ray count B, 2: shadow paths, 3: wave index, 4: shadow rays
     float4* records;     // 3 per slot
     const WaveDesc* waves;
     const WaveSeg* segs;
@@ -119,6 +120,7 @@ __global__ void wf_begin(WfView v) {
         v.counters[0] = v.waves[w].paths;
         v.counters[1] = 0u;
         v.counters[2] = 0u;
+        v.counters[4] = 0u;
     }
 }
 
@@ -177,6 +179,7 @@ __global__ void __launch_bounds__(256) wf_shade(WfView v, DevScene s, uint32_t c
     for (uint32_t it = 0; it < iters; ++it, i += stride) {
         const bool valid = i < count;
         bool pushRay = false, pushShadow = false;
+        uint32_t lightMask = 0;
         uint32_t j = 0;
         if (valid) {
             j = qin[i];
@@ -218,6 +221,7 @@ __global__ void __launch_bounds__(256) wf_shade(WfView v, DevScene s, uint32_t c
                     V3 dir{0.0f, 0.0f, 0.0f}, c{0.0f, 0.0f, 0.0f};
                     const bool ok = light_sample(s, q, vx, smp, depth, k, &dir, &c, ctr);
                     anyLight |= ok;
+                    lightMask |= ok ? (1u << k) : 0u;
                     const size_t e = static_cast<size_t>(k) * v.P + j;
                     v.shDir[e] = make_float4(dir.x, dir.y, dir.z, ok ? 1.0f : 0.0f);
                     v.shC[e] = make_float4(c.x, c.y, c.z, 0.0f);
@@ -243,22 +247,34 @@ __global__ void __launch_bounds__(256) wf_shade(WfView v, DevScene s, uint32_t c
         }
         warp_push(cout, qout, pushRay, j);
         warp_push(&v.counters[2], v.shadowQ, pushShadow, j);
+        for (uint32_t k = 0; k < v.lightSamples; ++k)
+            warp_push(&v.counters[4], v.shadowRayQ, (lightMask >> k) & 1u, (j << 3) | k);
     }
 }
 
+// One occlusion ray per thread; an occluded sample's flag is cleared.
+__global__ void __launch_bounds__(256) wf_occlude(WfView v, DevScene s) {
+    const uint32_t count = v.counters[4];
+    NullCounter ctr;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t item = v.shadowRayQ[i];
+        const uint32_t j = item >> 3, k = item & 7u;
+        const size_t e = static_cast<size_t>(k) * v.P + j;
+        const float4 o4 = v.shOrigin[j], d4 = v.shDir[e];
+        if (trace_occluded(s, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX, ctr)) v.shDir[e].w = 0.0f;
+    }
+}
+
+// In-order sum of a path's unoccluded light samples (sum_direct's order).
 __global__ void __launch_bounds__(256) wf_shadow(WfView v, DevScene s) {
     const uint32_t count = v.counters[2];
-    NullCounter ctr;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t j = v.shadowQ[i];
         const DevRequest& q = v.reqs[v.ident[j].w].q;
-        const float4 o4 = v.shOrigin[j], t4 = v.shT[j], r4 = v.rad[j];
-        const V3 org{o4.x, o4.y, o4.z};
+        const float4 t4 = v.shT[j], r4 = v.rad[j];
         const V3 direct = sum_direct(s, q, [&](uint32_t k, V3* c) {
             const size_t e = static_cast<size_t>(k) * v.P + j;
-            const float4 d4 = v.shDir[e];
-            if (d4.w == 0.0f) return false;
-            if (trace_occluded(s, org, V3{d4.x, d4.y, d4.z}, FLT_MAX, ctr)) return false;
+            if (v.shDir[e].w == 0.0f) return false;
             const float4 c4 = v.shC[e];
             *c = V3{c4.x, c4.y, c4.z};
             return true;
@@ -273,6 +289,7 @@ __global__ void wf_end_bounce(WfView v, uint32_t cur) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         v.counters[cur] = 0u;
         v.counters[2] = 0u;
+        v.counters[4] = 0u;
     }
 }
 
@@ -349,7 +366,7 @@ bool ensure_pool(ContextImpl* ctx, WavefrontState* wf, uint32_t P, uint32_t ligh
     const size_t p = P;
     const size_t stateBytes = p * (6 * sizeof(float4) + sizeof(uint32_t));
     const size_t shadowBytes = p * (2 + 2 * static_cast<size_t>(std::max(1u, lightSamples))) * sizeof(float4);
-    const size_t queueBytes = p * 3 * sizeof(uint32_t) + 64;
+    const size_t queueBytes = p * (3 + static_cast<size_t>(std::max(1u, lightSamples))) * sizeof(uint32_t) + 64;
     const size_t recordBytes = p * 3 * sizeof(float4);
     if (!ensure_block(ctx, &wf->state, stateBytes, "wavefront state")) return false;
     if (!ensure_block(ctx, &wf->shadow, shadowBytes, "wavefront shadow records")) return false;
@@ -382,6 +399,7 @@ WfView make_view(WavefrontState* wf, uint32_t P, uint32_t lightSamples, const Wa
     v.rayQ0 = qb + 16;
     v.rayQ1 = v.rayQ0 + p;
     v.shadowQ = v.rayQ1 + p;
+    v.shadowRayQ = v.shadowQ + p;
     v.records = static_cast<float4*>(wf->records.ptr);
     v.waves = waves;
     v.segs = segs;
@@ -452,7 +470,7 @@ Plan plan_waves(const std::vector<DevRequest>& qs, uint32_t P) {
 struct Launch {
     WfView v;
     DevScene s;
-    int gGen, gExt, gShade, gShadow, gRes;
+    int gGen, gExt, gShade, gShadow, gOcc, gRes;
     int bExt, bShade, bShadow;
     uint32_t depth;
 };
@@ -464,7 +482,8 @@ void enqueue_wave(const Launch& L, cudaStream_t st) {
         const uint32_t cur = d & 1u;
         wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur);
         wf_shade<<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
-        wf_shadow<<<L.gShadow, L.bShadow, 0, st>>>(L.v, L.s);
+        wf_occlude<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s);
+        wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s);
         wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur);
     }
     wf_resolve<<<L.gRes, 128, 0, st>>>(L.v);
@@ -487,7 +506,8 @@ void enqueue_wave_timed(const Launch& L, cudaStream_t st, std::vector<std::pair<
         const uint32_t cur = d & 1u;
         timed(1, [&] { wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur); });
         timed(2, [&] { wf_shade<<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d); });
-        timed(3, [&] { wf_shadow<<<L.gShadow, L.bShadow, 0, st>>>(L.v, L.s); });
+        timed(3, [&] { wf_occlude<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s); });
+        timed(5, [&] { wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s); });
         timed(5, [&] { wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur); });
     }
     timed(4, [&] { wf_resolve<<<L.gRes, 128, 0, st>>>(L.v); });
@@ -540,7 +560,8 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.gGen = grid_for(wf_generate, 128, wf->smCount);
     L.gExt = grid_for(wf_extend, L.bExt, wf->smCount);
     L.gShade = grid_for(wf_shade, L.bShade, wf->smCount);
-    L.gShadow = grid_for(wf_shadow, L.bShadow, wf->smCount);
+    L.gShadow = grid_for(wf_shadow, 256, wf->smCount);
+    L.gOcc = grid_for(wf_occlude, L.bShadow, wf->smCount);
     L.gRes = grid_for(wf_resolve, 128, wf->smCount);
     L.depth = pl.maxDepth;
     const uint32_t minus1 = 0xffffffffu;
@@ -578,7 +599,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             enqueue_wave_timed(L, st, ev);
             e = cudaGetLastError();
         }
-        launches += 3 + 4ull * L.depth;
+        launches += 3 + 5ull * L.depth;
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront launch");
     }
     cudaEventRecord(e1, st);
