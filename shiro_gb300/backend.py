@@ -72,6 +72,7 @@ def load_library(path: str = LIB_PATH):
         "shiro_gpu_last_stats": ([_P, _P], C.c_int),
         "shiro_gpu_count_work": ([_P, _P, _U, _P], C.c_int),
         "shiro_gpu_render_frozen": ([_P, _P, _P, _P, _P, _P, _P], C.c_int),
+        "shiro_gpu_set_bvh_width": ([_P, _U], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -210,6 +211,12 @@ class GpuBackend:
         if rc != 0:
             raise self._err(rc)
         return fbs
+
+    def set_bvh_width(self, width: int):
+        """2: traverse the binary BVH (default); 8: the wide quantised BVH."""
+        rc = self.lib.shiro_gpu_set_bvh_width(self._ctx, int(width))
+        if rc != 0:
+            raise ShiroGpuError(rc, "bvh width must be 2 or 8")
 
     def wavefront_config(self) -> dict:
         c = WavefrontConfig()

@@ -275,10 +275,6 @@ __global__ void k_write_root(float4* out, float4 b0lo, float4 b0hi, int l0, floa
     out[3] = make_float4(__int_as_float(l0), __int_as_float(l1), 0.0f, 0.0f);
 }
 
-__global__ void k_copy_box(const float4* __restrict__ nodeBox, float4* __restrict__ dst) {
-    dst[0] = nodeBox[0];
-    dst[1] = nodeBox[1];
-}
 
 #define BVH_CHECK(x)                                                       \
     do {                                                                   \
@@ -467,6 +463,168 @@ int build_bvh(const BvhInput& in, cudaStream_t stream, BvhOutput* out, std::stri
     BVH_CHECK(cudaStreamSynchronize(stream));
     out->depth = depthHost + offset + 1u;
     out->maxLeaf = kMaxLeaf;
+    return SHIRO_OK;
+}
+
+namespace {
+
+struct Entry {
+    int link;
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ float entry_area(const Entry& e) {
+    const float dx = e.hi[0] - e.lo[0], dy = e.hi[1] - e.lo[1], dz = e.hi[2] - e.lo[2];
+    return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+__device__ __forceinline__ void node2_children(const float4* nodes2, int n, Entry* a, Entry* b) {
+    const float4 n0 = nodes2[4 * static_cast<size_t>(n)], n1 = nodes2[4 * static_cast<size_t>(n) + 1];
+    const float4 n2 = nodes2[4 * static_cast<size_t>(n) + 2], n3 = nodes2[4 * static_cast<size_t>(n) + 3];
+    a->link = __float_as_int(n3.x);
+    a->lo[0] = n0.x; a->hi[0] = n0.y; a->lo[1] = n0.z; a->hi[1] = n0.w; a->lo[2] = n2.x; a->hi[2] = n2.y;
+    b->link = __float_as_int(n3.y);
+    b->lo[0] = n1.x; b->hi[0] = n1.y; b->lo[1] = n1.z; b->hi[1] = n1.w; b->lo[2] = n2.z; b->hi[2] = n2.w;
+}
+
+// One thread per task (binary node -> wide node).  New internal children get
+// wide-node indices from `counter` and are appended to the next task list.
+__global__ void k_collapse8(const float4* __restrict__ nodes2, const int2* __restrict__ tasks, uint32_t taskCount,
+                            int2* __restrict__ nextTasks, unsigned int* __restrict__ nextCount,
+                            unsigned int* __restrict__ counter, float4* __restrict__ out) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= taskCount) return;
+    const int2 task = tasks[t];
+    Entry e[8];
+    int n = 0;
+    {
+        Entry a, b;
+        node2_children(nodes2, task.x, &a, &b);
+        if (a.lo[0] <= a.hi[0]) e[n++] = a;
+        if (b.lo[0] <= b.hi[0]) e[n++] = b;
+    }
+    while (n < 8) {
+        int best = -1;
+        float bestArea = -1.0f;
+        for (int i = 0; i < n; ++i)
+            if (e[i].link >= 0 && entry_area(e[i]) > bestArea) {
+                bestArea = entry_area(e[i]);
+                best = i;
+            }
+        if (best < 0) break;
+        Entry a, b;
+        node2_children(nodes2, e[best].link, &a, &b);
+        const bool va = a.lo[0] <= a.hi[0], vb = b.lo[0] <= b.hi[0];
+        if (va && vb) {
+            e[best] = a;
+            e[n++] = b;
+        } else if (va) {
+            e[best] = a;
+        } else if (vb) {
+            e[best] = b;
+        } else {
+            e[best] = e[--n];
+        }
+    }
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(lo[k], e[i].lo[k]);
+            hi[k] = fmaxf(hi[k], e[i].hi[k]);
+        }
+    // per axis a power-of-two scale with extent / scale <= 255
+    uint32_t ex[3];
+    float sc[3];
+    for (int k = 0; k < 3; ++k) {
+        const float ext = __fsub_ru(hi[k], lo[k]);
+        int eb = 1;  // smallest normal exponent
+        if (ext > 0.0f) {
+            int e2;
+            frexpf(ext / 255.0f, &e2);  // ext/255 < 2^e2
+            eb = min(max(e2 + 127, 1), 254);
+        }
+        ex[k] = static_cast<uint32_t>(eb);
+        sc[k] = __uint_as_float(static_cast<uint32_t>(eb) << 23);
+        while (__fmul_ru(255.0f, sc[k]) < ext && ex[k] < 254) {  // guard the rounding of ext / 255
+            ++ex[k];
+            sc[k] = __uint_as_float(ex[k] << 23);
+        }
+    }
+    uint8_t q[6][8];
+    int links[8];
+    for (int i = 0; i < 8; ++i) {
+        if (i >= n) {
+            links[i] = kEmptyChild;
+            for (int k = 0; k < 3; ++k) {
+                q[k][i] = 255;
+                q[3 + k][i] = 0;
+            }
+            continue;
+        }
+        for (int k = 0; k < 3; ++k) {
+            const float a = floorf(__fdiv_rd(__fsub_rd(e[i].lo[k], lo[k]), sc[k]));
+            const float b = ceilf(__fdiv_ru(__fsub_ru(e[i].hi[k], lo[k]), sc[k]));
+            q[k][i] = static_cast<uint8_t>(fminf(fmaxf(a, 0.0f), 255.0f));
+            q[3 + k][i] = static_cast<uint8_t>(fminf(fmaxf(b, 0.0f), 255.0f));
+        }
+        if (e[i].link >= 0) {
+            const int child = static_cast<int>(atomicAdd(counter, 1u));
+            const unsigned int slot = atomicAdd(nextCount, 1u);
+            nextTasks[slot] = make_int2(e[i].link, child);
+            links[i] = child;
+        } else {
+            links[i] = e[i].link;
+        }
+    }
+    float4* o = out + 6 * static_cast<size_t>(task.y);
+    o[0] = make_float4(lo[0], lo[1], lo[2], __uint_as_float(ex[0] | (ex[1] << 8) | (ex[2] << 16)));
+    o[1] = make_float4(__int_as_float(links[0]), __int_as_float(links[1]), __int_as_float(links[2]), __int_as_float(links[3]));
+    o[2] = make_float4(__int_as_float(links[4]), __int_as_float(links[5]), __int_as_float(links[6]), __int_as_float(links[7]));
+    uint32_t w[12];
+    for (int r = 0; r < 6; ++r) {
+        w[2 * r] = q[r][0] | (q[r][1] << 8) | (q[r][2] << 16) | (static_cast<uint32_t>(q[r][3]) << 24);
+        w[2 * r + 1] = q[r][4] | (q[r][5] << 8) | (q[r][6] << 16) | (static_cast<uint32_t>(q[r][7]) << 24);
+    }
+    o[3] = make_float4(__uint_as_float(w[0]), __uint_as_float(w[1]), __uint_as_float(w[2]), __uint_as_float(w[3]));
+    o[4] = make_float4(__uint_as_float(w[4]), __uint_as_float(w[5]), __uint_as_float(w[6]), __uint_as_float(w[7]));
+    o[5] = make_float4(__uint_as_float(w[8]), __uint_as_float(w[9]), __uint_as_float(w[10]), __uint_as_float(w[11]));
+}
+
+}  // namespace
+
+int collapse_bvh8(const float4* nodes2, uint32_t nodeCount2, cudaStream_t stream, Bvh8Output* out, std::string& err) {
+    Scratch sc;
+    int2 *ta = nullptr, *tb = nullptr;
+    unsigned int* cnt = nullptr;  // [0] node counter, [1] next task count
+    const uint32_t cap = std::max<uint32_t>(nodeCount2, 1);
+    BVH_CHECK(sc.alloc(&ta, cap));
+    BVH_CHECK(sc.alloc(&tb, cap));
+    BVH_CHECK(sc.alloc(&cnt, 2));
+    float4* nodes = nullptr;
+    BVH_CHECK(cudaMalloc(&nodes, 6 * sizeof(float4) * static_cast<size_t>(cap)));
+    out->nodes = nodes;
+    const int2 root = make_int2(0, 0);
+    const unsigned int init[2] = {1u, 0u};
+    BVH_CHECK(cudaMemcpyAsync(ta, &root, sizeof(root), cudaMemcpyHostToDevice, stream));
+    BVH_CHECK(cudaMemcpyAsync(cnt, init, sizeof(init), cudaMemcpyHostToDevice, stream));
+    uint32_t tasks = 1, depth = 0;
+    while (tasks > 0) {
+        k_collapse8<<<blocks(tasks, 128), 128, 0, stream>>>(nodes2, ta, tasks, tb, cnt + 1, cnt, nodes);
+        BVH_CHECK(cudaGetLastError());
+        unsigned int h[2];
+        BVH_CHECK(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, stream));
+        BVH_CHECK(cudaMemsetAsync(cnt + 1, 0, sizeof(unsigned int), stream));
+        BVH_CHECK(cudaStreamSynchronize(stream));
+        tasks = h[1];
+        out->nodeCount = h[0];
+        std::swap(ta, tb);
+        ++depth;
+        if (depth > 64) {
+            err = "wide BVH collapse did not terminate";
+            return SHIRO_ERR_INVALID_ARGUMENT;
+        }
+    }
+    out->depth = depth;
     return SHIRO_OK;
 }
 

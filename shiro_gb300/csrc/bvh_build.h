@@ -35,6 +35,27 @@ struct BvhOutput {
 
 inline int leaf_link_host(int first, int count) { return ~((first << 3) | (count - 1)); }
 
+// 8-wide BVH with quantised child boxes, collapsed from the binary BVH.
+// Node layout (96 B = 6 x float4):
+//   [0] origin.xyz, bits: ex | ey << 8 | ez << 16 (biased float exponents of
+//       the per-axis power-of-two scales)
+//   [1] child links 0-3, [2] child links 4-7: >= 0 wide node index, < 0 the
+//       binary BVH's leaf link ~((first << 3) | (count - 1)), kEmptyChild empty
+//   [3..5] 8 x (qlo.x, qlo.y, qlo.z, qhi.x, qhi.y, qhi.z) bytes, stored as
+//       qlo.x[8] qlo.y[8] qlo.z[8] qhi.x[8] qhi.y[8] qhi.z[8]; a child box is
+//       origin + q * scale, rounded outward at build time.
+constexpr int kEmptyChild = 0x7fffffff;
+
+struct Bvh8Output {
+    float4* nodes = nullptr;  // cudaMalloc'ed, 6 float4 per node
+    uint32_t nodeCount = 0;
+    uint32_t depth = 0;
+};
+
+// Collapses the binary BVH (scene.cuh layout, root = node 0) into 8-wide
+// nodes by repeatedly opening the largest-area internal child.
+int collapse_bvh8(const float4* nodes2, uint32_t nodeCount2, cudaStream_t stream, Bvh8Output* out, std::string& err);
+
 int build_bvh(const BvhInput& in, cudaStream_t stream, BvhOutput* out, std::string& err);
 
 }  // namespace shiro_gpu

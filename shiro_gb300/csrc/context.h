@@ -46,6 +46,11 @@ struct ContextImpl {
     std::vector<ShiroMaterialDesc> materialsHost;
     uint32_t materialCount = 0;        // user materials (the default one follows)
     uint32_t bvhDepth = 0, bvhMaxLeaf = 0;
+    const float4* nodes8 = nullptr;   // wide BVH (kept even while the binary one is selected)
+    uint32_t node8Count = 0, bvh8Depth = 0;
+    // 2: traverse the binary BVH (default, measured faster on GB300 for
+    // L2-resident scenes), 8: the wide quantised BVH
+    uint32_t bvhWidth = 2;
 
     // scratch (grown on demand, kept between calls)
     DeviceBlock pathRecords;

@@ -42,6 +42,7 @@ struct DevDistant {
 
 struct DevScene {
     const float4* nodes;
+    const float4* nodes8;           // 8-wide quantised BVH (bvh_build.h); NULL: traverse the binary BVH
     const float4* tris;
     const uint4* triVerts;
     const float4* normals;

@@ -440,6 +440,18 @@ const char* shiro_gpu_last_error(const ShiroGpuContext* ctx) {
     return ctx->impl.lastError.c_str();
 }
 
+int shiro_gpu_set_bvh_width(ShiroGpuContext* ctx, uint32_t width) {
+    if (!ctx || (width != 2 && width != 8)) return SHIRO_ERR_INVALID_ARGUMENT;
+    ContextImpl& c = ctx->impl;
+    c.bvhWidth = width;
+    c.scene.nodes8 = (width == 8 && c.hasScene) ? c.nodes8 : nullptr;
+    if (c.hasScene) {
+        c.stats.bvh_nodes = c.scene.nodes8 ? c.node8Count : c.scene.nodeCount;
+        c.stats.bvh_depth = c.scene.nodes8 ? c.bvh8Depth : c.bvhDepth;
+    }
+    return SHIRO_OK;
+}
+
 int shiro_gpu_set_stream(ShiroGpuContext* ctx, void* stream) {
     if (!ctx) return SHIRO_ERR_INVALID_ARGUMENT;
     ctx->impl.stream = stream ? static_cast<cudaStream_t>(stream) : ctx->impl.ownStream;
@@ -616,6 +628,16 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     }
     ctx->sceneBlocks.push_back({bout.nodes, 4 * sizeof(float4) * bout.nodeCount});
     ctx->sceneBlocks.push_back({bout.tris, 3 * sizeof(float4) * bout.triCount});
+    Bvh8Output b8;
+    rc = collapse_bvh8(bout.nodes, bout.nodeCount, ctx->stream, &b8, berr);
+    if (rc != SHIRO_OK) {
+        if (b8.nodes) cudaFree(b8.nodes);
+        return fail(ctx, rc, "wide BVH: " + berr);
+    }
+    ctx->sceneBlocks.push_back({b8.nodes, 6 * sizeof(float4) * std::max<uint32_t>(bout.nodeCount, 1)});
+    ctx->nodes8 = b8.nodes;
+    ctx->node8Count = b8.nodeCount;
+    ctx->bvh8Depth = b8.depth;
     ctx->bvhDepth = bout.depth;
     ctx->bvhMaxLeaf = bout.maxLeaf;
     DevScene& s = ctx->scene;
@@ -623,6 +645,7 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     s.tris = bout.tris;
     s.nodeCount = bout.nodeCount;
     s.triCount = bout.triCount;
+    s.nodes8 = ctx->bvhWidth == 8 ? ctx->nodes8 : nullptr;
 
     // --- shading data ----------------------------------------------------------
     ctx->materialsHost.assign(sd->materials, sd->materials + sd->material_count);
@@ -671,9 +694,9 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     if (e != cudaSuccess) return cuda_fail(ctx, e, "scene upload");
     ctx->hasScene = true;
     ctx->stats = ShiroRenderStats{};
-    ctx->stats.bvh_nodes = s.nodeCount;
+    ctx->stats.bvh_nodes = s.nodes8 ? ctx->node8Count : s.nodeCount;
     ctx->stats.triangles = s.triCount;
-    ctx->stats.bvh_depth = ctx->bvhDepth;
+    ctx->stats.bvh_depth = s.nodes8 ? ctx->bvh8Depth : ctx->bvhDepth;
     ctx->stats.bvh_max_leaf = ctx->bvhMaxLeaf;
     ctx->stats.device_bytes = ctx->deviceBytes();
     return SHIRO_OK;

@@ -116,9 +116,185 @@ __device__ __forceinline__ bool tri_test(const V3& o, const V3& d, float tMin, f
     return true;
 }
 
+// ---- 8-wide BVH with quantised boxes (layout in bvh_build.h) ---------------
+constexpr int kStack8 = 128;
+constexpr int kEmptyWide = 0x7fffffff;
+
+__device__ __forceinline__ float qbyte(uint32_t lo4, uint32_t hi4, int i) {
+    const uint32_t w = i < 4 ? lo4 : hi4;
+    return static_cast<float>((w >> (8 * (i & 3))) & 0xffu);
+}
+
+// Entry distances of the 8 children of a wide node (+inf for a miss or an
+// empty slot) and their links.
+__device__ __forceinline__ void wide_children(const DevScene& s, int node, const RayInv& r, float tmax, float t[8], int l[8]) {
+    const float4* np = s.nodes8 + 6 * static_cast<size_t>(node);
+    const float4 a = __ldg(np), l0 = __ldg(np + 1), l1 = __ldg(np + 2);
+    const float4 q0 = __ldg(np + 3), q1 = __ldg(np + 4), q2 = __ldg(np + 5);
+    const uint32_t eb = __float_as_uint(a.w);
+    const float sx = __uint_as_float((eb & 0xffu) << 23), sy = __uint_as_float(((eb >> 8) & 0xffu) << 23),
+                sz = __uint_as_float(((eb >> 16) & 0xffu) << 23);
+    // child plane = origin + q * scale:  t = q * (scale * inv) + (origin * inv - o * inv)
+    const float ax = sx * r.inv.x, ay = sy * r.inv.y, az = sz * r.inv.z;
+    const float bx = __fmaf_rn(a.x, r.inv.x, -r.ood.x), by = __fmaf_rn(a.y, r.inv.y, -r.ood.y),
+                bz = __fmaf_rn(a.z, r.inv.z, -r.ood.z);
+    const uint32_t qlx0 = __float_as_uint(q0.x), qlx1 = __float_as_uint(q0.y), qly0 = __float_as_uint(q0.z),
+                   qly1 = __float_as_uint(q0.w), qlz0 = __float_as_uint(q1.x), qlz1 = __float_as_uint(q1.y),
+                   qhx0 = __float_as_uint(q1.z), qhx1 = __float_as_uint(q1.w), qhy0 = __float_as_uint(q2.x),
+                   qhy1 = __float_as_uint(q2.y), qhz0 = __float_as_uint(q2.z), qhz1 = __float_as_uint(q2.w);
+    const int links[8] = {__float_as_int(l0.x), __float_as_int(l0.y), __float_as_int(l0.z), __float_as_int(l0.w),
+                          __float_as_int(l1.x), __float_as_int(l1.y), __float_as_int(l1.z), __float_as_int(l1.w)};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const float x0 = __fmaf_rn(qbyte(qlx0, qlx1, i), ax, bx), x1 = __fmaf_rn(qbyte(qhx0, qhx1, i), ax, bx);
+        const float y0 = __fmaf_rn(qbyte(qly0, qly1, i), ay, by), y1 = __fmaf_rn(qbyte(qhy0, qhy1, i), ay, by);
+        const float z0 = __fmaf_rn(qbyte(qlz0, qlz1, i), az, bz), z1 = __fmaf_rn(qbyte(qhz0, qhz1, i), az, bz);
+        const float lo = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.0f));
+        const float hi = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tmax));
+        const bool hit = links[i] != kEmptyWide && lo <= hi;
+        t[i] = hit ? lo : __int_as_float(0x7f800000);
+        l[i] = links[i];
+    }
+}
+
+__device__ __forceinline__ void cswap(float t[8], int l[8], int i, int j) {
+    const bool sw = t[j] < t[i];
+    const float ti = t[i], tj = t[j];
+    const int li = l[i], lj = l[j];
+    t[i] = sw ? tj : ti;
+    t[j] = sw ? ti : tj;
+    l[i] = sw ? lj : li;
+    l[j] = sw ? li : lj;
+}
+
+// 19-comparator sorting network for 8 entries (ascending distance).
+__device__ __forceinline__ void sort8(float t[8], int l[8]) {
+    cswap(t, l, 0, 2); cswap(t, l, 1, 3); cswap(t, l, 4, 6); cswap(t, l, 5, 7);
+    cswap(t, l, 0, 4); cswap(t, l, 1, 5); cswap(t, l, 2, 6); cswap(t, l, 3, 7);
+    cswap(t, l, 0, 1); cswap(t, l, 2, 3); cswap(t, l, 4, 5); cswap(t, l, 6, 7);
+    cswap(t, l, 2, 4); cswap(t, l, 3, 5);
+    cswap(t, l, 1, 4); cswap(t, l, 3, 6);
+    cswap(t, l, 1, 2); cswap(t, l, 3, 4); cswap(t, l, 5, 6);
+}
+
+template <typename Ctr>
+__device__ bool trace_closest8(const DevScene& s, const V3& o, const V3& d, HitRec* out, Ctr& ctr) {
+    const RayInv r = ray_inv(o, d);
+    float bestT = FLT_MAX;
+    uint32_t bestGid = 0xffffffffu, bestSlot = 0xffffffffu;
+    float bu = 0.0f, bv = 0.0f;
+    int stackLink[kStack8];
+    float stackT[kStack8];
+    int sp = 0;
+    int cur = 0;
+    uint32_t visits = 0;
+    for (;;) {
+        if (++visits > kMaxVisits) {
+            atomicOr(s.error, kErrTraversalLimit);
+            bestSlot = 0xffffffffu;
+            break;
+        }
+        if (cur >= 0) {
+            ctr.node();
+            float t[8];
+            int l[8];
+            wide_children(s, cur, r, bestT, t, l);
+            sort8(t, l);
+            if (sp + 8 > kStack8) {
+                atomicOr(s.error, kErrStackOverflow);
+                bestSlot = 0xffffffffu;
+                break;
+            }
+#pragma unroll
+            for (int i = 7; i >= 0; --i) {
+                if (t[i] <= bestT) {
+                    stackLink[sp] = l[i];
+                    stackT[sp] = t[i];
+                    ++sp;
+                }
+            }
+        } else {
+            const uint32_t enc = ~static_cast<uint32_t>(cur);
+            const uint32_t first = enc >> 3, cnt = (enc & 7u) + 1u;
+            for (uint32_t k = first; k < first + cnt; ++k) {
+                ctr.tri();
+                const float4* tp = s.tris + 3 * static_cast<size_t>(k);
+                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                float tt, u, v;
+                if (!tri_test(o, d, kRayEpsilon, FLT_MAX, a, b, c, &tt, &u, &v)) continue;
+                const uint32_t gid = __float_as_uint(a.w);
+                if (tt < bestT || (tt == bestT && gid < bestGid)) {
+                    bestT = tt;
+                    bestGid = gid;
+                    bestSlot = k;
+                    bu = u;
+                    bv = v;
+                }
+            }
+        }
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            if (stackT[sp] <= bestT) {
+                cur = stackLink[sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    out->t = bestT;
+    out->u = bu;
+    out->v = bv;
+    out->slot = bestSlot;
+    out->gid = bestGid;
+    return bestSlot != 0xffffffffu;
+}
+
+template <typename Ctr>
+__device__ bool trace_occluded8(const DevScene& s, const V3& o, const V3& d, float maxDist, Ctr& ctr) {
+    const RayInv r = ray_inv(o, d);
+    int stack[kStack8];
+    int sp = 0;
+    int cur = 0;
+    uint32_t visits = 0;
+    for (;;) {
+        if (++visits > kMaxVisits) {
+            atomicOr(s.error, kErrTraversalLimit);
+            return false;
+        }
+        if (cur >= 0) {
+            ctr.onode();
+            float t[8];
+            int l[8];
+            wide_children(s, cur, r, maxDist, t, l);
+            if (sp + 8 > kStack8) {
+                atomicOr(s.error, kErrStackOverflow);
+                return false;
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (t[i] <= maxDist) stack[sp++] = l[i];
+        } else {
+            const uint32_t enc = ~static_cast<uint32_t>(cur);
+            const uint32_t first = enc >> 3, cnt = (enc & 7u) + 1u;
+            for (uint32_t k = first; k < first + cnt; ++k) {
+                ctr.otri();
+                const float4* tp = s.tris + 3 * static_cast<size_t>(k);
+                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                float tt, u, v;
+                if (tri_test(o, d, kRayEpsilon, maxDist, a, b, c, &tt, &u, &v)) return true;
+            }
+        }
+        if (sp == 0) return false;
+        cur = stack[--sp];
+    }
+}
+
 template <typename Ctr>
 __device__ __noinline__ bool trace_closest(const DevScene& s, const V3 o, const V3 d, HitRec* out, Ctr& ctr) {
     ctr.closest();
+    if (s.nodes8) return trace_closest8(s, o, d, out, ctr);
     const RayInv r = ray_inv(o, d);
     float bestT = FLT_MAX;
     uint32_t bestGid = 0xffffffffu, bestSlot = 0xffffffffu;
@@ -206,6 +382,7 @@ __device__ __noinline__ bool trace_closest(const DevScene& s, const V3 o, const 
 template <typename Ctr>
 __device__ __noinline__ bool trace_occluded(const DevScene& s, const V3 o, const V3 d, float maxDist, Ctr& ctr) {
     ctr.occlusion();
+    if (s.nodes8) return trace_occluded8(s, o, d, maxDist, ctr);
     const RayInv r = ray_inv(o, d);
     int stackNode[kStack];
     int sp = 0;

@@ -181,3 +181,32 @@ def test_cancel(gpu):
     with pytest.raises(ShiroGpuError) as ei:
         gpu.render(w.scene, w.camera, w.settings, cancel=flag)
     assert ei.value.code == -6
+
+
+def test_bvh_widths_agree(gpu, port):
+    """The binary BVH (default) and the wide quantised BVH collapsed from it
+    return identical hits, distances and occlusion."""
+    from shiro_gb300 import scenes
+
+    scene = scenes.field_scene(instances=40, levels=4, materials=4, env_width=16, env_height=8, seed=33, plane=20.0)
+    rng = np.random.default_rng(8)
+    n = 60000
+    o = rng.uniform(-10, 10, (n, 3)).astype(np.float32)
+    o[:, 1] = rng.uniform(0.02, 4.0, n)
+    d = rng.normal(size=(n, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    tmax = rng.uniform(0.2, 40.0, n).astype(np.float32)
+    binary = gpu.trace_rays(scene, o, d, tmax)
+    gpu.set_bvh_width(8)
+    try:
+        wide = gpu.trace_rays(scene, o, d, tmax)
+        # a frame through the wide BVH equals the binary one bit for bit
+        w = scenes.sphere_workload(40, 32, 4, 8, env_width=64, env_height=32)
+        fw = gpu.render(w.scene, w.camera, w.settings)
+    finally:
+        gpu.set_bvh_width(2)
+    fb = gpu.render(w.scene, w.camera, w.settings)
+    assert np.array_equal(fw.beauty, fb.beauty)
+    brute = api.trace_rays(port, scene, o, d, tmax, bruteforce=True)
+    for a, b, c in zip(wide, binary, brute):
+        assert np.array_equal(a, b) and np.array_equal(a, c)
