@@ -60,6 +60,9 @@ struct WfRequest {
 constexpr uint32_t kFlagPrevDelta = 1u << 16;
 constexpr uint32_t kFlagDone = 1u << 17;
 
+// Work-fetch counters of the persistent stages (slots of WfView::counters).
+constexpr uint32_t kFetchExtend = 5, kFetchShade = 6, kFetchOcclude = 7;
+
 struct WfView {
     // path state, one entry per slot of the wave
     float4* ro;      // ro.xyz, unused
@@ -121,6 +124,9 @@ __global__ void wf_begin(WfView v) {
         v.counters[1] = 0u;
         v.counters[2] = 0u;
         v.counters[4] = 0u;
+        v.counters[kFetchExtend] = 0u;
+        v.counters[kFetchShade] = 0u;
+        v.counters[kFetchOcclude] = 0u;
     }
 }
 
@@ -147,11 +153,24 @@ __global__ void __launch_bounds__(128) wf_generate(WfView v) {
     }
 }
 
+// Persistent warps take their next 32 queue entries from a per-stage counter
+// (reset by wf_begin / wf_end_bounce), so rays of very different cost do not
+// leave an SM idle behind one slow block.  Returns the first entry for the warp.
+__device__ __forceinline__ uint32_t warp_fetch(uint32_t* counter) {
+    uint32_t base = 0;
+    if (lane_id() == 0) base = atomicAdd(counter, 32u);
+    return __shfl_sync(0xffffffffu, base, 0);
+}
+
 __global__ void __launch_bounds__(256) wf_extend(WfView v, DevScene s, uint32_t cur) {
     const uint32_t count = v.counters[cur];
     const uint32_t* q = cur ? v.rayQ1 : v.rayQ0;
     NullCounter ctr;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    for (;;) {
+        const uint32_t base = warp_fetch(&v.counters[kFetchExtend]);
+        if (base >= count) break;
+        const uint32_t i = base + lane_id();
+        if (i >= count) continue;
         const uint32_t j = q[i];
         const float4 o = v.ro[j], d = v.rd[j];
         HitRec h;
@@ -171,12 +190,12 @@ __global__ void __launch_bounds__(256) wf_shade(WfView v, DevScene s, uint32_t c
     uint32_t* qout = cur ? v.rayQ0 : v.rayQ1;
     uint32_t* cout = &v.counters[cur ^ 1u];
     NullCounter ctr;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    // every lane of a warp runs the same number of iterations so that the
-    // warp-aggregated pushes see the whole warp
-    const uint32_t iters = (count + stride - 1u) / stride;
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    for (uint32_t it = 0; it < iters; ++it, i += stride) {
+    // whole warps fetch work together, so the warp-aggregated pushes below
+    // always see the whole warp
+    for (;;) {
+        const uint32_t wbase = warp_fetch(&v.counters[kFetchShade]);
+        if (wbase >= count) break;
+        const uint32_t i = wbase + lane_id();
         const bool valid = i < count;
         bool pushRay = false, pushShadow = false;
         uint32_t lightMask = 0;
@@ -256,7 +275,11 @@ __global__ void __launch_bounds__(256) wf_shade(WfView v, DevScene s, uint32_t c
 __global__ void __launch_bounds__(256) wf_occlude(WfView v, DevScene s) {
     const uint32_t count = v.counters[4];
     NullCounter ctr;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    for (;;) {
+        const uint32_t base = warp_fetch(&v.counters[kFetchOcclude]);
+        if (base >= count) break;
+        const uint32_t i = base + lane_id();
+        if (i >= count) continue;
         const uint32_t item = v.shadowRayQ[i];
         const uint32_t j = item >> 3, k = item & 7u;
         const size_t e = static_cast<size_t>(k) * v.P + j;
@@ -290,6 +313,9 @@ __global__ void wf_end_bounce(WfView v, uint32_t cur) {
         v.counters[cur] = 0u;
         v.counters[2] = 0u;
         v.counters[4] = 0u;
+        v.counters[kFetchExtend] = 0u;
+        v.counters[kFetchShade] = 0u;
+        v.counters[kFetchOcclude] = 0u;
     }
 }
 
