@@ -233,7 +233,7 @@ __device__ __forceinline__ bool continue_path(const DevScene& s, const DevReques
     if (tw <= 0.0f) return false;
     const float sel = smp.next1d(base + 1u) * tw;
     const V2 ds = smp.next2d(base + 2u);
-    V3 next, f;
+    V3 next;
     float pdf;
     bool delta = false;
     const float rs = sel - 0.0f;
@@ -243,8 +243,6 @@ __device__ __forceinline__ bool continue_path(const DevScene& s, const DevReques
         next = cosine_hemisphere(v.n, ds);
         const float cpdf = sclamp(dot(v.n, next), 0.0f, 1.0f) * kInvPi;
         pdf = smax((rw / tw) * (1.0f * cpdf + 0.0f * 0.0f), 1.0e-6f);
-        ctr.bsdf_eval();
-        f = bsdf_eval(m, v.n, v.cn, v.view, next);
     } else {
         const bool coat = !(rs < v.w.diffuse + v.w.spec);
         if (ps.specDepth >= q.specularDepth) return false;
@@ -257,11 +255,13 @@ __device__ __forceinline__ bool continue_path(const DevScene& s, const DevReques
         const float rc = sclamp(dot(sn, next), 0.0f, 1.0f);
         if (rc <= 0.0f) return false;
         ctr.bsdf_pdf();
-        ctr.bsdf_eval();
         pdf = smax((rw / tw) * bsdf_pdf(m, v.w, v.n, v.cn, v.view, next), 1.0e-6f);
-        f = bsdf_eval(m, v.n, v.cn, v.view, next);
         delta = sr <= kDeltaRoughness;
     }
+    // one evaluation site for both lobes, so a warp whose lanes chose
+    // different lobes runs the BSDF once
+    ctr.bsdf_eval();
+    const V3 f = bsdf_eval(m, v.n, v.cn, v.view, next);
     const float cosT = sclamp(dot(v.n, next), 0.0f, 1.0f);
     if (cosT <= 0.0f) return false;
     ps.T = clamp12(q, ps.T * f * (cosT / pdf));

@@ -62,6 +62,9 @@ constexpr uint32_t kFlagDone = 1u << 17;
 
 // Work-fetch counters of the persistent stages (slots of WfView::counters).
 constexpr uint32_t kFetchExtend = 5, kFetchShade = 6, kFetchOcclude = 7;
+// Lengths of the two halves of the shade queue: hits fill it from the front,
+// misses from the back.
+constexpr uint32_t kHitCount = 8, kMissCount = 9;
 
 struct WfView {
     // path state, one entry per slot of the wave
@@ -81,7 +84,9 @@ struct WfView {
     uint32_t* rayQ1;
     uint32_t* shadowQ;     // paths with light samples to accumulate
     uint32_t* shadowRayQ;  // one item per light sample to test: slot << 3 | sample
-    uint32_t* counters;  // 0: ray count A, 1: ray count B, 2: shadow paths, 3: wave index, 4: shadow rays
+    uint32_t* shadeQ;      // rays after extend: hits from the front, misses from the back
+    uint32_t* counters;  // 0: ray count A, 1: ray count B, 2: shadow paths, 3: wave index, 4: shadow rays,
+                         // 5-7: work fetch, 8: hits, 9: misses
     float4* records;     // 3 per slot
     const WaveDesc* waves;
     const WaveSeg* segs;
@@ -127,6 +132,8 @@ __global__ void wf_begin(WfView v) {
         v.counters[kFetchExtend] = 0u;
         v.counters[kFetchShade] = 0u;
         v.counters[kFetchOcclude] = 0u;
+        v.counters[kHitCount] = 0u;
+        v.counters[kMissCount] = 0u;
     }
 }
 
@@ -162,7 +169,20 @@ __device__ __forceinline__ uint32_t warp_fetch(uint32_t* counter) {
     return __shfl_sync(0xffffffffu, base, 0);
 }
 
-__global__ void __launch_bounds__(256) wf_extend(WfView v, DevScene s, uint32_t cur) {
+// Claims a slot per predicated lane of the (converged) warp; one atomicAdd.
+__device__ __forceinline__ uint32_t warp_claim(uint32_t* counter, bool pred) {
+    const uint32_t ballot = __ballot_sync(0xffffffffu, pred);
+    uint32_t base = 0;
+    if (ballot != 0u && lane_id() == 0) base = atomicAdd(counter, static_cast<uint32_t>(__popc(ballot)));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return base + __popc(ballot & ((1u << lane_id()) - 1u));
+}
+
+// Closest hit of every queued ray.  The ray is then queued for shading with
+// the hits at the front of the shade queue and the misses at its back, so the
+// shade stage runs warps of hits and warps of misses instead of warps that
+// take both branches.
+__global__ void __launch_bounds__(256, 4) wf_extend(WfView v, DevScene s, uint32_t cur) {
     const uint32_t count = v.counters[cur];
     const uint32_t* q = cur ? v.rayQ1 : v.rayQ0;
     NullCounter ctr;
@@ -170,13 +190,21 @@ __global__ void __launch_bounds__(256) wf_extend(WfView v, DevScene s, uint32_t 
         const uint32_t base = warp_fetch(&v.counters[kFetchExtend]);
         if (base >= count) break;
         const uint32_t i = base + lane_id();
-        if (i >= count) continue;
-        const uint32_t j = q[i];
-        const float4 o = v.ro[j], d = v.rd[j];
-        HitRec h;
-        trace_closest(s, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, &h, ctr);
-        v.hit[j] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
-        v.hitGid[j] = h.gid;
+        const bool valid = i < count;
+        uint32_t j = 0;
+        bool hit = false;
+        if (valid) {
+            j = q[i];
+            const float4 o = v.ro[j], d = v.rd[j];
+            HitRec h;
+            trace_closest(s, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, &h, ctr);
+            v.hit[j] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+            v.hitGid[j] = h.gid;
+            hit = h.slot != 0xffffffffu;
+        }
+        const uint32_t hs = warp_claim(&v.counters[kHitCount], valid && hit);
+        const uint32_t ms = warp_claim(&v.counters[kMissCount], valid && !hit);
+        if (valid) v.shadeQ[hit ? hs : v.P - 1u - ms] = j;
     }
 }
 
@@ -185,13 +213,13 @@ __device__ __forceinline__ void write_record(const WfView& v, uint32_t j, const 
 }
 
 __global__ void __launch_bounds__(256) wf_shade(WfView v, DevScene s, uint32_t cur, uint32_t depth) {
-    const uint32_t count = v.counters[cur];
-    const uint32_t* qin = cur ? v.rayQ1 : v.rayQ0;
+    const uint32_t hits = v.counters[kHitCount];
+    const uint32_t count = hits + v.counters[kMissCount];
     uint32_t* qout = cur ? v.rayQ0 : v.rayQ1;
     uint32_t* cout = &v.counters[cur ^ 1u];
     NullCounter ctr;
     // whole warps fetch work together, so the warp-aggregated pushes below
-    // always see the whole warp
+    // always see the whole warp; entries [0, hits) are hits, the rest misses
     for (;;) {
         const uint32_t wbase = warp_fetch(&v.counters[kFetchShade]);
         if (wbase >= count) break;
@@ -201,7 +229,7 @@ __global__ void __launch_bounds__(256) wf_shade(WfView v, DevScene s, uint32_t c
         uint32_t lightMask = 0;
         uint32_t j = 0;
         if (valid) {
-            j = qin[i];
+            j = v.shadeQ[i < hits ? i : v.P - 1u - (i - hits)];
             const uint4 id = v.ident[j];
             const DevRequest& q = v.reqs[id.w].q;
             const float4 o = v.ro[j], d = v.rd[j], t4 = v.T[j], r4 = v.rad[j], h4 = v.hit[j];
@@ -316,6 +344,8 @@ __global__ void wf_end_bounce(WfView v, uint32_t cur) {
         v.counters[kFetchExtend] = 0u;
         v.counters[kFetchShade] = 0u;
         v.counters[kFetchOcclude] = 0u;
+        v.counters[kHitCount] = 0u;
+        v.counters[kMissCount] = 0u;
     }
 }
 
@@ -392,7 +422,7 @@ bool ensure_pool(ContextImpl* ctx, WavefrontState* wf, uint32_t P, uint32_t ligh
     const size_t p = P;
     const size_t stateBytes = p * (6 * sizeof(float4) + sizeof(uint32_t));
     const size_t shadowBytes = p * (2 + 2 * static_cast<size_t>(std::max(1u, lightSamples))) * sizeof(float4);
-    const size_t queueBytes = p * (3 + static_cast<size_t>(std::max(1u, lightSamples))) * sizeof(uint32_t) + 64;
+    const size_t queueBytes = p * (4 + static_cast<size_t>(std::max(1u, lightSamples))) * sizeof(uint32_t) + 64;
     const size_t recordBytes = p * 3 * sizeof(float4);
     if (!ensure_block(ctx, &wf->state, stateBytes, "wavefront state")) return false;
     if (!ensure_block(ctx, &wf->shadow, shadowBytes, "wavefront shadow records")) return false;
@@ -426,6 +456,7 @@ WfView make_view(WavefrontState* wf, uint32_t P, uint32_t lightSamples, const Wa
     v.rayQ1 = v.rayQ0 + p;
     v.shadowQ = v.rayQ1 + p;
     v.shadowRayQ = v.shadowQ + p;
+    v.shadeQ = v.shadowRayQ + p * static_cast<size_t>(std::max(1u, lightSamples));
     v.records = static_cast<float4*>(wf->records.ptr);
     v.waves = waves;
     v.segs = segs;
