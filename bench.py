@@ -60,6 +60,7 @@ def parse():
     p.add_argument("--height", type=int, default=0)
     p.add_argument("--spp", type=int, default=0)
     p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--bvh-width", type=int, choices=[2, 8], default=2, help="binary or compressed 8-wide BVH")
     return p.parse_args()
 
 
@@ -232,7 +233,7 @@ def cpu_baseline(w, seconds: float, rank: int = 0) -> dict:
             "cpu": cpu, "seconds": t_render, "paths": int(paths)}
 
 
-def adjoint_bench(local: int, iters: int = 5, warmup: int = 2) -> dict:
+def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 2) -> dict:
     """Gradient throughput of the differentiable form on the 256-material
     sphere scene: 512x512, 32 spp, depth 6, L2 loss against a seeded target,
     gradients for 256 x (base colour, roughness, metalness) and the 512x256x3
@@ -247,6 +248,7 @@ def adjoint_bench(local: int, iters: int = 5, warmup: int = 2) -> dict:
                         backend=1)
     cam = scenes.sphere_camera(1.0)
     gpu = GpuBackend(local)
+    gpu.set_bvh_width(bvh_width)
     stream = torch.cuda.current_stream()
     gpu.lib.shiro_gpu_set_stream(gpu.handle, stream.cuda_stream)
     gpu.upload_scene(scene)
@@ -331,6 +333,8 @@ def main():
     st = w.settings
     spp = st.samples_per_pixel
     gpu = GpuBackend(local)
+    gpu.set_bvh_width(args.bvh_width)
+    BYTES["node"] = 64 if args.bvh_width == 2 else 80
     stream = torch.cuda.current_stream()
     gpu.lib.shiro_gpu_set_stream(gpu.handle, stream.cuda_stream)
     t0 = time.perf_counter()
@@ -477,14 +481,14 @@ def main():
 
     adjoint = None
     if rank == 0 and not args.no_adjoint and args.workload == "field" and not (args.width or args.height or args.spp):
-        adjoint = adjoint_bench(local)
+        adjoint = adjoint_bench(local, bvh_width=args.bvh_width)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(w, args.cpu_seconds)
     if rank == 0:
         cfg = workload_config(w, "flushed (512 MiB memset between steps)")
-        cfg.update({"form": head, "parallelism": f"replicas x{world}", "scene_upload_s": upload_s,
+        cfg.update({"form": head, "parallelism": f"replicas x{world}", "scene_upload_s": upload_s, "bvh_width": args.bvh_width,
                     "bvh_nodes": int(stats["bvh_nodes"]), "bvh_depth": int(stats["bvh_depth"]),
                     "forms": {f: {"Mpaths_s": results[f]["value"], "ms_per_step": results[f]["ms"] / args.steps}
                               for f in forms}, "wavefront_config": tuned})

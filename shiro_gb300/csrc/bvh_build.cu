@@ -29,7 +29,7 @@ namespace {
 
 constexpr float kCostNode = 1.2f;
 constexpr float kCostTri = 1.0f;
-constexpr uint32_t kMaxLeaf = 8;
+constexpr uint32_t kMaxLeafLimit = 8;
 
 __device__ __forceinline__ uint32_t f2ord(float f) {
     const uint32_t u = __float_as_uint(f);
@@ -158,7 +158,7 @@ __global__ void k_bottom_up(int n, const uint32_t* __restrict__ sortedPrim, cons
                             const int2* __restrict__ child, const int* __restrict__ nodeParent,
                             const int* __restrict__ leafParent, unsigned int* __restrict__ arrivals,
                             float4* __restrict__ nodeBox, float* __restrict__ nodeCost, int* __restrict__ nodeCount,
-                            uint8_t* __restrict__ collapse) {
+                            uint8_t* __restrict__ collapse, int maxLeaf) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int node = leafParent[j];
@@ -193,7 +193,7 @@ __global__ void k_bottom_up(int n, const uint32_t* __restrict__ sortedPrim, cons
         const int count = cnt[0] + cnt[1];
         const float split = kCostNode * area + cost[0] + cost[1];
         const float leaf = kCostTri * area * static_cast<float>(count);
-        const bool asLeaf = count <= static_cast<int>(kMaxLeaf) && leaf <= split;
+        const bool asLeaf = count <= maxLeaf && leaf <= split;
         nodeBox[2 * node] = make_float4(u.lo[0], u.lo[1], u.lo[2], 0.0f);
         nodeBox[2 * node + 1] = make_float4(u.hi[0], u.hi[1], u.hi[2], 0.0f);
         nodeCount[node] = count;
@@ -317,6 +317,10 @@ int build_bvh(const BvhInput& in, cudaStream_t stream, BvhOutput* out, std::stri
         err = "too many triangles for the leaf encoding (2^28)";
         return SHIRO_ERR_INVALID_ARGUMENT;
     }
+    if (in.maxLeaf < 1 || in.maxLeaf > kMaxLeafLimit) {
+        err = "leaf size out of range [1, 8]";
+        return SHIRO_ERR_INVALID_ARGUMENT;
+    }
     Scratch sc;
     float4* triOut = nullptr;
     BVH_CHECK(cudaMalloc(&triOut, 3 * sizeof(float4) * static_cast<size_t>(total)));
@@ -380,7 +384,8 @@ int build_bvh(const BvhInput& in, cudaStream_t stream, BvhOutput* out, std::stri
             k_karras<<<blocks(nInternal, 256), 256, 0, stream>>>(keysOut, static_cast<int>(m), child, range, nodeParent,
                                                                   leafParent);
             k_bottom_up<<<blocks(m, 256), 256, 0, stream>>>(static_cast<int>(m), sortedPrim, in.primBoxes, child, nodeParent,
-                                                             leafParent, arrivals, nodeBox, nodeCost, nodeCount, collapse);
+                                                             leafParent, arrivals, nodeBox, nodeCost, nodeCount, collapse,
+                                                             static_cast<int>(in.maxLeaf));
             k_emit_flags<<<blocks(nInternal, 256), 256, 0, stream>>>(nInternal, nodeParent, collapse, flag, maxDepth);
             BVH_CHECK(cudaGetLastError());
             size_t scanBytes = 0;
@@ -462,14 +467,14 @@ int build_bvh(const BvhInput& in, cudaStream_t stream, BvhOutput* out, std::stri
     }
     BVH_CHECK(cudaStreamSynchronize(stream));
     out->depth = depthHost + offset + 1u;
-    out->maxLeaf = kMaxLeaf;
+    out->maxLeaf = in.maxLeaf;
     return SHIRO_OK;
 }
 
 namespace {
 
 struct Entry {
-    int link;
+    int link;  // >= 0 binary node, < 0 binary leaf link
     float lo[3], hi[3];
 };
 
@@ -477,6 +482,8 @@ __device__ __forceinline__ float entry_area(const Entry& e) {
     const float dx = e.hi[0] - e.lo[0], dy = e.hi[1] - e.lo[1], dz = e.hi[2] - e.lo[2];
     return 2.0f * (dx * dy + dy * dz + dz * dx);
 }
+
+__device__ __forceinline__ int leaf_count(int link) { return static_cast<int>((~static_cast<uint32_t>(link)) & 7u) + 1; }
 
 __device__ __forceinline__ void node2_children(const float4* nodes2, int n, Entry* a, Entry* b) {
     const float4 n0 = nodes2[4 * static_cast<size_t>(n)], n1 = nodes2[4 * static_cast<size_t>(n) + 1];
@@ -487,41 +494,58 @@ __device__ __forceinline__ void node2_children(const float4* nodes2, int n, Entr
     b->lo[0] = n1.x; b->hi[0] = n1.y; b->lo[1] = n1.z; b->hi[1] = n1.w; b->lo[2] = n2.z; b->hi[2] = n2.w;
 }
 
-// One thread per task (binary node -> wide node).  New internal children get
-// wide-node indices from `counter` and are appended to the next task list.
-__global__ void k_collapse8(const float4* __restrict__ nodes2, const int2* __restrict__ tasks, uint32_t taskCount,
-                            int2* __restrict__ nextTasks, unsigned int* __restrict__ nextCount,
-                            unsigned int* __restrict__ counter, float4* __restrict__ out) {
+// One thread per task (binary node -> wide node).  The wide node's internal
+// children get consecutive wide-node indices from `nodeCounter` and become
+// the next level's tasks; its leaf children's triangles get consecutive
+// slots of the wide triangle array from `triCounter` and are copied there.
+__global__ void k_collapse_wide(const float4* __restrict__ nodes2, const float4* __restrict__ tris2,
+                                const int2* __restrict__ tasks, uint32_t taskCount, int2* __restrict__ nextTasks,
+                                unsigned int* __restrict__ nextCount, unsigned int* __restrict__ nodeCounter,
+                                unsigned int* __restrict__ triCounter, float4* __restrict__ out,
+                                float4* __restrict__ trisOut) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= taskCount) return;
     const int2 task = tasks[t];
     Entry e[8];
-    int n = 0;
+    int n = 0, tris = 0;
     {
         Entry a, b;
         node2_children(nodes2, task.x, &a, &b);
         if (a.lo[0] <= a.hi[0]) e[n++] = a;
         if (b.lo[0] <= b.hi[0]) e[n++] = b;
+        for (int i = 0; i < n; ++i)
+            if (e[i].link < 0) tris += leaf_count(e[i].link);
     }
+    // open the largest internal child while there is a free slot and its
+    // leaf children fit the node's triangle bits
     while (n < 8) {
         int best = -1;
         float bestArea = -1.0f;
-        for (int i = 0; i < n; ++i)
-            if (e[i].link >= 0 && entry_area(e[i]) > bestArea) {
-                bestArea = entry_area(e[i]);
-                best = i;
-            }
+        Entry ba, bb;
+        for (int i = 0; i < n; ++i) {
+            if (e[i].link < 0 || entry_area(e[i]) <= bestArea) continue;
+            Entry a, b;
+            node2_children(nodes2, e[i].link, &a, &b);
+            int add = 0;
+            if (a.lo[0] <= a.hi[0] && a.link < 0) add += leaf_count(a.link);
+            if (b.lo[0] <= b.hi[0] && b.link < 0) add += leaf_count(b.link);
+            if (tris + add > static_cast<int>(kWideMaxTris)) continue;
+            bestArea = entry_area(e[i]);
+            best = i;
+            ba = a;
+            bb = b;
+        }
         if (best < 0) break;
-        Entry a, b;
-        node2_children(nodes2, e[best].link, &a, &b);
-        const bool va = a.lo[0] <= a.hi[0], vb = b.lo[0] <= b.hi[0];
+        const bool va = ba.lo[0] <= ba.hi[0], vb = bb.lo[0] <= bb.hi[0];
+        if (va && ba.link < 0) tris += leaf_count(ba.link);
+        if (vb && bb.link < 0) tris += leaf_count(bb.link);
         if (va && vb) {
-            e[best] = a;
-            e[n++] = b;
+            e[best] = ba;
+            e[n++] = bb;
         } else if (va) {
-            e[best] = a;
+            e[best] = ba;
         } else if (vb) {
-            e[best] = b;
+            e[best] = bb;
         } else {
             e[best] = e[--n];
         }
@@ -532,6 +556,36 @@ __global__ void k_collapse8(const float4* __restrict__ nodes2, const int2* __res
             lo[k] = fminf(lo[k], e[i].lo[k]);
             hi[k] = fmaxf(hi[k], e[i].hi[k]);
         }
+    // slot s takes the child lying most in direction D(s) from the centre
+    // (greedy assignment by decreasing projection)
+    int slotOf[8];
+    int childIn[8];
+    for (int s = 0; s < 8; ++s) childIn[s] = -1;
+    {
+        float proj[8][8];
+        for (int i = 0; i < n; ++i) {
+            float c[3];
+            for (int k = 0; k < 3; ++k) c[k] = 0.5f * (e[i].lo[k] + e[i].hi[k]) - 0.5f * (lo[k] + hi[k]);
+            for (int s = 0; s < 8; ++s)
+                proj[i][s] = ((s & 1) ? -c[0] : c[0]) + ((s & 2) ? -c[1] : c[1]) + ((s & 4) ? -c[2] : c[2]);
+            slotOf[i] = -1;
+        }
+        for (int r = 0; r < n; ++r) {
+            int bi = -1, bs = -1;
+            float bv = -FLT_MAX;
+            for (int i = 0; i < n; ++i) {
+                if (slotOf[i] >= 0) continue;
+                for (int s = 0; s < 8; ++s)
+                    if (childIn[s] < 0 && (bi < 0 || proj[i][s] > bv)) {
+                        bv = proj[i][s];
+                        bi = i;
+                        bs = s;
+                    }
+            }
+            slotOf[bi] = bs;
+            childIn[bs] = bi;
+        }
+    }
     // per axis a power-of-two scale with extent / scale <= 255
     uint32_t ex[3];
     float sc[3];
@@ -550,68 +604,91 @@ __global__ void k_collapse8(const float4* __restrict__ nodes2, const int2* __res
             sc[k] = __uint_as_float(ex[k] << 23);
         }
     }
+    int inner = 0;
+    for (int i = 0; i < n; ++i) inner += e[i].link >= 0 ? 1 : 0;
+    const uint32_t childBase = inner ? atomicAdd(nodeCounter, static_cast<unsigned int>(inner)) : 0u;
+    const uint32_t triBase = tris ? atomicAdd(triCounter, static_cast<unsigned int>(tris)) : 0u;
     uint8_t q[6][8];
-    int links[8];
-    for (int i = 0; i < 8; ++i) {
-        if (i >= n) {
-            links[i] = kEmptyChild;
+    uint8_t meta[8];
+    uint32_t imask = 0;
+    int rank = 0, off = 0;
+    for (int s = 0; s < 8; ++s) {
+        const int i = childIn[s];
+        if (i < 0) {
+            meta[s] = static_cast<uint8_t>(kWideEmptyMeta);
             for (int k = 0; k < 3; ++k) {
-                q[k][i] = 255;
-                q[3 + k][i] = 0;
+                q[k][s] = 255;
+                q[3 + k][s] = 0;
             }
             continue;
         }
         for (int k = 0; k < 3; ++k) {
             const float a = floorf(__fdiv_rd(__fsub_rd(e[i].lo[k], lo[k]), sc[k]));
             const float b = ceilf(__fdiv_ru(__fsub_ru(e[i].hi[k], lo[k]), sc[k]));
-            q[k][i] = static_cast<uint8_t>(fminf(fmaxf(a, 0.0f), 255.0f));
-            q[3 + k][i] = static_cast<uint8_t>(fminf(fmaxf(b, 0.0f), 255.0f));
+            q[k][s] = static_cast<uint8_t>(fminf(fmaxf(a, 0.0f), 255.0f));
+            q[3 + k][s] = static_cast<uint8_t>(fminf(fmaxf(b, 0.0f), 255.0f));
         }
         if (e[i].link >= 0) {
-            const int child = static_cast<int>(atomicAdd(counter, 1u));
+            imask |= 1u << s;
+            meta[s] = 0;
             const unsigned int slot = atomicAdd(nextCount, 1u);
-            nextTasks[slot] = make_int2(e[i].link, child);
-            links[i] = child;
+            nextTasks[slot] = make_int2(e[i].link, static_cast<int>(childBase) + rank);
+            ++rank;
         } else {
-            links[i] = e[i].link;
+            const uint32_t enc = ~static_cast<uint32_t>(e[i].link);
+            const uint32_t first = enc >> 3, cnt = (enc & 7u) + 1u;
+            meta[s] = static_cast<uint8_t>(((cnt - 1u) << 5) | static_cast<uint32_t>(off));
+            for (uint32_t k = 0; k < cnt; ++k) {
+                const size_t src = 3 * static_cast<size_t>(first + k), dst = 3 * (static_cast<size_t>(triBase) + off + k);
+                trisOut[dst] = tris2[src];
+                trisOut[dst + 1] = tris2[src + 1];
+                trisOut[dst + 2] = tris2[src + 2];
+            }
+            off += static_cast<int>(cnt);
         }
     }
-    float4* o = out + 6 * static_cast<size_t>(task.y);
-    o[0] = make_float4(lo[0], lo[1], lo[2], __uint_as_float(ex[0] | (ex[1] << 8) | (ex[2] << 16)));
-    o[1] = make_float4(__int_as_float(links[0]), __int_as_float(links[1]), __int_as_float(links[2]), __int_as_float(links[3]));
-    o[2] = make_float4(__int_as_float(links[4]), __int_as_float(links[5]), __int_as_float(links[6]), __int_as_float(links[7]));
+    float4* o = out + 5 * static_cast<size_t>(task.y);
+    o[0] = make_float4(lo[0], lo[1], lo[2], __uint_as_float(ex[0] | (ex[1] << 8) | (ex[2] << 16) | (imask << 24)));
+    const uint32_t m0 = meta[0] | (meta[1] << 8) | (meta[2] << 16) | (static_cast<uint32_t>(meta[3]) << 24);
+    const uint32_t m1 = meta[4] | (meta[5] << 8) | (meta[6] << 16) | (static_cast<uint32_t>(meta[7]) << 24);
+    o[1] = make_float4(__uint_as_float(childBase), __uint_as_float(triBase), __uint_as_float(m0), __uint_as_float(m1));
     uint32_t w[12];
     for (int r = 0; r < 6; ++r) {
         w[2 * r] = q[r][0] | (q[r][1] << 8) | (q[r][2] << 16) | (static_cast<uint32_t>(q[r][3]) << 24);
         w[2 * r + 1] = q[r][4] | (q[r][5] << 8) | (q[r][6] << 16) | (static_cast<uint32_t>(q[r][7]) << 24);
     }
-    o[3] = make_float4(__uint_as_float(w[0]), __uint_as_float(w[1]), __uint_as_float(w[2]), __uint_as_float(w[3]));
-    o[4] = make_float4(__uint_as_float(w[4]), __uint_as_float(w[5]), __uint_as_float(w[6]), __uint_as_float(w[7]));
-    o[5] = make_float4(__uint_as_float(w[8]), __uint_as_float(w[9]), __uint_as_float(w[10]), __uint_as_float(w[11]));
+    o[2] = make_float4(__uint_as_float(w[0]), __uint_as_float(w[1]), __uint_as_float(w[2]), __uint_as_float(w[3]));
+    o[3] = make_float4(__uint_as_float(w[4]), __uint_as_float(w[5]), __uint_as_float(w[6]), __uint_as_float(w[7]));
+    o[4] = make_float4(__uint_as_float(w[8]), __uint_as_float(w[9]), __uint_as_float(w[10]), __uint_as_float(w[11]));
 }
 
 }  // namespace
 
-int collapse_bvh8(const float4* nodes2, uint32_t nodeCount2, cudaStream_t stream, Bvh8Output* out, std::string& err) {
+int collapse_wide(const float4* nodes2, uint32_t nodeCount2, const float4* tris2, uint32_t triCount2, cudaStream_t stream,
+                  WideOutput* out, std::string& err) {
     Scratch sc;
     int2 *ta = nullptr, *tb = nullptr;
-    unsigned int* cnt = nullptr;  // [0] node counter, [1] next task count
+    unsigned int* cnt = nullptr;  // [0] node counter, [1] next task count, [2] triangle counter
     const uint32_t cap = std::max<uint32_t>(nodeCount2, 1);
     BVH_CHECK(sc.alloc(&ta, cap));
     BVH_CHECK(sc.alloc(&tb, cap));
-    BVH_CHECK(sc.alloc(&cnt, 2));
+    BVH_CHECK(sc.alloc(&cnt, 3));
     float4* nodes = nullptr;
-    BVH_CHECK(cudaMalloc(&nodes, 6 * sizeof(float4) * static_cast<size_t>(cap)));
+    BVH_CHECK(cudaMalloc(&nodes, 5 * sizeof(float4) * static_cast<size_t>(cap)));
     out->nodes = nodes;
+    float4* tris = nullptr;
+    BVH_CHECK(cudaMalloc(&tris, 3 * sizeof(float4) * static_cast<size_t>(std::max<uint32_t>(triCount2, 1))));
+    out->tris = tris;
     const int2 root = make_int2(0, 0);
-    const unsigned int init[2] = {1u, 0u};
+    const unsigned int init[3] = {1u, 0u, 0u};
     BVH_CHECK(cudaMemcpyAsync(ta, &root, sizeof(root), cudaMemcpyHostToDevice, stream));
     BVH_CHECK(cudaMemcpyAsync(cnt, init, sizeof(init), cudaMemcpyHostToDevice, stream));
     uint32_t tasks = 1, depth = 0;
+    unsigned int h[3] = {0, 0, 0};
     while (tasks > 0) {
-        k_collapse8<<<blocks(tasks, 128), 128, 0, stream>>>(nodes2, ta, tasks, tb, cnt + 1, cnt, nodes);
+        k_collapse_wide<<<blocks(tasks, 128), 128, 0, stream>>>(nodes2, tris2, ta, tasks, tb, cnt + 1, cnt, cnt + 2, nodes,
+                                                                 tris);
         BVH_CHECK(cudaGetLastError());
-        unsigned int h[2];
         BVH_CHECK(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, stream));
         BVH_CHECK(cudaMemsetAsync(cnt + 1, 0, sizeof(unsigned int), stream));
         BVH_CHECK(cudaStreamSynchronize(stream));
@@ -624,6 +701,11 @@ int collapse_bvh8(const float4* nodes2, uint32_t nodeCount2, cudaStream_t stream
             return SHIRO_ERR_INVALID_ARGUMENT;
         }
     }
+    if (h[2] != triCount2) {
+        err = "wide BVH collapse lost triangles";
+        return SHIRO_ERR_INVALID_ARGUMENT;
+    }
+    out->triCount = h[2];
     out->depth = depth;
     return SHIRO_OK;
 }

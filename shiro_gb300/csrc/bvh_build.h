@@ -22,6 +22,7 @@ struct BvhInput {
     const float4* centroids;  // device, 1 per small triangle
     uint32_t smallCount;
     std::vector<LargeTri> largeSlots;  // at most 8
+    uint32_t maxLeaf = 8;              // largest SAH leaf (1..8)
 };
 
 struct BvhOutput {
@@ -35,26 +36,40 @@ struct BvhOutput {
 
 inline int leaf_link_host(int first, int count) { return ~((first << 3) | (count - 1)); }
 
-// 8-wide BVH with quantised child boxes, collapsed from the binary BVH.
-// Node layout (96 B = 6 x float4):
-//   [0] origin.xyz, bits: ex | ey << 8 | ez << 16 (biased float exponents of
-//       the per-axis power-of-two scales)
-//   [1] child links 0-3, [2] child links 4-7: >= 0 wide node index, < 0 the
-//       binary BVH's leaf link ~((first << 3) | (count - 1)), kEmptyChild empty
-//   [3..5] 8 x (qlo.x, qlo.y, qlo.z, qhi.x, qhi.y, qhi.z) bytes, stored as
-//       qlo.x[8] qlo.y[8] qlo.z[8] qhi.x[8] qhi.y[8] qhi.z[8]; a child box is
-//       origin + q * scale, rounded outward at build time.
-constexpr int kEmptyChild = 0x7fffffff;
+// Compressed 8-wide BVH (after Ylitie, Karras and Laine, "Efficient
+// incoherent ray traversal on GPUs through compressed wide BVHs", HPG 2017),
+// collapsed from a binary BVH.  Node layout (80 B = 5 x float4):
+//   [0] origin.xyz, bits: ex | ey << 8 | ez << 16 | imask << 24; ex..ez are
+//       biased float exponents of the per-axis power-of-two scales, imask
+//       bit i marks child slot i as an internal node
+//   [1] childBase, triBase, meta[0..3], meta[4..7]: internal children are
+//       wide nodes childBase + (number of internal children in lower slots);
+//       a leaf child's meta byte is (count - 1) << 5 | offset, its triangles
+//       are triBase + offset .. + count - 1 of the wide BVH's own triangle
+//       array (offset + count <= 32); an empty slot has meta 0xff
+//   [2..4] qlo.x[8] qlo.y[8] qlo.z[8] qhi.x[8] qhi.y[8] qhi.z[8] bytes; a
+//       child box is origin + q * scale, rounded outward at build time
+// Child slot s holds the child lying most in direction
+// ((s & 1) ? -x : +x, (s & 2) ? -y : +y, (s & 4) ? -z : +z) from the node
+// centre, so a ray visits slots in the order of s ^ (7 ^ octant) to go
+// roughly front to back without sorting.
+constexpr uint32_t kWideEmptyMeta = 0xffu;
+constexpr uint32_t kWideMaxTris = 32;  // triangle bits of one node
+constexpr uint32_t kWideLeaf = 3;      // SAH leaf size of the binary tree the wide BVH is collapsed from
 
-struct Bvh8Output {
-    float4* nodes = nullptr;  // cudaMalloc'ed, 6 float4 per node
+struct WideOutput {
+    float4* nodes = nullptr;  // cudaMalloc'ed, 5 float4 per node
     uint32_t nodeCount = 0;
+    float4* tris = nullptr;   // cudaMalloc'ed, 3 float4 per triangle, wide-leaf order
+    uint32_t triCount = 0;
     uint32_t depth = 0;
 };
 
-// Collapses the binary BVH (scene.cuh layout, root = node 0) into 8-wide
-// nodes by repeatedly opening the largest-area internal child.
-int collapse_bvh8(const float4* nodes2, uint32_t nodeCount2, cudaStream_t stream, Bvh8Output* out, std::string& err);
+// Collapses a binary BVH (scene.cuh layout, root = node 0, leaves of at most
+// 8 triangles in `tris2`) into compressed wide nodes by repeatedly opening
+// the largest-area internal child while the node's triangle budget allows.
+int collapse_wide(const float4* nodes2, uint32_t nodeCount2, const float4* tris2, uint32_t triCount2, cudaStream_t stream,
+                  WideOutput* out, std::string& err);
 
 int build_bvh(const BvhInput& in, cudaStream_t stream, BvhOutput* out, std::string& err);
 

@@ -67,6 +67,7 @@ constexpr uint32_t kDirectSampleStride = 2u;
 
 // Entries of the per-thread BVH traversal stack (the builder rejects deeper trees).
 constexpr int kStack = 96;
+constexpr int kStackWide = 64;  // entries of the wide-BVH traversal stack (one per level at most)
 
 // Device-side error bits (ShiroGpu error word).
 constexpr uint32_t kErrTraversalLimit = 1u;

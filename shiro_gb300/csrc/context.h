@@ -47,6 +47,8 @@ struct ContextImpl {
     uint32_t materialCount = 0;        // user materials (the default one follows)
     uint32_t bvhDepth = 0, bvhMaxLeaf = 0;
     const float4* nodes8 = nullptr;   // wide BVH (kept even while the binary one is selected)
+    const float4* tris8 = nullptr;    // triangles in the wide BVH's leaf order
+    const float4* tris2 = nullptr;    // triangles in the binary BVH's leaf order
     uint32_t node8Count = 0, bvh8Depth = 0;
     // 2: traverse the binary BVH (default, measured faster on GB300 for
     // L2-resident scenes), 8: the wide quantised BVH

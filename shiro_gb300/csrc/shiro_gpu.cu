@@ -125,6 +125,7 @@ void ContextImpl::freeScene() {
     materialsHost.clear();
     hasScene = false;
     scene = DevScene{};
+    nodes8 = tris8 = tris2 = nullptr;
 }
 
 size_t ContextImpl::deviceBytes() const {
@@ -445,6 +446,8 @@ int shiro_gpu_set_bvh_width(ShiroGpuContext* ctx, uint32_t width) {
     ContextImpl& c = ctx->impl;
     c.bvhWidth = width;
     c.scene.nodes8 = (width == 8 && c.hasScene) ? c.nodes8 : nullptr;
+    // hit slots index the triangle array of the BVH that produced them
+    if (c.hasScene) c.scene.tris = c.scene.nodes8 ? c.tris8 : c.tris2;
     if (c.hasScene) {
         c.stats.bvh_nodes = c.scene.nodes8 ? c.node8Count : c.scene.nodeCount;
         c.stats.bvh_depth = c.scene.nodes8 ? c.bvh8Depth : c.bvhDepth;
@@ -608,36 +611,58 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     bin.primBoxes = dBox;
     bin.centroids = dCen;
     bin.smallCount = static_cast<uint32_t>(centroids.size());
-    BvhOutput bout;
+    BvhOutput bout, bwide;
     std::string berr;
     rc = build_bvh(bin, ctx->stream, &bout, berr);
+    // the wide BVH is collapsed from a binary tree with small leaves (the
+    // node's triangle bits bound the leaves it can hold)
+    if (rc == SHIRO_OK) {
+        BvhInput small = bin;
+        small.maxLeaf = kWideLeaf;
+        rc = build_bvh(small, ctx->stream, &bwide, berr);
+    }
     // staging blocks are no longer needed
     for (int k = 0; k < 3; ++k) {
         free_block(&ctx->sceneBlocks.back());
         ctx->sceneBlocks.pop_back();
     }
+    auto drop = [](BvhOutput& b) {
+        if (b.nodes) cudaFree(b.nodes);
+        if (b.tris) cudaFree(b.tris);
+        b.nodes = nullptr;
+        b.tris = nullptr;
+    };
     if (rc != SHIRO_OK) {
-        if (bout.nodes) cudaFree(bout.nodes);
-        if (bout.tris) cudaFree(bout.tris);
+        drop(bout);
+        drop(bwide);
         return fail(ctx, rc, "BVH build: " + berr);
     }
     if (bout.depth + 4 > static_cast<uint32_t>(kStack)) {
-        cudaFree(bout.nodes);
-        cudaFree(bout.tris);
+        drop(bout);
+        drop(bwide);
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "BVH deeper than the traversal stack");
     }
     ctx->sceneBlocks.push_back({bout.nodes, 4 * sizeof(float4) * bout.nodeCount});
     ctx->sceneBlocks.push_back({bout.tris, 3 * sizeof(float4) * bout.triCount});
-    Bvh8Output b8;
-    rc = collapse_bvh8(bout.nodes, bout.nodeCount, ctx->stream, &b8, berr);
+    WideOutput w8;
+    rc = collapse_wide(bwide.nodes, bwide.nodeCount, bwide.tris, bwide.triCount, ctx->stream, &w8, berr);
+    drop(bwide);
+    if (rc == SHIRO_OK && w8.depth > static_cast<uint32_t>(kStackWide)) {
+        rc = SHIRO_ERR_INVALID_ARGUMENT;
+        berr = "deeper than the traversal stack";
+    }
     if (rc != SHIRO_OK) {
-        if (b8.nodes) cudaFree(b8.nodes);
+        if (w8.nodes) cudaFree(w8.nodes);
+        if (w8.tris) cudaFree(w8.tris);
         return fail(ctx, rc, "wide BVH: " + berr);
     }
-    ctx->sceneBlocks.push_back({b8.nodes, 6 * sizeof(float4) * std::max<uint32_t>(bout.nodeCount, 1)});
-    ctx->nodes8 = b8.nodes;
-    ctx->node8Count = b8.nodeCount;
-    ctx->bvh8Depth = b8.depth;
+    ctx->sceneBlocks.push_back({w8.nodes, 5 * sizeof(float4) * std::max<uint32_t>(bwide.nodeCount, 1)});
+    ctx->sceneBlocks.push_back({w8.tris, 3 * sizeof(float4) * std::max<uint32_t>(w8.triCount, 1)});
+    ctx->nodes8 = w8.nodes;
+    ctx->tris8 = w8.tris;
+    ctx->tris2 = bout.tris;
+    ctx->node8Count = w8.nodeCount;
+    ctx->bvh8Depth = w8.depth;
     ctx->bvhDepth = bout.depth;
     ctx->bvhMaxLeaf = bout.maxLeaf;
     DevScene& s = ctx->scene;
@@ -646,6 +671,7 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     s.nodeCount = bout.nodeCount;
     s.triCount = bout.triCount;
     s.nodes8 = ctx->bvhWidth == 8 ? ctx->nodes8 : nullptr;
+    s.tris = s.nodes8 ? ctx->tris8 : ctx->tris2;
 
     // --- shading data ----------------------------------------------------------
     ctx->materialsHost.assign(sd->materials, sd->materials + sd->material_count);

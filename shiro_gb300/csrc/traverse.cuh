@@ -23,6 +23,7 @@ namespace shiro_gpu {
 
 
 constexpr uint32_t kMaxVisits = 1u << 22;
+constexpr uint32_t kWideEmptyMetaDev = 0xffu;  // empty slot of a wide node (bvh_build.h)
 
 // Work counters of the roofline probe (shiro_gpu_count_work).  NullCounter
 // compiles every increment away in the render kernels.
@@ -116,21 +117,18 @@ __device__ __forceinline__ bool tri_test(const V3& o, const V3& d, float tMin, f
     return true;
 }
 
-// ---- 8-wide BVH with quantised boxes (layout in bvh_build.h) ---------------
-constexpr int kStack8 = 128;
-constexpr int kEmptyWide = 0x7fffffff;
+// ---- compressed 8-wide BVH (layout in bvh_build.h) -------------------------
 
-__device__ __forceinline__ float qbyte(uint32_t lo4, uint32_t hi4, int i) {
-    const uint32_t w = i < 4 ? lo4 : hi4;
-    return static_cast<float>((w >> (8 * (i & 3))) & 0xffu);
-}
 
-// Entry distances of the 8 children of a wide node (+inf for a miss or an
-// empty slot) and their links.
-__device__ __forceinline__ void wide_children(const DevScene& s, int node, const RayInv& r, float tmax, float t[8], int l[8]) {
-    const float4* np = s.nodes8 + 6 * static_cast<size_t>(node);
-    const float4 a = __ldg(np), l0 = __ldg(np + 1), l1 = __ldg(np + 2);
-    const float4 q0 = __ldg(np + 3), q1 = __ldg(np + 4), q2 = __ldg(np + 5);
+// Children of wide node `node` hit within [0, tmax]: internal ones as bits
+// (slot ^ octInv) of *inner (nearest first = lowest bit), leaf triangles as
+// bits of *tris relative to *triBase.
+__device__ __forceinline__ void wide_node(const DevScene& s, uint32_t node, const RayInv& r, float tmax, uint32_t octInv,
+                                          uint32_t* childBase, uint32_t* imask, uint32_t* inner, uint32_t* triBase,
+                                          uint32_t* tris) {
+    const float4* np = s.nodes8 + 5 * static_cast<size_t>(node);
+    const float4 a = __ldg(np), b = __ldg(np + 1);
+    const float4 q0 = __ldg(np + 2), q1 = __ldg(np + 3), q2 = __ldg(np + 4);
     const uint32_t eb = __float_as_uint(a.w);
     const float sx = __uint_as_float((eb & 0xffu) << 23), sy = __uint_as_float(((eb >> 8) & 0xffu) << 23),
                 sz = __uint_as_float(((eb >> 16) & 0xffu) << 23);
@@ -138,110 +136,101 @@ __device__ __forceinline__ void wide_children(const DevScene& s, int node, const
     const float ax = sx * r.inv.x, ay = sy * r.inv.y, az = sz * r.inv.z;
     const float bx = __fmaf_rn(a.x, r.inv.x, -r.ood.x), by = __fmaf_rn(a.y, r.inv.y, -r.ood.y),
                 bz = __fmaf_rn(a.z, r.inv.z, -r.ood.z);
-    const uint32_t qlx0 = __float_as_uint(q0.x), qlx1 = __float_as_uint(q0.y), qly0 = __float_as_uint(q0.z),
-                   qly1 = __float_as_uint(q0.w), qlz0 = __float_as_uint(q1.x), qlz1 = __float_as_uint(q1.y),
-                   qhx0 = __float_as_uint(q1.z), qhx1 = __float_as_uint(q1.w), qhy0 = __float_as_uint(q2.x),
-                   qhy1 = __float_as_uint(q2.y), qhz0 = __float_as_uint(q2.z), qhz1 = __float_as_uint(q2.w);
-    const int links[8] = {__float_as_int(l0.x), __float_as_int(l0.y), __float_as_int(l0.z), __float_as_int(l0.w),
-                          __float_as_int(l1.x), __float_as_int(l1.y), __float_as_int(l1.z), __float_as_int(l1.w)};
+    const uint32_t im = eb >> 24;
+    const uint32_t m[2] = {__float_as_uint(b.z), __float_as_uint(b.w)};
+    const uint32_t qw[12] = {__float_as_uint(q0.x), __float_as_uint(q0.y), __float_as_uint(q0.z), __float_as_uint(q0.w),
+                             __float_as_uint(q1.x), __float_as_uint(q1.y), __float_as_uint(q1.z), __float_as_uint(q1.w),
+                             __float_as_uint(q2.x), __float_as_uint(q2.y), __float_as_uint(q2.z), __float_as_uint(q2.w)};
+    uint32_t hitsInner = 0, hitsTris = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        const float x0 = __fmaf_rn(qbyte(qlx0, qlx1, i), ax, bx), x1 = __fmaf_rn(qbyte(qhx0, qhx1, i), ax, bx);
-        const float y0 = __fmaf_rn(qbyte(qly0, qly1, i), ay, by), y1 = __fmaf_rn(qbyte(qhy0, qhy1, i), ay, by);
-        const float z0 = __fmaf_rn(qbyte(qlz0, qlz1, i), az, bz), z1 = __fmaf_rn(qbyte(qhz0, qhz1, i), az, bz);
+        const int h = i >> 2;
+        // byte i of a word pair as the float 2^23 + q, minus 2^23 exactly
+        const uint32_t sel = static_cast<uint32_t>(i & 3) | 0x7540u;
+        const float x0 = __fmaf_rn(__uint_as_float(__byte_perm(qw[0 + h], 0x4b000000u, sel)) - 8388608.0f, ax, bx);
+        const float y0 = __fmaf_rn(__uint_as_float(__byte_perm(qw[2 + h], 0x4b000000u, sel)) - 8388608.0f, ay, by);
+        const float z0 = __fmaf_rn(__uint_as_float(__byte_perm(qw[4 + h], 0x4b000000u, sel)) - 8388608.0f, az, bz);
+        const float x1 = __fmaf_rn(__uint_as_float(__byte_perm(qw[6 + h], 0x4b000000u, sel)) - 8388608.0f, ax, bx);
+        const float y1 = __fmaf_rn(__uint_as_float(__byte_perm(qw[8 + h], 0x4b000000u, sel)) - 8388608.0f, ay, by);
+        const float z1 = __fmaf_rn(__uint_as_float(__byte_perm(qw[10 + h], 0x4b000000u, sel)) - 8388608.0f, az, bz);
         const float lo = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.0f));
         const float hi = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tmax));
-        const bool hit = links[i] != kEmptyWide && lo <= hi;
-        t[i] = hit ? lo : __int_as_float(0x7f800000);
-        l[i] = links[i];
+        const uint32_t meta = (m[h] >> (8 * (i & 3))) & 0xffu;
+        if (lo <= hi) {
+            if ((im >> i) & 1u) {
+                hitsInner |= 1u << (static_cast<uint32_t>(i) ^ octInv);
+            } else if (meta != kWideEmptyMetaDev) {
+                hitsTris |= ((2u << (meta >> 5)) - 1u) << (meta & 31u);
+            }
+        }
     }
+    *childBase = __float_as_uint(b.x);
+    *triBase = __float_as_uint(b.y);
+    *imask = im;
+    *inner = hitsInner;
+    *tris = hitsTris;
 }
 
-__device__ __forceinline__ void cswap(float t[8], int l[8], int i, int j) {
-    const bool sw = t[j] < t[i];
-    const float ti = t[i], tj = t[j];
-    const int li = l[i], lj = l[j];
-    t[i] = sw ? tj : ti;
-    t[j] = sw ? ti : tj;
-    l[i] = sw ? lj : li;
-    l[j] = sw ? li : lj;
+__device__ __forceinline__ uint32_t ray_oct_inv(const V3& d) {
+    return 7u ^ ((d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u));
 }
 
-// 19-comparator sorting network for 8 entries (ascending distance).
-__device__ __forceinline__ void sort8(float t[8], int l[8]) {
-    cswap(t, l, 0, 2); cswap(t, l, 1, 3); cswap(t, l, 4, 6); cswap(t, l, 5, 7);
-    cswap(t, l, 0, 4); cswap(t, l, 1, 5); cswap(t, l, 2, 6); cswap(t, l, 3, 7);
-    cswap(t, l, 0, 1); cswap(t, l, 2, 3); cswap(t, l, 4, 5); cswap(t, l, 6, 7);
-    cswap(t, l, 2, 4); cswap(t, l, 3, 5);
-    cswap(t, l, 1, 4); cswap(t, l, 3, 6);
-    cswap(t, l, 1, 2); cswap(t, l, 3, 4); cswap(t, l, 5, 6);
-}
-
+// Stack entries are groups of sibling wide nodes still to visit:
+// (childBase, remaining inner bits << 8 | imask).
 template <typename Ctr>
-__device__ bool trace_closest8(const DevScene& s, const V3& o, const V3& d, HitRec* out, Ctr& ctr) {
+__device__ bool trace_closest_wide(const DevScene& s, const V3& o, const V3& d, HitRec* out, Ctr& ctr) {
     const RayInv r = ray_inv(o, d);
+    const uint32_t octInv = ray_oct_inv(d);
     float bestT = FLT_MAX;
     uint32_t bestGid = 0xffffffffu, bestSlot = 0xffffffffu;
     float bu = 0.0f, bv = 0.0f;
-    int stackLink[kStack8];
-    float stackT[kStack8];
+    uint2 stack[kStackWide];
     int sp = 0;
-    int cur = 0;
-    uint32_t visits = 0;
+    uint32_t node = 0, visits = 0;
     for (;;) {
         if (++visits > kMaxVisits) {
             atomicOr(s.error, kErrTraversalLimit);
             bestSlot = 0xffffffffu;
             break;
         }
-        if (cur >= 0) {
-            ctr.node();
-            float t[8];
-            int l[8];
-            wide_children(s, cur, r, bestT, t, l);
-            sort8(t, l);
-            if (sp + 8 > kStack8) {
+        ctr.node();
+        uint32_t gBase, gImask, gInner, tBase, tBits;
+        wide_node(s, node, r, bestT, octInv, &gBase, &gImask, &gInner, &tBase, &tBits);
+        while (tBits) {
+            const uint32_t k = tBase + static_cast<uint32_t>(__ffs(tBits) - 1);
+            tBits &= tBits - 1u;
+            ctr.tri();
+            const float4* tp = s.tris + 3 * static_cast<size_t>(k);
+            const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
+            float tt, u, v;
+            if (!tri_test(o, d, kRayEpsilon, FLT_MAX, ta, tb, tc, &tt, &u, &v)) continue;
+            const uint32_t gid = __float_as_uint(ta.w);
+            if (tt < bestT || (tt == bestT && gid < bestGid)) {
+                bestT = tt;
+                bestGid = gid;
+                bestSlot = k;
+                bu = u;
+                bv = v;
+            }
+        }
+        if (gInner == 0u) {
+            if (sp == 0) break;
+            --sp;
+            gBase = stack[sp].x;
+            gInner = stack[sp].y >> 8;
+            gImask = stack[sp].y & 0xffu;
+        }
+        const uint32_t slot = static_cast<uint32_t>(__ffs(gInner) - 1) ^ octInv;
+        gInner &= gInner - 1u;
+        node = gBase + __popc(gImask & ((1u << slot) - 1u));
+        if (gInner) {
+            if (sp >= kStackWide) {
                 atomicOr(s.error, kErrStackOverflow);
                 bestSlot = 0xffffffffu;
                 break;
             }
-#pragma unroll
-            for (int i = 7; i >= 0; --i) {
-                if (t[i] <= bestT) {
-                    stackLink[sp] = l[i];
-                    stackT[sp] = t[i];
-                    ++sp;
-                }
-            }
-        } else {
-            const uint32_t enc = ~static_cast<uint32_t>(cur);
-            const uint32_t first = enc >> 3, cnt = (enc & 7u) + 1u;
-            for (uint32_t k = first; k < first + cnt; ++k) {
-                ctr.tri();
-                const float4* tp = s.tris + 3 * static_cast<size_t>(k);
-                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                float tt, u, v;
-                if (!tri_test(o, d, kRayEpsilon, FLT_MAX, a, b, c, &tt, &u, &v)) continue;
-                const uint32_t gid = __float_as_uint(a.w);
-                if (tt < bestT || (tt == bestT && gid < bestGid)) {
-                    bestT = tt;
-                    bestGid = gid;
-                    bestSlot = k;
-                    bu = u;
-                    bv = v;
-                }
-            }
+            stack[sp++] = make_uint2(gBase, (gInner << 8) | gImask);
         }
-        bool found = false;
-        while (sp > 0) {
-            --sp;
-            if (stackT[sp] <= bestT) {
-                cur = stackLink[sp];
-                found = true;
-                break;
-            }
-        }
-        if (!found) break;
     }
     out->t = bestT;
     out->u = bu;
@@ -252,49 +241,53 @@ __device__ bool trace_closest8(const DevScene& s, const V3& o, const V3& d, HitR
 }
 
 template <typename Ctr>
-__device__ bool trace_occluded8(const DevScene& s, const V3& o, const V3& d, float maxDist, Ctr& ctr) {
+__device__ bool trace_occluded_wide(const DevScene& s, const V3& o, const V3& d, float maxDist, Ctr& ctr) {
     const RayInv r = ray_inv(o, d);
-    int stack[kStack8];
+    const uint32_t octInv = ray_oct_inv(d);
+    uint2 stack[kStackWide];
     int sp = 0;
-    int cur = 0;
-    uint32_t visits = 0;
+    uint32_t node = 0, visits = 0;
     for (;;) {
         if (++visits > kMaxVisits) {
             atomicOr(s.error, kErrTraversalLimit);
             return false;
         }
-        if (cur >= 0) {
-            ctr.onode();
-            float t[8];
-            int l[8];
-            wide_children(s, cur, r, maxDist, t, l);
-            if (sp + 8 > kStack8) {
+        ctr.onode();
+        uint32_t gBase, gImask, gInner, tBase, tBits;
+        wide_node(s, node, r, maxDist, octInv, &gBase, &gImask, &gInner, &tBase, &tBits);
+        while (tBits) {
+            const uint32_t k = tBase + static_cast<uint32_t>(__ffs(tBits) - 1);
+            tBits &= tBits - 1u;
+            ctr.otri();
+            const float4* tp = s.tris + 3 * static_cast<size_t>(k);
+            const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
+            float tt, u, v;
+            if (tri_test(o, d, kRayEpsilon, maxDist, ta, tb, tc, &tt, &u, &v)) return true;
+        }
+        if (gInner == 0u) {
+            if (sp == 0) return false;
+            --sp;
+            gBase = stack[sp].x;
+            gInner = stack[sp].y >> 8;
+            gImask = stack[sp].y & 0xffu;
+        }
+        const uint32_t slot = static_cast<uint32_t>(__ffs(gInner) - 1) ^ octInv;
+        gInner &= gInner - 1u;
+        node = gBase + __popc(gImask & ((1u << slot) - 1u));
+        if (gInner) {
+            if (sp >= kStackWide) {
                 atomicOr(s.error, kErrStackOverflow);
                 return false;
             }
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-                if (t[i] <= maxDist) stack[sp++] = l[i];
-        } else {
-            const uint32_t enc = ~static_cast<uint32_t>(cur);
-            const uint32_t first = enc >> 3, cnt = (enc & 7u) + 1u;
-            for (uint32_t k = first; k < first + cnt; ++k) {
-                ctr.otri();
-                const float4* tp = s.tris + 3 * static_cast<size_t>(k);
-                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                float tt, u, v;
-                if (tri_test(o, d, kRayEpsilon, maxDist, a, b, c, &tt, &u, &v)) return true;
-            }
+            stack[sp++] = make_uint2(gBase, (gInner << 8) | gImask);
         }
-        if (sp == 0) return false;
-        cur = stack[--sp];
     }
 }
 
 template <typename Ctr>
 __device__ __noinline__ bool trace_closest(const DevScene& s, const V3 o, const V3 d, HitRec* out, Ctr& ctr) {
     ctr.closest();
-    if (s.nodes8) return trace_closest8(s, o, d, out, ctr);
+    if (s.nodes8) return trace_closest_wide(s, o, d, out, ctr);
     const RayInv r = ray_inv(o, d);
     float bestT = FLT_MAX;
     uint32_t bestGid = 0xffffffffu, bestSlot = 0xffffffffu;
@@ -382,7 +375,7 @@ __device__ __noinline__ bool trace_closest(const DevScene& s, const V3 o, const 
 template <typename Ctr>
 __device__ __noinline__ bool trace_occluded(const DevScene& s, const V3 o, const V3 d, float maxDist, Ctr& ctr) {
     ctr.occlusion();
-    if (s.nodes8) return trace_occluded8(s, o, d, maxDist, ctr);
+    if (s.nodes8) return trace_occluded_wide(s, o, d, maxDist, ctr);
     const RayInv r = ray_inv(o, d);
     int stackNode[kStack];
     int sp = 0;
