@@ -61,6 +61,9 @@ def parse():
     p.add_argument("--spp", type=int, default=0)
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--bvh-width", type=int, choices=[2, 8], default=2, help="binary or compressed 8-wide BVH")
+    p.add_argument("--no-rmse", action="store_true", help="skip the equal-RMSE check against a converged image")
+    p.add_argument("--no-batch", action="store_true", help="skip the 48-request batch measurement")
+    p.add_argument("--no-autotune", action="store_true", help="keep the current wavefront configuration")
     return p.parse_args()
 
 
@@ -288,6 +291,102 @@ def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 
             "param_gradients_per_s": nparams * 1000.0 / ms}
 
 
+def rmse_check(local: int, bvh_width: int, with_cpu: bool) -> dict:
+    """The equal-RMSE rule on the sphere frame (256x256, 16 spp, depth 8):
+    RMSE of the plain and wavefront renders (and of the CPU oracle, which
+    traces the same paths) against a 65 536-spp float64-accumulated image
+    rendered from disjoint sample indices."""
+    import torch
+
+    from shiro_gb300 import GpuBackend
+    from shiro_gb300.converge import converged, expected_mc_rmse, rmse
+
+    w = workload("sphere")
+    st = w.settings
+    gpu = GpuBackend(local)
+    gpu.set_bvh_width(bvh_width)
+    gpu.upload_scene(w.scene)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref = converged(gpu, w.camera, st, total_spp=65536, batch_spp=256, first=st.samples_per_pixel)
+    torch.cuda.synchronize()
+    ref_s = time.perf_counter() - t0
+    plain = gpu.render_device(w.camera, st, 0, st.samples_per_pixel)
+    wave = gpu.render_device(w.camera, st, 0, st.samples_per_pixel, wavefront=True)
+    a, b = rmse(plain, ref.mean), rmse(wave, ref.mean)
+    out = {"workload": w.name, "reference_spp": ref.spp, "reference_first_sample": ref.first,
+           "reference_accumulation": "float64 over 256-spp batch means", "reference_seconds": ref_s,
+           "plain": a, "wavefront": b, "relative_difference": abs(a - b) / max(a, 1e-30),
+           "identical_images": bool((plain == wave).all()), "expected_mc_rmse": expected_mc_rmse(ref, st.samples_per_pixel)}
+    if with_cpu:
+        import oracle
+        from oracle import api
+
+        oracle.build_port()
+        ck = oracle.port_checker()
+        cpu = api.render(ck, w.scene, w.camera, st, 0, st.samples_per_pixel)
+        out["cpu_oracle"] = rmse(torch.from_numpy(cpu.beauty.reshape(st.height, st.width, 4).copy()), ref.mean.cpu())
+    gpu.close()
+    return out
+
+
+def batch_bench(local: int, bvh_width: int, reps: int = 2) -> dict:
+    """48 requests of uneven resolution / spp / depth on the sphere scene in
+    one wavefront call, against the same requests rendered one by one with
+    the plain form (device AOV planes, CUDA events)."""
+    import ctypes as C
+
+    import torch
+
+    from shiro_gb300 import GpuBackend, scenes
+    from shiro_gb300.abi import Aovs, RenderDesc, render_desc
+
+    reqs = scenes.batch_requests(48)
+    scene = scenes.sphere_scene()
+    gpu = GpuBackend(local)
+    gpu.set_bvh_width(bvh_width)
+    stream = torch.cuda.current_stream()
+    gpu.lib.shiro_gpu_set_stream(gpu.handle, stream.cuda_stream)
+    gpu.upload_scene(scene)
+    n = len(reqs)
+    descs = (RenderDesc * n)()
+    outs = (Aovs * n)()
+    keep = []
+    paths = 0
+    for i, r in enumerate(reqs):
+        st = r.settings
+        npx = st.width * st.height
+        planes = [torch.empty(npx * c, dtype=torch.float32, device="cuda") for c in (4, 3, 3, 1)]
+        keep.append(planes)
+        outs[i] = Aovs(*[C.cast(C.c_void_p(p.data_ptr()), C.POINTER(C.c_float)) for p in planes], 1, 0)
+        descs[i] = render_desc(r.camera, st, 0, st.samples_per_pixel)
+        paths += npx * st.samples_per_pixel
+
+    def batched():
+        if gpu.lib.shiro_gpu_render_batch(gpu.handle, descs, n, None, outs) != 0:
+            raise RuntimeError(gpu.lib.shiro_gpu_last_error(gpu.handle).decode())
+
+    def sequential():
+        for i in range(n):
+            if gpu.lib.shiro_gpu_render(gpu.handle, C.byref(descs[i]), None, C.byref(outs[i])) != 0:
+                raise RuntimeError(gpu.lib.shiro_gpu_last_error(gpu.handle).decode())
+
+    res = {}
+    for name, fn in (("wavefront_batch", batched), ("plain_sequential", sequential)):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res[name] = paths * reps / (e0.elapsed_time(e1) / 1000.0) / 1e6
+    gpu.close()
+    return {"requests": n, "pixels": int(sum(r.settings.width * r.settings.height for r in reqs)), "paths": int(paths),
+            "unit": UNIT, **res}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -352,7 +451,11 @@ def main():
 
     aov = Aovs(*[C.cast(C.c_void_p(dev[k].data_ptr()), C.POINTER(C.c_float)) for k in ("beauty", "albedo", "normal", "depth")],
                1, 0)
-    start = rank * spp
+    # weak scaling: every rank traces the full frame at `spp` samples per
+    # pixel from its own range of sample indices (the job renders world x spp)
+    from shiro_gb300.replicas import combine, sample_range
+
+    start, _ = sample_range(rank, world, 0, world * spp)
 
     def render_dev(form):
         req = render_desc(w.camera, st, start, spp)
@@ -366,7 +469,7 @@ def main():
 
     tuned = None
     if "wavefront" in forms:
-        tuned = gpu.autotune(w.scene, w.camera, st)
+        tuned = gpu.wavefront_config() if args.no_autotune else gpu.autotune(w.scene, w.camera, st)
 
     def timed(form):
         for _ in range(args.warmup):
@@ -440,6 +543,24 @@ def main():
                "d2h_bytes_per_step": npx * 44, "form": head, "note": "scene resident (uploaded once, "
                f"{upload_s:.2f} s incl. BVH build); per step: request in, 4 AOV planes out"}
 
+    # replicas: one host-staged combination of the ranks' frames (outside the
+    # timed region; the data path has no collective)
+    combine_s = None
+    if dist:
+        gloo = dist.new_group(backend="gloo")
+        render_dev(head)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fb = FrameBuffer(st.width, st.height)
+        fb.beauty[:] = dev["beauty"].cpu().numpy().reshape(fb.beauty.shape)
+        fb.albedo[:] = dev["albedo"].cpu().numpy().reshape(fb.albedo.shape)
+        fb.normal[:] = dev["normal"].cpu().numpy().reshape(fb.normal.shape)
+        fb.depth[:] = dev["depth"].cpu().numpy().reshape(fb.depth.shape)
+        combined = combine(fb, spp, group=gloo)
+        combine_s = time.perf_counter() - t0
+        if combined is not None:
+            assert combined.width == st.width
+
     # roofline of the headline form's dominant kernel
     wc = gpu.count_work(w.scene, w.camera, st, stride=64, sample_start=start)
     npth = max(wc["paths"], 1)
@@ -483,12 +604,18 @@ def main():
     if rank == 0 and not args.no_adjoint and args.workload == "field" and not (args.width or args.height or args.spp):
         adjoint = adjoint_bench(local, bvh_width=args.bvh_width)
 
+    extra = {}
+    if rank == 0 and not args.no_rmse and args.workload == "field" and not (args.width or args.height or args.spp):
+        extra["rmse"] = rmse_check(local, args.bvh_width, not args.no_cpu_baseline)
+    if rank == 0 and not args.no_batch and args.workload == "field" and not (args.width or args.height or args.spp):
+        extra["batch"] = batch_bench(local, args.bvh_width)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(w, args.cpu_seconds)
     if rank == 0:
         cfg = workload_config(w, "flushed (512 MiB memset between steps)")
         cfg.update({"form": head, "parallelism": f"replicas x{world}", "scene_upload_s": upload_s, "bvh_width": args.bvh_width,
+                    "replica_combine_s": combine_s,
                     "bvh_nodes": int(stats["bvh_nodes"]), "bvh_depth": int(stats["bvh_depth"]),
                     "forms": {f: {"Mpaths_s": results[f]["value"], "ms_per_step": results[f]["ms"] / args.steps}
                               for f in forms}, "wavefront_config": tuned})
@@ -496,7 +623,7 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene, random-init HDRI)",
                 "config": cfg, "clocks": clocks.summary(), "gpu_launches": launches, "e2e": e2e,
-                "roofline": roofline, "cpu_baseline": cpu, "adjoint": adjoint}
+                "roofline": roofline, "cpu_baseline": cpu, "adjoint": adjoint, **extra}
         print(json.dumps(line), flush=True)
     gpu.close()
     if dist:

@@ -7,6 +7,13 @@ per-material base colour [M, 3], roughness [M], metalness [M] and the texels
 after writing the parameters into the resident scene; the backward runs the
 adjoint path-replay kernel (shiro_gpu_adjoint), which recomputes every path
 from its QMC seed instead of storing it.
+
+For a loss that is non-linear in the image (an L2 loss), replaying the same
+samples in the backward pass as in the forward one correlates the upstream
+gradient with the image noise: the expected gradient then also carries the
+derivative of the image variance, which with bright environments pushes
+materials darker.  `adjoint_sample_start` replays an independent range of
+sample indices instead (a decorrelated gradient estimate).
 """
 from __future__ import annotations
 
@@ -17,7 +24,7 @@ from .abi import Camera, RenderSettings
 
 class _Render(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, base_color, roughness, metallic, env, backend, camera, settings, sample_start, flags):
+    def forward(ctx, base_color, roughness, metallic, env, backend, camera, settings, sample_start, flags, adj_start):
         tensors = [t.detach().contiguous().float() if t is not None else None
                    for t in (base_color, roughness, metallic, env)]
         backend.set_params(*tensors)
@@ -25,7 +32,7 @@ class _Render(torch.autograd.Function):
         ctx.backend = backend
         ctx.camera = camera
         ctx.settings = settings
-        ctx.sample_start = sample_start
+        ctx.sample_start = sample_start if adj_start is None else adj_start
         ctx.flags = flags
         ctx.shapes = [None if t is None else t.shape for t in (base_color, roughness, metallic, env)]
         return beauty
@@ -39,10 +46,11 @@ class _Render(torch.autograd.Function):
                 grads[name] = torch.zeros(shape, dtype=torch.float32, device="cuda")
         ctx.backend.adjoint(ctx.camera, ctx.settings, d_beauty.contiguous().float(), grads, ctx.sample_start,
                             ctx.settings.samples_per_pixel, ctx.flags)
-        return tuple(grads.get(n) for n in names) + (None, None, None, None, None)
+        return tuple(grads.get(n) for n in names) + (None, None, None, None, None, None)
 
 
 def render(backend, camera: Camera, settings: RenderSettings, base_color, roughness, metallic, env=None,
-           sample_start: int = 0, flags: int = 0):
+           sample_start: int = 0, flags: int = 0, adjoint_sample_start=None):
     """Differentiable render of the backend's uploaded scene (see module doc)."""
-    return _Render.apply(base_color, roughness, metallic, env, backend, camera, settings, sample_start, flags)
+    return _Render.apply(base_color, roughness, metallic, env, backend, camera, settings, sample_start, flags,
+                         adjoint_sample_start)

@@ -1,0 +1,117 @@
+"""Replica host logic on CPU: sample-range partition, the reference's frame
+accumulation, and the host-staged combination over two gloo ranks.
+
+The ranks render their sample ranges with the CPU oracle (the same paths the
+GPU traces); rank 0's combined frame must equal the frame accumulated from
+the same batches in one process, bit for bit, and agree with a single render
+of all samples to float rounding.
+"""
+import os
+import socket
+import tempfile
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+
+def test_sample_range_partitions():
+    from shiro_gb300.replicas import sample_range
+
+    for world in (1, 2, 3, 4, 8):
+        for count in (0, 1, 5, 16, 64, 67):
+            got = [sample_range(r, world, 100, count) for r in range(world)]
+            assert sum(c for _, c in got) == count
+            nxt = 100
+            for first, c in got:
+                assert first == nxt
+                nxt += c
+            assert max(c for _, c in got) - min(c for _, c in got) <= 1
+    with pytest.raises(ValueError):
+        sample_range(2, 2, 0, 4)
+
+
+def test_accumulator_semantics():
+    """Known answers of FrameAccumulator (Renderer.cpp:60-110): weighted
+    means, depth averaged over the batches that hit, +inf without hits."""
+    from shiro_gb300.abi import FrameBuffer
+    from shiro_gb300.replicas import accumulate
+
+    a, b = FrameBuffer(2, 1), FrameBuffer(2, 1)
+    a.beauty[:] = [[1, 2, 3, 1], [0, 0, 0, 0]]
+    b.beauty[:] = [[3, 2, 1, 0], [4, 4, 4, 1]]
+    a.albedo[:] = 0.5
+    b.albedo[:] = 0.25
+    a.depth[:] = [2.0, np.inf]
+    b.depth[:] = [5.0, np.inf]
+    out = accumulate([a, b], [1, 3])
+    np.testing.assert_array_equal(out.beauty[0], np.float32([2.5, 2.0, 1.5, 0.25]))
+    np.testing.assert_array_equal(out.beauty[1], np.float32([3.0, 3.0, 3.0, 0.75]))
+    np.testing.assert_array_equal(out.albedo, np.full((2, 3), 0.3125, np.float32))
+    assert out.depth[0] == np.float32((2.0 * 1 + 5.0 * 3) / 4) and np.isinf(out.depth[1])
+    empty = accumulate([a], [0])
+    assert (empty.beauty == 0).all()
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _workload():
+    from shiro_gb300 import scenes
+
+    return scenes.sphere_workload(16, 12, 8, 3, env_width=32, env_height=16)
+
+
+def _rank_main(rank, world, port, out_path):
+    import torch.distributed as dist
+
+    import oracle
+    from oracle import api
+    from shiro_gb300.replicas import combine, sample_range
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        w = _workload()
+        st = w.settings
+        first, count = sample_range(rank, world, 0, st.samples_per_pixel)
+        ck = oracle.port_checker()
+        fb = api.render(ck, w.scene, w.camera, st, first, count)
+        out = combine(fb, count)
+        if rank == 0:
+            np.savez(out_path, beauty=out.beauty, albedo=out.albedo, normal=out.normal, depth=out.depth)
+        else:
+            assert out is None
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_combine():
+    import torch.multiprocessing as mp
+
+    import oracle
+    from oracle import api
+    from shiro_gb300.replicas import accumulate, sample_range
+
+    oracle.build_port()
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "combined.npz")
+        mp.start_processes(_rank_main, args=(2, _free_port(), path), nprocs=2, join=True, start_method="spawn")
+        got = np.load(path)
+    w = _workload()
+    st = w.settings
+    ck = oracle.port_checker()
+    parts = [sample_range(r, 2, 0, st.samples_per_pixel) for r in range(2)]
+    frames = [api.render(ck, w.scene, w.camera, st, f, c) for f, c in parts]
+    want = accumulate(frames, [c for _, c in parts])
+    for k in ("beauty", "albedo", "normal", "depth"):
+        assert np.array_equal(got[k], getattr(want, k)), k
+    full = api.render(ck, w.scene, w.camera, st, 0, st.samples_per_pixel)
+    np.testing.assert_allclose(got["beauty"], full.beauty, rtol=1e-5, atol=1e-6)
+    hit = np.isfinite(full.depth)
+    assert np.array_equal(np.isfinite(got["depth"]), hit)
