@@ -60,7 +60,8 @@ def parse():
     p.add_argument("--height", type=int, default=0)
     p.add_argument("--spp", type=int, default=0)
     p.add_argument("--no-adjoint", action="store_true")
-    p.add_argument("--bvh-width", type=int, choices=[2, 8], default=2, help="binary or compressed 8-wide BVH")
+    p.add_argument("--bvh-width", type=int, choices=[0, 2, 8], default=0,
+                   help="2 binary, 8 compressed 8-wide BVH, 0 each form its faster one (wavefront: wide, plain: binary)")
     p.add_argument("--no-rmse", action="store_true", help="skip the equal-RMSE check against a converged image")
     p.add_argument("--no-batch", action="store_true", help="skip the 48-request batch measurement")
     p.add_argument("--no-autotune", action="store_true", help="keep the current wavefront configuration")
@@ -433,7 +434,6 @@ def main():
     spp = st.samples_per_pixel
     gpu = GpuBackend(local)
     gpu.set_bvh_width(args.bvh_width)
-    BYTES["node"] = 64 if args.bvh_width == 2 else 80
     stream = torch.cuda.current_stream()
     gpu.lib.shiro_gpu_set_stream(gpu.handle, stream.cuda_stream)
     t0 = time.perf_counter()
@@ -561,8 +561,13 @@ def main():
         if combined is not None:
             assert combined.width == st.width
 
-    # roofline of the headline form's dominant kernel
+    # roofline of the headline form's dominant kernel, with the work counted
+    # on the BVH that form traverses
+    wide = args.bvh_width == 8 or (args.bvh_width == 0 and head == "wavefront")
+    BYTES["node"] = 80 if wide else 64
+    gpu.set_bvh_width(8 if wide else 2)
     wc = gpu.count_work(w.scene, w.camera, st, stride=64, sample_start=start)
+    gpu.set_bvh_width(args.bvh_width)
     npth = max(wc["paths"], 1)
     cn = wc["node_visits"] - wc["occlusion_node_visits"]
     ct = wc["tri_tests"] - wc["occlusion_tri_tests"]

@@ -248,10 +248,12 @@ void shiro_gpu_destroy(ShiroGpuContext* ctx);
  * is NULL). Never NULL. */
 const char* shiro_gpu_last_error(const ShiroGpuContext* ctx);
 
-/* Selects the acceleration structure traversed by every kernel: 2 (default)
- * the binary BVH, 8 the 8-wide BVH with quantised child boxes collapsed from
- * it.  Both give identical hits; the choice only changes speed (on GB300 the
- * binary traversal is faster for scenes that stay resident in L2). */
+/* Selects the acceleration structure the kernels traverse: 2 the binary
+ * BVH, 8 the compressed 8-wide BVH (quantised child boxes, octant-ordered
+ * slots), 0 (default) each form its faster one on GB300: the wavefront
+ * stages the wide BVH, the one-thread-per-path kernels (plain, adjoint,
+ * probes) the binary one.  Both give identical hits; the choice only changes
+ * speed. */
 int shiro_gpu_set_bvh_width(ShiroGpuContext* ctx, uint32_t width);
 
 /* Renders on this CUDA stream (cudaStream_t cast to void*; NULL = the

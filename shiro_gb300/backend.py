@@ -213,10 +213,12 @@ class GpuBackend:
         return fbs
 
     def set_bvh_width(self, width: int):
-        """2: traverse the binary BVH (default); 8: the wide quantised BVH."""
+        """2: the binary BVH everywhere; 8: the compressed wide BVH everywhere;
+        0 (default): the wide BVH in the wavefront form, the binary one in the
+        one-thread-per-path kernels.  Hits are identical."""
         rc = self.lib.shiro_gpu_set_bvh_width(self._ctx, int(width))
         if rc != 0:
-            raise ShiroGpuError(rc, "bvh width must be 2 or 8")
+            raise ShiroGpuError(rc, "bvh width must be 0, 2 or 8")
 
     def wavefront_config(self) -> dict:
         c = WavefrontConfig()

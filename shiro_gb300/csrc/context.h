@@ -50,9 +50,10 @@ struct ContextImpl {
     const float4* tris8 = nullptr;    // triangles in the wide BVH's leaf order
     const float4* tris2 = nullptr;    // triangles in the binary BVH's leaf order
     uint32_t node8Count = 0, bvh8Depth = 0;
-    // 2: traverse the binary BVH (default, measured faster on GB300 for
-    // L2-resident scenes), 8: the wide quantised BVH
-    uint32_t bvhWidth = 2;
+    // 2: traverse the binary BVH, 8: the compressed wide BVH, 0: the wide one
+    // in the wavefront stages and the binary one in the one-thread-per-path
+    // kernels (each measured faster there on GB300)
+    uint32_t bvhWidth = 0;
 
     // scratch (grown on demand, kept between calls)
     DeviceBlock pathRecords;

@@ -442,7 +442,7 @@ const char* shiro_gpu_last_error(const ShiroGpuContext* ctx) {
 }
 
 int shiro_gpu_set_bvh_width(ShiroGpuContext* ctx, uint32_t width) {
-    if (!ctx || (width != 2 && width != 8)) return SHIRO_ERR_INVALID_ARGUMENT;
+    if (!ctx || (width != 0 && width != 2 && width != 8)) return SHIRO_ERR_INVALID_ARGUMENT;
     ContextImpl& c = ctx->impl;
     c.bvhWidth = width;
     c.scene.nodes8 = (width == 8 && c.hasScene) ? c.nodes8 : nullptr;

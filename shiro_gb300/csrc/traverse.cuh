@@ -76,6 +76,19 @@ __device__ __forceinline__ RayInv ray_inv(const V3& o, const V3& d) {
     return r;
 }
 
+// Three-input minimum / maximum (PTX min.f32 / max.f32 with three sources,
+// sm_100 and later); for non-NaN inputs equal to two nested fminf / fmaxf.
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 // Entry / exit of both child boxes of a node (slab test, fused form).
 __device__ __forceinline__ void node_boxes(const float4& n0, const float4& n1, const float4& n2, const RayInv& r,
                                            float tmax, float* t0, float* t1, bool* h0, bool* h1) {
@@ -85,10 +98,10 @@ __device__ __forceinline__ void node_boxes(const float4& n0, const float4& n1, c
     const float cx = __fmaf_rn(n1.x, r.inv.x, -r.ood.x), dx = __fmaf_rn(n1.y, r.inv.x, -r.ood.x);
     const float cy = __fmaf_rn(n1.z, r.inv.y, -r.ood.y), dy = __fmaf_rn(n1.w, r.inv.y, -r.ood.y);
     const float cz = __fmaf_rn(n2.z, r.inv.z, -r.ood.z), dz = __fmaf_rn(n2.w, r.inv.z, -r.ood.z);
-    const float lo0 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fmaxf(fminf(az, bz), 0.0f));
-    const float hi0 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fminf(fmaxf(az, bz), tmax));
-    const float lo1 = fmaxf(fmaxf(fminf(cx, dx), fminf(cy, dy)), fmaxf(fminf(cz, dz), 0.0f));
-    const float hi1 = fminf(fminf(fmaxf(cx, dx), fmaxf(cy, dy)), fminf(fmaxf(cz, dz), tmax));
+    const float lo0 = fmax3(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), 0.0f));
+    const float hi0 = fmin3(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
+    const float lo1 = fmax3(fminf(cx, dx), fminf(cy, dy), fmaxf(fminf(cz, dz), 0.0f));
+    const float hi1 = fmin3(fmaxf(cx, dx), fmaxf(cy, dy), fminf(fmaxf(cz, dz), tmax));
     *t0 = lo0;
     *t1 = lo1;
     *h0 = lo0 <= hi0;
@@ -138,23 +151,29 @@ __device__ __forceinline__ void wide_node(const DevScene& s, uint32_t node, cons
                 bz = __fmaf_rn(a.z, r.inv.z, -r.ood.z);
     const uint32_t im = eb >> 24;
     const uint32_t m[2] = {__float_as_uint(b.z), __float_as_uint(b.w)};
-    const uint32_t qw[12] = {__float_as_uint(q0.x), __float_as_uint(q0.y), __float_as_uint(q0.z), __float_as_uint(q0.w),
-                             __float_as_uint(q1.x), __float_as_uint(q1.y), __float_as_uint(q1.z), __float_as_uint(q1.w),
-                             __float_as_uint(q2.x), __float_as_uint(q2.y), __float_as_uint(q2.z), __float_as_uint(q2.w)};
+    // near / far plane words per axis: a negative direction enters through
+    // the upper planes (inv < 0 makes their distances the smaller ones)
+    const bool nx = r.inv.x < 0.0f, ny = r.inv.y < 0.0f, nz = r.inv.z < 0.0f;
+    const uint32_t lx0 = __float_as_uint(q0.x), lx1 = __float_as_uint(q0.y), ly0 = __float_as_uint(q0.z),
+                   ly1 = __float_as_uint(q0.w), lz0 = __float_as_uint(q1.x), lz1 = __float_as_uint(q1.y),
+                   hx0 = __float_as_uint(q1.z), hx1 = __float_as_uint(q1.w), hy0 = __float_as_uint(q2.x),
+                   hy1 = __float_as_uint(q2.y), hz0 = __float_as_uint(q2.z), hz1 = __float_as_uint(q2.w);
+    const uint32_t nw[6] = {nx ? hx0 : lx0, nx ? hx1 : lx1, ny ? hy0 : ly0, ny ? hy1 : ly1, nz ? hz0 : lz0, nz ? hz1 : lz1};
+    const uint32_t fw[6] = {nx ? lx0 : hx0, nx ? lx1 : hx1, ny ? ly0 : hy0, ny ? ly1 : hy1, nz ? lz0 : hz0, nz ? lz1 : hz1};
     uint32_t hitsInner = 0, hitsTris = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const int h = i >> 2;
         // byte i of a word pair as the float 2^23 + q, minus 2^23 exactly
         const uint32_t sel = static_cast<uint32_t>(i & 3) | 0x7540u;
-        const float x0 = __fmaf_rn(__uint_as_float(__byte_perm(qw[0 + h], 0x4b000000u, sel)) - 8388608.0f, ax, bx);
-        const float y0 = __fmaf_rn(__uint_as_float(__byte_perm(qw[2 + h], 0x4b000000u, sel)) - 8388608.0f, ay, by);
-        const float z0 = __fmaf_rn(__uint_as_float(__byte_perm(qw[4 + h], 0x4b000000u, sel)) - 8388608.0f, az, bz);
-        const float x1 = __fmaf_rn(__uint_as_float(__byte_perm(qw[6 + h], 0x4b000000u, sel)) - 8388608.0f, ax, bx);
-        const float y1 = __fmaf_rn(__uint_as_float(__byte_perm(qw[8 + h], 0x4b000000u, sel)) - 8388608.0f, ay, by);
-        const float z1 = __fmaf_rn(__uint_as_float(__byte_perm(qw[10 + h], 0x4b000000u, sel)) - 8388608.0f, az, bz);
-        const float lo = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.0f));
-        const float hi = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tmax));
+        const float x0 = __fmaf_rn(__uint_as_float(__byte_perm(nw[0 + h], 0x4b000000u, sel)) - 8388608.0f, ax, bx);
+        const float y0 = __fmaf_rn(__uint_as_float(__byte_perm(nw[2 + h], 0x4b000000u, sel)) - 8388608.0f, ay, by);
+        const float z0 = __fmaf_rn(__uint_as_float(__byte_perm(nw[4 + h], 0x4b000000u, sel)) - 8388608.0f, az, bz);
+        const float x1 = __fmaf_rn(__uint_as_float(__byte_perm(fw[0 + h], 0x4b000000u, sel)) - 8388608.0f, ax, bx);
+        const float y1 = __fmaf_rn(__uint_as_float(__byte_perm(fw[2 + h], 0x4b000000u, sel)) - 8388608.0f, ay, by);
+        const float z1 = __fmaf_rn(__uint_as_float(__byte_perm(fw[4 + h], 0x4b000000u, sel)) - 8388608.0f, az, bz);
+        const float lo = fmax3(x0, y0, fmaxf(z0, 0.0f));
+        const float hi = fmin3(x1, y1, fminf(z1, tmax));
         const uint32_t meta = (m[h] >> (8 * (i & 3))) & 0xffu;
         if (lo <= hi) {
             if ((im >> i) & 1u) {

@@ -611,6 +611,10 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     Launch L;
     L.v = make_view(wf, poolP, lightSamples, dWaves, dSegs, dReqs);
     L.s = ctx->scene;
+    if (ctx->bvhWidth != 2 && ctx->nodes8) {  // the wavefront stages traverse the wide BVH unless told otherwise
+        L.s.nodes8 = ctx->nodes8;
+        L.s.tris = ctx->tris8;
+    }
     L.bExt = static_cast<int>(cfg.extend_block);
     L.bShade = static_cast<int>(cfg.shade_block);
     L.bShadow = static_cast<int>(cfg.shadow_block);

@@ -184,8 +184,10 @@ def test_cancel(gpu):
 
 
 def test_bvh_widths_agree(gpu, port):
-    """The binary BVH (default) and the wide quantised BVH collapsed from it
-    return identical hits, distances and occlusion."""
+    """The binary BVH and the compressed wide BVH return identical hits,
+    distances and occlusion (the default lets the wavefront form traverse
+    the wide one and the plain form the binary one, so the wavefront tests'
+    bit-identity covers whole frames across the two)."""
     from shiro_gb300 import scenes
 
     scene = scenes.field_scene(instances=40, levels=4, materials=4, env_width=16, env_height=8, seed=33, plane=20.0)
@@ -206,6 +208,7 @@ def test_bvh_widths_agree(gpu, port):
     finally:
         gpu.set_bvh_width(2)
     fb = gpu.render(w.scene, w.camera, w.settings)
+    gpu.set_bvh_width(0)
     assert np.array_equal(fw.beauty, fb.beauty)
     brute = api.trace_rays(port, scene, o, d, tmax, bruteforce=True)
     for a, b, c in zip(wide, binary, brute):
