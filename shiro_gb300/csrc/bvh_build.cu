@@ -586,7 +586,11 @@ __global__ void k_collapse_wide(const float4* __restrict__ nodes2, const float4*
             childIn[bs] = bi;
         }
     }
-    // per axis a power-of-two scale with extent / scale <= 255
+    // Per axis a power-of-two scale with extent / scale <= 252 and the
+    // quantisation origin one step below the node box.  Every child box is
+    // widened by one step on each side: the traversal folds the float
+    // conversion of the 8-bit plane into its FMA (bias 2^23 * scale * inv),
+    // which can err by half a step.
     uint32_t ex[3];
     float sc[3];
     for (int k = 0; k < 3; ++k) {
@@ -594,15 +598,16 @@ __global__ void k_collapse_wide(const float4* __restrict__ nodes2, const float4*
         int eb = 1;  // smallest normal exponent
         if (ext > 0.0f) {
             int e2;
-            frexpf(ext / 255.0f, &e2);  // ext/255 < 2^e2
+            frexpf(ext / 252.0f, &e2);  // ext/252 < 2^e2
             eb = min(max(e2 + 127, 1), 254);
         }
         ex[k] = static_cast<uint32_t>(eb);
         sc[k] = __uint_as_float(static_cast<uint32_t>(eb) << 23);
-        while (__fmul_ru(255.0f, sc[k]) < ext && ex[k] < 254) {  // guard the rounding of ext / 255
+        while (__fmul_ru(252.0f, sc[k]) < ext && ex[k] < 254) {  // guard the rounding of ext / 252
             ++ex[k];
             sc[k] = __uint_as_float(ex[k] << 23);
         }
+        lo[k] = __fsub_rd(lo[k], sc[k]);
     }
     int inner = 0;
     for (int i = 0; i < n; ++i) inner += e[i].link >= 0 ? 1 : 0;
@@ -623,8 +628,8 @@ __global__ void k_collapse_wide(const float4* __restrict__ nodes2, const float4*
             continue;
         }
         for (int k = 0; k < 3; ++k) {
-            const float a = floorf(__fdiv_rd(__fsub_rd(e[i].lo[k], lo[k]), sc[k]));
-            const float b = ceilf(__fdiv_ru(__fsub_ru(e[i].hi[k], lo[k]), sc[k]));
+            const float a = floorf(__fdiv_rd(__fsub_rd(e[i].lo[k], lo[k]), sc[k])) - 1.0f;
+            const float b = ceilf(__fdiv_ru(__fsub_ru(e[i].hi[k], lo[k]), sc[k])) + 1.0f;
             q[k][s] = static_cast<uint8_t>(fminf(fmaxf(a, 0.0f), 255.0f));
             q[3 + k][s] = static_cast<uint8_t>(fminf(fmaxf(b, 0.0f), 255.0f));
         }

@@ -48,7 +48,8 @@ inline int leaf_link_host(int first, int count) { return ~((first << 3) | (count
 //       are triBase + offset .. + count - 1 of the wide BVH's own triangle
 //       array (offset + count <= 32); an empty slot has meta 0xff
 //   [2..4] qlo.x[8] qlo.y[8] qlo.z[8] qhi.x[8] qhi.y[8] qhi.z[8] bytes; a
-//       child box is origin + q * scale, rounded outward at build time
+//       child box is origin + q * scale, rounded outward and widened by one
+//       step per side at build time (origin = node box minus one step)
 // Child slot s holds the child lying most in direction
 // ((s & 1) ? -x : +x, (s & 2) ? -y : +y, (s & 4) ? -z : +z) from the node
 // centre, so a ray visits slots in the order of s ^ (7 ^ octant) to go

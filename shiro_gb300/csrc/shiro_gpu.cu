@@ -615,8 +615,11 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     std::string berr;
     rc = build_bvh(bin, ctx->stream, &bout, berr);
     // the wide BVH is collapsed from a binary tree with small leaves (the
-    // node's triangle bits bound the leaves it can hold)
-    if (rc == SHIRO_OK) {
+    // node's triangle bits bound the leaves it can hold); its box test folds
+    // 2^23 * scale / direction into a bias, so it is built only while that
+    // stays far from float overflow (coordinates below 1e9)
+    const bool wideOk = mag < 1.0e9f;
+    if (rc == SHIRO_OK && wideOk) {
         BvhInput small = bin;
         small.maxLeaf = kWideLeaf;
         rc = build_bvh(small, ctx->stream, &bwide, berr);
@@ -645,7 +648,7 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     ctx->sceneBlocks.push_back({bout.nodes, 4 * sizeof(float4) * bout.nodeCount});
     ctx->sceneBlocks.push_back({bout.tris, 3 * sizeof(float4) * bout.triCount});
     WideOutput w8;
-    rc = collapse_wide(bwide.nodes, bwide.nodeCount, bwide.tris, bwide.triCount, ctx->stream, &w8, berr);
+    if (wideOk) rc = collapse_wide(bwide.nodes, bwide.nodeCount, bwide.tris, bwide.triCount, ctx->stream, &w8, berr);
     drop(bwide);
     if (rc == SHIRO_OK && w8.depth > static_cast<uint32_t>(kStackWide)) {
         rc = SHIRO_ERR_INVALID_ARGUMENT;
@@ -656,8 +659,8 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
         if (w8.tris) cudaFree(w8.tris);
         return fail(ctx, rc, "wide BVH: " + berr);
     }
-    ctx->sceneBlocks.push_back({w8.nodes, 5 * sizeof(float4) * std::max<uint32_t>(bwide.nodeCount, 1)});
-    ctx->sceneBlocks.push_back({w8.tris, 3 * sizeof(float4) * std::max<uint32_t>(w8.triCount, 1)});
+    if (w8.nodes) ctx->sceneBlocks.push_back({w8.nodes, 5 * sizeof(float4) * std::max<uint32_t>(bwide.nodeCount, 1)});
+    if (w8.tris) ctx->sceneBlocks.push_back({w8.tris, 3 * sizeof(float4) * std::max<uint32_t>(w8.triCount, 1)});
     ctx->nodes8 = w8.nodes;
     ctx->tris8 = w8.tris;
     ctx->tris2 = bout.tris;

@@ -23,7 +23,6 @@ namespace shiro_gpu {
 
 
 constexpr uint32_t kMaxVisits = 1u << 22;
-constexpr uint32_t kWideEmptyMetaDev = 0xffu;  // empty slot of a wide node (bvh_build.h)
 
 // Work counters of the roofline probe (shiro_gpu_count_work).  NullCounter
 // compiles every increment away in the render kernels.
@@ -136,6 +135,15 @@ __device__ __forceinline__ bool tri_test(const V3& o, const V3& d, float tMin, f
 // Children of wide node `node` hit within [0, tmax]: internal ones as bits
 // (slot ^ octInv) of *inner (nearest first = lowest bit), leaf triangles as
 // bits of *tris relative to *triBase.
+//
+// A quantised plane q of an axis lies at t = (origin + q * scale - o) * inv
+// = (2^23 + q) * A + (B - 2^23 * A) with A = scale * inv (exact: scale is a
+// power of two) and B = origin * inv - o * inv.  A byte permute turns q into
+// the float 2^23 + q, and the bias B - 2^23 * A is formed once per node, so a
+// plane costs one permute and one FMA; the bias rounds to within half a
+// quantisation step, which the builder covers by widening every child box by
+// one step.  Empty slots hold an inverted box (q_lo = 255, q_hi = 0) and the
+// meta byte 0xff.
 __device__ __forceinline__ void wide_node(const DevScene& s, uint32_t node, const RayInv& r, float tmax, uint32_t octInv,
                                           uint32_t* childBase, uint32_t* imask, uint32_t* inner, uint32_t* triBase,
                                           uint32_t* tris) {
@@ -145,12 +153,11 @@ __device__ __forceinline__ void wide_node(const DevScene& s, uint32_t node, cons
     const uint32_t eb = __float_as_uint(a.w);
     const float sx = __uint_as_float((eb & 0xffu) << 23), sy = __uint_as_float(((eb >> 8) & 0xffu) << 23),
                 sz = __uint_as_float(((eb >> 16) & 0xffu) << 23);
-    // child plane = origin + q * scale:  t = q * (scale * inv) + (origin * inv - o * inv)
     const float ax = sx * r.inv.x, ay = sy * r.inv.y, az = sz * r.inv.z;
-    const float bx = __fmaf_rn(a.x, r.inv.x, -r.ood.x), by = __fmaf_rn(a.y, r.inv.y, -r.ood.y),
-                bz = __fmaf_rn(a.z, r.inv.z, -r.ood.z);
+    const float bx = __fmaf_rn(-8388608.0f, ax, __fmaf_rn(a.x, r.inv.x, -r.ood.x));
+    const float by = __fmaf_rn(-8388608.0f, ay, __fmaf_rn(a.y, r.inv.y, -r.ood.y));
+    const float bz = __fmaf_rn(-8388608.0f, az, __fmaf_rn(a.z, r.inv.z, -r.ood.z));
     const uint32_t im = eb >> 24;
-    const uint32_t m[2] = {__float_as_uint(b.z), __float_as_uint(b.w)};
     // near / far plane words per axis: a negative direction enters through
     // the upper planes (inv < 0 makes their distances the smaller ones)
     const bool nx = r.inv.x < 0.0f, ny = r.inv.y < 0.0f, nz = r.inv.z < 0.0f;
@@ -160,34 +167,42 @@ __device__ __forceinline__ void wide_node(const DevScene& s, uint32_t node, cons
                    hy1 = __float_as_uint(q2.y), hz0 = __float_as_uint(q2.z), hz1 = __float_as_uint(q2.w);
     const uint32_t nw[6] = {nx ? hx0 : lx0, nx ? hx1 : lx1, ny ? hy0 : ly0, ny ? hy1 : ly1, nz ? hz0 : lz0, nz ? hz1 : lz1};
     const uint32_t fw[6] = {nx ? lx0 : hx0, nx ? lx1 : hx1, ny ? ly0 : hy0, ny ? ly1 : hy1, nz ? lz0 : hz0, nz ? lz1 : hz1};
-    uint32_t hitsInner = 0, hitsTris = 0;
+    uint32_t hit = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const int h = i >> 2;
-        // byte i of a word pair as the float 2^23 + q, minus 2^23 exactly
-        const uint32_t sel = static_cast<uint32_t>(i & 3) | 0x7540u;
-        const float x0 = __fmaf_rn(__uint_as_float(__byte_perm(nw[0 + h], 0x4b000000u, sel)) - 8388608.0f, ax, bx);
-        const float y0 = __fmaf_rn(__uint_as_float(__byte_perm(nw[2 + h], 0x4b000000u, sel)) - 8388608.0f, ay, by);
-        const float z0 = __fmaf_rn(__uint_as_float(__byte_perm(nw[4 + h], 0x4b000000u, sel)) - 8388608.0f, az, bz);
-        const float x1 = __fmaf_rn(__uint_as_float(__byte_perm(fw[0 + h], 0x4b000000u, sel)) - 8388608.0f, ax, bx);
-        const float y1 = __fmaf_rn(__uint_as_float(__byte_perm(fw[2 + h], 0x4b000000u, sel)) - 8388608.0f, ay, by);
-        const float z1 = __fmaf_rn(__uint_as_float(__byte_perm(fw[4 + h], 0x4b000000u, sel)) - 8388608.0f, az, bz);
+        const uint32_t sel = static_cast<uint32_t>(i & 3) | 0x7540u;  // byte i -> float 2^23 + q
+        const float x0 = __fmaf_rn(__uint_as_float(__byte_perm(nw[0 + h], 0x4b000000u, sel)), ax, bx);
+        const float y0 = __fmaf_rn(__uint_as_float(__byte_perm(nw[2 + h], 0x4b000000u, sel)), ay, by);
+        const float z0 = __fmaf_rn(__uint_as_float(__byte_perm(nw[4 + h], 0x4b000000u, sel)), az, bz);
+        const float x1 = __fmaf_rn(__uint_as_float(__byte_perm(fw[0 + h], 0x4b000000u, sel)), ax, bx);
+        const float y1 = __fmaf_rn(__uint_as_float(__byte_perm(fw[2 + h], 0x4b000000u, sel)), ay, by);
+        const float z1 = __fmaf_rn(__uint_as_float(__byte_perm(fw[4 + h], 0x4b000000u, sel)), az, bz);
         const float lo = fmax3(x0, y0, fmaxf(z0, 0.0f));
         const float hi = fmin3(x1, y1, fminf(z1, tmax));
-        const uint32_t meta = (m[h] >> (8 * (i & 3))) & 0xffu;
-        if (lo <= hi) {
-            if ((im >> i) & 1u) {
-                hitsInner |= 1u << (static_cast<uint32_t>(i) ^ octInv);
-            } else if (meta != kWideEmptyMetaDev) {
-                hitsTris |= ((2u << (meta >> 5)) - 1u) << (meta & 31u);
-            }
-        }
+        hit |= (lo <= hi ? 1u : 0u) << i;
+    }
+    // internal children: bit i moves to bit i ^ octInv
+    uint32_t in = hit & im;
+    if (octInv & 1u) in = ((in & 0x55u) << 1) | ((in >> 1) & 0x55u);
+    if (octInv & 2u) in = ((in & 0x33u) << 2) | ((in >> 2) & 0x33u);
+    if (octInv & 4u) in = ((in & 0x0fu) << 4) | ((in >> 4) & 0x0fu);
+    // leaf children: their triangles' bits from the meta bytes
+    const uint64_t meta = (static_cast<uint64_t>(__float_as_uint(b.w)) << 32) | __float_as_uint(b.z);
+    uint32_t lf = hit & ~im, tb = 0;
+    while (lf) {
+        const uint32_t i = static_cast<uint32_t>(__ffs(lf) - 1);
+        lf &= lf - 1u;
+        const uint32_t mt = static_cast<uint32_t>(meta >> (8u * i)) & 0xffu;
+        // an empty slot's inverted box can only pass when rounding collapses
+        // all its planes to one distance; it never contributes triangles
+        if (mt != 0xffu) tb |= ((2u << (mt >> 5)) - 1u) << (mt & 31u);
     }
     *childBase = __float_as_uint(b.x);
     *triBase = __float_as_uint(b.y);
     *imask = im;
-    *inner = hitsInner;
-    *tris = hitsTris;
+    *inner = in;
+    *tris = tb;
 }
 
 __device__ __forceinline__ uint32_t ray_oct_inv(const V3& d) {
