@@ -209,113 +209,144 @@ __device__ __forceinline__ uint32_t ray_oct_inv(const V3& d) {
     return 7u ^ ((d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u));
 }
 
-// Stack entries are groups of sibling wide nodes still to visit:
-// (childBase, remaining inner bits << 8 | imask).
+// Wide-BVH traversal as resumable state (one node and its triangles per
+// step), so a caller may interleave rays: the wavefront stages refill a lane
+// with a new ray as soon as its ray finishes.  Stack entries are groups of
+// sibling wide nodes still to visit: (childBase, remaining inner bits << 8 |
+// imask); the caller owns the stack array.
+struct WideTrav {
+    V3 o, d;
+    RayInv r;
+    uint32_t octInv;
+    float tmax;                 // closest: the best distance so far; occlusion: maxDist
+    float bu, bv;
+    uint32_t bestGid, bestSlot;
+    uint32_t node;              // next node to visit
+    int sp;
+    uint32_t visits;
+};
+
+__device__ __forceinline__ void wide_init(WideTrav& t, const V3& o, const V3& d, float tmax) {
+    t.o = o;
+    t.d = d;
+    t.r = ray_inv(o, d);
+    t.octInv = ray_oct_inv(d);
+    t.tmax = tmax;
+    t.bu = 0.0f;
+    t.bv = 0.0f;
+    t.bestGid = 0xffffffffu;
+    t.bestSlot = 0xffffffffu;
+    t.node = 0;
+    t.sp = 0;
+    t.visits = 0;
+}
+
+// Moves to the next node of the traversal; false when none is left (or on a
+// violated bound, which also sets the error word and clears the hit).
+__device__ __forceinline__ bool wide_next(const DevScene& s, WideTrav& t, uint2* stack, uint32_t gBase, uint32_t gImask,
+                                          uint32_t gInner) {
+    if (gInner == 0u) {
+        if (t.sp == 0) return false;
+        --t.sp;
+        gBase = stack[t.sp].x;
+        gInner = stack[t.sp].y >> 8;
+        gImask = stack[t.sp].y & 0xffu;
+    }
+    const uint32_t slot = static_cast<uint32_t>(__ffs(gInner) - 1) ^ t.octInv;
+    gInner &= gInner - 1u;
+    t.node = gBase + __popc(gImask & ((1u << slot) - 1u));
+    if (gInner) {
+        if (t.sp >= kStackWide) {
+            atomicOr(s.error, kErrStackOverflow);
+            t.bestSlot = 0xffffffffu;
+            return false;
+        }
+        stack[t.sp++] = make_uint2(gBase, (gInner << 8) | gImask);
+    }
+    return true;
+}
+
+// Closest hit: up to `steps` nodes; true when finished (result in t.tmax,
+// t.bu, t.bv, t.bestSlot, t.bestGid).
 template <typename Ctr>
-__device__ bool trace_closest_wide(const DevScene& s, const V3& o, const V3& d, HitRec* out, Ctr& ctr) {
-    const RayInv r = ray_inv(o, d);
-    const uint32_t octInv = ray_oct_inv(d);
-    float bestT = FLT_MAX;
-    uint32_t bestGid = 0xffffffffu, bestSlot = 0xffffffffu;
-    float bu = 0.0f, bv = 0.0f;
-    uint2 stack[kStackWide];
-    int sp = 0;
-    uint32_t node = 0, visits = 0;
-    for (;;) {
-        if (++visits > kMaxVisits) {
+__device__ __forceinline__ bool wide_closest_advance(const DevScene& s, WideTrav& t, uint2* stack, int steps, Ctr& ctr) {
+    for (int k = 0; k < steps; ++k) {
+        if (++t.visits > kMaxVisits) {
             atomicOr(s.error, kErrTraversalLimit);
-            bestSlot = 0xffffffffu;
-            break;
+            t.bestSlot = 0xffffffffu;
+            return true;
         }
         ctr.node();
         uint32_t gBase, gImask, gInner, tBase, tBits;
-        wide_node(s, node, r, bestT, octInv, &gBase, &gImask, &gInner, &tBase, &tBits);
+        wide_node(s, t.node, t.r, t.tmax, t.octInv, &gBase, &gImask, &gInner, &tBase, &tBits);
         while (tBits) {
-            const uint32_t k = tBase + static_cast<uint32_t>(__ffs(tBits) - 1);
+            const uint32_t kk = tBase + static_cast<uint32_t>(__ffs(tBits) - 1);
             tBits &= tBits - 1u;
             ctr.tri();
-            const float4* tp = s.tris + 3 * static_cast<size_t>(k);
+            const float4* tp = s.tris + 3 * static_cast<size_t>(kk);
             const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
             float tt, u, v;
-            if (!tri_test(o, d, kRayEpsilon, FLT_MAX, ta, tb, tc, &tt, &u, &v)) continue;
+            if (!tri_test(t.o, t.d, kRayEpsilon, FLT_MAX, ta, tb, tc, &tt, &u, &v)) continue;
             const uint32_t gid = __float_as_uint(ta.w);
-            if (tt < bestT || (tt == bestT && gid < bestGid)) {
-                bestT = tt;
-                bestGid = gid;
-                bestSlot = k;
-                bu = u;
-                bv = v;
+            if (tt < t.tmax || (tt == t.tmax && gid < t.bestGid)) {
+                t.tmax = tt;
+                t.bestGid = gid;
+                t.bestSlot = kk;
+                t.bu = u;
+                t.bv = v;
             }
         }
-        if (gInner == 0u) {
-            if (sp == 0) break;
-            --sp;
-            gBase = stack[sp].x;
-            gInner = stack[sp].y >> 8;
-            gImask = stack[sp].y & 0xffu;
-        }
-        const uint32_t slot = static_cast<uint32_t>(__ffs(gInner) - 1) ^ octInv;
-        gInner &= gInner - 1u;
-        node = gBase + __popc(gImask & ((1u << slot) - 1u));
-        if (gInner) {
-            if (sp >= kStackWide) {
-                atomicOr(s.error, kErrStackOverflow);
-                bestSlot = 0xffffffffu;
-                break;
-            }
-            stack[sp++] = make_uint2(gBase, (gInner << 8) | gImask);
-        }
+        if (!wide_next(s, t, stack, gBase, gImask, gInner)) return true;
     }
-    out->t = bestT;
-    out->u = bu;
-    out->v = bv;
-    out->slot = bestSlot;
-    out->gid = bestGid;
-    return bestSlot != 0xffffffffu;
+    return false;
+}
+
+// Any hit in [1e-4, t.tmax]: up to `steps` nodes; -1 while running, else
+// 1 occluded / 0 clear.
+template <typename Ctr>
+__device__ __forceinline__ int wide_occluded_advance(const DevScene& s, WideTrav& t, uint2* stack, int steps, Ctr& ctr) {
+    for (int k = 0; k < steps; ++k) {
+        if (++t.visits > kMaxVisits) {
+            atomicOr(s.error, kErrTraversalLimit);
+            return 0;
+        }
+        ctr.onode();
+        uint32_t gBase, gImask, gInner, tBase, tBits;
+        wide_node(s, t.node, t.r, t.tmax, t.octInv, &gBase, &gImask, &gInner, &tBase, &tBits);
+        while (tBits) {
+            const uint32_t kk = tBase + static_cast<uint32_t>(__ffs(tBits) - 1);
+            tBits &= tBits - 1u;
+            ctr.otri();
+            const float4* tp = s.tris + 3 * static_cast<size_t>(kk);
+            const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
+            float tt, u, v;
+            if (tri_test(t.o, t.d, kRayEpsilon, t.tmax, ta, tb, tc, &tt, &u, &v)) return 1;
+        }
+        if (!wide_next(s, t, stack, gBase, gImask, gInner)) return 0;
+    }
+    return -1;
+}
+
+template <typename Ctr>
+__device__ bool trace_closest_wide(const DevScene& s, const V3& o, const V3& d, HitRec* out, Ctr& ctr) {
+    WideTrav t;
+    uint2 stack[kStackWide];
+    wide_init(t, o, d, FLT_MAX);
+    wide_closest_advance(s, t, stack, 0x7fffffff, ctr);
+    out->t = t.tmax;
+    out->u = t.bu;
+    out->v = t.bv;
+    out->slot = t.bestSlot;
+    out->gid = t.bestGid;
+    return t.bestSlot != 0xffffffffu;
 }
 
 template <typename Ctr>
 __device__ bool trace_occluded_wide(const DevScene& s, const V3& o, const V3& d, float maxDist, Ctr& ctr) {
-    const RayInv r = ray_inv(o, d);
-    const uint32_t octInv = ray_oct_inv(d);
+    WideTrav t;
     uint2 stack[kStackWide];
-    int sp = 0;
-    uint32_t node = 0, visits = 0;
-    for (;;) {
-        if (++visits > kMaxVisits) {
-            atomicOr(s.error, kErrTraversalLimit);
-            return false;
-        }
-        ctr.onode();
-        uint32_t gBase, gImask, gInner, tBase, tBits;
-        wide_node(s, node, r, maxDist, octInv, &gBase, &gImask, &gInner, &tBase, &tBits);
-        while (tBits) {
-            const uint32_t k = tBase + static_cast<uint32_t>(__ffs(tBits) - 1);
-            tBits &= tBits - 1u;
-            ctr.otri();
-            const float4* tp = s.tris + 3 * static_cast<size_t>(k);
-            const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
-            float tt, u, v;
-            if (tri_test(o, d, kRayEpsilon, maxDist, ta, tb, tc, &tt, &u, &v)) return true;
-        }
-        if (gInner == 0u) {
-            if (sp == 0) return false;
-            --sp;
-            gBase = stack[sp].x;
-            gInner = stack[sp].y >> 8;
-            gImask = stack[sp].y & 0xffu;
-        }
-        const uint32_t slot = static_cast<uint32_t>(__ffs(gInner) - 1) ^ octInv;
-        gInner &= gInner - 1u;
-        node = gBase + __popc(gImask & ((1u << slot) - 1u));
-        if (gInner) {
-            if (sp >= kStackWide) {
-                atomicOr(s.error, kErrStackOverflow);
-                return false;
-            }
-            stack[sp++] = make_uint2(gBase, (gInner << 8) | gImask);
-        }
-    }
+    wide_init(t, o, d, maxDist);
+    return wide_occluded_advance(s, t, stack, 0x7fffffff, ctr) == 1;
 }
 
 template <typename Ctr>

@@ -178,14 +178,118 @@ __device__ __forceinline__ uint32_t warp_claim(uint32_t* counter, bool pred) {
     return base + __popc(ballot & ((1u << lane_id()) - 1u));
 }
 
+// Lane-level work distribution for the wide-BVH traversal.  A warp claims
+// kFetchChunk queue entries with one atomicAdd and hands them to its lanes;
+// once kRefillIdle lanes have finished their rays they take the next
+// entries, so a warp is not held back by its slowest ray.  Between refills a
+// busy lane visits up to kTravSteps wide nodes (each visit is the same
+// 8-child test for every lane, so lanes at different depths still run it
+// together).
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr uint32_t kFetchChunk = 64;
+constexpr int kTravSteps = 4;
+constexpr int kRefillIdle = 8;
+
+struct LaneFeed {
+    uint32_t next = 0, end = 0;  // the warp's claimed entries [next, end)
+    bool exhausted = false;
+};
+
+// Assigns queue entries to idle lanes (`has` false); warp-uniform call.
+// Returns the entry index this lane received, or 0xffffffff.
+__device__ __forceinline__ uint32_t feed_lanes(LaneFeed& f, uint32_t* counter, uint32_t count, bool has) {
+    const uint32_t lane = lane_id();
+    uint32_t got = 0xffffffffu;
+    uint32_t idle = __ballot_sync(kFull, !has);
+    if (f.exhausted || __popc(idle) < kRefillIdle) return got;
+    while (idle != 0u) {
+        if (f.next >= f.end) {
+            uint32_t b = 0;
+            if (lane == 0) b = atomicAdd(counter, kFetchChunk);
+            b = __shfl_sync(kFull, b, 0);
+            if (b >= count) {
+                f.exhausted = true;
+                break;
+            }
+            f.next = b;
+            f.end = min(b + kFetchChunk, count);
+        }
+        const uint32_t rank = __popc(idle & ((1u << lane) - 1u));
+        const uint32_t take = min(f.end - f.next, static_cast<uint32_t>(__popc(idle)));
+        if (((idle >> lane) & 1u) && rank < take) got = f.next + rank;
+        f.next += take;
+        idle = __ballot_sync(kFull, !has && got == 0xffffffffu);
+    }
+    return got;
+}
+
+// Per-warp staging of finished rays for the shade queue: entries collect in
+// shared memory and leave `cnt` at a time with one atomicAdd.
+__device__ __forceinline__ void flush_stage(uint32_t* buf, uint32_t& n, uint32_t cnt, uint32_t* counter, uint32_t* shadeQ,
+                                            uint32_t P, bool back) {
+    const uint32_t lane = lane_id();
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(counter, cnt);
+    base = __shfl_sync(kFull, base, 0);
+    if (lane < cnt) shadeQ[back ? P - 1u - (base + lane) : base + lane] = buf[lane];
+    __syncwarp();
+    const uint32_t rest = n - cnt;
+    uint32_t x = 0;
+    if (lane < rest) x = buf[cnt + lane];
+    __syncwarp();
+    if (lane < rest) buf[lane] = x;
+    __syncwarp();
+    n = rest;
+}
+
 // Closest hit of every queued ray.  The ray is then queued for shading with
 // the hits at the front of the shade queue and the misses at its back, so the
 // shade stage runs warps of hits and warps of misses instead of warps that
 // take both branches.
 __global__ void __launch_bounds__(256, 4) wf_extend(WfView v, DevScene s, uint32_t cur) {
+    __shared__ uint32_t stage[8][2][64];
     const uint32_t count = v.counters[cur];
     const uint32_t* q = cur ? v.rayQ1 : v.rayQ0;
     NullCounter ctr;
+    if (s.nodes8) {
+        uint32_t* hb = stage[threadIdx.x >> 5][0];
+        uint32_t* mb = stage[threadIdx.x >> 5][1];
+        const uint32_t ltMask = (1u << lane_id()) - 1u;
+        uint2 stack[kStackWide];
+        WideTrav t;
+        LaneFeed feed;
+        bool has = false;
+        uint32_t j = 0, hc = 0, mc = 0;
+        for (;;) {
+            const uint32_t got = feed_lanes(feed, &v.counters[kFetchExtend], count, has);
+            if (got != 0xffffffffu) {
+                j = q[got];
+                const float4 o = v.ro[j], d = v.rd[j];
+                wide_init(t, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, FLT_MAX);
+                has = true;
+            }
+            if (__ballot_sync(kFull, has) == 0u) break;
+            bool fin = false;
+            if (has && wide_closest_advance(s, t, stack, kTravSteps, ctr)) {
+                v.hit[j] = make_float4(t.tmax, t.bu, t.bv, __uint_as_float(t.bestSlot));
+                v.hitGid[j] = t.bestGid;
+                fin = true;
+                has = false;
+            }
+            const bool hit = fin && t.bestSlot != 0xffffffffu;
+            const uint32_t hbal = __ballot_sync(kFull, hit), mbal = __ballot_sync(kFull, fin && !hit);
+            if (hit) hb[hc + __popc(hbal & ltMask)] = j;
+            if (fin && !hit) mb[mc + __popc(mbal & ltMask)] = j;
+            hc += __popc(hbal);
+            mc += __popc(mbal);
+            __syncwarp();
+            if (hc >= 32u) flush_stage(hb, hc, 32u, &v.counters[kHitCount], v.shadeQ, v.P, false);
+            if (mc >= 32u) flush_stage(mb, mc, 32u, &v.counters[kMissCount], v.shadeQ, v.P, true);
+        }
+        if (hc) flush_stage(hb, hc, hc, &v.counters[kHitCount], v.shadeQ, v.P, false);
+        if (mc) flush_stage(mb, mc, mc, &v.counters[kMissCount], v.shadeQ, v.P, true);
+        return;
+    }
     for (;;) {
         const uint32_t base = warp_fetch(&v.counters[kFetchExtend]);
         if (base >= count) break;
@@ -300,7 +404,10 @@ __global__ void __launch_bounds__(256) wf_shade(WfView v, DevScene s, uint32_t c
 }
 
 // One occlusion ray per thread; an occluded sample's flag is cleared.
-__global__ void __launch_bounds__(256) wf_occlude(WfView v, DevScene s) {
+// (Lane refill as in wf_extend measured slower here: shadow rays are short
+// and an any-hit ends them early, so the refill bookkeeping outweighs the
+// divergence it removes.)
+__global__ void __launch_bounds__(256, 4) wf_occlude(WfView v, DevScene s) {
     const uint32_t count = v.counters[4];
     NullCounter ctr;
     for (;;) {
