@@ -297,7 +297,9 @@ typedef struct ShiroWavefrontConfig {
     uint32_t shade_block;
     uint32_t shadow_block;
     uint32_t use_graph;
-    uint32_t reserved[3];
+    uint32_t shade_regs;    /* register cap of the shade stage: 128 or 96 */
+    uint32_t extend_steps;  /* wide-BVH nodes a lane visits between refills, 1-32 */
+    uint32_t refill_idle;   /* idle lanes that make a warp refill, 1-32 */
 } ShiroWavefrontConfig;
 int shiro_gpu_get_wavefront_config(const ShiroGpuContext* ctx, ShiroWavefrontConfig* out);
 int shiro_gpu_set_wavefront_config(ShiroGpuContext* ctx, const ShiroWavefrontConfig* cfg);

@@ -223,8 +223,7 @@ class GpuBackend:
     def wavefront_config(self) -> dict:
         c = WavefrontConfig()
         self.lib.shiro_gpu_get_wavefront_config(self._ctx, C.byref(c))
-        return dict(paths_in_flight=c.paths_in_flight, extend_block=c.extend_block, shade_block=c.shade_block,
-                    shadow_block=c.shadow_block, use_graph=c.use_graph)
+        return {name: int(getattr(c, name)) for name, _ in WavefrontConfig._fields_}
 
     def set_wavefront_config(self, **kw):
         c = WavefrontConfig()

@@ -93,6 +93,8 @@ struct WfView {
     const WfRequest* reqs;
     uint32_t P;
     uint32_t lightSamples;
+    int travSteps;     // wide-BVH nodes per lane between refills
+    int refillIdle;    // idle lanes that trigger a refill
 };
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -180,15 +182,13 @@ __device__ __forceinline__ uint32_t warp_claim(uint32_t* counter, bool pred) {
 
 // Lane-level work distribution for the wide-BVH traversal.  A warp claims
 // kFetchChunk queue entries with one atomicAdd and hands them to its lanes;
-// once kRefillIdle lanes have finished their rays they take the next
+// once `refillIdle` lanes have finished their rays they take the next
 // entries, so a warp is not held back by its slowest ray.  Between refills a
-// busy lane visits up to kTravSteps wide nodes (each visit is the same
+// busy lane visits up to `travSteps` wide nodes (each visit is the same
 // 8-child test for every lane, so lanes at different depths still run it
 // together).
 constexpr uint32_t kFull = 0xffffffffu;
 constexpr uint32_t kFetchChunk = 64;
-constexpr int kTravSteps = 4;
-constexpr int kRefillIdle = 8;
 
 struct LaneFeed {
     uint32_t next = 0, end = 0;  // the warp's claimed entries [next, end)
@@ -197,11 +197,11 @@ struct LaneFeed {
 
 // Assigns queue entries to idle lanes (`has` false); warp-uniform call.
 // Returns the entry index this lane received, or 0xffffffff.
-__device__ __forceinline__ uint32_t feed_lanes(LaneFeed& f, uint32_t* counter, uint32_t count, bool has) {
+__device__ __forceinline__ uint32_t feed_lanes(LaneFeed& f, uint32_t* counter, uint32_t count, bool has, int refillIdle) {
     const uint32_t lane = lane_id();
     uint32_t got = 0xffffffffu;
     uint32_t idle = __ballot_sync(kFull, !has);
-    if (f.exhausted || __popc(idle) < kRefillIdle) return got;
+    if (f.exhausted || __popc(idle) < refillIdle) return got;
     while (idle != 0u) {
         if (f.next >= f.end) {
             uint32_t b = 0;
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(256, 4) wf_extend(WfView v, DevScene s, uint32
         bool has = false;
         uint32_t j = 0, hc = 0, mc = 0;
         for (;;) {
-            const uint32_t got = feed_lanes(feed, &v.counters[kFetchExtend], count, has);
+            const uint32_t got = feed_lanes(feed, &v.counters[kFetchExtend], count, has, v.refillIdle);
             if (got != 0xffffffffu) {
                 j = q[got];
                 const float4 o = v.ro[j], d = v.rd[j];
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(256, 4) wf_extend(WfView v, DevScene s, uint32
             }
             if (__ballot_sync(kFull, has) == 0u) break;
             bool fin = false;
-            if (has && wide_closest_advance(s, t, stack, kTravSteps, ctr)) {
+            if (has && wide_closest_advance(s, t, stack, v.travSteps, ctr)) {
                 v.hit[j] = make_float4(t.tmax, t.bu, t.bv, __uint_as_float(t.bestSlot));
                 v.hitGid[j] = t.bestGid;
                 fin = true;
@@ -316,7 +316,9 @@ __device__ __forceinline__ void write_record(const WfView& v, uint32_t j, const 
     v.records[3 * static_cast<size_t>(j)] = make_float4(rad.x, rad.y, rad.z, depth0);
 }
 
-__global__ void __launch_bounds__(256) wf_shade(WfView v, DevScene s, uint32_t cur, uint32_t depth) {
+// Shade stage, compiled with several register caps (the autotuner picks).
+template <int kRegs>
+__global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, uint32_t depth) {
     const uint32_t hits = v.counters[kHitCount];
     const uint32_t count = hits + v.counters[kMissCount];
     uint32_t* qout = cur ? v.rayQ0 : v.rayQ1;
@@ -520,6 +522,9 @@ WavefrontState* wf_state(ContextImpl* ctx) {
         c.shade_block = 128;
         c.shadow_block = 128;
         c.use_graph = 1;
+        c.shade_regs = 128;
+        c.extend_steps = 4;
+        c.refill_idle = 8;
         cudaDeviceGetAttribute(&ctx->wavefront->smCount, cudaDevAttrMultiProcessorCount, ctx->device);
     }
     return ctx->wavefront;
@@ -637,7 +642,15 @@ struct Launch {
     int gGen, gExt, gShade, gShadow, gOcc, gRes;
     int bExt, bShade, bShadow;
     uint32_t depth;
+    uint32_t shadeRegs;
 };
+
+void launch_shade(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t d) {
+    if (L.shadeRegs == 96)
+        wf_shade<96><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
+    else
+        wf_shade<128><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
+}
 
 void enqueue_wave(const Launch& L, cudaStream_t st) {
     wf_begin<<<1, 32, 0, st>>>(L.v);
@@ -645,7 +658,7 @@ void enqueue_wave(const Launch& L, cudaStream_t st) {
     for (uint32_t d = 0; d < L.depth; ++d) {
         const uint32_t cur = d & 1u;
         wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur);
-        wf_shade<<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
+        launch_shade(L, st, cur, d);
         wf_occlude<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s);
         wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s);
         wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur);
@@ -669,7 +682,7 @@ void enqueue_wave_timed(const Launch& L, cudaStream_t st, std::vector<std::pair<
     for (uint32_t d = 0; d < L.depth; ++d) {
         const uint32_t cur = d & 1u;
         timed(1, [&] { wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur); });
-        timed(2, [&] { wf_shade<<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d); });
+        timed(2, [&] { launch_shade(L, st, cur, d); });
         timed(3, [&] { wf_occlude<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s); });
         timed(5, [&] { wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s); });
         timed(5, [&] { wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur); });
@@ -727,7 +740,11 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.bShadow = static_cast<int>(cfg.shadow_block);
     L.gGen = grid_for(wf_generate, 128, wf->smCount);
     L.gExt = grid_for(wf_extend, L.bExt, wf->smCount);
-    L.gShade = grid_for(wf_shade, L.bShade, wf->smCount);
+    L.shadeRegs = cfg.shade_regs;
+    L.gShade = L.shadeRegs == 96 ? grid_for(wf_shade<96>, L.bShade, wf->smCount)
+                                 : grid_for(wf_shade<128>, L.bShade, wf->smCount);
+    L.v.travSteps = static_cast<int>(cfg.extend_steps ? cfg.extend_steps : 4);
+    L.v.refillIdle = static_cast<int>(cfg.refill_idle ? cfg.refill_idle : 8);
     L.gShadow = grid_for(wf_shadow, 256, wf->smCount);
     L.gOcc = grid_for(wf_occlude, L.bShadow, wf->smCount);
     L.gRes = grid_for(wf_resolve, 128, wf->smCount);
@@ -900,9 +917,16 @@ int wavefront_set_config(ContextImpl* ctx, const ShiroWavefrontConfig* cfg) {
             return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "paths_in_flight out of range [1024, 2^27]");
         wf->cfg.paths_in_flight = cfg->paths_in_flight;
     }
+    if (cfg->shade_regs && cfg->shade_regs != 96 && cfg->shade_regs != 128)
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "shade_regs must be 96 or 128");
+    if (cfg->extend_steps > 32 || cfg->refill_idle > 32)
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "extend_steps and refill_idle must be in [1, 32]");
     if (cfg->extend_block) wf->cfg.extend_block = cfg->extend_block;
     if (cfg->shade_block) wf->cfg.shade_block = cfg->shade_block;
     if (cfg->shadow_block) wf->cfg.shadow_block = cfg->shadow_block;
+    if (cfg->shade_regs) wf->cfg.shade_regs = cfg->shade_regs;
+    if (cfg->extend_steps) wf->cfg.extend_steps = cfg->extend_steps;
+    if (cfg->refill_idle) wf->cfg.refill_idle = cfg->refill_idle;
     wf->cfg.use_graph = cfg->use_graph;
     return SHIRO_OK;
 }
@@ -961,6 +985,23 @@ int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefr
         ShiroWavefrontConfig c = best;
         c.shadow_block = blk;
         if ((rc = trial(c)) != SHIRO_OK) return rc;
+    }
+    for (uint32_t regs : {96u, 128u}) {
+        ShiroWavefrontConfig c = best;
+        c.shade_regs = regs;
+        if ((rc = trial(c)) != SHIRO_OK) return rc;
+    }
+    if (ctx->nodes8 && ctx->bvhWidth != 2) {  // the lane refill of the wide-BVH extend stage
+        for (uint32_t steps : {2u, 4u, 8u}) {
+            ShiroWavefrontConfig c = best;
+            c.extend_steps = steps;
+            if ((rc = trial(c)) != SHIRO_OK) return rc;
+        }
+        for (uint32_t idle : {4u, 8u, 16u}) {
+            ShiroWavefrontConfig c = best;
+            c.refill_idle = idle;
+            if ((rc = trial(c)) != SHIRO_OK) return rc;
+        }
     }
     wf->cfg = best;
     wf->tuned = true;

@@ -72,6 +72,28 @@ def test_uneven_batch_small_pool(gpu):
                                  use_graph=1)
 
 
+@pytest.mark.parametrize("knobs", [dict(shade_regs=96), dict(extend_steps=1, refill_idle=1),
+                                   dict(extend_steps=32, refill_idle=32), dict(extend_steps=3, refill_idle=5)])
+def test_tuning_knobs_keep_frames_identical(gpu, knobs):
+    """Register cap of the shade stage and the lane-refill parameters of the
+    wide-BVH extend stage change scheduling only."""
+    from shiro_gb300 import scenes
+
+    sc = scenes.field_scene(instances=12, levels=4, materials=6, env_width=128, env_height=64, seed=9, plane=12.0)
+    st = scenes.RenderSettings(width=64, height=36, samples_per_pixel=4, max_depth=8, diffuse_depth=8,
+                               specular_depth=8, backend=1)
+    cam = scenes.look_at((0.0, 3.5, 8.0), (0.0, 0.3, 0.0), 45.0, 64 / 36)
+    plain = gpu.render(sc, cam, st)
+    base = gpu.wavefront_config()
+    gpu.set_wavefront_config(**knobs)
+    try:
+        (wave,) = gpu.render_batch(sc, [(cam, st)])
+    finally:
+        gpu.set_wavefront_config(**base)
+    ok, k, n = same(plain, wave)
+    assert ok, (knobs, k, n)
+
+
 def test_direct_launch_matches_graph_and_reports_stages(gpu):
     from shiro_gb300 import scenes
 
