@@ -73,6 +73,8 @@ constexpr uint32_t kDirectDimBase = 256u;
 constexpr uint32_t kDirectDepthStride = 512u;
 constexpr uint32_t kDirectLightStride = 128u;
 constexpr uint32_t kDirectSampleStride = 2u;
+constexpr uint32_t kEmissiveDimBase = 8192u;
+constexpr uint32_t kEmissiveDepthStride = 8u;
 
 // ---------------------------------------------------------------------------
 // QMC fallback sampler (OpenQmcSampler.cpp:20-71, 110-135)
@@ -342,6 +344,16 @@ struct SceneData {
     std::vector<V3> tv0, te1, te2;
     std::vector<uint32_t> bvhPrims;
     std::vector<Node> nodes;
+    // emissive triangles (AccelerationScene::emissiveTriangles,
+    // CpuPathTracer.cpp:482-522) and, per global triangle, its entry or -1
+    struct Emissive {
+        uint32_t mesh, prim, gid;
+        float area, weight, cumulative;
+        V3 radiance, ng;
+    };
+    std::vector<Emissive> emissive;
+    float emissiveSum = 0.0f;
+    std::vector<int32_t> emissiveOf;
 };
 
 struct Ray {
@@ -671,6 +683,7 @@ struct SurfaceHit {
     float t;
     V3 position, ng, ns;
     uint32_t material;
+    uint32_t gid;
 };
 
 // Hit record of IntersectSceneBruteForce (CpuPathTracer.cpp:448-456) and
@@ -678,6 +691,7 @@ struct SurfaceHit {
 SurfaceHit MakeSurface(const SceneData& s, const Ray& r, const Hit& h) {
     SurfaceHit sh;
     sh.t = h.t;
+    sh.gid = h.gid;
     sh.position = r.o + r.d * h.t;
     const uint32_t mesh = s.triMesh[h.gid], prim = s.triPrim[h.gid];
     const MeshData& m = s.meshes[mesh];
@@ -949,6 +963,132 @@ inline float Power(float a, float b) {  // :1218-1222
     return a2 / std::max(a2 + b2, 1.0e-6f);
 }
 
+// --- transmission, media and emitters -------------------------------------
+inline float TransmissionRoughness(const Mat& m) {  // :930-932
+    return Clampf(m.roughness + m.transmission_extra_roughness, 0.0f, 1.0f);
+}
+float FresnelDielectric(float cosThetaI, float etaI, float etaT) {  // :1011-1033
+    float c = Clampf(cosThetaI, -1.0f, 1.0f);
+    float ei = std::max(etaI, 1.0e-6f);
+    float et = std::max(etaT, 1.0e-6f);
+    if (c <= 0.0f) {
+        std::swap(ei, et);
+        c = std::fabs(c);
+    }
+    const float sinI = std::sqrt(std::max(0.0f, 1.0f - c * c));
+    const float sinT = ei / et * sinI;
+    if (sinT >= 1.0f) return 1.0f;
+    const float cosT = std::sqrt(std::max(0.0f, 1.0f - sinT * sinT));
+    const float rPar = ((et * c) - (ei * cosT)) / std::max((et * c) + (ei * cosT), 1.0e-6f);
+    const float rPer = ((ei * c) - (et * cosT)) / std::max((ei * c) + (et * cosT), 1.0e-6f);
+    return 0.5f * (rPar * rPar + rPer * rPer);
+}
+inline V3 InterfaceTransmittance(const V3& f0, float a, float b) {  // TransmissionInterfaceTransmittance, :1059-1063
+    const V3 fa = Schlick(f0, Clampf(std::fabs(a), 0.0f, 1.0f));
+    const V3 fb = Schlick(f0, Clampf(std::fabs(b), 0.0f, 1.0f));
+    return OneMinusClamped((fa + fb) * 0.5f);
+}
+inline V3 CoatTransmissionScale(const Mat& m, const V3& cn, const V3& v, const V3& l) {  // :1084-1094
+    return CoatTint(m) * InterfaceTransmittance(CoatF0(m), Dot(cn, v), Dot(cn, l));
+}
+inline V3 TransmissionSurfaceTint(const Mat& m) {  // :1405-1410
+    if (!m.thin_walled && m.transmission_depth > 0.0f) return {1.0f, 1.0f, 1.0f};
+    return Clamp3(L3(m.transmission_color), 0.0f, 1.0f);
+}
+inline float ThinPaneTransmittance(float r) {  // ThinWalledPaneTransmittance, :1412-1418
+    const float c = Clampf(r, 0.0f, 1.0f);
+    return Clampf((1.0f - c) / std::max(1.0f + c, 1.0e-6f), 0.0f, 1.0f);
+}
+V3 MediumExtinction(const Mat& m) {  // :1420-1437
+    V3 e{std::max(m.transmission_scatter[0], 0.0f), std::max(m.transmission_scatter[1], 0.0f),
+         std::max(m.transmission_scatter[2], 0.0f)};
+    if (m.thin_walled || m.transmission_depth <= 0.0f) return e;
+    const float depth = std::max(m.transmission_depth, 1.0e-3f);
+    const V3 tint = Clamp3(L3(m.transmission_color), 1.0e-4f, 1.0f);
+    e.x += -std::log(tint.x) / depth;
+    e.y += -std::log(tint.y) / depth;
+    e.z += -std::log(tint.z) / depth;
+    return e;
+}
+inline V3 MediumAttenuation(const V3& e, float d) {  // :1439-1441, Exp :841-843
+    return {std::exp(-e.x * d), std::exp(-e.y * d), std::exp(-e.z * d)};
+}
+bool Refract(const V3& i, const V3& n, float eta, V3* out) {  // RefractDirection, :1355-1373
+    const float c = Clampf(-Dot(i, n), -1.0f, 1.0f);
+    const float sin2 = std::max(0.0f, 1.0f - c * c);
+    const float k = 1.0f - eta * eta * sin2;
+    if (k <= 0.0f) return false;
+    *out = Normalize(i * eta + n * (eta * c - std::sqrt(k)));
+    return true;
+}
+V3 TransmissionLobe(const Mat& m, const V3& n, const V3& cn, const V3& v, const V3& l, float etaI, float etaT,
+                    float r) {  // EvaluateTransmissionLobe, :1136-1181
+    const float cosWo = Dot(n, v), cosWi = Dot(n, l);
+    const float aWo = std::fabs(cosWo), aWi = std::fabs(cosWi);
+    if (aWo <= 0.0f || aWi <= 0.0f || cosWo * cosWi >= 0.0f) return {};
+    const float rel = etaT / std::max(etaI, 1.0e-6f);
+    V3 h = SafeNormalized(v + l * rel, n);
+    if (Dot(n, h) < 0.0f) h = h * -1.0f;
+    const float woH = Dot(v, h), wiH = Dot(l, h);
+    if (woH * wiH >= 0.0f) return {};
+    const float nh = Clampf(Dot(n, h), 0.0f, 1.0f);
+    const float sd = woH + rel * wiH;
+    if (nh <= 0.0f || std::fabs(sd) <= 1.0e-6f) return {};
+    const float dist = GgxD(nh, r);
+    const float vis = GgxVis(aWo, aWi, r);
+    const float fres = 1.0f - FresnelDielectric(std::fabs(woH), etaI, etaT);
+    const V3 scale = TransmissionSurfaceTint(m) * CoatTransmissionScale(m, cn, v, l) *
+                     (Clampf(m.transmission, 0.0f, 1.0f) * (1.0f - Clampf(m.metallic, 0.0f, 1.0f)));
+    const float factor = std::fabs(dist * vis * std::fabs(wiH) * std::fabs(woH) / std::max(aWo * aWi * Sq(sd), 1.0e-6f));
+    const float transport = 1.0f / std::max(rel * rel, 1.0e-6f);
+    return scale * fres * (factor * transport);
+}
+float TransmissionPdf(const V3& n, const V3& v, const V3& l, float eta, float r) {  // :1183-1212
+    const float cosWo = Dot(n, v), cosWi = Dot(n, l);
+    if (std::fabs(cosWo) <= 0.0f || std::fabs(cosWi) <= 0.0f || cosWo * cosWi >= 0.0f) return 0.0f;
+    V3 h = SafeNormalized(v + l * eta, n);
+    if (Dot(n, h) < 0.0f) h = h * -1.0f;
+    const float woH = Dot(v, h), wiH = Dot(l, h);
+    const float sd = woH + eta * wiH;
+    if (woH * wiH >= 0.0f || std::fabs(sd) <= 1.0e-6f) return 0.0f;
+    const float nh = Clampf(Dot(n, h), 0.0f, 1.0f);
+    const float pdfWh = GgxD(nh, r) * nh;
+    const float dwh = std::fabs((eta * eta * wiH) / Sq(sd));
+    return pdfWh * dwh;
+}
+inline V3 EmittedRadiance(const Mat& m) {  // :1722-1727, :486-490
+    return {std::max(m.emission_color[0] * m.emission_strength, 0.0f),
+            std::max(m.emission_color[1] * m.emission_strength, 0.0f),
+            std::max(m.emission_color[2] * m.emission_strength, 0.0f)};
+}
+// SampleEmissiveTriangleLight (:1443-1460): first entry whose cumulative
+// weight is not below the target, else the last.
+const SceneData::Emissive* SampleEmitter(const SceneData& s, float u) {
+    if (s.emissive.empty() || s.emissiveSum <= 0.0f) return nullptr;
+    const float target = Clampf(u, 0.0f, 0.99999994f) * s.emissiveSum;
+    size_t lo = 0, hi = s.emissive.size();
+    while (lo < hi) {
+        const size_t mid = (lo + hi) / 2;
+        if (s.emissive[mid].cumulative < target) lo = mid + 1; else hi = mid;
+    }
+    return lo == s.emissive.size() ? &s.emissive.back() : &s.emissive[lo];
+}
+// EmissiveTrianglePdf (:1475-1495) of global triangle `gid`.
+float EmitterPdf(const SceneData& s, uint32_t gid, const V3& origin, const V3& position) {
+    const int32_t k = s.emissiveOf[gid];
+    if (k < 0 || s.emissive[k].area <= 0.0f || s.emissiveSum <= 0.0f) return 0.0f;
+    const SceneData::Emissive& e = s.emissive[k];
+    const V3 to = position - origin;
+    const float d2 = Dot(to, to);
+    if (d2 <= 1.0e-10f) return 0.0f;
+    const V3 ld = Normalize(to);
+    const float cosL = std::max(std::fabs(Dot(e.ng, ld * -1.0f)), 1.0e-6f);
+    const float sel = e.weight / s.emissiveSum;
+    const float areaPdf = sel / e.area;
+    return areaPdf * d2 / cosL;
+}
+
+
 // ---------------------------------------------------------------------------
 // Lights (CpuPathTracer.cpp:315-384, 1497-1509)
 // ---------------------------------------------------------------------------
@@ -1017,7 +1157,7 @@ struct Tracer {
     V3 Clamp24(const V3& v) const { return (flags & SHIRO_RENDER_NO_CLAMP) ? v : ClampMax(v, kDirectSampleClamp); }
     V3 Clamp12(const V3& v) const { return (flags & SHIRO_RENDER_NO_CLAMP) ? v : ClampMax(v, kThroughputClamp); }
 
-    // DirectLighting without the emissive-triangle part (CpuPathTracer.cpp:1511-1576).
+    // DirectLighting (CpuPathTracer.cpp:1511-1631).
     V3 Direct(const ShiroSettingsDesc& st, const SurfaceHit& hit, const V3& n, const V3& cn, const Mat& m,
               const V3& view, const Sampler& smp, uint32_t depth) const {
         V3 out{};
@@ -1045,17 +1185,55 @@ struct Tracer {
             }
             out = out + acc / static_cast<float>(spl);
         }
+        // one emissive-triangle sample (:1578-1628)
+        if (!s.emissive.empty() && s.emissiveSum > 0.0f) {
+            const uint32_t db = kEmissiveDimBase + depth * kEmissiveDepthStride;
+            const SceneData::Emissive* e = SampleEmitter(s, smp.Next1D(db + 0u));
+            if (e && e->gid != hit.gid) {
+                const MeshData& md = s.meshes[e->mesh];
+                const V2 u = smp.Next2D(db + 1u);
+                const float su = std::sqrt(Clampf(u.x, 0.0f, 1.0f));  // UniformTriangleBarycentrics, :240-253
+                const float b0 = 1.0f - su;
+                const float b1 = Clampf(u.y, 0.0f, 1.0f) * su;
+                const float b2 = 1.0f - b0 - b1;
+                const V3 p = md.pos[md.idx[3 * e->prim]] * b0 + md.pos[md.idx[3 * e->prim + 1]] * b1 +
+                             md.pos[md.idx[3 * e->prim + 2]] * b2;  // TrianglePoint, :224-238
+                const V3 to = p - hit.position;
+                const float d2 = Dot(to, to);
+                if (d2 > 1.0e-10f) {
+                    const float dist = std::sqrt(d2);
+                    const V3 ld = to / dist;
+                    const float nl = Clampf(Dot(n, ld), 0.0f, 1.0f);
+                    const float cosL = std::fabs(Dot(e->ng, ld * -1.0f));
+                    if (nl > 0.0f && cosL > 0.0f &&
+                        !Blocked(origin, ld, std::max(dist - 2.0f * kRayEpsilon, kRayEpsilon))) {
+                        const float sel = e->weight / s.emissiveSum;
+                        const float areaPdf = sel / std::max(e->area, 1.0e-6f);
+                        const float lp = areaPdf * d2 / std::max(cosL, 1.0e-6f);
+                        if (lp > 0.0f) {
+                            const float bp = BsdfPdf(m, n, cn, view, ld);
+                            const float mis = Power(lp, bp);
+                            out = out + Clamp24(Bsdf(m, n, cn, view, ld) * e->radiance * (nl * mis / lp));
+                        }
+                    }
+                }
+            }
+        }
         return out;
     }
 
-    // TracePath (CpuPathTracer.cpp:1650-2017) for scenes without
-    // transmission, opacity, emission or an active path guide.
+    // TracePath (CpuPathTracer.cpp:1650-2017); the path guide is empty in
+    // the first batch of a scene (:2054-2062) and is not restated.
     PathResult Trace(const ShiroSettingsDesc& st, Ray ray, const Sampler& smp) const {
+        enum Bounce { kNone, kDiffuse, kReflective, kTransmission };
         PathResult res;
         V3 T{1.0f, 1.0f, 1.0f};
         uint32_t diffDepth = 0, specDepth = 0;
+        Bounce prevType = kNone;
         bool prevDelta = true;
         float prevPdf = 0.0f;
+        bool inside = false, mediumActive = false;
+        V3 extinction{};
         for (uint32_t depth = 0; depth < st.max_depth; ++depth) {
             const uint32_t base = depth * kPathDimStride;
             SurfaceHit hit;
@@ -1063,7 +1241,7 @@ struct Tracer {
                 if (depth > 0 || st.background_visible) {
                     const V3 env = EnvRadiance(s, ray.d);
                     V3 delta;
-                    if (s.domes.empty() || depth == 0 || prevDelta) {
+                    if (s.domes.empty() || depth == 0 || prevDelta || prevType == kTransmission) {
                         delta = T * env;
                     } else {
                         float sum = 0.0f;
@@ -1079,6 +1257,7 @@ struct Tracer {
                 }
                 break;
             }
+            if (mediumActive) T = T * MediumAttenuation(extinction, hit.t);
             const Mat& m = s.materials[hit.material];
             const bool front = Dot(hit.ng, ray.d) < 0.0f;
             const V3 ng = front ? hit.ng : hit.ng * -1.0f;
@@ -1088,51 +1267,173 @@ struct Tracer {
             if (Dot(n, ng) < 0.0f) n = n * -1.0f;
             const V3 cn = ResolveNormal(m, n, true);
             const V3 view = ray.d * -1.0f;
+            const float opacity = Clampf(m.opacity, 0.0f, 1.0f);
+            if (opacity < 0.999f) {  // :1713-1720
+                if (smp.Next1D(base + 0u) > opacity) {
+                    ray.o = hit.position + ray.d * kRayEpsilon;
+                    continue;
+                }
+                T = T / std::max(opacity, 1.0e-4f);
+            }
             if (depth == 0) {
                 res.albedo = DiffuseColor(m);
                 res.normal = n * 0.5f + V3{0.5f, 0.5f, 0.5f};
                 res.depth = hit.t;
             }
+            if (m.emission_strength > 0.0f) {  // :1728-1744
+                const V3 le = EmittedRadiance(m);
+                V3 delta;
+                if (depth == 0 || prevDelta || prevType == kTransmission) {
+                    delta = T * le;
+                } else {
+                    const float lp = EmitterPdf(s, hit.gid, ray.o, hit.position);
+                    const float mis = lp > 0.0f ? Power(prevPdf, lp) : 1.0f;
+                    delta = T * le * mis;
+                }
+                res.radiance = res.radiance + delta;
+            }
             res.radiance = res.radiance + T * Direct(st, hit, n, cn, m, view, smp, depth);
 
-            const float dw = DiffuseWeight(m), bw = SpecWeight(m), cw = CoatWeight(m);
+            const float dw = DiffuseWeight(m), cw = CoatWeight(m), rawTw = TransmissionWeight(m);
+            float bw = SpecWeight(m);
+            float tw = rawTw;
+            if (rawTw > 0.0f) {  // :1763-1772
+                const float etaI = inside ? std::max(m.ior, 1.0f) : 1.0f;
+                const float etaT = inside ? 1.0f : std::max(m.ior, 1.0f);
+                const float refl = FresnelDielectric(std::fabs(Dot(ng, view)), etaI, etaT);
+                const float pass = m.thin_walled ? ThinPaneTransmittance(refl) : (1.0f - refl);
+                tw = rawTw * pass;
+                bw += rawTw * (1.0f - pass);
+            }
             const float rw = dw + bw + cw;
-            const float tw = rw + 0.0f;
-            if (tw <= 0.0f) break;
-            const float sel = smp.Next1D(base + 1u) * tw;
+            const float total = rw + tw;
+            if (total <= 0.0f) break;
+            const float sel = smp.Next1D(base + 1u) * total;
             const V2 ds = smp.Next2D(base + 2u);
-            V3 next, f;
+            V3 next{}, f{};
             float pdf = 1.0f;
+            Bounce type = kDiffuse;
             bool delta = false;
-            const float rs = sel - 0.0f;
-            if (rs < dw) {
-                if (diffDepth >= st.diffuse_depth) break;
-                ++diffDepth;
-                next = CosineHemisphere(n, ds);
-                const float cpdf = Clampf(Dot(n, next), 0.0f, 1.0f) * kInvPi;
-                pdf = std::max((rw / tw) * (1.0f * cpdf + 0.0f * 0.0f), 1.0e-6f);
-                f = Bsdf(m, n, cn, view, next);
+            bool chooseT = false, chooseB = false, chooseC = false;
+            if (sel < tw) {
+                chooseT = true;
             } else {
-                const bool coat = !(rs < dw + bw);
+                const float rs = sel - tw;
+                if (rs < dw) {
+                } else if (rs < dw + bw) {
+                    chooseB = true;
+                } else {
+                    chooseC = true;
+                }
+            }
+            if (chooseT) {  // :1811-1925
                 if (specDepth >= st.specular_depth) break;
                 ++specDepth;
-                const V3 sn = coat ? cn : n;
-                const float sr = coat ? RoughnessFor(m.coat_roughness, m.coat_anisotropy, m.coat_rotation)
-                                      : RoughnessFor(BaseRoughness(m), m.specular_anisotropy, m.specular_rotation);
+                type = kTransmission;
+                const float tp = std::max(tw / total, 1.0e-6f);
+                const float tr = m.thin_walled
+                                     ? 0.0f
+                                     : RoughnessFor(TransmissionRoughness(m), m.specular_anisotropy, m.specular_rotation);
+                if (m.thin_walled) {
+                    next = ray.d;
+                    const float refl = FresnelDielectric(std::fabs(Dot(ng, view)), 1.0f, std::max(m.ior, 1.0f));
+                    const float pane = ThinPaneTransmittance(refl);
+                    const V3 scale = TransmissionSurfaceTint(m) * CoatTransmissionScale(m, cn, view, next) *
+                                     (Clampf(m.transmission, 0.0f, 1.0f) * (1.0f - Clampf(m.metallic, 0.0f, 1.0f)));
+                    const float ac = std::max(std::fabs(Dot(ng, next)), 1.0e-4f);
+                    f = scale * pane / ac;
+                    pdf = tp;
+                    delta = true;
+                } else {
+                    const float etaI = inside ? std::max(m.ior, 1.0f) : 1.0f;
+                    const float etaT = inside ? 1.0f : std::max(m.ior, 1.0f);
+                    const float ratio = etaI / etaT;
+                    const float rel = etaT / std::max(etaI, 1.0f);
+                    const float refl = FresnelDielectric(std::fabs(Dot(ng, view)), etaI, etaT);
+                    const float mt = Clampf(m.transmission, 0.0f, 1.0f) * (1.0f - Clampf(m.metallic, 0.0f, 1.0f));
+                    if (tr <= kDeltaRoughness) {
+                        if (!Refract(ray.d, ng, ratio, &next)) {
+                            next = Normalize(Reflect(ray.d, ng));
+                            if (rw <= 0.0f) break;
+                            f = Bsdf(m, n, cn, view, next);
+                            pdf = std::max((rw / total) * BsdfPdf(m, n, cn, view, next), 1.0e-6f);
+                            type = kReflective;
+                            delta = true;
+                            chooseT = false;
+                            chooseB = true;
+                        } else {
+                            const V3 scale = TransmissionSurfaceTint(m) * CoatTransmissionScale(m, cn, view, next) * mt;
+                            const float ac = std::max(std::fabs(Dot(ng, next)), 1.0e-4f);
+                            const float transport = 1.0f / std::max(rel * rel, 1.0e-6f);
+                            f = scale * (1.0f - refl) * transport / ac;
+                            pdf = tp;
+                            inside = !inside;
+                            if (inside) {
+                                extinction = MediumExtinction(m);
+                                mediumActive = m.transmission_depth > 0.0f ||
+                                               MaxComponent(L3(m.transmission_scatter)) > 0.0f;
+                            } else {
+                                mediumActive = false;
+                            }
+                            delta = true;
+                        }
+                    } else {
+                        V3 mn = GgxHalf(ng, ds, tr);
+                        if (Dot(mn, view) < 0.0f) mn = mn * -1.0f;
+                        if (!Refract(ray.d, mn, ratio, &next)) {
+                            next = Normalize(Reflect(ray.d, mn));
+                            if (rw <= 0.0f) break;
+                            f = Bsdf(m, n, cn, view, next);
+                            pdf = std::max((rw / total) * BsdfPdf(m, n, cn, view, next), 1.0e-6f);
+                            type = kReflective;
+                            delta = false;
+                            chooseT = false;
+                            chooseB = true;
+                        } else {
+                            f = TransmissionLobe(m, ng, cn, view, next, etaI, etaT, tr);
+                            pdf = std::max(tp * TransmissionPdf(ng, view, next, etaT / etaI, tr), 1.0e-6f);
+                            inside = !inside;
+                            if (inside) {
+                                extinction = MediumExtinction(m);
+                                mediumActive = m.transmission_depth > 0.0f ||
+                                               MaxComponent(L3(m.transmission_scatter)) > 0.0f;
+                            } else {
+                                mediumActive = false;
+                            }
+                            delta = tr <= kDeltaRoughness;
+                        }
+                    }
+                }
+            } else if (chooseB || chooseC) {
+                if (specDepth >= st.specular_depth) break;
+                ++specDepth;
+                type = kReflective;
+                const V3 sn = chooseC ? cn : n;
+                const float sr = chooseC ? RoughnessFor(m.coat_roughness, m.coat_anisotropy, m.coat_rotation)
+                                         : RoughnessFor(BaseRoughness(m), m.specular_anisotropy, m.specular_rotation);
                 const V3 h = GgxHalf(sn, ds, sr);
                 next = Normalize(Reflect(ray.d, h));
                 const float rc = Clampf(Dot(sn, next), 0.0f, 1.0f);
                 if (rc <= 0.0f) break;
-                pdf = std::max((rw / tw) * BsdfPdf(m, n, cn, view, next), 1.0e-6f);
+                pdf = std::max((rw / total) * BsdfPdf(m, n, cn, view, next), 1.0e-6f);
                 f = Bsdf(m, n, cn, view, next);
                 delta = sr <= kDeltaRoughness;
+            } else {
+                if (diffDepth >= st.diffuse_depth) break;
+                ++diffDepth;
+                next = CosineHemisphere(n, ds);
+                const float cpdf = Clampf(Dot(n, next), 0.0f, 1.0f) * kInvPi;
+                pdf = std::max((rw / total) * (1.0f * cpdf + 0.0f * 0.0f), 1.0e-6f);
+                f = Bsdf(m, n, cn, view, next);
             }
-            const float cosT = Clampf(Dot(n, next), 0.0f, 1.0f);
+            const float cosT = chooseT ? std::max(std::fabs(Dot(ng, next)), 1.0e-4f) : Clampf(Dot(n, next), 0.0f, 1.0f);
             if (cosT <= 0.0f) break;
             T = Clamp12(T * f * (cosT / pdf));
-            const float off = Dot(n, next) >= 0.0f ? 1.0f : -1.0f;
-            ray.o = hit.position + n * (kRayEpsilon * off);
+            const V3 rn = chooseT ? ng : n;
+            const float off = Dot(rn, next) >= 0.0f ? 1.0f : -1.0f;
+            ray.o = hit.position + rn * (kRayEpsilon * off);
             ray.d = next;
+            prevType = type;
             prevDelta = delta;
             prevPdf = pdf;
             if (depth >= 2) {
@@ -1157,15 +1458,9 @@ Ray CameraRay(const ShiroCameraDesc& c, const ShiroSettingsDesc& st, uint32_t x,
     return r;
 }
 
-bool Supported(const ShiroSceneDesc& d) {
-    for (uint32_t i = 0; i < d.material_count; ++i) {
-        const Mat& m = d.materials[i];
-        if (TransmissionWeight(m) > 0.0f) return false;
-        if (Clampf(m.opacity, 0.0f, 1.0f) < 0.999f) return false;
-        if (m.emission_strength > 0.0f) return false;
-    }
-    return true;
-}
+// Every material is handled (transmission, media, opacity, emitters); only
+// the progressive path guide, empty in a scene's first batch, is not.
+bool Supported(const ShiroSceneDesc& d) { return d.material_count == 0 || d.materials != nullptr; }
 
 int Convert(const ShiroSceneDesc& d, SceneData* s) {
     if (!Supported(d)) return SHIRO_ERR_UNSUPPORTED_SCENE;
@@ -1207,6 +1502,31 @@ int Convert(const ShiroSceneDesc& d, SceneData* s) {
     s->envTop = L3(d.environment_top);
     s->envBottom = L3(d.environment_bottom);
     BuildBvh(*s);
+    // emissive triangles in mesh / primitive order with float running sums
+    // (BuildAccelerationScene, CpuPathTracer.cpp:482-522; TriangleArea :198-222)
+    s->emissiveOf.assign(s->triMesh.size(), -1);
+    uint32_t gid = 0;
+    for (uint32_t i = 0; i < s->meshes.size(); ++i) {
+        const MeshData& md = s->meshes[i];
+        const uint32_t prims = static_cast<uint32_t>(md.idx.size() / 3u);
+        const V3 le = EmittedRadiance(s->materials[md.material]);
+        const float w = std::max(0.2126f * le.x + 0.7152f * le.y + 0.0722f * le.z, 0.0f);
+        if (md.idx.size() < 3 || md.idx.size() % 3 != 0 || w <= 0.0f) {
+            gid += prims;
+            continue;
+        }
+        for (uint32_t t = 0; t < prims; ++t, ++gid) {
+            const V3 p0 = md.pos[md.idx[3 * t]], p1 = md.pos[md.idx[3 * t + 1]], p2 = md.pos[md.idx[3 * t + 2]];
+            const V3 av = Cross(p1 - p0, p2 - p0);
+            const float dbl = Length(av);
+            if (dbl <= 1.0e-8f) continue;
+            const float area = dbl * 0.5f;
+            const float sel = area * w;
+            s->emissiveSum += sel;
+            s->emissiveOf[gid] = static_cast<int32_t>(s->emissive.size());
+            s->emissive.push_back({i, t, gid, area, sel, s->emissiveSum, le, av / dbl});
+        }
+    }
     return SHIRO_OK;
 }
 

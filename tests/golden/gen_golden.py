@@ -4,7 +4,8 @@ Run in a tree where the reference sources exist (they are compiled by
 oracle/Makefile into oracle/_ref/libshiro_ref.so together with
 oracle/ref/ref_harness.cpp):
 
-    python tests/golden/gen_golden.py
+    python tests/golden/gen_golden.py            # everything
+    python tests/golden/gen_golden.py emissive   # just the named render cases
 
 Every output comes from the reference's own code (CpuPathTracer.cpp,
 EnvironmentMap.cpp, OpenQmcSampler.cpp built with SHIRO_HAVE_EMBREE=0,
@@ -213,6 +214,55 @@ def render_cases():
                          specular_depth=12, backend=1)
     cases["field_small"] = (field, scenes.look_at((0.0, 3.5, 7.5), (0.0, 0.3, 0.0), 45.0, 16 / 9), st5, 0, 4, 0)
 
+    # emissive triangles: a lamp quad and a small glowing sphere (emission
+    # with MIS at hits, the emissive-triangle light sample), plus the dome
+    spos, snrm, sidx = scenes.uv_sphere(center=(0.0, 1.0, 0.0), radius=1.0, segments=24, rings=12)
+    lpos, lnrm, lidx = scenes.uv_sphere(center=(1.4, 0.5, 0.9), radius=0.35, segments=12, rings=6)
+    gpos, gnrm, gidx = scenes.ground_quad(10.0)
+    quad = np.array([[-0.8, 2.6, -0.6], [0.8, 2.6, -0.6], [0.8, 2.6, 0.6], [-0.8, 2.6, 0.6]], np.float32)
+    qidx = np.array([0, 2, 1, 0, 3, 2], np.uint32)  # facing down
+    lamp = Material(emission_color=(1.0, 0.85, 0.6), emission_strength=6.0, base_color=(0.1, 0.1, 0.1))
+    glow = Material(emission_color=(0.3, 0.6, 1.0), emission_strength=3.0, base_color=(0.2, 0.2, 0.2))
+    emi = Scene(materials=[mats["preview"], lambert((0.6, 0.6, 0.6)), lamp, glow],
+                meshes=[Mesh(spos, sidx, snrm, 0), Mesh(gpos, gidx, gnrm, 1), Mesh(quad, qidx, None, 2),
+                        Mesh(lpos, lidx, lnrm, 3)],
+                dome_lights=[DomeLight((0.3, 0.3, 0.3), scenes.procedural_hdri(64, 32, seed=3))])
+    st7 = RenderSettings(width=40, height=40, samples_per_pixel=4, max_depth=6, diffuse_depth=6, specular_depth=6,
+                         backend=1)
+    cases["emissive"] = (emi, scenes.look_at((2.5, 2.0, 4.0), (0.0, 1.0, 0.0), 50.0, 1.0), st7, 0, 4, 0)
+
+    # opacity cut-outs (UsdPreviewSurface opacity < 1 is thin-walled)
+    cut = Scene(materials=[scenes.usd_preview_surface((0.7, 0.3, 0.2), 0.4, opacity=0.45),
+                           standard_surface((0.3, 0.5, 0.8), 0.3, 0.0, 1.5, opacity=0.8), lambert((0.5, 0.5, 0.5))],
+                meshes=[Mesh(spos, sidx, snrm, 0), Mesh(lpos, lidx, lnrm, 1), Mesh(gpos, gidx, gnrm, 2)],
+                distant_lights=[DistantLight((-0.3, -1.0, -0.2), (2.0, 2.0, 2.0))],
+                dome_lights=[DomeLight((0.5, 0.5, 0.5), scenes.procedural_hdri(64, 32, seed=4))])
+    cases["opacity"] = (cut, scenes.look_at((2.5, 2.0, 4.0), (0.0, 1.0, 0.0), 50.0, 1.0), st7, 0, 4, 0)
+
+    # transmission: smooth and rough solid glass, a tinted absorbing medium,
+    # a scattering medium and a thin-walled pane
+    g1pos, g1nrm, g1idx = scenes.uv_sphere(center=(-1.2, 0.7, 0.0), radius=0.7, segments=24, rings=12)
+    g2pos, g2nrm, g2idx = scenes.uv_sphere(center=(0.4, 0.6, 0.6), radius=0.6, segments=24, rings=12)
+    g3pos, g3nrm, g3idx = scenes.uv_sphere(center=(1.5, 0.5, -0.4), radius=0.5, segments=24, rings=12)
+    pane = np.array([[-1.8, 0.0, -1.4], [1.8, 0.0, -1.4], [1.8, 2.2, -1.4], [-1.8, 2.2, -1.4]], np.float32)
+    pidx = np.array([0, 1, 2, 0, 2, 3], np.uint32)
+    glass = standard_surface((1.0, 1.0, 1.0), 0.0, 0.0, 1.5, transmission=1.0)
+    rough = standard_surface((1.0, 1.0, 1.0), 0.25, 0.0, 1.45, transmission=0.9, transmission_extra_roughness=0.1,
+                             coat_weight=0.3, coat_roughness=0.05)
+    tinted = standard_surface((1.0, 1.0, 1.0), 0.0, 0.0, 1.33, transmission=1.0,
+                              transmission_color=(0.5, 0.8, 0.9), transmission_depth=0.8,
+                              transmission_scatter=(0.3, 0.1, 0.05))
+    thin = standard_surface((1.0, 1.0, 1.0), 0.1, 0.0, 1.5, transmission=0.8, thin_walled=True,
+                            transmission_color=(0.9, 0.95, 1.0))
+    tra = Scene(materials=[glass, rough, tinted, thin, lambert((0.55, 0.5, 0.45))],
+                meshes=[Mesh(g1pos, g1idx, g1nrm, 0), Mesh(g2pos, g2idx, g2nrm, 1), Mesh(g3pos, g3idx, g3nrm, 2),
+                        Mesh(pane, pidx, None, 3), Mesh(gpos, gidx, gnrm, 4)],
+                distant_lights=[DistantLight((-0.2, -1.0, 0.5), (2.5, 2.4, 2.2))],
+                dome_lights=[DomeLight((1.0, 1.0, 1.0), scenes.procedural_hdri(64, 32, seed=6))])
+    st8 = RenderSettings(width=48, height=40, samples_per_pixel=4, max_depth=10, diffuse_depth=4, specular_depth=10,
+                         backend=1)
+    cases["transmission"] = (tra, scenes.look_at((0.5, 1.6, 4.5), (0.0, 0.7, 0.0), 50.0, 48 / 40), st8, 0, 4, 0)
+
     # single path per pixel at a non-zero sample index (per-path golden)
     st6 = RenderSettings(width=64, height=64, samples_per_pixel=1, max_depth=8, diffuse_depth=8, specular_depth=8,
                          backend=1)
@@ -220,10 +270,12 @@ def render_cases():
     return cases
 
 
-def gen_renders():
+def gen_renders(only=None):
     out = {}
     cases = render_cases()
     for name, (scene, cam, st, start, count, flags) in cases.items():
+        if only and name not in only:
+            continue
         fb = api.render(REF, scene, cam, st, start, count)
         out[name] = dict(scene_to_arrays(scene), cam=camera_to_array(cam), settings=settings_to_array(st),
                          start=np.array(start), count=np.array(count), flags=np.array(flags),
@@ -237,6 +289,11 @@ def main():
     REF = oracle.ref_checker()
     if REF is None:
         sys.exit("reference tree not found; golden vectors can only be generated where it exists")
+    only = sys.argv[1:]  # render case names: regenerate just those frames
+    if only:
+        for name, arrays in gen_renders(only).items():
+            np.savez_compressed(os.path.join(HERE, f"render_{name}.npz"), **arrays)
+        return
     rng = np.random.default_rng(20261203)
     np.savez_compressed(os.path.join(HERE, "sampler_kat.npz"), **gen_sampler(rng))
     np.savez_compressed(os.path.join(HERE, "camera_rays.npz"), **gen_camera())

@@ -124,7 +124,8 @@ def test_env_tables_and_queries(port):
             assert_same(v, g[pre + k], rtol=1e-4, atol=1e-6, what=pre + k)
 
 
-RENDERS = ["sphere", "rich", "features_gradient_env", "angular_env", "field_small", "sphere_1spp_start5"]
+RENDERS = ["sphere", "rich", "features_gradient_env", "angular_env", "field_small", "sphere_1spp_start5", "emissive",
+           "opacity", "transmission"]
 
 
 @pytest.mark.parametrize("name", RENDERS)
