@@ -198,7 +198,7 @@ __device__ V3 adj_path(const DevScene& s, const DevRequest& q, const AdjView& a,
         const V3 origin = shadow_origin(v);
         // light samples, in sum_direct's order
         const V3 dT = delta * ps.T;
-        const V3 direct = sum_direct(s, q, [&](uint32_t k, V3* c) {
+        const V3 direct = sum_direct<false>(s, q, [&](uint32_t k, V3* c) {
             V3 ld, L;
             float w;
             int32_t envIdx = -1;
@@ -448,6 +448,9 @@ int adjoint_set_params(ContextImpl* ctx, const float* base, const float* rough, 
 
 int adjoint_run(ContextImpl* ctx, const ShiroRenderDesc* req, const float* dBeauty, float* dBase, float* dRough, float* dMetal,
                 float* dEnv) {
+    if (ctx->hasScene && ctx->extendedMaterials)
+        return fail(ctx, SHIRO_ERR_UNSUPPORTED_SCENE,
+                    "the differentiable form covers reflecting materials only (no transmission, opacity or emission)");
     int rc = validate_request(ctx, *req);
     if (rc != SHIRO_OK) return rc;
     const DevRequest q = make_request(*req);
@@ -502,6 +505,9 @@ void adjoint_free(ContextImpl* ctx) {
 
 int adjoint_render_frozen(ContextImpl* ctx, const ShiroRenderDesc* req, const float* base, const float* rough,
                           const float* metal, const float* env, float* beauty) {
+    if (ctx->hasScene && ctx->extendedMaterials)
+        return fail(ctx, SHIRO_ERR_UNSUPPORTED_SCENE,
+                    "the differentiable form covers reflecting materials only (no transmission, opacity or emission)");
     int rc = validate_request(ctx, *req);
     if (rc != SHIRO_OK) return rc;
     AdjointState* st = adj_state(ctx);

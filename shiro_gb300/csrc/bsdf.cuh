@@ -255,6 +255,107 @@ static __device__ __noinline__ V3 bsdf_eval(const Mat& m, const V3& n, const V3&
     return diffuse + spec + coat + sheen;
 }
 
+// ---- transmission, media, emitters (CpuPathTracer.cpp:930-932, 1011-1033,
+// 1059-1063, 1084-1094, 1136-1212, 1355-1373, 1405-1441) ------------------
+__device__ __forceinline__ float transmission_roughness(const Mat& m) {
+    return sclamp(m.roughness + m.transmission_extra_roughness, 0.0f, 1.0f);
+}
+__device__ __forceinline__ float fresnel_dielectric(float cosThetaI, float etaI, float etaT) {
+    float c = sclamp(cosThetaI, -1.0f, 1.0f);
+    float ei = smax(etaI, 1.0e-6f);
+    float et = smax(etaT, 1.0e-6f);
+    if (c <= 0.0f) {
+        const float t = ei;
+        ei = et;
+        et = t;
+        c = fabsf(c);
+    }
+    const float sinI = sqrtf(smax(0.0f, 1.0f - c * c));
+    const float sinT = ei / et * sinI;
+    if (sinT >= 1.0f) return 1.0f;
+    const float cosT = sqrtf(smax(0.0f, 1.0f - sinT * sinT));
+    const float rPar = ((et * c) - (ei * cosT)) / smax((et * c) + (ei * cosT), 1.0e-6f);
+    const float rPer = ((ei * c) - (et * cosT)) / smax((ei * c) + (et * cosT), 1.0e-6f);
+    return 0.5f * (rPar * rPar + rPer * rPer);
+}
+__device__ __forceinline__ V3 interface_transmittance(const V3& f0, float a, float b) {
+    const V3 fa = schlick(f0, sclamp(fabsf(a), 0.0f, 1.0f));
+    const V3 fb = schlick(f0, sclamp(fabsf(b), 0.0f, 1.0f));
+    return one_minus_clamped((fa + fb) * 0.5f);
+}
+__device__ __forceinline__ V3 coat_transmission_scale(const Mat& m, const V3& cn, const V3& v, const V3& l) {
+    return coat_tint(m) * interface_transmittance(coat_f0(m), dot(cn, v), dot(cn, l));
+}
+__device__ __forceinline__ V3 transmission_surface_tint(const Mat& m) {
+    if (!m.thin_walled && m.transmission_depth > 0.0f) return {1.0f, 1.0f, 1.0f};
+    return sclamp3(ld3(m.transmission_color), 0.0f, 1.0f);
+}
+__device__ __forceinline__ float thin_pane_transmittance(float r) {
+    const float c = sclamp(r, 0.0f, 1.0f);
+    return sclamp((1.0f - c) / smax(1.0f + c, 1.0e-6f), 0.0f, 1.0f);
+}
+__device__ __forceinline__ V3 medium_extinction(const Mat& m) {
+    V3 e{smax(m.transmission_scatter[0], 0.0f), smax(m.transmission_scatter[1], 0.0f),
+         smax(m.transmission_scatter[2], 0.0f)};
+    if (m.thin_walled || m.transmission_depth <= 0.0f) return e;
+    const float depth = smax(m.transmission_depth, 1.0e-3f);
+    const V3 tint = sclamp3(ld3(m.transmission_color), 1.0e-4f, 1.0f);
+    e.x += -logf(tint.x) / depth;
+    e.y += -logf(tint.y) / depth;
+    e.z += -logf(tint.z) / depth;
+    return e;
+}
+__device__ __forceinline__ V3 medium_attenuation(const V3& e, float d) {
+    return {expf(-e.x * d), expf(-e.y * d), expf(-e.z * d)};
+}
+__device__ __forceinline__ bool refract_dir(const V3& i, const V3& n, float eta, V3* out) {
+    const float c = sclamp(-dot(i, n), -1.0f, 1.0f);
+    const float sin2 = smax(0.0f, 1.0f - c * c);
+    const float k = 1.0f - eta * eta * sin2;
+    if (k <= 0.0f) return false;
+    *out = normalize(i * eta + n * (eta * c - sqrtf(k)));
+    return true;
+}
+static __device__ __noinline__ V3 transmission_lobe(const Mat& m, const V3& n, const V3& cn, const V3& v, const V3& l,
+                                                    float etaI, float etaT, float r) {
+    const float cosWo = dot(n, v), cosWi = dot(n, l);
+    const float aWo = fabsf(cosWo), aWi = fabsf(cosWi);
+    if (aWo <= 0.0f || aWi <= 0.0f || cosWo * cosWi >= 0.0f) return {0.0f, 0.0f, 0.0f};
+    const float rel = etaT / smax(etaI, 1.0e-6f);
+    V3 h = safe_normalized(v + l * rel, n);
+    if (dot(n, h) < 0.0f) h = h * -1.0f;
+    const float woH = dot(v, h), wiH = dot(l, h);
+    if (woH * wiH >= 0.0f) return {0.0f, 0.0f, 0.0f};
+    const float nh = sclamp(dot(n, h), 0.0f, 1.0f);
+    const float sd = woH + rel * wiH;
+    if (nh <= 0.0f || fabsf(sd) <= 1.0e-6f) return {0.0f, 0.0f, 0.0f};
+    const float dist = ggx_d(nh, r);
+    const float vis = ggx_vis(aWo, aWi, r);
+    const float fres = 1.0f - fresnel_dielectric(fabsf(woH), etaI, etaT);
+    const V3 scale = transmission_surface_tint(m) * coat_transmission_scale(m, cn, v, l) *
+                     (sclamp(m.transmission, 0.0f, 1.0f) * (1.0f - sclamp(m.metallic, 0.0f, 1.0f)));
+    const float factor = fabsf(dist * vis * fabsf(wiH) * fabsf(woH) / smax(aWo * aWi * sq(sd), 1.0e-6f));
+    const float transport = 1.0f / smax(rel * rel, 1.0e-6f);
+    return scale * fres * (factor * transport);
+}
+static __device__ __noinline__ float transmission_pdf(const V3& n, const V3& v, const V3& l, float eta, float r) {
+    const float cosWo = dot(n, v), cosWi = dot(n, l);
+    if (fabsf(cosWo) <= 0.0f || fabsf(cosWi) <= 0.0f || cosWo * cosWi >= 0.0f) return 0.0f;
+    V3 h = safe_normalized(v + l * eta, n);
+    if (dot(n, h) < 0.0f) h = h * -1.0f;
+    const float woH = dot(v, h), wiH = dot(l, h);
+    const float sd = woH + eta * wiH;
+    if (woH * wiH >= 0.0f || fabsf(sd) <= 1.0e-6f) return 0.0f;
+    const float nh = sclamp(dot(n, h), 0.0f, 1.0f);
+    const float pdfWh = ggx_d(nh, r) * nh;
+    const float dwh = fabsf((eta * eta * wiH) / sq(sd));
+    return pdfWh * dwh;
+}
+__device__ __forceinline__ V3 emitted_radiance(const Mat& m) {  // :1722-1727
+    return {smax(m.emission_color[0] * m.emission_strength, 0.0f), smax(m.emission_color[1] * m.emission_strength, 0.0f),
+            smax(m.emission_color[2] * m.emission_strength, 0.0f)};
+}
+
 __device__ __forceinline__ V3 cosine_hemisphere(const V3& n, const V2& s) {
     const float phi = 2.0f * kPi * s.x;
     const float r = sqrtf(s.y);

@@ -64,6 +64,8 @@ constexpr uint32_t kDirectDimBase = 256u;
 constexpr uint32_t kDirectDepthStride = 512u;
 constexpr uint32_t kDirectLightStride = 128u;
 constexpr uint32_t kDirectSampleStride = 2u;
+constexpr uint32_t kEmissiveDimBase = 8192u;
+constexpr uint32_t kEmissiveDepthStride = 8u;
 
 // Entries of the per-thread BVH traversal stack (the builder rejects deeper trees).
 constexpr int kStack = 96;

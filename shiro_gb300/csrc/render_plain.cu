@@ -14,6 +14,7 @@ namespace shiro_gpu {
 
 namespace {
 
+template <bool kExt>
 __global__ void __launch_bounds__(128) k_plain_paths(const DevScene s, const DevRequest q, uint64_t pathBase,
                                                      uint32_t count, float4* __restrict__ records) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -24,7 +25,7 @@ __global__ void __launch_bounds__(128) k_plain_paths(const DevScene s, const Dev
     const uint32_t y = static_cast<uint32_t>(pixel / q.width);
     const uint32_t x = static_cast<uint32_t>(pixel - static_cast<uint64_t>(y) * q.width);
     NullCounter ctr;
-    const PathResult r = trace_path(s, q, x, y, q.sampleStart + smp, ctr);
+    const PathResult r = trace_path<kExt>(s, q, x, y, q.sampleStart + smp, ctr);
     float4* o = records + 3 * static_cast<size_t>(i);
     o[0] = make_float4(r.radiance.x, r.radiance.y, r.radiance.z, r.depth);
     o[1] = make_float4(r.albedo.x, r.albedo.y, r.albedo.z, 0.0f);
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(128) k_count_paths(const DevScene s, const Dev
         const uint32_t smp = static_cast<uint32_t>(path - pixel * q.sampleCount);
         const uint32_t y = static_cast<uint32_t>(pixel / q.width);
         const uint32_t x = static_cast<uint32_t>(pixel - static_cast<uint64_t>(y) * q.width);
-        trace_path(s, q, x, y, q.sampleStart + smp, c);
+        trace_path<true>(s, q, x, y, q.sampleStart + smp, c);
         traced = 1;
     }
     const uint32_t v[12] = {traced,  c.closestRays, c.occlusionRays, c.nodes + c.onodes, c.tris + c.otris, c.hits,
@@ -129,7 +130,10 @@ inline unsigned grid(uint64_t n, unsigned b) { return static_cast<unsigned>((n +
 void launch_plain_paths(const DevScene& s, const DevRequest& q, uint64_t pathBase, uint32_t count, float4* records,
                         cudaStream_t stream) {
     if (count == 0) return;
-    k_plain_paths<<<grid(count, 128), 128, 0, stream>>>(s, q, pathBase, count, records);
+    if (s.extended)
+        k_plain_paths<true><<<grid(count, 128), 128, 0, stream>>>(s, q, pathBase, count, records);
+    else
+        k_plain_paths<false><<<grid(count, 128), 128, 0, stream>>>(s, q, pathBase, count, records);
 }
 
 void launch_resolve_pixels(const DevRequest& q, uint64_t pixelBase, uint32_t count, const float4* records, AovPtrs aov,

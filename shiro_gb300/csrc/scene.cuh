@@ -13,6 +13,9 @@
 //   materials  ShiroMaterialDesc, the PbrMaterial fields verbatim
 //   envs       per dome texture: texels (rgb, pixel probability mass),
 //              row / conditional CDFs, alias table
+//   emissive   the emissive triangles in mesh / primitive order with the
+//              float running sums of their selection weights (area x
+//              luminance), as BuildAccelerationScene forms them
 #pragma once
 
 #include "../../include/shiro_gpu.h"
@@ -60,7 +63,13 @@ struct DevScene {
     uint32_t domeCount;
     V3 envTop, envBottom;
     uint32_t rootIsLeaf;            // scene of <= 8 triangles: node 0 holds them all
-    uint32_t pad;
+    uint32_t emissiveCount;         // emissive triangles (AccelerationScene::emissiveTriangles)
+    const float4* emissive;         // 3 per emissive triangle: (area, selection weight, running sum, gid bits),
+                                    // (radiance, 0), (unit geometric normal, 0)
+    const float* emissiveCdf;       // running sums of the selection weights
+    const int32_t* emissiveOf;      // per global triangle: its emissive entry or -1
+    float emissiveSum;
+    uint32_t extended;              // some material uses transmission, opacity or emission
 };
 
 // Per-request constants.

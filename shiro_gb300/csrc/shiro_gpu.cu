@@ -349,21 +349,12 @@ int supports(const ShiroSceneDesc* scene, std::string* why) {
         *why = "null scene";
         return 0;
     }
-    for (uint32_t i = 0; i < scene->material_count; ++i) {
-        const ShiroMaterialDesc& m = scene->materials[i];
-        if (has_transmission(m)) {
-            *why = "material " + std::to_string(i) + " uses transmission";
-            return 0;
-        }
-        if (hclamp(m.opacity, 0.0f, 1.0f) < 0.999f) {
-            *why = "material " + std::to_string(i) + " uses opacity";
-            return 0;
-        }
-        if (m.emission_strength > 0.0f) {
-            *why = "material " + std::to_string(i) + " is emissive";
-            return 0;
-        }
+    if (scene->material_count && !scene->materials) {
+        *why = "null material array";
+        return 0;
     }
+    // every lobe of TracePath is implemented (transmission and media,
+    // opacity cut-outs, emitters with their light sample)
     return 1;
 }
 
@@ -554,6 +545,50 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     }
     if (ttotal == 0) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene has no triangles");
 
+    // --- emissive triangles (BuildAccelerationScene, CpuPathTracer.cpp:482-522;
+    // TriangleArea :198-222), float running sums in mesh / primitive order ----
+    std::vector<float4> emissive;
+    std::vector<float> emissiveCdf;
+    std::vector<int32_t> emissiveOf(ttotal, -1);
+    float emissiveSum = 0.0f;
+    {
+        const ShiroMaterialDesc dflt = default_material();
+        uint32_t g = 0;
+        for (uint32_t i = 0; i < sd->mesh_count; ++i) {
+            const ShiroMeshDesc& m = sd->meshes[i];
+            const uint32_t prims = m.index_count / 3u;
+            const ShiroMaterialDesc& mat = m.material_index < sd->material_count ? sd->materials[m.material_index] : dflt;
+            const float le[3] = {std::max(mat.emission_color[0] * mat.emission_strength, 0.0f),
+                                 std::max(mat.emission_color[1] * mat.emission_strength, 0.0f),
+                                 std::max(mat.emission_color[2] * mat.emission_strength, 0.0f)};
+            const float w = std::max(0.2126f * le[0] + 0.7152f * le[1] + 0.0722f * le[2], 0.0f);
+            if (m.index_count < 3 || m.index_count % 3 != 0 || w <= 0.0f) {
+                g += prims;
+                continue;
+            }
+            for (uint32_t t = 0; t < prims; ++t, ++g) {
+                const float* p0 = m.positions + 3 * static_cast<size_t>(m.indices[3 * t]);
+                const float* p1 = m.positions + 3 * static_cast<size_t>(m.indices[3 * t + 1]);
+                const float* p2 = m.positions + 3 * static_cast<size_t>(m.indices[3 * t + 2]);
+                const float a[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+                const float b[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+                const float av[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+                const float dbl = std::sqrt(av[0] * av[0] + av[1] * av[1] + av[2] * av[2]);
+                if (dbl <= 1.0e-8f) continue;
+                const float area = dbl * 0.5f;
+                const float sel = area * w;
+                emissiveSum += sel;
+                emissiveOf[g] = static_cast<int32_t>(emissiveCdf.size());
+                float gbits;
+                std::memcpy(&gbits, &g, 4);
+                emissive.push_back(make_float4(area, sel, emissiveSum, gbits));
+                emissive.push_back(make_float4(le[0], le[1], le[2], 0.0f));
+                emissive.push_back(make_float4(av[0] / dbl, av[1] / dbl, av[2] / dbl, 0.0f));
+                emissiveCdf.push_back(emissiveSum);
+            }
+        }
+    }
+
     // --- large triangles + inflated boxes -----------------------------------
     auto area = [](const float* lo, const float* hi) {
         const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
@@ -685,6 +720,20 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     if ((rc = upload(ctx, positions, &s.positions, "positions")) != SHIRO_OK) return rc;
     if ((rc = upload(ctx, meshMaterial, &s.meshMaterial, "mesh materials")) != SHIRO_OK) return rc;
     if ((rc = upload(ctx, meshHasNormals, &s.meshHasNormals, "mesh normal flags")) != SHIRO_OK) return rc;
+    s.emissiveCount = static_cast<uint32_t>(emissiveCdf.size());
+    s.emissiveSum = emissiveSum;
+    if (s.emissiveCount) {
+        if ((rc = upload(ctx, emissive, &s.emissive, "emissive triangles")) != SHIRO_OK) return rc;
+        if ((rc = upload(ctx, emissiveCdf, &s.emissiveCdf, "emissive weights")) != SHIRO_OK) return rc;
+        if ((rc = upload(ctx, emissiveOf, &s.emissiveOf, "emissive index")) != SHIRO_OK) return rc;
+    }
+    ctx->extendedMaterials = false;
+    for (uint32_t i = 0; i < sd->material_count; ++i) {
+        const ShiroMaterialDesc& m = sd->materials[i];
+        if (has_transmission(m) || hclamp(m.opacity, 0.0f, 1.0f) < 0.999f || m.emission_strength > 0.0f)
+            ctx->extendedMaterials = true;
+    }
+    s.extended = ctx->extendedMaterials ? 1u : 0u;
     if ((rc = upload(ctx, ctx->materialsHost, &s.materials, "materials")) != SHIRO_OK) return rc;
     std::vector<DevDistant> distant(sd->distant_light_count);
     for (uint32_t i = 0; i < sd->distant_light_count; ++i)

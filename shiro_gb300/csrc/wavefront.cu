@@ -56,9 +56,19 @@ struct WfRequest {
     AovPtrs aov;
 };
 
-// State flag bits (T.w)
+// State flag bits (T.w): diffuse depth (bits 0-7), specular depth (8-15),
+// previous bounce delta, path done, previous bounce type (18-19), inside a
+// transmissive object, its medium attenuating.
 constexpr uint32_t kFlagPrevDelta = 1u << 16;
 constexpr uint32_t kFlagDone = 1u << 17;
+constexpr uint32_t kTypeShift = 18;
+constexpr uint32_t kFlagInside = 1u << 20;
+constexpr uint32_t kFlagMedium = 1u << 21;
+
+__device__ __forceinline__ uint32_t pack_state(const PathState& ps) {
+    return (ps.diffDepth & 0xffu) | ((ps.specDepth & 0xffu) << 8) | (ps.prevDelta ? kFlagPrevDelta : 0u) |
+           ((ps.prevType & 3u) << kTypeShift) | (ps.inside ? kFlagInside : 0u) | (ps.mediumActive ? kFlagMedium : 0u);
+}
 
 // Work-fetch counters of the persistent stages (slots of WfView::counters).
 constexpr uint32_t kFetchExtend = 5, kFetchShade = 6, kFetchOcclude = 7;
@@ -74,11 +84,12 @@ struct WfView {
     float4* rad;     // radiance.xyz, first-hit depth
     uint4* ident;    // px, py, sample index, request
     float4* hit;     // t, u, v, slot bits
+    float4* medium;  // extinction of the medium the path is in (while it attenuates)
     uint32_t* hitGid;
     // shadow records
     float4* shOrigin;  // origin.xyz
     float4* shT;       // throughput at the vertex
-    float4* shDir;     // [lightSamples][P]: dir.xyz, valid
+    float4* shDir;     // [lightSamples][P]: dir.xyz, reach of the shadow ray (0: no sample / occluded)
     float4* shC;       // [lightSamples][P]: contribution
     uint32_t* rayQ0;
     uint32_t* rayQ1;
@@ -316,8 +327,9 @@ __device__ __forceinline__ void write_record(const WfView& v, uint32_t j, const 
     v.records[3 * static_cast<size_t>(j)] = make_float4(rad.x, rad.y, rad.z, depth0);
 }
 
-// Shade stage, compiled with several register caps (the autotuner picks).
-template <int kRegs>
+// Shade stage, compiled with several register caps (the autotuner picks) and
+// with / without the extended lobes (kExt, chosen by the scene).
+template <int kRegs, bool kExt>
 __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, uint32_t depth) {
     const uint32_t hits = v.counters[kHitCount];
     const uint32_t count = hits + v.counters[kMissCount];
@@ -349,6 +361,14 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
             ps.diffDepth = bits & 0xffu;
             ps.specDepth = (bits >> 8) & 0xffu;
             ps.prevDelta = (bits & kFlagPrevDelta) != 0u;
+            ps.prevType = (bits >> kTypeShift) & 3u;
+            ps.inside = (bits & kFlagInside) != 0u;
+            ps.mediumActive = (bits & kFlagMedium) != 0u;
+            ps.extinction = V3{0.0f, 0.0f, 0.0f};
+            if (kExt && ps.mediumActive) {
+                const float4 m4 = v.medium[j];
+                ps.extinction = V3{m4.x, m4.y, m4.z};
+            }
             float depth0 = r4.w;
             HitRec h;
             h.t = h4.x;
@@ -361,34 +381,44 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
                 write_record(v, j, ps.radiance, depth0);
             } else {
                 const Vertex vx = make_vertex(s, ps.ro, ps.rd, h);
-                if (depth == 0) {
-                    const V3 alb = diffuse_color(s.materials[vx.hit.material]);
-                    const V3 nn = vx.n * 0.5f + V3{0.5f, 0.5f, 0.5f};
-                    v.records[3 * static_cast<size_t>(j) + 1] = make_float4(alb.x, alb.y, alb.z, 0.0f);
-                    v.records[3 * static_cast<size_t>(j) + 2] = make_float4(nn.x, nn.y, nn.z, 0.0f);
-                    depth0 = h.t;
-                }
                 const Sampler smp{id.x, id.y, id.z};
-                bool anyLight = false;
-                for (uint32_t k = 0; k < v.lightSamples; ++k) {
-                    V3 dir{0.0f, 0.0f, 0.0f}, c{0.0f, 0.0f, 0.0f};
-                    const bool ok = light_sample(s, q, vx, smp, depth, k, &dir, &c, ctr);
-                    anyLight |= ok;
-                    lightMask |= ok ? (1u << k) : 0u;
-                    const size_t e = static_cast<size_t>(k) * v.P + j;
-                    v.shDir[e] = make_float4(dir.x, dir.y, dir.z, ok ? 1.0f : 0.0f);
-                    v.shC[e] = make_float4(c.x, c.y, c.z, 0.0f);
+                bool anyLight = false, cont;
+                if (kExt && !enter_hit(s, smp, depth, vx, h.t, ps)) {
+                    cont = depth + 1u < q.maxDepth;  // passes through an opacity cut-out
+                } else {
+                    if (depth == 0) {
+                        const V3 alb = diffuse_color(s.materials[vx.hit.material]);
+                        const V3 nn = vx.n * 0.5f + V3{0.5f, 0.5f, 0.5f};
+                        v.records[3 * static_cast<size_t>(j) + 1] = make_float4(alb.x, alb.y, alb.z, 0.0f);
+                        v.records[3 * static_cast<size_t>(j) + 2] = make_float4(nn.x, nn.y, nn.z, 0.0f);
+                        depth0 = h.t;
+                    }
+                    if constexpr (kExt) add_emission(s, vx, depth, ps);
+                    // this request's light samples (requests of a batch may differ in dome samples)
+                    const uint32_t nls = light_sample_count<kExt>(s, q);
+                    for (uint32_t k = 0; k < nls; ++k) {
+                        V3 dir{0.0f, 0.0f, 0.0f}, c{0.0f, 0.0f, 0.0f};
+                        float reach = 0.0f;
+                        const bool ok = light_sample<kExt>(s, q, vx, smp, depth, k, &dir, &c, &reach, ctr);
+                        anyLight |= ok;
+                        lightMask |= ok ? (1u << k) : 0u;
+                        const size_t e = static_cast<size_t>(k) * v.P + j;
+                        v.shDir[e] = make_float4(dir.x, dir.y, dir.z, ok ? reach : 0.0f);
+                        v.shC[e] = make_float4(c.x, c.y, c.z, 0.0f);
+                    }
+                    if (anyLight) {
+                        const V3 org = shadow_origin(vx);
+                        v.shOrigin[j] = make_float4(org.x, org.y, org.z, 0.0f);
+                        v.shT[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, 0.0f);
+                        pushShadow = true;
+                    }
+                    cont = continue_path<kExt>(s, q, vx, smp, depth, ps, ctr) && depth + 1u < q.maxDepth;
                 }
-                if (anyLight) {
-                    const V3 org = shadow_origin(vx);
-                    v.shOrigin[j] = make_float4(org.x, org.y, org.z, 0.0f);
-                    v.shT[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, 0.0f);
-                    pushShadow = true;
-                }
-                const bool cont = continue_path(s, q, vx, smp, depth, ps, ctr) && depth + 1u < q.maxDepth;
-                uint32_t nb = (ps.diffDepth & 0xffu) | ((ps.specDepth & 0xffu) << 8) | (ps.prevDelta ? kFlagPrevDelta : 0u);
+                uint32_t nb = pack_state(ps);
                 if (!cont && anyLight) nb |= kFlagDone;
                 v.T[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, __uint_as_float(nb));
+                if (kExt && ps.mediumActive)
+                    v.medium[j] = make_float4(ps.extinction.x, ps.extinction.y, ps.extinction.z, 0.0f);
                 if (cont) {
                     v.ro[j] = make_float4(ps.ro.x, ps.ro.y, ps.ro.z, 0.0f);
                     v.rd[j] = make_float4(ps.rd.x, ps.rd.y, ps.rd.z, ps.prevPdf);
@@ -421,7 +451,7 @@ __global__ void __launch_bounds__(256, 4) wf_occlude(WfView v, DevScene s) {
         const uint32_t j = item >> 3, k = item & 7u;
         const size_t e = static_cast<size_t>(k) * v.P + j;
         const float4 o4 = v.shOrigin[j], d4 = v.shDir[e];
-        if (trace_occluded(s, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, FLT_MAX, ctr)) v.shDir[e].w = 0.0f;
+        if (trace_occluded(s, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, d4.w, ctr)) v.shDir[e].w = 0.0f;
     }
 }
 
@@ -432,7 +462,7 @@ __global__ void __launch_bounds__(256) wf_shadow(WfView v, DevScene s) {
         const uint32_t j = v.shadowQ[i];
         const DevRequest& q = v.reqs[v.ident[j].w].q;
         const float4 t4 = v.shT[j], r4 = v.rad[j];
-        const V3 direct = sum_direct(s, q, [&](uint32_t k, V3* c) {
+        const V3 direct = sum_direct<true>(s, q, [&](uint32_t k, V3* c) {
             const size_t e = static_cast<size_t>(k) * v.P + j;
             if (v.shDir[e].w == 0.0f) return false;
             const float4 c4 = v.shC[e];
@@ -532,7 +562,7 @@ WavefrontState* wf_state(ContextImpl* ctx) {
 
 bool ensure_pool(ContextImpl* ctx, WavefrontState* wf, uint32_t P, uint32_t lightSamples) {
     const size_t p = P;
-    const size_t stateBytes = p * (6 * sizeof(float4) + sizeof(uint32_t));
+    const size_t stateBytes = p * (7 * sizeof(float4) + sizeof(uint32_t));
     const size_t shadowBytes = p * (2 + 2 * static_cast<size_t>(std::max(1u, lightSamples))) * sizeof(float4);
     const size_t queueBytes = p * (4 + static_cast<size_t>(std::max(1u, lightSamples))) * sizeof(uint32_t) + 64;
     const size_t recordBytes = p * 3 * sizeof(float4);
@@ -556,7 +586,8 @@ WfView make_view(WavefrontState* wf, uint32_t P, uint32_t lightSamples, const Wa
     v.rad = v.T + p;
     v.ident = reinterpret_cast<uint4*>(v.rad + p);
     v.hit = reinterpret_cast<float4*>(v.ident + p);
-    v.hitGid = reinterpret_cast<uint32_t*>(v.hit + p);
+    v.medium = v.hit + p;
+    v.hitGid = reinterpret_cast<uint32_t*>(v.medium + p);
     float4* sh = static_cast<float4*>(wf->shadow.ptr);
     v.shOrigin = sh;
     v.shT = sh + p;
@@ -643,13 +674,20 @@ struct Launch {
     int bExt, bShade, bShadow;
     uint32_t depth;
     uint32_t shadeRegs;
+    bool ext;  // the scene uses transmission, opacity or emitters
 };
 
 void launch_shade(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t d) {
-    if (L.shadeRegs == 96)
-        wf_shade<96><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
-    else
-        wf_shade<128><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
+    if (L.ext) {
+        if (L.shadeRegs == 96)
+            wf_shade<96, true><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
+        else
+            wf_shade<128, true><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
+    } else if (L.shadeRegs == 96) {
+        wf_shade<96, false><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
+    } else {
+        wf_shade<128, false><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
+    }
 }
 
 void enqueue_wave(const Launch& L, cudaStream_t st) {
@@ -699,6 +737,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     uint32_t domeSamplesMax = 1;
     for (const DevRequest& q : qs) domeSamplesMax = std::max(domeSamplesMax, q.domeSamples);
     lightSamples += ctx->scene.domeCount * domeSamplesMax;
+    if (ctx->scene.emissiveCount > 0 && ctx->scene.emissiveSum > 0.0f) lightSamples += 1;
     if (lightSamples > kMaxLightSamples)
         return fail(ctx, SHIRO_ERR_UNSUPPORTED_SCENE, "wavefront form: more than 8 light samples per shading point");
     uint32_t maxSpp = 1;
@@ -741,8 +780,11 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.gGen = grid_for(wf_generate, 128, wf->smCount);
     L.gExt = grid_for(wf_extend, L.bExt, wf->smCount);
     L.shadeRegs = cfg.shade_regs;
-    L.gShade = L.shadeRegs == 96 ? grid_for(wf_shade<96>, L.bShade, wf->smCount)
-                                 : grid_for(wf_shade<128>, L.bShade, wf->smCount);
+    L.ext = ctx->extendedMaterials;
+    L.gShade = L.shadeRegs == 96 ? (L.ext ? grid_for(wf_shade<96, true>, L.bShade, wf->smCount)
+                                          : grid_for(wf_shade<96, false>, L.bShade, wf->smCount))
+                                 : (L.ext ? grid_for(wf_shade<128, true>, L.bShade, wf->smCount)
+                                          : grid_for(wf_shade<128, false>, L.bShade, wf->smCount));
     L.v.travSteps = static_cast<int>(cfg.extend_steps ? cfg.extend_steps : 4);
     L.v.refillIdle = static_cast<int>(cfg.refill_idle ? cfg.refill_idle : 8);
     L.gShadow = grid_for(wf_shadow, 256, wf->smCount);

@@ -83,7 +83,9 @@ def test_status_without_device_is_unavailable(lib):
         GpuBackend(0)  # no silent CPU fallback
 
 
-def test_unsupported_scene_detection_on_host(lib):
+def test_scene_support_on_host(lib):
+    """Every lobe of the reference's TracePath is implemented: opacity,
+    transmission and emitters are accepted; only a malformed snapshot is not."""
     from shiro_gb300 import scenes
     from shiro_gb300.abi import MarshalledScene
 
@@ -91,5 +93,9 @@ def test_unsupported_scene_detection_on_host(lib):
     buf = C.create_string_buffer(128)
     assert lib.shiro_gpu_supports_scene(MarshalledScene(sc).ref(), buf, 128) == 1
     sc.materials[0].opacity = 0.5
-    assert lib.shiro_gpu_supports_scene(MarshalledScene(sc).ref(), buf, 128) == 0
-    assert b"opacity" in buf.value
+    sc.materials[0].transmission = 1.0
+    sc.materials[1].emission_strength = 3.0
+    sc.materials[1].emission_color = (1.0, 1.0, 1.0)
+    assert lib.shiro_gpu_supports_scene(MarshalledScene(sc).ref(), buf, 128) == 1
+    assert lib.shiro_gpu_supports_scene(None, buf, 128) == 0
+    assert b"null" in buf.value

@@ -169,3 +169,24 @@ def test_autograd_function(setup):
     gpu.adjoint(cam, st, d, grads, flags=NO_CLAMP)
     for k in p:
         torch.testing.assert_close(params[k].grad, grads[k], rtol=1e-4, atol=1e-7)
+
+
+def test_adjoint_rejects_extended_lobes():
+    """The differentiable form covers reflecting materials; a scene with
+    transmission (or opacity, or emitters) is refused, not approximated."""
+    from shiro_gb300 import GpuBackend, ShiroGpuError, scenes
+    from shiro_gb300.abi import RenderSettings
+
+    scene = scenes.split_sphere_scene(parts=4, env_width=32, env_height=16, seed=4)
+    scene.materials[1].transmission = 1.0
+    st = RenderSettings(width=16, height=16, samples_per_pixel=2, max_depth=3, diffuse_depth=3, specular_depth=3,
+                        backend=1)
+    cam = scenes.look_at((0.0, 1.6, 4.5), (0.0, 0.9, 0.0), 45.0, 1.0)
+    with GpuBackend(0) as gpu:
+        gpu.upload_scene(scene)
+        gpu.render(scene, cam, st)  # rendering is supported
+        d = torch.zeros((16, 16, 4), device="cuda")
+        grads = {"base_color": torch.zeros((len(scene.materials), 3), device="cuda")}
+        with pytest.raises(ShiroGpuError) as ei:
+            gpu.adjoint(cam, st, d, grads)
+        assert ei.value.code == -5

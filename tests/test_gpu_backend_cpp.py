@@ -62,7 +62,9 @@ def test_batched_requests_through_adapter(backend_lib, gpu):
         assert np.array_equal(fb.beauty, ref.beauty)
 
 
-def test_unsupported_scene_is_declined(backend_lib):
+def test_emissive_scene_renders_through_adapter(backend_lib, gpu):
+    """A scene with an emitter (once declined by SupportsScene) now renders on
+    the GPU through the adapter and equals the direct C ABI render."""
     from shiro_gb300 import scenes
     from shiro_gb300.abi import FrameBuffer, MarshalledScene, render_desc
 
@@ -72,4 +74,6 @@ def test_unsupported_scene_is_declined(backend_lib):
     fb = FrameBuffer(8, 8)
     aov = fb.aovs()
     req = render_desc(w.camera, w.settings, 0, 1)
-    assert backend_lib.shiro_backend_selftest(MarshalledScene(w.scene).ref(), C.byref(req), 1, C.byref(aov)) == 0
+    assert backend_lib.shiro_backend_selftest(MarshalledScene(w.scene).ref(), C.byref(req), 1, C.byref(aov)) == 1
+    ref = gpu.render(w.scene, w.camera, w.settings, 0, 1)
+    assert np.array_equal(fb.beauty, ref.beauty)

@@ -91,7 +91,8 @@ def test_field_rays_vs_bruteforce(gpu, port):
     assert np.array_equal(occ, bo)
 
 
-RENDERS = ["sphere", "rich", "features_gradient_env", "angular_env", "field_small", "sphere_1spp_start5"]
+RENDERS = ["sphere", "rich", "features_gradient_env", "angular_env", "field_small", "sphere_1spp_start5", "emissive",
+           "opacity", "transmission"]
 
 
 @pytest.mark.parametrize("name", RENDERS)
@@ -161,10 +162,8 @@ def test_errors_are_reported(gpu):
     from shiro_gb300.abi import Mesh, Scene
 
     sc = scenes.sphere_scene(16, 8)
-    sc.materials[0].transmission = 1.0
-    assert not gpu.supports_scene(sc)
-    with pytest.raises(ShiroGpuError):
-        gpu.upload_scene(sc, force=True)
+    sc.materials[0].transmission = 1.0  # every lobe of the reference is supported
+    assert gpu.supports_scene(sc)
     bad = Scene(materials=[], meshes=[Mesh(np.zeros((3, 3), np.float32), np.array([0, 1, 5], np.uint32))])
     with pytest.raises(ShiroGpuError):
         gpu.upload_scene(bad, force=True)

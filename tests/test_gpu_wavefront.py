@@ -53,6 +53,35 @@ def test_field_scene_bit_identical(gpu, flags):
     assert ok, (k, n)
 
 
+@pytest.mark.parametrize("name", ["emissive", "opacity", "transmission"])
+def test_extended_lobes_bit_identical(gpu, name):
+    """Transmission and media, opacity cut-outs and emitters: the wavefront
+    stages (pass-through hits, the emissive light sample with its finite
+    shadow ray, medium state across bounces) match the plain form."""
+    from conftest import golden
+    from scene_io import camera_from_array, scene_from_arrays, settings_from_array
+
+    g = golden(f"render_{name}.npz")
+    sc, cam, st = scene_from_arrays(g), camera_from_array(g["cam"]), settings_from_array(g["settings"])
+    plain = gpu.render(sc, cam, st, 0, 16)
+    (wave,) = gpu.render_batch(sc, [(cam, st, 0, 16)])
+    ok, k, n = same(plain, wave)
+    assert ok, (name, k, n)
+
+
+def test_mixed_dome_samples_in_batch(gpu):
+    """Requests of one batch with different dome-sample counts each use their
+    own light samples."""
+    from shiro_gb300 import scenes
+
+    w = scenes.sphere_workload(24, 16, 4, 5, env_width=64, env_height=32)
+    a = w.settings
+    b = scenes.RenderSettings(**{**a.__dict__, "dome_light_samples": 3})
+    outs = gpu.render_batch(w.scene, [(w.camera, a), (w.camera, b)])
+    assert same(outs[0], gpu.render(w.scene, w.camera, a))[0]
+    assert same(outs[1], gpu.render(w.scene, w.camera, b))[0]
+
+
 def test_uneven_batch_small_pool(gpu):
     """Many requests of uneven size / spp / depth, packed into waves much
     smaller than a frame (pixels of one request straddle several waves)."""
