@@ -516,13 +516,13 @@ def main():
     # end to end through the public API with host FrameBuffer planes
     e2e = None
     if not args.no_e2e:
-        fb = FrameBuffer(st.width, st.height)
+        fb = FrameBuffer(st.width, st.height, pinned=True)  # the caller's frame, page-locked, reused per step
 
         def api_step():
             if head == "plain":
                 gpu.render(w.scene, w.camera, st, start, spp, out=fb)
             else:
-                gpu.render_batch(w.scene, [(w.camera, st, start, spp)])
+                gpu.render_batch(w.scene, [(w.camera, st, start, spp)], outs_fb=[fb])
 
         api_step()
         if dist:
@@ -541,7 +541,8 @@ def main():
         req_bytes = C.sizeof(render_desc(w.camera, st, 0, 1))
         e2e = {"value": total_paths / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": req_bytes,
                "d2h_bytes_per_step": npx * 44, "form": head, "note": "scene resident (uploaded once, "
-               f"{upload_s:.2f} s incl. BVH build); per step: request in, 4 AOV planes out"}
+               f"{upload_s:.2f} s incl. BVH build); per step: request in, 4 AOV planes out into a page-locked "
+               "host FrameBuffer"}
 
     # replicas: one host-staged combination of the ranks' frames (outside the
     # timed region; the data path has no collective)

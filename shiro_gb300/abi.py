@@ -382,15 +382,33 @@ class MarshalledScene:
 
 
 class FrameBuffer:
-    """shiro::render::FrameBuffer (FrameBuffer.h:10-37) as numpy planes."""
+    """shiro::render::FrameBuffer (FrameBuffer.h:10-37) as numpy planes.
 
-    def __init__(self, width: int, height: int):
+    pinned=True places the planes in page-locked host memory (allocated
+    through torch), so a render's device-to-host copy of the AOVs runs at
+    full link speed instead of through the driver's pageable staging."""
+
+    def __init__(self, width: int, height: int, pinned: bool = False):
         self.width, self.height = int(width), int(height)
         n = self.width * self.height
-        self.beauty = np.zeros((n, 4), np.float32)
-        self.albedo = np.zeros((n, 3), np.float32)
-        self.normal = np.zeros((n, 3), np.float32)
-        self.depth = np.full((n,), np.inf, np.float32)
+        if pinned:
+            import torch
+
+            self._pinned = torch.empty(11 * n, dtype=torch.float32, pin_memory=True)
+            flat = self._pinned.numpy()
+            self.beauty = flat[:4 * n].reshape(n, 4)
+            self.albedo = flat[4 * n:7 * n].reshape(n, 3)
+            self.normal = flat[7 * n:10 * n].reshape(n, 3)
+            self.depth = flat[10 * n:]
+            self.beauty[:] = 0.0
+            self.albedo[:] = 0.0
+            self.normal[:] = 0.0
+            self.depth[:] = np.inf
+        else:
+            self.beauty = np.zeros((n, 4), np.float32)
+            self.albedo = np.zeros((n, 3), np.float32)
+            self.normal = np.zeros((n, 3), np.float32)
+            self.depth = np.full((n,), np.inf, np.float32)
 
     def aovs(self) -> Aovs:
         return Aovs(_fptr(self.beauty), _fptr(self.albedo), _fptr(self.normal), _fptr(self.depth), 0, 0)

@@ -192,8 +192,10 @@ class GpuBackend:
 
     # -- wavefront ---------------------------------------------------------
     def render_batch(self, scene: Scene, requests: Sequence[tuple], flags: int = 0,
-                     cancel: Optional[C.c_int] = None) -> List[FrameBuffer]:
-        """requests: (camera, settings[, sample_start[, sample_count]])."""
+                     cancel: Optional[C.c_int] = None, outs_fb: Optional[Sequence[FrameBuffer]] = None
+                     ) -> List[FrameBuffer]:
+        """requests: (camera, settings[, sample_start[, sample_count]]);
+        outs_fb: frame buffers to fill (reused across calls), else new ones."""
         self.upload_scene(scene)
         n = len(requests)
         descs = (RenderDesc * max(1, n))()
@@ -204,7 +206,7 @@ class GpuBackend:
             start = r[2] if len(r) > 2 else 0
             count = r[3] if len(r) > 3 else st.samples_per_pixel
             descs[i] = render_desc(cam, st, start, count, flags)
-            fb = FrameBuffer(st.width, st.height)
+            fb = outs_fb[i] if outs_fb is not None else FrameBuffer(st.width, st.height)
             fbs.append(fb)
             outs[i] = fb.aovs()
         rc = self.lib.shiro_gpu_render_batch(self._ctx, descs, n, C.byref(cancel) if cancel is not None else None, outs)

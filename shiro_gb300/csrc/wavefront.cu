@@ -539,6 +539,11 @@ struct WavefrontState {
     uint32_t P = 0, lightSamples = 0;
     int smCount = 0;
     bool tuned = false;
+    // the last instantiated wave graph and the launch parameters it bakes in
+    // (reused while a call's parameters are byte-identical: only the tables'
+    // contents differ between such calls, and the kernels read them from memory)
+    cudaGraphExec_t exec = nullptr;
+    std::vector<unsigned char> execKey;
 };
 
 namespace {
@@ -768,6 +773,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     if (e == cudaSuccess) e = cudaMemcpyAsync(dReqs, rq.data(), rq.size() * sizeof(WfRequest), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "wavefront tables");
     Launch L;
+    std::memset(&L, 0, sizeof(L));  // padding too: the bytes key the graph cache
     L.v = make_view(wf, poolP, lightSamples, dWaves, dSegs, dReqs);
     L.s = ctx->scene;
     if (ctx->bvhWidth != 2 && ctx->nodes8) {  // the wavefront stages traverse the wide BVH unless told otherwise
@@ -804,15 +810,29 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     cudaGraphExec_t exec = nullptr;
     int rc = SHIRO_OK;
     if (cfg.use_graph) {
-        cudaGraph_t graph = nullptr;
-        e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            enqueue_wave(L, st);
-            e = cudaStreamEndCapture(st, &graph);
+        const unsigned char* key = reinterpret_cast<const unsigned char*>(&L);
+        if (wf->exec && wf->execKey.size() == sizeof(Launch) && std::memcmp(wf->execKey.data(), key, sizeof(Launch)) == 0) {
+            exec = wf->exec;
+        } else {
+            if (wf->exec) cudaGraphExecDestroy(wf->exec);
+            wf->exec = nullptr;
+            wf->execKey.clear();
+            cudaGraph_t graph = nullptr;
+            e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                enqueue_wave(L, st);
+                e = cudaStreamEndCapture(st, &graph);
+            }
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                exec = nullptr;
+                rc = cuda_fail(ctx, e, "wavefront graph");
+            } else {
+                wf->exec = exec;
+                wf->execKey.assign(key, key + sizeof(Launch));
+            }
         }
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
-        if (graph) cudaGraphDestroy(graph);
-        if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront graph");
     }
     uint64_t launches = 0;
     for (uint32_t w = 0; w < used && rc == SHIRO_OK; ++w) {
@@ -836,7 +856,6 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (exec) cudaGraphExecDestroy(exec);
     double stageMs[6] = {0, 0, 0, 0, 0, 0};
     uint64_t stageN[6] = {0, 0, 0, 0, 0, 0};
     for (auto& x : ev) {
@@ -937,6 +956,7 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
 void wavefront_free(ContextImpl* ctx) {
     if (!ctx->wavefront) return;
     WavefrontState* wf = ctx->wavefront;
+    if (wf->exec) cudaGraphExecDestroy(wf->exec);
     for (DeviceBlock* b : {&wf->state, &wf->shadow, &wf->queues, &wf->records, &wf->tables})
         if (b->ptr) cudaFree(b->ptr);
     delete wf;
