@@ -494,6 +494,116 @@ __device__ __forceinline__ void node2_children(const float4* nodes2, int n, Entr
     b->lo[0] = n1.x; b->hi[0] = n1.y; b->lo[1] = n1.z; b->hi[1] = n1.w; b->lo[2] = n2.z; b->hi[2] = n2.w;
 }
 
+// ---- slot assignment by dynamic programming ----------------------------------
+// Which binary nodes become wide nodes is chosen to minimise a surface-area
+// cost (the optimal collapse of Ylitie, Karras and Laine 2017, restated):
+// G(n, k) is the least cost of representing the subtree of binary node n with
+// at most k child slots of a wide node,
+//   G(n, 1)  = kWideNodeCost * area(n) + S(n, 8)       (n becomes a wide node)
+//   G(n, k)  = min(G(n, k - 1), S(n, k))               (k >= 2: n is opened)
+//   S(n, k)  = min over j of Gc(left, j) + Gc(right, k - j)
+// where Gc of a binary leaf is kWideTriCost * area * triangles for any k.
+// Costs are evaluated bottom-up (a node after both children), decisions are
+// kept per (node, k) and replayed top-down by k_collapse_wide.
+constexpr float kWideNodeCost = 1.0f;
+constexpr float kWideTriCost = 0.3f;
+
+struct WideDp {
+    float* G;            // [node][8]: G(n, k + 1)
+    uint8_t* split;      // [node][8]: best j of S(n, k + 1) (k >= 1)
+    uint8_t* keep;       // [node]: bit k set when G(n, k + 1) = G(n, k)
+    int* parent;         // binary parent (-1: root)
+    unsigned int* ready; // children whose costs are known
+    uint8_t* start;      // both children are leaves / absent
+};
+
+__global__ void k_wide_parents(const float4* __restrict__ nodes2, uint32_t n2, WideDp dp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n2) return;
+    Entry a, b;
+    node2_children(nodes2, static_cast<int>(i), &a, &b);
+    unsigned int known = 0;
+    for (const Entry* e : {&a, &b}) {
+        if (e->lo[0] > e->hi[0] || e->link < 0) {
+            ++known;
+        } else {
+            dp.parent[e->link] = static_cast<int>(i);
+        }
+    }
+    dp.ready[i] = known;
+    dp.start[i] = known == 2 ? 1 : 0;
+}
+
+// Gc(child, j) for j = 1..8 into g[0..7].
+__device__ __forceinline__ void child_costs(const WideDp& dp, const Entry& e, float g[8]) {
+    if (e.lo[0] > e.hi[0]) {
+        for (int j = 0; j < 8; ++j) g[j] = 0.0f;
+    } else if (e.link < 0) {
+        const float c = kWideTriCost * entry_area(e) * static_cast<float>(leaf_count(e.link));
+        for (int j = 0; j < 8; ++j) g[j] = c;
+    } else {
+        for (int j = 0; j < 8; ++j) g[j] = __ldcg(&dp.G[8 * static_cast<size_t>(e.link) + j]);
+    }
+}
+
+__global__ void k_wide_costs(const float4* __restrict__ nodes2, uint32_t n2, WideDp dp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n2 || !dp.start[i]) return;
+    int n = static_cast<int>(i);
+    for (;;) {
+        Entry a, b;
+        node2_children(nodes2, n, &a, &b);
+        float ga[8], gb[8];
+        child_costs(dp, a, ga);
+        child_costs(dp, b, gb);
+        float S[9];
+        uint8_t js[9];
+        for (int k = 2; k <= 8; ++k) {
+            float best = FLT_MAX;
+            uint8_t bj = 1;
+            for (int j = 1; j < k; ++j) {
+                const float c = ga[j - 1] + gb[k - j - 1];
+                if (c < best) {
+                    best = c;
+                    bj = static_cast<uint8_t>(j);
+                }
+            }
+            S[k] = best;
+            js[k] = bj;
+        }
+        float lo[3], hi[3];
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(a.lo[k] <= a.hi[k] ? a.lo[k] : FLT_MAX, b.lo[k] <= b.hi[k] ? b.lo[k] : FLT_MAX);
+            hi[k] = fmaxf(a.lo[k] <= a.hi[k] ? a.hi[k] : -FLT_MAX, b.lo[k] <= b.hi[k] ? b.hi[k] : -FLT_MAX);
+        }
+        const float area = 2.0f * ((hi[0] - lo[0]) * (hi[1] - lo[1]) + (hi[1] - lo[1]) * (hi[2] - lo[2]) +
+                                   (hi[2] - lo[2]) * (hi[0] - lo[0]));
+        float* G = dp.G + 8 * static_cast<size_t>(n);
+        uint8_t* sp = dp.split + 8 * static_cast<size_t>(n);
+        float prev = kWideNodeCost * area + S[8];
+        G[0] = prev;
+        sp[0] = js[8];  // the split of n as a wide node
+        uint8_t keep = 0;
+        for (int k = 2; k <= 8; ++k) {
+            if (S[k] < prev) {
+                prev = S[k];
+                sp[k - 1] = js[k];
+            } else {
+                keep |= static_cast<uint8_t>(1u << (k - 1));
+                sp[k - 1] = 0;
+            }
+            G[k - 1] = prev;
+        }
+        dp.keep[n] = keep;
+        __threadfence();
+        const int p = dp.parent[n];
+        if (p < 0) break;
+        if (atomicAdd(&dp.ready[p], 1u) != 1u) break;
+        __threadfence();
+        n = p;
+    }
+}
+
 // One thread per task (binary node -> wide node).  The wide node's internal
 // children get consecutive wide-node indices from `nodeCounter` and become
 // the next level's tasks; its leaf children's triangles get consecutive
@@ -502,53 +612,48 @@ __global__ void k_collapse_wide(const float4* __restrict__ nodes2, const float4*
                                 const int2* __restrict__ tasks, uint32_t taskCount, int2* __restrict__ nextTasks,
                                 unsigned int* __restrict__ nextCount, unsigned int* __restrict__ nodeCounter,
                                 unsigned int* __restrict__ triCounter, float4* __restrict__ out,
-                                float4* __restrict__ trisOut) {
+                                float4* __restrict__ trisOut, WideDp dp) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= taskCount) return;
     const int2 task = tasks[t];
+    // the slots of this wide node: replay the cost table's decisions from
+    // binary node task.x with 8 slots
     Entry e[8];
     int n = 0, tris = 0;
     {
+        struct Pending {
+            Entry e;
+            int k;
+        };
+        Pending st[16];
+        int sp = 0;
         Entry a, b;
         node2_children(nodes2, task.x, &a, &b);
-        if (a.lo[0] <= a.hi[0]) e[n++] = a;
-        if (b.lo[0] <= b.hi[0]) e[n++] = b;
+        const int j0 = dp.split[8 * static_cast<size_t>(task.x)];
+        st[sp++] = {a, j0};
+        st[sp++] = {b, 8 - j0};
+        while (sp > 0) {
+            const Pending pe = st[--sp];
+            if (pe.e.lo[0] > pe.e.hi[0]) continue;  // absent child
+            if (pe.e.link < 0 || n + sp >= 8) {
+                if (n < 8) e[n++] = pe.e;
+                continue;
+            }
+            int k = pe.k;
+            const uint8_t keep = dp.keep[pe.e.link];
+            while (k > 1 && ((keep >> (k - 1)) & 1u)) --k;
+            if (k <= 1) {
+                if (n < 8) e[n++] = pe.e;  // its own wide node
+                continue;
+            }
+            const int j = dp.split[8 * static_cast<size_t>(pe.e.link) + (k - 1)];
+            Entry ca, cb;
+            node2_children(nodes2, pe.e.link, &ca, &cb);
+            st[sp++] = {ca, j};
+            st[sp++] = {cb, k - j};
+        }
         for (int i = 0; i < n; ++i)
             if (e[i].link < 0) tris += leaf_count(e[i].link);
-    }
-    // open the largest internal child while there is a free slot and its
-    // leaf children fit the node's triangle bits
-    while (n < 8) {
-        int best = -1;
-        float bestArea = -1.0f;
-        Entry ba, bb;
-        for (int i = 0; i < n; ++i) {
-            if (e[i].link < 0 || entry_area(e[i]) <= bestArea) continue;
-            Entry a, b;
-            node2_children(nodes2, e[i].link, &a, &b);
-            int add = 0;
-            if (a.lo[0] <= a.hi[0] && a.link < 0) add += leaf_count(a.link);
-            if (b.lo[0] <= b.hi[0] && b.link < 0) add += leaf_count(b.link);
-            if (tris + add > static_cast<int>(kWideMaxTris)) continue;
-            bestArea = entry_area(e[i]);
-            best = i;
-            ba = a;
-            bb = b;
-        }
-        if (best < 0) break;
-        const bool va = ba.lo[0] <= ba.hi[0], vb = bb.lo[0] <= bb.hi[0];
-        if (va && ba.link < 0) tris += leaf_count(ba.link);
-        if (vb && bb.link < 0) tris += leaf_count(bb.link);
-        if (va && vb) {
-            e[best] = ba;
-            e[n++] = bb;
-        } else if (va) {
-            e[best] = ba;
-        } else if (vb) {
-            e[best] = bb;
-        } else {
-            e[best] = e[--n];
-        }
     }
     float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     for (int i = 0; i < n; ++i)
@@ -684,6 +789,18 @@ int collapse_wide(const float4* nodes2, uint32_t nodeCount2, const float4* tris2
     float4* tris = nullptr;
     BVH_CHECK(cudaMalloc(&tris, 3 * sizeof(float4) * static_cast<size_t>(std::max<uint32_t>(triCount2, 1))));
     out->tris = tris;
+    // cost table of the slot assignment (bottom-up over the binary tree)
+    WideDp dp;
+    BVH_CHECK(sc.alloc(&dp.G, 8 * static_cast<size_t>(cap)));
+    BVH_CHECK(sc.alloc(&dp.split, 8 * static_cast<size_t>(cap)));
+    BVH_CHECK(sc.alloc(&dp.keep, cap));
+    BVH_CHECK(sc.alloc(&dp.parent, cap));
+    BVH_CHECK(sc.alloc(&dp.ready, cap));
+    BVH_CHECK(sc.alloc(&dp.start, cap));
+    BVH_CHECK(cudaMemsetAsync(dp.parent, 0xff, sizeof(int) * cap, stream));
+    k_wide_parents<<<blocks(nodeCount2, 128), 128, 0, stream>>>(nodes2, nodeCount2, dp);
+    k_wide_costs<<<blocks(nodeCount2, 128), 128, 0, stream>>>(nodes2, nodeCount2, dp);
+    BVH_CHECK(cudaGetLastError());
     const int2 root = make_int2(0, 0);
     const unsigned int init[3] = {1u, 0u, 0u};
     BVH_CHECK(cudaMemcpyAsync(ta, &root, sizeof(root), cudaMemcpyHostToDevice, stream));
@@ -692,7 +809,7 @@ int collapse_wide(const float4* nodes2, uint32_t nodeCount2, const float4* tris2
     unsigned int h[3] = {0, 0, 0};
     while (tasks > 0) {
         k_collapse_wide<<<blocks(tasks, 128), 128, 0, stream>>>(nodes2, tris2, ta, tasks, tb, cnt + 1, cnt, cnt + 2, nodes,
-                                                                 tris);
+                                                                 tris, dp);
         BVH_CHECK(cudaGetLastError());
         BVH_CHECK(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, stream));
         BVH_CHECK(cudaMemsetAsync(cnt + 1, 0, sizeof(unsigned int), stream));

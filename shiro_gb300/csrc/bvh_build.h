@@ -67,8 +67,9 @@ struct WideOutput {
 };
 
 // Collapses a binary BVH (scene.cuh layout, root = node 0, leaves of at most
-// 8 triangles in `tris2`) into compressed wide nodes by repeatedly opening
-// the largest-area internal child while the node's triangle budget allows.
+// 8 triangles in `tris2`) into compressed wide nodes; which binary nodes
+// become wide nodes minimises a surface-area cost (optimal collapse over
+// at most 8 slots per node, evaluated bottom-up on the device).
 int collapse_wide(const float4* nodes2, uint32_t nodeCount2, const float4* tris2, uint32_t triCount2, cudaStream_t stream,
                   WideOutput* out, std::string& err);
 
