@@ -1009,17 +1009,33 @@ int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefr
     ShiroWavefrontConfig best = wf->cfg;
     best.use_graph = 1;
     double bestRate = 0.0;
-    auto trial = [&](ShiroWavefrontConfig c) -> int {
-        c.use_graph = 1;
+    // a candidate's rate: one warm run, then the faster of two timed runs
+    // (single timings of a few waves vary by several percent)
+    auto measure = [&](const ShiroWavefrontConfig& c, double* rate) -> int {
         // enough waves for ~1/8 of the frame, at least two
         const uint32_t waves = static_cast<uint32_t>(std::max<uint64_t>(2, (total / 8) / std::max<uint32_t>(c.paths_in_flight, 1)));
         uint64_t paths = 0;
         double ms = 0.0;
         int r = run_waves(ctx, wf, c, qs, aov, nullptr, waves, &paths, &ms);  // warm
         if (r != SHIRO_OK) return r;
-        r = run_waves(ctx, wf, c, qs, aov, nullptr, waves, &paths, &ms);
+        *rate = 0.0;
+        for (int rep = 0; rep < 2; ++rep) {
+            r = run_waves(ctx, wf, c, qs, aov, nullptr, waves, &paths, &ms);
+            if (r != SHIRO_OK) return r;
+            *rate = std::max(*rate, static_cast<double>(paths) / std::max(ms, 1e-6));
+        }
+        return SHIRO_OK;
+    };
+    {  // bring the clocks up before anything is compared
+        double warm = 0.0;
+        ShiroWavefrontConfig c = best;
+        if ((rc = measure(c, &warm)) != SHIRO_OK) return rc;
+    }
+    auto trial = [&](ShiroWavefrontConfig c) -> int {
+        c.use_graph = 1;
+        double rate = 0.0;
+        const int r = measure(c, &rate);
         if (r != SHIRO_OK) return r;
-        const double rate = static_cast<double>(paths) / std::max(ms, 1e-6);
         if (rate > bestRate) {
             bestRate = rate;
             best = c;
