@@ -82,9 +82,12 @@ __global__ void k_morton(const float4* __restrict__ cen, uint32_t n, const uint3
     const float hi[3] = {ord2f(b6[3]), ord2f(b6[4]), ord2f(b6[5])};
     const float4 c = cen[i];
     const float cc[3] = {c.x, c.y, c.z};
+    // one scale for all axes (the largest extent): a flat scene's short axis
+    // then splits only once the long axes are refined to its size, instead
+    // of cutting every object at the top of the tree
+    const float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
     uint64_t q[3];
     for (int k = 0; k < 3; ++k) {
-        const float ext = hi[k] - lo[k];
         float f = ext > 0.0f ? (cc[k] - lo[k]) / ext : 0.5f;
         f = fminf(fmaxf(f, 0.0f), 1.0f);
         q[k] = static_cast<uint64_t>(fminf(f * 2097152.0f, 2097151.0f));
