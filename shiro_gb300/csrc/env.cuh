@@ -67,20 +67,64 @@ __device__ __forceinline__ V3 env_evaluate(const DevEnv& e, const V3& local) {  
     return env_bilinear(e, env_wrap(phi / kTwoPi), sclamp(theta / kPi, 0.0f, 1.0f));
 }
 
-__device__ __forceinline__ float env_pdf(const DevEnv& e, const V3& local) {  // :165-183, 302-313
-    if (e.w == 0 || e.h == 0) return 0.0f;
-    if (!e.latlong || !e.hasTable) return kInvFourPi;
+// Lat-long angles of a local direction (EvaluateLatLong :238-245 and
+// LatLongPdf :302-313 form them the same way).
+struct EnvAngles {
+    float phi, theta;
+};
+__device__ __forceinline__ EnvAngles env_angles(const V3& local) {
     const V3 d = normalize(local);
-    const float phi = atan2f(d.x, d.z);
-    const float theta = acosf(sclamp(d.y, -1.0f, 1.0f));
-    const float u = env_wrap(phi / kTwoPi);
-    const float v = sclamp(theta / kPi, 0.0f, 1.0f);
+    return {atan2f(d.x, d.z), acosf(sclamp(d.y, -1.0f, 1.0f))};
+}
+
+// LatLongPdf (:302-313) from the angles.
+__device__ __forceinline__ float env_latlong_pdf(const DevEnv& e, const EnvAngles& a) {
+    const float u = env_wrap(a.phi / kTwoPi);
+    const float v = sclamp(a.theta / kPi, 0.0f, 1.0f);
     const uint32_t x = ::min(static_cast<uint32_t>(u * static_cast<float>(e.w)), e.w - 1u);
     const uint32_t y = ::min(static_cast<uint32_t>(v * static_cast<float>(e.h)), e.h - 1u);
-    const float sinT = sinf(theta);
+    const float sinT = sinf(a.theta);
     if (sinT <= 1.0e-6f) return 0.0f;
     const float mass = __ldg(&e.texels[static_cast<size_t>(y) * e.w + x]).w;
     return mass * static_cast<float>(e.w * e.h) / (2.0f * kPi * kPi * sinT);
+}
+
+__device__ __forceinline__ float env_pdf(const DevEnv& e, const V3& local) {  // :165-183, 302-313
+    if (e.w == 0 || e.h == 0) return 0.0f;
+    if (!e.latlong || !e.hasTable) return kInvFourPi;
+    return env_latlong_pdf(e, env_angles(local));
+}
+
+// Radiance and (when wantPdf) pdf of one direction with the angles formed
+// once: the miss of a path needs both.
+__device__ __forceinline__ V3 env_evaluate_pdf(const DevEnv& e, const V3& local, bool wantPdf, float* pdf) {
+    if (e.w == 0 || e.h == 0) {
+        *pdf = 0.0f;
+        return {0.0f, 0.0f, 0.0f};
+    }
+    if (!e.latlong) {
+        *pdf = kInvFourPi;
+        return env_evaluate(e, local);
+    }
+    const EnvAngles a = env_angles(local);
+    *pdf = !wantPdf ? 0.0f : (e.hasTable ? env_latlong_pdf(e, a) : kInvFourPi);
+    return env_bilinear(e, env_wrap(a.phi / kTwoPi), sclamp(a.theta / kPi, 0.0f, 1.0f));
+}
+
+// Sampling texel (row, col) of a lat-long map (EnvironmentMap::Sample
+// :137-162): its centre direction, the reference's pdf, the radiance there.
+// Evaluated once per texel when the tables are built (k_env_samples).
+__device__ __forceinline__ V3 env_centre_sample(const DevEnv& e, uint32_t row, uint32_t col, float mass, V3* dir,
+                                                float* pdf) {
+    const float uu = (static_cast<float>(col) + 0.5f) / static_cast<float>(e.w);
+    const float vv = (static_cast<float>(row) + 0.5f) / static_cast<float>(e.h);
+    const float theta = vv * kPi;
+    const float phi = uu * kTwoPi;
+    const float sinT = sinf(theta);
+    const V3 d{sinf(phi) * sinT, cosf(theta), cosf(phi) * sinT};
+    *dir = d;
+    *pdf = sinT > 1.0e-6f ? mass * static_cast<float>(e.w * e.h) / (2.0f * kPi * kPi * sinT) : 0.0f;
+    return env_evaluate(e, d);
 }
 
 // lower_bound over cdf[begin+1 .. end] (SampleCdf, :315-330); returns the
@@ -110,36 +154,25 @@ __device__ __forceinline__ V3 env_sample(const DevEnv& e, const V2& u, bool useC
         return {0.0f, 0.0f, 0.0f};
     }
     if (e.latlong && e.hasTable) {
-        uint32_t row, col;
-        float mass;
+        // the texel; its centre direction, pdf (mass rowMass * columnMass)
+        // and radiance come from the per-texel sample records
+        size_t t;
         if (useCdf) {
             const uint32_t r = env_cdf_search(e.rowCdf, 0u, e.h, u.y);
-            const float rowMass = __ldg(&e.rowCdf[r + 1u]) - __ldg(&e.rowCdf[r]);
             const uint32_t off = r * (e.w + 1u);
             const uint32_t c = env_cdf_search(e.condCdf, off, off + e.w, u.x);
-            const float colMass = __ldg(&e.condCdf[c + 1u]) - __ldg(&e.condCdf[c]);
-            row = r;
-            col = c - off;
-            mass = rowMass * colMass;
+            t = static_cast<size_t>(r) * e.w + (c - off);
         } else {
             const uint32_t n = e.w * e.h;
             uint32_t i = static_cast<uint32_t>(u.y * static_cast<float>(n));
             i = i >= n ? n - 1u : i;
             const uint2 a = __ldg(&e.alias[i]);
-            const uint32_t pick = u.x < __uint_as_float(a.x) ? i : a.y;
-            row = pick / e.w;
-            col = pick - row * e.w;
-            mass = __ldg(&e.texels[pick]).w;
+            t = u.x < __uint_as_float(a.x) ? i : a.y;
         }
-        const float uu = (static_cast<float>(col) + 0.5f) / static_cast<float>(e.w);
-        const float vv = (static_cast<float>(row) + 0.5f) / static_cast<float>(e.h);
-        const float theta = vv * kPi;
-        const float phi = uu * kTwoPi;
-        const float sinT = sinf(theta);
-        const V3 d{sinf(phi) * sinT, cosf(theta), cosf(phi) * sinT};
-        *dir = d;
-        *pdf = sinT > 1.0e-6f ? mass * static_cast<float>(e.w * e.h) / (2.0f * kPi * kPi * sinT) : 0.0f;
-        return env_evaluate(e, d);
+        const float4 a = __ldg(&e.samples[2 * t]), b = __ldg(&e.samples[2 * t + 1]);
+        *dir = V3{a.x, a.y, a.z};
+        *pdf = a.w;
+        return {b.x, b.y, b.z};
     }
     const float y = 1.0f - 2.0f * u.y;
     const float r = sqrtf(smax(0.0f, 1.0f - y * y));

@@ -306,18 +306,38 @@ __device__ __forceinline__ float env_miss_mis(const DevScene& s, float prevPdf, 
     return b2 / smax(b2 + sum, 1.0e-6f);
 }
 
-// Ray leaving the scene at `depth` (:1675-1693).
+// Ray leaving the scene at `depth` (:1675-1693): EnvironmentRadiance, and
+// after a non-delta reflection its MIS weight against the dome lights'
+// sampling (:1679-1688); each dome's direction angles are formed once for
+// both.
 template <typename Ctr>
 __device__ __forceinline__ void add_miss(const DevScene& s, const DevRequest& q, PathState& ps, uint32_t depth, Ctr& ctr) {
-    if (depth > 0 || q.backgroundVisible) {
-        const V3 env = environment_radiance(s, ps.rd);
-        ctr.env_eval(s.domeCount);
-        if (s.domeCount == 0 || depth == 0 || ps.prevDelta || ps.prevType == kBounceTransmission) {
-            ps.radiance = ps.radiance + ps.T * env;
+    if (!(depth > 0 || q.backgroundVisible)) return;
+    ctr.env_eval(s.domeCount);
+    const bool weighted = !(s.domeCount == 0 || depth == 0 || ps.prevDelta || ps.prevType == kBounceTransmission);
+    if (s.domeCount == 0) {
+        const float t = sclamp(ps.rd.y * 0.5f + 0.5f, 0.0f, 1.0f);
+        ps.radiance = ps.radiance + ps.T * lerp(s.envBottom, s.envTop, t);
+        return;
+    }
+    V3 env{0.0f, 0.0f, 0.0f};
+    float sum = 0.0f;
+    for (uint32_t i = 0; i < s.domeCount; ++i) {
+        const DevDome& d = s.domes[i];
+        float p = kInvFourPi;
+        if (d.env >= 0) {
+            env = env + env_evaluate_pdf(s.envs[d.env], world_to_light(d, ps.rd), weighted, &p) * d.radiance;
         } else {
-            ctr.env_sample(s.domeCount);
-            ps.radiance = ps.radiance + ps.T * env * env_miss_mis(s, ps.prevPdf, ps.rd);
+            env = env + d.radiance;
         }
+        sum += p * p;
+    }
+    if (!weighted) {
+        ps.radiance = ps.radiance + ps.T * env;
+    } else {
+        ctr.env_sample(s.domeCount);
+        const float b2 = ps.prevPdf * ps.prevPdf;
+        ps.radiance = ps.radiance + ps.T * env * (b2 / smax(b2 + sum, 1.0e-6f));
     }
 }
 

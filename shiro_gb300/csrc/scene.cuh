@@ -12,7 +12,8 @@
 //              fall back to the geometric normal (meshHasNormals = 0)
 //   materials  ShiroMaterialDesc, the PbrMaterial fields verbatim
 //   envs       per dome texture: texels (rgb, pixel probability mass),
-//              row / conditional CDFs, alias table
+//              row / conditional CDFs, alias table, and per texel the result
+//              of sampling it (centre direction, pdf, radiance there)
 //   emissive   the emissive triangles in mesh / primitive order with the
 //              float running sums of their selection weights (area x
 //              luminance), as BuildAccelerationScene forms them
@@ -28,6 +29,7 @@ struct DevEnv {
     const float* rowCdf;    // h + 1
     const float* condCdf;   // h * (w + 1)
     const uint2* alias;     // (acceptance threshold bits, alias index), w * h
+    const float4* samples;  // 2 per texel: (centre direction, pdf), (radiance at the centre, 0)
     uint32_t w, h;
     uint32_t latlong;       // 1: lat-long, 0: angular
     uint32_t hasTable;      // importance table present (lat-long, non-empty)

@@ -18,6 +18,7 @@
 
 #include "bvh_build.h"
 #include "context.h"
+#include "env.cuh"
 #include "kernels.h"
 
 using namespace shiro_gpu;
@@ -278,6 +279,19 @@ std::vector<uint2> build_alias(const std::vector<float>& mass) {
 
 }  // namespace
 
+// Per-texel sample records of a lat-long map (EnvironmentMap::Sample's
+// result for each texel): (centre direction, pdf), (radiance there, 0).
+__global__ void k_env_samples(DevEnv e, float4* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= e.w * e.h) return;
+    const uint32_t row = i / e.w, col = i - row * e.w;
+    V3 d;
+    float pdf;
+    const V3 rad = env_centre_sample(e, row, col, e.texels[i].w, &d, &pdf);
+    out[2 * static_cast<size_t>(i)] = make_float4(d.x, d.y, d.z, pdf);
+    out[2 * static_cast<size_t>(i) + 1] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+}
+
 int upload_envs(ContextImpl* ctx) {
     // env blocks are appended to sceneBlocks; the env table itself is
     // rewritten in place.
@@ -316,6 +330,17 @@ int upload_envs(ContextImpl* ctx) {
         d.h = e.h;
         d.latlong = e.latlong ? 1u : 0u;
         d.hasTable = (e.latlong && !e.rowCdf.empty()) ? 1u : 0u;
+        if (d.hasTable) {
+            if (!d.samples) {
+                DeviceBlock b;
+                if (!ensure_block(ctx, &b, 2 * n * sizeof(float4), "env sample records")) return SHIRO_ERR_OUT_OF_MEMORY;
+                ctx->sceneBlocks.push_back(b);
+                d.samples = static_cast<const float4*>(b.ptr);
+            }
+            k_env_samples<<<static_cast<unsigned>((n + 255) / 256), 256, 0, ctx->stream>>>(d, const_cast<float4*>(d.samples));
+            const cudaError_t err = cudaGetLastError();
+            if (err != cudaSuccess) return cuda_fail(ctx, err, "env sample records");
+        }
     }
     return SHIRO_OK;
 }
