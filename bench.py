@@ -98,7 +98,7 @@ class ClockSampler:
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,clocks.mem,clocks.max.mem")
 
     def __init__(self, index: int):
         self.index = index
@@ -140,7 +140,7 @@ class ClockSampler:
                 self.t.join(timeout=2)
 
     def summary(self) -> dict:
-        sm, mx, reasons = [], [], set()
+        sm, mx, mem, memx, power, reasons = [], [], [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [x.strip() for x in ln.split(",")]
@@ -151,12 +151,23 @@ class ClockSampler:
                 mx.append(float(parts[2]))
             except ValueError:
                 continue
+            try:
+                power.append(float(parts[3]))
+                mem.append(float(parts[9]))
+                memx.append(float(parts[10]))
+            except (ValueError, IndexError):
+                pass
             for n, v in zip(names, parts[5:9]):
                 if v.lower().startswith("active") or v == "1":
                     reasons.add(n)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+        if mem:
+            out.update({"mem_mhz": statistics.median(mem), "mem_min_mhz": min(mem), "mem_max_mhz": max(memx)})
+        if power:
+            out["power_w_median"] = statistics.median(power)
+        return out
 
 
 def peaks() -> dict:
