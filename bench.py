@@ -190,7 +190,7 @@ def ncu_traffic(kernel: str, workload_name: str):
 
 def cpu_baseline(w, seconds: float, rank: int = 0) -> dict:
     """The CPU path tracer (oracle restatement of CpuPathTracer) on every host
-    thread, over evenly spaced bands of rows of the same frame."""
+    thread, over single rows spread evenly over the same frame."""
     import ctypes as C
 
     import oracle
@@ -215,26 +215,24 @@ def cpu_baseline(w, seconds: float, rank: int = 0) -> dict:
     req = render_desc(w.camera, st, 0, st.samples_per_pixel)
     fb = FrameBuffer(st.width, st.height)
     aovs = fb.aovs()
-    # calibrate on one band of 2 rows, then spread the budget over bands
+    # calibrate on the middle row, then render single rows spread evenly over
+    # the frame (rows differ widely in cost: sky rows are cheap), so the
+    # sample's mix of sky and field does not depend on the time budget
     paths = 0
     t_render = 0.0
     y = st.height // 2
     t0 = time.perf_counter()
-    paths += lib.oracle_scene_render_rows(h, C.byref(req), y, y + 2, C.byref(aovs))
+    paths += lib.oracle_scene_render_rows(h, C.byref(req), y, y + 1, C.byref(aovs))
     t_render += time.perf_counter() - t0
     rate = paths / max(t_render, 1e-6)
-    rows_budget = max(2, int(seconds * rate / (st.width * st.samples_per_pixel)))
-    bands = 8
-    per = max(1, rows_budget // bands)
-    rows = 2
-    for b in range(bands):
-        y0 = int((b + 0.5) * st.height / bands) - per // 2
-        y0 = min(max(0, y0), st.height - per)
+    rows_budget = int(min(st.height, max(4, seconds * rate / (st.width * st.samples_per_pixel))))
+    paths, t_render = 0, 0.0
+    for k in range(rows_budget):
+        yk = min(st.height - 1, int((k + 0.5) * st.height / rows_budget))
         t0 = time.perf_counter()
-        n = lib.oracle_scene_render_rows(h, C.byref(req), y0, y0 + per, C.byref(aovs))
+        paths += lib.oracle_scene_render_rows(h, C.byref(req), yk, yk + 1, C.byref(aovs))
         t_render += time.perf_counter() - t0
-        paths += n
-        rows += per
+    rows = rows_budget
     lib.oracle_scene_destroy(h)
     value = paths / t_render / 1e6
     cpu = ""
@@ -243,8 +241,8 @@ def cpu_baseline(w, seconds: float, rank: int = 0) -> dict:
     except Exception:
         pass
     return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{rows} rows x {st.width} px x {st.samples_per_pixel} spp ({paths} paths, "
-                      f"{rows / st.height:.1%} of the frame, 9 bands), {t_render:.1f} s render + {build_s:.1f} s BVH build",
+            "sample": f"{rows} rows evenly spread over the frame x {st.width} px x {st.samples_per_pixel} spp ({paths} paths, "
+                      f"{rows / st.height:.1%} of the frame), {t_render:.1f} s render + {build_s:.1f} s BVH build",
             "cpu": cpu, "seconds": t_render, "paths": int(paths)}
 
 
