@@ -431,6 +431,8 @@ int adjoint_set_params(ContextImpl* ctx, const float* base, const float* rough, 
             const_cast<Mat*>(ctx->scene.materials), ctx->materialCount, base, rough, metal);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return cuda_fail(ctx, e, "set material params");
+        const int rc = build_bsdf_recs(ctx);
+        if (rc != SHIRO_OK) return rc;
     }
     if (env) {
         const int32_t e0 = dome0_env(ctx);

@@ -189,35 +189,84 @@ __device__ __forceinline__ float transmission_weight(const Mat& m) {
     return smax(0.0f, maxc(sclamp3(ld3(m.transmission_color), 0.0f, 1.0f) * uc * ub)) * tr * (1.0f - metal);
 }
 
-static __device__ __noinline__ float bsdf_pdf(const Mat& m, const LobeWeights& w, const V3& n, const V3& cn, const V3& v,
-                                       const V3& l) {
-    const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
-    if (nl <= 0.0f) return 0.0f;
-    const float rw = w.diffuse + w.spec + w.coat;
-    if (rw <= 0.0f) return 0.0f;
-    const float dp = w.diffuse / rw, bp = w.spec / rw, cp = w.coat / rw;
-    const float sr = roughness_for(base_roughness(m), m.specular_anisotropy, m.specular_rotation, m, n, v, l);
-    float coatTerm = 0.0f;
-    if (cp != 0.0f) {
-        const float cr = roughness_for(m.coat_roughness, m.coat_anisotropy, m.coat_rotation, m, cn, v, l);
-        coatTerm = cp * spec_pdf(cn, v, l, cr);
-    }
-    return dp * nl * kInvPi + bp * spec_pdf(n, v, l, sr) + coatTerm;
-}
+// Per-material record of the quantities EvaluateBsdf / EvaluateBsdfPdf
+// derive from the material alone (6 x float4), evaluated once per material
+// with the same expressions as above, so every float is unchanged:
+//   [0] SpecularF0, diffuse roughness sigma     [1] CoatF0, subsurface wrap
+//   [2] coat underlayer tint, base GGX roughness (clamped; valid without anisotropy)
+//   [3] DiffuseColor, coat GGX roughness (clamped; valid without anisotropy)
+//   [4] sheen colour x sheen weight, 1 - 0.5 sheen roughness
+//   [5] lobe sample weights (diffuse, base specular, coat), flag bits
+constexpr uint32_t kRecAnisoSpec = 1u, kRecAnisoCoat = 2u, kRecSheen = 4u;
+constexpr int kBsdfRec = 6;
 
-static __device__ __noinline__ V3 bsdf_eval(const Mat& m, const V3& n, const V3& cn, const V3& v, const V3& l) {
-    const float nv = sclamp(dot(n, v), 0.0f, 1.0f);
-    const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
-    if (nv <= 0.0f || nl <= 0.0f) return {0.0f, 0.0f, 0.0f};
-    const V3 baseF0 = spec_f0(m);
-    const V3 cF0 = coat_f0(m);
-    const V3 underCoat = coat_tint(m) * layer_transmittance(cF0, dot(cn, v), dot(cn, l));
-    const V3 underBase = layer_transmittance(baseF0, nv, nl);
+__device__ __forceinline__ void make_bsdf_rec(const Mat& m, float4 r[kBsdfRec]) {
+    const V3 f0 = spec_f0(m), cf0 = coat_f0(m), ct = coat_tint(m), dc = diffuse_color(m);
     const float sigma = sclamp(m.diffuse_roughness, 0.0f, 1.0f);
     const float wrap = sclamp(m.subsurface * m.subsurface_scale *
                                   (0.35f + 0.15f * sclamp(m.subsurface_anisotropy, -1.0f, 1.0f) +
                                    0.1f * sclamp(maxc(ld3(m.subsurface_radius)) / 3.0f, 0.0f, 1.0f)),
                               0.0f, 0.9f);
+    const float sw = sclamp(m.sheen, 0.0f, 1.0f);
+    const V3 scw = ld3(m.sheen_color) * sw;
+    const LobeWeights w = lobe_weights(m);
+    uint32_t flags = 0;
+    if (sclamp(m.specular_anisotropy, -0.95f, 0.95f) != 0.0f) flags |= kRecAnisoSpec;
+    if (sclamp(m.coat_anisotropy, -0.95f, 0.95f) != 0.0f) flags |= kRecAnisoCoat;
+    if (sw != 0.0f) flags |= kRecSheen;
+    r[0] = make_float4(f0.x, f0.y, f0.z, sigma);
+    r[1] = make_float4(cf0.x, cf0.y, cf0.z, wrap);
+    r[2] = make_float4(ct.x, ct.y, ct.z, sclamp(base_roughness(m), 0.02f, 1.0f));
+    r[3] = make_float4(dc.x, dc.y, dc.z, sclamp(m.coat_roughness, 0.02f, 1.0f));
+    r[4] = make_float4(scw.x, scw.y, scw.z, 1.0f - 0.5f * sclamp(m.sheen_roughness, 0.0f, 1.0f));
+    r[5] = make_float4(w.diffuse, w.spec, w.coat, __uint_as_float(flags));
+}
+__device__ __forceinline__ LobeWeights rec_weights(const float4* r) {
+    const float4 x = r[5];
+    return {x.x, x.y, x.z};
+}
+// AdjustedRoughness of the base / coat lobe: the record's clamped value
+// unless the lobe is anisotropic (then the half-vector phase is needed).
+__device__ __forceinline__ float rec_spec_roughness(const float4* r, uint32_t flags, const Mat& m, const V3& n, const V3& v,
+                                                    const V3& l) {
+    return (flags & kRecAnisoSpec) ? roughness_for(base_roughness(m), m.specular_anisotropy, m.specular_rotation, m, n, v, l)
+                                   : r[2].w;
+}
+__device__ __forceinline__ float rec_coat_roughness(const float4* r, uint32_t flags, const Mat& m, const V3& cn, const V3& v,
+                                                    const V3& l) {
+    return (flags & kRecAnisoCoat) ? roughness_for(m.coat_roughness, m.coat_anisotropy, m.coat_rotation, m, cn, v, l)
+                                   : r[3].w;
+}
+
+static __device__ __noinline__ float bsdf_pdf_rec(const float4* r, const Mat& m, const LobeWeights& w, const V3& n,
+                                                  const V3& cn, const V3& v, const V3& l) {
+    const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
+    if (nl <= 0.0f) return 0.0f;
+    const float rw = w.diffuse + w.spec + w.coat;
+    if (rw <= 0.0f) return 0.0f;
+    const float dp = w.diffuse / rw, bp = w.spec / rw, cp = w.coat / rw;
+    const uint32_t flags = __float_as_uint(r[5].w);
+    const float sr = rec_spec_roughness(r, flags, m, n, v, l);
+    float coatTerm = 0.0f;
+    if (cp != 0.0f) {
+        const float cr = rec_coat_roughness(r, flags, m, cn, v, l);
+        coatTerm = cp * spec_pdf(cn, v, l, cr);
+    }
+    return dp * nl * kInvPi + bp * spec_pdf(n, v, l, sr) + coatTerm;
+}
+
+static __device__ __noinline__ V3 bsdf_eval_rec(const float4* r, const Mat& m, const V3& n, const V3& cn, const V3& v,
+                                               const V3& l) {
+    const float nv = sclamp(dot(n, v), 0.0f, 1.0f);
+    const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
+    if (nv <= 0.0f || nl <= 0.0f) return {0.0f, 0.0f, 0.0f};
+    const float4 r0 = r[0], r1 = r[1], r2 = r[2];
+    const V3 baseF0{r0.x, r0.y, r0.z};
+    const V3 cF0{r1.x, r1.y, r1.z};
+    const V3 underCoat = V3{r2.x, r2.y, r2.z} * layer_transmittance(cF0, dot(cn, v), dot(cn, l));
+    const V3 underBase = layer_transmittance(baseF0, nv, nl);
+    const float sigma = r0.w;
+    const float wrap = r1.w;
     const float wrapped = sclamp((nl + wrap) / (1.0f + wrap), 0.0f, 1.0f);
     float term;
     if (sigma == 0.0f) {
@@ -237,22 +286,38 @@ static __device__ __noinline__ V3 bsdf_eval(const Mat& m, const V3& n, const V3&
         const float tanBeta = smin(sinV / smax(nv, 1.0e-6f), sinL / smax(nl, 1.0e-6f));
         term = (orenA + orenB * smax(0.0f, cosPhi) * sinAlpha * tanBeta) * (wrapped / smax(nl, 1.0e-6f));
     }
-    const V3 diffuse = diffuse_color(m) * underCoat * underBase * (kInvPi * term);
-    const float sr = roughness_for(base_roughness(m), m.specular_anisotropy, m.specular_rotation, m, n, v, l);
+    const float4 r3 = r[3];
+    const V3 diffuse = V3{r3.x, r3.y, r3.z} * underCoat * underBase * (kInvPi * term);
+    const uint32_t flags = __float_as_uint(r[5].w);
+    const float sr = rec_spec_roughness(r, flags, m, n, v, l);
     const V3 spec = underCoat * thin_film(spec_lobe(n, v, l, baseF0, sr), m, n, v, l);
-    const float cr = roughness_for(m.coat_roughness, m.coat_anisotropy, m.coat_rotation, m, cn, v, l);
+    const float cr = rec_coat_roughness(r, flags, m, cn, v, l);
     const V3 coat = thin_film(spec_lobe(cn, v, l, cF0, cr), m, cn, v, l);
-    const float sw = sclamp(m.sheen, 0.0f, 1.0f);
     // With zero sheen weight the factor sf (finite, >= 0) only multiplies a
     // signed zero; 1 gives the same signed zero without the powf.
     float sf = 1.0f;
-    if (sw != 0.0f) {
+    const float4 r4 = r[4];
+    if (flags & kRecSheen) {
         const V3 h = safe_normalized(v + l, n);
         const float lh = sclamp(dot(l, h), 0.0f, 1.0f);
-        sf = powf(1.0f - lh, 5.0f) * (1.0f - 0.5f * sclamp(m.sheen_roughness, 0.0f, 1.0f));
+        sf = powf(1.0f - lh, 5.0f) * r4.w;
     }
-    const V3 sheen = ld3(m.sheen_color) * sw * sf * underCoat * underBase;
+    const V3 sheen = V3{r4.x, r4.y, r4.z} * sf * underCoat * underBase;
     return diffuse + spec + coat + sheen;
+}
+
+// The same from the material alone (record formed on the spot): the
+// differentiable form, whose evaluation materials have no stored record.
+__device__ __forceinline__ float bsdf_pdf(const Mat& m, const LobeWeights& w, const V3& n, const V3& cn, const V3& v,
+                                          const V3& l) {
+    float4 r[kBsdfRec];
+    make_bsdf_rec(m, r);
+    return bsdf_pdf_rec(r, m, w, n, cn, v, l);
+}
+__device__ __forceinline__ V3 bsdf_eval(const Mat& m, const V3& n, const V3& cn, const V3& v, const V3& l) {
+    float4 r[kBsdfRec];
+    make_bsdf_rec(m, r);
+    return bsdf_eval_rec(r, m, n, cn, v, l);
 }
 
 // ---- transmission, media, emitters (CpuPathTracer.cpp:930-932, 1011-1033,

@@ -85,6 +85,8 @@ int validate_request(ContextImpl* ctx, const ShiroRenderDesc& r);
 
 // Uploads / refreshes the dome textures of envHost (texels + CDF + alias).
 int upload_envs(ContextImpl* ctx);
+// (Re)computes the per-material BSDF records (after the materials change).
+int build_bsdf_recs(ContextImpl* ctx);
 // Builds the reference importance table (EnvironmentMap.cpp:185-236).
 void build_env_table(EnvHost& e);
 

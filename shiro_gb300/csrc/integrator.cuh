@@ -117,13 +117,17 @@ __device__ __forceinline__ void shading_frame(const Mat& m, const Surface& hit, 
     *cn = resolve_normal(m, nn, true);
 }
 
+__device__ __forceinline__ const float4* bsdf_rec(const DevScene& s, uint32_t material) {
+    return s.bsdfRecs + kBsdfRec * static_cast<size_t>(material);
+}
+
 __device__ __forceinline__ Vertex make_vertex(const DevScene& s, const V3& ro, const V3& rd, const HitRec& h) {
     Vertex v;
     v.hit = make_surface(s, ro, rd, h);
     const Mat& m = s.materials[v.hit.material];
     shading_frame(m, v.hit, rd, &v.n, &v.cn, &v.ngf);
     v.view = rd * -1.0f;
-    v.w = lobe_weights(m);
+    v.w = rec_weights(bsdf_rec(s, v.hit.material));
     return v;
 }
 
@@ -181,7 +185,7 @@ __device__ __forceinline__ bool light_distant(const DevScene& s, const DevReques
     const Mat& m = s.materials[v.hit.material];
     ctr.bsdf_eval();
     *dir = ld;
-    *c = clamp24(q, bsdf_eval(m, v.n, v.cn, v.view, ld) * l.radiance * nl);
+    *c = clamp24(q, bsdf_eval_rec(bsdf_rec(s, v.hit.material), m, v.n, v.cn, v.view, ld) * l.radiance * nl);
     return true;
 }
 
@@ -203,10 +207,11 @@ __device__ __forceinline__ bool light_dome(const DevScene& s, const DevRequest& 
     const Mat& m = s.materials[v.hit.material];
     ctr.bsdf_pdf();
     ctr.bsdf_eval();
-    const float bp = bsdf_pdf(m, v.w, v.n, v.cn, v.view, ld);
+    const float4* rec = bsdf_rec(s, v.hit.material);
+    const float bp = bsdf_pdf_rec(rec, m, v.w, v.n, v.cn, v.view, ld);
     const float mis = power_heuristic(lp, bp);
     *dir = ld;
-    *c = clamp24(q, bsdf_eval(m, v.n, v.cn, v.view, ld) * lr * (nl * mis / lp));
+    *c = clamp24(q, bsdf_eval_rec(rec, m, v.n, v.cn, v.view, ld) * lr * (nl * mis / lp));
     return true;
 }
 
@@ -272,11 +277,12 @@ __device__ __forceinline__ bool light_emissive(const DevScene& s, const DevReque
     const Mat& m = s.materials[v.hit.material];
     ctr.bsdf_pdf();
     ctr.bsdf_eval();
-    const float bp = bsdf_pdf(m, v.w, v.n, v.cn, v.view, ld);
+    const float4* rec = bsdf_rec(s, v.hit.material);
+    const float bp = bsdf_pdf_rec(rec, m, v.w, v.n, v.cn, v.view, ld);
     const float mis = power_heuristic(lp, bp);
     *dir = ld;
     *maxDist = smax(dist - 2.0f * kRayEpsilon, kRayEpsilon);
-    *c = clamp24(q, bsdf_eval(m, v.n, v.cn, v.view, ld) * f4xyz(e1) * (nl * mis / lp));
+    *c = clamp24(q, bsdf_eval_rec(rec, m, v.n, v.cn, v.view, ld) * f4xyz(e1) * (nl * mis / lp));
     return true;
 }
 
@@ -391,6 +397,7 @@ __device__ __forceinline__ bool continue_path(const DevScene& s, const DevReques
                                               uint32_t depth, PathState& ps, Ctr& ctr) {
     const uint32_t base = depth * kPathDimStride;
     const Mat& m = s.materials[v.hit.material];
+    const float4* rec = bsdf_rec(s, v.hit.material);
     const float dw = v.w.diffuse, cw = v.w.coat;
     float bw = v.w.spec;
     const float rawTw = kExt ? transmission_weight(m) : 0.0f;
@@ -452,7 +459,7 @@ __device__ __forceinline__ bool continue_path(const DevScene& s, const DevReques
                 next = normalize(reflect(ps.rd, mn));
                 if (rw <= 0.0f) return false;
                 ctr.bsdf_pdf();
-                pdf = smax((rw / total) * bsdf_pdf(m, v.w, v.n, v.cn, v.view, next), 1.0e-6f);
+                pdf = smax((rw / total) * bsdf_pdf_rec(rec, m, v.w, v.n, v.cn, v.view, next), 1.0e-6f);
                 type = kBounceReflective;
                 delta = tr <= kDeltaRoughness;
                 chooseT = false;
@@ -484,7 +491,7 @@ __device__ __forceinline__ bool continue_path(const DevScene& s, const DevReques
         const float rc = sclamp(dot(sn, next), 0.0f, 1.0f);
         if (rc <= 0.0f) return false;
         ctr.bsdf_pdf();
-        pdf = smax((rw / total) * bsdf_pdf(m, v.w, v.n, v.cn, v.view, next), 1.0e-6f);
+        pdf = smax((rw / total) * bsdf_pdf_rec(rec, m, v.w, v.n, v.cn, v.view, next), 1.0e-6f);
         delta = sr <= kDeltaRoughness;
     } else {  // diffuse
         if (ps.diffDepth >= q.diffuseDepth) return false;
@@ -497,7 +504,7 @@ __device__ __forceinline__ bool continue_path(const DevScene& s, const DevReques
     // chose different lobes runs the BSDF once
     if (reflEval) {
         ctr.bsdf_eval();
-        f = bsdf_eval(m, v.n, v.cn, v.view, next);
+        f = bsdf_eval_rec(rec, m, v.n, v.cn, v.view, next);
     }
     const float cosT = chooseT ? smax(fabsf(dot(v.ngf, next)), 1.0e-4f) : sclamp(dot(v.n, next), 0.0f, 1.0f);
     if (cosT <= 0.0f) return false;

@@ -55,6 +55,7 @@ struct DevScene {
     const uint32_t* meshMaterial;   // per mesh, already mapped to the default material when out of range
     const uint32_t* meshHasNormals;
     const ShiroMaterialDesc* materials;
+    const float4* bsdfRecs;         // kBsdfRec per material: the BSDF's material-only quantities (bsdf.cuh)
     const DevDistant* distant;
     const DevDome* domes;
     const DevEnv* envs;

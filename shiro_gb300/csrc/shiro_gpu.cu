@@ -18,6 +18,7 @@
 
 #include "bvh_build.h"
 #include "context.h"
+#include "bsdf.cuh"
 #include "env.cuh"
 #include "kernels.h"
 
@@ -290,6 +291,28 @@ __global__ void k_env_samples(DevEnv e, float4* out) {
     const V3 rad = env_centre_sample(e, row, col, e.texels[i].w, &d, &pdf);
     out[2 * static_cast<size_t>(i)] = make_float4(d.x, d.y, d.z, pdf);
     out[2 * static_cast<size_t>(i) + 1] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+}
+
+__global__ void k_bsdf_recs(const ShiroMaterialDesc* mats, uint32_t n, float4* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 r[kBsdfRec];
+    make_bsdf_rec(mats[i], r);
+    for (int k = 0; k < kBsdfRec; ++k) out[kBsdfRec * static_cast<size_t>(i) + k] = r[k];
+}
+
+// (Re)computes the per-material BSDF records from the resident materials.
+int build_bsdf_recs(ContextImpl* ctx) {
+    const uint32_t n = ctx->materialCount + 1u;  // + the default material
+    if (!ctx->scene.bsdfRecs) {
+        DeviceBlock b;
+        if (!ensure_block(ctx, &b, kBsdfRec * sizeof(float4) * n, "BSDF records")) return SHIRO_ERR_OUT_OF_MEMORY;
+        ctx->sceneBlocks.push_back(b);
+        ctx->scene.bsdfRecs = static_cast<const float4*>(b.ptr);
+    }
+    k_bsdf_recs<<<(n + 127) / 128, 128, 0, ctx->stream>>>(ctx->scene.materials, n, const_cast<float4*>(ctx->scene.bsdfRecs));
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? SHIRO_OK : cuda_fail(ctx, e, "BSDF records");
 }
 
 int upload_envs(ContextImpl* ctx) {
@@ -760,6 +783,8 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     }
     s.extended = ctx->extendedMaterials ? 1u : 0u;
     if ((rc = upload(ctx, ctx->materialsHost, &s.materials, "materials")) != SHIRO_OK) return rc;
+    s.bsdfRecs = nullptr;
+    if ((rc = build_bsdf_recs(ctx)) != SHIRO_OK) return rc;
     std::vector<DevDistant> distant(sd->distant_light_count);
     for (uint32_t i = 0; i < sd->distant_light_count; ++i)
         distant[i] = DevDistant{ld3(sd->distant_lights[i].direction), ld3(sd->distant_lights[i].radiance)};
