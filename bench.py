@@ -190,7 +190,8 @@ def ncu_traffic(kernel: str, workload_name: str):
 
 def cpu_baseline(w, seconds: float, rank: int = 0) -> dict:
     """The CPU path tracer (oracle restatement of CpuPathTracer) on every host
-    thread, over single rows spread evenly over the same frame."""
+    thread (rows handed out dynamically), over rows spread evenly over the
+    same frame."""
     import ctypes as C
 
     import oracle
@@ -199,8 +200,8 @@ def cpu_baseline(w, seconds: float, rank: int = 0) -> dict:
     lib = oracle.load_port()
     lib.oracle_scene_create.argtypes = [C.c_void_p, C.c_void_p]
     lib.oracle_scene_create.restype = C.c_int
-    lib.oracle_scene_render_rows.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
-    lib.oracle_scene_render_rows.restype = C.c_int64
+    lib.oracle_scene_render_row_list.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
+    lib.oracle_scene_render_row_list.restype = C.c_int64
     lib.oracle_scene_destroy.argtypes = [C.c_void_p]
     threads = os.cpu_count() or 1
     lib.oracle_set_threads(threads)
@@ -215,24 +216,28 @@ def cpu_baseline(w, seconds: float, rank: int = 0) -> dict:
     req = render_desc(w.camera, st, 0, st.samples_per_pixel)
     fb = FrameBuffer(st.width, st.height)
     aovs = fb.aovs()
-    # calibrate on the middle row, then render single rows spread evenly over
-    # the frame (rows differ widely in cost: sky rows are cheap), so the
-    # sample's mix of sky and field does not depend on the time budget
-    paths = 0
-    t_render = 0.0
-    y = st.height // 2
-    t0 = time.perf_counter()
-    paths += lib.oracle_scene_render_rows(h, C.byref(req), y, y + 1, C.byref(aovs))
-    t_render += time.perf_counter() - t0
-    rate = paths / max(t_render, 1e-6)
-    rows_budget = int(min(st.height, max(4, seconds * rate / (st.width * st.samples_per_pixel))))
-    paths, t_render = 0, 0.0
-    for k in range(rows_budget):
-        yk = min(st.height - 1, int((k + 0.5) * st.height / rows_budget))
+
+    def spread(n):
+        # n rows spread evenly over the frame (rows differ widely in cost: sky
+        # rows are cheap), so the sample's mix of sky and field does not
+        # depend on the time budget
+        return (C.c_uint32 * n)(*[min(st.height - 1, int((k + 0.5) * st.height / n)) for k in range(n)])
+
+    def render(n):
+        rows_n = spread(n)
         t0 = time.perf_counter()
-        paths += lib.oracle_scene_render_rows(h, C.byref(req), yk, yk + 1, C.byref(aovs))
-        t_render += time.perf_counter() - t0
-    rows = rows_budget
+        got = lib.oracle_scene_render_row_list(h, C.byref(req), rows_n, n, C.byref(aovs))
+        dt = time.perf_counter() - t0
+        if got < 0:
+            raise RuntimeError(f"oracle render failed: {got}")
+        return got, dt
+
+    # calibrate on two rows per thread (one row per thread leaves the slowest
+    # row alone at the end), then render the sized sample in one call
+    paths, t_render = render(min(st.height, 2 * threads))
+    rate = paths / max(t_render, 1e-6)
+    rows = int(min(st.height, max(threads, seconds * rate / (st.width * st.samples_per_pixel))))
+    paths, t_render = render(rows)
     lib.oracle_scene_destroy(h)
     value = paths / t_render / 1e6
     cpu = ""

@@ -1556,13 +1556,11 @@ void ParallelRows(uint32_t y0, uint32_t y1, F&& fn) {
     for (auto& t : ws) t.join();
 }
 
-// Per-pixel batch average (CpuPathTracer.cpp:2093-2137).
-int64_t RenderRows(const SceneData& s, const ShiroRenderDesc& req, uint32_t y0, uint32_t y1, ShiroAovs* out,
-                   bool brute = false) {
+// One row of pixels (the per-pixel loop of RenderSampleBatch,
+// CpuPathTracer.cpp:2093-2137).
+void RenderRow(const Tracer& tr, const ShiroRenderDesc& req, uint32_t y, ShiroAovs* out) {
     const ShiroSettingsDesc& st = req.settings;
-    if (req.sample_count == 0) return 0;
-    Tracer tr{s, req.flags, brute};
-    ParallelRows(y0, y1, [&](uint32_t y) {
+    {
         for (uint32_t x = 0; x < st.width; ++x) {
             float b[4] = {0, 0, 0, 0};
             V3 alb{}, nrm{};
@@ -1592,8 +1590,15 @@ int64_t RenderRows(const SceneData& s, const ShiroRenderDesc& req, uint32_t y0, 
             out->normal[3 * i + 2] = nn.z;
             out->depth[i] = depth;
         }
-    });
-    return static_cast<int64_t>(y1 - y0) * st.width * req.sample_count;
+    }
+}
+
+int64_t RenderRows(const SceneData& s, const ShiroRenderDesc& req, uint32_t y0, uint32_t y1, ShiroAovs* out,
+                   bool brute = false) {
+    if (req.sample_count == 0) return 0;
+    Tracer tr{s, req.flags, brute};
+    ParallelRows(y0, y1, [&](uint32_t y) { RenderRow(tr, req, y, out); });
+    return static_cast<int64_t>(y1 - y0) * req.settings.width * req.sample_count;
 }
 
 }  // namespace
@@ -1801,6 +1806,18 @@ void oracle_scene_destroy(OracleScene* s) { delete s; }
 int64_t oracle_scene_render_rows(OracleScene* s, const ShiroRenderDesc* req, uint32_t y0, uint32_t y1, ShiroAovs* out) {
     if (!s || !req || !out || y1 > req->settings.height || y0 > y1) return SHIRO_ERR_INVALID_ARGUMENT;
     return RenderRows(s->data, *req, y0, y1, out);
+}
+
+// An arbitrary set of rows, rendered in parallel (a sample of a frame).
+int64_t oracle_scene_render_row_list(OracleScene* s, const ShiroRenderDesc* req, const uint32_t* rows, uint32_t n,
+                                     ShiroAovs* out) {
+    if (!s || !req || !out || (n && !rows)) return SHIRO_ERR_INVALID_ARGUMENT;
+    for (uint32_t k = 0; k < n; ++k)
+        if (rows[k] >= req->settings.height) return SHIRO_ERR_INVALID_ARGUMENT;
+    if (req->sample_count == 0) return 0;
+    Tracer tr{s->data, req->flags, false};
+    ParallelRows(0, n, [&](uint32_t k) { RenderRow(tr, *req, rows[k], out); });
+    return static_cast<int64_t>(n) * req->settings.width * req->sample_count;
 }
 
 }  // extern "C"

@@ -60,6 +60,11 @@ void oracle_scene_destroy(OracleScene* s);
  * planes); returns the number of paths traced or a negative error. */
 int64_t oracle_scene_render_rows(OracleScene* s, const ShiroRenderDesc* req, uint32_t y0, uint32_t y1,
                                  ShiroAovs* out);
+/* Renders the n listed rows (each < height) with all host threads into
+ * out (full-frame planes); returns the number of paths traced or a
+ * negative error. */
+int64_t oracle_scene_render_row_list(OracleScene* s, const ShiroRenderDesc* req, const uint32_t* rows, uint32_t n,
+                                     ShiroAovs* out);
 /* 1 if the scene is within the restated scope (see above), else 0. */
 int oracle_supports_scene(const ShiroSceneDesc* scene);
 
