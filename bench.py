@@ -41,8 +41,11 @@ METRIC = "Mpaths/s 1080p 1M-tri (plain vs wavefront) at equal RMSE; adjoint grad
 UNIT = "Mpaths/s"
 
 # Bytes moved per unit of counted work in this backend's layout (the
-# algorithmic-bytes model of the roofline).
-BYTES = dict(node=64, tri=48, hit=16 + 3 * 16 + 4 + 4 + 276, env_eval=4 * 16, env_sample=16 + 8, record=2 * 48)
+# algorithmic-bytes model of the roofline): a binary node (64) or wide node
+# (80), a triangle (48), a hit (its 64-byte shading record + the 276-byte
+# material), a bilinear environment lookup (4 texels), an environment sample
+# (alias entry + per-texel sample record), the plain form's path record.
+BYTES = dict(node=64, tri=48, hit=64 + 276, env_eval=4 * 16, env_sample=8 + 32, record=2 * 48)
 
 
 def parse():

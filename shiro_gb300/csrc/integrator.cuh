@@ -69,21 +69,20 @@ struct Vertex {
 __device__ __forceinline__ Surface make_surface(const DevScene& s, const V3& o, const V3& d, const HitRec& h) {
     Surface sf;
     sf.position = o + d * h.t;
-    const float4* tp = s.tris + 3 * static_cast<size_t>(h.slot);
-    const V3 e1 = f4xyz(__ldg(tp + 1)), e2 = f4xyz(__ldg(tp + 2));
-    const V3 ng = normalize(cross(e1, e2));
+    const float4* r = s.shade + kShadeRec * static_cast<size_t>(h.gid);
+    const float4 r0 = __ldg(r);
+    const uint32_t bits = __float_as_uint(r0.w);
+    const V3 ng = f4xyz(r0);  // normalize(cross(e1, e2)) of the triangle, formed at upload
     sf.ng = ng;
-    const uint4 tv = __ldg(&s.triVerts[h.gid]);
     V3 ns = ng;
-    if (__ldg(&s.meshHasNormals[tv.w])) {
+    if (bits & kShadeNormals) {
         const float b0 = 1.0f - h.u - h.v, b1 = h.u, b2 = h.v;
-        const V3 n0 = f4xyz(__ldg(&s.normals[tv.x])), n1 = f4xyz(__ldg(&s.normals[tv.y])),
-                 n2 = f4xyz(__ldg(&s.normals[tv.z]));
+        const V3 n0 = f4xyz(__ldg(r + 1)), n1 = f4xyz(__ldg(r + 2)), n2 = f4xyz(__ldg(r + 3));
         const V3 interp = n0 * b0 + n1 * b1 + n2 * b2;
         if (length(interp) > 0.0f) ns = normalize(interp);
     }
     sf.ns = ns;
-    sf.material = __ldg(&s.meshMaterial[tv.w]);
+    sf.material = bits & ~kShadeNormals;
     sf.gid = h.gid;
     return sf;
 }
@@ -561,7 +560,8 @@ __device__ __forceinline__ PathResult trace_path(const DevScene& s, const DevReq
             if (!enter_hit(s, smp, depth, v, h.t, ps)) continue;
         }
         if (depth == 0) {
-            res.albedo = diffuse_color(s.materials[v.hit.material]);
+            const float4 dc = __ldg(bsdf_rec(s, v.hit.material) + 3);  // DiffuseColor
+            res.albedo = V3{dc.x, dc.y, dc.z};
             res.normal = v.n * 0.5f + V3{0.5f, 0.5f, 0.5f};
             res.depth = h.t;
         }

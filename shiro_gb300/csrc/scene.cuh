@@ -45,15 +45,23 @@ struct DevDistant {
     V3 direction, radiance;
 };
 
+// Shading record of a triangle (make_surface): everything a hit needs past
+// the intersection, indexed by global triangle, so the hit's normal and
+// material come from one 64-byte record instead of triangle -> vertex
+// indices -> normals / mesh -> material chains.  The material index is the
+// mesh's (mapped to the default material when out of range); bit 31 says
+// the mesh carries vertex normals.
+constexpr int kShadeRec = 4;
+constexpr uint32_t kShadeNormals = 0x80000000u;
+
 struct DevScene {
     const float4* nodes;
     const float4* nodes8;           // 8-wide quantised BVH (bvh_build.h); NULL: traverse the binary BVH
     const float4* tris;
     const uint4* triVerts;
-    const float4* normals;
     const float4* positions;
-    const uint32_t* meshMaterial;   // per mesh, already mapped to the default material when out of range
-    const uint32_t* meshHasNormals;
+    const float4* shade;            // kShadeRec per global triangle: (unit geometric normal, material | kShadeNormals),
+                                    // then its three vertex normals (zero when the mesh has none)
     const ShiroMaterialDesc* materials;
     const float4* bsdfRecs;         // kBsdfRec per material: the BSDF's material-only quantities (bsdf.cuh)
     const DevDistant* distant;

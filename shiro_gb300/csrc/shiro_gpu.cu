@@ -301,6 +301,20 @@ __global__ void k_bsdf_recs(const ShiroMaterialDesc* mats, uint32_t n, float4* o
     for (int k = 0; k < kBsdfRec; ++k) out[kBsdfRec * static_cast<size_t>(i) + k] = r[k];
 }
 
+// Geometric normals of the triangle shading records, from the binary BVH's
+// triangle slots (v0 with the global index in w, e1, e2): the same
+// normalize(cross(e1, e2)) a hit formed from its slot.  A triangle held in
+// several slots is written with the same value by each.
+__global__ void k_shade_normals(const float4* __restrict__ tris, uint32_t n, float4* __restrict__ shade) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4* tp = tris + 3 * static_cast<size_t>(i);
+    const uint32_t gid = __float_as_uint(tp[0].w);
+    const V3 ng = normalize(cross(f4xyz(tp[1]), f4xyz(tp[2])));
+    float4* r = shade + kShadeRec * static_cast<size_t>(gid);
+    *r = make_float4(ng.x, ng.y, ng.z, r->w);
+}
+
 // (Re)computes the per-material BSDF records from the resident materials.
 int build_bsdf_recs(ContextImpl* ctx) {
     const uint32_t n = ctx->materialCount + 1u;  // + the default material
@@ -519,9 +533,8 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     ctx->freeScene();
 
     // --- flatten ------------------------------------------------------------
-    std::vector<float4> positions, normals;
+    std::vector<float4> positions;
     std::vector<uint4> triVerts;
-    std::vector<uint32_t> meshMaterial(sd->mesh_count), meshHasNormals(sd->mesh_count);
     size_t vtotal = 0, ttotal = 0;
     for (uint32_t i = 0; i < sd->mesh_count; ++i) {
         const ShiroMeshDesc& m = sd->meshes[i];
@@ -532,9 +545,11 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     }
     if (ttotal >= (1ull << 28) || vtotal >= (1ull << 32))
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene exceeds 2^28 triangles");
+    if (sd->material_count >= kShadeNormals)
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene exceeds 2^31 - 1 materials");
     positions.reserve(vtotal);
-    normals.reserve(vtotal);
     triVerts.reserve(ttotal);
+    std::vector<float4> shade(kShadeRec * ttotal);
     std::vector<float4> triData;      // small triangles: 3 per
     std::vector<float4> primBoxes;    // 2 per
     std::vector<float4> centroids;
@@ -556,16 +571,10 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
             mag = std::max(mag, std::max(std::fabs(p[0]), std::max(std::fabs(p[1]), std::fabs(p[2]))));
         }
         const bool hasN = m.normals && m.normal_count == m.vertex_count;
-        for (uint32_t v = 0; v < m.vertex_count; ++v) {
-            if (hasN) {
-                const float* n = m.normals + 3 * static_cast<size_t>(v);
-                normals.push_back(make_float4(n[0], n[1], n[2], 0.0f));
-            } else {
-                normals.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
-            }
-        }
-        meshHasNormals[i] = hasN ? 1u : 0u;
-        meshMaterial[i] = m.material_index < sd->material_count ? m.material_index : sd->material_count;
+        const uint32_t material = m.material_index < sd->material_count ? m.material_index : sd->material_count;
+        float recBits;
+        const uint32_t rb = material | (hasN ? kShadeNormals : 0u);
+        std::memcpy(&recBits, &rb, 4);
         const uint32_t tris = m.index_count / 3u;
         for (uint32_t t = 0; t < tris; ++t, ++gid) {
             const uint32_t a = m.indices[3 * t], b = m.indices[3 * t + 1], c = m.indices[3 * t + 2];
@@ -573,6 +582,13 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
                 return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT,
                             "mesh " + std::to_string(i) + ": index out of range at triangle " + std::to_string(t));
             triVerts.push_back(make_uint4(base + a, base + b, base + c, i));
+            float4* rec = &shade[kShadeRec * static_cast<size_t>(gid)];
+            rec[0] = make_float4(0.0f, 0.0f, 0.0f, recBits);  // the normal is formed on the device
+            const uint32_t vi[3] = {a, b, c};
+            for (int k = 0; k < 3; ++k) {
+                const float* n = hasN ? m.normals + 3 * static_cast<size_t>(vi[k]) : nullptr;
+                rec[1 + k] = n ? make_float4(n[0], n[1], n[2], 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
             const float* p0 = m.positions + 3 * static_cast<size_t>(a);
             const float* p1 = m.positions + 3 * static_cast<size_t>(b);
             const float* p2 = m.positions + 3 * static_cast<size_t>(c);
@@ -764,10 +780,11 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     ctx->materialsHost.push_back(default_material());
     ctx->materialCount = sd->material_count;
     if ((rc = upload(ctx, triVerts, &s.triVerts, "triangle vertices")) != SHIRO_OK) return rc;
-    if ((rc = upload(ctx, normals, &s.normals, "normals")) != SHIRO_OK) return rc;
     if ((rc = upload(ctx, positions, &s.positions, "positions")) != SHIRO_OK) return rc;
-    if ((rc = upload(ctx, meshMaterial, &s.meshMaterial, "mesh materials")) != SHIRO_OK) return rc;
-    if ((rc = upload(ctx, meshHasNormals, &s.meshHasNormals, "mesh normal flags")) != SHIRO_OK) return rc;
+    if ((rc = upload(ctx, shade, &s.shade, "triangle shading records")) != SHIRO_OK) return rc;
+    k_shade_normals<<<(bout.triCount + 255) / 256, 256, 0, ctx->stream>>>(ctx->tris2, bout.triCount,
+                                                                         const_cast<float4*>(s.shade));
+    if (const cudaError_t e = cudaGetLastError(); e != cudaSuccess) return cuda_fail(ctx, e, "shading records");
     s.emissiveCount = static_cast<uint32_t>(emissiveCdf.size());
     s.emissiveSum = emissiveSum;
     if (s.emissiveCount) {

@@ -387,7 +387,8 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
                     cont = depth + 1u < q.maxDepth;  // passes through an opacity cut-out
                 } else {
                     if (depth == 0) {
-                        const V3 alb = diffuse_color(s.materials[vx.hit.material]);
+                        const float4 dc = __ldg(bsdf_rec(s, vx.hit.material) + 3);  // DiffuseColor
+                        const V3 alb{dc.x, dc.y, dc.z};
                         const V3 nn = vx.n * 0.5f + V3{0.5f, 0.5f, 0.5f};
                         v.records[3 * static_cast<size_t>(j) + 1] = make_float4(alb.x, alb.y, alb.z, 0.0f);
                         v.records[3 * static_cast<size_t>(j) + 2] = make_float4(nn.x, nn.y, nn.z, 0.0f);
