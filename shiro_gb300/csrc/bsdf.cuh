@@ -238,8 +238,11 @@ __device__ __forceinline__ float rec_coat_roughness(const float4* r, uint32_t fl
                                    : r[3].w;
 }
 
-static __device__ __noinline__ float bsdf_pdf_rec(const float4* r, const Mat& m, const LobeWeights& w, const V3& n,
-                                                  const V3& cn, const V3& v, const V3& l) {
+// The out-of-line functions take their vectors by value: a reference
+// argument of a call that is not inlined makes the caller store the vector
+// to its stack and the callee load it back.
+static __device__ __noinline__ float bsdf_pdf_rec(const float4* r, const Mat& m, const LobeWeights w, const V3 n,
+                                                  const V3 cn, const V3 v, const V3 l) {
     const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
     if (nl <= 0.0f) return 0.0f;
     const float rw = w.diffuse + w.spec + w.coat;
@@ -255,8 +258,8 @@ static __device__ __noinline__ float bsdf_pdf_rec(const float4* r, const Mat& m,
     return dp * nl * kInvPi + bp * spec_pdf(n, v, l, sr) + coatTerm;
 }
 
-static __device__ __noinline__ V3 bsdf_eval_rec(const float4* r, const Mat& m, const V3& n, const V3& cn, const V3& v,
-                                               const V3& l) {
+static __device__ __noinline__ V3 bsdf_eval_rec(const float4* r, const Mat& m, const V3 n, const V3 cn, const V3 v,
+                                               const V3 l) {
     const float nv = sclamp(dot(n, v), 0.0f, 1.0f);
     const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
     if (nv <= 0.0f || nl <= 0.0f) return {0.0f, 0.0f, 0.0f};
@@ -381,7 +384,7 @@ __device__ __forceinline__ bool refract_dir(const V3& i, const V3& n, float eta,
     *out = normalize(i * eta + n * (eta * c - sqrtf(k)));
     return true;
 }
-static __device__ __noinline__ V3 transmission_lobe(const Mat& m, const V3& n, const V3& cn, const V3& v, const V3& l,
+static __device__ __noinline__ V3 transmission_lobe(const Mat& m, const V3 n, const V3 cn, const V3 v, const V3 l,
                                                     float etaI, float etaT, float r) {
     const float cosWo = dot(n, v), cosWi = dot(n, l);
     const float aWo = fabsf(cosWo), aWi = fabsf(cosWi);
@@ -403,7 +406,7 @@ static __device__ __noinline__ V3 transmission_lobe(const Mat& m, const V3& n, c
     const float transport = 1.0f / smax(rel * rel, 1.0e-6f);
     return scale * fres * (factor * transport);
 }
-static __device__ __noinline__ float transmission_pdf(const V3& n, const V3& v, const V3& l, float eta, float r) {
+static __device__ __noinline__ float transmission_pdf(const V3 n, const V3 v, const V3 l, float eta, float r) {
     const float cosWo = dot(n, v), cosWi = dot(n, l);
     if (fabsf(cosWo) <= 0.0f || fabsf(cosWi) <= 0.0f || cosWo * cosWi >= 0.0f) return 0.0f;
     V3 h = safe_normalized(v + l * eta, n);

@@ -331,13 +331,12 @@ __device__ __forceinline__ void write_record(const WfView& v, uint32_t j, const 
 // with / without the extended lobes (kExt, chosen by the scene).
 template <int kRegs, bool kExt>
 __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, uint32_t depth) {
-    const uint32_t hits = v.counters[kHitCount];
-    const uint32_t count = hits + v.counters[kMissCount];
+    const uint32_t count = v.counters[kHitCount];
     uint32_t* qout = cur ? v.rayQ0 : v.rayQ1;
     uint32_t* cout = &v.counters[cur ^ 1u];
     NullCounter ctr;
     // whole warps fetch work together, so the warp-aggregated pushes below
-    // always see the whole warp; entries [0, hits) are hits, the rest misses
+    // always see the whole warp; entries [0, hits) of the shade queue
     for (;;) {
         const uint32_t wbase = warp_fetch(&v.counters[kFetchShade]);
         if (wbase >= count) break;
@@ -347,7 +346,7 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
         uint32_t lightMask = 0;
         uint32_t j = 0;
         if (valid) {
-            j = v.shadeQ[i < hits ? i : v.P - 1u - (i - hits)];
+            j = v.shadeQ[i];
             const uint4 id = v.ident[j];
             const DevRequest& q = v.reqs[id.w].q;
             const float4 o = v.ro[j], d = v.rd[j], t4 = v.T[j], r4 = v.rad[j], h4 = v.hit[j];
@@ -376,10 +375,7 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
             h.v = h4.z;
             h.slot = __float_as_uint(h4.w);
             h.gid = v.hitGid[j];
-            if (h.slot == 0xffffffffu) {
-                add_miss(s, q, ps, depth, ctr);
-                write_record(v, j, ps.radiance, depth0);
-            } else {
+            {
                 const Vertex vx = make_vertex(s, ps.ro, ps.rd, h);
                 const Sampler smp{id.x, id.y, id.z};
                 bool anyLight = false, cont;
@@ -433,6 +429,30 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
         warp_push(&v.counters[2], v.shadowQ, pushShadow, j);
         for (uint32_t k = 0; k < v.lightSamples; ++k)
             warp_push(&v.counters[4], v.shadowRayQ, (lightMask >> k) & 1u, (j << 3) | k);
+    }
+}
+
+// Miss shading (the environment and its MIS weight), one queued miss per
+// thread: entries [P - misses, P) of the shade queue.  A kernel of its own so
+// that the misses, half of the shade work, run at the occupancy of their own
+// small register count instead of the hit shading's.
+__global__ void __launch_bounds__(256) wf_miss(WfView v, DevScene s, uint32_t depth) {
+    const uint32_t count = v.counters[kMissCount];
+    NullCounter ctr;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t j = v.shadeQ[v.P - 1u - i];
+        const DevRequest& q = v.reqs[v.ident[j].w].q;
+        const float4 d = v.rd[j], t4 = v.T[j], r4 = v.rad[j];
+        const uint32_t bits = __float_as_uint(t4.w);
+        PathState ps;
+        ps.rd = V3{d.x, d.y, d.z};
+        ps.prevPdf = d.w;
+        ps.T = V3{t4.x, t4.y, t4.z};
+        ps.radiance = V3{r4.x, r4.y, r4.z};
+        ps.prevDelta = (bits & kFlagPrevDelta) != 0u;
+        ps.prevType = (bits >> kTypeShift) & 3u;
+        add_miss(s, q, ps, depth, ctr);
+        write_record(v, j, ps.radiance, r4.w);
     }
 }
 
@@ -676,7 +696,7 @@ Plan plan_waves(const std::vector<DevRequest>& qs, uint32_t P) {
 struct Launch {
     WfView v;
     DevScene s;
-    int gGen, gExt, gShade, gShadow, gOcc, gRes;
+    int gGen, gExt, gShade, gMiss, gShadow, gOcc, gRes;
     int bExt, bShade, bShadow;
     uint32_t depth;
     uint32_t shadeRegs;
@@ -694,6 +714,7 @@ void launch_shade(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t d) {
     } else {
         wf_shade<128, false><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
     }
+    wf_miss<<<L.gMiss, 256, 0, st>>>(L.v, L.s, d);
 }
 
 void enqueue_wave(const Launch& L, cudaStream_t st) {
@@ -794,6 +815,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
                                           : grid_for(wf_shade<128, false>, L.bShade, wf->smCount));
     L.v.travSteps = static_cast<int>(cfg.extend_steps ? cfg.extend_steps : 4);
     L.v.refillIdle = static_cast<int>(cfg.refill_idle ? cfg.refill_idle : 8);
+    L.gMiss = grid_for(wf_miss, 256, wf->smCount);
     L.gShadow = grid_for(wf_shadow, 256, wf->smCount);
     L.gOcc = grid_for(wf_occlude, L.bShadow, wf->smCount);
     L.gRes = grid_for(wf_resolve, 128, wf->smCount);
