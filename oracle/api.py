@@ -103,6 +103,22 @@ def render(ck: Checker, scene, camera, settings, sample_start=0, sample_count=No
     return fb
 
 
+def render_batches(ck: Checker, scene, camera, settings, sample_start, sample_count, batches) -> FrameBuffer:
+    """The last of `batches` consecutive batches rendered by ONE reference
+    tracer (reference checker only), as a progressive render issues them."""
+    ms = MarshalledScene(scene) if not isinstance(scene, MarshalledScene) else scene
+    req = render_desc(camera, settings, sample_start, sample_count)
+    fb = FrameBuffer(settings.width, settings.height)
+    aovs = fb.aovs()
+    f = ck.lib.ref_render_batches
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
+    f.restype = C.c_int
+    rc = f(ms.ref(), C.byref(req), batches, C.byref(aovs))
+    if rc != 0:
+        raise RuntimeError(f"ref_render_batches failed: {rc}")
+    return fb
+
+
 def render_paths(ck: Checker, scene, camera, settings, sample_start, pixels, sample_index):
     """Per-path results of the port: radiance (n,3), albedo (n,3), normal
     (n,3), depth (n,) for paths (pixel index, sample index)."""

@@ -191,6 +191,26 @@ uint32_t GlobalPrim(const Scene& scene, size_t mesh, uint32_t prim) {
 
 }  // namespace
 
+// Host copy of a reference frame into flat AOV planes.
+namespace {
+void CopyFrame(const FrameBuffer& fb, ShiroAovs* out) {
+    const size_t n = static_cast<size_t>(fb.Width()) * fb.Height();
+    for (size_t i = 0; i < n; ++i) {
+        out->beauty[4 * i + 0] = fb.Beauty()[i].x;
+        out->beauty[4 * i + 1] = fb.Beauty()[i].y;
+        out->beauty[4 * i + 2] = fb.Beauty()[i].z;
+        out->beauty[4 * i + 3] = fb.Beauty()[i].w;
+        out->albedo[3 * i + 0] = fb.Albedo()[i].x;
+        out->albedo[3 * i + 1] = fb.Albedo()[i].y;
+        out->albedo[3 * i + 2] = fb.Albedo()[i].z;
+        out->normal[3 * i + 0] = fb.Normal()[i].x;
+        out->normal[3 * i + 1] = fb.Normal()[i].y;
+        out->normal[3 * i + 2] = fb.Normal()[i].z;
+        out->depth[i] = fb.Depth()[i];
+    }
+}
+}  // namespace
+
 extern "C" {
 
 int ref_sampler(uint32_t n, const uint32_t* px, const uint32_t* py, const uint32_t* index,
@@ -342,28 +362,35 @@ int ref_env_query(uint32_t w, uint32_t h, const float* rgb, uint32_t layout, uin
 }
 
 // CpuPathTracer::RenderSampleBatch (CpuPathTracer.cpp:2043-2170) on a fresh
-// tracer instance (so the path guide starts empty and stays inactive).
+// tracer instance (so the path guide starts empty).
 int ref_render(const ShiroSceneDesc* sd, const ShiroRenderDesc* req, ShiroAovs* out) {
     const Scene scene = ToScene(*sd);
     const Camera cam = ToCamera(req->camera);
     const RenderSettings st = ToSettings(req->settings);
     cpu::CpuPathTracer tracer;
     shiro::backend::RenderRequest request{scene, cam, st, req->sample_start, req->sample_count, nullptr};
-    const FrameBuffer fb = tracer.RenderSampleBatch(request);
-    const size_t n = static_cast<size_t>(fb.Width()) * fb.Height();
-    for (size_t i = 0; i < n; ++i) {
-        out->beauty[4 * i + 0] = fb.Beauty()[i].x;
-        out->beauty[4 * i + 1] = fb.Beauty()[i].y;
-        out->beauty[4 * i + 2] = fb.Beauty()[i].z;
-        out->beauty[4 * i + 3] = fb.Beauty()[i].w;
-        out->albedo[3 * i + 0] = fb.Albedo()[i].x;
-        out->albedo[3 * i + 1] = fb.Albedo()[i].y;
-        out->albedo[3 * i + 2] = fb.Albedo()[i].z;
-        out->normal[3 * i + 0] = fb.Normal()[i].x;
-        out->normal[3 * i + 1] = fb.Normal()[i].y;
-        out->normal[3 * i + 2] = fb.Normal()[i].z;
-        out->depth[i] = fb.Depth()[i];
+    CopyFrame(tracer.RenderSampleBatch(request), out);
+    return 0;
+}
+
+// `batches` consecutive batches of req->sample_count samples, starting at
+// req->sample_start, on ONE tracer instance and the same Scene object, as a
+// progressive render issues them (RenderParam.cpp:790): the tracer keeps its
+// path-guide weights between batches of the same scene
+// (CpuPathTracer.cpp:2054-2062, 2158-2167).  Writes the last batch's frame.
+int ref_render_batches(const ShiroSceneDesc* sd, const ShiroRenderDesc* req, uint32_t batches, ShiroAovs* out) {
+    if (batches == 0) return -1;
+    const Scene scene = ToScene(*sd);
+    const Camera cam = ToCamera(req->camera);
+    const RenderSettings st = ToSettings(req->settings);
+    cpu::CpuPathTracer tracer;
+    FrameBuffer fb;
+    for (uint32_t b = 0; b < batches; ++b) {
+        shiro::backend::RenderRequest request{scene, cam, st, req->sample_start + b * req->sample_count,
+                                              req->sample_count, nullptr};
+        fb = tracer.RenderSampleBatch(request);
     }
+    CopyFrame(fb, out);
     return 0;
 }
 

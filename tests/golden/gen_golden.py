@@ -168,6 +168,10 @@ def gen_env(rng):
     return out
 
 
+# frames rendered as the n-th consecutive batch of one reference tracer
+PROGRESSIVE = {"progressive_batch3": 3}
+
+
 def render_cases():
     """Small frames covering the integrator's branches."""
     cases = {}
@@ -263,6 +267,14 @@ def render_cases():
                          backend=1)
     cases["transmission"] = (tra, scenes.look_at((0.5, 1.6, 4.5), (0.0, 0.7, 0.0), 50.0, 48 / 40), st8, 0, 4, 0)
 
+    # third batch of a progressive render: batches of 4 samples at indices
+    # 0, 4, 8 on one reference tracer, which keeps its path-guide weights
+    # between batches of a scene; the frame is stored as the batch it is
+    # (start 8, 4 samples), to be matched by a single render of that batch
+    st9 = RenderSettings(width=48, height=48, samples_per_pixel=4, max_depth=8, diffuse_depth=8, specular_depth=8,
+                         backend=1)
+    cases["progressive_batch3"] = (base, cam, st9, 8, 4, 0)
+
     # single path per pixel at a non-zero sample index (per-path golden)
     st6 = RenderSettings(width=64, height=64, samples_per_pixel=1, max_depth=8, diffuse_depth=8, specular_depth=8,
                          backend=1)
@@ -276,9 +288,14 @@ def gen_renders(only=None):
     for name, (scene, cam, st, start, count, flags) in cases.items():
         if only and name not in only:
             continue
-        fb = api.render(REF, scene, cam, st, start, count)
+        batches = PROGRESSIVE.get(name, 1)
+        if batches > 1:
+            fb = api.render_batches(REF, scene, cam, st, start - (batches - 1) * count, count, batches)
+        else:
+            fb = api.render(REF, scene, cam, st, start, count)
         out[name] = dict(scene_to_arrays(scene), cam=camera_to_array(cam), settings=settings_to_array(st),
                          start=np.array(start), count=np.array(count), flags=np.array(flags),
+                         batches=np.array(batches),
                          beauty=fb.beauty, albedo=fb.albedo, normal=fb.normal, depth=fb.depth)
         print(f"  render {name}: {st.width}x{st.height} {count} spp, mean {fb.beauty[:, :3].mean():.4f}")
     return out

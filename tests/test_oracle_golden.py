@@ -124,8 +124,12 @@ def test_env_tables_and_queries(port):
             assert_same(v, g[pre + k], rtol=1e-4, atol=1e-6, what=pre + k)
 
 
+# progressive_batch3: the third consecutive batch of one reference tracer,
+# matched by a single render of that batch (the reference's path guide,
+# CpuPathTracer.cpp:1953-1987, never becomes active: its weights start at zero
+# and grow only through records pushed while it is active)
 RENDERS = ["sphere", "rich", "features_gradient_env", "angular_env", "field_small", "sphere_1spp_start5", "emissive",
-           "opacity", "transmission"]
+           "opacity", "transmission", "progressive_batch3"]
 
 
 @pytest.mark.parametrize("name", RENDERS)
