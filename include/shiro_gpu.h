@@ -401,6 +401,51 @@ typedef struct ShiroWorkCounts {
 int shiro_gpu_count_work(ShiroGpuContext* ctx, const ShiroRenderDesc* request, uint32_t stride,
                          ShiroWorkCounts* out);
 
+/* ---- device-resident progressive accumulation --------------------------
+ * Renderer::FrameAccumulator (Renderer.cpp:47-110) kept in device memory:
+ * the per-pixel running sums of a progressive render stay on the GPU, each
+ * batch is folded in where it was rendered, and a resolved frame is copied
+ * out only when the caller asks for one (instead of one host frame per batch
+ * plus the host accumulation of HdShiroRenderParam's worker,
+ * RenderParam.cpp:790-806).  The sums use the reference's float32 arithmetic
+ * (sum + frame * sampleCount; resolve by 1 / total samples; depth averaged
+ * over the samples that hit).  An accumulator belongs to the context it was
+ * created on and uses its stream; once the context is destroyed only
+ * shiro_gpu_accum_destroy may still be called on it. */
+typedef struct ShiroAccumulator ShiroAccumulator;
+int shiro_gpu_accum_create(ShiroGpuContext* ctx, ShiroAccumulator** out);
+void shiro_gpu_accum_destroy(ShiroAccumulator* acc);
+/* FrameAccumulator::Reset (Renderer.cpp:47-58). */
+int shiro_gpu_accum_reset(ShiroAccumulator* acc, uint32_t width, uint32_t height);
+/* FrameAccumulator::Accumulate (Renderer.cpp:60-84): folds a width x height
+ * frame (host or device planes, per frame->on_device) rendered with
+ * sample_count samples per pixel; a frame of another size resets the sums
+ * first; an empty frame or sample_count 0 is ignored. */
+int shiro_gpu_accum_add(ShiroAccumulator* acc, const ShiroAovs* frame, uint32_t width, uint32_t height,
+                        uint32_t sample_count);
+/* One step of the progressive loop (RenderParam.cpp:790-806): renders the
+ * request's batch into device planes (wavefront != 0: the batched wavefront
+ * form, else the plain one); unless the batch was cancelled, resets the sums
+ * when it starts at sample 0 or nothing is accumulated yet, then folds it in.
+ * Returns the render's status (a cancelled batch is not accumulated). */
+int shiro_gpu_accum_render(ShiroAccumulator* acc, const ShiroRenderDesc* request, const volatile int* cancel,
+                           uint32_t wavefront);
+/* The same step in two halves, for callers that decide after the render
+ * whether the batch counts (RenderParam.cpp:791-798 reads its cancel flag
+ * once the batch returns): _stage renders the batch into the accumulator's
+ * pending frame, _commit folds the pending frame in with the rule above
+ * (SHIRO_ERR_INVALID_ARGUMENT when nothing is pending).  A new _stage
+ * replaces an uncommitted pending frame. */
+int shiro_gpu_accum_stage(ShiroAccumulator* acc, const ShiroRenderDesc* request, const volatile int* cancel,
+                          uint32_t wavefront);
+int shiro_gpu_accum_commit(ShiroAccumulator* acc);
+/* FrameAccumulator::Resolve (Renderer.cpp:86-110) into host or device planes
+ * (per out->on_device) of the accumulated size; with nothing accumulated the
+ * frame is cleared (FrameBuffer::Resize: zeros, depth +inf). */
+int shiro_gpu_accum_resolve(ShiroAccumulator* acc, ShiroAovs* out);
+/* FrameAccumulator::SampleCount and the accumulated size. */
+int shiro_gpu_accum_info(const ShiroAccumulator* acc, uint32_t* sample_count, uint32_t* width, uint32_t* height);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,6 +18,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 import sys
+import weakref
 from dataclasses import dataclass
 from typing import List, Optional, Sequence
 
@@ -73,6 +74,13 @@ def load_library(path: str = LIB_PATH):
         "shiro_gpu_count_work": ([_P, _P, _U, _P], C.c_int),
         "shiro_gpu_render_frozen": ([_P, _P, _P, _P, _P, _P, _P], C.c_int),
         "shiro_gpu_set_bvh_width": ([_P, _U], C.c_int),
+        "shiro_gpu_accum_create": ([_P, _P], C.c_int),
+        "shiro_gpu_accum_destroy": ([_P], None),
+        "shiro_gpu_accum_reset": ([_P, _U, _U], C.c_int),
+        "shiro_gpu_accum_add": ([_P, _P, _U, _U, _U], C.c_int),
+        "shiro_gpu_accum_render": ([_P, _P, _P, _U], C.c_int),
+        "shiro_gpu_accum_resolve": ([_P, _P], C.c_int),
+        "shiro_gpu_accum_info": ([_P, _P, _P, _P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -112,10 +120,13 @@ class GpuBackend:
         self._scene_key = None
         self._marshalled: Optional[MarshalledScene] = None
         self.last_error = ""
+        self._accumulators = weakref.WeakSet()
 
     # -- lifetime ----------------------------------------------------------
     def close(self):
         if self._ctx:
+            for acc in list(self._accumulators):  # they use the context: free them first
+                acc.close()
             self.lib.shiro_gpu_destroy(self._ctx)
             self._ctx = C.c_void_p()
 
@@ -286,6 +297,11 @@ class GpuBackend:
             raise self._err(rc)
         return {k: getattr(wc, k) for k, _ in WorkCounts._fields_}
 
+    # -- progressive accumulation ---------------------------------------------
+    def accumulator(self) -> "DeviceAccumulator":
+        """A device-resident Renderer::FrameAccumulator on this context."""
+        return DeviceAccumulator(self)
+
     # -- differentiable form -------------------------------------------------
     @staticmethod
     def _dptr(t):
@@ -363,3 +379,70 @@ class GpuBackend:
     @property
     def handle(self):
         return self._ctx
+
+
+class DeviceAccumulator:
+    """Renderer::FrameAccumulator (Renderer.cpp:47-110) with its running sums
+    in device memory: ``reset`` / ``accumulate`` / ``resolve`` /
+    ``sample_count`` follow Reset / Accumulate / Resolve / SampleCount, and
+    ``render_step`` is one step of HdShiroRenderParam's progressive worker
+    (RenderParam.cpp:790-806): render a batch on the device and fold it in
+    there, with no host frame per batch."""
+
+    def __init__(self, backend: GpuBackend):
+        self.backend = backend
+        self.lib = backend.lib
+        self._h = C.c_void_p()
+        if not backend._ctx:
+            raise ShiroGpuError(abi.SHIRO_ERR_INVALID_ARGUMENT, "backend is closed")
+        rc = self.lib.shiro_gpu_accum_create(backend._ctx, C.byref(self._h))
+        if rc != 0:
+            raise backend._err(rc)
+        backend._accumulators.add(self)
+
+    def close(self):
+        if self._h:
+            self.lib.shiro_gpu_accum_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise self.backend._err(rc)
+
+    def reset(self, width: int, height: int):
+        self._check(self.lib.shiro_gpu_accum_reset(self._h, int(width), int(height)))
+
+    def accumulate(self, fb: FrameBuffer, sample_count: int):
+        """Folds a host FrameBuffer rendered with `sample_count` samples."""
+        aovs = fb.aovs()
+        self._check(self.lib.shiro_gpu_accum_add(self._h, C.byref(aovs), fb.width, fb.height, int(sample_count)))
+
+    def render_step(self, scene: Scene, camera: Camera, settings: RenderSettings, sample_start: int,
+                    sample_count: int, flags: int = 0, cancel: Optional[C.c_int] = None, wavefront: bool = False):
+        self.backend.upload_scene(scene)
+        req = render_desc(camera, settings, sample_start, sample_count, flags)
+        self._check(self.lib.shiro_gpu_accum_render(self._h, C.byref(req),
+                                                    C.byref(cancel) if cancel is not None else None,
+                                                    1 if wavefront else 0))
+
+    def info(self) -> tuple:
+        n, w, h = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        self._check(self.lib.shiro_gpu_accum_info(self._h, C.byref(n), C.byref(w), C.byref(h)))
+        return n.value, w.value, h.value
+
+    def sample_count(self) -> int:
+        return self.info()[0]
+
+    def resolve(self, out: Optional[FrameBuffer] = None) -> FrameBuffer:
+        """The accumulated frame, copied to the host once."""
+        _, w, h = self.info()
+        fb = out if out is not None else FrameBuffer(w, h)
+        aovs = fb.aovs()
+        self._check(self.lib.shiro_gpu_accum_resolve(self._h, C.byref(aovs)))
+        return fb

@@ -198,6 +198,7 @@ bool Cancelled(const std::atomic<bool>* c) { return c && c->load(std::memory_ord
 GpuBackend::GpuBackend(int device) : device_(device) {}
 
 GpuBackend::~GpuBackend() {
+    if (accum_) shiro_gpu_accum_destroy(accum_);
     if (ctx_) shiro_gpu_destroy(ctx_);
 }
 
@@ -292,6 +293,52 @@ std::vector<render::FrameBuffer> GpuBackend::RenderSampleBatches(const std::vect
     }
     for (size_t i = 0; i < requests.size(); ++i) planes[i].CopyTo(&frames[i]);
     return frames;
+}
+
+bool GpuBackend::RenderAndAccumulate(const RenderRequest& request, bool wavefront) const {
+    if (request.sampleCount == 0 || Cancelled(request.cancel)) return false;
+    std::scoped_lock lock(mutex_);
+    if (!EnsureRuntime(request.scene)) return false;
+    if (!accum_ && shiro_gpu_accum_create(ctx_, &accum_) != SHIRO_OK) {
+        accum_ = nullptr;
+        return false;
+    }
+    const ShiroRenderDesc desc = ToRequest(request);
+    const int rc = shiro_gpu_accum_stage(accum_, &desc, nullptr, wavefront ? 1u : 0u);
+    if (rc != SHIRO_OK) {
+        std::fprintf(stderr, "[shiro gb300] render failed (%d): %s\n", rc, shiro_gpu_last_error(ctx_));
+        return false;
+    }
+    if (Cancelled(request.cancel)) return false;  // RenderParam.cpp:791-798: a cancelled batch is discarded
+    if (shiro_gpu_accum_commit(accum_) != SHIRO_OK) {
+        std::fprintf(stderr, "[shiro gb300] accumulation failed: %s\n", shiro_gpu_last_error(ctx_));
+        return false;
+    }
+    return true;
+}
+
+render::FrameBuffer GpuBackend::ResolveAccumulation() const {
+    std::scoped_lock lock(mutex_);
+    render::FrameBuffer frame;
+    uint32_t samples = 0, w = 0, h = 0;
+    if (!accum_ || shiro_gpu_accum_info(accum_, &samples, &w, &h) != SHIRO_OK) return frame;
+    frame.Resize(w, h);
+    Planes planes(static_cast<size_t>(w) * h);
+    ShiroAovs aovs = planes.Aovs();
+    if (shiro_gpu_accum_resolve(accum_, &aovs) != SHIRO_OK) {
+        std::fprintf(stderr, "[shiro gb300] resolve failed: %s\n", shiro_gpu_last_error(ctx_));
+        frame.Clear();
+        return frame;
+    }
+    planes.CopyTo(&frame);
+    return frame;
+}
+
+uint32_t GpuBackend::AccumulatedSampleCount() const {
+    std::scoped_lock lock(mutex_);
+    uint32_t samples = 0;
+    if (accum_) shiro_gpu_accum_info(accum_, &samples, nullptr, nullptr);
+    return samples;
 }
 
 }  // namespace shiro::backend::gb300

@@ -18,6 +18,7 @@
 #include "shiro/backend/RenderBackend.h"
 
 struct ShiroGpuContext;
+struct ShiroAccumulator;
 
 namespace shiro::backend::gb300 {
 
@@ -37,12 +38,25 @@ public:
     // call (all requests must reference the same Scene object).
     std::vector<render::FrameBuffer> RenderSampleBatches(const std::vector<RenderRequest>& requests) const;
 
+    // Progressive accumulation kept in device memory
+    // (Renderer::FrameAccumulator, Renderer.cpp:47-110): one call per step of
+    // HdShiroRenderParam's worker (RenderParam.cpp:790-806) renders the batch
+    // and, unless request.cancel was set by the time it returned, folds it into
+    // the device sums (restarting them for a batch at sample 0); nothing is
+    // copied to the host.  Returns false when the batch was not accumulated.
+    bool RenderAndAccumulate(const RenderRequest& request, bool wavefront = false) const;
+    // FrameAccumulator::Resolve: the accumulated frame, copied out once.
+    render::FrameBuffer ResolveAccumulation() const;
+    // FrameAccumulator::SampleCount.
+    uint32_t AccumulatedSampleCount() const;
+
 private:
     bool EnsureRuntime(const render::Scene& scene) const;
 
     int device_;
     mutable std::mutex mutex_;
     mutable ShiroGpuContext* ctx_ = nullptr;
+    mutable ShiroAccumulator* accum_ = nullptr;
     mutable bool runtimeAttempted_ = false;
     mutable bool runtimeFailed_ = false;
     mutable const render::Scene* cachedScene_ = nullptr;

@@ -123,10 +123,14 @@ void Copy(const FrameBuffer& fb, ShiroAovs* out) {
 
 extern "C" {
 
-// Renders `count` requests of one scene through GpuBackend: count == 1 uses
-// RenderSampleBatch, count > 1 RenderSampleBatches.  Returns 1 when the
-// backend reported itself available and supported the scene, 0 otherwise.
-int shiro_backend_selftest(const ShiroSceneDesc* sd, const ShiroRenderDesc* reqs, uint32_t count, ShiroAovs* outs) {
+// Renders `count` requests of one scene through GpuBackend.  mode 0:
+// count == 1 uses RenderSampleBatch, count > 1 RenderSampleBatches.  mode 1:
+// the requests are consecutive steps of a progressive render
+// (RenderAndAccumulate, plain or wavefront form) and outs[0] receives
+// ResolveAccumulation().  Returns 1 when the backend reported itself available
+// and supported the scene, 0 otherwise, -1 when a step was not accumulated.
+int shiro_backend_selftest(const ShiroSceneDesc* sd, const ShiroRenderDesc* reqs, uint32_t count, ShiroAovs* outs,
+                           uint32_t mode, uint32_t wavefront) {
     static shiro::backend::gb300::GpuBackend backend(0);
     if (!backend.GetStatus().available) return 0;
     const Scene scene = ToScene(*sd);
@@ -154,6 +158,12 @@ int shiro_backend_selftest(const ShiroSceneDesc* sd, const ShiroRenderDesc* reqs
     for (uint32_t i = 0; i < count; ++i)
         rq.push_back(shiro::backend::RenderRequest{scene, cams[i], settings[i], reqs[i].sample_start, reqs[i].sample_count,
                                                    nullptr});
+    if (mode == 1) {  // progressive: every request is one step, then one resolve
+        for (uint32_t i = 0; i < count; ++i)
+            if (!backend.RenderAndAccumulate(rq[i], wavefront != 0)) return -1;
+        Copy(backend.ResolveAccumulation(), &outs[0]);
+        return 1;
+    }
     if (count == 1) {
         Copy(backend.RenderSampleBatch(rq[0]), &outs[0]);
     } else {
