@@ -106,6 +106,7 @@ struct WfView {
     uint32_t lightSamples;
     int travSteps;     // wide-BVH nodes per lane between refills
     int refillIdle;    // idle lanes that trigger a refill
+    uint32_t waveStride;  // waves in flight at once: this pool runs waves k, k + stride, ...
 };
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -136,7 +137,7 @@ __device__ __forceinline__ const WaveSeg& find_seg(const WfView& v, const WaveDe
 
 __global__ void wf_begin(WfView v) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
-        const uint32_t w = v.counters[3] + 1u;
+        const uint32_t w = v.counters[3] + v.waveStride;
         v.counters[3] = w;
         v.counters[0] = v.waves[w].paths;
         v.counters[1] = 0u;
@@ -554,17 +555,28 @@ __global__ void __launch_bounds__(128) wf_resolve(WfView v) {
 // ===========================================================================
 // host side
 // ===========================================================================
-struct WavefrontState {
-    ShiroWavefrontConfig cfg{};
-    DeviceBlock state, shadow, queues, records, tables;
-    uint32_t P = 0, lightSamples = 0;
-    int smCount = 0;
-    bool tuned = false;
+// One pool of paths in flight with its queues, and the wave graph it replays.
+struct WavePool {
+    DeviceBlock state, shadow, queues, records;
     // the last instantiated wave graph and the launch parameters it bakes in
     // (reused while a call's parameters are byte-identical: only the tables'
     // contents differ between such calls, and the kernels read them from memory)
     cudaGraphExec_t exec = nullptr;
     std::vector<unsigned char> execKey;
+};
+
+constexpr uint32_t kMaxConcurrentWaves = 2;
+
+struct WavefrontState {
+    ShiroWavefrontConfig cfg{};
+    WavePool pools[kMaxConcurrentWaves];
+    DeviceBlock tables;
+    int smCount = 0;
+    bool tuned = false;
+    // second stream for the second wave in flight, and the events that fork
+    // it from / join it to the context's stream
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 namespace {
@@ -581,12 +593,13 @@ WavefrontState* wf_state(ContextImpl* ctx) {
         c.shade_regs = 128;
         c.extend_steps = 4;
         c.refill_idle = 8;
+        c.concurrent_waves = 1;
         cudaDeviceGetAttribute(&ctx->wavefront->smCount, cudaDevAttrMultiProcessorCount, ctx->device);
     }
     return ctx->wavefront;
 }
 
-bool ensure_pool(ContextImpl* ctx, WavefrontState* wf, uint32_t P, uint32_t lightSamples) {
+bool ensure_pool(ContextImpl* ctx, WavePool* wf, uint32_t P, uint32_t lightSamples) {
     const size_t p = P;
     const size_t stateBytes = p * (7 * sizeof(float4) + sizeof(uint32_t));
     const size_t shadowBytes = p * (2 + 2 * static_cast<size_t>(std::max(1u, lightSamples))) * sizeof(float4);
@@ -596,14 +609,13 @@ bool ensure_pool(ContextImpl* ctx, WavefrontState* wf, uint32_t P, uint32_t ligh
     if (!ensure_block(ctx, &wf->shadow, shadowBytes, "wavefront shadow records")) return false;
     if (!ensure_block(ctx, &wf->queues, queueBytes, "wavefront queues")) return false;
     if (!ensure_block(ctx, &wf->records, recordBytes, "wavefront path records")) return false;
-    wf->P = P;
-    wf->lightSamples = lightSamples;
     return true;
 }
 
-WfView make_view(WavefrontState* wf, uint32_t P, uint32_t lightSamples, const WaveDesc* waves, const WaveSeg* segs,
+WfView make_view(WavePool* wf, uint32_t P, uint32_t lightSamples, const WaveDesc* waves, const WaveSeg* segs,
                  const WfRequest* reqs) {
-    WfView v{};
+    WfView v;
+    std::memset(&v, 0, sizeof(v));  // padding too: the bytes key the graph cache
     const size_t p = P;
     char* st = static_cast<char*>(wf->state.ptr);
     v.ro = reinterpret_cast<float4*>(st);
@@ -776,9 +788,19 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
         return SHIRO_OK;
     }
     uint32_t used = std::min<uint32_t>(static_cast<uint32_t>(pl.waves.size()), maxWaves);
-    uint32_t poolP = 0;
-    for (uint32_t w = 0; w < used; ++w) poolP = std::max(poolP, pl.waves[w].paths);
-    if (!ensure_pool(ctx, wf, poolP, lightSamples)) return SHIRO_ERR_OUT_OF_MEMORY;
+    // waves in flight at once: pool k runs waves k, k + nl, ... on its own
+    // stream (graphs only; the diagnostic per-stage timing runs one)
+    const uint32_t nl = (cfg.use_graph && cfg.concurrent_waves >= 2 && used >= 2) ? 2u : 1u;
+    uint32_t poolP[kMaxConcurrentWaves] = {0, 0};
+    for (uint32_t w = 0; w < used; ++w) poolP[w % nl] = std::max(poolP[w % nl], pl.waves[w].paths);
+    for (uint32_t k = 0; k < nl; ++k)
+        if (!ensure_pool(ctx, &wf->pools[k], poolP[k], lightSamples)) return SHIRO_ERR_OUT_OF_MEMORY;
+    if (nl > 1 && !wf->side) {
+        cudaError_t ce = cudaStreamCreateWithFlags(&wf->side, cudaStreamNonBlocking);
+        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&wf->fork, cudaEventDisableTiming);
+        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&wf->join, cudaEventDisableTiming);
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "wavefront side stream");
+    }
     // tables: waves, segments, requests
     std::vector<WfRequest> rq(qs.size());
     for (size_t r = 0; r < qs.size(); ++r) rq[r] = WfRequest{qs[r], aovs[r]};
@@ -796,7 +818,8 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     if (e != cudaSuccess) return cuda_fail(ctx, e, "wavefront tables");
     Launch L;
     std::memset(&L, 0, sizeof(L));  // padding too: the bytes key the graph cache
-    L.v = make_view(wf, poolP, lightSamples, dWaves, dSegs, dReqs);
+    L.v = make_view(&wf->pools[0], poolP[0], lightSamples, dWaves, dSegs, dReqs);
+    L.v.waveStride = nl;
     L.s = ctx->scene;
     if (ctx->bvhWidth != 2 && ctx->nodes8) {  // the wavefront stages traverse the wide BVH unless told otherwise
         L.s.nodes8 = ctx->nodes8;
@@ -820,42 +843,65 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.gOcc = grid_for(wf_occlude, L.bShadow, wf->smCount);
     L.gRes = grid_for(wf_resolve, 128, wf->smCount);
     L.depth = pl.maxDepth;
-    const uint32_t minus1 = 0xffffffffu;
-    e = cudaMemsetAsync(L.v.counters, 0, 16 * sizeof(uint32_t), st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(L.v.counters + 3, &minus1, 4, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "wavefront counters");
+    Launch lanes[kMaxConcurrentWaves];
+    for (uint32_t k = 0; k < nl; ++k) {
+        std::memcpy(&lanes[k], &L, sizeof(Launch));  // bytes, padding included: they key the graph cache
+        if (k > 0) {
+            WfView v = make_view(&wf->pools[k], poolP[k], lightSamples, dWaves, dSegs, dReqs);
+            v.waveStride = nl;
+            v.travSteps = L.v.travSteps;
+            v.refillIdle = L.v.refillIdle;
+            std::memcpy(&lanes[k].v, &v, sizeof(WfView));
+        }
+        // wf_begin adds the stride to the wave index: start one stride below k
+        const uint32_t first = k - nl;
+        e = cudaMemsetAsync(lanes[k].v.counters, 0, 16 * sizeof(uint32_t), st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(lanes[k].v.counters + 3, &first, 4, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "wavefront counters");
+    }
 
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev;
-    cudaGraphExec_t exec = nullptr;
+    cudaGraphExec_t exec[kMaxConcurrentWaves] = {nullptr, nullptr};
     int rc = SHIRO_OK;
     if (cfg.use_graph) {
-        const unsigned char* key = reinterpret_cast<const unsigned char*>(&L);
-        if (wf->exec && wf->execKey.size() == sizeof(Launch) && std::memcmp(wf->execKey.data(), key, sizeof(Launch)) == 0) {
-            exec = wf->exec;
-        } else {
-            if (wf->exec) cudaGraphExecDestroy(wf->exec);
-            wf->exec = nullptr;
-            wf->execKey.clear();
+        for (uint32_t k = 0; k < nl && rc == SHIRO_OK; ++k) {
+            WavePool& pool = wf->pools[k];
+            const unsigned char* key = reinterpret_cast<const unsigned char*>(&lanes[k]);
+            if (pool.exec && pool.execKey.size() == sizeof(Launch) &&
+                std::memcmp(pool.execKey.data(), key, sizeof(Launch)) == 0) {
+                exec[k] = pool.exec;
+                continue;
+            }
+            if (pool.exec) cudaGraphExecDestroy(pool.exec);
+            pool.exec = nullptr;
+            pool.execKey.clear();
             cudaGraph_t graph = nullptr;
             e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
-                enqueue_wave(L, st);
+                enqueue_wave(lanes[k], st);
                 e = cudaStreamEndCapture(st, &graph);
             }
-            if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&exec[k], graph, 0);
             if (graph) cudaGraphDestroy(graph);
             if (e != cudaSuccess) {
-                exec = nullptr;
+                exec[k] = nullptr;
                 rc = cuda_fail(ctx, e, "wavefront graph");
             } else {
-                wf->exec = exec;
-                wf->execKey.assign(key, key + sizeof(Launch));
+                pool.exec = exec[k];
+                pool.execKey.assign(key, key + sizeof(Launch));
             }
         }
+    }
+    // the second wave in flight runs on the side stream, after the tables and
+    // counters written above, and the context's stream waits for it at the end
+    if (rc == SHIRO_OK && nl > 1) {
+        e = cudaEventRecord(wf->fork, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(wf->side, wf->fork, 0);
+        if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront fork");
     }
     uint64_t launches = 0;
     for (uint32_t w = 0; w < used && rc == SHIRO_OK; ++w) {
@@ -863,14 +909,19 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             rc = fail(ctx, SHIRO_ERR_CANCELLED, "cancelled");
             break;
         }
-        if (exec) {
-            e = cudaGraphLaunch(exec, st);
+        const uint32_t k = w % nl;
+        if (exec[k]) {
+            e = cudaGraphLaunch(exec[k], k == 0 ? st : wf->side);
         } else {
             enqueue_wave_timed(L, st, ev);
             e = cudaGetLastError();
         }
-        launches += 3 + 5ull * L.depth;
+        launches += 3 + 6ull * L.depth;
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront launch");
+    }
+    if (nl > 1) {  // join (also after a failed launch: the side stream's work must be done before we return)
+        cudaEventRecord(wf->join, wf->side);
+        cudaStreamWaitEvent(st, wf->join, 0);
     }
     cudaEventRecord(e1, st);
     e = cudaEventSynchronize(e1);
@@ -979,9 +1030,16 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
 void wavefront_free(ContextImpl* ctx) {
     if (!ctx->wavefront) return;
     WavefrontState* wf = ctx->wavefront;
-    if (wf->exec) cudaGraphExecDestroy(wf->exec);
-    for (DeviceBlock* b : {&wf->state, &wf->shadow, &wf->queues, &wf->records, &wf->tables})
-        if (b->ptr) cudaFree(b->ptr);
+    if (wf->side) cudaStreamSynchronize(wf->side);
+    for (WavePool& pool : wf->pools) {
+        if (pool.exec) cudaGraphExecDestroy(pool.exec);
+        for (DeviceBlock* b : {&pool.state, &pool.shadow, &pool.queues, &pool.records})
+            if (b->ptr) cudaFree(b->ptr);
+    }
+    if (wf->tables.ptr) cudaFree(wf->tables.ptr);
+    if (wf->fork) cudaEventDestroy(wf->fork);
+    if (wf->join) cudaEventDestroy(wf->join);
+    if (wf->side) cudaStreamDestroy(wf->side);
     delete wf;
     ctx->wavefront = nullptr;
 }
@@ -1012,6 +1070,9 @@ int wavefront_set_config(ContextImpl* ctx, const ShiroWavefrontConfig* cfg) {
     if (cfg->shade_regs) wf->cfg.shade_regs = cfg->shade_regs;
     if (cfg->extend_steps) wf->cfg.extend_steps = cfg->extend_steps;
     if (cfg->refill_idle) wf->cfg.refill_idle = cfg->refill_idle;
+    if (cfg->concurrent_waves > kMaxConcurrentWaves)
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "concurrent_waves must be 1 or 2");
+    if (cfg->concurrent_waves) wf->cfg.concurrent_waves = cfg->concurrent_waves;
     wf->cfg.use_graph = cfg->use_graph;
     return SHIRO_OK;
 }
@@ -1091,6 +1152,17 @@ int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefr
         ShiroWavefrontConfig c = best;
         c.shade_regs = regs;
         if ((rc = trial(c)) != SHIRO_OK) return rc;
+    }
+    // two waves in flight (each with a pool of the chosen size or half of it)
+    if (total > best.paths_in_flight) {
+        const uint32_t p1 = best.paths_in_flight;
+        for (uint32_t p : {p1, p1 / 2}) {
+            if (p < (1u << 20)) continue;
+            ShiroWavefrontConfig c = best;
+            c.concurrent_waves = 2;
+            c.paths_in_flight = p;
+            if ((rc = trial(c)) != SHIRO_OK) return rc;
+        }
     }
     if (ctx->nodes8 && ctx->bvhWidth != 2) {  // the lane refill of the wide-BVH extend stage
         for (uint32_t steps : {2u, 4u, 8u}) {

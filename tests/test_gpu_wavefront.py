@@ -101,8 +101,33 @@ def test_uneven_batch_small_pool(gpu):
                                  use_graph=1)
 
 
+@pytest.mark.parametrize("pool", [4096, 5000])
+def test_two_waves_in_flight_uneven_batch(gpu, pool):
+    """Two pools, each on its own stream, take alternate waves (an odd and an
+    even count of waves, requests straddling waves of both pools): frames
+    equal the plain ones bit for bit, and a second call reuses both graphs."""
+    from shiro_gb300 import scenes
+
+    scene = scenes.sphere_scene(env_width=128, env_height=64)
+    reqs = scenes.batch_requests(count=7, seed=11, lo=8, hi=40)
+    base = gpu.wavefront_config()
+    gpu.set_wavefront_config(paths_in_flight=pool, concurrent_waves=2, use_graph=1)
+    try:
+        for _ in range(2):
+            outs = gpu.render_batch(scene, [(r.camera, r.settings) for r in reqs])
+            assert gpu.last_stats()["waves"] >= 3
+            for r, fb in zip(reqs, outs):
+                ref = gpu.render(scene, r.camera, r.settings)
+                ok, k, n = same(ref, fb)
+                assert ok, (pool, r.settings.width, r.settings.samples_per_pixel, k, n)
+    finally:
+        gpu.set_wavefront_config(**base)
+    assert gpu.wavefront_config()["concurrent_waves"] == base["concurrent_waves"]
+
+
 @pytest.mark.parametrize("knobs", [dict(shade_regs=96), dict(extend_steps=1, refill_idle=1),
-                                   dict(extend_steps=32, refill_idle=32), dict(extend_steps=3, refill_idle=5)])
+                                   dict(extend_steps=32, refill_idle=32), dict(extend_steps=3, refill_idle=5),
+                                   dict(concurrent_waves=2, paths_in_flight=2048)])
 def test_tuning_knobs_keep_frames_identical(gpu, knobs):
     """Register cap of the shade stage and the lane-refill parameters of the
     wide-BVH extend stage change scheduling only."""
