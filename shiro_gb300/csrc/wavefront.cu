@@ -1119,6 +1119,7 @@ int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefr
         c.use_graph = 1;
         double rate = 0.0;
         const int r = measure(c, &rate);
+        if (r == SHIRO_ERR_OUT_OF_MEMORY) return SHIRO_OK;  // a pool that does not fit is no candidate
         if (r != SHIRO_OK) return r;
         if (rate > bestRate) {
             bestRate = rate;
@@ -1126,7 +1127,7 @@ int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefr
         }
         return SHIRO_OK;
     };
-    const uint32_t pools[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24};
+    const uint32_t pools[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24, 1u << 25};
     for (uint32_t p : pools) {
         if (p > total * 2 && p != pools[0]) break;
         ShiroWavefrontConfig c = best;
