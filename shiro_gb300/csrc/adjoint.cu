@@ -2,10 +2,10 @@
 //
 // Gradients of an image loss with respect to per-material base colour,
 // specular roughness and metalness and to the texels of dome light 0's
-// environment map, by path replay: every path is recomputed from its QMC
-// seed twice - once for its radiance L, once to push the adjoint radiance
-// dL/dL_path = d_beauty(pixel) / spp into the parameters - so no path
-// vertex is stored.
+// environment map, by path replay: every path is traced twice from its QMC
+// seed - once by the plain megakernel for its radiance L (its path record),
+// once here to push the adjoint radiance dL/dL_path = d_beauty(pixel) / spp
+// into the parameters - so no path vertex is stored.
 //
 // Estimator: the one of integrator.cuh (same sample dimensions, lobe
 // choice, MIS, clamps, Russian roulette).  Sampling decisions, pdfs, MIS
@@ -44,8 +44,7 @@ struct AdjView {
     float* dBase;          // 3 per material
     float* dRough;
     float* dMetal;
-    float* dEnv;  // 3 per texel of env0
-    uint32_t useShared;
+    float4* dEnv4;  // per texel of env0: gradient (rgb, unused), summed into the caller's 3-per-texel array after
     uint32_t distinctEval;  // evalMats differ from the scene's: track the sampling throughput too
 };
 
@@ -97,38 +96,41 @@ __device__ __forceinline__ int env_footprint(const DevEnv& e, const V3& local, u
     return 4;
 }
 
+// One vector atomic per texel of the bilinear footprint (16-byte aligned
+// float4 accumulators instead of three scalar atomics on the caller's rgb).
 __device__ __forceinline__ void add_env_grad(const AdjView& a, const DevEnv& e, const V3& local, const V3& coef) {
-    if (!a.dEnv || (coef.x == 0.0f && coef.y == 0.0f && coef.z == 0.0f)) return;
+    if (!a.dEnv4 || (coef.x == 0.0f && coef.y == 0.0f && coef.z == 0.0f)) return;
     uint32_t idx[4];
     float w[4];
     const int n = env_footprint(e, local, idx, w);
     for (int k = 0; k < n; ++k) {
         if (w[k] == 0.0f) continue;
-        atomicAdd(&a.dEnv[3 * static_cast<size_t>(idx[k])], coef.x * w[k]);
-        atomicAdd(&a.dEnv[3 * static_cast<size_t>(idx[k]) + 1], coef.y * w[k]);
-        atomicAdd(&a.dEnv[3 * static_cast<size_t>(idx[k]) + 2], coef.z * w[k]);
+        atomicAdd(&a.dEnv4[idx[k]], make_float4(coef.x * w[k], coef.y * w[k], coef.z * w[k], 0.0f));
     }
 }
 
 // dL/dparams of material `mat` += sum_c coef_c * df_c (df from the duals).
-__device__ __forceinline__ void add_mat_grad(const AdjView& a, float* smem, uint32_t mat, const DV3& f, const V3& coef) {
+// A full warp on one material (the common case: a warp holds consecutive
+// samples of one pixel) sums its lanes first and adds once; otherwise each
+// lane adds its own.
+__device__ __forceinline__ void add_mat_grad(const AdjView& a, uint32_t mat, const DV3& f, const V3& coef) {
     if (mat >= a.materialCount) return;
     float g[kDualN];
 #pragma unroll
     for (int p = 0; p < kDualN; ++p) g[p] = coef.x * f.x.d[p] + coef.y * f.y.d[p] + coef.z * f.z.d[p];
-    if (a.useShared) {
-        float* m = smem + 5 * mat;
+    const uint32_t active = __activemask();
+    if (__match_any_sync(active, mat) == 0xffffffffu) {
 #pragma unroll
         for (int p = 0; p < kDualN; ++p)
-            if (g[p] != 0.0f) atomicAdd(&m[p], g[p]);
-    } else {
-        if (a.dBase) {
-            for (int c = 0; c < 3; ++c)
-                if (g[c] != 0.0f) atomicAdd(&a.dBase[3 * mat + c], g[c]);
-        }
-        if (a.dRough && g[kDRough] != 0.0f) atomicAdd(&a.dRough[mat], g[kDRough]);
-        if (a.dMetal && g[kDMetal] != 0.0f) atomicAdd(&a.dMetal[mat], g[kDMetal]);
+            for (int o = 16; o > 0; o >>= 1) g[p] += __shfl_xor_sync(0xffffffffu, g[p], o);
+        if ((threadIdx.x & 31u) != 0u) return;
     }
+    if (a.dBase) {
+        for (int c = 0; c < 3; ++c)
+            if (g[c] != 0.0f) atomicAdd(&a.dBase[3 * mat + c], g[c]);
+    }
+    if (a.dRough && g[kDRough] != 0.0f) atomicAdd(&a.dRough[mat], g[kDRough]);
+    if (a.dMetal && g[kDMetal] != 0.0f) atomicAdd(&a.dMetal[mat], g[kDMetal]);
 }
 
 __device__ __forceinline__ float clamp_scale(const DevRequest& q, const V3& v, float mx) {
@@ -155,10 +157,12 @@ __device__ __forceinline__ V3 env_radiance_eval(const DevScene& s, const AdjView
 // One path of the estimator with sampling from the scene and values from
 // (a.evalMats, a.evalEnv).  kGrad = false returns the radiance; kGrad = true
 // replays it and accumulates the gradients of delta . radiance, given the
-// path's total radiance Ltot.
-template <bool kGrad>
-__device__ V3 adj_path(const DevScene& s, const DevRequest& q, const AdjView& a, float* smem, uint32_t x, uint32_t y,
-                       uint32_t sampleIndex, const V3& delta, const V3& Ltot, float* depthOut) {
+// path's total radiance Ltot.  One out-of-line body serves both passes (the
+// flag is a run-time argument): two inlined copies of the whole estimator
+// overflowed the instruction cache.
+__device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, const AdjView& a, uint32_t x, uint32_t y,
+                                    uint32_t sampleIndex, const V3 delta, const V3 Ltot, float* depthOut,
+                                    const bool kGrad) {
     NullCounter ctr;
     const Sampler smp{x, y, sampleIndex};
     PathState ps;
@@ -246,7 +250,7 @@ __device__ V3 adj_path(const DevScene& s, const DevRequest& q, const AdjView& a,
             if (kGrad) {
                 const float sc = clamp_scale(q, raw, kDirectSampleClamp);
                 const DV3 fd = bsdf_eval_d(me, v.n, v.cn, v.view, ld);
-                add_mat_grad(a, smem, v.hit.material, fd, dT * L * (w * sc));
+                add_mat_grad(a, v.hit.material, fd, dT * L * (w * sc));
                 if (envIdx >= 0 && envIdx == a.env0) add_env_grad(a, a.evalEnv, local, dT * f * domeRad * (w * sc));
             }
             return true;
@@ -312,7 +316,7 @@ __device__ V3 adj_path(const DevScene& s, const DevRequest& q, const AdjView& a,
             const DV3 fd = bsdf_eval_d(me, v.n, v.cn, v.view, next);
             const V3 coef{f.x > 0.0f ? delta.x * Lrem.x / f.x : 0.0f, f.y > 0.0f ? delta.y * Lrem.y / f.y : 0.0f,
                           f.z > 0.0f ? delta.z * Lrem.z / f.z : 0.0f};
-            add_mat_grad(a, smem, v.hit.material, fd, coef);
+            add_mat_grad(a, v.hit.material, fd, coef);
         }
         (void)prevDir;
         if (!alive) break;
@@ -321,13 +325,14 @@ __device__ V3 adj_path(const DevScene& s, const DevRequest& q, const AdjView& a,
     return ps.radiance;
 }
 
-__global__ void __launch_bounds__(128) k_adjoint(const DevScene s, const DevRequest q, const AdjView a, uint64_t pathBase,
-                                                 uint32_t count) {
-    extern __shared__ float smem[];
-    if (a.useShared) {
-        for (uint32_t i = threadIdx.x; i < 5 * a.materialCount; i += blockDim.x) smem[i] = 0.0f;
-        __syncthreads();
-    }
+// The gradient pass.  Each path's total radiance comes from the plain
+// megakernel's path record of the same path (same estimator, same sample),
+// rendered just before into `records`, so only the replay that accumulates
+// gradients runs here.  (4 blocks per SM: 128 registers measured faster than
+// the 168 the compiler otherwise takes.)
+__global__ void __launch_bounds__(128, 4) k_adjoint(const __grid_constant__ DevScene s, const __grid_constant__ DevRequest q,
+                                                    const __grid_constant__ AdjView a, uint64_t pathBase, uint32_t count,
+                                                    const float4* __restrict__ records) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < count) {
         const uint64_t path = pathBase + i;
@@ -339,29 +344,25 @@ __global__ void __launch_bounds__(128) k_adjoint(const DevScene s, const DevRequ
         const float4 g = reinterpret_cast<const float4*>(a.dBeauty)[pixel];
         const V3 delta{g.x / cnt, g.y / cnt, g.z / cnt};
         if (delta.x != 0.0f || delta.y != 0.0f || delta.z != 0.0f) {
-            const V3 L = adj_path<false>(s, q, a, smem, x, y, q.sampleStart + smp, delta, V3{0, 0, 0}, nullptr);
-            adj_path<true>(s, q, a, smem, x, y, q.sampleStart + smp, delta, L, nullptr);
-        }
-    }
-    if (a.useShared) {
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < 5 * a.materialCount; k += blockDim.x) {
-            const float v = smem[k];
-            if (v == 0.0f) continue;
-            const uint32_t mat = k / 5, p = k - mat * 5;
-            if (p < 3) {
-                if (a.dBase) atomicAdd(&a.dBase[3 * mat + p], v);
-            } else if (p == 3) {
-                if (a.dRough) atomicAdd(&a.dRough[mat], v);
-            } else if (a.dMetal) {
-                atomicAdd(&a.dMetal[mat], v);
-            }
+            const float4 r = records[3 * static_cast<size_t>(i)];
+            adj_path(s, q, a, x, y, q.sampleStart + smp, delta, V3{r.x, r.y, r.z}, nullptr, true);
         }
     }
 }
 
+// Adds the float4 texel accumulators into the caller's rgb gradient.
+__global__ void k_env_grad_out(const float4* __restrict__ acc, float* __restrict__ dEnv, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 g = acc[i];
+    dEnv[3 * static_cast<size_t>(i)] += g.x;
+    dEnv[3 * static_cast<size_t>(i) + 1] += g.y;
+    dEnv[3 * static_cast<size_t>(i) + 2] += g.z;
+}
+
 // Frozen-sampling forward: radiance + first-hit depth per path as a record.
-__global__ void __launch_bounds__(128) k_frozen(const DevScene s, const DevRequest q, const AdjView a, uint64_t pathBase,
+__global__ void __launch_bounds__(128) k_frozen(const __grid_constant__ DevScene s, const __grid_constant__ DevRequest q,
+                                                const __grid_constant__ AdjView a, uint64_t pathBase,
                                                 uint32_t count, float4* __restrict__ records) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
@@ -371,7 +372,7 @@ __global__ void __launch_bounds__(128) k_frozen(const DevScene s, const DevReque
     const uint32_t y = static_cast<uint32_t>(pixel / q.width);
     const uint32_t x = static_cast<uint32_t>(pixel - static_cast<uint64_t>(y) * q.width);
     float depth0;
-    const V3 L = adj_path<false>(s, q, a, nullptr, x, y, q.sampleStart + smp, V3{0, 0, 0}, V3{0, 0, 0}, &depth0);
+    const V3 L = adj_path(s, q, a, x, y, q.sampleStart + smp, V3{0, 0, 0}, V3{0, 0, 0}, &depth0, false);
     float4* o = records + 3 * static_cast<size_t>(i);
     o[0] = make_float4(L.x, L.y, L.z, depth0);
     o[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -401,7 +402,7 @@ inline unsigned grid(uint64_t n, unsigned b) { return static_cast<unsigned>((n +
 }  // namespace
 
 struct AdjointState {
-    DeviceBlock evalMats, evalTexels;
+    DeviceBlock evalMats, evalTexels, envGrad;
 };
 
 namespace {
@@ -461,11 +462,20 @@ int adjoint_run(ContextImpl* ctx, const ShiroRenderDesc* req, const float* dBeau
     a.dBase = dBase;
     a.dRough = dRough;
     a.dMetal = dMetal;
-    a.dEnv = a.env0 >= 0 ? dEnv : nullptr;
-    const size_t shared = 5ull * a.materialCount * sizeof(float);
-    a.useShared = (shared > 0 && shared <= 32 * 1024) ? 1u : 0u;
+    const uint32_t texels = a.env0 >= 0 ? a.evalEnv.w * a.evalEnv.h : 0u;
+    if (dEnv && texels) {
+        AdjointState* st = adj_state(ctx);
+        if (!ensure_block(ctx, &st->envGrad, texels * sizeof(float4), "environment gradient")) return SHIRO_ERR_OUT_OF_MEMORY;
+        const cudaError_t e = cudaMemsetAsync(st->envGrad.ptr, 0, texels * sizeof(float4), ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "environment gradient");
+        a.dEnv4 = static_cast<float4*>(st->envGrad.ptr);
+    }
     const uint64_t total = static_cast<uint64_t>(q.width) * q.height * q.sampleCount;
     const uint64_t chunk = 1ull << 24;
+    if (!ensure_block(ctx, &ctx->pathRecords, std::min(chunk, std::max<uint64_t>(total, 1)) * kPathRecordBytes,
+                      "path records"))
+        return SHIRO_ERR_OUT_OF_MEMORY;
+    float4* rec = static_cast<float4*>(ctx->pathRecords.ptr);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -473,14 +483,19 @@ int adjoint_run(ContextImpl* ctx, const ShiroRenderDesc* req, const float* dBeau
     uint64_t launches = 0;
     for (uint64_t p0 = 0; p0 < total; p0 += chunk) {
         const uint32_t n = static_cast<uint32_t>(std::min(chunk, total - p0));
-        k_adjoint<<<grid(n, 128), 128, a.useShared ? shared : 0, ctx->stream>>>(ctx->scene, q, a, p0, n);
-        ++launches;
+        launch_plain_paths(ctx->scene, q, p0, n, rec, ctx->stream);  // the paths' radiance
+        k_adjoint<<<grid(n, 128), 128, 0, ctx->stream>>>(ctx->scene, q, a, p0, n, rec);
+        launches += 2;
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             return cuda_fail(ctx, e, "adjoint launch");
         }
+    }
+    if (a.dEnv4) {
+        k_env_grad_out<<<grid(texels, 256), 256, 0, ctx->stream>>>(a.dEnv4, dEnv, texels);
+        ++launches;
     }
     cudaEventRecord(e1, ctx->stream);
     cudaError_t e = cudaEventSynchronize(e1);
@@ -499,7 +514,7 @@ int adjoint_run(ContextImpl* ctx, const ShiroRenderDesc* req, const float* dBeau
 
 void adjoint_free(ContextImpl* ctx) {
     if (!ctx->adjoint) return;
-    for (DeviceBlock* b : {&ctx->adjoint->evalMats, &ctx->adjoint->evalTexels})
+    for (DeviceBlock* b : {&ctx->adjoint->evalMats, &ctx->adjoint->evalTexels, &ctx->adjoint->envGrad})
         if (b->ptr) cudaFree(b->ptr);
     delete ctx->adjoint;
     ctx->adjoint = nullptr;

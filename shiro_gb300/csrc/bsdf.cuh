@@ -311,13 +311,14 @@ static __device__ __noinline__ V3 bsdf_eval_rec(const float4* r, const Mat& m, c
 
 // The same from the material alone (record formed on the spot): the
 // differentiable form, whose evaluation materials have no stored record.
-__device__ __forceinline__ float bsdf_pdf(const Mat& m, const LobeWeights& w, const V3& n, const V3& cn, const V3& v,
-                                          const V3& l) {
+// (Out of line: the differentiable form calls them from many sites.)
+static __device__ __noinline__ float bsdf_pdf(const Mat& m, const LobeWeights w, const V3 n, const V3 cn, const V3 v,
+                                              const V3 l) {
     float4 r[kBsdfRec];
     make_bsdf_rec(m, r);
     return bsdf_pdf_rec(r, m, w, n, cn, v, l);
 }
-__device__ __forceinline__ V3 bsdf_eval(const Mat& m, const V3& n, const V3& cn, const V3& v, const V3& l) {
+static __device__ __noinline__ V3 bsdf_eval(const Mat& m, const V3 n, const V3 cn, const V3 v, const V3 l) {
     float4 r[kBsdfRec];
     make_bsdf_rec(m, r);
     return bsdf_eval_rec(r, m, n, cn, v, l);
