@@ -68,6 +68,9 @@ def parse():
     p.add_argument("--no-rmse", action="store_true", help="skip the equal-RMSE check against a converged image")
     p.add_argument("--no-batch", action="store_true", help="skip the 48-request batch measurement")
     p.add_argument("--no-autotune", action="store_true", help="keep the current wavefront configuration")
+    p.add_argument("--wf-config", default="",
+                   help="wavefront configuration to set before measuring (with --no-autotune: the one measured), "
+                        "e.g. paths_in_flight=33554432,concurrent_waves=2")
     return p.parse_args()
 
 
@@ -486,6 +489,8 @@ def main():
 
     tuned = None
     if "wavefront" in forms:
+        if args.wf_config:
+            gpu.set_wavefront_config(**{k: int(v) for k, v in (kv.split("=") for kv in args.wf_config.split(","))})
         tuned = gpu.wavefront_config() if args.no_autotune else gpu.autotune(w.scene, w.camera, st)
 
     def timed(form):
