@@ -337,6 +337,12 @@ int shiro_gpu_render_frozen(ShiroGpuContext* ctx, const ShiroRenderDesc* request
  * Primary closest hit of every pixel's camera ray for sample sample_start:
  * prim_out[i] = global triangle index (meshes in order, triangles in order)
  * or 0xffffffff on a miss; t_out[i] = hit distance. */
+/* OpenQmcSampler::Next2D (OpenQmcSampler.cpp:110-135; fallback sequence
+ * :56-71) on the device for n host tuples (px, py, sample index, branch):
+ * out2 receives 2 floats per tuple.  Diagnostic: the sampler the kernels use,
+ * for bit-exact checks against the reference's values. */
+int shiro_gpu_sample(ShiroGpuContext* ctx, const uint32_t* px, const uint32_t* py, const uint32_t* index,
+                     const uint32_t* branch, uint32_t n, float* out2);
 int shiro_gpu_primary_hits(ShiroGpuContext* ctx, const ShiroRenderDesc* request, uint32_t* prim_out,
                            float* t_out, uint32_t on_device);
 /* Closest hit / occlusion for arbitrary rays: origins, directions [n*3];

@@ -69,6 +69,7 @@ def load_library(path: str = LIB_PATH):
         "shiro_gpu_set_params": ([_P, _P, _P, _P, _P], C.c_int),
         "shiro_gpu_adjoint": ([_P, _P, _P, _P, _P, _P, _P], C.c_int),
         "shiro_gpu_primary_hits": ([_P, _P, _P, _P, _U], C.c_int),
+        "shiro_gpu_sample": ([_P, _P, _P, _P, _P, _U, _P], C.c_int),
         "shiro_gpu_trace_rays": ([_P, _P, _P, _P, _U, _P, _P, _P], C.c_int),
         "shiro_gpu_last_stats": ([_P, _P], C.c_int),
         "shiro_gpu_count_work": ([_P, _P, _U, _P], C.c_int),
@@ -256,6 +257,15 @@ class GpuBackend:
         return self.wavefront_config()
 
     # -- probes --------------------------------------------------------------
+    def sample(self, px, py, index, branch) -> np.ndarray:
+        """OpenQmcSampler::Next2D of the device sampler for each tuple: (n, 2)."""
+        px, py, index, branch = (np.ascontiguousarray(a, np.uint32) for a in (px, py, index, branch))
+        out = np.zeros((px.size, 2), np.float32)
+        rc = self.lib.shiro_gpu_sample(self._ctx, _ptr(px), _ptr(py), _ptr(index), _ptr(branch), px.size, _ptr(out))
+        if rc != 0:
+            raise self._err(rc)
+        return out
+
     def primary_hits(self, scene: Scene, camera: Camera, settings: RenderSettings, sample_start: int = 0):
         self.upload_scene(scene)
         req = render_desc(camera, settings, sample_start, 1)

@@ -27,6 +27,9 @@ void launch_plain_paths(const DevScene& s, const DevRequest& q, uint64_t pathBas
 // (CpuPathTracer.cpp:2093-2137).
 void launch_resolve_pixels(const DevRequest& q, uint64_t pixelBase, uint32_t count, const float4* records, AovPtrs aov,
                            cudaStream_t stream);
+// out[2k], out[2k+1] = Sampler{px, py, index}.next2d(branch) of tuple k
+// (tuples packed as uint4 px, py, index, branch).
+void launch_sample_probe(const uint4* tuples, uint32_t n, float* out, cudaStream_t stream);
 void launch_primary_hits(const DevScene& s, const DevRequest& q, uint32_t* prim, float* t, cudaStream_t stream);
 // Work counts of every stride-th path (12 totals, see ShiroWorkCounts).
 void launch_count_paths(const DevScene& s, const DevRequest& q, uint32_t stride, unsigned long long* totals,

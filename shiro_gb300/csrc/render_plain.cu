@@ -123,9 +123,24 @@ __global__ void __launch_bounds__(128) k_count_paths(const DevScene s, const Dev
     }
 }
 
+// The sampler of the kernels on explicit tuples (diagnostic).
+__global__ void k_sample_probe(const uint4* __restrict__ tuples, uint32_t n, float* __restrict__ out) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint4 t = tuples[k];
+    const V2 v = Sampler{t.x, t.y, t.z}.next2d(t.w);
+    out[2 * static_cast<size_t>(k)] = v.x;
+    out[2 * static_cast<size_t>(k) + 1] = v.y;
+}
+
 inline unsigned grid(uint64_t n, unsigned b) { return static_cast<unsigned>((n + b - 1) / b); }
 
 }  // namespace
+
+void launch_sample_probe(const uint4* tuples, uint32_t n, float* out, cudaStream_t stream) {
+    if (n == 0) return;
+    k_sample_probe<<<grid(n, 256), 256, 0, stream>>>(tuples, n, out);
+}
 
 void launch_plain_paths(const DevScene& s, const DevRequest& q, uint64_t pathBase, uint32_t count, float4* records,
                         cudaStream_t stream) {

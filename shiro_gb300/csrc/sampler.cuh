@@ -24,48 +24,50 @@ __device__ __forceinline__ uint32_t qmc_scramble(uint32_t s) {  // MixBits, :30-
     return s;
 }
 
-// Radical inverse with a compile-time base (division by a constant).
-template <uint32_t B>
-__device__ __forceinline__ float qmc_radical(uint32_t i) {  // RadicalInverse, :43-54
-    const float invBase = 1.0f / static_cast<float>(B);
+// RadicalInverse (:43-54) in base prime[dim mod 24]: digits d = i mod B
+// summed as acc += float(d) * scale, scale *= 1 / B, in the reference's
+// order.  One loop for every base: the quotient i / B comes from a
+// multiply-high by a per-base constant (Granlund & Montgomery 1994, unsigned
+// division by invariant integers, Fig. 4.1: m = floor(2^32 (2^l - B) / B) + 1,
+// l = ceil(log2 B); q = (t + ((i - t) >> 1)) >> (l - 1), t = mulhi(m, i)),
+// exact for every 32-bit i; 1 / B is the IEEE float quotient the reference
+// forms.  (One small body instead of 24 specialised loops behind a jump
+// table keeps the samplers' code compact in the instruction cache.)
+static __constant__ uint32_t kQmcPrime[24] = {
+    2u, 3u, 5u, 7u, 11u, 13u, 17u, 19u, 23u, 29u, 31u, 37u,
+    41u, 43u, 47u, 53u, 59u, 61u, 67u, 71u, 73u, 79u, 83u, 89u,
+};
+static __constant__ uint32_t kQmcMagic[24] = {
+    0x00000001u, 0x55555556u, 0x9999999au, 0x24924925u, 0x745d1746u, 0x3b13b13cu,
+    0xe1e1e1e2u, 0xaf286bcbu, 0x642c8591u, 0x1a7b9612u, 0x08421085u, 0xbacf914du,
+    0x8f9c18fau, 0x7d05f418u, 0x5c9882bau, 0x3521cfb3u, 0x15b1e5f8u, 0x0c9714fcu,
+    0xe9131ac0u, 0xcd856891u, 0xc0e07039u, 0x9ec8e952u, 0x8acb90f7u, 0x702e05c1u,
+};
+static __constant__ uint32_t kQmcShift[24] = {
+    0u, 1u, 2u, 2u, 3u, 3u, 4u, 4u, 4u, 4u, 4u, 5u,
+    5u, 5u, 5u, 5u, 5u, 5u, 6u, 6u, 6u, 6u, 6u, 6u,
+};
+static __constant__ uint32_t kQmcInvBase[24] = {  // float bits of 1.0f / prime
+    0x3f000000u, 0x3eaaaaabu, 0x3e4ccccdu, 0x3e124925u, 0x3dba2e8cu, 0x3d9d89d9u,
+    0x3d70f0f1u, 0x3d579436u, 0x3d321643u, 0x3d0d3dcbu, 0x3d042108u, 0x3cdd67c9u,
+    0x3cc7ce0cu, 0x3cbe82fau, 0x3cae4c41u, 0x3c9a90e8u, 0x3c8ad8f3u, 0x3c864b8au,
+    0x3c74898du, 0x3c66c2b4u, 0x3c607038u, 0x3c4f6475u, 0x3c4565c8u, 0x3c381703u,
+};
+
+static __device__ __noinline__ float qmc_radical_dim(uint32_t dim, uint32_t i) {
+    const uint32_t k = dim % 24u;
+    const uint32_t base = kQmcPrime[k], magic = kQmcMagic[k], shift = kQmcShift[k];
+    const float invBase = __uint_as_float(kQmcInvBase[k]);
     float scale = invBase;
     float acc = 0.0f;
     while (i > 0u) {
-        const uint32_t q = i / B;
-        acc += static_cast<float>(i - q * B) * scale;
+        const uint32_t t = __umulhi(magic, i);
+        const uint32_t q = (t + ((i - t) >> 1)) >> shift;
+        acc += static_cast<float>(i - q * base) * scale;
         i = q;
         scale *= invBase;
     }
     return acc;
-}
-
-static __device__ __noinline__ float qmc_radical_dim(uint32_t dim, uint32_t i) {
-    switch (dim % 24u) {
-        case 0: return qmc_radical<2>(i);
-        case 1: return qmc_radical<3>(i);
-        case 2: return qmc_radical<5>(i);
-        case 3: return qmc_radical<7>(i);
-        case 4: return qmc_radical<11>(i);
-        case 5: return qmc_radical<13>(i);
-        case 6: return qmc_radical<17>(i);
-        case 7: return qmc_radical<19>(i);
-        case 8: return qmc_radical<23>(i);
-        case 9: return qmc_radical<29>(i);
-        case 10: return qmc_radical<31>(i);
-        case 11: return qmc_radical<37>(i);
-        case 12: return qmc_radical<41>(i);
-        case 13: return qmc_radical<43>(i);
-        case 14: return qmc_radical<47>(i);
-        case 15: return qmc_radical<53>(i);
-        case 16: return qmc_radical<59>(i);
-        case 17: return qmc_radical<61>(i);
-        case 18: return qmc_radical<67>(i);
-        case 19: return qmc_radical<71>(i);
-        case 20: return qmc_radical<73>(i);
-        case 21: return qmc_radical<79>(i);
-        case 22: return qmc_radical<83>(i);
-        default: return qmc_radical<89>(i);
-    }
 }
 
 __device__ __forceinline__ float qmc_dim(uint32_t px, uint32_t py, uint32_t index, uint32_t dim) {  // :56-71

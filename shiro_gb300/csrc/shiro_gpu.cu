@@ -1011,6 +1011,27 @@ int shiro_gpu_render_frozen(ShiroGpuContext* ctx, const ShiroRenderDesc* req, co
     return adjoint_render_frozen(&ctx->impl, req, base, rough, metal, env, beauty);
 }
 
+int shiro_gpu_sample(ShiroGpuContext* handle, const uint32_t* px, const uint32_t* py, const uint32_t* index,
+                     const uint32_t* branch, uint32_t n, float* out2) {
+    if (!handle || (n && (!px || !py || !index || !branch || !out2))) return SHIRO_ERR_INVALID_ARGUMENT;
+    ContextImpl* ctx = &handle->impl;
+    cudaSetDevice(ctx->device);
+    if (n == 0) return SHIRO_OK;
+    std::vector<uint4> tuples(n);
+    for (uint32_t k = 0; k < n; ++k) tuples[k] = make_uint4(px[k], py[k], index[k], branch[k]);
+    if (!ensure_block(ctx, &ctx->probeScratch, static_cast<size_t>(n) * (sizeof(uint4) + 2 * sizeof(float)), "probe"))
+        return SHIRO_ERR_OUT_OF_MEMORY;
+    uint4* dt = static_cast<uint4*>(ctx->probeScratch.ptr);
+    float* dout = reinterpret_cast<float*>(dt + n);
+    cudaError_t e = cudaMemcpyAsync(dt, tuples.data(), n * sizeof(uint4), cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "sample probe upload");
+    launch_sample_probe(dt, n, dout, ctx->stream);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out2, dout, n * 2 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? SHIRO_OK : cuda_fail(ctx, e, "sample probe");
+}
+
 int shiro_gpu_primary_hits(ShiroGpuContext* handle, const ShiroRenderDesc* req, uint32_t* prim, float* t, uint32_t on_device) {
     if (!handle || !req || !prim || !t) return SHIRO_ERR_INVALID_ARGUMENT;
     ContextImpl* ctx = &handle->impl;

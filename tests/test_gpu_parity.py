@@ -91,6 +91,14 @@ def test_field_rays_vs_bruteforce(gpu, port):
     assert np.array_equal(occ, bo)
 
 
+def test_sampler_kat_bit_exact(gpu):
+    """The device sampler on the 64 000 reference tuples (pixels, sample
+    indices up to 2^32 - 1, branches over every prime base): bit for bit."""
+    g = golden("sampler_kat.npz")
+    out = gpu.sample(g["px"], g["py"], g["index"], g["branch"])
+    assert (out.view(np.uint32) == g["out"].view(np.uint32)).all()
+
+
 # progressive_batch3: the third consecutive batch of one reference tracer,
 # matched by a single render of that batch (the reference's path guide,
 # CpuPathTracer.cpp:1953-1987, never becomes active: its weights start at zero
