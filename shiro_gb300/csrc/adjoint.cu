@@ -198,6 +198,12 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
         const Vertex v = make_vertex(s, ps.ro, ps.rd, h);
         const Mat& me = a.evalMats[v.hit.material];
         const Mat& ms = s.materials[v.hit.material];
+        // the scene's materials have their BSDF records on the device; values
+        // from a second parameter set (frozen renders) build theirs per call
+        const float4* rec = bsdf_rec(s, v.hit.material);
+        auto evalE = [&](const V3& l) {
+            return a.distinctEval ? bsdf_eval(me, v.n, v.cn, v.view, l) : bsdf_eval_rec(rec, ms, v.n, v.cn, v.view, l);
+        };
         if (depth == 0) depth0 = h.t;
         const V3 origin = shadow_origin(v);
         // light samples, in sum_direct's order
@@ -239,12 +245,12 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
                 ld = light_to_world(d, local);
                 const float nl = sclamp(dot(v.n, ld), 0.0f, 1.0f);
                 if (nl <= 0.0f) return false;
-                const float bp = bsdf_pdf(ms, v.w, v.n, v.cn, v.view, ld);
+                const float bp = bsdf_pdf_rec(rec, ms, v.w, v.n, v.cn, v.view, ld);
                 const float mis = power_heuristic(lp, bp);
                 w = nl * mis / lp;
             }
             if (trace_occluded(s, origin, ld, FLT_MAX, ctr)) return false;
-            const V3 f = bsdf_eval(me, v.n, v.cn, v.view, ld);
+            const V3 f = evalE(ld);
             const V3 raw = f * L * w;
             *c = clamp24(q, raw);
             if (kGrad) {
@@ -274,7 +280,7 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
             next = cosine_hemisphere(v.n, ds);
             const float cpdf = sclamp(dot(v.n, next), 0.0f, 1.0f) * kInvPi;
             pdf = smax((rw / tw) * (1.0f * cpdf + 0.0f * 0.0f), 1.0e-6f);
-            f = bsdf_eval(me, v.n, v.cn, v.view, next);
+            f = evalE(next);
         } else {
             const bool coat = !(rs < v.w.diffuse + v.w.spec);
             if (ps.specDepth >= q.specularDepth) break;
@@ -286,13 +292,13 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
             next = normalize(reflect(ps.rd, hv));
             const float rc = sclamp(dot(sn, next), 0.0f, 1.0f);
             if (rc <= 0.0f) break;
-            pdf = smax((rw / tw) * bsdf_pdf(ms, v.w, v.n, v.cn, v.view, next), 1.0e-6f);
-            f = bsdf_eval(me, v.n, v.cn, v.view, next);
+            pdf = smax((rw / tw) * bsdf_pdf_rec(rec, ms, v.w, v.n, v.cn, v.view, next), 1.0e-6f);
+            f = evalE(next);
             delta2 = sr <= kDeltaRoughness;
         }
         const float cosT = sclamp(dot(v.n, next), 0.0f, 1.0f);
         if (cosT <= 0.0f) break;
-        if (a.distinctEval) Ts = clamp12(q, Ts * bsdf_eval(ms, v.n, v.cn, v.view, next) * (cosT / pdf));
+        if (a.distinctEval) Ts = clamp12(q, Ts * bsdf_eval_rec(rec, ms, v.n, v.cn, v.view, next) * (cosT / pdf));
         ps.T = clamp12(q, ps.T * f * (cosT / pdf));
         if (!a.distinctEval) Ts = ps.T;
         const float off = dot(v.n, next) >= 0.0f ? 1.0f : -1.0f;
