@@ -194,10 +194,12 @@ class GpuBackend:
 
     def render_sample_batch(self, request: RenderRequest) -> FrameBuffer:
         """RenderBackend::RenderSampleBatch with the reference's error
-        convention (cleared FrameBuffer + stderr message on failure)."""
+        convention (cleared FrameBuffer + stderr message on failure), on the
+        wavefront form (frames bit-identical to ``render``'s)."""
         try:
-            return self.render(request.scene, request.camera, request.settings, request.sample_start,
-                               request.sample_count, request.flags, request.cancel)
+            (fb,) = self.render_batch(request.scene, [(request.camera, request.settings, request.sample_start,
+                                                       request.sample_count)], request.flags, request.cancel)
+            return fb
         except ShiroGpuError as e:
             sys.stderr.write(f"shiro gb300 backend: {e}\n")
             return FrameBuffer(request.settings.width, request.settings.height)

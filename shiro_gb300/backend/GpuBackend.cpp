@@ -253,7 +253,9 @@ render::FrameBuffer GpuBackend::RenderSampleBatch(const RenderRequest& request) 
     const ShiroRenderDesc desc = ToRequest(request);
     Planes planes(static_cast<size_t>(request.settings.width) * request.settings.height);
     ShiroAovs aovs = planes.Aovs();
-    const int rc = shiro_gpu_render(ctx_, &desc, nullptr, &aovs);
+    // the wavefront form: the faster one, with frames bit-identical to the
+    // one-thread-per-path form's
+    const int rc = shiro_gpu_render_batch(ctx_, &desc, 1, nullptr, &aovs);
     if (rc != SHIRO_OK) {
         std::fprintf(stderr, "[shiro gb300] render failed (%d): %s\n", rc, shiro_gpu_last_error(ctx_));
         return frame;

@@ -585,7 +585,7 @@ WavefrontState* wf_state(ContextImpl* ctx) {
     if (!ctx->wavefront) {
         ctx->wavefront = new WavefrontState();
         ShiroWavefrontConfig& c = ctx->wavefront->cfg;
-        c.paths_in_flight = 1u << 22;
+        c.paths_in_flight = 1u << 23;
         c.extend_block = 128;
         c.shade_block = 128;
         c.shadow_block = 128;
@@ -593,7 +593,7 @@ WavefrontState* wf_state(ContextImpl* ctx) {
         c.shade_regs = 128;
         c.extend_steps = 4;
         c.refill_idle = 8;
-        c.concurrent_waves = 1;
+        c.concurrent_waves = 2;
         cudaDeviceGetAttribute(&ctx->wavefront->smCount, cudaDevAttrMultiProcessorCount, ctx->device);
     }
     return ctx->wavefront;

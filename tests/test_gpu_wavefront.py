@@ -127,7 +127,8 @@ def test_two_waves_in_flight_uneven_batch(gpu, pool):
 
 @pytest.mark.parametrize("knobs", [dict(shade_regs=96), dict(extend_steps=1, refill_idle=1),
                                    dict(extend_steps=32, refill_idle=32), dict(extend_steps=3, refill_idle=5),
-                                   dict(concurrent_waves=2, paths_in_flight=2048)])
+                                   dict(concurrent_waves=2, paths_in_flight=2048),
+                                   dict(concurrent_waves=1, paths_in_flight=2048)])
 def test_tuning_knobs_keep_frames_identical(gpu, knobs):
     """Register cap of the shade stage and the lane-refill parameters of the
     wide-BVH extend stage change scheduling only."""
