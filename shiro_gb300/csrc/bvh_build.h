@@ -56,7 +56,7 @@ inline int leaf_link_host(int first, int count) { return ~((first << 3) | (count
 // roughly front to back without sorting.
 constexpr uint32_t kWideEmptyMeta = 0xffu;
 constexpr uint32_t kWideMaxTris = 32;  // triangle bits of one node
-constexpr uint32_t kWideLeaf = 3;      // SAH leaf size of the binary tree the wide BVH is collapsed from
+constexpr uint32_t kWideLeaf = 1;      // leaf size of the binary tree the wide BVH is collapsed from
 
 struct WideOutput {
     float4* nodes = nullptr;  // cudaMalloc'ed, 5 float4 per node
