@@ -309,15 +309,10 @@ static __device__ __noinline__ V3 bsdf_eval_rec(const float4* r, const Mat& m, c
     return diffuse + spec + coat + sheen;
 }
 
-// The same from the material alone (record formed on the spot): the
-// differentiable form, whose evaluation materials have no stored record.
-// (Out of line: the differentiable form calls them from many sites.)
-static __device__ __noinline__ float bsdf_pdf(const Mat& m, const LobeWeights w, const V3 n, const V3 cn, const V3 v,
-                                              const V3 l) {
-    float4 r[kBsdfRec];
-    make_bsdf_rec(m, r);
-    return bsdf_pdf_rec(r, m, w, n, cn, v, l);
-}
+// The BSDF value from the material alone (record formed per call): for
+// materials that have no stored record, i.e. the second parameter set of a
+// frozen render of the differentiable form.  Out of line, so the record code
+// exists once.
 static __device__ __noinline__ V3 bsdf_eval(const Mat& m, const V3 n, const V3 cn, const V3 v, const V3 l) {
     float4 r[kBsdfRec];
     make_bsdf_rec(m, r);
