@@ -68,6 +68,8 @@ def parse():
     p.add_argument("--no-rmse", action="store_true", help="skip the equal-RMSE check against a converged image")
     p.add_argument("--no-batch", action="store_true", help="skip the 48-request batch measurement")
     p.add_argument("--no-autotune", action="store_true", help="keep the current wavefront configuration")
+    p.add_argument("--adjoint-only", type=int, default=0, metavar="SIZE",
+                   help="only the adjoint measurement, on a SIZE x SIZE frame (profiling cases); prints its JSON")
     p.add_argument("--wf-config", default="",
                    help="wavefront configuration to set before measuring (with --no-autotune: the one measured), "
                         "e.g. paths_in_flight=33554432,concurrent_waves=2")
@@ -257,18 +259,19 @@ def cpu_baseline(w, seconds: float, rank: int = 0) -> dict:
             "cpu": cpu, "seconds": t_render, "paths": int(paths)}
 
 
-def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 2) -> dict:
+def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 2, size: int = 512) -> dict:
     """Gradient throughput of the differentiable form on the 256-material
-    sphere scene: 512x512, 32 spp, depth 6, L2 loss against a seeded target,
-    gradients for 256 x (base colour, roughness, metalness) and the 512x256x3
-    environment texels.  One gradient = one forward render + one adjoint pass."""
+    sphere scene: 512x512 (`size` for profiling cases), 32 spp, depth 6, L2
+    loss against a seeded target, gradients for 256 x (base colour, roughness,
+    metalness) and the 512x256x3 environment texels.  One gradient = one
+    forward render + one adjoint pass."""
     import torch
 
     from shiro_gb300 import GpuBackend, scenes
     from shiro_gb300.abi import RenderSettings
 
     scene = scenes.split_sphere_scene(parts=256, env_width=512, env_height=256, seed=4)
-    st = RenderSettings(width=512, height=512, samples_per_pixel=32, max_depth=6, diffuse_depth=6, specular_depth=6,
+    st = RenderSettings(width=size, height=size, samples_per_pixel=32, max_depth=6, diffuse_depth=6, specular_depth=6,
                         backend=1)
     cam = scenes.sphere_camera(1.0)
     gpu = GpuBackend(local)
@@ -280,7 +283,7 @@ def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 
              roughness=torch.tensor([m.roughness for m in scene.materials], dtype=torch.float32, device="cuda"),
              metallic=torch.tensor([m.metallic for m in scene.materials], dtype=torch.float32, device="cuda"),
              env=torch.tensor(scene.dome_lights[0].env, dtype=torch.float32, device="cuda"))
-    target = torch.rand((512, 512, 3), generator=torch.Generator().manual_seed(9)).cuda()
+    target = torch.rand((size, size, 3), generator=torch.Generator().manual_seed(9)).cuda()
     grads = {k: torch.zeros_like(v) for k, v in p.items()}
 
     def step():
@@ -304,9 +307,9 @@ def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / iters
     nparams = sum(v.numel() for v in p.values())
-    paths = 512 * 512 * 32
+    paths = size * size * 32
     gpu.close()
-    return {"workload": "256-material sphere scene, 512x256 env, 512x512, 32 spp, depth 6, L2 loss",
+    return {"workload": f"256-material sphere scene, 512x256 env, {size}x{size}, 32 spp, depth 6, L2 loss",
             "params": int(nparams), "ms_per_gradient": ms, "grads_per_s": 1000.0 / ms,
             "adjoint_ms": adj_ms / iters, "adjoint_Mpaths_s": paths / (adj_ms / iters / 1000.0) / 1e6,
             "param_gradients_per_s": nparams * 1000.0 / ms}
@@ -437,6 +440,12 @@ def main():
         return run_reference(args)
     import torch
 
+    if args.adjoint_only:
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        res = adjoint_bench(int(os.environ.get("LOCAL_RANK", "0")), iters=args.steps, warmup=args.warmup,
+                            bvh_width=args.bvh_width, size=args.adjoint_only)
+        print(json.dumps(res), flush=True)
+        return 0
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
