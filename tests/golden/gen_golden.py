@@ -267,6 +267,29 @@ def render_cases():
                          backend=1)
     cases["transmission"] = (tra, scenes.look_at((0.5, 1.6, 4.5), (0.0, 0.7, 0.0), 50.0, 48 / 40), st8, 0, 4, 0)
 
+    # degenerate geometry: an exact duplicate of the sphere under another
+    # material (every hit ties in t: the first mesh must win), zero-area and
+    # repeated-vertex triangles, vertex normals of zero length (the geometric
+    # normal stands in), a material index out of range (default material),
+    # an empty mesh, and a distant light from below the ground
+    dup = Mesh(spos, sidx, snrm, 1)
+    zpos = np.array([[-1.5, 0.3, 1.0], [-1.0, 0.8, 1.0], [-0.5, 1.3, 1.0],   # collinear
+                     [0.6, 0.2, 1.2], [0.6, 0.2, 1.2], [1.0, 0.9, 1.2],     # repeated vertex
+                     [-0.3, 1.9, 1.5], [0.3, 1.9, 1.5], [0.0, 2.4, 1.5]], np.float32)
+    zidx = np.arange(9, dtype=np.uint32)
+    znrm = np.zeros((9, 3), np.float32)
+    znrm[6:] = [[0.0, 0.0, 1.0], [0.0, 0.0, 0.0], [0.0, 0.0, 1.0]]
+    qpos = np.array([[1.2, 0.0, -0.5], [2.2, 0.0, -0.5], [2.2, 1.0, -0.5], [1.2, 1.0, -0.5]], np.float32)
+    qidx = np.array([0, 1, 2, 0, 2, 3], np.uint32)
+    empty = Mesh(np.zeros((0, 3), np.float32), np.zeros(0, np.uint32), None, 0)
+    deg = Scene(materials=[lambert((0.7, 0.6, 0.5)), lambert((0.1, 0.9, 0.1)), mats["metal"]],
+                meshes=[Mesh(spos, sidx, snrm, 0), dup, Mesh(zpos, zidx, znrm, 2), Mesh(qpos, qidx, None, 99), empty,
+                        Mesh(gpos, gidx, gnrm, 0)],
+                distant_lights=[DistantLight((-0.3, -1.0, -0.2), (2.0, 2.0, 2.0)),
+                                DistantLight((0.0, 1.0, 0.0), (5.0, 5.0, 5.0))],
+                dome_lights=[DomeLight((0.5, 0.5, 0.5), scenes.procedural_hdri(64, 32, seed=8))])
+    cases["degenerate"] = (deg, scenes.look_at((0.5, 1.6, 4.5), (0.0, 0.9, 0.0), 50.0, 1.0), st7, 0, 4, 0)
+
     # third batch of a progressive render: batches of 4 samples at indices
     # 0, 4, 8 on one reference tracer, which keeps its path-guide weights
     # between batches of a scene; the frame is stored as the batch it is

@@ -104,7 +104,7 @@ def test_sampler_kat_bit_exact(gpu):
 # CpuPathTracer.cpp:1953-1987, never becomes active: its weights start at zero
 # and grow only through records pushed while it is active)
 RENDERS = ["sphere", "rich", "features_gradient_env", "angular_env", "field_small", "sphere_1spp_start5", "emissive",
-           "opacity", "transmission", "progressive_batch3"]
+           "opacity", "transmission", "progressive_batch3", "degenerate"]
 
 
 @pytest.mark.parametrize("name", RENDERS)
