@@ -288,8 +288,11 @@ int shiro_gpu_render(ShiroGpuContext* ctx, const ShiroRenderDesc* request,
 int shiro_gpu_render_batch(ShiroGpuContext* ctx, const ShiroRenderDesc* requests, uint32_t count,
                            const volatile int* cancel, ShiroAovs* outs);
 
-/* Wavefront tuning (tile of paths in flight per wave and block sizes). Zero
- * fields leave the current value. The autotuner sets these itself when
+/* Wavefront tuning (tile of paths in flight per wave, waves in flight, block
+ * sizes, register cap, lane refill).  Zero fields leave the current value
+ * (use_graph is always taken).  Defaults: 8 388 608 paths per wave, two waves
+ * in flight, blocks of 128, graphs on, 128 registers, refill every 4 nodes
+ * once 8 lanes are idle.  The autotuner sets these itself when
  * shiro_gpu_autotune is called. */
 typedef struct ShiroWavefrontConfig {
     uint32_t paths_in_flight;
