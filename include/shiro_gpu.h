@@ -284,7 +284,9 @@ int shiro_gpu_render(ShiroGpuContext* ctx, const ShiroRenderDesc* request,
 /* Batched wavefront form: renders `count` requests (each with its own
  * camera, resolution, spp and depth) against the uploaded scene with
  * persistent stage kernels and per-stage queues.  Results equal those of
- * shiro_gpu_render for each request. */
+ * shiro_gpu_render for each request.  cancel (may be NULL) is polled between
+ * waves; a set flag returns SHIRO_ERR_CANCELLED with every request's AOVs
+ * cleared. */
 int shiro_gpu_render_batch(ShiroGpuContext* ctx, const ShiroRenderDesc* requests, uint32_t count,
                            const volatile int* cancel, ShiroAovs* outs);
 

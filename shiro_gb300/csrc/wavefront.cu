@@ -1011,6 +1011,27 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
     }
     uint64_t paths = 0;
     int rc = run_waves(ctx, wf, wf->cfg, qs, aov, cancel, 0xffffffffu, &paths, nullptr);
+    if (rc == SHIRO_ERR_CANCELLED) {
+        // a cancelled batch is discarded (RenderParam.cpp:791-798): cleared
+        // planes, as FrameBuffer::Clear leaves them (FrameBuffer.cpp:19-24)
+        for (uint32_t r = 0; r < count; ++r) {
+            const uint64_t px = static_cast<uint64_t>(reqs[r].settings.width) * reqs[r].settings.height;
+            if (outs[r].on_device) {
+                cudaMemsetAsync(outs[r].beauty, 0, px * 16, ctx->stream);
+                cudaMemsetAsync(outs[r].albedo, 0, px * 12, ctx->stream);
+                cudaMemsetAsync(outs[r].normal, 0, px * 12, ctx->stream);
+                std::vector<float> inf(px, __builtin_inff());
+                if (px) cudaMemcpyAsync(outs[r].depth, inf.data(), px * 4, cudaMemcpyHostToDevice, ctx->stream);
+                cudaStreamSynchronize(ctx->stream);
+            } else {
+                std::fill(outs[r].beauty, outs[r].beauty + 4 * px, 0.0f);
+                std::fill(outs[r].albedo, outs[r].albedo + 3 * px, 0.0f);
+                std::fill(outs[r].normal, outs[r].normal + 3 * px, 0.0f);
+                std::fill(outs[r].depth, outs[r].depth + px, __builtin_inff());
+            }
+        }
+        return rc;
+    }
     if (rc != SHIRO_OK) return rc;
     for (uint32_t r = 0; r < count; ++r) {
         if (outs[r].on_device) continue;

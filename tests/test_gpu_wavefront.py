@@ -188,7 +188,14 @@ def test_autotune_picks_a_valid_config(gpu):
 def test_cancel_batch(gpu):
     from shiro_gb300 import ShiroGpuError, scenes
 
+    from shiro_gb300.abi import FrameBuffer
+
     w = scenes.sphere_workload(16, 16, 4, 4, env_width=32, env_height=16)
+    fb = FrameBuffer(16, 16)
+    fb.beauty[:] = 7.0
+    fb.depth[:] = 1.0
     with pytest.raises(ShiroGpuError) as ei:
-        gpu.render_batch(w.scene, [(w.camera, w.settings)], cancel=C.c_int(1))
+        gpu.render_batch(w.scene, [(w.camera, w.settings)], cancel=C.c_int(1), outs_fb=[fb])
     assert ei.value.code == -6
+    # the discarded batch leaves cleared planes (FrameBuffer::Clear)
+    assert not fb.beauty.any() and np.isinf(fb.depth).all()
