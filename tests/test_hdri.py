@@ -303,3 +303,30 @@ def test_loaded_environment_renders_on_the_cpu_checker(rgb):
     env = hdri.load_exr(exr_bytes({c: (rgb[..., i], HALF) for i, c in enumerate("RGB")}, 3))
     row, cond = api.env_tables(oracle.port_checker(), env)
     assert row[-1] == pytest.approx(1.0) and np.all(np.diff(row) >= 0)
+
+
+def test_hdr_header_variants(texels):
+    # "#?RGBE" signature, comment and extra variable lines, no FORMAT line
+    data = hdr_bytes(texels, "new", header=b"#?RGBE\n# made by a test\nGAMMA=1.0\nSOFTWARE=x\n\n")
+    np.testing.assert_array_equal(hdri.load_hdr(data), rgbe_decode_ref(texels))
+
+
+def test_exr_random_line_order_and_extra_attributes(rgb):
+    planes = {c: (rgb[..., i], HALF) for i, c in enumerate("RGB")}
+    data = bytearray(exr_bytes(planes, 3))
+    # a reader must not depend on attribute order or unknown attributes: insert
+    # one before the end of the header, shifting the offsets accordingly
+    extra = attr("owner", "string", b"test")
+    end = data.index(b"screenWindowWidth\0float\0") + len(b"screenWindowWidth\0float\0") + 4 + 4
+    assert data[end] == 0
+    nchunks = (rgb.shape[0] + 15) // 16
+    offs = list(struct.unpack_from(f"<{nchunks}Q", data, end + 1))
+    shifted = bytes(data[:end]) + extra + b"\0" + struct.pack(f"<{nchunks}Q", *[o + len(extra) for o in offs]) + \
+        bytes(data[end + 1 + 8 * nchunks:])
+    want = rgb.astype(np.float16).astype(np.float32)
+    np.testing.assert_array_equal(hdri.load_exr(shifted), want)
+    # lineOrder RANDOM_Y: chunks located through the offset table only
+    rnd = bytearray(shifted)
+    i = rnd.index(b"lineOrder\0lineOrder\0") + len(b"lineOrder\0lineOrder\0") + 4
+    rnd[i] = 2
+    np.testing.assert_array_equal(hdri.load_exr(bytes(rnd)), want)
