@@ -337,21 +337,98 @@ def rmse_check(local: int, bvh_width: int, with_cpu: bool) -> dict:
     ref_s = time.perf_counter() - t0
     plain = gpu.render_device(w.camera, st, 0, st.samples_per_pixel)
     wave = gpu.render_device(w.camera, st, 0, st.samples_per_pixel, wavefront=True)
+    plain_cdf = gpu.render_device(w.camera, st, 0, st.samples_per_pixel, flags=1)
     a, b = rmse(plain, ref.mean), rmse(wave, ref.mean)
     out = {"workload": w.name, "reference_spp": ref.spp, "reference_first_sample": ref.first,
            "reference_accumulation": "float64 over 256-spp batch means", "reference_seconds": ref_s,
            "plain": a, "wavefront": b, "relative_difference": abs(a - b) / max(a, 1e-30),
-           "identical_images": bool((plain == wave).all()), "expected_mc_rmse": expected_mc_rmse(ref, st.samples_per_pixel)}
+           "identical_images": bool((plain == wave).all()), "expected_mc_rmse": expected_mc_rmse(ref, st.samples_per_pixel),
+           "plain_env_cdf": rmse(plain_cdf, ref.mean),
+           "note": "plain / wavefront pick dome-sample texels by the alias table (the timed path), plain_env_cdf by "
+                   "the reference's CDF search; cpu_oracle (CDF search, as the reference) pairs with plain_env_cdf and "
+                   "cpu_oracle_alias (the port given the backend's alias table) with plain: like for like, same paths"}
     if with_cpu:
         import oracle
         from oracle import api
 
         oracle.build_port()
         ck = oracle.port_checker()
-        cpu = api.render(ck, w.scene, w.camera, st, 0, st.samples_per_pixel)
-        out["cpu_oracle"] = rmse(torch.from_numpy(cpu.beauty.reshape(st.height, st.width, 4).copy()), ref.mean.cpu())
+        ps = api.PortScene(ck, w.scene)
+        rows = np.arange(st.height)
+
+        def cpu_rmse(fb):
+            return rmse(torch.from_numpy(fb.beauty.reshape(st.height, st.width, 4).copy()), ref.mean.cpu())
+
+        cpu_cdf = ps.render_rows(w.camera, st, rows, 0, st.samples_per_pixel, flags=1)
+        tab = gpu.env_tables(0)
+        ps.set_alias(0, tab["alias_threshold_bits"], tab["alias_index"])
+        cpu_alias = ps.render_rows(w.camera, st, rows, 0, st.samples_per_pixel, flags=0)
+        ps.close()
+        out["cpu_oracle"] = cpu_rmse(cpu_cdf)
+        out["cpu_oracle_alias"] = cpu_rmse(cpu_alias)
+
+        def differing(gimg, fb):
+            g = gimg.cpu().numpy().reshape(-1, 4)
+            c = fb.beauty.reshape(-1, 4)
+            return int((~np.isclose(g, c, rtol=1e-3, atol=1e-4).all(1)).sum())
+
+        out["pixels_differing_cdf"] = differing(plain_cdf, cpu_cdf)
+        out["pixels_differing_alias"] = differing(plain, cpu_alias)
     gpu.close()
     return out
+
+
+def adapter_e2e(w, steps: int, warmup: int) -> dict:
+    """End to end through the C++ RenderBackend adapter (GpuBackend), the call
+    Shiro's Renderer makes: RenderSampleBatch with the renderer-owned scene
+    snapshot in and a host FrameBuffer (the AOVs in the FrameBuffer's own
+    storage) out, timed on the host clock around each call; the adapter's
+    default wavefront configuration, no tuning.  Driven through the test
+    harness's C entry point (tests/cpp)."""
+    import ctypes as C
+
+    from tests.cpp.harness import load_harness
+    from shiro_gb300.abi import FrameBuffer, MarshalledScene, render_desc
+
+    lib = load_harness()
+    st = w.settings
+    ms = MarshalledScene(w.scene)
+    req = render_desc(w.camera, st, 0, st.samples_per_pixel)
+    times = (C.c_double * steps)()
+    fb = FrameBuffer(st.width, st.height)
+    aov = fb.aovs()
+    rc = lib.shiro_harness_time_render(ms.ref(), C.byref(req), warmup, steps, times, C.byref(aov))
+    if rc != 1:
+        return {"unavailable": f"adapter harness returned {rc}"}
+    ms_steps = [times[k] for k in range(steps)]
+    mean = statistics.mean(ms_steps)
+    return {"value": w.paths / (mean / 1000.0) / 1e6, "unit": UNIT, "ms_per_step": mean, "ms_steps": ms_steps,
+            "h2d_bytes_per_step": C.sizeof(req), "d2h_bytes_per_step": st.width * st.height * 44,
+            "note": "GpuBackend::RenderSampleBatch (C++ adapter) -> FrameBuffer in pageable host memory; the scene "
+                    "signature is checked every call, the scene uploaded once"}
+
+
+def c5_bench(local: int, steps: int = 3) -> dict:
+    """Inverse rendering (the 16-view configuration: 1.31 M-triangle field
+    scene, 512 x 512, 16 spp, depth 8, 65 materials + a 1024 x 512 dome as
+    unknowns, Adam lr 1e-2): a few optimisation steps with the wavefront
+    forward and the adjoint backward, for steps/s; the 200-step run's parameter
+    errors are recorded separately (python -m shiro_gb300.inverse)."""
+    from shiro_gb300 import GpuBackend, scenes
+    from shiro_gb300.abi import RenderSettings
+    from shiro_gb300.inverse import inverse_render, orbit_views
+
+    scene = scenes.field_scene(env_width=1024, env_height=512)
+    st = RenderSettings(width=512, height=512, samples_per_pixel=16, max_depth=8, diffuse_depth=8, specular_depth=8,
+                        dome_light_samples=1, background_visible=True, backend=1)
+    views = orbit_views(16, 30.0, 12.0, seed=11)
+    with GpuBackend(local) as gpu:
+        inverse_render(gpu, scene, views, st, steps=1)  # warm-up (targets, pools, graphs)
+        r = inverse_render(gpu, scene, views, st, steps=steps)
+    return {"workload": "field 1310720 tris, 16 views 512x512, 16 spp, depth 8, 65 materials + 1024x512 env",
+            "forward": "wavefront", "steps": steps, "steps_per_s": r.steps_per_s,
+            "gradient_views_per_s": r.steps_per_s * r.views,
+            "Mpaths_s_forward_plus_adjoint": r.steps_per_s * r.paths_per_step / 1e6}
 
 
 def batch_bench(local: int, bvh_width: int, reps: int = 2) -> dict:
@@ -642,6 +719,14 @@ def main():
         adjoint = adjoint_bench(local, bvh_width=args.bvh_width)
 
     extra = {}
+    full = args.workload == "field" and not (args.width or args.height or args.spp)
+    if rank == 0 and not args.no_e2e and full:
+        try:
+            extra["e2e_adapter"] = adapter_e2e(w, args.steps, max(1, args.warmup))
+        except Exception as ex:  # the harness needs a host C++ compiler
+            extra["e2e_adapter"] = {"unavailable": str(ex)[:200]}
+    if rank == 0 and not args.no_adjoint and full:
+        extra["inverse"] = c5_bench(local)
     if rank == 0 and not args.no_rmse and args.workload == "field" and not (args.width or args.height or args.spp):
         extra["rmse"] = rmse_check(local, args.bvh_width, not args.no_cpu_baseline)
     if rank == 0 and not args.no_batch and args.workload == "field" and not (args.width or args.height or args.spp):

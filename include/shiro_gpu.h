@@ -256,6 +256,14 @@ const char* shiro_gpu_last_error(const ShiroGpuContext* ctx);
  * speed. */
 int shiro_gpu_set_bvh_width(ShiroGpuContext* ctx, uint32_t width);
 
+/* How the next shiro_gpu_upload_scene builds its binary BVHs (the wide one
+ * is collapsed from them): sah_cluster_triangles > 1 keeps the Morton (LBVH)
+ * subtrees of at most that many triangles as clusters and rebuilds the tree
+ * above them by binned SAH over the clusters' boxes (16 bins per axis, on the
+ * device); 0 keeps the Morton hierarchy throughout.  Default 8.  Both give
+ * identical hits; the choice only changes speed. */
+int shiro_gpu_set_bvh_build(ShiroGpuContext* ctx, uint32_t sah_cluster_triangles);
+
 /* Renders on this CUDA stream (cudaStream_t cast to void*; NULL = the
  * context's own stream). */
 int shiro_gpu_set_stream(ShiroGpuContext* ctx, void* stream);
@@ -266,6 +274,36 @@ int shiro_gpu_set_stream(ShiroGpuContext* ctx, void* stream);
  * Renderer.cpp:19-30).  reason (may be NULL) receives a short explanation. */
 int shiro_gpu_supports_scene(const ShiroSceneDesc* scene, char* reason, size_t reason_size);
 
+/* 64-bit content signature of a scene snapshot: a hash of everything
+ * shiro_gpu_upload_scene reads (every material field, each mesh's material
+ * index, positions, normals and indices, the lights, each dome's radiance,
+ * frame, layout and texels, the gradient environment).  Callers that cache the
+ * uploaded scene compare it to decide whether to upload again, as the OptiX
+ * backend compares ComputeSceneSignature (OptixBackend.cpp:150-232,
+ * 1079-1092): a snapshot edited in place, or a new one built at a freed
+ * address (RenderParam.cpp:614-659), gets a new signature.  Large scenes are
+ * hashed on several host threads (about 20 GB/s); the value does not depend on
+ * the thread count. */
+int shiro_gpu_scene_signature(const ShiroSceneDesc* scene, uint64_t* out);
+
+/* Environment images from disk: EnvironmentMap::Load (EnvironmentMap.cpp:
+ * 49-92) without OpenImageIO, for hosts whose EnvironmentMap is built without
+ * it (it then loads nothing).  Reads a Radiance RGBE file (.hdr: flat,
+ * old- and new-style run-length scanlines, all eight orientations; a texel is
+ * mantissa * 2^(exponent - 136)) or a single-part scanline OpenEXR file
+ * (.exr: HALF / FLOAT / UINT channels; NONE, RLE, ZIPS, ZIP compression; R, G,
+ * B used when present, else Y, else the first non-alpha channels), told apart
+ * by their magic bytes.  *pixels receives width * height RGB float triples,
+ * row 0 at the top (EnvironmentMap::Pixels()'s layout, ready for
+ * ShiroDomeLightDesc.env_pixels); free it with shiro_hdri_free.  On failure
+ * returns SHIRO_ERR_INVALID_ARGUMENT (SHIRO_ERR_OUT_OF_MEMORY) with the reason
+ * in error (may be NULL).  Host code only: no device is needed. */
+int shiro_hdri_load(const char* path, uint32_t* width, uint32_t* height, float** pixels, char* error,
+                    size_t error_size);
+int shiro_hdri_decode(const void* data, size_t size, uint32_t* width, uint32_t* height, float** pixels, char* error,
+                      size_t error_size);
+void shiro_hdri_free(float* pixels);
+
 /* Uploads a scene snapshot: flattens meshes, builds the device BVH, the
  * material table and the dome-light importance tables (CDF and alias).
  * Counterpart of OptixBackend::UploadSceneData (OptixBackend.cpp:751-1026) and
@@ -275,9 +313,10 @@ int shiro_gpu_upload_scene(ShiroGpuContext* ctx, const ShiroSceneDesc* scene);
 /* FrameBuffer RenderSampleBatch(const RenderRequest&)
  * (RenderBackend.h:33; CpuPathTracer.cpp:2043-2170) with the plain
  * one-thread-per-path megakernel.  cancel (may be NULL) is polled between
- * launches; a set flag returns SHIRO_ERR_CANCELLED and leaves the AOVs
- * cleared, as the reference discards a cancelled batch
- * (RenderParam.cpp:791-798). */
+ * launches of at most 2^24 paths while they run (with a flag given, two
+ * launches are queued at most, so another host thread may set it mid-frame);
+ * a set flag returns SHIRO_ERR_CANCELLED and leaves the AOVs cleared, as the
+ * reference discards a cancelled batch (RenderParam.cpp:791-798). */
 int shiro_gpu_render(ShiroGpuContext* ctx, const ShiroRenderDesc* request,
                      const volatile int* cancel, ShiroAovs* out);
 
@@ -285,8 +324,9 @@ int shiro_gpu_render(ShiroGpuContext* ctx, const ShiroRenderDesc* request,
  * camera, resolution, spp and depth) against the uploaded scene with
  * persistent stage kernels and per-stage queues.  Results equal those of
  * shiro_gpu_render for each request.  cancel (may be NULL) is polled between
- * waves; a set flag returns SHIRO_ERR_CANCELLED with every request's AOVs
- * cleared. */
+ * waves while they run (with a flag given, at most waves-in-flight + 1 waves
+ * are queued ahead); a set flag returns SHIRO_ERR_CANCELLED with every
+ * request's AOVs cleared, and last_stats().waves counts the waves that ran. */
 int shiro_gpu_render_batch(ShiroGpuContext* ctx, const ShiroRenderDesc* requests, uint32_t count,
                            const volatile int* cancel, ShiroAovs* outs);
 
@@ -357,6 +397,29 @@ int shiro_gpu_trace_rays(ShiroGpuContext* ctx, const float* origins, const float
                          const float* t_max, uint32_t n, uint32_t* prim_out, float* t_out,
                          uint32_t* occluded_out);
 
+/* Importance tables of dome texture `env` (the domes that carry a texture,
+ * counted in dome order from 0), copied from device memory into the caller's
+ * host arrays; any array may be NULL.  row_cdf: h + 1 floats, cond_cdf:
+ * h * (w + 1) floats (EnvironmentMap::BuildImportanceTable,
+ * EnvironmentMap.cpp:185-236), mass: w * h per-texel probabilities
+ * rowMass * columnMass (LatLongPdf, :302-313), alias_threshold / alias_index:
+ * w * h entries of the alias table (acceptance threshold as float bits, alias
+ * texel).  Diagnostic: lets tests check the tables the kernels sample. */
+int shiro_gpu_env_tables(ShiroGpuContext* ctx, uint32_t env, uint32_t* w_out, uint32_t* h_out, float* row_cdf,
+                         float* cond_cdf, float* mass, uint32_t* alias_threshold, uint32_t* alias_index);
+/* The texel the kernels' dome sampler picks (EnvironmentMap::Sample's row and
+ * column, :109-163) for n host 2-D points u2 (u.x, u.y pairs): the alias
+ * lookup, or the CDF search when flags has SHIRO_RENDER_ENV_CDF.  texel_out[i]
+ * = row * w + column, pdf_out[i] = the reference's pdf of that sample. */
+int shiro_gpu_env_sample(ShiroGpuContext* ctx, uint32_t env, uint32_t n, const float* u2, uint32_t flags,
+                         uint32_t* texel_out, float* pdf_out);
+/* Per-path results of the plain form for listed paths (TracePath,
+ * CpuPathTracer.cpp:1650-2017): out[10 i .. 10 i + 9] = radiance rgb, albedo
+ * rgb, normal rgb, depth of the path of pixel pixels[i] (y * width + x) with
+ * sample index sample_index[i].  Diagnostic: pins differing pixels to paths. */
+int shiro_gpu_render_paths(ShiroGpuContext* ctx, const ShiroRenderDesc* request, const uint32_t* pixels, uint32_t n,
+                           const uint32_t* sample_index, float* out);
+
 /* Render without allocating device memory.  No counterpart in the reference:
  * this entry point exists for callers that must not allocate device memory
  * while they render - e.g. a process that hands all device memory to its own
@@ -369,8 +432,15 @@ int shiro_gpu_trace_rays(ShiroGpuContext* ctx, const float* origins, const float
  * Rules: the AOV planes must be device pointers (on_device = 1); a request
  * with sample_count > 1 048 576 is refused (SHIRO_ERR_INVALID_ARGUMENT);
  * all calls share the array, so calls that overlap on the GPU race and must be
- * serialised by the caller; the first call on a device looks the array's
- * address up - make it before any stream capture. */
+ * serialised by the caller.  shiro_gpu_create sets the array up for its device
+ * (looks its address up and loads its module and the plain-form kernels), so
+ * the device memory this entry point relies on is taken when the context is
+ * made, before a caller's allocator claims the rest; if that set-up failed,
+ * this entry point returns SHIRO_ERR_CUDA with the reason.  The thread-local
+ * memory the kernels use is sized by the CUDA driver at the first launch of a
+ * kernel that needs it: a caller that must see no allocation at all renders
+ * once with shiro_gpu_render (or this entry point) before claiming the
+ * device's memory. */
 int shiro_gpu_render_static(ShiroGpuContext* ctx, const ShiroRenderDesc* request, const volatile int* cancel,
                             ShiroAovs* out);
 

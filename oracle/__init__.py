@@ -72,6 +72,18 @@ def load_port():
         lib.oracle_supports_scene.restype = C.c_int
         lib.oracle_trace_rays_bruteforce.argtypes = [_P, _P, _P, _P, _U, _P, _P, _P]
         lib.oracle_trace_rays_bruteforce.restype = C.c_int
+        lib.oracle_scene_create.argtypes = [_P, _P]
+        lib.oracle_scene_create.restype = C.c_int
+        lib.oracle_scene_destroy.argtypes = [_P]
+        lib.oracle_scene_destroy.restype = None
+        lib.oracle_scene_render_row_list.argtypes = [_P, _P, _P, _U, _P]
+        lib.oracle_scene_render_row_list.restype = C.c_int64
+        lib.oracle_scene_render_paths.argtypes = [_P, _P, _P, _U, _P, _P]
+        lib.oracle_scene_render_paths.restype = C.c_int
+        lib.oracle_scene_set_env_alias.argtypes = [_P, _U, _P, _P, _U]
+        lib.oracle_scene_set_env_alias.restype = C.c_int
+        lib.oracle_env_alias.argtypes = [_U, _U, _P, _P, _P]
+        lib.oracle_env_alias.restype = C.c_int
         _port = lib
     return _port
 

@@ -76,6 +76,19 @@ def env_tables(ck: Checker, env):
     return row, cond
 
 
+def env_alias(ck: Checker, env):
+    """The GPU backend's alias table by the port's sequential sweep:
+    (threshold bits, alias index), each h * w."""
+    env = np.ascontiguousarray(env, np.float32)
+    h, w = env.shape[:2]
+    thr = np.zeros(h * w, np.uint32)
+    al = np.zeros(h * w, np.uint32)
+    rc = ck.lib.oracle_env_alias(w, h, _p(env), _p(thr), _p(al))
+    if rc != 0:
+        raise RuntimeError(f"oracle_env_alias failed: {rc}")
+    return thr, al
+
+
 def env_query(ck: Checker, env, u2, dirs, layout=1):
     env = np.ascontiguousarray(env, np.float32)
     h, w = env.shape[:2]
@@ -130,3 +143,54 @@ def render_paths(ck: Checker, scene, camera, settings, sample_start, pixels, sam
     out = np.zeros((n, 10), np.float32)
     ck.lib.oracle_render_paths(ms.ref(), C.byref(req), _p(px), n, _p(si), _p(out), None, None)
     return out
+
+
+class PortScene:
+    """A scene built once in the port (oracle_scene_*), for repeated renders
+    of row lists and path lists.  ``set_alias`` gives a dome texture the GPU
+    backend's alias table, so that renders without SHIRO_RENDER_ENV_CDF pick
+    dome-sample texels exactly as the backend's default (timed) sampler does."""
+
+    def __init__(self, ck: Checker, scene):
+        self.lib = ck.lib
+        self.ms = MarshalledScene(scene) if not isinstance(scene, MarshalledScene) else scene
+        self.h = C.c_void_p()
+        rc = self.lib.oracle_scene_create(self.ms.ref(), C.byref(self.h))
+        if rc != 0:
+            raise RuntimeError(f"oracle_scene_create failed: {rc}")
+
+    def set_alias(self, dome: int, threshold_bits, alias):
+        thr = np.ascontiguousarray(threshold_bits, np.uint32)
+        al = np.ascontiguousarray(alias, np.uint32)
+        rc = self.lib.oracle_scene_set_env_alias(self.h, dome, _p(thr), _p(al), thr.size)
+        if rc != 0:
+            raise RuntimeError(f"oracle_scene_set_env_alias failed: {rc}")
+
+    def render_rows(self, camera, settings, rows, sample_start=0, sample_count=None, flags=0) -> FrameBuffer:
+        count = settings.samples_per_pixel if sample_count is None else sample_count
+        req = render_desc(camera, settings, sample_start, count, flags)
+        fb = FrameBuffer(settings.width, settings.height)
+        aovs = fb.aovs()
+        r = np.ascontiguousarray(rows, np.uint32)
+        n = self.lib.oracle_scene_render_row_list(self.h, C.byref(req), _p(r), r.size, C.byref(aovs))
+        if n < 0:
+            raise RuntimeError(f"oracle_scene_render_row_list failed: {n}")
+        return fb
+
+    def render_paths(self, camera, settings, pixels, sample_index, flags=0) -> np.ndarray:
+        req = render_desc(camera, settings, 0, 1, flags)
+        px = np.ascontiguousarray(pixels, np.uint32)
+        si = np.ascontiguousarray(sample_index, np.uint32)
+        out = np.zeros((px.size, 10), np.float32)
+        rc = self.lib.oracle_scene_render_paths(self.h, C.byref(req), _p(px), px.size, _p(si), _p(out))
+        if rc != 0:
+            raise RuntimeError(f"oracle_scene_render_paths failed: {rc}")
+        return out
+
+    def close(self):
+        if self.h:
+            self.lib.oracle_scene_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        self.close()

@@ -132,6 +132,12 @@ struct Env {
     bool latlong = true;
     std::vector<V3> px;
     std::vector<float> rowCdf, condCdf;
+    // Optional alias table of the GPU backend (not part of the reference):
+    // per texel the acceptance threshold (float bits) and the alias texel.
+    // When present and the render does not ask for the CDF search, a sample
+    // picks its texel as the backend's alias lookup does; everything after
+    // the pick is EnvironmentMap::Sample's.
+    std::vector<uint32_t> aliasThr, aliasIdx;
 
     static float Wrap(float v) {  // :23-26
         v = std::fmod(v, 1.0f);
@@ -231,7 +237,7 @@ struct Env {
         return rowMass * colMass * static_cast<float>(w * h) / (2.0f * kPi * kPi * sinT);
     }
 
-    V3 Sample(const V2& u, V3* dir, float* pdf) const {  // :109-163
+    V3 Sample(const V2& u, V3* dir, float* pdf, bool useAlias = false) const {  // :109-163
         if (px.empty()) {
             *dir = {0.0f, 1.0f, 0.0f};
             *pdf = 0.0f;
@@ -239,9 +245,26 @@ struct Env {
         }
         if (latlong && !rowCdf.empty() && w > 0 && h > 0) {
             float rowMass = 0.0f, colMass = 0.0f;
-            const uint32_t row = SampleCdf(rowCdf, 0, h, u.y, &rowMass);
-            const uint32_t off = row * (w + 1u);
-            const uint32_t col = SampleCdf(condCdf, off, off + w, u.x, &colMass);
+            uint32_t row, col;
+            if (useAlias && aliasThr.size() == static_cast<size_t>(w) * h) {
+                // the backend's texel pick: bucket floor(u.y * n), accepted
+                // when u.x is below its threshold, else its alias
+                const uint32_t n = w * h;
+                uint32_t i = static_cast<uint32_t>(u.y * static_cast<float>(n));
+                i = i >= n ? n - 1u : i;
+                float thr;
+                std::memcpy(&thr, &aliasThr[i], 4);
+                const uint32_t t = u.x < thr ? i : aliasIdx[i];
+                row = t / w;
+                col = t - row * w;
+                rowMass = rowCdf[row + 1u] - rowCdf[row];
+                const size_t off = static_cast<size_t>(row) * (w + 1u);
+                colMass = condCdf[off + col + 1u] - condCdf[off + col];
+            } else {
+                row = SampleCdf(rowCdf, 0, h, u.y, &rowMass);
+                const uint32_t off = row * (w + 1u);
+                col = SampleCdf(condCdf, off, off + w, u.x, &colMass);
+            }
             const float uu = (static_cast<float>(col) + 0.5f) / static_cast<float>(w);
             const float vv = (static_cast<float>(row) + 0.5f) / static_cast<float>(h);
             const float theta = vv * kPi;
@@ -1113,12 +1136,12 @@ inline float DomePdf(const Dome& d, const V3& dir) {
     if (d.env) return d.env->Pdf(WorldToLight(d, dir));
     return kInvFourPi;
 }
-bool SampleDome(const Dome& d, const V2& u, V3* dir, V3* rad, float* pdf) {
+bool SampleDome(const Dome& d, const V2& u, V3* dir, V3* rad, float* pdf, bool useAlias) {
     V3 ld{};
     float lp = 0.0f;
     V3 lr{};
     if (d.env) {
-        lr = d.env->Sample(u, &ld, &lp);
+        lr = d.env->Sample(u, &ld, &lp, useAlias);
     } else {
         const float y = 1.0f - 2.0f * u.y;
         const float r = std::sqrt(std::max(0.0f, 1.0f - y * y));
@@ -1176,7 +1199,9 @@ struct Tracer {
                                      static_cast<uint32_t>(li) * kDirectLightStride + k * kDirectSampleStride;
                 V3 ld, lr;
                 float lp = 0.0f;
-                if (!SampleDome(s.domes[li], smp.Next2D(dim), &ld, &lr, &lp) || lp <= 0.0f) continue;
+                if (!SampleDome(s.domes[li], smp.Next2D(dim), &ld, &lr, &lp, !(flags & SHIRO_RENDER_ENV_CDF)) ||
+                    lp <= 0.0f)
+                    continue;
                 const float nl = Clampf(Dot(n, ld), 0.0f, 1.0f);
                 if (nl <= 0.0f || Blocked(origin, ld, FLT_MAX)) continue;
                 const float bp = BsdfPdf(m, n, cn, view, ld);
@@ -1726,6 +1751,68 @@ int oracle_env_tables(uint32_t w, uint32_t h, const float* rgb, float* row_cdf, 
     return 0;
 }
 
+// The GPU backend's alias table over the reference masses (its own sampler;
+// the reference has none), built by the sequential sweep the backend's
+// parallel construction must reproduce: weights floor(mass * 2^60), buckets
+// of C = ceil(T / n) units with the slack on the first heaviest texel; lights
+// are topped up from the current heavy while it holds more than C, otherwise
+// the heavy closes its own bucket and draws the rest from the next heavy.
+int oracle_env_alias(uint32_t w, uint32_t h, const float* rgb, uint32_t* threshold_bits, uint32_t* alias) {
+    auto e = MakeEnv(w, h, rgb, SHIRO_ENV_LAYOUT_LATLONG);
+    const uint64_t n = static_cast<uint64_t>(w) * h;
+    if (n == 0 || e->rowCdf.empty()) return SHIRO_ERR_INVALID_ARGUMENT;
+    using u64 = unsigned long long;
+    std::vector<u64> q(n);
+    u64 total = 0, best = 0;
+    uint64_t imax = 0;
+    for (uint32_t y = 0; y < h; ++y)
+        for (uint32_t x = 0; x < w; ++x) {
+            const size_t i = static_cast<size_t>(y) * w + x;
+            const float rowMass = e->rowCdf[y + 1u] - e->rowCdf[y];
+            const size_t off = static_cast<size_t>(y) * (w + 1u);
+            const float colMass = e->condCdf[off + x + 1u] - e->condCdf[off + x];
+            const float m = rowMass * colMass;
+            q[i] = m > 0.0f ? static_cast<u64>(static_cast<double>(m) * 1152921504606846976.0) : 0ull;
+            total += q[i];
+            if (q[i] > best) {
+                best = q[i];
+                imax = i;
+            }
+        }
+    auto put = [&](uint64_t i, u64 units, u64 cap, uint64_t to) {
+        const float t = static_cast<float>(static_cast<double>(units) / static_cast<double>(cap));
+        std::memcpy(&threshold_bits[i], &t, 4);
+        alias[i] = static_cast<uint32_t>(to);
+    };
+    if (total == 0) {
+        for (uint64_t i = 0; i < n; ++i) put(i, 1, 1, i);
+        return 0;
+    }
+    const u64 cap = (total + n - 1u) / n;
+    q[imax] += cap * n - total;
+    std::vector<uint64_t> lights, heavies;
+    for (uint64_t i = 0; i < n; ++i) (q[i] < cap ? lights : heavies).push_back(i);
+    size_t i = 0, j = 0;
+    u64 rest = q[heavies[0]];  // units the current heavy still holds
+    while (i < lights.size()) {
+        if (rest > cap || j + 1 == heavies.size()) {
+            put(lights[i], q[lights[i]], cap, heavies[j]);
+            rest -= cap - q[lights[i]];
+            ++i;
+        } else {
+            put(heavies[j], rest, cap, heavies[j + 1]);
+            rest = q[heavies[j + 1]] - (cap - rest);
+            ++j;
+        }
+    }
+    for (; j + 1 < heavies.size(); ++j) {
+        put(heavies[j], rest, cap, heavies[j + 1]);
+        rest = q[heavies[j + 1]] - (cap - rest);
+    }
+    put(heavies[j], 1, 1, heavies[j]);
+    return 0;
+}
+
 int oracle_env_query(uint32_t w, uint32_t h, const float* rgb, uint32_t layout, uint32_t n, const float* u2,
                      const float* dirs, float* sdir, float* spdf, float* srgb, float* pdf, float* rgb_out) {
     auto e = MakeEnv(w, h, rgb, layout);
@@ -1758,11 +1845,8 @@ int oracle_render(const ShiroSceneDesc* sd, const ShiroRenderDesc* req, ShiroAov
     return 0;
 }
 
-int oracle_render_paths(const ShiroSceneDesc* sd, const ShiroRenderDesc* req, const uint32_t* pixels, uint32_t n,
-                        const uint32_t* sample_index, float* out, void*, void*) {
-    SceneData s;
-    const int rc = Convert(*sd, &s);
-    if (rc != SHIRO_OK) return rc;
+static int RenderPathsImpl(const SceneData& s, const ShiroRenderDesc* req, const uint32_t* pixels, uint32_t n,
+                           const uint32_t* sample_index, float* out) {
     const ShiroSettingsDesc& st = req->settings;
     Tracer tr{s, req->flags, false};
     const uint32_t rows = (n + 255u) / 256u;
@@ -1786,6 +1870,14 @@ int oracle_render_paths(const ShiroSceneDesc* sd, const ShiroRenderDesc* req, co
         }
     });
     return 0;
+}
+
+int oracle_render_paths(const ShiroSceneDesc* sd, const ShiroRenderDesc* req, const uint32_t* pixels, uint32_t n,
+                        const uint32_t* sample_index, float* out, void*, void*) {
+    SceneData s;
+    const int rc = Convert(*sd, &s);
+    if (rc != SHIRO_OK) return rc;
+    return RenderPathsImpl(s, req, pixels, n, sample_index, out);
 }
 
 int oracle_scene_create(const ShiroSceneDesc* sd, OracleScene** out) {
@@ -1818,6 +1910,27 @@ int64_t oracle_scene_render_row_list(OracleScene* s, const ShiroRenderDesc* req,
     Tracer tr{s->data, req->flags, false};
     ParallelRows(0, n, [&](uint32_t k) { RenderRow(tr, *req, rows[k], out); });
     return static_cast<int64_t>(n) * req->settings.width * req->sample_count;
+}
+
+int oracle_scene_render_paths(OracleScene* s, const ShiroRenderDesc* req, const uint32_t* pixels, uint32_t n,
+                              const uint32_t* sample_index, float* out) {
+    if (!s || !req || (n && (!pixels || !sample_index || !out))) return SHIRO_ERR_INVALID_ARGUMENT;
+    const uint64_t px = static_cast<uint64_t>(req->settings.width) * req->settings.height;
+    for (uint32_t i = 0; i < n; ++i)
+        if (pixels[i] >= px) return SHIRO_ERR_INVALID_ARGUMENT;
+    return RenderPathsImpl(s->data, req, pixels, n, sample_index, out);
+}
+
+int oracle_scene_set_env_alias(OracleScene* s, uint32_t dome, const uint32_t* threshold_bits, const uint32_t* alias,
+                               uint32_t n) {
+    if (!s || dome >= s->data.domes.size() || !s->data.domes[dome].env) return SHIRO_ERR_INVALID_ARGUMENT;
+    Env& e = *s->data.domes[dome].env;
+    if (n != static_cast<uint64_t>(e.w) * e.h || (n && (!threshold_bits || !alias))) return SHIRO_ERR_INVALID_ARGUMENT;
+    for (uint32_t i = 0; i < n; ++i)
+        if (alias[i] >= n) return SHIRO_ERR_INVALID_ARGUMENT;
+    e.aliasThr.assign(threshold_bits, threshold_bits + n);
+    e.aliasIdx.assign(alias, alias + n);
+    return SHIRO_OK;
 }
 
 }  // extern "C"

@@ -41,6 +41,11 @@ int oracle_env_query(uint32_t w, uint32_t h, const float* rgb, uint32_t layout, 
                      const float* dirs, float* sample_dir, float* sample_pdf, float* sample_rgb, float* pdf,
                      float* rgb_out);
 int oracle_render(const ShiroSceneDesc* scene, const ShiroRenderDesc* req, ShiroAovs* out);
+/* The GPU backend's alias table (not part of the reference) over the
+ * reference's texel masses of a w x h lat-long texture, by a sequential sweep:
+ * the checker of the backend's parallel construction.  threshold_bits,
+ * alias: w * h entries each. */
+int oracle_env_alias(uint32_t w, uint32_t h, const float* rgb, uint32_t* threshold_bits, uint32_t* alias);
 
 /* Worker threads of the render calls (0 = hardware_concurrency - 1, as the
  * reference, CpuPathTracer.cpp:2064-2067). */
@@ -65,6 +70,18 @@ int64_t oracle_scene_render_rows(OracleScene* s, const ShiroRenderDesc* req, uin
  * negative error. */
 int64_t oracle_scene_render_row_list(OracleScene* s, const ShiroRenderDesc* req, const uint32_t* rows, uint32_t n,
                                      ShiroAovs* out);
+/* Per-path results as oracle_render_paths, on a created scene (with its
+ * alias tables, if set). */
+int oracle_scene_render_paths(OracleScene* s, const ShiroRenderDesc* req, const uint32_t* pixels, uint32_t n,
+                              const uint32_t* sample_index, float* out);
+/* Gives dome `dome`'s environment the GPU backend's alias table (n = w * h
+ * entries: acceptance threshold as float bits, alias texel).  Renders without
+ * SHIRO_RENDER_ENV_CDF then pick dome-sample texels by that table (bucket
+ * floor(u.y * n), accepted when u.x < threshold, else the alias) and follow
+ * EnvironmentMap::Sample from the picked texel on: the backend's timed
+ * sampler, checked path by path.  Not part of the reference. */
+int oracle_scene_set_env_alias(OracleScene* s, uint32_t dome, const uint32_t* threshold_bits, const uint32_t* alias,
+                               uint32_t n);
 /* 1 if the scene is within the restated scope (see above), else 0. */
 int oracle_supports_scene(const ShiroSceneDesc* scene);
 

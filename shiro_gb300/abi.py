@@ -336,11 +336,31 @@ def _uptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_uint32))
 
 
+def _same_memory(src, arr: np.ndarray) -> bool:
+    return isinstance(src, np.ndarray) and src.size > 0 and src.ctypes.data == arr.ctypes.data
+
+
+def scene_structure_key(scene: Scene) -> tuple:
+    """Every small field of a scene by value and every large array by object
+    identity: equal keys mean a MarshalledScene built earlier still describes
+    the scene, provided it aliases the arrays (edits inside them are then seen
+    through its pointers)."""
+    return (tuple(tuple(vars(m).values()) for m in scene.materials),
+            tuple((id(m.positions), id(m.indices), id(m.normals), int(m.material_index)) for m in scene.meshes),
+            tuple((tuple(l.direction), tuple(l.radiance)) for l in scene.distant_lights),
+            tuple((id(d.env), tuple(d.radiance), tuple(d.right), tuple(d.up), tuple(d.forward), int(d.layout))
+                  for d in scene.dome_lights),
+            tuple(scene.environment_top), tuple(scene.environment_bottom))
+
+
 class MarshalledScene:
-    """Holds a SceneDesc and every array it points into (keeps them alive)."""
+    """Holds a SceneDesc and every array it points into (keeps them alive).
+    ``aliased`` is True when every array of the descriptor is the caller's own
+    memory (float32 / uint32 and contiguous already), not a converted copy."""
 
     def __init__(self, scene: Scene):
         self._keep = []
+        self.aliased = True
         mats = (MaterialDesc * max(1, len(scene.materials)))()
         for i, m in enumerate(scene.materials):
             mats[i] = m.to_desc()
@@ -349,9 +369,11 @@ class MarshalledScene:
             pos = np.ascontiguousarray(m.positions, dtype=np.float32).reshape(-1, 3)
             idx = np.ascontiguousarray(m.indices, dtype=np.uint32).reshape(-1)
             self._keep += [pos, idx]
+            self.aliased &= (pos.size == 0 or _same_memory(m.positions, pos)) and (idx.size == 0 or _same_memory(m.indices, idx))
             nrm_ptr, ncount = None, 0
             if m.normals is not None:
                 nrm = np.ascontiguousarray(m.normals, dtype=np.float32).reshape(-1, 3)
+                self.aliased &= nrm.size == 0 or _same_memory(m.normals, nrm)
                 self._keep.append(nrm)
                 nrm_ptr, ncount = _fptr(nrm), nrm.shape[0]
             meshes[i] = MeshDesc(_fptr(pos), pos.shape[0], nrm_ptr, ncount, _uptr(idx), idx.size,
@@ -364,6 +386,7 @@ class MarshalledScene:
             ptr, w, h = None, 0, 0
             if d.env is not None:
                 env = np.ascontiguousarray(d.env, dtype=np.float32)
+                self.aliased &= env.size == 0 or _same_memory(d.env, env)
                 self._keep.append(env)
                 h, w = env.shape[0], env.shape[1]
                 ptr = _fptr(env)

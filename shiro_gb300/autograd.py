@@ -3,8 +3,9 @@
 ``render(backend, camera, settings, base_color, roughness, metallic, env)``
 returns the beauty image [H, W, 4] as a differentiable function of the
 per-material base colour [M, 3], roughness [M], metalness [M] and the texels
-[H_env, W_env, 3] of dome light 0.  The forward renders with the plain GPU form
-after writing the parameters into the resident scene; the backward runs the
+[H_env, W_env, 3] of dome light 0.  The forward renders with the batched
+wavefront form (or the plain form) after writing the parameters into the
+resident scene; the backward runs the
 adjoint path-replay kernel (shiro_gpu_adjoint), which recomputes every path
 from its QMC seed instead of storing it.
 
@@ -24,11 +25,13 @@ from .abi import Camera, RenderSettings
 
 class _Render(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, base_color, roughness, metallic, env, backend, camera, settings, sample_start, flags, adj_start):
+    def forward(ctx, base_color, roughness, metallic, env, backend, camera, settings, sample_start, flags, adj_start,
+                wavefront):
         tensors = [t.detach().contiguous().float() if t is not None else None
                    for t in (base_color, roughness, metallic, env)]
         backend.set_params(*tensors)
-        beauty = backend.render_device(camera, settings, sample_start, settings.samples_per_pixel, flags)
+        beauty = backend.render_device(camera, settings, sample_start, settings.samples_per_pixel, flags,
+                                       wavefront=wavefront)
         ctx.backend = backend
         ctx.camera = camera
         ctx.settings = settings
@@ -46,11 +49,14 @@ class _Render(torch.autograd.Function):
                 grads[name] = torch.zeros(shape, dtype=torch.float32, device="cuda")
         ctx.backend.adjoint(ctx.camera, ctx.settings, d_beauty.contiguous().float(), grads, ctx.sample_start,
                             ctx.settings.samples_per_pixel, ctx.flags)
-        return tuple(grads.get(n) for n in names) + (None, None, None, None, None, None)
+        return tuple(grads.get(n) for n in names) + (None, None, None, None, None, None, None)
 
 
 def render(backend, camera: Camera, settings: RenderSettings, base_color, roughness, metallic, env=None,
-           sample_start: int = 0, flags: int = 0, adjoint_sample_start=None):
-    """Differentiable render of the backend's uploaded scene (see module doc)."""
+           sample_start: int = 0, flags: int = 0, adjoint_sample_start=None, wavefront: bool = True):
+    """Differentiable render of the backend's uploaded scene (see module doc).
+    The forward runs the batched wavefront form (wavefront=True, the faster
+    one; its frames equal the plain form's bit for bit) or the plain
+    one-thread-per-path form."""
     return _Render.apply(base_color, roughness, metallic, env, backend, camera, settings, sample_start, flags,
-                         adjoint_sample_start)
+                         adjoint_sample_start, wavefront)

@@ -35,6 +35,25 @@ _P = C.c_void_p
 _U = C.c_uint32
 
 
+def load_environment_file(path: str) -> np.ndarray:
+    """An environment image (Radiance .hdr or OpenEXR .exr) read by the native
+    library's reader (shiro_hdri_load, the counterpart of EnvironmentMap::Load
+    for hosts without OpenImageIO) as (height, width, 3) float32 texels, row 0
+    at the top.  Raises ShiroGpuError with the reader's reason on failure."""
+    lib = load_library()
+    w, h = C.c_uint32(), C.c_uint32()
+    px = C.POINTER(C.c_float)()
+    err = C.create_string_buffer(256)
+    rc = lib.shiro_hdri_load(os.fsencode(path), C.byref(w), C.byref(h), C.byref(px), err, 256)
+    if rc != 0:
+        raise ShiroGpuError(rc, err.value.decode())
+    try:
+        n = w.value * h.value * 3
+        return np.ctypeslib.as_array(px, shape=(n,)).copy().reshape(h.value, w.value, 3)
+    finally:
+        lib.shiro_hdri_free(C.cast(px, C.c_void_p))
+
+
 class ShiroGpuError(RuntimeError):
     def __init__(self, code: int, message: str):
         super().__init__(f"[{code}] {message}")
@@ -75,6 +94,14 @@ def load_library(path: str = LIB_PATH):
         "shiro_gpu_count_work": ([_P, _P, _U, _P], C.c_int),
         "shiro_gpu_render_frozen": ([_P, _P, _P, _P, _P, _P, _P], C.c_int),
         "shiro_gpu_set_bvh_width": ([_P, _U], C.c_int),
+        "shiro_gpu_set_bvh_build": ([_P, _U], C.c_int),
+        "shiro_gpu_env_tables": ([_P, _U, _P, _P, _P, _P, _P, _P, _P], C.c_int),
+        "shiro_gpu_scene_signature": ([_P, _P], C.c_int),
+        "shiro_hdri_load": ([C.c_char_p, _P, _P, _P, C.c_char_p, C.c_size_t], C.c_int),
+        "shiro_hdri_decode": ([C.c_char_p, C.c_size_t, _P, _P, _P, C.c_char_p, C.c_size_t], C.c_int),
+        "shiro_hdri_free": ([_P], None),
+        "shiro_gpu_env_sample": ([_P, _U, _U, _P, _U, _P, _P], C.c_int),
+        "shiro_gpu_render_paths": ([_P, _P, _P, _U, _P, _P], C.c_int),
         "shiro_gpu_accum_create": ([_P, _P], C.c_int),
         "shiro_gpu_accum_destroy": ([_P], None),
         "shiro_gpu_accum_reset": ([_P, _U, _U], C.c_int),
@@ -120,6 +147,8 @@ class GpuBackend:
             raise ShiroGpuError(rc, self.lib.shiro_gpu_last_error(None).decode())
         self._scene_key = None
         self._marshalled: Optional[MarshalledScene] = None
+        self._scene_ref = None
+        self._structure_key = None
         self.last_error = ""
         self._accumulators = weakref.WeakSet()
 
@@ -163,19 +192,29 @@ class GpuBackend:
         return ShiroGpuError(rc, msg)
 
     def upload_scene(self, scene: Scene, force: bool = False):
-        """Uploads (and caches by object identity, as CpuPathTracer caches by
-        Scene pointer, CpuPathTracer.cpp:2030-2041) the scene snapshot."""
-        key = id(scene)
+        """Uploads the scene snapshot unless the device already holds one of
+        the same content: the cache key is the object and the native content
+        signature (shiro_gpu_scene_signature: every material field, the mesh
+        arrays, lights, dome frames and texels), so a scene edited in place -
+        a light, a vertex - is uploaded again (the OptiX backend compares
+        ComputeSceneSignature the same way, OptixBackend.cpp:150-232)."""
+        skey = abi.scene_structure_key(scene)
+        ms = self._marshalled
+        if (ms is None or self._scene_ref is not scene or self._structure_key != skey or not ms.aliased):
+            ms = MarshalledScene(scene)
+        sig = C.c_uint64(0)
+        self.lib.shiro_gpu_scene_signature(ms.ref(), C.byref(sig))
+        key = (id(scene), sig.value)
+        self._marshalled = ms
+        self._scene_ref = scene
+        self._structure_key = skey
         if not force and self._scene_key == key:
             return
-        ms = MarshalledScene(scene)
         rc = self.lib.shiro_gpu_upload_scene(self._ctx, ms.ref())
         if rc != 0:
             self._scene_key = None
             raise self._err(rc)
         self._scene_key = key
-        self._marshalled = ms
-        self._scene_ref = scene
 
     def render(self, scene: Scene, camera: Camera, settings: RenderSettings, sample_start: int = 0,
                sample_count: Optional[int] = None, flags: int = 0, cancel: Optional[C.c_int] = None,
@@ -235,6 +274,15 @@ class GpuBackend:
         rc = self.lib.shiro_gpu_set_bvh_width(self._ctx, int(width))
         if rc != 0:
             raise ShiroGpuError(rc, "bvh width must be 0, 2 or 8")
+
+    def set_bvh_build(self, sah_cluster_triangles: int):
+        """Binary BVHs of the next upload: > 1 rebuilds the tree above Morton
+        clusters of at most that many triangles by binned SAH; 0 keeps the
+        Morton hierarchy.  Hits are identical.  Forces the next upload."""
+        rc = self.lib.shiro_gpu_set_bvh_build(self._ctx, int(sah_cluster_triangles))
+        if rc != 0:
+            raise ShiroGpuError(rc, "cluster size must be 0 or in [2, 65536]")
+        self._scene_key = None
 
     def wavefront_config(self) -> dict:
         c = WavefrontConfig()
@@ -378,6 +426,55 @@ class GpuBackend:
         if rc != 0:
             raise self._err(rc)
         return out.view(settings.height, settings.width, 4)
+
+    # -- diagnostics -----------------------------------------------------
+    def env_tables(self, env: int = 0) -> dict:
+        """The device importance tables of dome texture `env`: row_cdf,
+        cond_cdf (h, w + 1), mass (h, w), alias_threshold (float32 view of the
+        threshold bits) and alias_index (h * w)."""
+        w, h = C.c_uint32(), C.c_uint32()
+        rc = self.lib.shiro_gpu_env_tables(self._ctx, env, C.byref(w), C.byref(h), None, None, None, None, None)
+        if rc != 0:
+            raise self._err(rc)
+        w, h = w.value, h.value
+        row = np.zeros(h + 1, np.float32)
+        cond = np.zeros(h * (w + 1), np.float32)
+        mass = np.zeros(h * w, np.float32)
+        thr = np.zeros(h * w, np.uint32)
+        al = np.zeros(h * w, np.uint32)
+        p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        rc = self.lib.shiro_gpu_env_tables(self._ctx, env, None, None, p(row), p(cond), p(mass), p(thr), p(al))
+        if rc != 0:
+            raise self._err(rc)
+        return dict(width=w, height=h, row_cdf=row, cond_cdf=cond.reshape(h, w + 1), mass=mass.reshape(h, w),
+                    alias_threshold_bits=thr, alias_threshold=thr.view(np.float32), alias_index=al)
+
+    def env_sample(self, u2, env: int = 0, flags: int = 0):
+        """(texel index, pdf) the kernels' dome sampler gives each 2-D point."""
+        u2 = np.ascontiguousarray(u2, np.float32).reshape(-1, 2)
+        n = u2.shape[0]
+        texel = np.zeros(n, np.uint32)
+        pdf = np.zeros(n, np.float32)
+        p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        rc = self.lib.shiro_gpu_env_sample(self._ctx, env, n, p(u2), flags, p(texel), p(pdf))
+        if rc != 0:
+            raise self._err(rc)
+        return texel, pdf
+
+    def render_paths(self, scene: Scene, camera: Camera, settings: RenderSettings, pixels, sample_index,
+                     flags: int = 0) -> np.ndarray:
+        """Per-path results of the plain form, (n, 10): radiance, albedo,
+        normal, depth of path (pixel index, sample index)."""
+        self.upload_scene(scene)
+        req = render_desc(camera, settings, 0, 1, flags)
+        px = np.ascontiguousarray(pixels, np.uint32)
+        si = np.ascontiguousarray(sample_index, np.uint32)
+        out = np.zeros((px.size, 10), np.float32)
+        p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        rc = self.lib.shiro_gpu_render_paths(self._ctx, C.byref(req), p(px), px.size, p(si), p(out))
+        if rc != 0:
+            raise self._err(rc)
+        return out
 
     def last_stats(self) -> dict:
         s = RenderStats()

@@ -1,9 +1,11 @@
 // GpuBackend.cpp - RenderBackend adapter over the GB300 C ABI.
 #include "GpuBackend.h"
 
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <thread>
 
 #include "shiro/render/EnvironmentMap.h"
 #include "shiro_gpu.h"
@@ -129,32 +131,38 @@ struct SceneView {
     }
 };
 
-// FNV-1a over the scene's sizes and a few samples of its arrays: detects a
-// new snapshot placed at the same address.
-uint64_t Signature(const Scene& s) {
-    uint64_t h = 1469598103934665603ull;
-    auto mix = [&h](const void* p, size_t n) {
-        const unsigned char* b = static_cast<const unsigned char*>(p);
-        for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
-    };
-    const size_t counts[4] = {s.materials.size(), s.meshes.size(), s.distantLights.size(), s.domeLights.size()};
-    mix(counts, sizeof(counts));
-    for (const TriangleMesh& m : s.meshes) {
-        const size_t c[3] = {m.positions.size(), m.normals.size(), m.indices.size()};
-        mix(c, sizeof(c));
-        if (!m.positions.empty()) {
-            mix(&m.positions.front(), sizeof(Vec3f));
-            mix(&m.positions.back(), sizeof(Vec3f));
+// Forwards a RenderRequest's std::atomic<bool> cancel flag to the int the C
+// ABI polls between launches: a watcher thread copies it every 200 us while
+// the render runs (Hydra sets the flag from another thread,
+// RenderParam.cpp:790-806; RenderBackend.h:18).
+class CancelForward {
+public:
+    explicit CancelForward(const std::atomic<bool>* source) : source_(source) {
+        if (source_) watcher_ = std::thread([this] { Watch(); });
+    }
+    ~CancelForward() {
+        done_.store(true, std::memory_order_release);
+        if (watcher_.joinable()) watcher_.join();
+    }
+    CancelForward(const CancelForward&) = delete;
+    CancelForward& operator=(const CancelForward&) = delete;
+    const volatile int* Flag() const { return source_ ? &flag_ : nullptr; }
+
+private:
+    void Watch() {
+        while (!done_.load(std::memory_order_acquire)) {
+            if (source_->load(std::memory_order_relaxed)) {
+                flag_ = 1;
+                return;
+            }
+            std::this_thread::sleep_for(std::chrono::microseconds(200));
         }
     }
-    for (const PbrMaterial& m : s.materials) mix(&m, sizeof(PbrMaterial) - 4);
-    for (const DomeLight& d : s.domeLights) {
-        const void* env = d.environment.get();
-        mix(&env, sizeof(env));
-        mix(&d.radiance, sizeof(Vec3f));
-    }
-    return h;
-}
+    const std::atomic<bool>* source_;
+    volatile int flag_ = 0;
+    std::atomic<bool> done_{false};
+    std::thread watcher_;
+};
 
 ShiroRenderDesc ToRequest(const RenderRequest& r) {
     ShiroRenderDesc d{};
@@ -174,22 +182,15 @@ ShiroRenderDesc ToRequest(const RenderRequest& r) {
     return d;
 }
 
-struct Planes {
-    std::vector<float> beauty, albedo, normal, depth;
-    explicit Planes(size_t n) : beauty(4 * n), albedo(3 * n), normal(3 * n), depth(n) {}
-    ShiroAovs Aovs() { return ShiroAovs{beauty.data(), albedo.data(), normal.data(), depth.data(), 0, 0}; }
-    void CopyTo(FrameBuffer* fb) const {
-        const uint32_t w = fb->Width(), h = fb->Height();
-        for (uint32_t y = 0; y < h; ++y)
-            for (uint32_t x = 0; x < w; ++x) {
-                const size_t i = static_cast<size_t>(y) * w + x;
-                fb->SetBeauty(x, y, {beauty[4 * i], beauty[4 * i + 1], beauty[4 * i + 2], beauty[4 * i + 3]});
-                fb->SetAlbedo(x, y, {albedo[3 * i], albedo[3 * i + 1], albedo[3 * i + 2]});
-                fb->SetNormal(x, y, {normal[3 * i], normal[3 * i + 1], normal[3 * i + 2]});
-                fb->SetDepth(x, y, depth[i]);
-            }
-    }
-};
+static_assert(sizeof(Vec4f) == 4 * sizeof(float), "Vec4f must be four packed floats");
+
+// The FrameBuffer's own planes as the C ABI's host AOVs: the render writes
+// straight into the vectors Resize sized (FrameBuffer.h exposes them const;
+// the FrameBuffer itself is ours and not const, so writing is well defined).
+ShiroAovs FrameAovs(FrameBuffer& fb) {
+    return ShiroAovs{const_cast<float*>(&fb.Beauty().data()->x), const_cast<float*>(&fb.Albedo().data()->x),
+                     const_cast<float*>(&fb.Normal().data()->x), const_cast<float*>(fb.Depth().data()), 0, 0};
+}
 
 bool Cancelled(const std::atomic<bool>* c) { return c && c->load(std::memory_order_relaxed); }
 
@@ -229,9 +230,15 @@ bool GpuBackend::EnsureRuntime(const render::Scene& scene) const {
             return false;
         }
     }
-    const uint64_t sig = Signature(scene);
+    // The device copy is reused while the snapshot's content is unchanged: the
+    // signature hashes every field the upload reads (what the OptiX backend's
+    // ComputeSceneSignature hashes, OptixBackend.cpp:150-232).  Hydra builds an
+    // edited snapshot as a new Scene that may land at the address just freed
+    // (RenderParam.cpp:614-659), so the address alone cannot identify it.
+    SceneView view(scene);
+    uint64_t sig = 0;
+    shiro_gpu_scene_signature(&view.desc, &sig);
     if (cachedScene_ != &scene || cachedSignature_ != sig) {
-        SceneView view(scene);
         if (shiro_gpu_upload_scene(ctx_, &view.desc) != SHIRO_OK) {
             std::fprintf(stderr, "[shiro gb300] scene upload failed: %s\n", shiro_gpu_last_error(ctx_));
             cachedScene_ = nullptr;
@@ -239,6 +246,7 @@ bool GpuBackend::EnsureRuntime(const render::Scene& scene) const {
         }
         cachedScene_ = &scene;
         cachedSignature_ = sig;
+        ++uploads_;
     }
     return true;
 }
@@ -251,17 +259,22 @@ render::FrameBuffer GpuBackend::RenderSampleBatch(const RenderRequest& request) 
     std::scoped_lock lock(mutex_);
     if (!EnsureRuntime(request.scene)) return frame;
     const ShiroRenderDesc desc = ToRequest(request);
-    Planes planes(static_cast<size_t>(request.settings.width) * request.settings.height);
-    ShiroAovs aovs = planes.Aovs();
+    ShiroAovs aovs = FrameAovs(frame);
     // the wavefront form: the faster one, with frames bit-identical to the
     // one-thread-per-path form's
-    const int rc = shiro_gpu_render_batch(ctx_, &desc, 1, nullptr, &aovs);
+    int rc;
+    {
+        CancelForward cancel(request.cancel);
+        rc = shiro_gpu_render_batch(ctx_, &desc, 1, cancel.Flag(), &aovs);
+    }
+    lastStatus_ = rc;
     if (rc != SHIRO_OK) {
-        std::fprintf(stderr, "[shiro gb300] render failed (%d): %s\n", rc, shiro_gpu_last_error(ctx_));
+        if (rc != SHIRO_ERR_CANCELLED)
+            std::fprintf(stderr, "[shiro gb300] render failed (%d): %s\n", rc, shiro_gpu_last_error(ctx_));
+        frame.Clear();
         return frame;
     }
-    if (Cancelled(request.cancel)) return frame;
-    planes.CopyTo(&frame);
+    if (Cancelled(request.cancel)) frame.Clear();  // RenderParam.cpp:791-798 discards it anyway
     return frame;
 }
 
@@ -280,20 +293,22 @@ std::vector<render::FrameBuffer> GpuBackend::RenderSampleBatches(const std::vect
     std::scoped_lock lock(mutex_);
     if (!EnsureRuntime(requests.front().scene)) return frames;
     std::vector<ShiroRenderDesc> descs;
-    std::vector<Planes> planes;
-    planes.reserve(requests.size());
     std::vector<ShiroAovs> aovs;
-    for (const RenderRequest& r : requests) {
-        descs.push_back(ToRequest(r));
-        planes.emplace_back(static_cast<size_t>(r.settings.width) * r.settings.height);
-        aovs.push_back(planes.back().Aovs());
+    for (size_t i = 0; i < requests.size(); ++i) {
+        descs.push_back(ToRequest(requests[i]));
+        aovs.push_back(FrameAovs(frames[i]));
     }
-    const int rc = shiro_gpu_render_batch(ctx_, descs.data(), static_cast<uint32_t>(descs.size()), nullptr, aovs.data());
+    int rc;
+    {  // one flag for the batch: the first request's (they are one call)
+        CancelForward cancel(requests.front().cancel);
+        rc = shiro_gpu_render_batch(ctx_, descs.data(), static_cast<uint32_t>(descs.size()), cancel.Flag(), aovs.data());
+    }
+    lastStatus_ = rc;
     if (rc != SHIRO_OK) {
-        std::fprintf(stderr, "[shiro gb300] batched render failed (%d): %s\n", rc, shiro_gpu_last_error(ctx_));
-        return frames;
+        if (rc != SHIRO_ERR_CANCELLED)
+            std::fprintf(stderr, "[shiro gb300] batched render failed (%d): %s\n", rc, shiro_gpu_last_error(ctx_));
+        for (render::FrameBuffer& f : frames) f.Clear();
     }
-    for (size_t i = 0; i < requests.size(); ++i) planes[i].CopyTo(&frames[i]);
     return frames;
 }
 
@@ -306,9 +321,15 @@ bool GpuBackend::RenderAndAccumulate(const RenderRequest& request, bool wavefron
         return false;
     }
     const ShiroRenderDesc desc = ToRequest(request);
-    const int rc = shiro_gpu_accum_stage(accum_, &desc, nullptr, wavefront ? 1u : 0u);
+    int rc;
+    {
+        CancelForward cancel(request.cancel);
+        rc = shiro_gpu_accum_stage(accum_, &desc, cancel.Flag(), wavefront ? 1u : 0u);
+    }
+    lastStatus_ = rc;
     if (rc != SHIRO_OK) {
-        std::fprintf(stderr, "[shiro gb300] render failed (%d): %s\n", rc, shiro_gpu_last_error(ctx_));
+        if (rc != SHIRO_ERR_CANCELLED)
+            std::fprintf(stderr, "[shiro gb300] render failed (%d): %s\n", rc, shiro_gpu_last_error(ctx_));
         return false;
     }
     if (Cancelled(request.cancel)) return false;  // RenderParam.cpp:791-798: a cancelled batch is discarded
@@ -325,15 +346,22 @@ render::FrameBuffer GpuBackend::ResolveAccumulation() const {
     uint32_t samples = 0, w = 0, h = 0;
     if (!accum_ || shiro_gpu_accum_info(accum_, &samples, &w, &h) != SHIRO_OK) return frame;
     frame.Resize(w, h);
-    Planes planes(static_cast<size_t>(w) * h);
-    ShiroAovs aovs = planes.Aovs();
+    ShiroAovs aovs = FrameAovs(frame);
     if (shiro_gpu_accum_resolve(accum_, &aovs) != SHIRO_OK) {
         std::fprintf(stderr, "[shiro gb300] resolve failed: %s\n", shiro_gpu_last_error(ctx_));
         frame.Clear();
-        return frame;
     }
-    planes.CopyTo(&frame);
     return frame;
+}
+
+int GpuBackend::LastStatus() const {
+    std::scoped_lock lock(mutex_);
+    return lastStatus_;
+}
+
+uint64_t GpuBackend::SceneUploads() const {
+    std::scoped_lock lock(mutex_);
+    return uploads_;
 }
 
 uint32_t GpuBackend::AccumulatedSampleCount() const {

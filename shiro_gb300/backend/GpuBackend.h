@@ -50,6 +50,13 @@ public:
     // FrameAccumulator::SampleCount.
     uint32_t AccumulatedSampleCount() const;
 
+    // Status code of the last render call (SHIRO_OK, SHIRO_ERR_CANCELLED, ...):
+    // the reference reports failures on stderr only; this lets a caller tell a
+    // cancelled batch from a failed one.
+    int LastStatus() const;
+    // Scene uploads so far (a changed snapshot is uploaded again).
+    uint64_t SceneUploads() const;
+
 private:
     bool EnsureRuntime(const render::Scene& scene) const;
 
@@ -61,6 +68,8 @@ private:
     mutable bool runtimeFailed_ = false;
     mutable const render::Scene* cachedScene_ = nullptr;
     mutable uint64_t cachedSignature_ = 0;
+    mutable int lastStatus_ = 0;
+    mutable uint64_t uploads_ = 0;
 };
 
 }  // namespace shiro::backend::gb300

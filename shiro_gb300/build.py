@@ -61,12 +61,13 @@ def _run(cmd: list, verbose: bool):
 
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    # CUDA translation units and the host-only ones (the image reader)
+    cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     deps = _deps()
     objs = []
     jobs = []
     for src in cu:
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + deps):
             jobs.append([nvcc()] + NVFLAGS + ["-c", src, "-o", obj])

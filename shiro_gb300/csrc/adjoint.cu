@@ -444,11 +444,13 @@ int adjoint_set_params(ContextImpl* ctx, const float* base, const float* rough, 
     if (env) {
         const int32_t e0 = dome0_env(ctx);
         if (e0 < 0) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "dome light 0 has no environment texture");
-        EnvHost& eh = ctx->envHost[e0];
-        cudaError_t e = cudaMemcpyAsync(eh.rgb.data(), env, eh.rgb.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "read env params");
-        const int rc = upload_envs(ctx);  // texels + rebuilt importance table
+        const DevEnv& de = ctx->envDev[e0];
+        const uint64_t n = static_cast<uint64_t>(de.w) * de.h;
+        // resident texels take the new radiance (masses are rebuilt below)
+        k_rgb_to_texels<<<grid(n, 256), 256, 0, ctx->stream>>>(env, const_cast<float4*>(de.texels), static_cast<uint32_t>(n));
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "set env params");
+        const int rc = finish_env(ctx, static_cast<size_t>(e0));  // rebuilt importance table + sample records
         if (rc != SHIRO_OK) return rc;
     }
     const cudaError_t e = cudaStreamSynchronize(ctx->stream);

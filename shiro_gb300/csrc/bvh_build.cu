@@ -161,7 +161,7 @@ __global__ void k_bottom_up(int n, const uint32_t* __restrict__ sortedPrim, cons
                             const int2* __restrict__ child, const int* __restrict__ nodeParent,
                             const int* __restrict__ leafParent, unsigned int* __restrict__ arrivals,
                             float4* __restrict__ nodeBox, float* __restrict__ nodeCost, int* __restrict__ nodeCount,
-                            uint8_t* __restrict__ collapse, int maxLeaf) {
+                            uint8_t* __restrict__ collapse, int maxLeaf, const uint8_t* __restrict__ noCollapse) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int node = leafParent[j];
@@ -196,7 +196,9 @@ __global__ void k_bottom_up(int n, const uint32_t* __restrict__ sortedPrim, cons
         const int count = cnt[0] + cnt[1];
         const float split = kCostNode * area + cost[0] + cost[1];
         const float leaf = kCostTri * area * static_cast<float>(count);
-        const bool asLeaf = count <= maxLeaf && leaf <= split;
+        // a node of the SAH top spans clusters that need not be adjacent in
+        // the triangle array, so it never becomes a (contiguous) leaf
+        const bool asLeaf = count <= maxLeaf && leaf <= split && !(noCollapse && noCollapse[node]);
         nodeBox[2 * node] = make_float4(u.lo[0], u.lo[1], u.lo[2], 0.0f);
         nodeBox[2 * node + 1] = make_float4(u.hi[0], u.hi[1], u.hi[2], 0.0f);
         nodeCount[node] = count;
@@ -204,6 +206,307 @@ __global__ void k_bottom_up(int n, const uint32_t* __restrict__ sortedPrim, cons
         collapse[node] = asLeaf ? 1 : 0;
         node = nodeParent[node];
     }
+}
+
+// ---- binned-SAH top (HLBVH style) -------------------------------------------
+// Subtrees of the Morton tree with at most `clusterSize` triangles are kept as
+// they are ("clusters"); the tree above them is rebuilt top-down by binned
+// SAH over the clusters' boxes (16 bins per axis, one block per node being
+// split, level by level).  The rebuilt top reuses the Karras node slots of
+// the old top (a binary tree over C clusters has C - 1 internal nodes either
+// way), so boxes, SAH leaf collapse, emission and the wide collapse run
+// unchanged afterwards.  Splits are chosen and partitions written in a fixed
+// order, so the build is deterministic.
+constexpr int kSahBins = 16;
+constexpr int kSahBlock = 256;
+
+// Top nodes (more than clusterSize triangles) and, at each cluster's first
+// sorted position, the cluster's root (internal node or ~leaf position).
+__global__ void k_mark_clusters(int nInternal, int m, const int2* __restrict__ range, const int* __restrict__ nodeParent,
+                                const int* __restrict__ leafParent, int clusterSize, uint8_t* __restrict__ top,
+                                uint32_t* __restrict__ topFlag, uint32_t* __restrict__ startFlag, int* __restrict__ rootAt) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    auto size = [&](int node) { return range[node].y - range[node].x + 1; };
+    if (k < nInternal) {
+        const int sz = size(k);
+        top[k] = sz > clusterSize ? 1 : 0;
+        topFlag[k] = sz > clusterSize ? 1u : 0u;
+        const int p = nodeParent[k];
+        if (sz <= clusterSize && (p < 0 || size(p) > clusterSize)) {
+            startFlag[range[k].x] = 1u;
+            rootAt[range[k].x] = k;
+        }
+    }
+    if (k < m && size(leafParent[k]) > clusterSize) {  // a single triangle hanging off the top
+        startFlag[k] = 1u;
+        rootAt[k] = ~k;
+    }
+}
+
+struct SahItem {
+    float lo[3], hi[3];
+    int ref;        // cluster root: internal node >= 0, ~leaf position < 0
+    float weight;   // triangles
+};
+
+__global__ void k_gather_clusters(int m, const uint32_t* __restrict__ startFlag, const uint32_t* __restrict__ startPos,
+                                  const int* __restrict__ rootAt, const float4* __restrict__ nodeBox,
+                                  const int* __restrict__ nodeCount, const uint32_t* __restrict__ sortedPrim,
+                                  const float4* __restrict__ primBox, SahItem* __restrict__ items,
+                                  uint32_t* __restrict__ perm) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= m || !startFlag[p]) return;
+    const uint32_t c = startPos[p];
+    const int ref = rootAt[p];
+    SahItem it;
+    float4 a, b;
+    if (ref >= 0) {
+        a = nodeBox[2 * ref];
+        b = nodeBox[2 * ref + 1];
+        it.weight = static_cast<float>(nodeCount[ref]);
+    } else {
+        const uint32_t prim = sortedPrim[~ref];
+        a = primBox[2 * prim];
+        b = primBox[2 * prim + 1];
+        it.weight = 1.0f;
+    }
+    it.lo[0] = a.x; it.lo[1] = a.y; it.lo[2] = a.z;
+    it.hi[0] = b.x; it.hi[1] = b.y; it.hi[2] = b.z;
+    it.ref = ref;
+    items[c] = it;
+    perm[c] = c;
+}
+
+__global__ void k_top_slots(int nInternal, const uint32_t* __restrict__ top, const uint32_t* __restrict__ topPos,
+                            int* __restrict__ slots) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nInternal && top[k]) slots[topPos[k]] = k;
+}
+
+struct SahTask {
+    uint32_t begin, end;  // range of perm
+    uint32_t node;        // SAH node id (0 = root)
+    uint32_t pad;
+};
+
+// What a split produced: per side either a cluster (one item) or a new task.
+struct SahResult {
+    uint32_t mid;         // first item of the right side
+    uint32_t pad;
+};
+
+__device__ __forceinline__ float item_centroid(const SahItem& it, int a) { return 0.5f * (it.lo[a] + it.hi[a]); }
+
+// Block-wide exclusive scan of one value per thread (kSahBlock threads).
+__device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* warpSums, uint32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warpSums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < kSahBlock / 32 ? warpSums[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < kSahBlock / 32) warpSums[lane] = w;  // inclusive
+    }
+    __syncthreads();
+    const uint32_t before = (warp > 0 ? warpSums[warp - 1] : 0u) + x - v;
+    *total = warpSums[kSahBlock / 32 - 1];
+    __syncthreads();
+    return before;
+}
+
+__global__ void __launch_bounds__(kSahBlock) k_sah_split(const SahTask* __restrict__ tasks, const SahItem* __restrict__ items,
+                                                        const uint32_t* __restrict__ permIn, uint32_t* __restrict__ permOut,
+                                                        SahResult* __restrict__ results, uint32_t* __restrict__ newTasks) {
+    __shared__ unsigned int cbo[6];
+    __shared__ unsigned int binLo[3][kSahBins][3], binHi[3][kSahBins][3];
+    __shared__ unsigned int binW[3][kSahBins], binN[3][kSahBins];
+    __shared__ float bestCost[3 * (kSahBins - 1)];
+    __shared__ int choice[2];
+    __shared__ uint32_t warpSums[kSahBlock / 32];
+    const SahTask t = tasks[blockIdx.x];
+    const uint32_t n = t.end - t.begin;
+    const int tid = threadIdx.x;
+    if (tid < 6) cbo[tid] = tid < 3 ? 0xffffffffu : 0u;
+    for (int e = tid; e < 3 * kSahBins * 3; e += kSahBlock) {
+        (&binLo[0][0][0])[e] = 0xffffffffu;
+        (&binHi[0][0][0])[e] = 0u;
+    }
+    for (int e = tid; e < 3 * kSahBins; e += kSahBlock) {
+        (&binW[0][0])[e] = 0u;
+        (&binN[0][0])[e] = 0u;
+    }
+    __syncthreads();
+    // centroid bounds of the node's clusters (ordered-integer min / max)
+    {
+        float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (uint32_t i = tid; i < n; i += kSahBlock) {
+            const SahItem& it = items[permIn[t.begin + i]];
+            for (int a = 0; a < 3; ++a) {
+                const float c = item_centroid(it, a);
+                lo[a] = fminf(lo[a], c);
+                hi[a] = fmaxf(hi[a], c);
+            }
+        }
+        for (int a = 0; a < 3; ++a) {
+            for (int o = 16; o > 0; o >>= 1) {
+                lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+                hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+            }
+            if ((tid & 31) == 0) {
+                atomicMin(&cbo[a], f2ord(lo[a]));
+                atomicMax(&cbo[3 + a], f2ord(hi[a]));
+            }
+        }
+    }
+    __syncthreads();
+    float clo[3], cext[3];
+    for (int a = 0; a < 3; ++a) {
+        clo[a] = ord2f(cbo[a]);
+        cext[a] = ord2f(cbo[3 + a]) - clo[a];
+    }
+    // binning: item weight and box per bin and axis
+    for (uint32_t i = tid; i < n; i += kSahBlock) {
+        const SahItem& it = items[permIn[t.begin + i]];
+        for (int a = 0; a < 3; ++a) {
+            if (!(cext[a] > 0.0f)) continue;
+            int b = static_cast<int>(kSahBins * ((item_centroid(it, a) - clo[a]) / cext[a]));
+            b = b < 0 ? 0 : (b >= kSahBins ? kSahBins - 1 : b);
+            atomicAdd(&binW[a][b], static_cast<unsigned int>(it.weight));
+            atomicAdd(&binN[a][b], 1u);
+            for (int k = 0; k < 3; ++k) {
+                atomicMin(&binLo[a][b][k], f2ord(it.lo[k]));
+                atomicMax(&binHi[a][b][k], f2ord(it.hi[k]));
+            }
+        }
+    }
+    __syncthreads();
+    // SAH cost of every split plane: area(left) * weight(left) + area(right) * weight(right)
+    if (tid < 3 * (kSahBins - 1)) {
+        const int a = tid / (kSahBins - 1), sp = tid % (kSahBins - 1);
+        float l[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, h[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        float r[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, g[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        unsigned int nl = 0, nr = 0, wl = 0, wr = 0;
+        for (int b = 0; b < kSahBins; ++b) {
+            if (binN[a][b] == 0u) continue;
+            float* bl = b <= sp ? l : r;
+            float* bh = b <= sp ? h : g;
+            for (int k = 0; k < 3; ++k) {
+                bl[k] = fminf(bl[k], ord2f(binLo[a][b][k]));
+                bh[k] = fmaxf(bh[k], ord2f(binHi[a][b][k]));
+            }
+            if (b <= sp) { wl += binW[a][b]; nl += binN[a][b]; } else { wr += binW[a][b]; nr += binN[a][b]; }
+        }
+        float cost = FLT_MAX;
+        if (cext[a] > 0.0f && nl > 0u && nr > 0u) {
+            const float al = 2.0f * ((h[0] - l[0]) * (h[1] - l[1]) + (h[1] - l[1]) * (h[2] - l[2]) + (h[2] - l[2]) * (h[0] - l[0]));
+            const float ar = 2.0f * ((g[0] - r[0]) * (g[1] - r[1]) + (g[1] - r[1]) * (g[2] - r[2]) + (g[2] - r[2]) * (g[0] - r[0]));
+            cost = al * static_cast<float>(wl) + ar * static_cast<float>(wr);
+        }
+        bestCost[tid] = cost;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int best = -1;
+        float bc = FLT_MAX;
+        for (int k = 0; k < 3 * (kSahBins - 1); ++k)
+            if (bestCost[k] < bc) {  // first of equal costs: lowest axis, lowest plane
+                bc = bestCost[k];
+                best = k;
+            }
+        choice[0] = best < 0 ? -1 : best / (kSahBins - 1);
+        choice[1] = best < 0 ? 0 : best % (kSahBins - 1);
+    }
+    __syncthreads();
+    const int axis = choice[0], plane = choice[1];
+    // stable partition: left side first, each side in its input order; with
+    // no usable plane (all centroids in one bin) the range splits in the
+    // middle of its Morton order
+    const uint32_t half = n / 2u;
+    auto goesLeft = [&](uint32_t i, const SahItem& it) {
+        if (axis < 0) return i < half;
+        int b = static_cast<int>(kSahBins * ((item_centroid(it, axis) - clo[axis]) / cext[axis]));
+        b = b < 0 ? 0 : (b >= kSahBins ? kSahBins - 1 : b);
+        return b <= plane;
+    };
+    uint32_t leftBase = 0, rightBase = 0, nLeft = 0;
+    {
+        uint32_t cnt = 0;
+        for (uint32_t i = tid; i < n; i += kSahBlock) cnt += goesLeft(i, items[permIn[t.begin + i]]) ? 1u : 0u;
+        uint32_t tot;
+        block_scan(cnt, warpSums, &tot);
+        nLeft = tot;
+    }
+    for (uint32_t base = 0; base < n; base += kSahBlock) {
+        const uint32_t i = base + tid;
+        const bool valid = i < n;
+        const uint32_t v = valid ? permIn[t.begin + i] : 0u;
+        const bool left = valid && goesLeft(i, items[v]);
+        uint32_t totL, totR;
+        const uint32_t rl = block_scan(left ? 1u : 0u, warpSums, &totL);
+        const uint32_t rr = block_scan((valid && !left) ? 1u : 0u, warpSums, &totR);
+        if (valid) permOut[t.begin + (left ? leftBase + rl : nLeft + rightBase + rr)] = v;
+        leftBase += totL;
+        rightBase += totR;
+    }
+    if (tid == 0) {
+        const uint32_t mid = t.begin + nLeft;
+        results[blockIdx.x] = SahResult{mid, 0u};
+        newTasks[blockIdx.x] = (nLeft > 1u ? 1u : 0u) + (n - nLeft > 1u ? 1u : 0u);
+    }
+}
+
+// Children of the level's tasks: a side of one item is a cluster, a larger
+// side a new task whose SAH node id follows the ids handed out so far.
+__global__ void k_sah_children(const SahTask* __restrict__ tasks, uint32_t count, const SahResult* __restrict__ results,
+                               const uint32_t* __restrict__ taskPos, uint32_t nextId, const uint32_t* __restrict__ perm,
+                               const SahItem* __restrict__ items, SahTask* __restrict__ next, int2* __restrict__ sahChild) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const SahTask t = tasks[k];
+    const SahResult r = results[k];
+    uint32_t pos = taskPos[k];
+    int link[2];
+    const uint32_t b[2] = {t.begin, r.mid}, e[2] = {r.mid, t.end};
+    for (int q = 0; q < 2; ++q) {
+        if (e[q] - b[q] == 1u) {
+            link[q] = ~static_cast<int>(perm[b[q]]);  // cluster (item index)
+        } else {
+            const uint32_t id = nextId + pos;
+            next[pos] = SahTask{b[q], e[q], id, 0u};
+            link[q] = static_cast<int>(id);
+            ++pos;
+        }
+    }
+    sahChild[t.node] = make_int2(link[0], link[1]);
+}
+
+// The SAH top written into the Karras arrays: SAH node i lives in top slot
+// slots[i]; a cluster child is the cluster's root node (or leaf).
+__global__ void k_sah_link(uint32_t nSah, const int2* __restrict__ sahChild, const int* __restrict__ slots,
+                           const SahItem* __restrict__ items, int2* __restrict__ child, int* __restrict__ nodeParent,
+                           int* __restrict__ leafParent) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nSah) return;
+    const int slot = slots[i];
+    const int2 c = sahChild[i];
+    const int cs[2] = {c.x, c.y};
+    int out[2];
+    for (int q = 0; q < 2; ++q) {
+        const int ref = cs[q] >= 0 ? slots[cs[q]] : items[~cs[q]].ref;
+        out[q] = ref;
+        if (ref >= 0) nodeParent[ref] = slot;
+        else leafParent[~ref] = slot;
+    }
+    child[slot] = make_int2(out[0], out[1]);
+    if (i == 0) nodeParent[slot] = -1;
 }
 
 // A node is emitted when neither it nor any ancestor became a leaf.
@@ -308,6 +611,104 @@ inline unsigned blocks(size_t n, unsigned b) { return static_cast<unsigned>((n +
 
 }  // namespace
 
+// Rebuilds the Morton tree's top above its clusters by binned SAH (kernels
+// above).  *topOut marks the rebuilt nodes (never collapsed into leaves).
+static int sah_top(Scratch& sc, int m, int nInternal, int clusterSize, const uint32_t* sortedPrim, const float4* primBox,
+            int2* child, const int2* range, int* nodeParent, int* leafParent, const float4* nodeBox,
+            const int* nodeCount, uint8_t** topOut, cudaStream_t stream, std::string& err) {
+    uint8_t* top = nullptr;
+    uint32_t *topFlag = nullptr, *topPos = nullptr, *startFlag = nullptr, *startPos = nullptr;
+    int* rootAt = nullptr;
+    BVH_CHECK(sc.alloc(&top, nInternal));
+    BVH_CHECK(sc.alloc(&topFlag, nInternal));
+    BVH_CHECK(sc.alloc(&topPos, nInternal));
+    BVH_CHECK(sc.alloc(&startFlag, m));
+    BVH_CHECK(sc.alloc(&startPos, m));
+    BVH_CHECK(sc.alloc(&rootAt, m));
+    BVH_CHECK(cudaMemsetAsync(startFlag, 0, sizeof(uint32_t) * m, stream));
+    k_mark_clusters<<<blocks(std::max(nInternal, m), 256), 256, 0, stream>>>(nInternal, m, range, nodeParent, leafParent,
+                                                                            clusterSize, top, topFlag, startFlag, rootAt);
+    BVH_CHECK(cudaGetLastError());
+    size_t need = 0, tmpBytes = 0;
+    BVH_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, need, startFlag, startPos, m, stream));
+    tmpBytes = std::max(tmpBytes, need);
+    BVH_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, need, topFlag, topPos, nInternal, stream));
+    tmpBytes = std::max(tmpBytes, need);
+    uint8_t* tmp = nullptr;
+    BVH_CHECK(sc.alloc(&tmp, tmpBytes));
+    BVH_CHECK(cub::DeviceScan::ExclusiveSum(tmp, tmpBytes, startFlag, startPos, m, stream));
+    BVH_CHECK(cub::DeviceScan::ExclusiveSum(tmp, tmpBytes, topFlag, topPos, nInternal, stream));
+    uint32_t h4[4];
+    BVH_CHECK(cudaMemcpyAsync(&h4[0], startPos + m - 1, 4, cudaMemcpyDeviceToHost, stream));
+    BVH_CHECK(cudaMemcpyAsync(&h4[1], startFlag + m - 1, 4, cudaMemcpyDeviceToHost, stream));
+    BVH_CHECK(cudaMemcpyAsync(&h4[2], topPos + nInternal - 1, 4, cudaMemcpyDeviceToHost, stream));
+    BVH_CHECK(cudaMemcpyAsync(&h4[3], topFlag + nInternal - 1, 4, cudaMemcpyDeviceToHost, stream));
+    BVH_CHECK(cudaStreamSynchronize(stream));
+    const uint32_t clusters = h4[0] + h4[1], tops = h4[2] + h4[3];
+    if (clusters < 2 || tops + 1u != clusters) {
+        err = "binned-SAH top: inconsistent cluster cut";
+        return SHIRO_ERR_DEVICE_CHECK;
+    }
+    SahItem* items = nullptr;
+    uint32_t *perm[2] = {nullptr, nullptr}, *newTasks = nullptr, *taskPos = nullptr;
+    int* slots = nullptr;
+    SahTask* tasks[2] = {nullptr, nullptr};
+    SahResult* results = nullptr;
+    int2* sahChild = nullptr;
+    BVH_CHECK(sc.alloc(&items, clusters));
+    BVH_CHECK(sc.alloc(&perm[0], clusters));
+    BVH_CHECK(sc.alloc(&perm[1], clusters));
+    BVH_CHECK(sc.alloc(&slots, tops));
+    BVH_CHECK(sc.alloc(&tasks[0], clusters));
+    BVH_CHECK(sc.alloc(&tasks[1], clusters));
+    BVH_CHECK(sc.alloc(&results, clusters));
+    BVH_CHECK(sc.alloc(&newTasks, clusters));
+    BVH_CHECK(sc.alloc(&taskPos, clusters));
+    BVH_CHECK(sc.alloc(&sahChild, tops));
+    k_gather_clusters<<<blocks(m, 256), 256, 0, stream>>>(m, startFlag, startPos, rootAt, nodeBox, nodeCount, sortedPrim,
+                                                           primBox, items, perm[0]);
+    k_top_slots<<<blocks(nInternal, 256), 256, 0, stream>>>(nInternal, topFlag, topPos, slots);
+    BVH_CHECK(cudaGetLastError());
+    const SahTask root{0u, clusters, 0u, 0u};
+    BVH_CHECK(cudaMemcpyAsync(tasks[0], &root, sizeof(root), cudaMemcpyHostToDevice, stream));
+    BVH_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, need, newTasks, taskPos, static_cast<int>(clusters), stream));
+    uint8_t* scanTmp = nullptr;
+    BVH_CHECK(sc.alloc(&scanTmp, need));
+    const size_t scanBytes = need;
+    uint32_t count = 1, nextId = 1;
+    int cur = 0, pin = 0;
+    for (int level = 0; count > 0; ++level) {
+        if (level > 64) {
+            err = "binned-SAH top deeper than 64 levels";
+            return SHIRO_ERR_DEVICE_CHECK;
+        }
+        k_sah_split<<<count, kSahBlock, 0, stream>>>(tasks[cur], items, perm[pin], perm[pin ^ 1], results, newTasks);
+        BVH_CHECK(cudaGetLastError());
+        size_t sb = scanBytes;
+        BVH_CHECK(cub::DeviceScan::ExclusiveSum(scanTmp, sb, newTasks, taskPos, static_cast<int>(count), stream));
+        uint32_t lastPos = 0, lastNew = 0;
+        BVH_CHECK(cudaMemcpyAsync(&lastPos, taskPos + count - 1, 4, cudaMemcpyDeviceToHost, stream));
+        BVH_CHECK(cudaMemcpyAsync(&lastNew, newTasks + count - 1, 4, cudaMemcpyDeviceToHost, stream));
+        BVH_CHECK(cudaStreamSynchronize(stream));
+        const uint32_t made = lastPos + lastNew;
+        k_sah_children<<<blocks(count, 128), 128, 0, stream>>>(tasks[cur], count, results, taskPos, nextId, perm[pin ^ 1],
+                                                               items, tasks[cur ^ 1], sahChild);
+        BVH_CHECK(cudaGetLastError());
+        nextId += made;
+        count = made;
+        cur ^= 1;
+        pin ^= 1;
+    }
+    if (nextId != tops) {
+        err = "binned-SAH top: node count mismatch";
+        return SHIRO_ERR_DEVICE_CHECK;
+    }
+    k_sah_link<<<blocks(tops, 128), 128, 0, stream>>>(tops, sahChild, slots, items, child, nodeParent, leafParent);
+    BVH_CHECK(cudaGetLastError());
+    *topOut = top;
+    return SHIRO_OK;
+}
+
 int build_bvh(const BvhInput& in, cudaStream_t stream, BvhOutput* out, std::string& err) {
     const uint32_t m = in.smallCount;
     const uint32_t L = static_cast<uint32_t>(in.largeSlots.size());
@@ -388,7 +789,19 @@ int build_bvh(const BvhInput& in, cudaStream_t stream, BvhOutput* out, std::stri
                                                                   leafParent);
             k_bottom_up<<<blocks(m, 256), 256, 0, stream>>>(static_cast<int>(m), sortedPrim, in.primBoxes, child, nodeParent,
                                                              leafParent, arrivals, nodeBox, nodeCost, nodeCount, collapse,
-                                                             static_cast<int>(in.maxLeaf));
+                                                             static_cast<int>(in.maxLeaf), nullptr);
+            BVH_CHECK(cudaGetLastError());
+            if (in.sahClusterSize > 0 && m > in.sahClusterSize) {
+                uint8_t* top = nullptr;
+                int rc = sah_top(sc, static_cast<int>(m), nInternal, static_cast<int>(in.sahClusterSize), sortedPrim,
+                                 in.primBoxes, child, range, nodeParent, leafParent, nodeBox, nodeCount, &top, stream, err);
+                if (rc != SHIRO_OK) return rc;
+                // boxes, counts, SAH costs and leaf decisions again, over the new top
+                BVH_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(unsigned int) * nInternal, stream));
+                k_bottom_up<<<blocks(m, 256), 256, 0, stream>>>(static_cast<int>(m), sortedPrim, in.primBoxes, child,
+                                                                 nodeParent, leafParent, arrivals, nodeBox, nodeCost,
+                                                                 nodeCount, collapse, static_cast<int>(in.maxLeaf), top);
+            }
             k_emit_flags<<<blocks(nInternal, 256), 256, 0, stream>>>(nInternal, nodeParent, collapse, flag, maxDepth);
             BVH_CHECK(cudaGetLastError());
             size_t scanBytes = 0;

@@ -23,6 +23,10 @@ struct BvhInput {
     uint32_t smallCount;
     std::vector<LargeTri> largeSlots;  // at most 8
     uint32_t maxLeaf = 8;              // largest SAH leaf (1..8)
+    // > 0: the Morton tree's subtrees of at most this many triangles are kept
+    // as clusters and the tree above them is rebuilt by binned SAH; 0: the
+    // Morton (LBVH) hierarchy throughout
+    uint32_t sahClusterSize = 0;
 };
 
 struct BvhOutput {

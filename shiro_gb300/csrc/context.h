@@ -22,10 +22,13 @@ struct DeviceBlock {
 struct EnvHost {
     uint32_t w = 0, h = 0;
     bool latlong = true;
-    std::vector<float> rgb;  // w * h * 3
-    std::vector<float> rowCdf, condCdf;
-    std::vector<float> mass;  // rowMass * columnMass per texel
+    std::vector<float> rgb;  // w * h * 3, as uploaded
 };
+
+// Default cluster size of the binned-SAH top (shiro_gpu_set_bvh_build):
+// measured on the 1.31 M-triangle field frame, 8 gave the fewest node visits
+// (binary 69.8 -> 65.1, wide 26.2 -> 25.5 per path; 16 and up fewer gains).
+constexpr uint32_t kDefaultSahCluster = 8;
 
 struct WavefrontState;
 struct AdjointState;
@@ -55,12 +58,20 @@ struct ContextImpl {
     // in the wavefront stages and the binary one in the one-thread-per-path
     // kernels (each measured faster there on GB300)
     uint32_t bvhWidth = 0;
+    // triangles per cluster below the binned-SAH top of the binary BVHs built
+    // at the next upload (0: the Morton hierarchy throughout)
+    uint32_t sahClusterSize = kDefaultSahCluster;
 
     // scratch (grown on demand, kept between calls)
     DeviceBlock pathRecords;
     DeviceBlock aovScratch;
     DeviceBlock probeScratch;
     uint32_t* errorWord = nullptr;
+    // device address of the static path-record array of shiro_gpu_render_static
+    // (render_static.cu), looked up when the context is created; staticError
+    // says why it is NULL
+    float4* staticRecords = nullptr;
+    std::string staticError;
 
     // last call statistics
     ShiroRenderStats stats{};
@@ -83,14 +94,45 @@ int cuda_fail(ContextImpl* ctx, cudaError_t e, const char* what);
 DevRequest make_request(const ShiroRenderDesc& r);
 int validate_request(ContextImpl* ctx, const ShiroRenderDesc& r);
 
-// Uploads / refreshes the dome textures of envHost (texels + CDF + alias).
+// Uploads the dome textures of envHost and builds their tables on the device.
 int upload_envs(ContextImpl* ctx);
+// (Re)builds env k's importance tables, texel masses and sample records from
+// its resident texels (after a scene upload or a parameter update).
+int finish_env(ContextImpl* ctx, size_t k);
+// env_tables.cu: the reference importance table, the texel masses (into
+// texels.w) and the alias table of one lat-long texture, on the device.
+int build_env_tables_device(ContextImpl* ctx, DevEnv& d);
 // (Re)computes the per-material BSDF records (after the materials change).
 int build_bsdf_recs(ContextImpl* ctx);
-// Builds the reference importance table (EnvironmentMap.cpp:185-236).
-void build_env_table(EnvHost& e);
 
 int check_device_error(ContextImpl* ctx);
+
+// Launches are asynchronous, so a loop that enqueues a whole frame finishes
+// before the GPU has run any of it and a cancel flag read there is read too
+// early.  Loops that take a cancel flag therefore keep at most a few launches
+// queued: before enqueueing launch k they wait for the event recorded after
+// launch k - depth, polling the flag meanwhile.  Returns true (without
+// waiting further) once the flag is set.
+bool wait_or_cancel(cudaEvent_t ev, const volatile int* cancel);
+
+// A ring of `depth` events for that throttling (created only when a cancel
+// flag is given; every method is a no-op otherwise).
+struct LaunchThrottle {
+    std::vector<cudaEvent_t> ring;
+    uint64_t issued = 0;
+    const volatile int* cancel = nullptr;
+    LaunchThrottle(const volatile int* c, uint32_t depth);
+    ~LaunchThrottle();
+    // Before launch number `issued`: false when the caller should stop (the
+    // flag was set while an earlier launch ran).
+    bool before_launch();
+    // After a launch on `stream`.
+    void after_launch(cudaStream_t stream);
+};
+
+// render_static.cu: sets up the static scratch of shiro_gpu_render_static for
+// the current device (called once per context by shiro_gpu_create).
+void static_scratch_setup(ContextImpl* ctx);
 
 // wavefront.cu / adjoint.cu
 int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t count, const volatile int* cancel,

@@ -145,6 +145,25 @@ __device__ __forceinline__ uint32_t env_cdf_search(const float* cdf, uint32_t be
     return lo - 1u;
 }
 
+// The texel a 2-D sample picks in a lat-long map with an importance table:
+// the CDF search of SampleCdf (row on u.y, column on u.x), or the alias
+// lookup (bucket floor(u.y * n) - exact for a power-of-two n, as u.y * n then
+// only shifts the exponent - accepted when u.x is below its threshold, else
+// its alias).
+__device__ __forceinline__ size_t env_pick(const DevEnv& e, const V2& u, bool useCdf) {
+    if (useCdf) {
+        const uint32_t r = env_cdf_search(e.rowCdf, 0u, e.h, u.y);
+        const uint32_t off = r * (e.w + 1u);
+        const uint32_t c = env_cdf_search(e.condCdf, off, off + e.w, u.x);
+        return static_cast<size_t>(r) * e.w + (c - off);
+    }
+    const uint32_t n = e.w * e.h;
+    uint32_t i = static_cast<uint32_t>(u.y * static_cast<float>(n));
+    i = i >= n ? n - 1u : i;
+    const uint2 a = __ldg(&e.alias[i]);
+    return u.x < __uint_as_float(a.x) ? i : a.y;
+}
+
 // EnvironmentMap::Sample (:109-163).  Returns the radiance; *pdf = 0 marks
 // a failed sample.
 __device__ __forceinline__ V3 env_sample(const DevEnv& e, const V2& u, bool useCdf, V3* dir, float* pdf) {
@@ -156,19 +175,7 @@ __device__ __forceinline__ V3 env_sample(const DevEnv& e, const V2& u, bool useC
     if (e.latlong && e.hasTable) {
         // the texel; its centre direction, pdf (mass rowMass * columnMass)
         // and radiance come from the per-texel sample records
-        size_t t;
-        if (useCdf) {
-            const uint32_t r = env_cdf_search(e.rowCdf, 0u, e.h, u.y);
-            const uint32_t off = r * (e.w + 1u);
-            const uint32_t c = env_cdf_search(e.condCdf, off, off + e.w, u.x);
-            t = static_cast<size_t>(r) * e.w + (c - off);
-        } else {
-            const uint32_t n = e.w * e.h;
-            uint32_t i = static_cast<uint32_t>(u.y * static_cast<float>(n));
-            i = i >= n ? n - 1u : i;
-            const uint2 a = __ldg(&e.alias[i]);
-            t = u.x < __uint_as_float(a.x) ? i : a.y;
-        }
+        const size_t t = env_pick(e, u, useCdf);
         const float4 a = __ldg(&e.samples[2 * t]), b = __ldg(&e.samples[2 * t + 1]);
         *dir = V3{a.x, a.y, a.z};
         *pdf = a.w;

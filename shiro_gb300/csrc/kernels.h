@@ -27,6 +27,17 @@ void launch_plain_paths(const DevScene& s, const DevRequest& q, uint64_t pathBas
 // (CpuPathTracer.cpp:2093-2137).
 void launch_resolve_pixels(const DevRequest& q, uint64_t pixelBase, uint32_t count, const float4* records, AovPtrs aov,
                            cudaStream_t stream);
+// Diagnostics: listed paths of the plain form (10 floats each: radiance,
+// albedo, normal, depth), and the texel a dome texture's sampler picks for
+// explicit 2-D points (with its pdf).
+void launch_render_paths(const DevScene& s, const DevRequest& q, const uint32_t* pixels, const uint32_t* sampleIdx,
+                         uint32_t n, float* out, cudaStream_t stream);
+void launch_env_pick(const DevEnv& e, const float2* u, uint32_t n, bool useCdf, uint32_t* texel, float* pdf,
+                     cudaStream_t stream);
+// Loads the plain-form kernels (both k_plain_paths variants and k_resolve)
+// into the current device's context now: under CUDA's lazy module loading a
+// kernel's code is otherwise placed in device memory at its first launch.
+cudaError_t preload_plain_kernels();
 // out[2k], out[2k+1] = Sampler{px, py, index}.next2d(branch) of tuple k
 // (tuples packed as uint4 px, py, index, branch).
 void launch_sample_probe(const uint4* tuples, uint32_t n, float* out, cudaStream_t stream);

@@ -135,6 +135,41 @@ __global__ void k_sample_probe(const uint4* __restrict__ tuples, uint32_t n, flo
     out[2 * static_cast<size_t>(k) + 1] = v.y;
 }
 
+// Listed paths of the plain form (diagnostic): out[10 i ..] = radiance,
+// albedo, normal, depth of path (pixels[i], sample index sampleIdx[i]).
+template <bool kExt>
+__global__ void __launch_bounds__(128) k_render_paths(const DevScene s, const DevRequest q, const uint32_t* __restrict__ pixels,
+                                                      const uint32_t* __restrict__ sampleIdx, uint32_t n,
+                                                      float* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t y = pixels[i] / q.width, x = pixels[i] - y * q.width;
+    NullCounter ctr;
+    const PathResult r = trace_path<kExt>(s, q, x, y, sampleIdx[i], ctr);
+    float* o = out + 10 * static_cast<size_t>(i);
+    o[0] = r.radiance.x;
+    o[1] = r.radiance.y;
+    o[2] = r.radiance.z;
+    o[3] = r.albedo.x;
+    o[4] = r.albedo.y;
+    o[5] = r.albedo.z;
+    o[6] = r.normal.x;
+    o[7] = r.normal.y;
+    o[8] = r.normal.z;
+    o[9] = r.depth;
+}
+
+// Texel picks of a dome texture for explicit 2-D points (diagnostic).
+__global__ void k_env_pick(const DevEnv e, const float2* __restrict__ u, uint32_t n, uint32_t useCdf,
+                           uint32_t* __restrict__ texel, float* __restrict__ pdf) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 v = u[i];
+    const size_t t = env_pick(e, V2{v.x, v.y}, useCdf != 0u);
+    texel[i] = static_cast<uint32_t>(t);
+    pdf[i] = e.samples[2 * t].w;
+}
+
 inline unsigned grid(uint64_t n, unsigned b) { return static_cast<unsigned>((n + b - 1) / b); }
 
 }  // namespace
@@ -151,6 +186,29 @@ void launch_plain_paths(const DevScene& s, const DevRequest& q, uint64_t pathBas
         k_plain_paths<true><<<grid(count, 128), 128, 0, stream>>>(s, q, pathBase, count, records);
     else
         k_plain_paths<false><<<grid(count, 128), 128, 0, stream>>>(s, q, pathBase, count, records);
+}
+
+void launch_render_paths(const DevScene& s, const DevRequest& q, const uint32_t* pixels, const uint32_t* sampleIdx,
+                         uint32_t n, float* out, cudaStream_t stream) {
+    if (n == 0) return;
+    if (s.extended)
+        k_render_paths<true><<<grid(n, 128), 128, 0, stream>>>(s, q, pixels, sampleIdx, n, out);
+    else
+        k_render_paths<false><<<grid(n, 128), 128, 0, stream>>>(s, q, pixels, sampleIdx, n, out);
+}
+
+void launch_env_pick(const DevEnv& e, const float2* u, uint32_t n, bool useCdf, uint32_t* texel, float* pdf,
+                     cudaStream_t stream) {
+    if (n == 0) return;
+    k_env_pick<<<grid(n, 256), 256, 0, stream>>>(e, u, n, useCdf ? 1u : 0u, texel, pdf);
+}
+
+cudaError_t preload_plain_kernels() {
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, k_plain_paths<false>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_plain_paths<true>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_resolve);
+    return e;
 }
 
 void launch_resolve_pixels(const DevRequest& q, uint64_t pixelBase, uint32_t count, const float4* records, AovPtrs aov,

@@ -6,7 +6,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -14,6 +16,7 @@
 #include <new>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "bvh_build.h"
@@ -191,95 +194,6 @@ int validate_request(ContextImpl* ctx, const ShiroRenderDesc& r) {
     return SHIRO_OK;
 }
 
-// EnvironmentMap::BuildImportanceTable (EnvironmentMap.cpp:185-236), float
-// arithmetic in the reference's order; also records each texel's probability
-// mass rowMass * columnMass (LatLongPdf, :302-313).
-void build_env_table(EnvHost& e) {
-    e.rowCdf.clear();
-    e.condCdf.clear();
-    e.mass.assign(static_cast<size_t>(e.w) * e.h, 0.0f);
-    if (e.w == 0 || e.h == 0 || !e.latlong) return;
-    const uint32_t w = e.w, h = e.h;
-    e.rowCdf.assign(h + 1u, 0.0f);
-    e.condCdf.assign(static_cast<size_t>(h) * (w + 1u), 0.0f);
-    float total = 0.0f;
-    for (uint32_t y = 0; y < h; ++y) {
-        const float theta = (static_cast<float>(y) + 0.5f) * kHostPi / static_cast<float>(h);
-        const float sinT = std::max(std::sin(theta), 1.0e-6f);
-        const size_t off = static_cast<size_t>(y) * (w + 1u);
-        float row = 0.0f;
-        for (uint32_t x = 0; x < w; ++x) {
-            const float* c = &e.rgb[3 * (static_cast<size_t>(y) * w + x)];
-            const float lum = c[0] * 0.2126f + c[1] * 0.7152f + c[2] * 0.0722f;
-            row += std::max(0.0f, lum) * sinT;
-            e.condCdf[off + x + 1u] = row;
-        }
-        if (row > 0.0f) {
-            for (uint32_t x = 1; x <= w; ++x) e.condCdf[off + x] /= row;
-        } else {
-            for (uint32_t x = 1; x <= w; ++x) e.condCdf[off + x] = static_cast<float>(x) / static_cast<float>(w);
-            row = 1.0f;
-        }
-        total += row;
-        e.rowCdf[y + 1u] = total;
-    }
-    if (total <= 0.0f) {
-        for (uint32_t y = 1; y <= h; ++y) e.rowCdf[y] = static_cast<float>(y) / static_cast<float>(h);
-    } else {
-        for (uint32_t y = 1; y <= h; ++y) e.rowCdf[y] /= total;
-    }
-    for (uint32_t y = 0; y < h; ++y) {
-        const float rowMass = e.rowCdf[y + 1u] - e.rowCdf[y];
-        const size_t off = static_cast<size_t>(y) * (w + 1u);
-        for (uint32_t x = 0; x < w; ++x) {
-            const float colMass = e.condCdf[off + x + 1u] - e.condCdf[off + x];
-            e.mass[static_cast<size_t>(y) * w + x] = rowMass * colMass;
-        }
-    }
-}
-
-namespace {
-
-// Walker / Vose alias table over the texel masses: entry i accepts itself
-// when u < threshold[i], else jumps to alias[i].
-std::vector<uint2> build_alias(const std::vector<float>& mass) {
-    const size_t n = mass.size();
-    std::vector<uint2> out(n);
-    double sum = 0.0;
-    for (float m : mass) sum += std::max(0.0f, m);
-    std::vector<double> scaled(n);
-    std::vector<uint32_t> small, large;
-    small.reserve(n);
-    large.reserve(n);
-    for (size_t i = 0; i < n; ++i) {
-        scaled[i] = sum > 0.0 ? std::max(0.0f, mass[i]) / sum * static_cast<double>(n) : 1.0;
-        (scaled[i] < 1.0 ? small : large).push_back(static_cast<uint32_t>(i));
-    }
-    std::vector<float> thr(n, 1.0f);
-    std::vector<uint32_t> alias(n);
-    std::iota(alias.begin(), alias.end(), 0u);
-    while (!small.empty() && !large.empty()) {
-        const uint32_t s = small.back();
-        small.pop_back();
-        const uint32_t l = large.back();
-        large.pop_back();
-        thr[s] = static_cast<float>(scaled[s]);
-        alias[s] = l;
-        scaled[l] = (scaled[l] + scaled[s]) - 1.0;
-        (scaled[l] < 1.0 ? small : large).push_back(l);
-    }
-    for (uint32_t i : large) thr[i] = 1.0f;
-    for (uint32_t i : small) thr[i] = 1.0f;  // rounding leftovers
-    for (size_t i = 0; i < n; ++i) {
-        uint32_t bits;
-        std::memcpy(&bits, &thr[i], 4);
-        out[i] = make_uint2(bits, alias[i]);
-    }
-    return out;
-}
-
-}  // namespace
-
 // Per-texel sample records of a lat-long map (EnvironmentMap::Sample's
 // result for each texel): (centre direction, pdf), (radiance there, 0).
 __global__ void k_env_samples(DevEnv e, float4* out) {
@@ -329,57 +243,98 @@ int build_bsdf_recs(ContextImpl* ctx) {
     return e == cudaSuccess ? SHIRO_OK : cuda_fail(ctx, e, "BSDF records");
 }
 
+int finish_env(ContextImpl* ctx, size_t k) {
+    DevEnv& d = ctx->envDev[k];
+    const size_t n = static_cast<size_t>(d.w) * d.h;
+    if (!d.hasTable) return SHIRO_OK;
+    int rc = build_env_tables_device(ctx, d);
+    if (rc != SHIRO_OK) return rc;
+    if (!d.samples) {
+        DeviceBlock b;
+        if (!ensure_block(ctx, &b, 2 * n * sizeof(float4), "env sample records")) return SHIRO_ERR_OUT_OF_MEMORY;
+        ctx->sceneBlocks.push_back(b);
+        d.samples = static_cast<const float4*>(b.ptr);
+    }
+    k_env_samples<<<static_cast<unsigned>((n + 255) / 256), 256, 0, ctx->stream>>>(d, const_cast<float4*>(d.samples));
+    const cudaError_t err = cudaGetLastError();
+    return err == cudaSuccess ? SHIRO_OK : cuda_fail(ctx, err, "env sample records");
+}
+
 int upload_envs(ContextImpl* ctx) {
-    // env blocks are appended to sceneBlocks; the env table itself is
-    // rewritten in place.
+    // texels go up as (r, g, b, 0); the importance tables, the masses in
+    // texels.w and the per-texel sample records are built on the device
     for (size_t k = 0; k < ctx->envHost.size(); ++k) {
         EnvHost& e = ctx->envHost[k];
-        build_env_table(e);
         const size_t n = static_cast<size_t>(e.w) * e.h;
         std::vector<float4> tex(n);
-        for (size_t i = 0; i < n; ++i) tex[i] = make_float4(e.rgb[3 * i], e.rgb[3 * i + 1], e.rgb[3 * i + 2], e.mass[i]);
+        for (size_t i = 0; i < n; ++i) tex[i] = make_float4(e.rgb[3 * i], e.rgb[3 * i + 1], e.rgb[3 * i + 2], 0.0f);
         DevEnv& d = ctx->envDev[k];
-        const bool fresh = d.texels == nullptr;
-        if (fresh) {
-            int rc;
-            if ((rc = upload(ctx, tex, &d.texels, "env texels")) != SHIRO_OK) return rc;
-            if ((rc = upload(ctx, e.rowCdf, &d.rowCdf, "env row cdf")) != SHIRO_OK) return rc;
-            if ((rc = upload(ctx, e.condCdf, &d.condCdf, "env conditional cdf")) != SHIRO_OK) return rc;
-            const std::vector<uint2> al = e.latlong ? build_alias(e.mass) : std::vector<uint2>();
-            if ((rc = upload(ctx, al, &d.alias, "env alias")) != SHIRO_OK) return rc;
-        } else {
-            cudaError_t err = cudaMemcpyAsync(const_cast<float4*>(d.texels), tex.data(), n * sizeof(float4),
-                                              cudaMemcpyHostToDevice, ctx->stream);
-            if (err == cudaSuccess && !e.rowCdf.empty())
-                err = cudaMemcpyAsync(const_cast<float*>(d.rowCdf), e.rowCdf.data(), e.rowCdf.size() * 4,
-                                      cudaMemcpyHostToDevice, ctx->stream);
-            if (err == cudaSuccess && !e.condCdf.empty())
-                err = cudaMemcpyAsync(const_cast<float*>(d.condCdf), e.condCdf.data(), e.condCdf.size() * 4,
-                                      cudaMemcpyHostToDevice, ctx->stream);
-            const std::vector<uint2> al = e.latlong ? build_alias(e.mass) : std::vector<uint2>();
-            if (err == cudaSuccess && !al.empty())
-                err = cudaMemcpyAsync(const_cast<uint2*>(d.alias), al.data(), al.size() * sizeof(uint2),
-                                      cudaMemcpyHostToDevice, ctx->stream);
-            if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
-            if (err != cudaSuccess) return cuda_fail(ctx, err, "env update");
-        }
         d.w = e.w;
         d.h = e.h;
         d.latlong = e.latlong ? 1u : 0u;
-        d.hasTable = (e.latlong && !e.rowCdf.empty()) ? 1u : 0u;
+        d.hasTable = (e.latlong && n > 0) ? 1u : 0u;
+        int rc;
+        if ((rc = upload(ctx, tex, &d.texels, "env texels")) != SHIRO_OK) return rc;
         if (d.hasTable) {
-            if (!d.samples) {
-                DeviceBlock b;
-                if (!ensure_block(ctx, &b, 2 * n * sizeof(float4), "env sample records")) return SHIRO_ERR_OUT_OF_MEMORY;
-                ctx->sceneBlocks.push_back(b);
-                d.samples = static_cast<const float4*>(b.ptr);
+            DeviceBlock rb, cb, ab;
+            if (!ensure_block(ctx, &rb, (e.h + 1u) * sizeof(float), "env row cdf") ||
+                !ensure_block(ctx, &cb, static_cast<size_t>(e.h) * (e.w + 1u) * sizeof(float), "env conditional cdf") ||
+                !ensure_block(ctx, &ab, n * sizeof(uint2), "env alias")) {
+                for (DeviceBlock* x : {&rb, &cb, &ab}) free_block(x);
+                return SHIRO_ERR_OUT_OF_MEMORY;
             }
-            k_env_samples<<<static_cast<unsigned>((n + 255) / 256), 256, 0, ctx->stream>>>(d, const_cast<float4*>(d.samples));
-            const cudaError_t err = cudaGetLastError();
-            if (err != cudaSuccess) return cuda_fail(ctx, err, "env sample records");
+            for (DeviceBlock* x : {&rb, &cb, &ab}) ctx->sceneBlocks.push_back(*x);
+            d.rowCdf = static_cast<const float*>(rb.ptr);
+            d.condCdf = static_cast<const float*>(cb.ptr);
+            d.alias = static_cast<const uint2*>(ab.ptr);
         }
+        if ((rc = finish_env(ctx, k)) != SHIRO_OK) return rc;
     }
     return SHIRO_OK;
+}
+
+bool wait_or_cancel(cudaEvent_t ev, const volatile int* cancel) {
+    for (;;) {
+        if (cancel && *cancel) return true;
+        const cudaError_t e = cudaEventQuery(ev);
+        if (e != cudaErrorNotReady) {
+            if (e != cudaSuccess) cudaGetLastError();  // reported by the caller's final synchronisation
+            return cancel && *cancel;
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(100));
+    }
+}
+
+LaunchThrottle::LaunchThrottle(const volatile int* c, uint32_t depth) : cancel(c) {
+    if (!cancel) return;
+    ring.resize(std::max(depth, 1u), nullptr);
+    for (cudaEvent_t& e : ring)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            e = nullptr;
+        }
+}
+
+LaunchThrottle::~LaunchThrottle() {
+    for (cudaEvent_t e : ring)
+        if (e) cudaEventDestroy(e);
+}
+
+bool LaunchThrottle::before_launch() {
+    if (!cancel) return true;
+    if (*cancel) return false;
+    if (issued >= ring.size()) {
+        cudaEvent_t e = ring[issued % ring.size()];
+        if (e && wait_or_cancel(e, cancel)) return false;
+    }
+    return true;
+}
+
+void LaunchThrottle::after_launch(cudaStream_t stream) {
+    if (!cancel) return;
+    cudaEvent_t e = ring[issued % ring.size()];
+    if (e) cudaEventRecord(e, stream);
+    ++issued;
 }
 
 int check_device_error(ContextImpl* ctx) {
@@ -420,9 +375,134 @@ int supports(const ShiroSceneDesc* scene, std::string* why) {
     return 1;
 }
 
+// ---- scene signature -------------------------------------------------------
+// 64-bit content hash of a scene descriptor, over everything
+// shiro_gpu_upload_scene reads.  Byte ranges are cut into pieces of at most
+// 4 MiB, each piece is hashed on its own (seeded by its position) - on
+// several host threads when the scene is large - and the piece digests are
+// folded in order, so the value does not depend on the thread count.  A
+// piece is hashed as 8-byte words in four independent lanes with the round of
+// xxHash64 (multiply, rotate, multiply).
+struct HashSpan {
+    const unsigned char* p;
+    size_t n;
+};
+
+inline uint64_t hash_round(uint64_t acc, uint64_t w) {
+    acc += w * 0xC2B2AE3D27D4EB4Full;
+    acc = (acc << 31) | (acc >> 33);
+    return acc * 0x9E3779B185EBCA87ull;
+}
+
+uint64_t hash_piece(const unsigned char* p, size_t n, uint64_t seed) {
+    uint64_t lane[4] = {seed + 0x60EA27EEADC0B5D6ull, seed ^ 0xC2B2AE3D27D4EB4Full, seed, seed - 0x61C8864E7A143579ull};
+    const size_t len = n;
+    uint64_t w[4];
+    while (n >= 32) {
+        std::memcpy(w, p, 32);
+        for (int k = 0; k < 4; ++k) lane[k] = hash_round(lane[k], w[k]);
+        p += 32;
+        n -= 32;
+    }
+    while (n >= 8) {
+        std::memcpy(w, p, 8);
+        lane[0] = hash_round(lane[0], w[0]);
+        p += 8;
+        n -= 8;
+    }
+    uint64_t tail = 0;
+    std::memcpy(&tail, p, n);
+    lane[1] = hash_round(lane[1], tail ^ (static_cast<uint64_t>(n) << 56));
+    uint64_t h = len;
+    for (uint64_t l : lane) h = hash_round(h ^ hash_round(0, l), 0x9E3779B97F4A7C15ull);
+    h ^= h >> 33;
+    h *= 0xC2B2AE3D27D4EB4Full;
+    h ^= h >> 29;
+    return h;
+}
+
+template <typename T>
+void put(std::vector<unsigned char>& b, const T& v) {
+    const unsigned char* p = reinterpret_cast<const unsigned char*>(&v);
+    b.insert(b.end(), p, p + sizeof(T));
+}
+
+uint64_t scene_signature(const ShiroSceneDesc& sd) {
+    // every scalar field first (counts, materials, lights, dome frames, sizes),
+    // then the large arrays
+    std::vector<unsigned char> head;
+    put(head, sd.material_count);
+    if (sd.material_count && sd.materials)
+        head.insert(head.end(), reinterpret_cast<const unsigned char*>(sd.materials),
+                    reinterpret_cast<const unsigned char*>(sd.materials + sd.material_count));
+    put(head, sd.mesh_count);
+    std::vector<HashSpan> spans;
+    for (uint32_t i = 0; i < sd.mesh_count && sd.meshes; ++i) {
+        const ShiroMeshDesc& m = sd.meshes[i];
+        const uint32_t vc = m.positions ? m.vertex_count : 0u, nc = m.normals ? m.normal_count : 0u,
+                       ic = m.indices ? m.index_count : 0u;
+        put(head, vc);
+        put(head, nc);
+        put(head, ic);
+        put(head, m.material_index);
+        spans.push_back({reinterpret_cast<const unsigned char*>(m.positions), 12ull * vc});
+        spans.push_back({reinterpret_cast<const unsigned char*>(m.normals), 12ull * nc});
+        spans.push_back({reinterpret_cast<const unsigned char*>(m.indices), 4ull * ic});
+    }
+    put(head, sd.distant_light_count);
+    for (uint32_t i = 0; i < sd.distant_light_count && sd.distant_lights; ++i) put(head, sd.distant_lights[i]);
+    put(head, sd.dome_light_count);
+    for (uint32_t i = 0; i < sd.dome_light_count && sd.dome_lights; ++i) {
+        const ShiroDomeLightDesc& d = sd.dome_lights[i];
+        for (const float* v : {d.radiance, d.right, d.up, d.forward}) head.insert(head.end(), reinterpret_cast<const unsigned char*>(v), reinterpret_cast<const unsigned char*>(v + 3));
+        const uint32_t has = d.env_pixels ? 1u : 0u;
+        put(head, d.layout);
+        put(head, has ? d.env_width : 0u);
+        put(head, has ? d.env_height : 0u);
+        if (has) spans.push_back({reinterpret_cast<const unsigned char*>(d.env_pixels), 12ull * d.env_width * d.env_height});
+    }
+    head.insert(head.end(), reinterpret_cast<const unsigned char*>(sd.environment_top),
+                reinterpret_cast<const unsigned char*>(sd.environment_top + 3));
+    head.insert(head.end(), reinterpret_cast<const unsigned char*>(sd.environment_bottom),
+                reinterpret_cast<const unsigned char*>(sd.environment_bottom + 3));
+    spans.insert(spans.begin(), HashSpan{head.data(), head.size()});
+    constexpr size_t kPiece = 4u << 20;
+    std::vector<HashSpan> pieces;
+    size_t total = 0;
+    for (const HashSpan& sp : spans) {
+        total += sp.n;
+        for (size_t off = 0; off < sp.n; off += kPiece) pieces.push_back({sp.p + off, std::min(kPiece, sp.n - off)});
+        if (sp.n == 0) pieces.push_back({sp.p, 0});
+    }
+    std::vector<uint64_t> dig(pieces.size());
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nt = total < (16u << 20) ? 1 : std::min<size_t>({static_cast<size_t>(hw), pieces.size(), 16});
+    if (nt <= 1) {
+        for (size_t i = 0; i < pieces.size(); ++i) dig[i] = hash_piece(pieces[i].p, pieces[i].n, i);
+    } else {
+        std::atomic<size_t> next{0};
+        std::vector<std::thread> ts;
+        for (size_t t = 0; t < nt; ++t)
+            ts.emplace_back([&]() {
+                for (size_t i = next.fetch_add(1); i < pieces.size(); i = next.fetch_add(1))
+                    dig[i] = hash_piece(pieces[i].p, pieces[i].n, i);
+            });
+        for (auto& t : ts) t.join();
+    }
+    uint64_t h = hash_round(0x27D4EB2F165667C5ull, total);
+    for (uint64_t d : dig) h = hash_round(h, d);
+    return h;
+}
+
 }  // namespace
 
 extern "C" {
+
+int shiro_gpu_scene_signature(const ShiroSceneDesc* scene, uint64_t* out) {
+    if (!scene || !out) return SHIRO_ERR_INVALID_ARGUMENT;
+    *out = scene_signature(*scene);
+    return SHIRO_OK;
+}
 
 int shiro_gpu_status(ShiroBackendStatus* out) {
     if (!out) return SHIRO_ERR_INVALID_ARGUMENT;
@@ -478,6 +558,7 @@ int shiro_gpu_create(int device, ShiroGpuContext** out) {
         return e == cudaErrorMemoryAllocation ? SHIRO_ERR_OUT_OF_MEMORY : SHIRO_ERR_CUDA;
     }
     c.stream = c.ownStream;
+    static_scratch_setup(&c);
     *out = ctx;
     return SHIRO_OK;
 }
@@ -505,6 +586,12 @@ int shiro_gpu_set_bvh_width(ShiroGpuContext* ctx, uint32_t width) {
         c.stats.bvh_nodes = c.scene.nodes8 ? c.node8Count : c.scene.nodeCount;
         c.stats.bvh_depth = c.scene.nodes8 ? c.bvh8Depth : c.bvhDepth;
     }
+    return SHIRO_OK;
+}
+
+int shiro_gpu_set_bvh_build(ShiroGpuContext* ctx, uint32_t sah_cluster_triangles) {
+    if (!ctx || sah_cluster_triangles == 1 || sah_cluster_triangles > (1u << 16)) return SHIRO_ERR_INVALID_ARGUMENT;
+    ctx->impl.sahClusterSize = sah_cluster_triangles;
     return SHIRO_OK;
 }
 
@@ -710,6 +797,7 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     bin.primBoxes = dBox;
     bin.centroids = dCen;
     bin.smallCount = static_cast<uint32_t>(centroids.size());
+    bin.sahClusterSize = ctx->sahClusterSize;
     BvhOutput bout, bwide;
     std::string berr;
     rc = build_bvh(bin, ctx->stream, &bout, berr);
@@ -914,11 +1002,20 @@ int shiro_gpu_render(ShiroGpuContext* handle, const ShiroRenderDesc* req, const 
     cudaEvent_t e0 = new_event();
     cudaEventRecord(e0, ctx->stream);
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pathEv;
+    LaunchThrottle throttle(cancel, 2);  // two chunks queued at most while a cancel flag is polled
     for (uint64_t p0 = 0; p0 < pixels; p0 += pixelsPerChunk) {
-        if (cancel && *cancel) {
+        if (!throttle.before_launch()) {
             cudaStreamSynchronize(ctx->stream);
             drop_events();
             clear_host();
+            if (out->on_device) {  // FrameBuffer::Clear semantics for device planes too
+                cudaMemsetAsync(out->beauty, 0, pixels * 16, ctx->stream);
+                cudaMemsetAsync(out->albedo, 0, pixels * 12, ctx->stream);
+                cudaMemsetAsync(out->normal, 0, pixels * 12, ctx->stream);
+                std::vector<float> inf(pixels, std::numeric_limits<float>::infinity());
+                cudaMemcpyAsync(out->depth, inf.data(), pixels * 4, cudaMemcpyHostToDevice, ctx->stream);
+                cudaStreamSynchronize(ctx->stream);
+            }
             return fail(ctx, SHIRO_ERR_CANCELLED, "cancelled");
         }
         const uint32_t np = static_cast<uint32_t>(std::min(pixelsPerChunk, pixels - p0));
@@ -929,6 +1026,7 @@ int shiro_gpu_render(ShiroGpuContext* handle, const ShiroRenderDesc* req, const 
         cudaEventRecord(b, ctx->stream);
         pathEv.emplace_back(a, b);
         launch_resolve_pixels(q, p0, np, rec, aov, ctx->stream);
+        throttle.after_launch(ctx->stream);
         ctx->stats.kernel_launches += 2;
         ctx->stats.paths += paths;
         const cudaError_t le = cudaGetLastError();
@@ -1123,6 +1221,91 @@ int shiro_gpu_count_work(ShiroGpuContext* handle, const ShiroRenderDesc* req, ui
     out->occlusion_node_visits = h[10];
     out->occlusion_tri_tests = h[11];
     return SHIRO_OK;
+}
+
+int shiro_gpu_env_tables(ShiroGpuContext* handle, uint32_t env, uint32_t* wOut, uint32_t* hOut, float* rowCdf,
+                         float* condCdf, float* mass, uint32_t* aliasThreshold, uint32_t* aliasIndex) {
+    if (!handle) return SHIRO_ERR_INVALID_ARGUMENT;
+    ContextImpl* ctx = &handle->impl;
+    cudaSetDevice(ctx->device);
+    if (!ctx->hasScene) return fail(ctx, SHIRO_ERR_NO_SCENE, "no scene uploaded");
+    if (env >= ctx->envDev.size()) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "no such dome texture");
+    const DevEnv& d = ctx->envDev[env];
+    if (wOut) *wOut = d.w;
+    if (hOut) *hOut = d.h;
+    const size_t n = static_cast<size_t>(d.w) * d.h;
+    const bool table = d.hasTable != 0;
+    if (!table && (rowCdf || condCdf || aliasThreshold || aliasIndex))
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "this dome texture has no importance table (angular layout)");
+    cudaError_t e = cudaSuccess;
+    if (rowCdf) e = cudaMemcpyAsync(rowCdf, d.rowCdf, (d.h + 1u) * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && condCdf)
+        e = cudaMemcpyAsync(condCdf, d.condCdf, static_cast<size_t>(d.h) * (d.w + 1u) * sizeof(float),
+                            cudaMemcpyDeviceToHost, ctx->stream);
+    std::vector<float4> tex(mass ? n : 0);
+    if (e == cudaSuccess && mass)
+        e = cudaMemcpyAsync(tex.data(), d.texels, n * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream);
+    std::vector<uint2> al((aliasThreshold || aliasIndex) ? n : 0);
+    if (e == cudaSuccess && !al.empty())
+        e = cudaMemcpyAsync(al.data(), d.alias, n * sizeof(uint2), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "env table readback");
+    for (size_t i = 0; i < tex.size(); ++i) mass[i] = tex[i].w;
+    for (size_t i = 0; i < al.size(); ++i) {
+        if (aliasThreshold) aliasThreshold[i] = al[i].x;
+        if (aliasIndex) aliasIndex[i] = al[i].y;
+    }
+    return SHIRO_OK;
+}
+
+int shiro_gpu_env_sample(ShiroGpuContext* handle, uint32_t env, uint32_t n, const float* u2, uint32_t flags,
+                         uint32_t* texel, float* pdf) {
+    if (!handle || (n && (!u2 || !texel || !pdf))) return SHIRO_ERR_INVALID_ARGUMENT;
+    ContextImpl* ctx = &handle->impl;
+    cudaSetDevice(ctx->device);
+    if (!ctx->hasScene) return fail(ctx, SHIRO_ERR_NO_SCENE, "no scene uploaded");
+    if (env >= ctx->envDev.size() || !ctx->envDev[env].hasTable)
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "no such dome texture with an importance table");
+    if (n == 0) return SHIRO_OK;
+    if (!ensure_block(ctx, &ctx->probeScratch, static_cast<size_t>(n) * 16, "probe")) return SHIRO_ERR_OUT_OF_MEMORY;
+    float2* du = static_cast<float2*>(ctx->probeScratch.ptr);
+    uint32_t* dt = reinterpret_cast<uint32_t*>(du + n);
+    float* dp = reinterpret_cast<float*>(dt + n);
+    cudaError_t e = cudaMemcpyAsync(du, u2, static_cast<size_t>(n) * 8, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "env sample upload");
+    launch_env_pick(ctx->envDev[env], du, n, (flags & SHIRO_RENDER_ENV_CDF) != 0u, dt, dp, ctx->stream);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(texel, dt, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(pdf, dp, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? SHIRO_OK : cuda_fail(ctx, e, "env sample probe");
+}
+
+int shiro_gpu_render_paths(ShiroGpuContext* handle, const ShiroRenderDesc* req, const uint32_t* pixels, uint32_t n,
+                           const uint32_t* sampleIndex, float* out) {
+    if (!handle || !req || (n && (!pixels || !sampleIndex || !out))) return SHIRO_ERR_INVALID_ARGUMENT;
+    ContextImpl* ctx = &handle->impl;
+    cudaSetDevice(ctx->device);
+    int rc = validate_request(ctx, *req);
+    if (rc != SHIRO_OK) return rc;
+    const uint64_t px = static_cast<uint64_t>(req->settings.width) * req->settings.height;
+    for (uint32_t i = 0; i < n; ++i)
+        if (pixels[i] >= px) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "pixel index out of range");
+    if (n == 0) return SHIRO_OK;
+    if (!ensure_block(ctx, &ctx->probeScratch, static_cast<size_t>(n) * 12 * 4, "probe")) return SHIRO_ERR_OUT_OF_MEMORY;
+    uint32_t* dpx = static_cast<uint32_t*>(ctx->probeScratch.ptr);
+    uint32_t* dsi = dpx + n;
+    float* dout = reinterpret_cast<float*>(dsi + n);
+    cudaError_t e = cudaMemcpyAsync(dpx, pixels, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dsi, sampleIndex, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "render paths upload");
+    launch_render_paths(ctx->scene, make_request(*req), dpx, dsi, n, dout, ctx->stream);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "render paths launch");
+    if ((rc = check_device_error(ctx)) != SHIRO_OK) return rc;
+    e = cudaMemcpyAsync(out, dout, static_cast<size_t>(n) * 40, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? SHIRO_OK : cuda_fail(ctx, e, "render paths readback");
 }
 
 int shiro_gpu_last_stats(const ShiroGpuContext* ctx, ShiroRenderStats* out) {

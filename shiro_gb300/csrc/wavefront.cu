@@ -904,8 +904,12 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront fork");
     }
     uint64_t launches = 0;
+    uint32_t launchedWaves = 0;
+    // with a cancel flag, nl + 1 waves are queued at most, so the flag is read
+    // between waves that ran (a wave takes milliseconds, a launch microseconds)
+    LaunchThrottle throttle(cancel, nl + 1);
     for (uint32_t w = 0; w < used && rc == SHIRO_OK; ++w) {
-        if (cancel && *cancel) {
+        if (!throttle.before_launch()) {
             rc = fail(ctx, SHIRO_ERR_CANCELLED, "cancelled");
             break;
         }
@@ -916,7 +920,9 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             enqueue_wave_timed(L, st, ev);
             e = cudaGetLastError();
         }
+        throttle.after_launch(exec[k] && k != 0 ? wf->side : st);
         launches += 3 + 6ull * L.depth;
+        ++launchedWaves;
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront launch");
     }
     if (nl > 1) {  // join (also after a failed launch: the side stream's work must be done before we return)
@@ -940,6 +946,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
         cudaEventDestroy(x.second.first);
         cudaEventDestroy(x.second.second);
     }
+    ctx->stats.waves = launchedWaves;  // also after a cancel: the waves that ran
     if (rc != SHIRO_OK) {
         cudaStreamSynchronize(st);
         return rc;
@@ -952,7 +959,6 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     ctx->stats.kernel_ms = ms;
     ctx->stats.kernel_launches = launches;
     ctx->stats.paths = paths;
-    ctx->stats.waves = used;
     if (!ev.empty()) {
         for (int k = 0; k < 6; ++k) {
             ctx->stats.stage_ms[k] = stageMs[k];

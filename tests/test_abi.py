@@ -99,3 +99,55 @@ def test_scene_support_on_host(lib):
     assert lib.shiro_gpu_supports_scene(MarshalledScene(sc).ref(), buf, 128) == 1
     assert lib.shiro_gpu_supports_scene(None, buf, 128) == 0
     assert b"null" in buf.value
+
+
+def test_scene_signature_tracks_every_uploaded_field(lib):
+    """shiro_gpu_scene_signature (host code, no device): equal for equal
+    content, different after an in-place edit of any field the upload reads."""
+    import numpy as np
+
+    from shiro_gb300 import scenes
+    from shiro_gb300.abi import DistantLight, MarshalledScene
+
+    def sig(sc):
+        out = C.c_uint64(0)
+        assert lib.shiro_gpu_scene_signature(MarshalledScene(sc).ref(), C.byref(out)) == 0
+        return out.value
+
+    sc = scenes.sphere_scene(env_width=64, env_height=32)
+    sc.distant_lights = [DistantLight(direction=(-0.3, -1.0, -0.4), radiance=(2.5, 2.4, 2.2))]
+    base = sig(sc)
+    assert sig(sc) == base
+    seen = {base}
+
+    def changed(mutate, undo):
+        mutate()
+        s = sig(sc)
+        undo()
+        assert sig(sc) == base
+        assert s not in seen
+        seen.add(s)
+
+    m0 = sc.meshes[0]
+    pos, nrm, idx = m0.positions.copy(), m0.normals.copy(), m0.indices.copy()
+    env = sc.dome_lights[0].env.copy()
+    changed(lambda: sc.distant_lights[0].__setattr__("radiance", (7.0, 3.0, 1.0)),
+            lambda: sc.distant_lights[0].__setattr__("radiance", (2.5, 2.4, 2.2)))
+    changed(lambda: m0.positions.__setitem__((5, 1), m0.positions[5, 1] + 1e-3),
+            lambda: m0.positions.__setitem__(slice(None), pos))
+    changed(lambda: m0.normals.__setitem__((7, 0), 0.5), lambda: m0.normals.__setitem__(slice(None), nrm))
+    changed(lambda: m0.indices.__setitem__(3, m0.indices[4]), lambda: m0.indices.__setitem__(slice(None), idx))
+    changed(lambda: setattr(m0, "material_index", 1), lambda: setattr(m0, "material_index", 0))
+    changed(lambda: setattr(sc.materials[1], "roughness", 0.77), lambda: setattr(sc.materials[1], "roughness", 1.0))
+    changed(lambda: sc.dome_lights[0].env.__setitem__((3, 4, 2), 9.0),
+            lambda: sc.dome_lights[0].env.__setitem__(slice(None), env))
+    changed(lambda: setattr(sc.dome_lights[0], "up", (0.0, 0.0, 1.0)),
+            lambda: setattr(sc.dome_lights[0], "up", (0.0, 1.0, 0.0)))
+    changed(lambda: setattr(sc, "environment_top", (0.1, 0.2, 0.3)),
+            lambda: setattr(sc, "environment_top", (0.0, 0.0, 0.0)))
+    # a scene large enough for the multi-threaded pieces: stable across calls
+    big = scenes.field_scene(instances=48, env_width=1024, env_height=512)
+    a, b = sig(big), sig(big)
+    assert a == b
+    big.meshes[-2].positions[-1, 2] += 1e-3
+    assert sig(big) != a

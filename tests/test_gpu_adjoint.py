@@ -4,9 +4,11 @@ The adjoint holds sampling decisions, pdfs, MIS weights, Russian-roulette
 probabilities (and clamp scales) constant and differentiates the BSDF values
 and environment radiance.  shiro_gpu_render_frozen renders exactly that
 estimator as a function of a second parameter set, so central finite
-differences of it (h = 1e-3, relative for environment texels) must match the
-adjoint to <= 1e-2 relative error on 64 random parameters (clamps disabled so
-the estimator is smooth).  Against finite differences of the plain renderer
+differences of it (Richardson-extrapolated central differences; steps of 1e-3,
+relative for roughness and environment texels) must match the adjoint to
+<= 1e-2 relative error on 64 parameters drawn uniformly among those with a
+nonzero gradient, on a small frame and at the full 256-material,
+512 x 512 x 32 spp configuration, with the reference's clamps off and on.  Against finite differences of the plain renderer
 itself (sampling moves with the parameters) the agreement is statistical.
 """
 import numpy as np
@@ -75,49 +77,111 @@ def _loss(d, img):
     return float((d.double() * img.double()).sum())
 
 
-def test_adjoint_matches_frozen_finite_differences(setup):
-    gpu, scene, cam, st, p = setup
-    gpu.set_params(**p)
-    gen = torch.Generator(device="cpu").manual_seed(7)
-    d = torch.rand((st.height, st.width, 4), generator=gen) - 0.3
-    d[..., 3] = 0.0
-    d = d.cuda()
-    grads = {k: torch.zeros_like(v) for k, v in p.items()}
-    gpu.adjoint(cam, st, d, grads, flags=NO_CLAMP)
+def _step(name, val):
+    """Central-difference step: 1e-3 for base colour and metalness; for
+    roughness 1e-3 of the value (at least 5e-5), so the GGX width alpha = r^2
+    moves by 0.2 % even for the sharpest lobes (a fixed 1e-3 on r = 0.18 is
+    1 % of alpha and the difference quotient no longer converged there);
+    1e-3 relative for environment texels."""
+    if name == "roughness":
+        return max(1e-3 * abs(val), 5e-5)
+    if name == "env":
+        return 1e-3 * max(1.0, abs(val))
+    return 1e-3
 
-    rng = np.random.default_rng(11)
+
+def _fd_check(gpu, cam, st, p, d, flags, n_mat=32, n_env=32, seed=11):
+    """Adjoint against finite differences of the frozen estimator on
+    parameters drawn uniformly among those with a nonzero gradient: n_mat of
+    the material parameters, n_env of the texels.  The difference quotient is
+    Richardson-extrapolated from steps h and h/2 ((4 D(h/2) - D(h)) / 3,
+    truncation error O(h^4)); a parameter passes when
+    |adjoint - fd| <= 1e-2 * max(|fd|, 1e-3 * largest |gradient| of its group).
+    Returns the errors, worst first."""
+    grads = {k: torch.zeros_like(v) for k, v in p.items()}
+    gpu.set_params(**p)
+    gpu.adjoint(cam, st, d, grads, flags=flags)
+    rng = np.random.default_rng(seed)
+    gmax = {k: float(v.abs().max()) for k, v in grads.items()}
     cands = []
     for name in ("base_color", "roughness", "metallic"):
         g = grads[name].flatten().cpu().numpy()
         v = p[name].flatten().cpu().numpy()
-        for i in np.nonzero(np.abs(g) > 0.02 * np.abs(g).max())[0]:
-            if name == "roughness" and (v[i] < 0.03 or abs(v[i] - 0.1414) < 0.01 or v[i] > 0.99):
+        for i in np.nonzero(g != 0.0)[0]:
+            if name == "roughness" and abs(v[i] - 0.1414) < 5e-3:  # alpha = max(0.02, r^2) has its kink here
                 continue
             if name == "metallic" and (v[i] < 0.01 or v[i] > 0.99):
                 continue
             cands.append((name, int(i)))
     ge = grads["env"].flatten().cpu().numpy()
-    env_c = [("env", int(i)) for i in np.nonzero(np.abs(ge) > 0.05 * np.abs(ge).max())[0]]
-    picks = [cands[i] for i in rng.choice(len(cands), size=min(32, len(cands)), replace=False)]
-    picks += [env_c[i] for i in rng.choice(len(env_c), size=min(64 - len(picks), len(env_c)), replace=False)]
-    assert len(picks) == 64
-    errs = []
-    for name, i in picks:
-        val = float(p[name].flatten()[i])
-        h = 1e-3 * max(1.0, abs(val)) if name == "env" else 1e-3
+    env_c = [("env", int(i)) for i in np.nonzero(ge != 0.0)[0]]
+    picks = [cands[i] for i in rng.choice(len(cands), size=min(n_mat, len(cands)), replace=False)]
+    picks += [env_c[i] for i in rng.choice(len(env_c), size=min(n_env, len(env_c)), replace=False)]
+    assert len(picks) == n_mat + n_env
+
+    def quotient(name, i, h):
         plus = {k: v.clone() for k, v in p.items()}
         minus = {k: v.clone() for k, v in p.items()}
         plus[name].view(-1)[i] += h
         minus[name].view(-1)[i] -= h
-        lp = _loss(d, gpu.render_frozen(cam, st, plus["base_color"], plus["roughness"], plus["metallic"], plus["env"],
-                                        flags=NO_CLAMP))
+        lp = _loss(d, gpu.render_frozen(cam, st, plus["base_color"], plus["roughness"], plus["metallic"],
+                                        plus["env"], flags=flags))
         lm = _loss(d, gpu.render_frozen(cam, st, minus["base_color"], minus["roughness"], minus["metallic"],
-                                        minus["env"], flags=NO_CLAMP))
-        fd = (lp - lm) / (2 * h)
+                                        minus["env"], flags=flags))
+        return (lp - lm) / (2.0 * h)
+
+    errs = []
+    for name, i in picks:
+        val = float(p[name].flatten()[i])
+        h = _step(name, val)
+        fd = (4.0 * quotient(name, i, 0.5 * h) - quotient(name, i, h)) / 3.0
         adj = float(grads[name].flatten()[i])
-        errs.append((abs(adj - fd) / max(abs(fd), 1e-6), name, i, adj, fd))
+        scale = max(abs(fd), 1e-3 * gmax[name])
+        errs.append((abs(adj - fd) / scale, name, i, adj, fd))
     errs.sort(reverse=True)
+    return errs
+
+
+def test_adjoint_matches_frozen_finite_differences(setup):
+    gpu, scene, cam, st, p = setup
+    gen = torch.Generator(device="cpu").manual_seed(7)
+    d = torch.rand((st.height, st.width, 4), generator=gen) - 0.3
+    d[..., 3] = 0.0
+    errs = _fd_check(gpu, cam, st, p, d.cuda(), NO_CLAMP)
     print("worst relative errors:", errs[:5])
+    assert errs[0][0] <= 1e-2, errs[:5]
+
+
+@pytest.mark.parametrize("flags", [NO_CLAMP, 0])
+def test_adjoint_finite_differences_at_full_size(flags):
+    """The differentiable configuration at its stated size: 256 materials
+    (seeded base colour, roughness, metalness) on the sphere scene cut into
+    256 meshes, a 512 x 256 environment, 512 x 512, 32 spp, depth 6, L2 loss
+    against a seeded target; 64 parameters drawn uniformly among those with a
+    nonzero gradient.  Once with the reference's clamps disabled and once with
+    them on (the frozen estimator holds each path's clamp scale constant, as
+    the adjoint does)."""
+    from shiro_gb300 import GpuBackend, scenes
+    from shiro_gb300.abi import RenderSettings
+
+    scene = scenes.split_sphere_scene(parts=256, env_width=512, env_height=256, seed=4)
+    st = RenderSettings(width=512, height=512, samples_per_pixel=32, max_depth=6, diffuse_depth=6, specular_depth=6,
+                        backend=1)
+    cam = scenes.sphere_camera(1.0)
+    with GpuBackend(0) as gpu:
+        gpu.upload_scene(scene)
+        p = dict(
+            base_color=torch.tensor([m.base_color for m in scene.materials], dtype=torch.float32, device="cuda"),
+            roughness=torch.tensor([m.roughness for m in scene.materials], dtype=torch.float32, device="cuda"),
+            metallic=torch.tensor([m.metallic for m in scene.materials], dtype=torch.float32, device="cuda"),
+            env=torch.tensor(scene.dome_lights[0].env, dtype=torch.float32, device="cuda"))
+        gpu.set_params(**p)
+        target = torch.rand((512, 512, 3), generator=torch.Generator().manual_seed(9)).cuda()
+        img = gpu.render_frozen(cam, st, flags=flags)
+        d = torch.zeros_like(img)
+        d[..., :3] = 2.0 * (img[..., :3] - target) / target.numel()
+        errs = _fd_check(gpu, cam, st, p, d, flags, seed=13 + flags)
+    print(f"flags {flags}: worst relative errors:", errs[:5])
     assert errs[0][0] <= 1e-2, errs[:5]
 
 

@@ -14,13 +14,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 @pytest.fixture(scope="module")
 def backend_lib():
-    from shiro_gb300 import build
+    from tests.cpp.harness import load_harness
 
-    path = build.build_backend()
-    lib = C.CDLL(path)
-    lib.shiro_backend_selftest.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32]
-    lib.shiro_backend_selftest.restype = C.c_int
-    return lib
+    return load_harness()
 
 
 @pytest.fixture(scope="module")
@@ -100,3 +96,75 @@ def test_progressive_accumulation_through_adapter(backend_lib, gpu, wavefront):
     ref = acc.resolve()
     for k in ("beauty", "albedo", "normal", "depth"):
         assert np.array_equal(getattr(fb, k).view(np.uint32), getattr(ref, k).view(np.uint32)), k
+
+
+def _cleared(fb):
+    return (not fb.beauty.any() and not fb.albedo.any() and not fb.normal.any()
+            and np.isinf(fb.depth).all())
+
+
+def test_cancel_set_mid_frame_through_adapter(backend_lib, gpu):
+    """Hydra cancels from another thread while a frame renders
+    (RenderBackend.h:18, RenderParam.cpp:790-798): the adapter forwards the
+    std::atomic<bool> to the device render, which stops between waves; the
+    call returns early with SHIRO_ERR_CANCELLED and a cleared frame."""
+    from shiro_gb300 import scenes
+    from shiro_gb300.abi import FrameBuffer, MarshalledScene, render_desc
+
+    # 1920 x 1080 x 128 spp on the sphere scene: dozens of waves of 8 M paths
+    w = scenes.sphere_workload(1920, 1080, 128, 8, env_width=128, env_height=64)
+    ms = MarshalledScene(w.scene)
+    req = render_desc(w.camera, w.settings, 0, 128)
+    fb = FrameBuffer(1920, 1080)
+    aov = fb.aovs()
+    status, elapsed = C.c_int(0), C.c_double(0.0)
+    # uncancelled (flag set long after the frame) for the full duration
+    assert backend_lib.shiro_harness_cancel_midframe(ms.ref(), C.byref(req), 60000.0, 0, C.byref(aov),
+                                                     C.byref(status), C.byref(elapsed)) == 1
+    assert status.value == 0
+    full = elapsed.value
+    assert not _cleared(fb)
+    for mode in (0, 1):
+        fb2 = FrameBuffer(1920, 1080)
+        aov2 = fb2.aovs()
+        assert backend_lib.shiro_harness_cancel_midframe(ms.ref(), C.byref(req), 0.1 * full, mode, C.byref(aov2),
+                                                         C.byref(status), C.byref(elapsed)) == 1
+        assert status.value == -6, (mode, status.value)  # SHIRO_ERR_CANCELLED; mode 1: not accumulated
+        assert elapsed.value < 0.6 * full, (mode, elapsed.value, full)
+        if mode == 0:
+            assert _cleared(fb2)
+
+
+def test_scene_edited_in_place_is_uploaded_again(backend_lib, gpu):
+    """A light or a vertex changed inside the same Scene object (Hydra may
+    also place a new snapshot at a freed address, RenderParam.cpp:614-659)
+    must not render from the stale device copy."""
+    from shiro_gb300 import scenes
+    from shiro_gb300.abi import FrameBuffer, MarshalledScene, render_desc
+
+    from shiro_gb300.abi import DistantLight
+
+    w = scenes.sphere_workload(40, 32, 2, 4, env_width=32, env_height=16)
+    w.scene.distant_lights = [DistantLight(direction=(-0.3, -1.0, -0.4), radiance=(2.5, 2.4, 2.2))]
+    ms = MarshalledScene(w.scene)
+    req = render_desc(w.camera, w.settings, 0, 2)
+    fbs = [FrameBuffer(40, 32) for _ in range(3)]
+    from shiro_gb300.abi import Aovs
+    outs = (Aovs * 3)(*[f.aovs() for f in fbs])
+    uploads = (C.c_uint64 * 3)()
+    rad = (C.c_float * 3)(7.0, 3.0, 1.0)
+    off = (C.c_float * 3)(0.0, 0.25, 0.0)
+    assert backend_lib.shiro_harness_edit_in_place(ms.ref(), C.byref(req), rad, off, outs, uploads) == 1
+    assert uploads[1] == uploads[0] + 1 and uploads[2] == uploads[1] + 1
+    expected = []
+    expected.append(gpu.render(w.scene, w.camera, w.settings, 0, 2))
+    w.scene.distant_lights[0].radiance = (7.0, 3.0, 1.0)
+    expected.append(gpu.render(w.scene, w.camera, w.settings, 0, 2))
+    m0 = w.scene.meshes[0]
+    m0.positions = np.array(m0.positions, dtype=np.float32, copy=True)
+    m0.positions[0] += np.array([0.0, 0.25, 0.0], dtype=np.float32)
+    expected.append(gpu.render(w.scene, w.camera, w.settings, 0, 2))
+    for k in range(3):
+        for name in ("beauty", "albedo", "normal", "depth"):
+            assert np.array_equal(getattr(fbs[k], name), getattr(expected[k], name)), (k, name)
+    assert not np.array_equal(fbs[0].beauty, fbs[1].beauty)

@@ -199,3 +199,44 @@ def test_cancel_batch(gpu):
     assert ei.value.code == -6
     # the discarded batch leaves cleared planes (FrameBuffer::Clear)
     assert not fb.beauty.any() and np.isinf(fb.depth).all()
+
+
+@pytest.mark.parametrize("form", ["plain", "wavefront"])
+def test_cancel_flag_set_by_another_thread_mid_frame(form):
+    """The C ABI polls its cancel flag between launches / waves that have run
+    (it does not queue the whole frame ahead), so a flag another host thread
+    sets mid-frame stops the render: SHIRO_ERR_CANCELLED, cleared AOVs, fewer
+    waves than the frame has, and an early return."""
+    import ctypes as C
+    import threading
+    import time
+
+    from shiro_gb300 import GpuBackend, scenes
+    from shiro_gb300.abi import FrameBuffer
+
+    w = scenes.sphere_workload(1920, 1080, 128, 8, env_width=128, env_height=64)
+    with GpuBackend(0) as gpu:
+        gpu.upload_scene(w.scene)
+        render = (lambda fb, cancel: gpu.render_batch(w.scene, [(w.camera, w.settings)], cancel=cancel, outs_fb=[fb])) \
+            if form == "wavefront" else (lambda fb, cancel: gpu.render(w.scene, w.camera, w.settings, cancel=cancel,
+                                                                        out=fb))
+        fb = FrameBuffer(1920, 1080)
+        t0 = time.perf_counter()
+        render(fb, C.c_int(0))
+        full = time.perf_counter() - t0
+        full_waves = gpu.last_stats()["waves"] if form == "wavefront" else None
+        flag = C.c_int(0)
+        timer = threading.Timer(0.1 * full, lambda: setattr(flag, "value", 1))
+        fb2 = FrameBuffer(1920, 1080)
+        fb2.beauty[:] = 1.0
+        timer.start()
+        t0 = time.perf_counter()
+        with pytest.raises(Exception) as ei:
+            render(fb2, flag)
+        took = time.perf_counter() - t0
+        timer.join()
+        assert getattr(ei.value, "code", None) == -6, ei.value
+        assert took < 0.6 * full, (took, full)
+        assert not fb2.beauty.any() and not fb2.albedo.any() and np.isinf(fb2.depth).all()
+        if form == "wavefront":
+            assert gpu.last_stats()["waves"] < full_waves

@@ -330,3 +330,92 @@ def test_exr_random_line_order_and_extra_attributes(rgb):
     i = rnd.index(b"lineOrder\0lineOrder\0") + len(b"lineOrder\0lineOrder\0") + 4
     rnd[i] = 2
     np.testing.assert_array_equal(hdri.load_exr(bytes(rnd)), want)
+
+
+# ------------------------------------------- the native (C ABI) reader -------
+
+def _native(data):
+    """shiro_hdri_decode of libshiro_gpu.so (host code, no device)."""
+    import ctypes as C
+
+    from shiro_gb300 import build
+    from shiro_gb300.backend import load_library
+
+    build.build()
+    lib = load_library()
+    lib.shiro_hdri_decode.argtypes = [C.c_char_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p,
+                                      C.c_size_t]
+    lib.shiro_hdri_decode.restype = C.c_int
+    lib.shiro_hdri_free.argtypes = [C.c_void_p]
+    w, h = C.c_uint32(), C.c_uint32()
+    px = C.POINTER(C.c_float)()
+    err = C.create_string_buffer(256)
+    rc = lib.shiro_hdri_decode(bytes(data), len(data), C.byref(w), C.byref(h), C.byref(px), err, 256)
+    if rc != 0:
+        return None, err.value.decode()
+    img = np.ctypeslib.as_array(px, shape=(h.value * w.value * 3,)).copy().reshape(h.value, w.value, 3)
+    lib.shiro_hdri_free(C.cast(px, C.c_void_p))
+    return img, ""
+
+
+def _native_cases(texels, rgb):
+    h, w = texels.shape[:2]
+    yield "hdr new", hdr_bytes(texels, "new")
+    yield "hdr old", hdr_bytes(texels, "old")
+    yield "hdr flat", hdr_bytes(texels, "flat")
+    yield "hdr +Y", hdr_bytes(texels[::-1], "flat", res=f"+Y {h} +X {w}\n".encode())
+    yield "hdr -X", hdr_bytes(texels[:, ::-1], "flat", res=f"-Y {h} -X {w}\n".encode())
+    yield "hdr cols", hdr_bytes(np.ascontiguousarray(texels.transpose(1, 0, 2)), "flat", res=f"+X {w} -Y {h}\n".encode())
+    yield "hdr cols rev", hdr_bytes(np.ascontiguousarray(texels.transpose(1, 0, 2)[::-1, ::-1]), "flat",
+                                    res=f"-X {w} +Y {h}\n".encode())
+    yield "hdr header", hdr_bytes(texels, "new", header=b"#?RGBE\n# comment\nGAMMA=1.0\n\n")
+    for comp in (0, 1, 2, 3):
+        for ptype in (HALF, FLOAT):
+            want = rgb.astype(np.float16).astype(np.float32) if ptype == HALF else rgb
+            planes = {c: (want[..., i], ptype) for i, c in enumerate("RGB")}
+            planes["A"] = (np.ones(want.shape[:2], np.float32), ptype)
+            yield f"exr comp {comp} type {ptype}", exr_bytes(planes, comp)
+    planes = {c: (rgb[..., i], FLOAT) for i, c in enumerate("RGB")}
+    for k, kw in enumerate((dict(window=(-4, 7)), dict(decreasing=True), dict(comp=3, force_raw=True),
+                            dict(comp=1, decreasing=True))):
+        yield f"exr layout {k}", exr_bytes(planes, **kw)
+    counts = np.arange(12, dtype=np.uint32).reshape(3, 4) * 1000 + 7
+    yield "exr uint", exr_bytes({"R": (counts, UINT), "G": (counts, UINT), "B": (counts, UINT)}, 2)
+    yield "exr Y", exr_bytes({"Y": (rgb[..., 1], FLOAT)}, 3)
+    yield "exr R only", exr_bytes({"R": (rgb[..., 0], FLOAT)}, 1)
+    yield "exr layers", exr_bytes({"diffuse.R": (rgb[..., 0], FLOAT), "diffuse.G": (rgb[..., 1], FLOAT),
+                                   "diffuse.B": (rgb[..., 2], FLOAT)}, 2)
+    specials = np.array([[0.0, -0.0, 6.1e-5, 5.96e-8, 65504.0, np.inf, -2.5, 1.0]], np.float16).astype(np.float32)
+    yield "exr half specials", exr_bytes({c: (specials, HALF) for c in "RGB"}, 0)
+    big = np.exp(np.random.default_rng(9).normal(0.0, 1.0, (80, 300, 3))).astype(np.float32)
+    yield "exr zip big", exr_bytes({c: (big[..., i], HALF) for i, c in enumerate("RGB")}, 3)
+
+
+def test_native_reader_equals_the_python_reader(texels, rgb):
+    """The C ABI's reader (for C++ hosts: EnvironmentMap::Load's counterpart)
+    returns exactly what shiro_gb300.hdri returns, file for file."""
+    for name, data in _native_cases(texels, rgb):
+        want = hdri.load_environment(data)
+        got, err = _native(data)
+        assert got is not None, (name, err)
+        assert got.shape == want.shape, name
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), name
+
+
+def test_native_reader_refuses_what_the_python_reader_refuses(rgb):
+    planes = {c: (rgb[..., i], HALF) for i, c in enumerate("RGB")}
+    data = bytearray(exr_bytes(planes, 0))
+    piz = bytearray(data)
+    i = piz.find(b"compression\0compression\0")
+    piz[i + 28] = 4
+    tiled = bytearray(data)
+    tiled[4:8] = struct.pack("<i", 2 | 0x200)
+    zipd = bytearray(exr_bytes(planes, 3))
+    for bad, word in ((bytes(piz), "compression"), (bytes(tiled), "tiled"), (bytes(data[:-40]), ""),
+                      (b"\x76\x2f\x31\x01\x02\0\0\0", ""), (b"P6\n1 1\n255\n\0\0\0", "unrecognised"),
+                      (b"#?RADIANCE\nFORMAT=32-bit_rle_xyze\n\n-Y 1 +X 1\n\0\0\0\0", "format"),
+                      (bytes(zipd[:-5]), "")):
+        got, err = _native(bad)
+        assert got is None and word in err, (word, err)
+        with pytest.raises(hdri.HdriError):
+            hdri.load_environment(bad)

@@ -176,3 +176,33 @@ def test_every_material_supported(port):
     sc.materials[1].emission_strength = 1.0
     sc.materials[1].emission_color = (1.0, 1.0, 1.0)
     assert port.lib.oracle_supports_scene(MarshalledScene(sc).ref()) == 1
+
+
+def test_sequential_alias_sweep_gives_the_reference_masses():
+    """oracle_env_alias (the checker of the GPU backend's alias table): every
+    texel's selection probability, reconstructed from thresholds and aliases,
+    equals its reference mass rowMass * columnMass / sum to float rounding;
+    texels without mass are never picked."""
+    import oracle
+    from oracle import api
+    from shiro_gb300 import scenes
+
+    ck = oracle.port_checker()
+    for w, h, seed in [(64, 32, 1), (512, 256, 0), (100, 50, 3)]:
+        env = scenes.procedural_hdri(w, h, seed)
+        env[3, :, :] = 0.0  # a black row: uniform columns in the reference
+        env[5, 7, :] = 0.0  # a black texel: never picked
+        thr, al = api.env_alias(ck, env)
+        t = thr.view(np.float32).astype(np.float64)
+        assert np.all((t >= 0.0) & (t <= 1.0)) and np.all(al < w * h)
+        p = t.copy()
+        np.add.at(p, al.astype(np.int64), 1.0 - t)
+        p /= w * h
+        row, cond = api.env_tables(ck, env)
+        cond = cond.reshape(h, w + 1)
+        m = ((row[1:] - row[:-1]).astype(np.float32)[:, None]
+             * (cond[:, 1:] - cond[:, :-1]).astype(np.float32)).astype(np.float32).reshape(-1).astype(np.float64)
+        target = m / m.sum()
+        live = m > 0
+        assert np.all(p[~live] == 0.0)
+        assert (np.abs(p - target)[live] / target[live]).max() < 1e-6
