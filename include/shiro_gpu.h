@@ -348,6 +348,12 @@ typedef struct ShiroWavefrontConfig {
     uint32_t concurrent_waves; /* 1 or 2: waves in flight at once, each with its own pool of
                                   paths_in_flight paths and its own stream (2 fills one wave's
                                   stage tails with the other's work); 0 leaves the current value */
+    uint32_t bin_rays;         /* 1: before each bounce after the first, the closest-hit queue is
+                                  counting-sorted into buckets of ray direction octant x origin
+                                  cell, so a warp's rays traverse similar nodes; 2: off; 0 leaves
+                                  the current value */
+    uint32_t bin_shadow;       /* the same for the occlusion queue (buckets of light sample x
+                                  octant x origin cell): 1 on, 2 off, 0 leaves the current value */
 } ShiroWavefrontConfig;
 int shiro_gpu_get_wavefront_config(const ShiroGpuContext* ctx, ShiroWavefrontConfig* out);
 int shiro_gpu_set_wavefront_config(ShiroGpuContext* ctx, const ShiroWavefrontConfig* cfg);

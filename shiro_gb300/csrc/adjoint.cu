@@ -210,6 +210,7 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
         const V3 dT = delta * ps.T;
         const V3 direct = sum_direct<false>(s, q, [&](uint32_t k, V3* c) {
             V3 ld, L;
+            V3 Ls;  // the radiance under the sampling (scene) parameters: the clamp's scale comes from it
             float w;
             int32_t envIdx = -1;
             V3 local{0.0f, 0.0f, 0.0f};
@@ -220,6 +221,7 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
                 const float nl = sclamp(dot(v.n, ld), 0.0f, 1.0f);
                 if (nl <= 0.0f) return false;
                 L = l.radiance;
+                Ls = L;
                 w = nl;
             } else {
                 const uint32_t r = k - s.distantCount;
@@ -232,6 +234,7 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
                     env_sample(s.envs[d.env], u, useCdf, &local, &lp);
                     if (lp <= 0.0f) return false;
                     L = env_evaluate(env_for_eval(s, a, d.env), local) * d.radiance;
+                    Ls = a.distinctEval ? env_evaluate(s.envs[d.env], local) * d.radiance : L;
                     envIdx = d.env;
                     domeRad = d.radiance;
                 } else {
@@ -242,6 +245,7 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
                     lp = kInvFourPi;
                     L = V3{1.0f, 1.0f, 1.0f} * d.radiance;
                 }
+                if (d.env < 0) Ls = L;
                 ld = light_to_world(d, local);
                 const float nl = sclamp(dot(v.n, ld), 0.0f, 1.0f);
                 if (nl <= 0.0f) return false;
@@ -252,7 +256,14 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
             if (trace_occluded(s, origin, ld, FLT_MAX, ctr)) return false;
             const V3 f = evalE(ld);
             const V3 raw = f * L * w;
-            *c = clamp24(q, raw);
+            if (a.distinctEval) {
+                // frozen render: the clamp scale of the sampling parameters'
+                // contribution (held constant, as the adjoint holds it)
+                const V3 rawS = bsdf_eval_rec(rec, ms, v.n, v.cn, v.view, ld) * Ls * w;
+                *c = raw * clamp_scale(q, rawS, kDirectSampleClamp);
+            } else {
+                *c = clamp24(q, raw);
+            }
             if (kGrad) {
                 const float sc = clamp_scale(q, raw, kDirectSampleClamp);
                 const DV3 fd = bsdf_eval_d(me, v.n, v.cn, v.view, ld);
@@ -298,9 +309,17 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
         }
         const float cosT = sclamp(dot(v.n, next), 0.0f, 1.0f);
         if (cosT <= 0.0f) break;
-        if (a.distinctEval) Ts = clamp12(q, Ts * bsdf_eval_rec(rec, ms, v.n, v.cn, v.view, next) * (cosT / pdf));
-        ps.T = clamp12(q, ps.T * f * (cosT / pdf));
-        if (!a.distinctEval) Ts = ps.T;
+        if (a.distinctEval) {
+            // frozen render: the throughput clamp's scale comes from the
+            // sampling throughput (clamp_max(v) == v * clamp_scale(v))
+            const V3 tsRaw = Ts * bsdf_eval_rec(rec, ms, v.n, v.cn, v.view, next) * (cosT / pdf);
+            const float sc = clamp_scale(q, tsRaw, kThroughputClamp);
+            Ts = tsRaw * sc;
+            ps.T = ps.T * f * (cosT / pdf) * sc;
+        } else {
+            ps.T = clamp12(q, ps.T * f * (cosT / pdf));
+            Ts = ps.T;
+        }
         const float off = dot(v.n, next) >= 0.0f ? 1.0f : -1.0f;
         ps.ro = v.hit.position + v.n * (kRayEpsilon * off);
         const V3 prevDir = ps.rd;
@@ -331,10 +350,10 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
     return ps.radiance;
 }
 
-// The gradient pass.  Each path's total radiance comes from the plain
-// megakernel's path record of the same path (same estimator, same sample),
-// rendered just before into `records`, so only the replay that accumulates
-// gradients runs here.  (4 blocks per SM: 128 registers measured faster than
+// The gradient pass.  Each path's total radiance comes from the record of the
+// same path (same estimator, same sample) rendered just before by the
+// wavefront form into `records` (one float4 per path, request path order), so
+// only the replay that accumulates gradients runs here.  (4 blocks per SM: 128 registers measured faster than
 // the 168 the compiler otherwise takes.)
 __global__ void __launch_bounds__(128, 4) k_adjoint(const __grid_constant__ DevScene s, const __grid_constant__ DevRequest q,
                                                     const __grid_constant__ AdjView a, uint64_t pathBase, uint32_t count,
@@ -350,7 +369,7 @@ __global__ void __launch_bounds__(128, 4) k_adjoint(const __grid_constant__ DevS
         const float4 g = reinterpret_cast<const float4*>(a.dBeauty)[pixel];
         const V3 delta{g.x / cnt, g.y / cnt, g.z / cnt};
         if (delta.x != 0.0f || delta.y != 0.0f || delta.z != 0.0f) {
-            const float4 r = records[3 * static_cast<size_t>(i)];
+            const float4 r = records[path];
             adj_path(s, q, a, x, y, q.sampleStart + smp, delta, V3{r.x, r.y, r.z}, nullptr, true);
         }
     }
@@ -480,8 +499,8 @@ int adjoint_run(ContextImpl* ctx, const ShiroRenderDesc* req, const float* dBeau
     }
     const uint64_t total = static_cast<uint64_t>(q.width) * q.height * q.sampleCount;
     const uint64_t chunk = 1ull << 24;
-    if (!ensure_block(ctx, &ctx->pathRecords, std::min(chunk, std::max<uint64_t>(total, 1)) * kPathRecordBytes,
-                      "path records"))
+    // one record (radiance, depth) per path of the request
+    if (!ensure_block(ctx, &ctx->pathRecords, std::max<uint64_t>(total, 1) * sizeof(float4), "path records"))
         return SHIRO_ERR_OUT_OF_MEMORY;
     float4* rec = static_cast<float4*>(ctx->pathRecords.ptr);
     cudaEvent_t e0, e1;
@@ -489,11 +508,19 @@ int adjoint_run(ContextImpl* ctx, const ShiroRenderDesc* req, const float* dBeau
     cudaEventCreate(&e1);
     cudaEventRecord(e0, ctx->stream);
     uint64_t launches = 0;
+    if (total) {  // the paths' radiance, by the wavefront form
+        rc = wavefront_path_records(ctx, *req, rec);
+        if (rc != SHIRO_OK) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return rc;
+        }
+        launches += ctx->stats.kernel_launches;
+    }
     for (uint64_t p0 = 0; p0 < total; p0 += chunk) {
         const uint32_t n = static_cast<uint32_t>(std::min(chunk, total - p0));
-        launch_plain_paths(ctx->scene, q, p0, n, rec, ctx->stream);  // the paths' radiance
         k_adjoint<<<grid(n, 128), 128, 0, ctx->stream>>>(ctx->scene, q, a, p0, n, rec);
-        launches += 2;
+        launches += 1;
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
             cudaEventDestroy(e0);

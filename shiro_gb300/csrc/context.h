@@ -138,6 +138,10 @@ void static_scratch_setup(ContextImpl* ctx);
 int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t count, const volatile int* cancel,
                      ShiroAovs* outs);
 void wavefront_free(ContextImpl* ctx);
+// Every path of one request by the wavefront form, its record (radiance,
+// first-hit depth) written to out[path] in request path order (pixel-major,
+// sample-minor) instead of resolved pixels: the radiance a path replay needs.
+int wavefront_path_records(ContextImpl* ctx, const ShiroRenderDesc& req, float4* out);
 int wavefront_get_config(const ContextImpl* ctx, ShiroWavefrontConfig* out);
 int wavefront_set_config(ContextImpl* ctx, const ShiroWavefrontConfig* cfg);
 int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefrontConfig* chosen);

@@ -73,6 +73,7 @@ struct DevScene {
     uint32_t distantCount;
     uint32_t domeCount;
     V3 envTop, envBottom;
+    V3 boundsLo, boundsHi;          // box of all triangles (queue binning by ray origin)
     uint32_t rootIsLeaf;            // scene of <= 8 triangles: node 0 holds them all
     uint32_t emissiveCount;         // emissive triangles (AccelerationScene::emissiveTriangles)
     const float4* emissive;         // 3 per emissive triangle: (area, selection weight, running sum, gid bits),

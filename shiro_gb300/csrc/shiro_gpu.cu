@@ -922,6 +922,8 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     s.domeCount = sd->dome_light_count;
     s.envTop = ld3(sd->environment_top);
     s.envBottom = ld3(sd->environment_bottom);
+    s.boundsLo = V3{slo[0], slo[1], slo[2]};
+    s.boundsHi = V3{shi[0], shi[1], shi[2]};
     s.error = ctx->errorWord;
     const cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "scene upload");

@@ -107,7 +107,19 @@ struct WfView {
     int travSteps;     // wide-BVH nodes per lane between refills
     int refillIdle;    // idle lanes that trigger a refill
     uint32_t waveStride;  // waves in flight at once: this pool runs waves k, k + stride, ...
+    // queue binning: bucket counters / offsets, the binned queue, and the map
+    // of a ray origin to its cell (cell = (o - binLo) * binScale, 8 per axis)
+    uint32_t* binCount;
+    uint32_t* sortedQ;
+    V3 binLo, binScale;
+    // non-NULL: instead of resolving pixels, the wave's path records go out
+    // per path (radiance, first-hit depth) in request path order
+    float4* recordsOut;
 };
+
+// Buckets of the queue binning: light sample (8) x direction octant (8) x
+// origin cell (8 x 8 x 8, Morton-interleaved).
+constexpr uint32_t kBins = 8u * 8u * 512u;
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
@@ -133,6 +145,106 @@ __device__ __forceinline__ const WaveSeg& find_seg(const WfView& v, const WaveDe
         if (key <= j) lo = mid; else hi = mid - 1u;
     }
     return v.segs[lo];
+}
+
+__device__ __forceinline__ uint32_t bin_key(const WfView& v, const float4& o, const float4& d, uint32_t k) {
+    const float f[3] = {(o.x - v.binLo.x) * v.binScale.x, (o.y - v.binLo.y) * v.binScale.y,
+                        (o.z - v.binLo.z) * v.binScale.z};
+    uint32_t c[3];
+    for (int a = 0; a < 3; ++a) {
+        const float x = f[a] < 0.0f ? 0.0f : (f[a] > 7.0f ? 7.0f : f[a]);  // NaN -> 7
+        c[a] = static_cast<uint32_t>(x);
+    }
+    uint32_t cell = 0;
+    for (int b = 0; b < 3; ++b) cell |= (((c[0] >> b) & 1u) << (3 * b + 2)) | (((c[1] >> b) & 1u) << (3 * b + 1)) |
+                                        (((c[2] >> b) & 1u) << (3 * b));
+    const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    return ((k & 7u) << 12) | (oct << 9) | cell;
+}
+
+// Queue binning (a counting sort into kBins buckets; the order inside a
+// bucket is whatever the atomics give - every path's result is independent
+// of the order its ray is traced in).  which = 0: the closest-hit queue
+// `cur`, 1: the occlusion queue.  Lanes with equal keys add with one atomic.
+__device__ __forceinline__ void bin_item(const WfView& v, uint32_t which, uint32_t item, uint32_t* key) {
+    if (which) {
+        const uint32_t j = item >> 3, k = item & 7u;
+        *key = bin_key(v, v.shOrigin[j], v.shDir[static_cast<size_t>(k) * v.P + j], k);
+    } else {
+        *key = bin_key(v, v.ro[item], v.rd[item], 0u);
+    }
+}
+
+__global__ void __launch_bounds__(256) wf_bin_count(WfView v, uint32_t which, uint32_t cur) {
+    const uint32_t count = which ? v.counters[4] : v.counters[cur];
+    const uint32_t* q = which ? v.shadowRayQ : (cur ? v.rayQ1 : v.rayQ0);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < count;
+        uint32_t key = 0xffffffffu;
+        if (valid) bin_item(v, which, q[i], &key);
+        const uint32_t peers = __match_any_sync(0xffffffffu, key);
+        if (valid && (threadIdx.x & 31u) == static_cast<uint32_t>(__ffs(peers) - 1))
+            atomicAdd(&v.binCount[key], static_cast<uint32_t>(__popc(peers)));
+    }
+}
+
+// Counts -> exclusive offsets, one block of 1024 threads, 32 buckets each.
+__global__ void __launch_bounds__(1024) wf_bin_scan(WfView v) {
+    __shared__ uint32_t warpSum[32];
+    constexpr uint32_t per = kBins / 1024u;
+    uint32_t* c = v.binCount + threadIdx.x * per;
+    uint32_t local[per];
+    uint32_t sum = 0;
+    for (uint32_t k = 0; k < per; ++k) {
+        local[k] = c[k];
+        sum += local[k];
+    }
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t x = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= static_cast<uint32_t>(o)) x += y;
+    }
+    if (lane == 31u) warpSum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warpSum[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= static_cast<uint32_t>(o)) w += y;
+        }
+        warpSum[lane] = w;
+    }
+    __syncthreads();
+    uint32_t run = (warp > 0 ? warpSum[warp - 1] : 0u) + x - sum;
+    for (uint32_t k = 0; k < per; ++k) {
+        c[k] = run;
+        run += local[k];
+    }
+}
+
+__global__ void __launch_bounds__(256) wf_bin_scatter(WfView v, uint32_t which, uint32_t cur) {
+    const uint32_t count = which ? v.counters[4] : v.counters[cur];
+    const uint32_t* q = which ? v.shadowRayQ : (cur ? v.rayQ1 : v.rayQ0);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < count;
+        uint32_t key = 0xffffffffu, item = 0;
+        if (valid) {
+            item = q[i];
+            bin_item(v, which, item, &key);
+        }
+        const uint32_t peers = __match_any_sync(0xffffffffu, key);
+        const uint32_t leader = static_cast<uint32_t>(__ffs(peers) - 1);
+        uint32_t pos = 0;
+        if (valid && lane == leader) pos = atomicAdd(&v.binCount[key], static_cast<uint32_t>(__popc(peers)));
+        pos = __shfl_sync(peers, pos, leader);
+        if (valid) v.sortedQ[pos + __popc(peers & ((1u << lane) - 1u))] = item;
+    }
 }
 
 __global__ void wf_begin(WfView v) {
@@ -258,10 +370,10 @@ __device__ __forceinline__ void flush_stage(uint32_t* buf, uint32_t& n, uint32_t
 // the hits at the front of the shade queue and the misses at its back, so the
 // shade stage runs warps of hits and warps of misses instead of warps that
 // take both branches.
-__global__ void __launch_bounds__(256, 4) wf_extend(WfView v, DevScene s, uint32_t cur) {
+__global__ void __launch_bounds__(256, 4) wf_extend(WfView v, DevScene s, uint32_t cur, uint32_t binned) {
     __shared__ uint32_t stage[8][2][64];
     const uint32_t count = v.counters[cur];
-    const uint32_t* q = cur ? v.rayQ1 : v.rayQ0;
+    const uint32_t* q = binned ? v.sortedQ : (cur ? v.rayQ1 : v.rayQ0);
     NullCounter ctr;
     if (s.nodes8) {
         uint32_t* hb = stage[threadIdx.x >> 5][0];
@@ -461,15 +573,16 @@ __global__ void __launch_bounds__(256) wf_miss(WfView v, DevScene s, uint32_t de
 // (Lane refill as in wf_extend measured slower here: shadow rays are short
 // and an any-hit ends them early, so the refill bookkeeping outweighs the
 // divergence it removes.)
-__global__ void __launch_bounds__(256, 4) wf_occlude(WfView v, DevScene s) {
+__global__ void __launch_bounds__(256, 4) wf_occlude(WfView v, DevScene s, uint32_t binned) {
     const uint32_t count = v.counters[4];
+    const uint32_t* sq = binned ? v.sortedQ : v.shadowRayQ;
     NullCounter ctr;
     for (;;) {
         const uint32_t base = warp_fetch(&v.counters[kFetchOcclude]);
         if (base >= count) break;
         const uint32_t i = base + lane_id();
         if (i >= count) continue;
-        const uint32_t item = v.shadowRayQ[i];
+        const uint32_t item = sq[i];
         const uint32_t j = item >> 3, k = item & 7u;
         const size_t e = static_cast<size_t>(k) * v.P + j;
         const float4 o4 = v.shOrigin[j], d4 = v.shDir[e];
@@ -550,6 +663,18 @@ __global__ void __launch_bounds__(128) wf_resolve(WfView v) {
     }
 }
 
+// Per-path records of the wave in request path order (pixel-major,
+// sample-minor): the radiance a path replay needs (adjoint).
+__global__ void __launch_bounds__(128) wf_records_out(WfView v) {
+    const WaveDesc w = cur_wave(v);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < w.paths; j += gridDim.x * blockDim.x) {
+        const WaveSeg& sg = find_seg(v, w, j, false);
+        const uint32_t spp = v.reqs[sg.req].q.sampleCount;
+        const size_t path = static_cast<size_t>(sg.pixelStart) * spp + (j - sg.pathOffset);
+        v.recordsOut[path] = v.records[3 * static_cast<size_t>(j)];
+    }
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -594,6 +719,8 @@ WavefrontState* wf_state(ContextImpl* ctx) {
         c.extend_steps = 4;
         c.refill_idle = 8;
         c.concurrent_waves = 2;
+        c.bin_rays = 2;
+        c.bin_shadow = 2;
         cudaDeviceGetAttribute(&ctx->wavefront->smCount, cudaDevAttrMultiProcessorCount, ctx->device);
     }
     return ctx->wavefront;
@@ -603,7 +730,8 @@ bool ensure_pool(ContextImpl* ctx, WavePool* wf, uint32_t P, uint32_t lightSampl
     const size_t p = P;
     const size_t stateBytes = p * (7 * sizeof(float4) + sizeof(uint32_t));
     const size_t shadowBytes = p * (2 + 2 * static_cast<size_t>(std::max(1u, lightSamples))) * sizeof(float4);
-    const size_t queueBytes = p * (4 + static_cast<size_t>(std::max(1u, lightSamples))) * sizeof(uint32_t) + 64;
+    const size_t ls = std::max(1u, lightSamples);
+    const size_t queueBytes = (p * (4 + ls) + p * ls + kBins) * sizeof(uint32_t) + 64;  // + binned queue, buckets
     const size_t recordBytes = p * 3 * sizeof(float4);
     if (!ensure_block(ctx, &wf->state, stateBytes, "wavefront state")) return false;
     if (!ensure_block(ctx, &wf->shadow, shadowBytes, "wavefront shadow records")) return false;
@@ -638,6 +766,8 @@ WfView make_view(WavePool* wf, uint32_t P, uint32_t lightSamples, const WaveDesc
     v.shadowQ = v.rayQ1 + p;
     v.shadowRayQ = v.shadowQ + p;
     v.shadeQ = v.shadowRayQ + p * static_cast<size_t>(std::max(1u, lightSamples));
+    v.sortedQ = v.shadeQ + p;
+    v.binCount = v.sortedQ + p * static_cast<size_t>(std::max(1u, lightSamples));
     v.records = static_cast<float4*>(wf->records.ptr);
     v.waves = waves;
     v.segs = segs;
@@ -712,8 +842,17 @@ struct Launch {
     int bExt, bShade, bShadow;
     uint32_t depth;
     uint32_t shadeRegs;
+    uint32_t binRays, binShadow;  // queue binning before extend (bounces >= 1) / occlude
+    int gBin;
     bool ext;  // the scene uses transmission, opacity or emitters
 };
+
+void enqueue_binning(const Launch& L, cudaStream_t st, uint32_t which, uint32_t cur) {
+    cudaMemsetAsync(L.v.binCount, 0, kBins * sizeof(uint32_t), st);
+    wf_bin_count<<<L.gBin, 256, 0, st>>>(L.v, which, cur);
+    wf_bin_scan<<<1, 1024, 0, st>>>(L.v);
+    wf_bin_scatter<<<L.gBin, 256, 0, st>>>(L.v, which, cur);
+}
 
 void launch_shade(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t d) {
     if (L.ext) {
@@ -734,13 +873,17 @@ void enqueue_wave(const Launch& L, cudaStream_t st) {
     wf_generate<<<L.gGen, 128, 0, st>>>(L.v);
     for (uint32_t d = 0; d < L.depth; ++d) {
         const uint32_t cur = d & 1u;
-        wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur);
+        const uint32_t br = (L.binRays && d > 0) ? 1u : 0u;  // camera rays are coherent already
+        if (br) enqueue_binning(L, st, 0u, cur);
+        wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, br);
         launch_shade(L, st, cur, d);
-        wf_occlude<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s);
+        if (L.binShadow) enqueue_binning(L, st, 1u, cur);
+        wf_occlude<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s, L.binShadow);
         wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s);
         wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur);
     }
-    wf_resolve<<<L.gRes, 128, 0, st>>>(L.v);
+    if (L.v.recordsOut) wf_records_out<<<L.gRes, 128, 0, st>>>(L.v);
+    else wf_resolve<<<L.gRes, 128, 0, st>>>(L.v);
 }
 
 // The same wave with events around every stage launch (diagnostic timing).
@@ -758,20 +901,30 @@ void enqueue_wave_timed(const Launch& L, cudaStream_t st, std::vector<std::pair<
     timed(0, [&] { wf_generate<<<L.gGen, 128, 0, st>>>(L.v); });
     for (uint32_t d = 0; d < L.depth; ++d) {
         const uint32_t cur = d & 1u;
-        timed(1, [&] { wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur); });
+        const uint32_t br = (L.binRays && d > 0) ? 1u : 0u;
+        timed(1, [&] {
+            if (br) enqueue_binning(L, st, 0u, cur);
+            wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, br);
+        });
         timed(2, [&] { launch_shade(L, st, cur, d); });
-        timed(3, [&] { wf_occlude<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s); });
+        timed(3, [&] {
+            if (L.binShadow) enqueue_binning(L, st, 1u, cur);
+            wf_occlude<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s, L.binShadow);
+        });
         timed(5, [&] { wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s); });
         timed(5, [&] { wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur); });
     }
-    timed(4, [&] { wf_resolve<<<L.gRes, 128, 0, st>>>(L.v); });
+    timed(4, [&] {
+        if (L.v.recordsOut) wf_records_out<<<L.gRes, 128, 0, st>>>(L.v);
+        else wf_resolve<<<L.gRes, 128, 0, st>>>(L.v);
+    });
 }
 
 // Renders the requests (device AOV planes in `aovs`) with configuration
 // `cfg`.  maxWaves limits the waves run (autotuning); returns paths traced.
 int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& cfg, const std::vector<DevRequest>& qs,
               const std::vector<AovPtrs>& aovs, const volatile int* cancel, uint32_t maxWaves, uint64_t* pathsOut,
-              double* msOut) {
+              double* msOut, float4* recordsOut = nullptr) {
     uint32_t lightSamples = ctx->scene.distantCount;
     uint32_t domeSamplesMax = 1;
     for (const DevRequest& q : qs) domeSamplesMax = std::max(domeSamplesMax, q.domeSamples);
@@ -820,6 +973,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     std::memset(&L, 0, sizeof(L));  // padding too: the bytes key the graph cache
     L.v = make_view(&wf->pools[0], poolP[0], lightSamples, dWaves, dSegs, dReqs);
     L.v.waveStride = nl;
+    L.v.recordsOut = recordsOut;
     L.s = ctx->scene;
     if (ctx->bvhWidth != 2 && ctx->nodes8) {  // the wavefront stages traverse the wide BVH unless told otherwise
         L.s.nodes8 = ctx->nodes8;
@@ -842,6 +996,16 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.gShadow = grid_for(wf_shadow, 256, wf->smCount);
     L.gOcc = grid_for(wf_occlude, L.bShadow, wf->smCount);
     L.gRes = grid_for(wf_resolve, 128, wf->smCount);
+    L.gBin = grid_for(wf_bin_scatter, 256, wf->smCount);
+    L.binRays = cfg.bin_rays == 1 ? 1u : 0u;
+    L.binShadow = cfg.bin_shadow == 1 ? 1u : 0u;
+    {
+        const DevScene& sc = ctx->scene;
+        const V3 ext{sc.boundsHi.x - sc.boundsLo.x, sc.boundsHi.y - sc.boundsLo.y, sc.boundsHi.z - sc.boundsLo.z};
+        L.v.binLo = sc.boundsLo;
+        L.v.binScale = V3{ext.x > 0.0f ? 8.0f / ext.x : 0.0f, ext.y > 0.0f ? 8.0f / ext.y : 0.0f,
+                          ext.z > 0.0f ? 8.0f / ext.z : 0.0f};
+    }
     L.depth = pl.maxDepth;
     Launch lanes[kMaxConcurrentWaves];
     for (uint32_t k = 0; k < nl; ++k) {
@@ -851,6 +1015,9 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             v.waveStride = nl;
             v.travSteps = L.v.travSteps;
             v.refillIdle = L.v.refillIdle;
+            v.binLo = L.v.binLo;
+            v.binScale = L.v.binScale;
+            v.recordsOut = recordsOut;
             std::memcpy(&lanes[k].v, &v, sizeof(WfView));
         }
         // wf_begin adds the stride to the wave index: start one stride below k
@@ -921,7 +1088,8 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             e = cudaGetLastError();
         }
         throttle.after_launch(exec[k] && k != 0 ? wf->side : st);
-        launches += 3 + 6ull * L.depth;
+        launches += 3 + 6ull * L.depth + (L.binShadow ? 3ull * L.depth : 0ull) +
+                (L.binRays && L.depth > 1 ? 3ull * (L.depth - 1) : 0ull);
         ++launchedWaves;
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront launch");
     }
@@ -1054,6 +1222,15 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
     return SHIRO_OK;
 }
 
+int wavefront_path_records(ContextImpl* ctx, const ShiroRenderDesc& req, float4* out) {
+    if (!ctx->hasScene) return fail(ctx, SHIRO_ERR_NO_SCENE, "no scene uploaded");
+    WavefrontState* wf = wf_state(ctx);
+    std::vector<DevRequest> qs{make_request(req)};
+    std::vector<AovPtrs> aov{AovPtrs{nullptr, nullptr, nullptr, nullptr}};
+    uint64_t paths = 0;
+    return run_waves(ctx, wf, wf->cfg, qs, aov, nullptr, 0xffffffffu, &paths, nullptr, out);
+}
+
 void wavefront_free(ContextImpl* ctx) {
     if (!ctx->wavefront) return;
     WavefrontState* wf = ctx->wavefront;
@@ -1100,6 +1277,10 @@ int wavefront_set_config(ContextImpl* ctx, const ShiroWavefrontConfig* cfg) {
     if (cfg->concurrent_waves > kMaxConcurrentWaves)
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "concurrent_waves must be 1 or 2");
     if (cfg->concurrent_waves) wf->cfg.concurrent_waves = cfg->concurrent_waves;
+    if (cfg->bin_rays > 2 || cfg->bin_shadow > 2)
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "bin_rays and bin_shadow must be 1 (on), 2 (off) or 0");
+    if (cfg->bin_rays) wf->cfg.bin_rays = cfg->bin_rays;
+    if (cfg->bin_shadow) wf->cfg.bin_shadow = cfg->bin_shadow;
     wf->cfg.use_graph = cfg->use_graph;
     return SHIRO_OK;
 }
@@ -1191,6 +1372,16 @@ int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefr
             c.paths_in_flight = p;
             if ((rc = trial(c)) != SHIRO_OK) return rc;
         }
+    }
+    for (uint32_t on : {1u, 2u}) {  // queue binning before the traversal stages
+        ShiroWavefrontConfig c = best;
+        c.bin_shadow = on;
+        if ((rc = trial(c)) != SHIRO_OK) return rc;
+    }
+    for (uint32_t on : {1u, 2u}) {
+        ShiroWavefrontConfig c = best;
+        c.bin_rays = on;
+        if ((rc = trial(c)) != SHIRO_OK) return rc;
     }
     if (ctx->nodes8 && ctx->bvhWidth != 2) {  // the lane refill of the wide-BVH extend stage
         for (uint32_t steps : {2u, 4u, 8u}) {
