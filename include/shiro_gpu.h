@@ -375,6 +375,16 @@ int shiro_gpu_set_params(ShiroGpuContext* ctx, const float* base_color, const fl
 int shiro_gpu_adjoint(ShiroGpuContext* ctx, const ShiroRenderDesc* request, const float* d_beauty,
                       float* d_base_color, float* d_roughness, float* d_metallic, float* d_env_rgb);
 
+/* How shiro_gpu_adjoint replays paths: 1 (default) with the wavefront form -
+ * each wave of paths runs its forward stages, then replays its paths with
+ * gradient stages on the same pool and queues (closest hit and occlusion
+ * shared with the forward; light-sample and continuation gradients after the
+ * visibility of the vertex's light samples is known); 0 one thread per path
+ * (the whole replay in one kernel, after a wavefront pass for the paths'
+ * radiance).  Both accumulate the same gradients (up to the order of their
+ * float atomics). */
+int shiro_gpu_set_adjoint_form(ShiroGpuContext* ctx, uint32_t wavefront);
+
 /* Frozen-sampling forward of the differentiable form: renders the beauty
  * plane (device pointer, 4 floats per pixel) with every sampling decision,
  * pdf and MIS weight taken from the uploaded scene's parameters and the BSDF

@@ -95,6 +95,7 @@ def load_library(path: str = LIB_PATH):
         "shiro_gpu_render_frozen": ([_P, _P, _P, _P, _P, _P, _P], C.c_int),
         "shiro_gpu_set_bvh_width": ([_P, _U], C.c_int),
         "shiro_gpu_set_bvh_build": ([_P, _U], C.c_int),
+        "shiro_gpu_set_adjoint_form": ([_P, _U], C.c_int),
         "shiro_gpu_env_tables": ([_P, _U, _P, _P, _P, _P, _P, _P, _P], C.c_int),
         "shiro_gpu_scene_signature": ([_P, _P], C.c_int),
         "shiro_hdri_load": ([C.c_char_p, _P, _P, _P, C.c_char_p, C.c_size_t], C.c_int),
@@ -283,6 +284,13 @@ class GpuBackend:
         if rc != 0:
             raise ShiroGpuError(rc, "cluster size must be 0 or in [2, 65536]")
         self._scene_key = None
+
+    def set_adjoint_form(self, wavefront: bool):
+        """True (default): the adjoint replays paths with the wavefront stages;
+        False: one thread per path."""
+        rc = self.lib.shiro_gpu_set_adjoint_form(self._ctx, 1 if wavefront else 0)
+        if rc != 0:
+            raise self._err(rc)
 
     def wavefront_config(self) -> dict:
         c = WavefrontConfig()

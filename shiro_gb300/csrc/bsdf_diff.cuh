@@ -242,7 +242,7 @@ __device__ __forceinline__ Dual roughness_for_d(const Dual& r, float aniso, floa
 }
 
 // EvaluateBsdf with derivatives (value identical to bsdf_eval).
-__device__ __noinline__ DV3 bsdf_eval_d(const Mat& m, const V3& n, const V3& cn, const V3& v, const V3& l) {
+static __device__ __noinline__ DV3 bsdf_eval_d(const Mat& m, const V3& n, const V3& cn, const V3& v, const V3& l) {
     const float nv = sclamp(dot(n, v), 0.0f, 1.0f);
     const float nl = sclamp(dot(n, l), 0.0f, 1.0f);
     if (nv <= 0.0f || nl <= 0.0f) return dv3(V3{0.0f, 0.0f, 0.0f});

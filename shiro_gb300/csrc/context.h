@@ -32,6 +32,7 @@ constexpr uint32_t kDefaultSahCluster = 8;
 
 struct WavefrontState;
 struct AdjointState;
+struct AdjView;
 
 struct ContextImpl {
     int device = 0;
@@ -61,6 +62,9 @@ struct ContextImpl {
     // triangles per cluster below the binned-SAH top of the binary BVHs built
     // at the next upload (0: the Morton hierarchy throughout)
     uint32_t sahClusterSize = kDefaultSahCluster;
+    // 1: the adjoint replays paths with the wavefront stages (after each
+    // wave's forward stages); 0: one thread per path (k_adjoint)
+    uint32_t adjointWavefront = 1;
 
     // scratch (grown on demand, kept between calls)
     DeviceBlock pathRecords;
@@ -142,6 +146,10 @@ void wavefront_free(ContextImpl* ctx);
 // first-hit depth) written to out[path] in request path order (pixel-major,
 // sample-minor) instead of resolved pixels: the radiance a path replay needs.
 int wavefront_path_records(ContextImpl* ctx, const ShiroRenderDesc& req, float4* out);
+// The adjoint of one request by the wavefront form: each wave runs its
+// forward stages, then replays its paths with the gradient stages into the
+// buffers of `adj` (host copy; its device pointers are used as they are).
+int wavefront_adjoint(ContextImpl* ctx, const ShiroRenderDesc& req, const AdjView& adj);
 int wavefront_get_config(const ContextImpl* ctx, ShiroWavefrontConfig* out);
 int wavefront_set_config(ContextImpl* ctx, const ShiroWavefrontConfig* cfg);
 int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefrontConfig* chosen);

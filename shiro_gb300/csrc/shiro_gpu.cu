@@ -595,6 +595,12 @@ int shiro_gpu_set_bvh_build(ShiroGpuContext* ctx, uint32_t sah_cluster_triangles
     return SHIRO_OK;
 }
 
+int shiro_gpu_set_adjoint_form(ShiroGpuContext* ctx, uint32_t wavefront) {
+    if (!ctx || wavefront > 1) return SHIRO_ERR_INVALID_ARGUMENT;
+    ctx->impl.adjointWavefront = wavefront;
+    return SHIRO_OK;
+}
+
 int shiro_gpu_set_stream(ShiroGpuContext* ctx, void* stream) {
     if (!ctx) return SHIRO_ERR_INVALID_ARGUMENT;
     ctx->impl.stream = stream ? static_cast<cudaStream_t>(stream) : ctx->impl.ownStream;

@@ -30,6 +30,7 @@
 #include <cstring>
 #include <vector>
 
+#include "adjoint.cuh"
 #include "context.h"
 #include "integrator.cuh"
 
@@ -120,6 +121,22 @@ struct WfView {
 // Buckets of the queue binning: light sample (8) x direction octant (8) x
 // origin cell (8 x 8 x 8, Morton-interleaved).
 constexpr uint32_t kBins = 8u * 8u * 512u;
+
+// Per-slot state of the adjoint replay, which runs in a wave after the
+// wave's forward stages, on the same pool, queues and slots (each path's
+// forward record, its total radiance, is still in its slot).
+struct AdjWave {
+    const AdjView* view;  // device copy (gradient buffers, d_beauty, dome 0's texture), written per call
+    float4* lrem;         // radiance of the path not yet accounted for
+    float4* delta;        // d loss / d path radiance: d_beauty of its pixel / spp
+    float4* vtx;          // 3 per slot: (shading normal, material bits), (coat normal), (view direction)
+    float4* cont;         // 2 per slot: (continuation direction, 1 when its gradient is due), (its BSDF value)
+    float4* lgrad;        // 3 per light sample and slot, [k][P]: (L w s), (f R w s, 1 for dome 0's texture), (local dir)
+    uint32_t on;          // replay stages follow the forward ones
+    uint32_t pad;
+};
+constexpr size_t kAdjSlotFloat4 = 7;      // lrem, delta, vtx (3), cont (2)
+constexpr size_t kAdjLightFloat4 = 3;     // per light sample
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
@@ -663,6 +680,306 @@ __global__ void __launch_bounds__(128) wf_resolve(WfView v) {
     }
 }
 
+// ---- adjoint replay stages ---------------------------------------------------
+// The estimator of adjoint.cu's path replay (adj_path with the scene's own
+// parameters), cut at the same seams as the forward stages: light samples and
+// continuation in wa_shade, their occlusion in wf_occlude, the gradients of
+// the visible samples and of the continuation in wa_shadow (they need the
+// radiance still to come, which is known once the vertex's direct light is),
+// the environment gradients of the misses in wa_miss.
+
+__global__ void wa_begin(WfView v) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        for (uint32_t k = 0; k < 10; ++k)
+            if (k != 3) v.counters[k] = 0u;  // every queue, keeping the wave index
+    }
+}
+
+// Paths restart from their QMC seed; those whose pixel has a nonzero
+// d_beauty are queued.
+__global__ void __launch_bounds__(128) wa_generate(WfView v, AdjWave aw) {
+    const WaveDesc w = cur_wave(v);
+    const AdjView& a = *aw.view;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < w.paths; base += stride) {
+        const uint32_t j = base + threadIdx.x;
+        bool push = false;
+        if (j < w.paths) {
+            const WaveSeg& sg = find_seg(v, w, j, false);
+            const DevRequest& q = v.reqs[sg.req].q;
+            const uint32_t local = j - sg.pathOffset;
+            const uint32_t pix = sg.pixelStart + local / q.sampleCount;
+            const uint32_t smpIdx = q.sampleStart + (local - (local / q.sampleCount) * q.sampleCount);
+            const uint32_t y = pix / q.width, x = pix - y * q.width;
+            const Sampler smp{x, y, smpIdx};
+            PathState ps;
+            init_path(q, smp, ps);
+            v.ro[j] = make_float4(ps.ro.x, ps.ro.y, ps.ro.z, 0.0f);
+            v.rd[j] = make_float4(ps.rd.x, ps.rd.y, ps.rd.z, ps.prevPdf);
+            v.T[j] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(kFlagPrevDelta));
+            v.ident[j] = make_uint4(x, y, smpIdx, sg.req);
+            const float cnt = static_cast<float>(q.sampleCount);
+            const float4 g = reinterpret_cast<const float4*>(a.dBeauty)[pix];
+            const float4 r = v.records[3 * static_cast<size_t>(j)];
+            aw.delta[j] = make_float4(g.x / cnt, g.y / cnt, g.z / cnt, 0.0f);
+            aw.lrem[j] = make_float4(r.x, r.y, r.z, 0.0f);
+            push = g.x != 0.0f || g.y != 0.0f || g.z != 0.0f;
+        }
+        warp_push(&v.counters[0], v.rayQ0, push, j);
+    }
+}
+
+// Light sample k of a vertex with the factors of its gradient: its clamped
+// contribution c, gL = L w s (material gradient = delta T gL . df) and
+// gE = f R w s (texel gradient of dome 0's texture = delta T gE at `local`),
+// with s the clamp scale held constant.
+__device__ __forceinline__ bool wa_light(const DevScene& s, const DevRequest& q, const AdjView& a, const Vertex& vx,
+                                         const Sampler& smp, uint32_t depth, uint32_t k, const float4* rec, const Mat& ms,
+                                         V3* ld, V3* c, V3* gL, V3* gE, V3* local, bool* envMark) {
+    V3 L, domeRad{0.0f, 0.0f, 0.0f};
+    float w;
+    int32_t envIdx = -1;
+    *local = V3{0.0f, 0.0f, 0.0f};
+    if (k < s.distantCount) {
+        const DevDistant l = s.distant[k];
+        *ld = normalize(l.direction * -1.0f);
+        const float nl = sclamp(dot(vx.n, *ld), 0.0f, 1.0f);
+        if (nl <= 0.0f) return false;
+        L = l.radiance;
+        w = nl;
+    } else {
+        const uint32_t r = k - s.distantCount;
+        const uint32_t li = r / q.domeSamples, jj = r - li * q.domeSamples;
+        const DevDome& d = s.domes[li];
+        const uint32_t dim = kDirectDimBase + depth * kDirectDepthStride + li * kDirectLightStride + jj * kDirectSampleStride;
+        const V2 u = smp.next2d(dim);
+        float lp;
+        if (d.env >= 0) {
+            env_sample(s.envs[d.env], u, (q.flags & SHIRO_RENDER_ENV_CDF) != 0u, local, &lp);
+            if (lp <= 0.0f) return false;
+            L = env_evaluate(env_for_eval(s, a, d.env), *local) * d.radiance;
+            envIdx = d.env;
+            domeRad = d.radiance;
+        } else {
+            const float yy = 1.0f - 2.0f * u.y;
+            const float rr = sqrtf(smax(0.0f, 1.0f - yy * yy));
+            const float phi = 2.0f * kPi * u.x;
+            *local = V3{sinf(phi) * rr, yy, cosf(phi) * rr};
+            lp = kInvFourPi;
+            L = V3{1.0f, 1.0f, 1.0f} * d.radiance;
+        }
+        *ld = light_to_world(d, *local);
+        const float nl = sclamp(dot(vx.n, *ld), 0.0f, 1.0f);
+        if (nl <= 0.0f) return false;
+        const float bp = bsdf_pdf_rec(rec, ms, vx.w, vx.n, vx.cn, vx.view, *ld);
+        const float mis = power_heuristic(lp, bp);
+        w = nl * mis / lp;
+    }
+    const V3 f = bsdf_eval_rec(rec, ms, vx.n, vx.cn, vx.view, *ld);
+    const V3 raw = f * L * w;
+    *c = clamp24(q, raw);
+    const float sc = clamp_scale(q, raw, kDirectSampleClamp);
+    *gL = L * (w * sc);
+    *gE = f * domeRad * (w * sc);
+    *envMark = envIdx >= 0 && envIdx == a.env0;
+    return true;
+}
+
+__global__ void __launch_bounds__(128) wa_shade(WfView v, DevScene s, AdjWave aw, uint32_t cur, uint32_t depth) {
+    const uint32_t count = v.counters[kHitCount];
+    uint32_t* qout = cur ? v.rayQ0 : v.rayQ1;
+    uint32_t* cout = &v.counters[cur ^ 1u];
+    const AdjView& a = *aw.view;
+    for (;;) {
+        const uint32_t wbase = warp_fetch(&v.counters[kFetchShade]);
+        if (wbase >= count) break;
+        const uint32_t i = wbase + lane_id();
+        bool pushRay = false;
+        uint32_t lightMask = 0, j = 0;
+        if (i < count) {
+            j = v.shadeQ[i];
+            const uint4 id = v.ident[j];
+            const DevRequest& q = v.reqs[id.w].q;
+            const float4 o = v.ro[j], d = v.rd[j], t4 = v.T[j], h4 = v.hit[j];
+            const uint32_t bits = __float_as_uint(t4.w);
+            PathState ps;
+            ps.ro = V3{o.x, o.y, o.z};
+            ps.rd = V3{d.x, d.y, d.z};
+            ps.prevPdf = d.w;
+            ps.T = V3{t4.x, t4.y, t4.z};
+            ps.diffDepth = bits & 0xffu;
+            ps.specDepth = (bits >> 8) & 0xffu;
+            ps.prevDelta = (bits & kFlagPrevDelta) != 0u;
+            ps.prevType = (bits >> kTypeShift) & 3u;
+            ps.inside = false;
+            ps.mediumActive = false;
+            HitRec h;
+            h.t = h4.x;
+            h.u = h4.y;
+            h.v = h4.z;
+            h.slot = __float_as_uint(h4.w);
+            h.gid = v.hitGid[j];
+            const Vertex vx = make_vertex(s, ps.ro, ps.rd, h);
+            const uint32_t mat = vx.hit.material;
+            const Mat& ms = s.materials[mat];
+            const float4* rec = bsdf_rec(s, mat);
+            aw.vtx[3 * static_cast<size_t>(j)] = make_float4(vx.n.x, vx.n.y, vx.n.z, __uint_as_float(mat));
+            aw.vtx[3 * static_cast<size_t>(j) + 1] = make_float4(vx.cn.x, vx.cn.y, vx.cn.z, 0.0f);
+            aw.vtx[3 * static_cast<size_t>(j) + 2] = make_float4(vx.view.x, vx.view.y, vx.view.z, 0.0f);
+            const Sampler smp{id.x, id.y, id.z};
+            const uint32_t nls = light_sample_count<false>(s, q);
+            for (uint32_t k = 0; k < nls; ++k) {
+                V3 ld{0.0f, 0.0f, 0.0f}, c{0.0f, 0.0f, 0.0f}, gL{0.0f, 0.0f, 0.0f}, gE{0.0f, 0.0f, 0.0f}, local;
+                bool mark = false;
+                const bool ok = wa_light(s, q, a, vx, smp, depth, k, rec, ms, &ld, &c, &gL, &gE, &local, &mark);
+                lightMask |= ok ? (1u << k) : 0u;
+                const size_t e = static_cast<size_t>(k) * v.P + j;
+                v.shDir[e] = make_float4(ld.x, ld.y, ld.z, ok ? FLT_MAX : 0.0f);
+                v.shC[e] = make_float4(c.x, c.y, c.z, 0.0f);
+                aw.lgrad[3 * e] = make_float4(gL.x, gL.y, gL.z, 0.0f);
+                aw.lgrad[3 * e + 1] = make_float4(gE.x, gE.y, gE.z, mark ? 1.0f : 0.0f);
+                aw.lgrad[3 * e + 2] = make_float4(local.x, local.y, local.z, 0.0f);
+            }
+            const V3 org = shadow_origin(vx);
+            v.shOrigin[j] = make_float4(org.x, org.y, org.z, 0.0f);
+            v.shT[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, 0.0f);
+            // continuation (the reflecting lobes of continue_path)
+            bool alive = false, due = false;
+            V3 next{0.0f, 0.0f, 0.0f}, f{0.0f, 0.0f, 0.0f};
+            const uint32_t base = depth * kPathDimStride;
+            const float rw = vx.w.diffuse + vx.w.spec + vx.w.coat;
+            const float tw = rw + 0.0f;
+            do {
+                if (tw <= 0.0f) break;
+                const float sel = smp.next1d(base + 1u) * tw;
+                const V2 ds = smp.next2d(base + 2u);
+                float pdf;
+                bool delta2 = false;
+                const float rs = sel - 0.0f;
+                uint32_t type = kBounceDiffuse;
+                if (rs < vx.w.diffuse) {
+                    if (ps.diffDepth >= q.diffuseDepth) break;
+                    ++ps.diffDepth;
+                    next = cosine_hemisphere(vx.n, ds);
+                    const float cpdf = sclamp(dot(vx.n, next), 0.0f, 1.0f) * kInvPi;
+                    pdf = smax((rw / tw) * (1.0f * cpdf + 0.0f * 0.0f), 1.0e-6f);
+                } else {
+                    type = kBounceReflective;
+                    const bool coat = !(rs < vx.w.diffuse + vx.w.spec);
+                    if (ps.specDepth >= q.specularDepth) break;
+                    ++ps.specDepth;
+                    const V3 sn = coat ? vx.cn : vx.n;
+                    const float sr = coat ? roughness_for(ms.coat_roughness, ms.coat_anisotropy, ms.coat_rotation)
+                                          : roughness_for(base_roughness(ms), ms.specular_anisotropy, ms.specular_rotation);
+                    const V3 hv = ggx_half(sn, ds, sr);
+                    next = normalize(reflect(ps.rd, hv));
+                    const float rc = sclamp(dot(sn, next), 0.0f, 1.0f);
+                    if (rc <= 0.0f) break;
+                    pdf = smax((rw / tw) * bsdf_pdf_rec(rec, ms, vx.w, vx.n, vx.cn, vx.view, next), 1.0e-6f);
+                    delta2 = sr <= kDeltaRoughness;
+                }
+                f = bsdf_eval_rec(rec, ms, vx.n, vx.cn, vx.view, next);
+                const float cosT = sclamp(dot(vx.n, next), 0.0f, 1.0f);
+                if (cosT <= 0.0f) break;
+                ps.T = clamp12(q, ps.T * f * (cosT / pdf));
+                const float off = dot(vx.n, next) >= 0.0f ? 1.0f : -1.0f;
+                ps.ro = vx.hit.position + vx.n * (kRayEpsilon * off);
+                ps.rd = next;
+                ps.prevDelta = delta2;
+                ps.prevPdf = pdf;
+                ps.prevType = type;
+                alive = true;
+                if (depth >= 2) {
+                    const float cp = sclamp(maxc(ps.T), 0.05f, 0.95f);
+                    if (smp.next1d(base + 4u) > cp) {
+                        alive = false;
+                    } else {
+                        ps.T = ps.T / cp;
+                    }
+                }
+                due = alive && depth + 1u < q.maxDepth;
+            } while (false);
+            aw.cont[2 * static_cast<size_t>(j)] = make_float4(next.x, next.y, next.z, due ? 1.0f : 0.0f);
+            aw.cont[2 * static_cast<size_t>(j) + 1] = make_float4(f.x, f.y, f.z, 0.0f);
+            if (due) {
+                v.T[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, __uint_as_float(pack_state(ps)));
+                v.ro[j] = make_float4(ps.ro.x, ps.ro.y, ps.ro.z, 0.0f);
+                v.rd[j] = make_float4(ps.rd.x, ps.rd.y, ps.rd.z, ps.prevPdf);
+                pushRay = true;
+            }
+        }
+        warp_push(cout, qout, pushRay, j);
+        for (uint32_t k = 0; k < v.lightSamples; ++k)
+            warp_push(&v.counters[4], v.shadowRayQ, (lightMask >> k) & 1u, (j << 3) | k);
+    }
+}
+
+// Gradients of a shaded vertex once its light samples' visibility is known.
+__global__ void __launch_bounds__(128) wa_shadow(WfView v, DevScene s, AdjWave aw) {
+    const uint32_t count = v.counters[kHitCount];
+    const AdjView& a = *aw.view;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t j = v.shadeQ[i];
+        const DevRequest& q = v.reqs[v.ident[j].w].q;
+        const float4 t4 = v.shT[j], dl4 = aw.delta[j], l4 = aw.lrem[j];
+        const float4 v0 = aw.vtx[3 * static_cast<size_t>(j)], v1 = aw.vtx[3 * static_cast<size_t>(j) + 1],
+                     v2 = aw.vtx[3 * static_cast<size_t>(j) + 2];
+        const V3 T0{t4.x, t4.y, t4.z}, dl{dl4.x, dl4.y, dl4.z};
+        const V3 n{v0.x, v0.y, v0.z}, cn{v1.x, v1.y, v1.z}, view{v2.x, v2.y, v2.z};
+        const uint32_t mat = __float_as_uint(v0.w);
+        const Mat& me = a.evalMats[mat];
+        const V3 dT = dl * T0;
+        const V3 direct = sum_direct<false>(s, q, [&](uint32_t k, V3* c) {
+            const size_t e = static_cast<size_t>(k) * v.P + j;
+            const float4 d4 = v.shDir[e];
+            if (d4.w == 0.0f) return false;
+            const float4 c4 = v.shC[e];
+            *c = V3{c4.x, c4.y, c4.z};
+            const float4 g0 = aw.lgrad[3 * e], g1 = aw.lgrad[3 * e + 1];
+            const DV3 fd = bsdf_eval_d(me, n, cn, view, V3{d4.x, d4.y, d4.z});
+            add_mat_grad(a, mat, fd, dT * V3{g0.x, g0.y, g0.z});
+            if (g1.w != 0.0f) {
+                const float4 g2 = aw.lgrad[3 * e + 2];
+                add_env_grad(a, a.evalEnv, V3{g2.x, g2.y, g2.z}, dT * V3{g1.x, g1.y, g1.z});
+            }
+            return true;
+        });
+        const V3 lrem = V3{l4.x, l4.y, l4.z} - T0 * direct;
+        const float4 c0 = aw.cont[2 * static_cast<size_t>(j)];
+        if (c0.w != 0.0f) {
+            const float4 f4 = aw.cont[2 * static_cast<size_t>(j) + 1];
+            const V3 f{f4.x, f4.y, f4.z};
+            const DV3 fd = bsdf_eval_d(me, n, cn, view, V3{c0.x, c0.y, c0.z});
+            const V3 coef{f.x > 0.0f ? dl.x * lrem.x / f.x : 0.0f, f.y > 0.0f ? dl.y * lrem.y / f.y : 0.0f,
+                          f.z > 0.0f ? dl.z * lrem.z / f.z : 0.0f};
+            add_mat_grad(a, mat, fd, coef);
+        }
+        aw.lrem[j] = make_float4(lrem.x, lrem.y, lrem.z, 0.0f);
+    }
+}
+
+// Texel gradients of dome 0's texture from the paths that left the scene.
+__global__ void __launch_bounds__(256) wa_miss(WfView v, DevScene s, AdjWave aw, uint32_t depth) {
+    const uint32_t count = v.counters[kMissCount];
+    const AdjView& a = *aw.view;
+    if (a.env0 < 0 || !a.dEnv4) return;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t j = v.shadeQ[v.P - 1u - i];
+        const DevRequest& q = v.reqs[v.ident[j].w].q;
+        if (!(depth > 0 || q.backgroundVisible)) continue;
+        const float4 d = v.rd[j], t4 = v.T[j], dl4 = aw.delta[j];
+        const V3 rd{d.x, d.y, d.z};
+        const bool prevDelta = (__float_as_uint(t4.w) & kFlagPrevDelta) != 0u;
+        const float mis = (s.domeCount == 0 || depth == 0 || prevDelta) ? 1.0f : env_miss_mis(s, d.w, rd);
+        const V3 T{t4.x, t4.y, t4.z}, dl{dl4.x, dl4.y, dl4.z};
+        for (uint32_t k = 0; k < s.domeCount; ++k) {
+            const DevDome& dm = s.domes[k];
+            if (dm.env != a.env0) continue;
+            add_env_grad(a, a.evalEnv, world_to_light(dm, rd), dl * T * dm.radiance * mis);
+        }
+    }
+}
+
 // Per-path records of the wave in request path order (pixel-major,
 // sample-minor): the radiance a path replay needs (adjoint).
 __global__ void __launch_bounds__(128) wf_records_out(WfView v) {
@@ -682,7 +999,7 @@ __global__ void __launch_bounds__(128) wf_records_out(WfView v) {
 // ===========================================================================
 // One pool of paths in flight with its queues, and the wave graph it replays.
 struct WavePool {
-    DeviceBlock state, shadow, queues, records;
+    DeviceBlock state, shadow, queues, records, adj;
     // the last instantiated wave graph and the launch parameters it bakes in
     // (reused while a call's parameters are byte-identical: only the tables'
     // contents differ between such calls, and the kernels read them from memory)
@@ -702,6 +1019,7 @@ struct WavefrontState {
     // it from / join it to the context's stream
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    DeviceBlock adjView;  // device copy of the adjoint's parameter view
 };
 
 namespace {
@@ -844,8 +1162,24 @@ struct Launch {
     uint32_t shadeRegs;
     uint32_t binRays, binShadow;  // queue binning before extend (bounces >= 1) / occlude
     int gBin;
+    AdjWave aw;                   // aw.on: the adjoint replay follows the forward stages
+    int gAdjShade, gAdjShadow, gAdjMiss;
     bool ext;  // the scene uses transmission, opacity or emitters
 };
+
+void enqueue_replay(const Launch& L, cudaStream_t st) {
+    wa_begin<<<1, 32, 0, st>>>(L.v);
+    wa_generate<<<L.gGen, 128, 0, st>>>(L.v, L.aw);
+    for (uint32_t d = 0; d < L.depth; ++d) {
+        const uint32_t cur = d & 1u;
+        wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, 0u);
+        wa_shade<<<L.gAdjShade, 128, 0, st>>>(L.v, L.s, L.aw, cur, d);
+        wa_miss<<<L.gAdjMiss, 256, 0, st>>>(L.v, L.s, L.aw, d);
+        wf_occlude<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s, 0u);
+        wa_shadow<<<L.gAdjShadow, 128, 0, st>>>(L.v, L.s, L.aw);
+        wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur);
+    }
+}
 
 void enqueue_binning(const Launch& L, cudaStream_t st, uint32_t which, uint32_t cur) {
     cudaMemsetAsync(L.v.binCount, 0, kBins * sizeof(uint32_t), st);
@@ -882,7 +1216,8 @@ void enqueue_wave(const Launch& L, cudaStream_t st) {
         wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s);
         wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur);
     }
-    if (L.v.recordsOut) wf_records_out<<<L.gRes, 128, 0, st>>>(L.v);
+    if (L.aw.on) enqueue_replay(L, st);
+    else if (L.v.recordsOut) wf_records_out<<<L.gRes, 128, 0, st>>>(L.v);
     else wf_resolve<<<L.gRes, 128, 0, st>>>(L.v);
 }
 
@@ -915,7 +1250,8 @@ void enqueue_wave_timed(const Launch& L, cudaStream_t st, std::vector<std::pair<
         timed(5, [&] { wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur); });
     }
     timed(4, [&] {
-        if (L.v.recordsOut) wf_records_out<<<L.gRes, 128, 0, st>>>(L.v);
+        if (L.aw.on) enqueue_replay(L, st);
+        else if (L.v.recordsOut) wf_records_out<<<L.gRes, 128, 0, st>>>(L.v);
         else wf_resolve<<<L.gRes, 128, 0, st>>>(L.v);
     });
 }
@@ -924,7 +1260,7 @@ void enqueue_wave_timed(const Launch& L, cudaStream_t st, std::vector<std::pair<
 // `cfg`.  maxWaves limits the waves run (autotuning); returns paths traced.
 int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& cfg, const std::vector<DevRequest>& qs,
               const std::vector<AovPtrs>& aovs, const volatile int* cancel, uint32_t maxWaves, uint64_t* pathsOut,
-              double* msOut, float4* recordsOut = nullptr) {
+              double* msOut, float4* recordsOut = nullptr, const AdjView* adj = nullptr) {
     uint32_t lightSamples = ctx->scene.distantCount;
     uint32_t domeSamplesMax = 1;
     for (const DevRequest& q : qs) domeSamplesMax = std::max(domeSamplesMax, q.domeSamples);
@@ -948,6 +1284,16 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     for (uint32_t w = 0; w < used; ++w) poolP[w % nl] = std::max(poolP[w % nl], pl.waves[w].paths);
     for (uint32_t k = 0; k < nl; ++k)
         if (!ensure_pool(ctx, &wf->pools[k], poolP[k], lightSamples)) return SHIRO_ERR_OUT_OF_MEMORY;
+    if (adj) {  // per-slot replay state of each pool, and the parameter view on the device
+        for (uint32_t k = 0; k < nl; ++k)
+            if (!ensure_block(ctx, &wf->pools[k].adj,
+                              static_cast<size_t>(poolP[k]) * (kAdjSlotFloat4 + kAdjLightFloat4 * std::max(1u, lightSamples)) *
+                                  sizeof(float4), "adjoint replay state"))
+                return SHIRO_ERR_OUT_OF_MEMORY;
+        if (!ensure_block(ctx, &wf->adjView, sizeof(AdjView), "adjoint view")) return SHIRO_ERR_OUT_OF_MEMORY;
+        const cudaError_t ce = cudaMemcpyAsync(wf->adjView.ptr, adj, sizeof(AdjView), cudaMemcpyHostToDevice, ctx->stream);
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "adjoint view");
+    }
     if (nl > 1 && !wf->side) {
         cudaError_t ce = cudaStreamCreateWithFlags(&wf->side, cudaStreamNonBlocking);
         if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&wf->fork, cudaEventDisableTiming);
@@ -997,6 +1343,9 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.gOcc = grid_for(wf_occlude, L.bShadow, wf->smCount);
     L.gRes = grid_for(wf_resolve, 128, wf->smCount);
     L.gBin = grid_for(wf_bin_scatter, 256, wf->smCount);
+    L.gAdjShade = grid_for(wa_shade, 128, wf->smCount);
+    L.gAdjShadow = grid_for(wa_shadow, 128, wf->smCount);
+    L.gAdjMiss = grid_for(wa_miss, 256, wf->smCount);
     L.binRays = cfg.bin_rays == 1 ? 1u : 0u;
     L.binShadow = cfg.bin_shadow == 1 ? 1u : 0u;
     {
@@ -1007,6 +1356,22 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
                           ext.z > 0.0f ? 8.0f / ext.z : 0.0f};
     }
     L.depth = pl.maxDepth;
+    auto adj_wave = [&](uint32_t k) {
+        AdjWave aw;
+        std::memset(&aw, 0, sizeof(aw));
+        if (!adj) return aw;
+        const size_t p = poolP[k];
+        float4* b = static_cast<float4*>(wf->pools[k].adj.ptr);
+        aw.view = static_cast<const AdjView*>(wf->adjView.ptr);
+        aw.lrem = b;
+        aw.delta = b + p;
+        aw.vtx = b + 2 * p;
+        aw.cont = b + 5 * p;
+        aw.lgrad = b + 7 * p;
+        aw.on = 1u;
+        return aw;
+    };
+    L.aw = adj_wave(0);
     Launch lanes[kMaxConcurrentWaves];
     for (uint32_t k = 0; k < nl; ++k) {
         std::memcpy(&lanes[k], &L, sizeof(Launch));  // bytes, padding included: they key the graph cache
@@ -1019,6 +1384,8 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             v.binScale = L.v.binScale;
             v.recordsOut = recordsOut;
             std::memcpy(&lanes[k].v, &v, sizeof(WfView));
+            const AdjWave aw = adj_wave(k);
+            std::memcpy(&lanes[k].aw, &aw, sizeof(AdjWave));
         }
         // wf_begin adds the stride to the wave index: start one stride below k
         const uint32_t first = k - nl;
@@ -1089,7 +1456,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
         }
         throttle.after_launch(exec[k] && k != 0 ? wf->side : st);
         launches += 3 + 6ull * L.depth + (L.binShadow ? 3ull * L.depth : 0ull) +
-                (L.binRays && L.depth > 1 ? 3ull * (L.depth - 1) : 0ull);
+                (L.binRays && L.depth > 1 ? 3ull * (L.depth - 1) : 0ull) + (adj ? 2ull + 6ull * L.depth - 1ull : 0ull);
         ++launchedWaves;
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront launch");
     }
@@ -1231,16 +1598,26 @@ int wavefront_path_records(ContextImpl* ctx, const ShiroRenderDesc& req, float4*
     return run_waves(ctx, wf, wf->cfg, qs, aov, nullptr, 0xffffffffu, &paths, nullptr, out);
 }
 
+int wavefront_adjoint(ContextImpl* ctx, const ShiroRenderDesc& req, const AdjView& adj) {
+    if (!ctx->hasScene) return fail(ctx, SHIRO_ERR_NO_SCENE, "no scene uploaded");
+    WavefrontState* wf = wf_state(ctx);
+    std::vector<DevRequest> qs{make_request(req)};
+    std::vector<AovPtrs> aov{AovPtrs{nullptr, nullptr, nullptr, nullptr}};
+    uint64_t paths = 0;
+    return run_waves(ctx, wf, wf->cfg, qs, aov, nullptr, 0xffffffffu, &paths, nullptr, nullptr, &adj);
+}
+
 void wavefront_free(ContextImpl* ctx) {
     if (!ctx->wavefront) return;
     WavefrontState* wf = ctx->wavefront;
     if (wf->side) cudaStreamSynchronize(wf->side);
     for (WavePool& pool : wf->pools) {
         if (pool.exec) cudaGraphExecDestroy(pool.exec);
-        for (DeviceBlock* b : {&pool.state, &pool.shadow, &pool.queues, &pool.records})
+        for (DeviceBlock* b : {&pool.state, &pool.shadow, &pool.queues, &pool.records, &pool.adj})
             if (b->ptr) cudaFree(b->ptr);
     }
     if (wf->tables.ptr) cudaFree(wf->tables.ptr);
+    if (wf->adjView.ptr) cudaFree(wf->adjView.ptr);
     if (wf->fork) cudaEventDestroy(wf->fork);
     if (wf->join) cudaEventDestroy(wf->join);
     if (wf->side) cudaStreamDestroy(wf->side);

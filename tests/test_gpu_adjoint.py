@@ -254,3 +254,34 @@ def test_adjoint_rejects_extended_lobes():
         with pytest.raises(ShiroGpuError) as ei:
             gpu.adjoint(cam, st, d, grads)
         assert ei.value.code == -5
+
+
+@pytest.mark.parametrize("pool", [0, 4096])
+@pytest.mark.parametrize("flags", [NO_CLAMP, 0])
+def test_wavefront_replay_equals_per_thread_replay(setup, flags, pool):
+    """The adjoint's two forms - replay stages in the wavefront pool after
+    each wave's forward stages (default), and one thread per path - add the
+    same gradients, up to the order of their float atomics; with a pool of
+    4096 paths the request spans several waves on two pools."""
+    gpu, scene, cam, st, p = setup
+    gpu.set_params(**p)
+    gen = torch.Generator(device="cpu").manual_seed(5)
+    d = (torch.rand((st.height, st.width, 4), generator=gen) - 0.3).cuda()
+    d[..., 3] = 0.0
+    base = gpu.wavefront_config()
+    out = {}
+    try:
+        if pool:
+            gpu.set_wavefront_config(paths_in_flight=pool, concurrent_waves=2, use_graph=1)
+        for form in (True, False):
+            g = {k: torch.zeros_like(v) for k, v in p.items()}
+            gpu.set_adjoint_form(form)
+            gpu.adjoint(cam, st, d, g, flags=flags)
+            out[form] = g
+    finally:
+        gpu.set_adjoint_form(True)
+        gpu.set_wavefront_config(**base)
+    for k in p:
+        a, b = out[True][k], out[False][k]
+        assert a.abs().max() > 0, k
+        torch.testing.assert_close(a, b, rtol=1e-3, atol=1e-5 * float(b.abs().max()), msg=k)
