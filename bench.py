@@ -70,6 +70,8 @@ def parse():
     p.add_argument("--no-autotune", action="store_true", help="keep the current wavefront configuration")
     p.add_argument("--adjoint-only", type=int, default=0, metavar="SIZE",
                    help="only the adjoint measurement, on a SIZE x SIZE frame (profiling cases); prints its JSON")
+    p.add_argument("--adjoint-form", choices=["wavefront", "thread"], default="wavefront",
+                   help="adjoint replay: wavefront stages (default) or one thread per path")
     p.add_argument("--wf-config", default="",
                    help="wavefront configuration to set before measuring (with --no-autotune: the one measured), "
                         "e.g. paths_in_flight=33554432,concurrent_waves=2")
@@ -259,7 +261,8 @@ def cpu_baseline(w, seconds: float, rank: int = 0) -> dict:
             "cpu": cpu, "seconds": t_render, "paths": int(paths)}
 
 
-def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 2, size: int = 512) -> dict:
+def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 2, size: int = 512,
+                  form: str = "wavefront") -> dict:
     """Gradient throughput of the differentiable form on the 256-material
     sphere scene: 512x512 (`size` for profiling cases), 32 spp, depth 6, L2
     loss against a seeded target, gradients for 256 x (base colour, roughness,
@@ -276,6 +279,7 @@ def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 
     cam = scenes.sphere_camera(1.0)
     gpu = GpuBackend(local)
     gpu.set_bvh_width(bvh_width)
+    gpu.set_adjoint_form(form == "wavefront")
     stream = torch.cuda.current_stream()
     gpu.lib.shiro_gpu_set_stream(gpu.handle, stream.cuda_stream)
     gpu.upload_scene(scene)
@@ -310,7 +314,7 @@ def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 
     paths = size * size * 32
     gpu.close()
     return {"workload": f"256-material sphere scene, 512x256 env, {size}x{size}, 32 spp, depth 6, L2 loss",
-            "params": int(nparams), "ms_per_gradient": ms, "grads_per_s": 1000.0 / ms,
+            "replay": form, "params": int(nparams), "ms_per_gradient": ms, "grads_per_s": 1000.0 / ms,
             "adjoint_ms": adj_ms / iters, "adjoint_Mpaths_s": paths / (adj_ms / iters / 1000.0) / 1e6,
             "param_gradients_per_s": nparams * 1000.0 / ms}
 
@@ -520,7 +524,7 @@ def main():
     if args.adjoint_only:
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         res = adjoint_bench(int(os.environ.get("LOCAL_RANK", "0")), iters=args.steps, warmup=args.warmup,
-                            bvh_width=args.bvh_width, size=args.adjoint_only)
+                            bvh_width=args.bvh_width, size=args.adjoint_only, form=args.adjoint_form)
         print(json.dumps(res), flush=True)
         return 0
     world = int(os.environ.get("WORLD_SIZE", "1"))

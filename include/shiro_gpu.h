@@ -354,6 +354,11 @@ typedef struct ShiroWavefrontConfig {
                                   the current value */
     uint32_t bin_shadow;       /* the same for the occlusion queue (buckets of light sample x
                                   octant x origin cell): 1 on, 2 off, 0 leaves the current value */
+    uint32_t coop_extend;      /* 1: the closest-hit stage visits one wide node per lane and step
+                                  and tests the step's leaf triangles with the whole warp (up to
+                                  32 ray-triangle pairs per round); 2: each lane tests its own;
+                                  0 leaves the current value.  Hits are identical either way. */
+    uint32_t coop_occlude;     /* the same for the occlusion stage: 1 on, 2 off, 0 leaves it */
 } ShiroWavefrontConfig;
 int shiro_gpu_get_wavefront_config(const ShiroGpuContext* ctx, ShiroWavefrontConfig* out);
 int shiro_gpu_set_wavefront_config(ShiroGpuContext* ctx, const ShiroWavefrontConfig* cfg);

@@ -70,35 +70,60 @@ __device__ __forceinline__ int env_footprint(const DevEnv& e, const V3& local, u
     return 4;
 }
 
+// Sums v over the lanes of `active` that hold the same key; the group's
+// lowest lane ends with the sum and is the one that returns true.  Each round
+// a lane adds the partial sum of the next remaining peer above it, then the
+// lanes of odd rank drop out: log2(group size) rounds of shuffles (the peer
+// reduction of E. Westphal, "Voting and Shuffling to Optimize Atomic
+// Operations", NVIDIA developer blog, 2015).  Every lane of `active` must call
+// it with the same N.
+template <int N>
+__device__ __forceinline__ bool group_sum(uint32_t active, uint32_t key, float (&v)[N]) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t peers = __match_any_sync(active, key);
+    const bool leader = static_cast<uint32_t>(__ffs(peers) - 1) == lane;
+    uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+    peers &= ~((2u << lane) - 1u);  // peers above this lane (none above lane 31)
+    while (__any_sync(active, peers != 0u)) {
+        const int next = __ffs(peers);
+        const int src = next ? next - 1 : static_cast<int>(lane);
+#pragma unroll
+        for (int p = 0; p < N; ++p) {
+            const float t = __shfl_sync(active, v[p], src);
+            if (next) v[p] += t;
+        }
+        peers &= __ballot_sync(active, (rank & 1u) == 0u);
+        rank >>= 1;
+    }
+    return leader;
+}
+
 // One vector atomic per texel of the bilinear footprint (16-byte aligned
-// float4 accumulators instead of three scalar atomics on the caller's rgb).
+// float4 accumulators instead of three scalar atomics on the caller's rgb),
+// after the lanes that add to the same texel have summed: importance-sampled
+// dome samples crowd onto the few brightest texels, and lanes adding to one
+// address one after another stalled the whole replay.
 __device__ __forceinline__ void add_env_grad(const AdjView& a, const DevEnv& e, const V3& local, const V3& coef) {
-    if (!a.dEnv4 || (coef.x == 0.0f && coef.y == 0.0f && coef.z == 0.0f)) return;
-    uint32_t idx[4];
-    float w[4];
-    const int n = env_footprint(e, local, idx, w);
-    for (int k = 0; k < n; ++k) {
-        if (w[k] == 0.0f) continue;
-        atomicAdd(&a.dEnv4[idx[k]], make_float4(coef.x * w[k], coef.y * w[k], coef.z * w[k], 0.0f));
+    if (!a.dEnv4) return;
+    uint32_t idx[4] = {0u, 0u, 0u, 0u};
+    float w[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const int n = (coef.x == 0.0f && coef.y == 0.0f && coef.z == 0.0f) ? 0 : env_footprint(e, local, idx, w);
+    const uint32_t active = __activemask();
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t key = (k < n && w[k] != 0.0f) ? idx[k] : 0xffffffffu;
+        float g[3] = {coef.x * w[k], coef.y * w[k], coef.z * w[k]};
+        if (group_sum(active, key, g) && key != 0xffffffffu) atomicAdd(&a.dEnv4[key], make_float4(g[0], g[1], g[2], 0.0f));
     }
 }
 
 // dL/dparams of material `mat` += sum_c coef_c * df_c (df from the duals).
-// A full warp on one material (the common case: a warp holds consecutive
-// samples of one pixel) sums its lanes first and adds once; otherwise each
-// lane adds its own.
+// The lanes on one material sum first and add once.
 __device__ __forceinline__ void add_mat_grad(const AdjView& a, uint32_t mat, const DV3& f, const V3& coef) {
-    if (mat >= a.materialCount) return;
     float g[kDualN];
 #pragma unroll
     for (int p = 0; p < kDualN; ++p) g[p] = coef.x * f.x.d[p] + coef.y * f.y.d[p] + coef.z * f.z.d[p];
-    const uint32_t active = __activemask();
-    if (__match_any_sync(active, mat) == 0xffffffffu) {
-#pragma unroll
-        for (int p = 0; p < kDualN; ++p)
-            for (int o = 16; o > 0; o >>= 1) g[p] += __shfl_xor_sync(0xffffffffu, g[p], o);
-        if ((threadIdx.x & 31u) != 0u) return;
-    }
+    const uint32_t key = mat < a.materialCount ? mat : 0xffffffffu;
+    if (!group_sum(__activemask(), key, g) || key == 0xffffffffu) return;
     if (a.dBase) {
         for (int c = 0; c < 3; ++c)
             if (g[c] != 0.0f) atomicAdd(&a.dBase[3 * mat + c], g[c]);

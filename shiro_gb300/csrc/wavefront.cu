@@ -383,15 +383,192 @@ __device__ __forceinline__ void flush_stage(uint32_t* buf, uint32_t& n, uint32_t
     n = rest;
 }
 
+// ---- warp-cooperative triangle tests ----------------------------------------
+// A wide node's leaf triangles are tested by the lanes whose ray reached it;
+// tested lane by lane, a step in which a few lanes hold triangles keeps the
+// rest of the warp waiting for the longest list.  Here every lane's pending
+// triangles are packed into rounds of 32 (lane, triangle) pairs, one pair per
+// lane, so a step costs ceil(total / 32) triangle tests instead of the
+// longest list.  The hit of a ray is the smallest key (t bits << 32 | global
+// triangle id) over its pairs - t > 0, so the float's bits order as the
+// float does, and the key order is exactly the (t, mesh order) tie rule -
+// which makes the result independent of which lane tested which triangle.
+struct CoopTris {
+    uint32_t tri[32];              // pair -> triangle (wide order)
+    uint32_t src[32];              // pair -> lane whose ray it tests
+    unsigned long long best[32];   // lane -> key of its closest hit so far
+    float2 uv[32];                 // lane -> barycentrics of that hit
+    uint32_t slot[32];             // lane -> its triangle
+};
+
+// Packs up to 32 of the warp's pending (lane, triangle) pairs into c.tri /
+// c.src, lanes in order, and removes them from `bits`; returns the number of
+// pairs (0: none pending anywhere).  Warp-uniform call.
+__device__ __forceinline__ uint32_t coop_pack(uint32_t tBase, uint32_t& bits, CoopTris& c) {
+    const uint32_t lane = lane_id();
+    const uint32_t cnt = __popc(bits);
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += y;
+    }
+    const uint32_t total = __shfl_sync(kFull, incl, 31);
+    if (total == 0u) return 0u;
+    const uint32_t excl = incl - cnt;
+    const uint32_t take = excl < 32u ? min(cnt, 32u - excl) : 0u;
+    for (uint32_t k = 0; k < take; ++k) {
+        const uint32_t b = static_cast<uint32_t>(__ffs(bits) - 1);
+        bits &= bits - 1u;
+        c.tri[excl + k] = tBase + b;
+        c.src[excl + k] = lane;
+    }
+    __syncwarp();
+    return min(total, 32u);
+}
+
+// Closest hits of the triangles each lane's current node left in
+// (tBase, tBits); updates the lane's WideTrav.  Warp-uniform call.
+__device__ __forceinline__ void coop_closest(const DevScene& s, WideTrav& t, uint32_t tBase, uint32_t tBits, CoopTris& c) {
+    const uint32_t lane = lane_id();
+    const unsigned long long mine = (static_cast<unsigned long long>(__float_as_uint(t.tmax)) << 32) | t.bestGid;
+    c.best[lane] = mine;
+    uint32_t bits = tBits;
+    bool any = false;
+    for (;;) {
+        const uint32_t n = coop_pack(tBase, bits, c);
+        if (n == 0u) break;
+        any = true;
+        const bool pair = lane < n;
+        const uint32_t tri = pair ? c.tri[lane] : 0u;
+        const uint32_t src = pair ? c.src[lane] : lane;
+        const V3 o{__shfl_sync(kFull, t.o.x, src), __shfl_sync(kFull, t.o.y, src), __shfl_sync(kFull, t.o.z, src)};
+        const V3 d{__shfl_sync(kFull, t.d.x, src), __shfl_sync(kFull, t.d.y, src), __shfl_sync(kFull, t.d.z, src)};
+        unsigned long long key = ~0ull;
+        float u = 0.0f, w = 0.0f;
+        if (pair) {
+            const float4* tp = s.tris + 3 * static_cast<size_t>(tri);
+            const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
+            float tt;
+            if (tri_test(o, d, kRayEpsilon, FLT_MAX, ta, tb, tc, &tt, &u, &w)) {
+                key = (static_cast<unsigned long long>(__float_as_uint(tt)) << 32) | __float_as_uint(ta.w);
+                atomicMin(&c.best[src], key);
+            }
+        }
+        __syncwarp();
+        if (key != ~0ull && c.best[src] == key) {  // one winner per ray: keys are unique
+            c.uv[src] = make_float2(u, w);
+            c.slot[src] = tri;
+        }
+        __syncwarp();
+    }
+    if (any) {
+        const unsigned long long b = c.best[lane];
+        if (b != mine) {
+            t.tmax = __uint_as_float(static_cast<uint32_t>(b >> 32));
+            t.bestGid = static_cast<uint32_t>(b);
+            t.bestSlot = c.slot[lane];
+            t.bu = c.uv[lane].x;
+            t.bv = c.uv[lane].y;
+        }
+    }
+    __syncwarp();
+}
+
+// Any hit in [1e-4, tmax] among the triangles each lane's current node left
+// in (tBase, tBits): returns the mask of lanes whose ray is occluded.
+// Warp-uniform call.
+__device__ __forceinline__ uint32_t coop_any(const DevScene& s, const WideTrav& t, uint32_t tBase, uint32_t tBits,
+                                             CoopTris& c) {
+    const uint32_t lane = lane_id();
+    uint32_t bits = tBits, occ = 0u;
+    for (;;) {
+        const uint32_t n = coop_pack(tBase, bits, c);
+        if (n == 0u) break;
+        const bool pair = lane < n;
+        const uint32_t tri = pair ? c.tri[lane] : 0u;
+        const uint32_t src = pair ? c.src[lane] : lane;
+        const V3 o{__shfl_sync(kFull, t.o.x, src), __shfl_sync(kFull, t.o.y, src), __shfl_sync(kFull, t.o.z, src)};
+        const V3 d{__shfl_sync(kFull, t.d.x, src), __shfl_sync(kFull, t.d.y, src), __shfl_sync(kFull, t.d.z, src)};
+        const float tmax = __shfl_sync(kFull, t.tmax, src);
+        bool hit = false;
+        if (pair) {
+            const float4* tp = s.tris + 3 * static_cast<size_t>(tri);
+            const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
+            float tt, u, w;
+            hit = tri_test(o, d, kRayEpsilon, tmax, ta, tb, tc, &tt, &u, &w);
+        }
+        occ |= __reduce_or_sync(kFull, hit ? (1u << src) : 0u);
+        if ((occ >> lane) & 1u) bits = 0u;  // an occluded ray needs no further tests
+        __syncwarp();
+    }
+    return occ;
+}
+
 // Closest hit of every queued ray.  The ray is then queued for shading with
 // the hits at the front of the shade queue and the misses at its back, so the
 // shade stage runs warps of hits and warps of misses instead of warps that
 // take both branches.
+template <bool kCoop>
 __global__ void __launch_bounds__(256, 4) wf_extend(WfView v, DevScene s, uint32_t cur, uint32_t binned) {
     __shared__ uint32_t stage[8][2][64];
     const uint32_t count = v.counters[cur];
     const uint32_t* q = binned ? v.sortedQ : (cur ? v.rayQ1 : v.rayQ0);
     NullCounter ctr;
+    if (kCoop && s.nodes8) {
+        // one node per lane and step, the step's triangles tested by the whole warp
+        __shared__ CoopTris coop[8];
+        CoopTris& c = coop[threadIdx.x >> 5];
+        uint32_t* hb = stage[threadIdx.x >> 5][0];
+        uint32_t* mb = stage[threadIdx.x >> 5][1];
+        const uint32_t ltMask = (1u << lane_id()) - 1u;
+        uint2 stack[kStackWide];
+        WideTrav t;
+        wide_init(t, V3{0.0f, 0.0f, 0.0f}, V3{0.0f, 0.0f, 1.0f}, 0.0f);
+        LaneFeed feed;
+        bool has = false;
+        uint32_t j = 0, hc = 0, mc = 0;
+        for (;;) {
+            const uint32_t got = feed_lanes(feed, &v.counters[kFetchExtend], count, has, v.refillIdle);
+            if (got != 0xffffffffu) {
+                j = q[got];
+                const float4 o = v.ro[j], d = v.rd[j];
+                wide_init(t, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, FLT_MAX);
+                has = true;
+            }
+            if (__ballot_sync(kFull, has) == 0u) break;
+            uint32_t gBase = 0, gImask = 0, gInner = 0, tBase = 0, tBits = 0;
+            bool fin = false;
+            if (has) {
+                if (++t.visits > kMaxVisits) {
+                    atomicOr(s.error, kErrTraversalLimit);
+                    t.bestSlot = 0xffffffffu;
+                    fin = true;
+                } else {
+                    wide_node(s, t.node, t.r, t.tmax, t.octInv, &gBase, &gImask, &gInner, &tBase, &tBits);
+                }
+            }
+            coop_closest(s, t, tBase, tBits, c);
+            if (has && !fin) fin = !wide_next(s, t, stack, gBase, gImask, gInner);
+            if (fin) {
+                v.hit[j] = make_float4(t.tmax, t.bu, t.bv, __uint_as_float(t.bestSlot));
+                v.hitGid[j] = t.bestGid;
+                has = false;
+            }
+            const bool hit = fin && t.bestSlot != 0xffffffffu;
+            const uint32_t hbal = __ballot_sync(kFull, hit), mbal = __ballot_sync(kFull, fin && !hit);
+            if (hit) hb[hc + __popc(hbal & ltMask)] = j;
+            if (fin && !hit) mb[mc + __popc(mbal & ltMask)] = j;
+            hc += __popc(hbal);
+            mc += __popc(mbal);
+            __syncwarp();
+            if (hc >= 32u) flush_stage(hb, hc, 32u, &v.counters[kHitCount], v.shadeQ, v.P, false);
+            if (mc >= 32u) flush_stage(mb, mc, 32u, &v.counters[kMissCount], v.shadeQ, v.P, true);
+        }
+        if (hc) flush_stage(hb, hc, hc, &v.counters[kHitCount], v.shadeQ, v.P, false);
+        if (mc) flush_stage(mb, mc, mc, &v.counters[kMissCount], v.shadeQ, v.P, true);
+        return;
+    }
     if (s.nodes8) {
         uint32_t* hb = stage[threadIdx.x >> 5][0];
         uint32_t* mb = stage[threadIdx.x >> 5][1];
@@ -590,10 +767,56 @@ __global__ void __launch_bounds__(256) wf_miss(WfView v, DevScene s, uint32_t de
 // (Lane refill as in wf_extend measured slower here: shadow rays are short
 // and an any-hit ends them early, so the refill bookkeeping outweighs the
 // divergence it removes.)
+template <bool kCoop>
 __global__ void __launch_bounds__(256, 4) wf_occlude(WfView v, DevScene s, uint32_t binned) {
     const uint32_t count = v.counters[4];
     const uint32_t* sq = binned ? v.sortedQ : v.shadowRayQ;
     NullCounter ctr;
+    if (kCoop && s.nodes8) {
+        // one node per lane and step, the step's triangles tested by the whole warp
+        __shared__ CoopTris coop[8];
+        CoopTris& c = coop[threadIdx.x >> 5];
+        uint2 stack[kStackWide];
+        for (;;) {
+            const uint32_t base = warp_fetch(&v.counters[kFetchOcclude]);
+            if (base >= count) break;
+            const uint32_t i = base + lane_id();
+            bool live = i < count;
+            size_t e = 0;
+            WideTrav t;
+            wide_init(t, V3{0.0f, 0.0f, 0.0f}, V3{0.0f, 0.0f, 1.0f}, 0.0f);
+            if (live) {
+                const uint32_t item = sq[i];
+                const uint32_t j = item >> 3, k = item & 7u;
+                e = static_cast<size_t>(k) * v.P + j;
+                const float4 o4 = v.shOrigin[j], d4 = v.shDir[e];
+                wide_init(t, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, d4.w);
+            }
+            bool occluded = false;
+            while (__ballot_sync(kFull, live) != 0u) {
+                uint32_t gBase = 0, gImask = 0, gInner = 0, tBase = 0, tBits = 0;
+                if (live) {
+                    if (++t.visits > kMaxVisits) {
+                        atomicOr(s.error, kErrTraversalLimit);
+                        live = false;
+                    } else {
+                        wide_node(s, t.node, t.r, t.tmax, t.octInv, &gBase, &gImask, &gInner, &tBase, &tBits);
+                    }
+                }
+                const uint32_t occ = coop_any(s, t, tBase, tBits, c);
+                if (live) {
+                    if ((occ >> lane_id()) & 1u) {
+                        occluded = true;
+                        live = false;
+                    } else if (!wide_next(s, t, stack, gBase, gImask, gInner)) {
+                        live = false;
+                    }
+                }
+            }
+            if (occluded) v.shDir[e].w = 0.0f;
+        }
+        return;
+    }
     for (;;) {
         const uint32_t base = warp_fetch(&v.counters[kFetchOcclude]);
         if (base >= count) break;
@@ -915,7 +1138,7 @@ __global__ void __launch_bounds__(128) wa_shade(WfView v, DevScene s, AdjWave aw
 }
 
 // Gradients of a shaded vertex once its light samples' visibility is known.
-__global__ void __launch_bounds__(128) wa_shadow(WfView v, DevScene s, AdjWave aw) {
+__global__ void __launch_bounds__(128, 4) wa_shadow(WfView v, DevScene s, AdjWave aw) {
     const uint32_t count = v.counters[kHitCount];
     const AdjView& a = *aw.view;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
@@ -1039,6 +1262,8 @@ WavefrontState* wf_state(ContextImpl* ctx) {
         c.concurrent_waves = 2;
         c.bin_rays = 2;
         c.bin_shadow = 2;
+        c.coop_extend = 2;
+        c.coop_occlude = 2;
         cudaDeviceGetAttribute(&ctx->wavefront->smCount, cudaDevAttrMultiProcessorCount, ctx->device);
     }
     return ctx->wavefront;
@@ -1161,21 +1386,36 @@ struct Launch {
     uint32_t depth;
     uint32_t shadeRegs;
     uint32_t binRays, binShadow;  // queue binning before extend (bounces >= 1) / occlude
+    uint32_t coopExt, coopOcc;    // warp-cooperative triangle tests in extend / occlude
     int gBin;
     AdjWave aw;                   // aw.on: the adjoint replay follows the forward stages
     int gAdjShade, gAdjShadow, gAdjMiss;
     bool ext;  // the scene uses transmission, opacity or emitters
 };
 
+void launch_extend(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t binned) {
+    if (L.coopExt)
+        wf_extend<true><<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, binned);
+    else
+        wf_extend<false><<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, binned);
+}
+
+void launch_occlude(const Launch& L, cudaStream_t st, uint32_t binned) {
+    if (L.coopOcc)
+        wf_occlude<true><<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s, binned);
+    else
+        wf_occlude<false><<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s, binned);
+}
+
 void enqueue_replay(const Launch& L, cudaStream_t st) {
     wa_begin<<<1, 32, 0, st>>>(L.v);
     wa_generate<<<L.gGen, 128, 0, st>>>(L.v, L.aw);
     for (uint32_t d = 0; d < L.depth; ++d) {
         const uint32_t cur = d & 1u;
-        wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, 0u);
+        launch_extend(L, st, cur, 0u);
         wa_shade<<<L.gAdjShade, 128, 0, st>>>(L.v, L.s, L.aw, cur, d);
         wa_miss<<<L.gAdjMiss, 256, 0, st>>>(L.v, L.s, L.aw, d);
-        wf_occlude<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s, 0u);
+        launch_occlude(L, st, 0u);
         wa_shadow<<<L.gAdjShadow, 128, 0, st>>>(L.v, L.s, L.aw);
         wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur);
     }
@@ -1209,10 +1449,10 @@ void enqueue_wave(const Launch& L, cudaStream_t st) {
         const uint32_t cur = d & 1u;
         const uint32_t br = (L.binRays && d > 0) ? 1u : 0u;  // camera rays are coherent already
         if (br) enqueue_binning(L, st, 0u, cur);
-        wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, br);
+        launch_extend(L, st, cur, br);
         launch_shade(L, st, cur, d);
         if (L.binShadow) enqueue_binning(L, st, 1u, cur);
-        wf_occlude<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s, L.binShadow);
+        launch_occlude(L, st, L.binShadow);
         wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s);
         wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur);
     }
@@ -1239,12 +1479,12 @@ void enqueue_wave_timed(const Launch& L, cudaStream_t st, std::vector<std::pair<
         const uint32_t br = (L.binRays && d > 0) ? 1u : 0u;
         timed(1, [&] {
             if (br) enqueue_binning(L, st, 0u, cur);
-            wf_extend<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, br);
+            launch_extend(L, st, cur, br);
         });
         timed(2, [&] { launch_shade(L, st, cur, d); });
         timed(3, [&] {
             if (L.binShadow) enqueue_binning(L, st, 1u, cur);
-            wf_occlude<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s, L.binShadow);
+            launch_occlude(L, st, L.binShadow);
         });
         timed(5, [&] { wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s); });
         timed(5, [&] { wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur); });
@@ -1329,7 +1569,9 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.bShade = static_cast<int>(cfg.shade_block);
     L.bShadow = static_cast<int>(cfg.shadow_block);
     L.gGen = grid_for(wf_generate, 128, wf->smCount);
-    L.gExt = grid_for(wf_extend, L.bExt, wf->smCount);
+    L.coopExt = cfg.coop_extend == 1 ? 1u : 0u;
+    L.coopOcc = cfg.coop_occlude == 1 ? 1u : 0u;
+    L.gExt = L.coopExt ? grid_for(wf_extend<true>, L.bExt, wf->smCount) : grid_for(wf_extend<false>, L.bExt, wf->smCount);
     L.shadeRegs = cfg.shade_regs;
     L.ext = ctx->extendedMaterials;
     L.gShade = L.shadeRegs == 96 ? (L.ext ? grid_for(wf_shade<96, true>, L.bShade, wf->smCount)
@@ -1340,7 +1582,8 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.v.refillIdle = static_cast<int>(cfg.refill_idle ? cfg.refill_idle : 8);
     L.gMiss = grid_for(wf_miss, 256, wf->smCount);
     L.gShadow = grid_for(wf_shadow, 256, wf->smCount);
-    L.gOcc = grid_for(wf_occlude, L.bShadow, wf->smCount);
+    L.gOcc = L.coopOcc ? grid_for(wf_occlude<true>, L.bShadow, wf->smCount)
+                       : grid_for(wf_occlude<false>, L.bShadow, wf->smCount);
     L.gRes = grid_for(wf_resolve, 128, wf->smCount);
     L.gBin = grid_for(wf_bin_scatter, 256, wf->smCount);
     L.gAdjShade = grid_for(wa_shade, 128, wf->smCount);
@@ -1658,6 +1901,10 @@ int wavefront_set_config(ContextImpl* ctx, const ShiroWavefrontConfig* cfg) {
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "bin_rays and bin_shadow must be 1 (on), 2 (off) or 0");
     if (cfg->bin_rays) wf->cfg.bin_rays = cfg->bin_rays;
     if (cfg->bin_shadow) wf->cfg.bin_shadow = cfg->bin_shadow;
+    if (cfg->coop_extend > 2 || cfg->coop_occlude > 2)
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "coop_extend and coop_occlude must be 1 (on), 2 (off) or 0");
+    if (cfg->coop_extend) wf->cfg.coop_extend = cfg->coop_extend;
+    if (cfg->coop_occlude) wf->cfg.coop_occlude = cfg->coop_occlude;
     wf->cfg.use_graph = cfg->use_graph;
     return SHIRO_OK;
 }
@@ -1759,6 +2006,18 @@ int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefr
         ShiroWavefrontConfig c = best;
         c.bin_rays = on;
         if ((rc = trial(c)) != SHIRO_OK) return rc;
+    }
+    if (ctx->nodes8 && ctx->bvhWidth != 2) {  // warp-cooperative triangle tests
+        for (uint32_t on : {1u, 2u}) {
+            ShiroWavefrontConfig c = best;
+            c.coop_occlude = on;
+            if ((rc = trial(c)) != SHIRO_OK) return rc;
+        }
+        for (uint32_t on : {1u, 2u}) {
+            ShiroWavefrontConfig c = best;
+            c.coop_extend = on;
+            if ((rc = trial(c)) != SHIRO_OK) return rc;
+        }
     }
     if (ctx->nodes8 && ctx->bvhWidth != 2) {  // the lane refill of the wide-BVH extend stage
         for (uint32_t steps : {2u, 4u, 8u}) {

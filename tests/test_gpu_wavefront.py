@@ -131,11 +131,14 @@ def test_two_waves_in_flight_uneven_batch(gpu, pool):
                                    dict(concurrent_waves=1, paths_in_flight=2048),
                                    dict(bin_rays=1, bin_shadow=1), dict(bin_rays=1, bin_shadow=2),
                                    dict(bin_rays=2, bin_shadow=1, concurrent_waves=2, paths_in_flight=2048),
-                                   dict(bin_rays=1, bin_shadow=1, use_graph=1)])
+                                   dict(bin_rays=1, bin_shadow=1, use_graph=1),
+                                   dict(coop_extend=1, coop_occlude=1), dict(coop_extend=1, coop_occlude=2, refill_idle=1),
+                                   dict(coop_extend=2, coop_occlude=1, concurrent_waves=2, paths_in_flight=2048),
+                                   dict(coop_extend=1, coop_occlude=1, bin_rays=1, bin_shadow=1, refill_idle=32)])
 def test_tuning_knobs_keep_frames_identical(gpu, knobs):
     """Register cap of the shade stage, the lane-refill parameters of the
-    wide-BVH extend stage and the binning of the ray / occlusion queues
-    change scheduling only."""
+    wide-BVH extend stage, the binning of the ray / occlusion queues and the
+    warp-cooperative triangle tests change scheduling only."""
     from shiro_gb300 import scenes
 
     sc = scenes.field_scene(instances=12, levels=4, materials=6, env_width=128, env_height=64, seed=9, plane=12.0)
