@@ -342,7 +342,7 @@ typedef struct ShiroWavefrontConfig {
     uint32_t shade_block;
     uint32_t shadow_block;
     uint32_t use_graph;
-    uint32_t shade_regs;    /* register cap of the shade stage: 128 or 96 */
+    uint32_t shade_regs;    /* register cap of the shade stage: 128, 96 or 80 */
     uint32_t extend_steps;  /* wide-BVH nodes a lane visits between refills, 1-32 */
     uint32_t refill_idle;   /* idle lanes that make a warp refill, 1-32 */
     uint32_t concurrent_waves; /* 1 or 2: waves in flight at once, each with its own pool of
@@ -359,6 +359,9 @@ typedef struct ShiroWavefrontConfig {
                                   32 ray-triangle pairs per round); 2: each lane tests its own;
                                   0 leaves the current value.  Hits are identical either way. */
     uint32_t coop_occlude;     /* the same for the occlusion stage: 1 on, 2 off, 0 leaves it */
+    uint32_t extend_regs;      /* register cap of the closest-hit stage (per-lane triangle tests):
+                                  64, 48 or 40 (more resident warps, some spilling); 0 leaves it */
+    uint32_t occlude_regs;     /* the same for the occlusion stage */
 } ShiroWavefrontConfig;
 int shiro_gpu_get_wavefront_config(const ShiroGpuContext* ctx, ShiroWavefrontConfig* out);
 int shiro_gpu_set_wavefront_config(ShiroGpuContext* ctx, const ShiroWavefrontConfig* cfg);

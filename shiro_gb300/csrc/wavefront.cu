@@ -430,15 +430,14 @@ __device__ __forceinline__ uint32_t coop_pack(uint32_t tBase, uint32_t& bits, Co
 // Closest hits of the triangles each lane's current node left in
 // (tBase, tBits); updates the lane's WideTrav.  Warp-uniform call.
 __device__ __forceinline__ void coop_closest(const DevScene& s, WideTrav& t, uint32_t tBase, uint32_t tBits, CoopTris& c) {
+    if (!__any_sync(kFull, tBits != 0u)) return;
     const uint32_t lane = lane_id();
     const unsigned long long mine = (static_cast<unsigned long long>(__float_as_uint(t.tmax)) << 32) | t.bestGid;
     c.best[lane] = mine;
     uint32_t bits = tBits;
-    bool any = false;
     for (;;) {
         const uint32_t n = coop_pack(tBase, bits, c);
         if (n == 0u) break;
-        any = true;
         const bool pair = lane < n;
         const uint32_t tri = pair ? c.tri[lane] : 0u;
         const uint32_t src = pair ? c.src[lane] : lane;
@@ -462,15 +461,13 @@ __device__ __forceinline__ void coop_closest(const DevScene& s, WideTrav& t, uin
         }
         __syncwarp();
     }
-    if (any) {
-        const unsigned long long b = c.best[lane];
-        if (b != mine) {
-            t.tmax = __uint_as_float(static_cast<uint32_t>(b >> 32));
-            t.bestGid = static_cast<uint32_t>(b);
-            t.bestSlot = c.slot[lane];
-            t.bu = c.uv[lane].x;
-            t.bv = c.uv[lane].y;
-        }
+    const unsigned long long b = c.best[lane];
+    if (b != mine) {
+        t.tmax = __uint_as_float(static_cast<uint32_t>(b >> 32));
+        t.bestGid = static_cast<uint32_t>(b);
+        t.bestSlot = c.slot[lane];
+        t.bu = c.uv[lane].x;
+        t.bv = c.uv[lane].y;
     }
     __syncwarp();
 }
@@ -480,6 +477,7 @@ __device__ __forceinline__ void coop_closest(const DevScene& s, WideTrav& t, uin
 // Warp-uniform call.
 __device__ __forceinline__ uint32_t coop_any(const DevScene& s, const WideTrav& t, uint32_t tBase, uint32_t tBits,
                                              CoopTris& c) {
+    if (!__any_sync(kFull, tBits != 0u)) return 0u;
     const uint32_t lane = lane_id();
     uint32_t bits = tBits, occ = 0u;
     for (;;) {
@@ -509,8 +507,9 @@ __device__ __forceinline__ uint32_t coop_any(const DevScene& s, const WideTrav& 
 // the hits at the front of the shade queue and the misses at its back, so the
 // shade stage runs warps of hits and warps of misses instead of warps that
 // take both branches.
-template <bool kCoop>
-__global__ void __launch_bounds__(256, 4) wf_extend(WfView v, DevScene s, uint32_t cur, uint32_t binned) {
+// kMinBlocks blocks of 256 per SM: 4, 5, 6 cap the registers at 64, 48, 40.
+template <bool kCoop, int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) wf_extend(WfView v, DevScene s, uint32_t cur, uint32_t binned) {
     __shared__ uint32_t stage[8][2][64];
     const uint32_t count = v.counters[cur];
     const uint32_t* q = binned ? v.sortedQ : (cur ? v.rayQ1 : v.rayQ0);
@@ -537,19 +536,28 @@ __global__ void __launch_bounds__(256, 4) wf_extend(WfView v, DevScene s, uint32
                 has = true;
             }
             if (__ballot_sync(kFull, has) == 0u) break;
-            uint32_t gBase = 0, gImask = 0, gInner = 0, tBase = 0, tBits = 0;
             bool fin = false;
-            if (has) {
-                if (++t.visits > kMaxVisits) {
-                    atomicOr(s.error, kErrTraversalLimit);
+            for (int k = 0; k < v.travSteps; ++k) {  // up to travSteps nodes per lane between refills
+                const bool step = has && !fin;
+                uint32_t gBase = 0, gImask = 0, gInner = 0, tBase = 0, tBits = 0;
+                bool bad = false;
+                if (step) {
+                    if (++t.visits > kMaxVisits) {
+                        atomicOr(s.error, kErrTraversalLimit);
+                        bad = true;
+                    } else {
+                        wide_node(s, t.node, t.r, t.tmax, t.octInv, &gBase, &gImask, &gInner, &tBase, &tBits);
+                    }
+                }
+                coop_closest(s, t, tBase, tBits, c);
+                if (bad) {
                     t.bestSlot = 0xffffffffu;
                     fin = true;
-                } else {
-                    wide_node(s, t.node, t.r, t.tmax, t.octInv, &gBase, &gImask, &gInner, &tBase, &tBits);
+                } else if (step) {
+                    fin = !wide_next(s, t, stack, gBase, gImask, gInner);
                 }
+                if (!__any_sync(kFull, has && !fin)) break;
             }
-            coop_closest(s, t, tBase, tBits, c);
-            if (has && !fin) fin = !wide_next(s, t, stack, gBase, gImask, gInner);
             if (fin) {
                 v.hit[j] = make_float4(t.tmax, t.bu, t.bv, __uint_as_float(t.bestSlot));
                 v.hitGid[j] = t.bestGid;
@@ -767,8 +775,8 @@ __global__ void __launch_bounds__(256) wf_miss(WfView v, DevScene s, uint32_t de
 // (Lane refill as in wf_extend measured slower here: shadow rays are short
 // and an any-hit ends them early, so the refill bookkeeping outweighs the
 // divergence it removes.)
-template <bool kCoop>
-__global__ void __launch_bounds__(256, 4) wf_occlude(WfView v, DevScene s, uint32_t binned) {
+template <bool kCoop, int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) wf_occlude(WfView v, DevScene s, uint32_t binned) {
     const uint32_t count = v.counters[4];
     const uint32_t* sq = binned ? v.sortedQ : v.shadowRayQ;
     NullCounter ctr;
@@ -1264,6 +1272,8 @@ WavefrontState* wf_state(ContextImpl* ctx) {
         c.bin_shadow = 2;
         c.coop_extend = 2;
         c.coop_occlude = 2;
+        c.extend_regs = 64;
+        c.occlude_regs = 64;
         cudaDeviceGetAttribute(&ctx->wavefront->smCount, cudaDevAttrMultiProcessorCount, ctx->device);
     }
     return ctx->wavefront;
@@ -1387,24 +1397,42 @@ struct Launch {
     uint32_t shadeRegs;
     uint32_t binRays, binShadow;  // queue binning before extend (bounces >= 1) / occlude
     uint32_t coopExt, coopOcc;    // warp-cooperative triangle tests in extend / occlude
+    uint32_t extRegs, occRegs;    // register caps of the per-lane traversal stages
     int gBin;
     AdjWave aw;                   // aw.on: the adjoint replay follows the forward stages
     int gAdjShade, gAdjShadow, gAdjMiss;
     bool ext;  // the scene uses transmission, opacity or emitters
 };
 
+// The traversal stages' instantiations: cooperative triangle tests (at 64
+// registers) or per-lane ones with a register cap of 64, 48 or 40.
+template <typename F>
+auto with_extend_kernel(uint32_t coop, uint32_t regs, F&& f) {
+    if (coop) return f(wf_extend<true, 4>);
+    if (regs == 48) return f(wf_extend<false, 5>);
+    if (regs == 40) return f(wf_extend<false, 6>);
+    return f(wf_extend<false, 4>);
+}
+template <typename F>
+auto with_occlude_kernel(uint32_t coop, uint32_t regs, F&& f) {
+    if (coop) return f(wf_occlude<true, 4>);
+    if (regs == 48) return f(wf_occlude<false, 5>);
+    if (regs == 40) return f(wf_occlude<false, 6>);
+    return f(wf_occlude<false, 4>);
+}
+
 void launch_extend(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t binned) {
-    if (L.coopExt)
-        wf_extend<true><<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, binned);
-    else
-        wf_extend<false><<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, binned);
+    with_extend_kernel(L.coopExt, L.extRegs, [&](auto kern) {
+        kern<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, binned);
+        return 0;
+    });
 }
 
 void launch_occlude(const Launch& L, cudaStream_t st, uint32_t binned) {
-    if (L.coopOcc)
-        wf_occlude<true><<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s, binned);
-    else
-        wf_occlude<false><<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s, binned);
+    with_occlude_kernel(L.coopOcc, L.occRegs, [&](auto kern) {
+        kern<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s, binned);
+        return 0;
+    });
 }
 
 void enqueue_replay(const Launch& L, cudaStream_t st) {
@@ -1428,17 +1456,25 @@ void enqueue_binning(const Launch& L, cudaStream_t st, uint32_t which, uint32_t 
     wf_bin_scatter<<<L.gBin, 256, 0, st>>>(L.v, which, cur);
 }
 
-void launch_shade(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t d) {
-    if (L.ext) {
-        if (L.shadeRegs == 96)
-            wf_shade<96, true><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
-        else
-            wf_shade<128, true><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
-    } else if (L.shadeRegs == 96) {
-        wf_shade<96, false><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
-    } else {
-        wf_shade<128, false><<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
+// The shade stage's instantiation for a register cap (80, 96 or 128) and
+// the scene's lobe set.
+template <typename F>
+auto with_shade_kernel(uint32_t regs, bool ext, F&& f) {
+    if (ext) {
+        if (regs == 80) return f(wf_shade<80, true>);
+        if (regs == 96) return f(wf_shade<96, true>);
+        return f(wf_shade<128, true>);
     }
+    if (regs == 80) return f(wf_shade<80, false>);
+    if (regs == 96) return f(wf_shade<96, false>);
+    return f(wf_shade<128, false>);
+}
+
+void launch_shade(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t d) {
+    with_shade_kernel(L.shadeRegs, L.ext, [&](auto kern) {
+        kern<<<L.gShade, L.bShade, 0, st>>>(L.v, L.s, cur, d);
+        return 0;
+    });
     wf_miss<<<L.gMiss, 256, 0, st>>>(L.v, L.s, d);
 }
 
@@ -1571,19 +1607,17 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.gGen = grid_for(wf_generate, 128, wf->smCount);
     L.coopExt = cfg.coop_extend == 1 ? 1u : 0u;
     L.coopOcc = cfg.coop_occlude == 1 ? 1u : 0u;
-    L.gExt = L.coopExt ? grid_for(wf_extend<true>, L.bExt, wf->smCount) : grid_for(wf_extend<false>, L.bExt, wf->smCount);
+    L.extRegs = cfg.extend_regs ? cfg.extend_regs : 64;
+    L.occRegs = cfg.occlude_regs ? cfg.occlude_regs : 64;
+    L.gExt = with_extend_kernel(L.coopExt, L.extRegs, [&](auto kern) { return grid_for(kern, L.bExt, wf->smCount); });
     L.shadeRegs = cfg.shade_regs;
     L.ext = ctx->extendedMaterials;
-    L.gShade = L.shadeRegs == 96 ? (L.ext ? grid_for(wf_shade<96, true>, L.bShade, wf->smCount)
-                                          : grid_for(wf_shade<96, false>, L.bShade, wf->smCount))
-                                 : (L.ext ? grid_for(wf_shade<128, true>, L.bShade, wf->smCount)
-                                          : grid_for(wf_shade<128, false>, L.bShade, wf->smCount));
+    L.gShade = with_shade_kernel(L.shadeRegs, L.ext, [&](auto kern) { return grid_for(kern, L.bShade, wf->smCount); });
     L.v.travSteps = static_cast<int>(cfg.extend_steps ? cfg.extend_steps : 4);
     L.v.refillIdle = static_cast<int>(cfg.refill_idle ? cfg.refill_idle : 8);
     L.gMiss = grid_for(wf_miss, 256, wf->smCount);
     L.gShadow = grid_for(wf_shadow, 256, wf->smCount);
-    L.gOcc = L.coopOcc ? grid_for(wf_occlude<true>, L.bShadow, wf->smCount)
-                       : grid_for(wf_occlude<false>, L.bShadow, wf->smCount);
+    L.gOcc = with_occlude_kernel(L.coopOcc, L.occRegs, [&](auto kern) { return grid_for(kern, L.bShadow, wf->smCount); });
     L.gRes = grid_for(wf_resolve, 128, wf->smCount);
     L.gBin = grid_for(wf_bin_scatter, 256, wf->smCount);
     L.gAdjShade = grid_for(wa_shade, 128, wf->smCount);
@@ -1879,13 +1913,15 @@ int wavefront_set_config(ContextImpl* ctx, const ShiroWavefrontConfig* cfg) {
     auto okBlock = [](uint32_t b) { return b == 0 || (b >= 32 && b <= 1024 && b % 32 == 0); };
     if (!okBlock(cfg->extend_block) || !okBlock(cfg->shade_block) || !okBlock(cfg->shadow_block))
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "block sizes must be multiples of 32 in [32, 1024]");
+    if (cfg->extend_block > 256 || cfg->shadow_block > 256)  // per-warp shared buffers for 8 warps
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "extend_block and shadow_block must be at most 256");
     if (cfg->paths_in_flight) {
         if (cfg->paths_in_flight < 1024 || cfg->paths_in_flight > (1u << 27))
             return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "paths_in_flight out of range [1024, 2^27]");
         wf->cfg.paths_in_flight = cfg->paths_in_flight;
     }
-    if (cfg->shade_regs && cfg->shade_regs != 96 && cfg->shade_regs != 128)
-        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "shade_regs must be 96 or 128");
+    if (cfg->shade_regs && cfg->shade_regs != 80 && cfg->shade_regs != 96 && cfg->shade_regs != 128)
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "shade_regs must be 80, 96 or 128");
     if (cfg->extend_steps > 32 || cfg->refill_idle > 32)
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "extend_steps and refill_idle must be in [1, 32]");
     if (cfg->extend_block) wf->cfg.extend_block = cfg->extend_block;
@@ -1905,6 +1941,11 @@ int wavefront_set_config(ContextImpl* ctx, const ShiroWavefrontConfig* cfg) {
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "coop_extend and coop_occlude must be 1 (on), 2 (off) or 0");
     if (cfg->coop_extend) wf->cfg.coop_extend = cfg->coop_extend;
     if (cfg->coop_occlude) wf->cfg.coop_occlude = cfg->coop_occlude;
+    auto okRegs = [](uint32_t r) { return r == 0 || r == 40 || r == 48 || r == 64; };
+    if (!okRegs(cfg->extend_regs) || !okRegs(cfg->occlude_regs))
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "extend_regs and occlude_regs must be 40, 48 or 64 (0 leaves them)");
+    if (cfg->extend_regs) wf->cfg.extend_regs = cfg->extend_regs;
+    if (cfg->occlude_regs) wf->cfg.occlude_regs = cfg->occlude_regs;
     wf->cfg.use_graph = cfg->use_graph;
     return SHIRO_OK;
 }
@@ -1981,7 +2022,7 @@ int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefr
         c.shadow_block = blk;
         if ((rc = trial(c)) != SHIRO_OK) return rc;
     }
-    for (uint32_t regs : {96u, 128u}) {
+    for (uint32_t regs : {80u, 96u, 128u}) {
         ShiroWavefrontConfig c = best;
         c.shade_regs = regs;
         if ((rc = trial(c)) != SHIRO_OK) return rc;
@@ -2005,6 +2046,16 @@ int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefr
     for (uint32_t on : {1u, 2u}) {
         ShiroWavefrontConfig c = best;
         c.bin_rays = on;
+        if ((rc = trial(c)) != SHIRO_OK) return rc;
+    }
+    for (uint32_t regs : {40u, 48u, 64u}) {  // register caps of the traversal stages
+        ShiroWavefrontConfig c = best;
+        c.occlude_regs = regs;
+        if ((rc = trial(c)) != SHIRO_OK) return rc;
+    }
+    for (uint32_t regs : {48u, 64u}) {
+        ShiroWavefrontConfig c = best;
+        c.extend_regs = regs;
         if ((rc = trial(c)) != SHIRO_OK) return rc;
     }
     if (ctx->nodes8 && ctx->bvhWidth != 2) {  // warp-cooperative triangle tests

@@ -125,7 +125,7 @@ def test_two_waves_in_flight_uneven_batch(gpu, pool):
     assert gpu.wavefront_config()["concurrent_waves"] == base["concurrent_waves"]
 
 
-@pytest.mark.parametrize("knobs", [dict(shade_regs=96), dict(extend_steps=1, refill_idle=1),
+@pytest.mark.parametrize("knobs", [dict(shade_regs=96), dict(shade_regs=80), dict(extend_steps=1, refill_idle=1),
                                    dict(extend_steps=32, refill_idle=32), dict(extend_steps=3, refill_idle=5),
                                    dict(concurrent_waves=2, paths_in_flight=2048),
                                    dict(concurrent_waves=1, paths_in_flight=2048),
@@ -134,7 +134,8 @@ def test_two_waves_in_flight_uneven_batch(gpu, pool):
                                    dict(bin_rays=1, bin_shadow=1, use_graph=1),
                                    dict(coop_extend=1, coop_occlude=1), dict(coop_extend=1, coop_occlude=2, refill_idle=1),
                                    dict(coop_extend=2, coop_occlude=1, concurrent_waves=2, paths_in_flight=2048),
-                                   dict(coop_extend=1, coop_occlude=1, bin_rays=1, bin_shadow=1, refill_idle=32)])
+                                   dict(coop_extend=1, coop_occlude=1, bin_rays=1, bin_shadow=1, refill_idle=32),
+                                   dict(extend_regs=48, occlude_regs=40), dict(extend_regs=40, occlude_regs=48)])
 def test_tuning_knobs_keep_frames_identical(gpu, knobs):
     """Register cap of the shade stage, the lane-refill parameters of the
     wide-BVH extend stage, the binning of the ray / occlusion queues and the
