@@ -260,7 +260,7 @@ int shiro_gpu_set_bvh_width(ShiroGpuContext* ctx, uint32_t width);
  * is collapsed from them): sah_cluster_triangles > 1 keeps the Morton (LBVH)
  * subtrees of at most that many triangles as clusters and rebuilds the tree
  * above them by binned SAH over the clusters' boxes (16 bins per axis, on the
- * device); 0 keeps the Morton hierarchy throughout.  Default 8.  Both give
+ * device); 0 keeps the Morton hierarchy throughout.  Default 2.  Both give
  * identical hits; the choice only changes speed. */
 int shiro_gpu_set_bvh_build(ShiroGpuContext* ctx, uint32_t sah_cluster_triangles);
 

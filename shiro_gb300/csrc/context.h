@@ -28,7 +28,7 @@ struct EnvHost {
 // Default cluster size of the binned-SAH top (shiro_gpu_set_bvh_build):
 // measured on the 1.31 M-triangle field frame, 8 gave the fewest node visits
 // (binary 69.8 -> 65.1, wide 26.2 -> 25.5 per path; 16 and up fewer gains).
-constexpr uint32_t kDefaultSahCluster = 8;
+constexpr uint32_t kDefaultSahCluster = 2;
 
 struct WavefrontState;
 struct AdjointState;

@@ -65,6 +65,10 @@ constexpr uint32_t kFlagDone = 1u << 17;
 constexpr uint32_t kTypeShift = 18;
 constexpr uint32_t kFlagInside = 1u << 20;
 constexpr uint32_t kFlagMedium = 1u << 21;
+// the path continues and its last vertex's direct light (its visible light
+// samples, weighted by that vertex's throughput) is still to be added: the
+// next bounce's shade or miss stage adds it first, in the reference's order
+constexpr uint32_t kFlagPending = 1u << 22;
 
 __device__ __forceinline__ uint32_t pack_state(const PathState& ps) {
     return (ps.diffDepth & 0xffu) | ((ps.specDepth & 0xffu) << 8) | (ps.prevDelta ? kFlagPrevDelta : 0u) |
@@ -297,9 +301,8 @@ __global__ void __launch_bounds__(128) wf_generate(WfView v) {
         v.T[j] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(kFlagPrevDelta));
         v.rad[j] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(0x7f800000));
         v.ident[j] = make_uint4(x, y, smpIdx, sg.req);
-        v.records[3 * static_cast<size_t>(j) + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        v.records[3 * static_cast<size_t>(j) + 2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        v.rayQ0[j] = j;
+        v.rayQ0[j] = j;  // albedo / normal records are written by a first hit and read only after one
+
     }
 }
 
@@ -642,6 +645,22 @@ __device__ __forceinline__ void write_record(const WfView& v, uint32_t j, const 
     v.records[3 * static_cast<size_t>(j)] = make_float4(rad.x, rad.y, rad.z, depth0);
 }
 
+// rad + the throughput of the path's last shaded vertex times the in-order
+// sum of that vertex's visible light samples (sum_direct's order, the
+// reference's radiance += throughput * DirectLighting).
+__device__ __forceinline__ V3 add_direct(const WfView& v, const DevScene& s, const DevRequest& q, uint32_t j,
+                                         const V3& rad) {
+    const float4 t4 = v.shT[j];
+    const V3 direct = sum_direct<true>(s, q, [&](uint32_t k, V3* c) {
+        const size_t e = static_cast<size_t>(k) * v.P + j;
+        if (v.shDir[e].w == 0.0f) return false;
+        const float4 c4 = v.shC[e];
+        *c = V3{c4.x, c4.y, c4.z};
+        return true;
+    });
+    return rad + V3{t4.x, t4.y, t4.z} * direct;
+}
+
 // Shade stage, compiled with several register caps (the autotuner picks) and
 // with / without the extended lobes (kExt, chosen by the scene).
 template <int kRegs, bool kExt>
@@ -672,6 +691,7 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
             ps.prevPdf = d.w;
             ps.T = V3{t4.x, t4.y, t4.z};
             ps.radiance = V3{r4.x, r4.y, r4.z};
+            if (bits & kFlagPending) ps.radiance = add_direct(v, s, q, j, ps.radiance);  // before this vertex's terms
             ps.diffDepth = bits & 0xffu;
             ps.specDepth = (bits >> 8) & 0xffu;
             ps.prevDelta = (bits & kFlagPrevDelta) != 0u;
@@ -722,12 +742,14 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
                         const V3 org = shadow_origin(vx);
                         v.shOrigin[j] = make_float4(org.x, org.y, org.z, 0.0f);
                         v.shT[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, 0.0f);
-                        pushShadow = true;
                     }
                     cont = continue_path<kExt>(s, q, vx, smp, depth, ps, ctr) && depth + 1u < q.maxDepth;
                 }
+                // the direct light waits for the occlusion stage: a continuing
+                // path takes it at its next bounce, an ending one in wf_shadow
                 uint32_t nb = pack_state(ps);
-                if (!cont && anyLight) nb |= kFlagDone;
+                if (anyLight) nb |= cont ? kFlagPending : kFlagDone;
+                pushShadow = anyLight && !cont;
                 v.T[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, __uint_as_float(nb));
                 if (kExt && ps.mediumActive)
                     v.medium[j] = make_float4(ps.extinction.x, ps.extinction.y, ps.extinction.z, 0.0f);
@@ -764,6 +786,7 @@ __global__ void __launch_bounds__(256) wf_miss(WfView v, DevScene s, uint32_t de
         ps.prevPdf = d.w;
         ps.T = V3{t4.x, t4.y, t4.z};
         ps.radiance = V3{r4.x, r4.y, r4.z};
+        if (bits & kFlagPending) ps.radiance = add_direct(v, s, q, j, ps.radiance);
         ps.prevDelta = (bits & kFlagPrevDelta) != 0u;
         ps.prevType = (bits >> kTypeShift) & 3u;
         add_miss(s, q, ps, depth, ctr);
@@ -838,23 +861,16 @@ __global__ void __launch_bounds__(256, kMinBlocks) wf_occlude(WfView v, DevScene
     }
 }
 
-// In-order sum of a path's unoccluded light samples (sum_direct's order).
+// Paths that end at a vertex with light samples: the in-order sum of the
+// unoccluded ones (sum_direct's order) completes the path's radiance.  (A
+// continuing path takes its vertex's direct light at the next bounce.)
 __global__ void __launch_bounds__(256) wf_shadow(WfView v, DevScene s) {
     const uint32_t count = v.counters[2];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t j = v.shadowQ[i];
         const DevRequest& q = v.reqs[v.ident[j].w].q;
-        const float4 t4 = v.shT[j], r4 = v.rad[j];
-        const V3 direct = sum_direct<true>(s, q, [&](uint32_t k, V3* c) {
-            const size_t e = static_cast<size_t>(k) * v.P + j;
-            if (v.shDir[e].w == 0.0f) return false;
-            const float4 c4 = v.shC[e];
-            *c = V3{c4.x, c4.y, c4.z};
-            return true;
-        });
-        const V3 rad = V3{r4.x, r4.y, r4.z} + V3{t4.x, t4.y, t4.z} * direct;
-        v.rad[j] = make_float4(rad.x, rad.y, rad.z, r4.w);
-        if (__float_as_uint(v.T[j].w) & kFlagDone) write_record(v, j, rad, r4.w);
+        const float4 r4 = v.rad[j];
+        write_record(v, j, add_direct(v, s, q, j, V3{r4.x, r4.y, r4.z}), r4.w);
     }
 }
 
@@ -884,13 +900,17 @@ __global__ void __launch_bounds__(128) wf_resolve(WfView v) {
         V3 alb{0.0f, 0.0f, 0.0f}, nrm{0.0f, 0.0f, 0.0f};
         float depth = __int_as_float(0x7f800000);
         for (uint32_t k = 0; k < n; ++k) {
-            const float4 a = rec[3 * k], b = rec[3 * k + 1], c = rec[3 * k + 2];
+            const float4 a = rec[3 * k];
             b0 = b0 + a.x;
             b1 = b1 + a.y;
             b2 = b2 + a.z;
-            b3 = b3 + (a.w < __int_as_float(0x7f800000) ? 1.0f : 0.0f);
-            alb = alb + V3{b.x, b.y, b.z};
-            nrm = nrm + V3{c.x, c.y, c.z};
+            const bool hit = a.w < __int_as_float(0x7f800000);
+            b3 = b3 + (hit ? 1.0f : 0.0f);
+            if (hit) {  // albedo and normal of a path whose first ray missed are zero (adding them changes nothing)
+                const float4 b = rec[3 * k + 1], c = rec[3 * k + 2];
+                alb = alb + V3{b.x, b.y, b.z};
+                nrm = nrm + V3{c.x, c.y, c.z};
+            }
             if (a.w < depth) depth = a.w;
         }
         const float cnt = static_cast<float>(n);

@@ -263,7 +263,7 @@ def test_binned_sah_top_keeps_hits_exact(gpu, port, cluster):
         print(f"cluster {cluster}: binary nodes {morton_nodes} (Morton) -> {gpu.last_stats()['bvh_nodes']}")
     finally:
         gpu.set_bvh_width(0)
-        gpu.set_bvh_build(8)  # the default
+        gpu.set_bvh_build(2)  # the default
     for k in ("beauty", "albedo", "normal", "depth"):
         assert np.array_equal(getattr(frame, k), getattr(morton_frame, k)), k
         assert np.array_equal(getattr(wf, k), getattr(morton_frame, k)), k
