@@ -661,6 +661,29 @@ __device__ __forceinline__ V3 add_direct(const WfView& v, const DevScene& s, con
     return rad + V3{t4.x, t4.y, t4.z} * direct;
 }
 
+// add_direct with the vertex throughput and the first two light samples'
+// records already loaded (the shade stage issues those loads together with
+// the path state instead of after reading the pending flag).
+__device__ __forceinline__ V3 add_direct_pre(const WfView& v, const DevScene& s, const DevRequest& q, uint32_t j,
+                                             const V3& rad, const float4& t4, const float4 (&dir)[2],
+                                             const float4 (&con)[2]) {
+    const V3 direct = sum_direct<true>(s, q, [&](uint32_t k, V3* c) {
+        float4 d4, c4;
+        if (k < 2) {
+            d4 = dir[k];
+            c4 = con[k];
+        } else {
+            const size_t e = static_cast<size_t>(k) * v.P + j;
+            d4 = v.shDir[e];
+            c4 = v.shC[e];
+        }
+        if (d4.w == 0.0f) return false;
+        *c = V3{c4.x, c4.y, c4.z};
+        return true;
+    });
+    return rad + V3{t4.x, t4.y, t4.z} * direct;
+}
+
 // Shade stage, compiled with several register caps (the autotuner picks) and
 // with / without the extended lobes (kExt, chosen by the scene).
 template <int kRegs, bool kExt>
@@ -684,6 +707,19 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
             const uint4 id = v.ident[j];
             const DevRequest& q = v.reqs[id.w].q;
             const float4 o = v.ro[j], d = v.rd[j], t4 = v.T[j], r4 = v.rad[j], h4 = v.hit[j];
+            // a path past its first bounce nearly always carries its last
+            // vertex's direct light: load it with the state (no second round trip)
+            float4 pT = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            float4 pDir[2] = {pT, pT}, pCon[2] = {pT, pT};
+            if (depth > 0) {
+                pT = v.shT[j];
+                pDir[0] = v.shDir[j];
+                pCon[0] = v.shC[j];
+                if (v.lightSamples > 1) {
+                    pDir[1] = v.shDir[static_cast<size_t>(v.P) + j];
+                    pCon[1] = v.shC[static_cast<size_t>(v.P) + j];
+                }
+            }
             const uint32_t bits = __float_as_uint(t4.w);
             PathState ps;
             ps.ro = V3{o.x, o.y, o.z};
@@ -691,7 +727,8 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
             ps.prevPdf = d.w;
             ps.T = V3{t4.x, t4.y, t4.z};
             ps.radiance = V3{r4.x, r4.y, r4.z};
-            if (bits & kFlagPending) ps.radiance = add_direct(v, s, q, j, ps.radiance);  // before this vertex's terms
+            if (bits & kFlagPending)  // before this vertex's terms
+                ps.radiance = add_direct_pre(v, s, q, j, ps.radiance, pT, pDir, pCon);
             ps.diffDepth = bits & 0xffu;
             ps.specDepth = (bits >> 8) & 0xffu;
             ps.prevDelta = (bits & kFlagPrevDelta) != 0u;
