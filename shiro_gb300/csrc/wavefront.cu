@@ -661,28 +661,6 @@ __device__ __forceinline__ V3 add_direct(const WfView& v, const DevScene& s, con
     return rad + V3{t4.x, t4.y, t4.z} * direct;
 }
 
-// add_direct with the vertex throughput and the first two light samples'
-// records already loaded (the shade stage issues those loads together with
-// the path state instead of after reading the pending flag).
-__device__ __forceinline__ V3 add_direct_pre(const WfView& v, const DevScene& s, const DevRequest& q, uint32_t j,
-                                             const V3& rad, const float4& t4, const float4 (&dir)[2],
-                                             const float4 (&con)[2]) {
-    const V3 direct = sum_direct<true>(s, q, [&](uint32_t k, V3* c) {
-        float4 d4, c4;
-        if (k < 2) {
-            d4 = dir[k];
-            c4 = con[k];
-        } else {
-            const size_t e = static_cast<size_t>(k) * v.P + j;
-            d4 = v.shDir[e];
-            c4 = v.shC[e];
-        }
-        if (d4.w == 0.0f) return false;
-        *c = V3{c4.x, c4.y, c4.z};
-        return true;
-    });
-    return rad + V3{t4.x, t4.y, t4.z} * direct;
-}
 
 // Shade stage, compiled with several register caps (the autotuner picks) and
 // with / without the extended lobes (kExt, chosen by the scene).
@@ -707,28 +685,13 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
             const uint4 id = v.ident[j];
             const DevRequest& q = v.reqs[id.w].q;
             const float4 o = v.ro[j], d = v.rd[j], t4 = v.T[j], r4 = v.rad[j], h4 = v.hit[j];
-            // a path past its first bounce nearly always carries its last
-            // vertex's direct light: load it with the state (no second round trip)
-            float4 pT = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            float4 pDir[2] = {pT, pT}, pCon[2] = {pT, pT};
-            if (depth > 0) {
-                pT = v.shT[j];
-                pDir[0] = v.shDir[j];
-                pCon[0] = v.shC[j];
-                if (v.lightSamples > 1) {
-                    pDir[1] = v.shDir[static_cast<size_t>(v.P) + j];
-                    pCon[1] = v.shC[static_cast<size_t>(v.P) + j];
-                }
-            }
             const uint32_t bits = __float_as_uint(t4.w);
             PathState ps;
             ps.ro = V3{o.x, o.y, o.z};
             ps.rd = V3{d.x, d.y, d.z};
             ps.prevPdf = d.w;
             ps.T = V3{t4.x, t4.y, t4.z};
-            ps.radiance = V3{r4.x, r4.y, r4.z};
-            if (bits & kFlagPending)  // before this vertex's terms
-                ps.radiance = add_direct_pre(v, s, q, j, ps.radiance, pT, pDir, pCon);
+            ps.radiance = V3{r4.x, r4.y, r4.z};  // with the previous vertex's direct light (wf_direct)
             ps.diffDepth = bits & 0xffu;
             ps.specDepth = (bits >> 8) & 0xffu;
             ps.prevDelta = (bits & kFlagPrevDelta) != 0u;
@@ -895,6 +858,22 @@ __global__ void __launch_bounds__(256, kMinBlocks) wf_occlude(WfView v, DevScene
         const size_t e = static_cast<size_t>(k) * v.P + j;
         const float4 o4 = v.shOrigin[j], d4 = v.shDir[e];
         if (trace_occluded(s, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, d4.w, ctr)) v.shDir[e].w = 0.0f;
+    }
+}
+
+// Hits of a bounce after the first whose path carries its previous vertex's
+// direct light: added before the shade stage adds this vertex's terms (a
+// small kernel of its own: folded into the shade stage, these loads cost
+// that latency-bound stage more than this pass costs).
+__global__ void __launch_bounds__(256) wf_direct(WfView v, DevScene s) {
+    const uint32_t count = v.counters[kHitCount];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t j = v.shadeQ[i];
+        if (!(__float_as_uint(v.T[j].w) & kFlagPending)) continue;
+        const DevRequest& q = v.reqs[v.ident[j].w].q;
+        const float4 r4 = v.rad[j];
+        const V3 rad = add_direct(v, s, q, j, V3{r4.x, r4.y, r4.z});
+        v.rad[j] = make_float4(rad.x, rad.y, rad.z, r4.w);
     }
 }
 
@@ -1543,6 +1522,7 @@ void enqueue_wave(const Launch& L, cudaStream_t st) {
         const uint32_t br = (L.binRays && d > 0) ? 1u : 0u;  // camera rays are coherent already
         if (br) enqueue_binning(L, st, 0u, cur);
         launch_extend(L, st, cur, br);
+        if (d > 0) wf_direct<<<L.gShadow, 256, 0, st>>>(L.v, L.s);
         launch_shade(L, st, cur, d);
         if (L.binShadow) enqueue_binning(L, st, 1u, cur);
         launch_occlude(L, st, L.binShadow);
@@ -1574,6 +1554,7 @@ void enqueue_wave_timed(const Launch& L, cudaStream_t st, std::vector<std::pair<
             if (br) enqueue_binning(L, st, 0u, cur);
             launch_extend(L, st, cur, br);
         });
+        if (d > 0) timed(5, [&] { wf_direct<<<L.gShadow, 256, 0, st>>>(L.v, L.s); });
         timed(2, [&] { launch_shade(L, st, cur, d); });
         timed(3, [&] {
             if (L.binShadow) enqueue_binning(L, st, 1u, cur);
@@ -1789,7 +1770,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             e = cudaGetLastError();
         }
         throttle.after_launch(exec[k] && k != 0 ? wf->side : st);
-        launches += 3 + 6ull * L.depth + (L.binShadow ? 3ull * L.depth : 0ull) +
+        launches += 3 + 6ull * L.depth + (L.depth > 1 ? L.depth - 1ull : 0ull) + (L.binShadow ? 3ull * L.depth : 0ull) +
                 (L.binRays && L.depth > 1 ? 3ull * (L.depth - 1) : 0ull) + (adj ? 2ull + 6ull * L.depth - 1ull : 0ull);
         ++launchedWaves;
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront launch");
