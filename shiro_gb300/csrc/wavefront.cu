@@ -65,10 +65,6 @@ constexpr uint32_t kFlagDone = 1u << 17;
 constexpr uint32_t kTypeShift = 18;
 constexpr uint32_t kFlagInside = 1u << 20;
 constexpr uint32_t kFlagMedium = 1u << 21;
-// the path continues and its last vertex's direct light (its visible light
-// samples, weighted by that vertex's throughput) is still to be added: the
-// next bounce's shade or miss stage adds it first, in the reference's order
-constexpr uint32_t kFlagPending = 1u << 22;
 
 __device__ __forceinline__ uint32_t pack_state(const PathState& ps) {
     return (ps.diffDepth & 0xffu) | ((ps.specDepth & 0xffu) << 8) | (ps.prevDelta ? kFlagPrevDelta : 0u) |
@@ -645,23 +641,6 @@ __device__ __forceinline__ void write_record(const WfView& v, uint32_t j, const 
     v.records[3 * static_cast<size_t>(j)] = make_float4(rad.x, rad.y, rad.z, depth0);
 }
 
-// rad + the throughput of the path's last shaded vertex times the in-order
-// sum of that vertex's visible light samples (sum_direct's order, the
-// reference's radiance += throughput * DirectLighting).
-__device__ __forceinline__ V3 add_direct(const WfView& v, const DevScene& s, const DevRequest& q, uint32_t j,
-                                         const V3& rad) {
-    const float4 t4 = v.shT[j];
-    const V3 direct = sum_direct<true>(s, q, [&](uint32_t k, V3* c) {
-        const size_t e = static_cast<size_t>(k) * v.P + j;
-        if (v.shDir[e].w == 0.0f) return false;
-        const float4 c4 = v.shC[e];
-        *c = V3{c4.x, c4.y, c4.z};
-        return true;
-    });
-    return rad + V3{t4.x, t4.y, t4.z} * direct;
-}
-
-
 // Shade stage, compiled with several register caps (the autotuner picks) and
 // with / without the extended lobes (kExt, chosen by the scene).
 template <int kRegs, bool kExt>
@@ -691,7 +670,7 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
             ps.rd = V3{d.x, d.y, d.z};
             ps.prevPdf = d.w;
             ps.T = V3{t4.x, t4.y, t4.z};
-            ps.radiance = V3{r4.x, r4.y, r4.z};  // with the previous vertex's direct light (wf_direct)
+            ps.radiance = V3{r4.x, r4.y, r4.z};
             ps.diffDepth = bits & 0xffu;
             ps.specDepth = (bits >> 8) & 0xffu;
             ps.prevDelta = (bits & kFlagPrevDelta) != 0u;
@@ -742,14 +721,15 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
                         const V3 org = shadow_origin(vx);
                         v.shOrigin[j] = make_float4(org.x, org.y, org.z, 0.0f);
                         v.shT[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, 0.0f);
+                        pushShadow = true;
                     }
                     cont = continue_path<kExt>(s, q, vx, smp, depth, ps, ctr) && depth + 1u < q.maxDepth;
                 }
-                // the direct light waits for the occlusion stage: a continuing
-                // path takes it at its next bounce, an ending one in wf_shadow
                 uint32_t nb = pack_state(ps);
-                if (anyLight) nb |= cont ? kFlagPending : kFlagDone;
-                pushShadow = anyLight && !cont;
+                if (!cont && anyLight) {
+                    nb |= kFlagDone;
+                    v.shT[j].w = 1.0f;  // read by wf_shadow with the throughput (no load of T for the flag)
+                }
                 v.T[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, __uint_as_float(nb));
                 if (kExt && ps.mediumActive)
                     v.medium[j] = make_float4(ps.extinction.x, ps.extinction.y, ps.extinction.z, 0.0f);
@@ -786,7 +766,6 @@ __global__ void __launch_bounds__(256) wf_miss(WfView v, DevScene s, uint32_t de
         ps.prevPdf = d.w;
         ps.T = V3{t4.x, t4.y, t4.z};
         ps.radiance = V3{r4.x, r4.y, r4.z};
-        if (bits & kFlagPending) ps.radiance = add_direct(v, s, q, j, ps.radiance);
         ps.prevDelta = (bits & kFlagPrevDelta) != 0u;
         ps.prevType = (bits >> kTypeShift) & 3u;
         add_miss(s, q, ps, depth, ctr);
@@ -861,32 +840,23 @@ __global__ void __launch_bounds__(256, kMinBlocks) wf_occlude(WfView v, DevScene
     }
 }
 
-// Hits of a bounce after the first whose path carries its previous vertex's
-// direct light: added before the shade stage adds this vertex's terms (a
-// small kernel of its own: folded into the shade stage, these loads cost
-// that latency-bound stage more than this pass costs).
-__global__ void __launch_bounds__(256) wf_direct(WfView v, DevScene s) {
-    const uint32_t count = v.counters[kHitCount];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const uint32_t j = v.shadeQ[i];
-        if (!(__float_as_uint(v.T[j].w) & kFlagPending)) continue;
-        const DevRequest& q = v.reqs[v.ident[j].w].q;
-        const float4 r4 = v.rad[j];
-        const V3 rad = add_direct(v, s, q, j, V3{r4.x, r4.y, r4.z});
-        v.rad[j] = make_float4(rad.x, rad.y, rad.z, r4.w);
-    }
-}
-
-// Paths that end at a vertex with light samples: the in-order sum of the
-// unoccluded ones (sum_direct's order) completes the path's radiance.  (A
-// continuing path takes its vertex's direct light at the next bounce.)
+// In-order sum of a path's unoccluded light samples (sum_direct's order).
 __global__ void __launch_bounds__(256) wf_shadow(WfView v, DevScene s) {
     const uint32_t count = v.counters[2];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t j = v.shadowQ[i];
         const DevRequest& q = v.reqs[v.ident[j].w].q;
-        const float4 r4 = v.rad[j];
-        write_record(v, j, add_direct(v, s, q, j, V3{r4.x, r4.y, r4.z}), r4.w);
+        const float4 t4 = v.shT[j], r4 = v.rad[j];
+        const V3 direct = sum_direct<true>(s, q, [&](uint32_t k, V3* c) {
+            const size_t e = static_cast<size_t>(k) * v.P + j;
+            if (v.shDir[e].w == 0.0f) return false;
+            const float4 c4 = v.shC[e];
+            *c = V3{c4.x, c4.y, c4.z};
+            return true;
+        });
+        const V3 rad = V3{r4.x, r4.y, r4.z} + V3{t4.x, t4.y, t4.z} * direct;
+        v.rad[j] = make_float4(rad.x, rad.y, rad.z, r4.w);
+        if (t4.w != 0.0f) write_record(v, j, rad, r4.w);  // the path ends here
     }
 }
 
@@ -1522,7 +1492,6 @@ void enqueue_wave(const Launch& L, cudaStream_t st) {
         const uint32_t br = (L.binRays && d > 0) ? 1u : 0u;  // camera rays are coherent already
         if (br) enqueue_binning(L, st, 0u, cur);
         launch_extend(L, st, cur, br);
-        if (d > 0) wf_direct<<<L.gShadow, 256, 0, st>>>(L.v, L.s);
         launch_shade(L, st, cur, d);
         if (L.binShadow) enqueue_binning(L, st, 1u, cur);
         launch_occlude(L, st, L.binShadow);
@@ -1554,7 +1523,6 @@ void enqueue_wave_timed(const Launch& L, cudaStream_t st, std::vector<std::pair<
             if (br) enqueue_binning(L, st, 0u, cur);
             launch_extend(L, st, cur, br);
         });
-        if (d > 0) timed(5, [&] { wf_direct<<<L.gShadow, 256, 0, st>>>(L.v, L.s); });
         timed(2, [&] { launch_shade(L, st, cur, d); });
         timed(3, [&] {
             if (L.binShadow) enqueue_binning(L, st, 1u, cur);
@@ -1770,7 +1738,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             e = cudaGetLastError();
         }
         throttle.after_launch(exec[k] && k != 0 ? wf->side : st);
-        launches += 3 + 6ull * L.depth + (L.depth > 1 ? L.depth - 1ull : 0ull) + (L.binShadow ? 3ull * L.depth : 0ull) +
+        launches += 3 + 6ull * L.depth + (L.binShadow ? 3ull * L.depth : 0ull) +
                 (L.binRays && L.depth > 1 ? 3ull * (L.depth - 1) : 0ull) + (adj ? 2ull + 6ull * L.depth - 1ull : 0ull);
         ++launchedWaves;
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront launch");
