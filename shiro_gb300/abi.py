@@ -139,7 +139,7 @@ class WavefrontConfig(C.Structure):
         ("use_graph", C.c_uint32), ("shade_regs", C.c_uint32), ("extend_steps", C.c_uint32),
         ("refill_idle", C.c_uint32), ("concurrent_waves", C.c_uint32), ("bin_rays", C.c_uint32),
         ("bin_shadow", C.c_uint32), ("coop_extend", C.c_uint32), ("coop_occlude", C.c_uint32),
-        ("extend_regs", C.c_uint32), ("occlude_regs", C.c_uint32),
+        ("extend_regs", C.c_uint32), ("occlude_regs", C.c_uint32), ("occlude_refill", C.c_uint32),
     ]
 
 

@@ -777,12 +777,43 @@ __global__ void __launch_bounds__(256) wf_miss(WfView v, DevScene s, uint32_t de
 // (Lane refill as in wf_extend measured slower here: shadow rays are short
 // and an any-hit ends them early, so the refill bookkeeping outweighs the
 // divergence it removes.)
-template <bool kCoop, int kMinBlocks>
+// kMode 0: one ray per lane for the warp's 32 entries; 1: cooperative
+// triangle tests; 2: lane refill on the wide BVH as in wf_extend (a lane takes
+// the next entry of its warp's chunk as soon as enough lanes are idle).
+template <int kMode, int kMinBlocks>
 __global__ void __launch_bounds__(256, kMinBlocks) wf_occlude(WfView v, DevScene s, uint32_t binned) {
     const uint32_t count = v.counters[4];
     const uint32_t* sq = binned ? v.sortedQ : v.shadowRayQ;
     NullCounter ctr;
-    if (kCoop && s.nodes8) {
+    if (kMode == 2 && s.nodes8) {
+        uint2 stack[kStackWide];
+        WideTrav t;
+        wide_init(t, V3{0.0f, 0.0f, 0.0f}, V3{0.0f, 0.0f, 1.0f}, 0.0f);
+        LaneFeed feed;
+        bool has = false;
+        size_t e = 0;
+        for (;;) {
+            const uint32_t got = feed_lanes(feed, &v.counters[kFetchOcclude], count, has, v.refillIdle);
+            if (got != 0xffffffffu) {
+                const uint32_t item = sq[got];
+                const uint32_t j = item >> 3, k = item & 7u;
+                e = static_cast<size_t>(k) * v.P + j;
+                const float4 o4 = v.shOrigin[j], d4 = v.shDir[e];
+                wide_init(t, V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z}, d4.w);
+                has = true;
+            }
+            if (__ballot_sync(kFull, has) == 0u) break;
+            if (has) {
+                const int r = wide_occluded_advance(s, t, stack, v.travSteps, ctr);
+                if (r >= 0) {
+                    if (r == 1) v.shDir[e].w = 0.0f;
+                    has = false;
+                }
+            }
+        }
+        return;
+    }
+    if (kMode == 1 && s.nodes8) {
         // one node per lane and step, the step's triangles tested by the whole warp
         __shared__ CoopTris coop[8];
         CoopTris& c = coop[threadIdx.x >> 5];
@@ -1280,6 +1311,7 @@ WavefrontState* wf_state(ContextImpl* ctx) {
         c.coop_occlude = 2;
         c.extend_regs = 64;
         c.occlude_regs = 64;
+        c.occlude_refill = 2;
         cudaDeviceGetAttribute(&ctx->wavefront->smCount, cudaDevAttrMultiProcessorCount, ctx->device);
     }
     return ctx->wavefront;
@@ -1404,6 +1436,7 @@ struct Launch {
     uint32_t binRays, binShadow;  // queue binning before extend (bounces >= 1) / occlude
     uint32_t coopExt, coopOcc;    // warp-cooperative triangle tests in extend / occlude
     uint32_t extRegs, occRegs;    // register caps of the per-lane traversal stages
+    uint32_t occRefill;           // lane refill in the occlusion stage
     int gBin;
     AdjWave aw;                   // aw.on: the adjoint replay follows the forward stages
     int gAdjShade, gAdjShadow, gAdjMiss;
@@ -1420,11 +1453,12 @@ auto with_extend_kernel(uint32_t coop, uint32_t regs, F&& f) {
     return f(wf_extend<false, 4>);
 }
 template <typename F>
-auto with_occlude_kernel(uint32_t coop, uint32_t regs, F&& f) {
-    if (coop) return f(wf_occlude<true, 4>);
-    if (regs == 48) return f(wf_occlude<false, 5>);
-    if (regs == 40) return f(wf_occlude<false, 6>);
-    return f(wf_occlude<false, 4>);
+auto with_occlude_kernel(uint32_t coop, uint32_t refill, uint32_t regs, F&& f) {
+    if (coop) return f(wf_occlude<1, 4>);
+    if (refill) return f(wf_occlude<2, 4>);
+    if (regs == 48) return f(wf_occlude<0, 5>);
+    if (regs == 40) return f(wf_occlude<0, 6>);
+    return f(wf_occlude<0, 4>);
 }
 
 void launch_extend(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t binned) {
@@ -1435,7 +1469,7 @@ void launch_extend(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t binn
 }
 
 void launch_occlude(const Launch& L, cudaStream_t st, uint32_t binned) {
-    with_occlude_kernel(L.coopOcc, L.occRegs, [&](auto kern) {
+    with_occlude_kernel(L.coopOcc, L.occRefill, L.occRegs, [&](auto kern) {
         kern<<<L.gOcc, L.bShadow, 0, st>>>(L.v, L.s, binned);
         return 0;
     });
@@ -1615,6 +1649,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.coopOcc = cfg.coop_occlude == 1 ? 1u : 0u;
     L.extRegs = cfg.extend_regs ? cfg.extend_regs : 64;
     L.occRegs = cfg.occlude_regs ? cfg.occlude_regs : 64;
+    L.occRefill = cfg.occlude_refill == 1 ? 1u : 0u;
     L.gExt = with_extend_kernel(L.coopExt, L.extRegs, [&](auto kern) { return grid_for(kern, L.bExt, wf->smCount); });
     L.shadeRegs = cfg.shade_regs;
     L.ext = ctx->extendedMaterials;
@@ -1623,7 +1658,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.v.refillIdle = static_cast<int>(cfg.refill_idle ? cfg.refill_idle : 8);
     L.gMiss = grid_for(wf_miss, 256, wf->smCount);
     L.gShadow = grid_for(wf_shadow, 256, wf->smCount);
-    L.gOcc = with_occlude_kernel(L.coopOcc, L.occRegs, [&](auto kern) { return grid_for(kern, L.bShadow, wf->smCount); });
+    L.gOcc = with_occlude_kernel(L.coopOcc, L.occRefill, L.occRegs, [&](auto kern) { return grid_for(kern, L.bShadow, wf->smCount); });
     L.gRes = grid_for(wf_resolve, 128, wf->smCount);
     L.gBin = grid_for(wf_bin_scatter, 256, wf->smCount);
     L.gAdjShade = grid_for(wa_shade, 128, wf->smCount);
@@ -1952,6 +1987,9 @@ int wavefront_set_config(ContextImpl* ctx, const ShiroWavefrontConfig* cfg) {
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "extend_regs and occlude_regs must be 40, 48 or 64 (0 leaves them)");
     if (cfg->extend_regs) wf->cfg.extend_regs = cfg->extend_regs;
     if (cfg->occlude_regs) wf->cfg.occlude_regs = cfg->occlude_regs;
+    if (cfg->occlude_refill > 2)
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "occlude_refill must be 1 (on), 2 (off) or 0");
+    if (cfg->occlude_refill) wf->cfg.occlude_refill = cfg->occlude_refill;
     wf->cfg.use_graph = cfg->use_graph;
     return SHIRO_OK;
 }
@@ -2063,6 +2101,13 @@ int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefr
         ShiroWavefrontConfig c = best;
         c.extend_regs = regs;
         if ((rc = trial(c)) != SHIRO_OK) return rc;
+    }
+    if (ctx->nodes8 && ctx->bvhWidth != 2) {  // lane refill in the occlusion stage
+        for (uint32_t on : {1u, 2u}) {
+            ShiroWavefrontConfig c = best;
+            c.occlude_refill = on;
+            if ((rc = trial(c)) != SHIRO_OK) return rc;
+        }
     }
     if (ctx->nodes8 && ctx->bvhWidth != 2) {  // warp-cooperative triangle tests
         for (uint32_t on : {1u, 2u}) {
