@@ -362,9 +362,9 @@ typedef struct ShiroWavefrontConfig {
     uint32_t extend_regs;      /* register cap of the closest-hit stage (per-lane triangle tests):
                                   64, 48 or 40 (more resident warps, some spilling); 0 leaves it */
     uint32_t occlude_regs;     /* the same for the occlusion stage */
-    uint32_t occlude_refill;   /* 1: the occlusion stage refills a warp's idle lanes from its chunk
-                                  of the queue (extend_steps, refill_idle as in the closest-hit
-                                  stage); 2: one ray per lane for 32 entries; 0 leaves it.
+    uint32_t occlude_refill;   /* 1 (default): the occlusion stage refills a warp's idle lanes from
+                                  its chunk of the queue (extend_steps, refill_idle as in the
+                                  closest-hit stage); 2: one ray per lane for 32 entries; 0 leaves it.
                                   Visibility is identical either way. */
 } ShiroWavefrontConfig;
 int shiro_gpu_get_wavefront_config(const ShiroGpuContext* ctx, ShiroWavefrontConfig* out);
