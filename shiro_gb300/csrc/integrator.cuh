@@ -188,39 +188,19 @@ __device__ __forceinline__ bool light_distant(const DevScene& s, const DevReques
     return true;
 }
 
-// The direction, radiance and pdf of sample k of dome light li: they depend
-// on the path's sampler only, not on the vertex, so a caller may take them
-// before the vertex is known (the texel pick's loads then overlap the hit's).
-struct DomePick {
-    V3 dir, rad;
-    float pdf;
-    bool ok;
-};
-
-__device__ __forceinline__ DomePick dome_pick(const DevScene& s, const DevRequest& q, const Sampler& smp, uint32_t depth,
-                                              uint32_t li, uint32_t k) {
-    const uint32_t dim = kDirectDimBase + depth * kDirectDepthStride + li * kDirectLightStride + k * kDirectSampleStride;
-    DomePick p;
-    p.pdf = 0.0f;
-    const bool useCdf = (q.flags & SHIRO_RENDER_ENV_CDF) != 0u;
-    p.ok = sample_dome(s, s.domes[li], smp.next2d(dim), useCdf, &p.dir, &p.rad, &p.pdf) && p.pdf > 0.0f;
-    return p;
-}
-
-// Sample k of dome light li (:1542-1573); `pre`, when given, is its
-// dome_pick.
+// Sample k of dome light li (:1542-1573).
 template <typename Ctr>
 __device__ __forceinline__ bool light_dome(const DevScene& s, const DevRequest& q, const Vertex& v, const Sampler& smp,
-                                           uint32_t depth, uint32_t li, uint32_t k, V3* dir, V3* c, Ctr& ctr,
-                                           const DomePick* pre = nullptr) {
+                                           uint32_t depth, uint32_t li, uint32_t k, V3* dir, V3* c, Ctr& ctr) {
+    const uint32_t dim = kDirectDimBase + depth * kDirectDepthStride + li * kDirectLightStride + k * kDirectSampleStride;
+    V3 ld, lr;
+    float lp = 0.0f;
     if (s.domes[li].env >= 0) {
         ctr.env_sample();
         ctr.env_eval();
     }
-    const DomePick p = pre ? *pre : dome_pick(s, q, smp, depth, li, k);
-    if (!p.ok) return false;
-    const V3 ld = p.dir, lr = p.rad;
-    const float lp = p.pdf;
+    const bool useCdf = (q.flags & SHIRO_RENDER_ENV_CDF) != 0u;
+    if (!sample_dome(s, s.domes[li], smp.next2d(dim), useCdf, &ld, &lr, &lp) || lp <= 0.0f) return false;
     const float nl = sclamp(dot(v.n, ld), 0.0f, 1.0f);
     if (nl <= 0.0f) return false;
     const Mat& m = s.materials[v.hit.material];
@@ -309,8 +289,7 @@ __device__ __forceinline__ bool light_emissive(const DevScene& s, const DevReque
 // of its shadow ray.
 template <bool kExt, typename Ctr>
 __device__ __forceinline__ bool light_sample(const DevScene& s, const DevRequest& q, const Vertex& v, const Sampler& smp,
-                                             uint32_t depth, uint32_t k, V3* dir, V3* c, float* maxDist, Ctr& ctr,
-                                             const DomePick* pre0 = nullptr) {
+                                             uint32_t depth, uint32_t k, V3* dir, V3* c, float* maxDist, Ctr& ctr) {
     *maxDist = FLT_MAX;
     if (k < s.distantCount) return light_distant(s, q, v, k, dir, c, ctr);
     const uint32_t r = k - s.distantCount;
@@ -318,7 +297,7 @@ __device__ __forceinline__ bool light_sample(const DevScene& s, const DevRequest
         if (r >= s.domeCount * q.domeSamples) return light_emissive(s, q, v, smp, depth, dir, c, maxDist, ctr);
     }
     const uint32_t li = r / q.domeSamples, j = r - li * q.domeSamples;
-    return light_dome(s, q, v, smp, depth, li, j, dir, c, ctr, (li == 0u && j == 0u) ? pre0 : nullptr);
+    return light_dome(s, q, v, smp, depth, li, j, dir, c, ctr);
 }
 
 // MIS weight of an environment hit after a non-delta bounce (:1679-1688).

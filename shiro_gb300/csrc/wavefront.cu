@@ -690,14 +690,8 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
             h.slot = __float_as_uint(h4.w);
             h.gid = v.hitGid[j];
             {
-                const Sampler smp{id.x, id.y, id.z};
-                // dome 0's first sample needs only the sampler: its texel pick
-                // and sample record load while the hit's records do
-                DomePick pre0;
-                pre0.ok = false;
-                const bool early = s.domeCount > 0u && q.domeSamples > 0u;
-                if (early) pre0 = dome_pick(s, q, smp, depth, 0u, 0u);
                 const Vertex vx = make_vertex(s, ps.ro, ps.rd, h);
+                const Sampler smp{id.x, id.y, id.z};
                 bool anyLight = false, cont;
                 if (kExt && !enter_hit(s, smp, depth, vx, h.t, ps)) {
                     cont = depth + 1u < q.maxDepth;  // passes through an opacity cut-out
@@ -716,8 +710,7 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
                     for (uint32_t k = 0; k < nls; ++k) {
                         V3 dir{0.0f, 0.0f, 0.0f}, c{0.0f, 0.0f, 0.0f};
                         float reach = 0.0f;
-                        const bool ok = light_sample<kExt>(s, q, vx, smp, depth, k, &dir, &c, &reach, ctr,
-                                                           early ? &pre0 : nullptr);
+                        const bool ok = light_sample<kExt>(s, q, vx, smp, depth, k, &dir, &c, &reach, ctr);
                         anyLight |= ok;
                         lightMask |= ok ? (1u << k) : 0u;
                         const size_t e = static_cast<size_t>(k) * v.P + j;
