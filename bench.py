@@ -291,22 +291,25 @@ def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 
     grads = {k: torch.zeros_like(v) for k, v in p.items()}
 
     def step():
-        img = gpu.render_device(cam, st)
+        img = gpu.render_device(cam, st, wavefront=True)  # the forward autograd.render runs
+        fwd_ms = gpu.last_stats()["kernel_ms"]
         d = torch.zeros_like(img)
         d[..., :3] = 2.0 * (img[..., :3] - target) / target.numel()
         for g in grads.values():
             g.zero_()
         gpu.adjoint(cam, st, d, grads)
-        return gpu.last_stats()["kernel_ms"]
+        return fwd_ms, gpu.last_stats()["kernel_ms"]
 
     for _ in range(warmup):
         step()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    adj_ms = 0.0
+    adj_ms = fwd_total = 0.0
     e0.record(stream)
     for _ in range(iters):
-        adj_ms += step()
+        f, a = step()
+        fwd_total += f
+        adj_ms += a
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / iters
@@ -314,7 +317,7 @@ def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 
     paths = size * size * 32
     gpu.close()
     return {"workload": f"256-material sphere scene, 512x256 env, {size}x{size}, 32 spp, depth 6, L2 loss",
-            "replay": form, "params": int(nparams), "ms_per_gradient": ms, "grads_per_s": 1000.0 / ms,
+            "replay": form, "forward": "wavefront", "forward_ms": fwd_total / iters, "params": int(nparams), "ms_per_gradient": ms, "grads_per_s": 1000.0 / ms,
             "adjoint_ms": adj_ms / iters, "adjoint_Mpaths_s": paths / (adj_ms / iters / 1000.0) / 1e6,
             "param_gradients_per_s": nparams * 1000.0 / ms}
 
