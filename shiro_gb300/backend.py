@@ -211,6 +211,7 @@ class GpuBackend:
         self._structure_key = skey
         if not force and self._scene_key == key:
             return
+        self._params_on_device = None  # the upload restores the scene's own parameters
         rc = self.lib.shiro_gpu_upload_scene(self._ctx, ms.ref())
         if rc != 0:
             self._scene_key = None
@@ -382,11 +383,27 @@ class GpuBackend:
 
     def set_params(self, base_color=None, roughness=None, metallic=None, env=None):
         """Overwrites the uploaded scene's base colour [M,3], roughness [M],
-        metalness [M] and dome-0 texels [H,W,3] (CUDA float32 tensors)."""
-        rc = self.lib.shiro_gpu_set_params(self._ctx, self._dptr(base_color), self._dptr(roughness),
-                                           self._dptr(metallic), self._dptr(env))
+        metalness [M] and dome-0 texels [H,W,3] (CUDA float32 tensors).
+
+        A group whose values equal (bit for bit, compared on the device) what
+        the last call wrote is not written again: an environment write
+        rebuilds the dome's importance tables, and a multi-view optimisation
+        sets the same parameters before every view's render."""
+        import torch
+
+        new = (base_color, roughness, metallic, env)
+        last = getattr(self, "_params_on_device", None) or (None, None, None, None)
+        def same(o, t):  # bit for bit (float equality would take -0.0 for 0.0)
+            return o is not None and o.shape == t.shape and torch.equal(o.view(torch.int32), t.view(torch.int32))
+
+        send = [t if t is not None and not same(o, t) else None for t, o in zip(new, last)]
+        if all(t is None for t in send):
+            return
+        rc = self.lib.shiro_gpu_set_params(self._ctx, *(self._dptr(t) for t in send))
         if rc != 0:
+            self._params_on_device = None
             raise self._err(rc)
+        self._params_on_device = tuple(t.detach().clone() if t is not None else o for t, o in zip(send, last))
 
     def render_device(self, camera: Camera, settings: RenderSettings, sample_start: int = 0,
                       sample_count: Optional[int] = None, flags: int = 0, wavefront: bool = False):

@@ -73,6 +73,32 @@ def test_set_params_equals_fresh_upload(setup):
     assert torch.equal(a, b)
 
 
+def test_set_params_rewrites_changed_values_only(setup):
+    """set_params skips a group whose values equal the last write (a
+    multi-view optimisation sets the same parameters before every view) but
+    picks up any change, including one made in place without autograd's
+    knowledge, and a fresh scene upload restores the scene's values."""
+    gpu, scene, cam, st, p = setup
+    gpu.set_params(**p)
+    ref = gpu.render_device(cam, st)
+    q = {k: v.clone() for k, v in p.items()}
+    gpu.set_params(**q)  # equal content: nothing is rewritten
+    assert torch.equal(gpu.render_device(cam, st), ref)
+    q["env"].data[5:9, 12:20] *= 4.0  # an in-place edit of the same tensor
+    q["roughness"].data[2] = 0.05
+    gpu.set_params(**q)
+    edited = gpu.render_device(cam, st)
+    assert not torch.equal(edited, ref)
+    gpu.set_params(**p)
+    assert torch.equal(gpu.render_device(cam, st), ref)
+    gpu.set_params(**q)
+    assert torch.equal(gpu.render_device(cam, st), edited)
+    gpu.upload_scene(scene, force=True)  # the scene's own values again
+    gpu.set_params(**q)
+    assert torch.equal(gpu.render_device(cam, st), edited)
+    gpu.set_params(**p)
+
+
 def _loss(d, img):
     return float((d.double() * img.double()).sum())
 
