@@ -116,6 +116,13 @@ struct WfView {
     // non-NULL: instead of resolving pixels, the wave's path records go out
     // per path (radiance, first-hit depth) in request path order
     float4* recordsOut;
+    // non-NULL (adjoint waves): the forward stages log, per bounce and slot
+    // ([depth][P]), the hit record, the hit triangle and the mask of light
+    // samples that were taken and unoccluded; the replay reads them instead
+    // of tracing its rays again
+    float4* hitLog;
+    uint32_t* gidLog;
+    uint8_t* visLog;
 };
 
 // Buckets of the queue binning: light sample (8) x direction octant (8) x
@@ -382,6 +389,14 @@ __device__ __forceinline__ void flush_stage(uint32_t* buf, uint32_t& n, uint32_t
     n = rest;
 }
 
+__device__ __forceinline__ void log_hit(const WfView& v, uint32_t depth, uint32_t j, const float4& h, uint32_t gid) {
+    if (v.hitLog) {
+        const size_t e = static_cast<size_t>(depth) * v.P + j;
+        v.hitLog[e] = h;
+        v.gidLog[e] = gid;
+    }
+}
+
 // ---- warp-cooperative triangle tests ----------------------------------------
 // A wide node's leaf triangles are tested by the lanes whose ray reached it;
 // tested lane by lane, a step in which a few lanes hold triangles keeps the
@@ -506,9 +521,11 @@ __device__ __forceinline__ uint32_t coop_any(const DevScene& s, const WideTrav& 
 // the hits at the front of the shade queue and the misses at its back, so the
 // shade stage runs warps of hits and warps of misses instead of warps that
 // take both branches.
-// kMinBlocks blocks of 256 per SM: 4, 5, 6 cap the registers at 64, 48, 40.
-template <bool kCoop, int kMinBlocks>
-__global__ void __launch_bounds__(256, kMinBlocks) wf_extend(WfView v, DevScene s, uint32_t cur, uint32_t binned) {
+// kMinBlocks blocks of 256 per SM: 4, 5, 6 cap the registers at 64, 48, 40;
+// kLog: an adjoint wave's forward stage, which logs its hits for the replay.
+template <bool kCoop, int kMinBlocks, bool kLog = false>
+__global__ void __launch_bounds__(256, kMinBlocks) wf_extend(WfView v, DevScene s, uint32_t cur, uint32_t binned,
+                                                             uint32_t depth) {
     __shared__ uint32_t stage[8][2][64];
     const uint32_t count = v.counters[cur];
     const uint32_t* q = binned ? v.sortedQ : (cur ? v.rayQ1 : v.rayQ0);
@@ -558,8 +575,10 @@ __global__ void __launch_bounds__(256, kMinBlocks) wf_extend(WfView v, DevScene 
                 if (!__any_sync(kFull, has && !fin)) break;
             }
             if (fin) {
-                v.hit[j] = make_float4(t.tmax, t.bu, t.bv, __uint_as_float(t.bestSlot));
+                const float4 h4 = make_float4(t.tmax, t.bu, t.bv, __uint_as_float(t.bestSlot));
+                v.hit[j] = h4;
                 v.hitGid[j] = t.bestGid;
+                if (kLog) log_hit(v, depth, j, h4, t.bestGid);
                 has = false;
             }
             const bool hit = fin && t.bestSlot != 0xffffffffu;
@@ -596,8 +615,10 @@ __global__ void __launch_bounds__(256, kMinBlocks) wf_extend(WfView v, DevScene 
             if (__ballot_sync(kFull, has) == 0u) break;
             bool fin = false;
             if (has && wide_closest_advance(s, t, stack, v.travSteps, ctr)) {
-                v.hit[j] = make_float4(t.tmax, t.bu, t.bv, __uint_as_float(t.bestSlot));
+                const float4 h4 = make_float4(t.tmax, t.bu, t.bv, __uint_as_float(t.bestSlot));
+                v.hit[j] = h4;
                 v.hitGid[j] = t.bestGid;
+                if (kLog) log_hit(v, depth, j, h4, t.bestGid);
                 fin = true;
                 has = false;
             }
@@ -627,8 +648,10 @@ __global__ void __launch_bounds__(256, kMinBlocks) wf_extend(WfView v, DevScene 
             const float4 o = v.ro[j], d = v.rd[j];
             HitRec h;
             trace_closest(s, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, &h, ctr);
-            v.hit[j] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+            const float4 h4 = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+            v.hit[j] = h4;
             v.hitGid[j] = h.gid;
+            if (kLog) log_hit(v, depth, j, h4, h.gid);
             hit = h.slot != 0xffffffffu;
         }
         const uint32_t hs = warp_claim(&v.counters[kHitCount], valid && hit);
@@ -725,6 +748,7 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
                     }
                     cont = continue_path<kExt>(s, q, vx, smp, depth, ps, ctr) && depth + 1u < q.maxDepth;
                 }
+                if (v.visLog && !anyLight) v.visLog[static_cast<size_t>(depth) * v.P + j] = 0u;
                 uint32_t nb = pack_state(ps);
                 if (!cont && anyLight) {
                     nb |= kFlagDone;
@@ -871,19 +895,22 @@ __global__ void __launch_bounds__(256, kMinBlocks) wf_occlude(WfView v, DevScene
 }
 
 // In-order sum of a path's unoccluded light samples (sum_direct's order).
-__global__ void __launch_bounds__(256) wf_shadow(WfView v, DevScene s) {
+__global__ void __launch_bounds__(256) wf_shadow(WfView v, DevScene s, uint32_t depth) {
     const uint32_t count = v.counters[2];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t j = v.shadowQ[i];
         const DevRequest& q = v.reqs[v.ident[j].w].q;
         const float4 t4 = v.shT[j], r4 = v.rad[j];
+        uint32_t visible = 0;
         const V3 direct = sum_direct<true>(s, q, [&](uint32_t k, V3* c) {
             const size_t e = static_cast<size_t>(k) * v.P + j;
             if (v.shDir[e].w == 0.0f) return false;
             const float4 c4 = v.shC[e];
             *c = V3{c4.x, c4.y, c4.z};
+            visible |= 1u << k;
             return true;
         });
+        if (v.visLog) v.visLog[static_cast<size_t>(depth) * v.P + j] = static_cast<uint8_t>(visible);
         const V3 rad = V3{r4.x, r4.y, r4.z} + V3{t4.x, t4.y, t4.z} * direct;
         v.rad[j] = make_float4(rad.x, rad.y, rad.z, r4.w);
         if (t4.w != 0.0f) write_record(v, j, rad, r4.w);  // the path ends here
@@ -996,6 +1023,33 @@ __global__ void __launch_bounds__(128) wa_generate(WfView v, AdjWave aw) {
     }
 }
 
+// The replay's rays of bounce `depth` take the hits the forward stages
+// logged for their slots (the same rays: the replay follows the forward's
+// decisions), split into the shade queue as wf_extend splits them.
+__global__ void __launch_bounds__(256) wa_hits(WfView v, uint32_t cur, uint32_t depth) {
+    const uint32_t count = v.counters[cur];
+    const uint32_t* q = cur ? v.rayQ1 : v.rayQ0;
+    for (;;) {
+        const uint32_t base = warp_fetch(&v.counters[kFetchExtend]);
+        if (base >= count) break;
+        const uint32_t i = base + lane_id();
+        const bool valid = i < count;
+        uint32_t j = 0;
+        bool hit = false;
+        if (valid) {
+            j = q[i];
+            const size_t e = static_cast<size_t>(depth) * v.P + j;
+            const float4 h4 = v.hitLog[e];
+            v.hit[j] = h4;
+            v.hitGid[j] = v.gidLog[e];
+            hit = __float_as_uint(h4.w) != 0xffffffffu;
+        }
+        const uint32_t hs = warp_claim(&v.counters[kHitCount], valid && hit);
+        const uint32_t ms = warp_claim(&v.counters[kMissCount], valid && !hit);
+        if (valid) v.shadeQ[hit ? hs : v.P - 1u - ms] = j;
+    }
+}
+
 // Light sample k of a vertex with the factors of its gradient: its clamped
 // contribution c, gL = L w s (material gradient = delta T gL . df) and
 // gE = f R w s (texel gradient of dome 0's texture = delta T gE at `local`),
@@ -1062,7 +1116,7 @@ __global__ void __launch_bounds__(128) wa_shade(WfView v, DevScene s, AdjWave aw
         if (wbase >= count) break;
         const uint32_t i = wbase + lane_id();
         bool pushRay = false;
-        uint32_t lightMask = 0, j = 0;
+        uint32_t j = 0;
         if (i < count) {
             j = v.shadeQ[i];
             const uint4 id = v.ident[j];
@@ -1095,20 +1149,19 @@ __global__ void __launch_bounds__(128) wa_shade(WfView v, DevScene s, AdjWave aw
             aw.vtx[3 * static_cast<size_t>(j) + 2] = make_float4(vx.view.x, vx.view.y, vx.view.z, 0.0f);
             const Sampler smp{id.x, id.y, id.z};
             const uint32_t nls = light_sample_count<false>(s, q);
+            // which samples the forward stages found taken and unoccluded at this vertex
+            const uint32_t seen = v.visLog[static_cast<size_t>(depth) * v.P + j];
             for (uint32_t k = 0; k < nls; ++k) {
                 V3 ld{0.0f, 0.0f, 0.0f}, c{0.0f, 0.0f, 0.0f}, gL{0.0f, 0.0f, 0.0f}, gE{0.0f, 0.0f, 0.0f}, local;
                 bool mark = false;
                 const bool ok = wa_light(s, q, a, vx, smp, depth, k, rec, ms, &ld, &c, &gL, &gE, &local, &mark);
-                lightMask |= ok ? (1u << k) : 0u;
                 const size_t e = static_cast<size_t>(k) * v.P + j;
-                v.shDir[e] = make_float4(ld.x, ld.y, ld.z, ok ? FLT_MAX : 0.0f);
+                v.shDir[e] = make_float4(ld.x, ld.y, ld.z, (ok && ((seen >> k) & 1u)) ? FLT_MAX : 0.0f);
                 v.shC[e] = make_float4(c.x, c.y, c.z, 0.0f);
                 aw.lgrad[3 * e] = make_float4(gL.x, gL.y, gL.z, 0.0f);
                 aw.lgrad[3 * e + 1] = make_float4(gE.x, gE.y, gE.z, mark ? 1.0f : 0.0f);
                 aw.lgrad[3 * e + 2] = make_float4(local.x, local.y, local.z, 0.0f);
             }
-            const V3 org = shadow_origin(vx);
-            v.shOrigin[j] = make_float4(org.x, org.y, org.z, 0.0f);
             v.shT[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, 0.0f);
             // continuation (the reflecting lobes of continue_path)
             bool alive = false, due = false;
@@ -1176,8 +1229,6 @@ __global__ void __launch_bounds__(128) wa_shade(WfView v, DevScene s, AdjWave aw
             }
         }
         warp_push(cout, qout, pushRay, j);
-        for (uint32_t k = 0; k < v.lightSamples; ++k)
-            warp_push(&v.counters[4], v.shadowRayQ, (lightMask >> k) & 1u, (j << 3) | k);
     }
 }
 
@@ -1266,7 +1317,7 @@ __global__ void __launch_bounds__(128) wf_records_out(WfView v) {
 // ===========================================================================
 // One pool of paths in flight with its queues, and the wave graph it replays.
 struct WavePool {
-    DeviceBlock state, shadow, queues, records, adj;
+    DeviceBlock state, shadow, queues, records, adj, adjLog;
     // the last instantiated wave graph and the launch parameters it bakes in
     // (reused while a call's parameters are byte-identical: only the tables'
     // contents differ between such calls, and the kernels read them from memory)
@@ -1438,14 +1489,15 @@ struct Launch {
     uint32_t occRefill;           // lane refill in the occlusion stage
     int gBin;
     AdjWave aw;                   // aw.on: the adjoint replay follows the forward stages
-    int gAdjShade, gAdjShadow, gAdjMiss;
+    int gAdjShade, gAdjShadow, gAdjMiss, gAdjHits;
     bool ext;  // the scene uses transmission, opacity or emitters
 };
 
 // The traversal stages' instantiations: cooperative triangle tests (at 64
 // registers) or per-lane ones with a register cap of 64, 48 or 40.
 template <typename F>
-auto with_extend_kernel(uint32_t coop, uint32_t regs, F&& f) {
+auto with_extend_kernel(uint32_t coop, uint32_t regs, bool log, F&& f) {
+    if (log) return f(wf_extend<false, 4, true>);
     if (coop) return f(wf_extend<true, 4>);
     if (regs == 48) return f(wf_extend<false, 5>);
     if (regs == 40) return f(wf_extend<false, 6>);
@@ -1460,9 +1512,9 @@ auto with_occlude_kernel(uint32_t coop, uint32_t refill, uint32_t regs, F&& f) {
     return f(wf_occlude<0, 4>);
 }
 
-void launch_extend(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t binned) {
-    with_extend_kernel(L.coopExt, L.extRegs, [&](auto kern) {
-        kern<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, binned);
+void launch_extend(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t binned, uint32_t depth) {
+    with_extend_kernel(L.coopExt, L.extRegs, L.v.hitLog != nullptr, [&](auto kern) {
+        kern<<<L.gExt, L.bExt, 0, st>>>(L.v, L.s, cur, binned, depth);
         return 0;
     });
 }
@@ -1479,10 +1531,9 @@ void enqueue_replay(const Launch& L, cudaStream_t st) {
     wa_generate<<<L.gGen, 128, 0, st>>>(L.v, L.aw);
     for (uint32_t d = 0; d < L.depth; ++d) {
         const uint32_t cur = d & 1u;
-        launch_extend(L, st, cur, 0u);
+        wa_hits<<<L.gAdjHits, 256, 0, st>>>(L.v, cur, d);  // no tracing: the forward stages' hits and visibility
         wa_shade<<<L.gAdjShade, 128, 0, st>>>(L.v, L.s, L.aw, cur, d);
         wa_miss<<<L.gAdjMiss, 256, 0, st>>>(L.v, L.s, L.aw, d);
-        launch_occlude(L, st, 0u);
         wa_shadow<<<L.gAdjShadow, 128, 0, st>>>(L.v, L.s, L.aw);
         wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur);
     }
@@ -1524,11 +1575,11 @@ void enqueue_wave(const Launch& L, cudaStream_t st) {
         const uint32_t cur = d & 1u;
         const uint32_t br = (L.binRays && d > 0) ? 1u : 0u;  // camera rays are coherent already
         if (br) enqueue_binning(L, st, 0u, cur);
-        launch_extend(L, st, cur, br);
+        launch_extend(L, st, cur, br, d);
         launch_shade(L, st, cur, d);
         if (L.binShadow) enqueue_binning(L, st, 1u, cur);
         launch_occlude(L, st, L.binShadow);
-        wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s);
+        wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s, d);
         wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur);
     }
     if (L.aw.on) enqueue_replay(L, st);
@@ -1554,14 +1605,14 @@ void enqueue_wave_timed(const Launch& L, cudaStream_t st, std::vector<std::pair<
         const uint32_t br = (L.binRays && d > 0) ? 1u : 0u;
         timed(1, [&] {
             if (br) enqueue_binning(L, st, 0u, cur);
-            launch_extend(L, st, cur, br);
+            launch_extend(L, st, cur, br, d);
         });
         timed(2, [&] { launch_shade(L, st, cur, d); });
         timed(3, [&] {
             if (L.binShadow) enqueue_binning(L, st, 1u, cur);
             launch_occlude(L, st, L.binShadow);
         });
-        timed(5, [&] { wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s); });
+        timed(5, [&] { wf_shadow<<<L.gShadow, 256, 0, st>>>(L.v, L.s, d); });
         timed(5, [&] { wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur); });
     }
     timed(4, [&] {
@@ -1603,7 +1654,10 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
         for (uint32_t k = 0; k < nl; ++k)
             if (!ensure_block(ctx, &wf->pools[k].adj,
                               static_cast<size_t>(poolP[k]) * (kAdjSlotFloat4 + kAdjLightFloat4 * std::max(1u, lightSamples)) *
-                                  sizeof(float4), "adjoint replay state"))
+                                  sizeof(float4), "adjoint replay state") ||
+                !ensure_block(ctx, &wf->pools[k].adjLog,
+                              static_cast<size_t>(poolP[k]) * std::max(1u, pl.maxDepth) *
+                                  (sizeof(float4) + sizeof(uint32_t) + sizeof(uint8_t)), "adjoint hit log"))
                 return SHIRO_ERR_OUT_OF_MEMORY;
         if (!ensure_block(ctx, &wf->adjView, sizeof(AdjView), "adjoint view")) return SHIRO_ERR_OUT_OF_MEMORY;
         const cudaError_t ce = cudaMemcpyAsync(wf->adjView.ptr, adj, sizeof(AdjView), cudaMemcpyHostToDevice, ctx->stream);
@@ -1649,7 +1703,8 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.extRegs = cfg.extend_regs ? cfg.extend_regs : 64;
     L.occRegs = cfg.occlude_regs ? cfg.occlude_regs : 64;
     L.occRefill = cfg.occlude_refill == 1 ? 1u : 0u;
-    L.gExt = with_extend_kernel(L.coopExt, L.extRegs, [&](auto kern) { return grid_for(kern, L.bExt, wf->smCount); });
+    L.gExt = with_extend_kernel(L.coopExt, L.extRegs, adj != nullptr,
+                                [&](auto kern) { return grid_for(kern, L.bExt, wf->smCount); });
     L.shadeRegs = cfg.shade_regs;
     L.ext = ctx->extendedMaterials;
     L.gShade = with_shade_kernel(L.shadeRegs, L.ext, [&](auto kern) { return grid_for(kern, L.bShade, wf->smCount); });
@@ -1663,6 +1718,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.gAdjShade = grid_for(wa_shade, 128, wf->smCount);
     L.gAdjShadow = grid_for(wa_shadow, 128, wf->smCount);
     L.gAdjMiss = grid_for(wa_miss, 256, wf->smCount);
+    L.gAdjHits = grid_for(wa_hits, 256, wf->smCount);
     L.binRays = cfg.bin_rays == 1 ? 1u : 0u;
     L.binShadow = cfg.bin_shadow == 1 ? 1u : 0u;
     {
@@ -1688,6 +1744,20 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
         aw.on = 1u;
         return aw;
     };
+    // the forward stages' hit / visibility logs of each pool; every hit record
+    // starts as a miss, so that a replay ray the forward did not trace (it
+    // cannot happen when both follow the same decisions) reads a miss, never
+    // a triangle of another call's scene
+    auto add_logs = [&](WfView& v, uint32_t k) -> cudaError_t {
+        if (!adj) return cudaSuccess;
+        const size_t n = static_cast<size_t>(poolP[k]) * std::max(1u, pl.maxDepth);
+        char* b = static_cast<char*>(wf->pools[k].adjLog.ptr);
+        v.hitLog = reinterpret_cast<float4*>(b);
+        v.gidLog = reinterpret_cast<uint32_t*>(b + n * sizeof(float4));
+        v.visLog = reinterpret_cast<uint8_t*>(b + n * (sizeof(float4) + sizeof(uint32_t)));
+        return cudaMemsetAsync(v.hitLog, 0xff, n * sizeof(float4), st);
+    };
+    if ((e = add_logs(L.v, 0)) != cudaSuccess) return cuda_fail(ctx, e, "adjoint hit log");
     L.aw = adj_wave(0);
     Launch lanes[kMaxConcurrentWaves];
     for (uint32_t k = 0; k < nl; ++k) {
@@ -1700,6 +1770,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             v.binLo = L.v.binLo;
             v.binScale = L.v.binScale;
             v.recordsOut = recordsOut;
+            if ((e = add_logs(v, k)) != cudaSuccess) return cuda_fail(ctx, e, "adjoint hit log");
             std::memcpy(&lanes[k].v, &v, sizeof(WfView));
             const AdjWave aw = adj_wave(k);
             std::memcpy(&lanes[k].aw, &aw, sizeof(AdjWave));
@@ -1773,7 +1844,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
         }
         throttle.after_launch(exec[k] && k != 0 ? wf->side : st);
         launches += 3 + 6ull * L.depth + (L.binShadow ? 3ull * L.depth : 0ull) +
-                (L.binRays && L.depth > 1 ? 3ull * (L.depth - 1) : 0ull) + (adj ? 2ull + 6ull * L.depth - 1ull : 0ull);
+                (L.binRays && L.depth > 1 ? 3ull * (L.depth - 1) : 0ull) + (adj ? 2ull + 5ull * L.depth - 1ull : 0ull);
         ++launchedWaves;
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront launch");
     }
@@ -1930,7 +2001,7 @@ void wavefront_free(ContextImpl* ctx) {
     if (wf->side) cudaStreamSynchronize(wf->side);
     for (WavePool& pool : wf->pools) {
         if (pool.exec) cudaGraphExecDestroy(pool.exec);
-        for (DeviceBlock* b : {&pool.state, &pool.shadow, &pool.queues, &pool.records, &pool.adj})
+        for (DeviceBlock* b : {&pool.state, &pool.shadow, &pool.queues, &pool.records, &pool.adj, &pool.adjLog})
             if (b->ptr) cudaFree(b->ptr);
     }
     if (wf->tables.ptr) cudaFree(wf->tables.ptr);
