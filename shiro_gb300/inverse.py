@@ -75,19 +75,23 @@ PARAMS = ("base_color", "roughness", "metallic", "env")
 
 def inverse_render(backend, scene: Scene, views: List[Camera], settings: RenderSettings, steps: int = 200,
                    lr: float = 1e-2, target_spp: int = 64, log_every: int = 0,
-                   optimize: tuple = PARAMS, decorrelate: bool = True) -> InverseResult:
+                   optimize: tuple = PARAMS, decorrelate: bool = True, autotune: bool = True) -> InverseResult:
     """Optimises the parameter groups `optimize` (all material parameters
     and the dome texels of `scene` by default; the others keep their true
     values) against targets rendered from `views`.  With both the lighting
     and the albedo unknown the problem is ambiguous (a brighter environment
     and darker materials give the same images), so the image loss falls
     faster than the parameter error.  `decorrelate` replays the adjoint from
-    sample indices independent of the forward render's (see autograd)."""
+    sample indices independent of the forward render's (see autograd).
+    `autotune` picks the wavefront configuration (pool size, waves in flight,
+    block sizes) for one view's request before the first step."""
     import torch
 
     from .autograd import render
 
     backend.upload_scene(scene, force=True)
+    if autotune:
+        backend.autotune(scene, views[0], settings)
     mats = scene.materials
     truth = dict(
         base_color=torch.tensor([m.base_color for m in mats], dtype=torch.float32, device="cuda"),
@@ -164,6 +168,7 @@ def main(argv=None) -> int:
     ap.add_argument("--lr", type=float, default=1e-2)
     ap.add_argument("--env-width", type=int, default=1024)
     ap.add_argument("--log-every", type=int, default=20)
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default wavefront configuration")
     a = ap.parse_args(argv)
     from .backend import GpuBackend
 
@@ -172,7 +177,9 @@ def main(argv=None) -> int:
                         specular_depth=a.depth, dome_light_samples=1, background_visible=True, backend=1)
     views = orbit_views(a.views, 30.0, 12.0, seed=11)
     with GpuBackend(0) as gpu:
-        r = inverse_render(gpu, scene, views, st, steps=a.steps, lr=a.lr, log_every=a.log_every)
+        r = inverse_render(gpu, scene, views, st, steps=a.steps, lr=a.lr, log_every=a.log_every,
+                           autotune=not a.no_autotune)
+        wf_config = gpu.wavefront_config()
     line = {"metric": "inverse rendering: Adam steps/s (forward + adjoint over all views)",
             "value": r.steps_per_s, "unit": "steps/s", "views": r.views, "steps": r.steps,
             "paths_per_step": r.paths_per_step, "gradient_views_per_s": r.steps_per_s * r.views,
@@ -180,7 +187,8 @@ def main(argv=None) -> int:
             "loss_first": r.loss[0], "loss_last": r.loss[-1], "param_rmse_start": r.rmse_start,
             "param_rmse_end": r.rmse_end, "unknowns": {"materials": len(scene.materials),
                                                        "env_texels": a.env_width * (a.env_width // 2) * 3},
-            "config": {"scene": "field 1310720 tris", "size": a.size, "spp": a.spp, "depth": a.depth, "lr": a.lr}}
+            "config": {"scene": "field 1310720 tris", "size": a.size, "spp": a.spp, "depth": a.depth, "lr": a.lr,
+                       "wavefront_config": wf_config}}
     print(json.dumps(line), flush=True)
     return 0
 
