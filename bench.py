@@ -431,7 +431,7 @@ def c5_bench(local: int, steps: int = 3) -> dict:
     views = orbit_views(16, 30.0, 12.0, seed=11)
     with GpuBackend(local) as gpu:
         inverse_render(gpu, scene, views, st, steps=1)  # warm-up (targets, pools, graphs)
-        r = inverse_render(gpu, scene, views, st, steps=steps, autotune=False)  # the warm-up call tuned
+        r = inverse_render(gpu, scene, views, st, steps=steps)
     return {"workload": "field 1310720 tris, 16 views 512x512, 16 spp, depth 8, 65 materials + 1024x512 env",
             "forward": "wavefront", "steps": steps, "steps_per_s": r.steps_per_s,
             "gradient_views_per_s": r.steps_per_s * r.views,

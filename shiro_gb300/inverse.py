@@ -75,7 +75,7 @@ PARAMS = ("base_color", "roughness", "metallic", "env")
 
 def inverse_render(backend, scene: Scene, views: List[Camera], settings: RenderSettings, steps: int = 200,
                    lr: float = 1e-2, target_spp: int = 64, log_every: int = 0,
-                   optimize: tuple = PARAMS, decorrelate: bool = True, autotune: bool = True) -> InverseResult:
+                   optimize: tuple = PARAMS, decorrelate: bool = True, autotune: bool = False) -> InverseResult:
     """Optimises the parameter groups `optimize` (all material parameters
     and the dome texels of `scene` by default; the others keep their true
     values) against targets rendered from `views`.  With both the lighting
@@ -84,7 +84,11 @@ def inverse_render(backend, scene: Scene, views: List[Camera], settings: RenderS
     faster than the parameter error.  `decorrelate` replays the adjoint from
     sample indices independent of the forward render's (see autograd).
     `autotune` picks the wavefront configuration (pool size, waves in flight,
-    block sizes) for one view's request before the first step."""
+    block sizes) on one view's forward request before the first step; off by
+    default: for the 512x512 16-spp views it picks two waves of 2 M paths in
+    flight, which suits the forward render but made the whole step (forward
+    + adjoint) slower than the default single 4 M-path wave (2.0 vs 3.3
+    steps/s)."""
     import torch
 
     from .autograd import render
@@ -168,7 +172,7 @@ def main(argv=None) -> int:
     ap.add_argument("--lr", type=float, default=1e-2)
     ap.add_argument("--env-width", type=int, default=1024)
     ap.add_argument("--log-every", type=int, default=20)
-    ap.add_argument("--no-autotune", action="store_true", help="keep the default wavefront configuration")
+    ap.add_argument("--autotune", action="store_true", help="autotune the wavefront configuration on one view first")
     a = ap.parse_args(argv)
     from .backend import GpuBackend
 
@@ -178,7 +182,7 @@ def main(argv=None) -> int:
     views = orbit_views(a.views, 30.0, 12.0, seed=11)
     with GpuBackend(0) as gpu:
         r = inverse_render(gpu, scene, views, st, steps=a.steps, lr=a.lr, log_every=a.log_every,
-                           autotune=not a.no_autotune)
+                           autotune=a.autotune)
         wf_config = gpu.wavefront_config()
     line = {"metric": "inverse rendering: Adam steps/s (forward + adjoint over all views)",
             "value": r.steps_per_s, "unit": "steps/s", "views": r.views, "steps": r.steps,
