@@ -388,13 +388,15 @@ int shiro_gpu_adjoint(ShiroGpuContext* ctx, const ShiroRenderDesc* request, cons
                       float* d_base_color, float* d_roughness, float* d_metallic, float* d_env_rgb);
 
 /* How shiro_gpu_adjoint replays paths: 1 (default) with the wavefront form -
- * each wave of paths runs its forward stages, then replays its paths with
- * gradient stages on the same pool and queues (closest hit and occlusion
- * shared with the forward; light-sample and continuation gradients after the
- * visibility of the vertex's light samples is known); 0 one thread per path
- * (the whole replay in one kernel, after a wavefront pass for the paths'
- * radiance).  Both accumulate the same gradients (up to the order of their
- * float atomics). */
+ * each wave of paths runs its forward stages, which also log every bounce's
+ * hits and light-sample visibility, then replays its paths with gradient
+ * stages on the same pool and queues (the logged hits instead of tracing
+ * again; light-sample and continuation gradients once the vertex's direct
+ * light is known); 0 one thread per path (the whole replay, tracing
+ * included, in one kernel, after a wavefront pass for the paths' radiance).
+ * Both accumulate the same gradients (up to the order of their float
+ * atomics).  The wavefront form holds 21 bytes per path slot and bounce of
+ * device memory for its logs. */
 int shiro_gpu_set_adjoint_form(ShiroGpuContext* ctx, uint32_t wavefront);
 
 /* Frozen-sampling forward of the differentiable form: renders the beauty
