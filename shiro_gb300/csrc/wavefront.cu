@@ -159,6 +159,27 @@ __device__ __forceinline__ void warp_push(uint32_t* counter, uint32_t* queue, bo
     if (pred) queue[base + __popc(ballot & ((1u << lane_id()) - 1u))] = item;
 }
 
+// Appends (j << 3 | k) for every bit k < n of `mask` to one queue with a
+// single atomicAdd per warp: the warp's entries of sample 0, then of sample
+// 1, ... (the order of per-sample pushes, without their atomics).
+__device__ __forceinline__ void warp_push_samples(uint32_t* counter, uint32_t* queue, uint32_t mask, uint32_t n,
+                                                  uint32_t j) {
+    const uint32_t active = __activemask();
+    uint32_t total = 0;
+    for (uint32_t k = 0; k < n; ++k) total += __popc(__ballot_sync(active, (mask >> k) & 1u));
+    if (total == 0u) return;
+    const uint32_t leader = __ffs(active) - 1u;
+    uint32_t base = 0;
+    if (lane_id() == leader) base = atomicAdd(counter, total);
+    base = __shfl_sync(active, base, leader);
+    const uint32_t lt = (1u << lane_id()) - 1u;
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t b = __ballot_sync(active, (mask >> k) & 1u);
+        if ((mask >> k) & 1u) queue[base + __popc(b & lt)] = (j << 3) | k;
+        base += __popc(b);
+    }
+}
+
 __device__ __forceinline__ const WaveDesc& cur_wave(const WfView& v) { return v.waves[v.counters[3]]; }
 
 __device__ __forceinline__ const WaveSeg& find_seg(const WfView& v, const WaveDesc& w, uint32_t j, bool byPixel) {
@@ -768,8 +789,7 @@ __global__ void __maxnreg__(kRegs) wf_shade(WfView v, DevScene s, uint32_t cur, 
         }
         warp_push(cout, qout, pushRay, j);
         warp_push(&v.counters[2], v.shadowQ, pushShadow, j);
-        for (uint32_t k = 0; k < v.lightSamples; ++k)
-            warp_push(&v.counters[4], v.shadowRayQ, (lightMask >> k) & 1u, (j << 3) | k);
+        warp_push_samples(&v.counters[4], v.shadowRayQ, lightMask, v.lightSamples, j);
     }
 }
 
@@ -1027,12 +1047,14 @@ __global__ void __launch_bounds__(128) wa_generate(WfView v, AdjWave aw) {
 // logged for their slots (the same rays: the replay follows the forward's
 // decisions), split into the shade queue as wf_extend splits them.
 __global__ void __launch_bounds__(256) wa_hits(WfView v, uint32_t cur, uint32_t depth) {
+    // one pair of queue atomics per 256 entries (per-warp atomics on the two
+    // counters serialised the kernel)
+    __shared__ uint32_t wHit[8], wMiss[8], base[2];
     const uint32_t count = v.counters[cur];
     const uint32_t* q = cur ? v.rayQ1 : v.rayQ0;
-    for (;;) {
-        const uint32_t base = warp_fetch(&v.counters[kFetchExtend]);
-        if (base >= count) break;
-        const uint32_t i = base + lane_id();
+    const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
+    for (uint32_t start = blockIdx.x * 256u; start < count; start += gridDim.x * 256u) {
+        const uint32_t i = start + threadIdx.x;
         const bool valid = i < count;
         uint32_t j = 0;
         bool hit = false;
@@ -1044,9 +1066,29 @@ __global__ void __launch_bounds__(256) wa_hits(WfView v, uint32_t cur, uint32_t 
             v.hitGid[j] = v.gidLog[e];
             hit = __float_as_uint(h4.w) != 0xffffffffu;
         }
-        const uint32_t hs = warp_claim(&v.counters[kHitCount], valid && hit);
-        const uint32_t ms = warp_claim(&v.counters[kMissCount], valid && !hit);
-        if (valid) v.shadeQ[hit ? hs : v.P - 1u - ms] = j;
+        const uint32_t hb = __ballot_sync(kFull, valid && hit), mb = __ballot_sync(kFull, valid && !hit);
+        if (lane == 0) {
+            wHit[w] = __popc(hb);
+            wMiss[w] = __popc(mb);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t th = 0, tm = 0;
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t a = wHit[k], b = wMiss[k];
+                wHit[k] = th;
+                wMiss[k] = tm;
+                th += a;
+                tm += b;
+            }
+            base[0] = th ? atomicAdd(&v.counters[kHitCount], th) : 0u;
+            base[1] = tm ? atomicAdd(&v.counters[kMissCount], tm) : 0u;
+        }
+        __syncthreads();
+        const uint32_t lt = (1u << lane) - 1u;
+        if (valid && hit) v.shadeQ[base[0] + wHit[w] + __popc(hb & lt)] = j;
+        if (valid && !hit) v.shadeQ[v.P - 1u - (base[1] + wMiss[w] + __popc(mb & lt))] = j;
+        __syncthreads();
     }
 }
 
