@@ -979,10 +979,14 @@ __global__ void __launch_bounds__(128) wf_resolve(WfView v) {
         const float cnt = static_cast<float>(n);
         const float inv = 1.0f / cnt;
         const size_t px = static_cast<size_t>(sg.pixelStart) + lp;
-        r.aov.beauty[4 * px + 0] = b0 / cnt;
-        r.aov.beauty[4 * px + 1] = b1 / cnt;
-        r.aov.beauty[4 * px + 2] = b2 / cnt;
-        r.aov.beauty[4 * px + 3] = b3 / cnt;
+        if ((reinterpret_cast<uintptr_t>(r.aov.beauty) & 15u) == 0u) {  // one 16-byte store (host planes too)
+            reinterpret_cast<float4*>(r.aov.beauty)[px] = make_float4(b0 / cnt, b1 / cnt, b2 / cnt, b3 / cnt);
+        } else {
+            r.aov.beauty[4 * px + 0] = b0 / cnt;
+            r.aov.beauty[4 * px + 1] = b1 / cnt;
+            r.aov.beauty[4 * px + 2] = b2 / cnt;
+            r.aov.beauty[4 * px + 3] = b3 / cnt;
+        }
         const V3 a = alb * inv, nn = nrm * inv;
         r.aov.albedo[3 * px + 0] = a.x;
         r.aov.albedo[3 * px + 1] = a.y;
@@ -1937,12 +1941,27 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
 
 }  // namespace
 
+// A host plane the device may write in place: page-locked and mapped at
+// the same address (unified addressing).
+static bool device_writable_host(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost && a.devicePointer == p;
+}
+
 int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t count, const volatile int* cancel,
                      ShiroAovs* outs) {
     if (!ctx->hasScene) return fail(ctx, SHIRO_ERR_NO_SCENE, "no scene uploaded");
     WavefrontState* wf = wf_state(ctx);
     std::vector<DevRequest> qs(count);
     std::vector<AovPtrs> aov(count);
+    // host planes that are page-locked and mapped are written in place by the
+    // resolve stage, wave by wave while later waves render (no copy after the
+    // last wave); other host planes go through device staging and one copy
+    std::vector<char> direct(count, 0);
     uint64_t stagingFloats = 0;
     for (uint32_t r = 0; r < count; ++r) {
         int rc = validate_request(ctx, reqs[r]);
@@ -1950,14 +1969,18 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
         if (!outs[r].beauty || !outs[r].albedo || !outs[r].normal || !outs[r].depth)
             return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "null AOV pointer");
         qs[r] = make_request(reqs[r]);
-        if (!outs[r].on_device) stagingFloats += 11ull * reqs[r].settings.width * reqs[r].settings.height;
+        const uint64_t px = static_cast<uint64_t>(reqs[r].settings.width) * reqs[r].settings.height;
+        direct[r] = !outs[r].on_device && px > 0 && reqs[r].sample_count > 0 && device_writable_host(outs[r].beauty) &&
+                    device_writable_host(outs[r].albedo) && device_writable_host(outs[r].normal) &&
+                    device_writable_host(outs[r].depth);
+        if (!outs[r].on_device && !direct[r]) stagingFloats += 11ull * px;
     }
     if (stagingFloats && !ensure_block(ctx, &ctx->aovScratch, stagingFloats * sizeof(float), "AOV staging"))
         return SHIRO_ERR_OUT_OF_MEMORY;
     uint64_t off = 0;
     for (uint32_t r = 0; r < count; ++r) {
         const uint64_t px = static_cast<uint64_t>(reqs[r].settings.width) * reqs[r].settings.height;
-        if (outs[r].on_device) {
+        if (outs[r].on_device || direct[r]) {
             aov[r] = AovPtrs{outs[r].beauty, outs[r].albedo, outs[r].normal, outs[r].depth};
         } else {
             float* b = static_cast<float*>(ctx->aovScratch.ptr) + off;
@@ -1984,7 +2007,9 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
     int rc = run_waves(ctx, wf, wf->cfg, qs, aov, cancel, 0xffffffffu, &paths, nullptr);
     if (rc == SHIRO_ERR_CANCELLED) {
         // a cancelled batch is discarded (RenderParam.cpp:791-798): cleared
-        // planes, as FrameBuffer::Clear leaves them (FrameBuffer.cpp:19-24)
+        // planes, as FrameBuffer::Clear leaves them (FrameBuffer.cpp:19-24);
+        // no wave may still be writing host planes in place
+        cudaStreamSynchronize(ctx->stream);
         for (uint32_t r = 0; r < count; ++r) {
             const uint64_t px = static_cast<uint64_t>(reqs[r].settings.width) * reqs[r].settings.height;
             if (outs[r].on_device) {
@@ -2005,7 +2030,7 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
     }
     if (rc != SHIRO_OK) return rc;
     for (uint32_t r = 0; r < count; ++r) {
-        if (outs[r].on_device) continue;
+        if (outs[r].on_device || direct[r]) continue;
         const uint64_t px = static_cast<uint64_t>(reqs[r].settings.width) * reqs[r].settings.height;
         cudaError_t e = cudaMemcpyAsync(outs[r].beauty, aov[r].beauty, px * 16, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(outs[r].albedo, aov[r].albedo, px * 12, cudaMemcpyDeviceToHost, ctx->stream);

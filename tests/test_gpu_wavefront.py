@@ -69,6 +69,40 @@ def test_extended_lobes_bit_identical(gpu, name):
     assert ok, (name, k, n)
 
 
+@pytest.mark.parametrize("pool", [0, 4096])
+def test_page_locked_planes_written_in_place(gpu, pool):
+    """Page-locked host planes are written by the resolve stage in place
+    (wave by wave, several waves with a small pool); pageable ones go through
+    device staging and one copy.  Both hold the plain frame bit for bit, in a
+    batch that mixes the two kinds and a frame whose width makes the beauty
+    plane's pixels of odd pixel count (so the albedo / normal planes start off
+    16-byte boundaries)."""
+    from shiro_gb300 import scenes
+    from shiro_gb300.abi import FrameBuffer
+
+    w = scenes.sphere_workload(37, 23, 6, 6, env_width=64, env_height=32)
+    w2 = scenes.sphere_workload(64, 48, 4, 8, env_width=64, env_height=32)
+    plain = gpu.render(w.scene, w.camera, w.settings)
+    plain2 = gpu.render(w.scene, w2.camera, w2.settings)  # one scene; the second request's camera / settings
+    base = gpu.wavefront_config()
+    if pool:
+        gpu.set_wavefront_config(paths_in_flight=pool, concurrent_waves=2)
+    try:
+        for _ in range(2):  # again into the same (reused) buffers
+            fbs = [FrameBuffer(37, 23, pinned=True), FrameBuffer(64, 48), FrameBuffer(37, 23)]
+            outs = gpu.render_batch(w.scene, [(w.camera, w.settings), (w2.camera, w2.settings),
+                                              (w.camera, w.settings)], outs_fb=fbs)
+            for fb, ref in zip(outs, (plain, plain2, plain)):
+                ok, k, n = same(ref, fb)
+                assert ok, (pool, k, n)
+            pinned2 = [FrameBuffer(64, 48, pinned=True)]
+            (fb2,) = gpu.render_batch(w.scene, [(w2.camera, w2.settings)], outs_fb=pinned2)
+            ok, k, n = same(plain2, fb2)
+            assert ok, (pool, k, n)
+    finally:
+        gpu.set_wavefront_config(**base)
+
+
 def test_mixed_dome_samples_in_batch(gpu):
     """Requests of one batch with different dome-sample counts each use their
     own light samples."""
