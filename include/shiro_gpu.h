@@ -286,6 +286,15 @@ int shiro_gpu_supports_scene(const ShiroSceneDesc* scene, char* reason, size_t r
  * the thread count. */
 int shiro_gpu_scene_signature(const ShiroSceneDesc* scene, uint64_t* out);
 
+/* Page-locked host memory (no counterpart in the reference).  AOV planes
+ * inside it are written in place by the wavefront form's resolve stage, wave
+ * by wave, so a render into them needs no copy after its last wave; a host
+ * that must hand frames over in its own (pageable) buffers, as
+ * RenderBackend::RenderSampleBatch returns a FrameBuffer by value, renders
+ * into such a buffer and copies out.  Free with shiro_gpu_host_free. */
+int shiro_gpu_host_alloc(size_t bytes, void** out);
+void shiro_gpu_host_free(void* ptr);
+
 /* Environment images from disk: EnvironmentMap::Load (EnvironmentMap.cpp:
  * 49-92) without OpenImageIO, for hosts whose EnvironmentMap is built without
  * it (it then loads nothing).  Reads a Radiance RGBE file (.hdr: flat,

@@ -98,6 +98,8 @@ def load_library(path: str = LIB_PATH):
         "shiro_gpu_set_adjoint_form": ([_P, _U], C.c_int),
         "shiro_gpu_env_tables": ([_P, _U, _P, _P, _P, _P, _P, _P, _P], C.c_int),
         "shiro_gpu_scene_signature": ([_P, _P], C.c_int),
+        "shiro_gpu_host_alloc": ([C.c_size_t, _P], C.c_int),
+        "shiro_gpu_host_free": ([_P], None),
         "shiro_hdri_load": ([C.c_char_p, _P, _P, _P, C.c_char_p, C.c_size_t], C.c_int),
         "shiro_hdri_decode": ([C.c_char_p, C.c_size_t, _P, _P, _P, C.c_char_p, C.c_size_t], C.c_int),
         "shiro_hdri_free": ([_P], None),

@@ -1,11 +1,14 @@
 // GpuBackend.cpp - RenderBackend adapter over the GB300 C ABI.
 #include "GpuBackend.h"
 
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <exception>
 #include <thread>
+#include <vector>
 
 #include "shiro/render/EnvironmentMap.h"
 #include "shiro_gpu.h"
@@ -194,6 +197,35 @@ ShiroAovs FrameAovs(FrameBuffer& fb) {
 
 bool Cancelled(const std::atomic<bool>* c) { return c && c->load(std::memory_order_relaxed); }
 
+// Copies the staged planes (beauty 4, albedo 3, normal 3, depth 1 floats per
+// pixel, back to back) into the frame's own, on several host threads for a
+// large frame.
+void CopyOut(const float* stage, FrameBuffer& fb, size_t px) {
+    const ShiroAovs dst = FrameAovs(fb);
+    struct Plane {
+        const float* src;
+        float* dst;
+        size_t n;
+    };
+    const Plane planes[4] = {{stage, dst.beauty, 4 * px}, {stage + 4 * px, dst.albedo, 3 * px},
+                             {stage + 7 * px, dst.normal, 3 * px}, {stage + 10 * px, dst.depth, px}};
+    const unsigned threads = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+    auto part = [&](unsigned t, unsigned of) {
+        for (const Plane& p : planes) {
+            const size_t a = p.n * t / of, b = p.n * (t + 1) / of;
+            if (b > a) std::memcpy(p.dst + a, p.src + a, (b - a) * sizeof(float));
+        }
+    };
+    if (threads == 1 || 11 * px < (size_t{1} << 20)) {
+        part(0, 1);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < threads; ++t) pool.emplace_back(part, t, threads);
+    part(0, threads);
+    for (std::thread& th : pool) th.join();
+}
+
 }  // namespace
 
 GpuBackend::GpuBackend(int device) : device_(device) {}
@@ -201,6 +233,18 @@ GpuBackend::GpuBackend(int device) : device_(device) {}
 GpuBackend::~GpuBackend() {
     if (accum_) shiro_gpu_accum_destroy(accum_);
     if (ctx_) shiro_gpu_destroy(ctx_);
+    shiro_gpu_host_free(staging_);
+}
+
+float* GpuBackend::Staging(size_t bytes) const {
+    if (stagingBytes_ < bytes) {
+        shiro_gpu_host_free(staging_);
+        staging_ = nullptr;
+        stagingBytes_ = 0;
+        if (shiro_gpu_host_alloc(bytes, &staging_) != SHIRO_OK || !staging_) return nullptr;
+        stagingBytes_ = bytes;
+    }
+    return static_cast<float*>(staging_);
 }
 
 BackendStatus GpuBackend::GetStatus() const {
@@ -253,13 +297,44 @@ bool GpuBackend::EnsureRuntime(const render::Scene& scene) const {
 
 render::FrameBuffer GpuBackend::RenderSampleBatch(const RenderRequest& request) const {
     render::FrameBuffer frame;
-    frame.Resize(request.settings.width, request.settings.height);
-    frame.Clear();
-    if (request.sampleCount == 0 || Cancelled(request.cancel)) return frame;
+    const uint32_t w = request.settings.width, h = request.settings.height;
+    if (request.sampleCount == 0 || Cancelled(request.cancel)) {
+        frame.Resize(w, h);
+        frame.Clear();
+        return frame;
+    }
     std::scoped_lock lock(mutex_);
-    if (!EnsureRuntime(request.scene)) return frame;
+    // The returned frame is sized and cleared (a 1080p one is 91 MB of fresh
+    // pages) on a helper thread while the device renders into page-locked
+    // staging, which the render writes in place; the planes are then copied
+    // over on several threads.
+    std::exception_ptr failure;  // an allocation failure reaches the caller as before
+    std::thread prepare([&frame, &failure, w, h] {
+        try {
+            frame.Resize(w, h);
+            frame.Clear();
+        } catch (...) {
+            failure = std::current_exception();
+        }
+    });
+    auto prepared = [&] {
+        if (prepare.joinable()) prepare.join();
+        if (failure) std::rethrow_exception(failure);
+    };
+    if (!EnsureRuntime(request.scene)) {
+        prepared();
+        return frame;
+    }
     const ShiroRenderDesc desc = ToRequest(request);
-    ShiroAovs aovs = FrameAovs(frame);
+    const size_t px = static_cast<size_t>(w) * h;
+    float* stage = Staging(11 * px * sizeof(float));
+    ShiroAovs aovs;
+    if (stage) {
+        aovs = ShiroAovs{stage, stage + 4 * px, stage + 7 * px, stage + 10 * px, 0, 0};
+    } else {  // no page-locked memory: render into the frame's own planes
+        prepared();
+        aovs = FrameAovs(frame);
+    }
     // the wavefront form: the faster one, with frames bit-identical to the
     // one-thread-per-path form's
     int rc;
@@ -268,13 +343,18 @@ render::FrameBuffer GpuBackend::RenderSampleBatch(const RenderRequest& request) 
         rc = shiro_gpu_render_batch(ctx_, &desc, 1, cancel.Flag(), &aovs);
     }
     lastStatus_ = rc;
+    prepared();
     if (rc != SHIRO_OK) {
         if (rc != SHIRO_ERR_CANCELLED)
             std::fprintf(stderr, "[shiro gb300] render failed (%d): %s\n", rc, shiro_gpu_last_error(ctx_));
         frame.Clear();
         return frame;
     }
-    if (Cancelled(request.cancel)) frame.Clear();  // RenderParam.cpp:791-798 discards it anyway
+    if (Cancelled(request.cancel)) {  // RenderParam.cpp:791-798 discards it anyway
+        frame.Clear();
+        return frame;
+    }
+    if (stage) CopyOut(stage, frame, px);
     return frame;
 }
 

@@ -59,6 +59,9 @@ public:
 
 private:
     bool EnsureRuntime(const render::Scene& scene) const;
+    // The page-locked staging planes of RenderSampleBatch (grown on demand;
+    // NULL when page-locked memory cannot be had).
+    float* Staging(size_t bytes) const;
 
     int device_;
     mutable std::mutex mutex_;
@@ -70,6 +73,8 @@ private:
     mutable uint64_t cachedSignature_ = 0;
     mutable int lastStatus_ = 0;
     mutable uint64_t uploads_ = 0;
+    mutable void* staging_ = nullptr;
+    mutable size_t stagingBytes_ = 0;
 };
 
 }  // namespace shiro::backend::gb300

@@ -498,6 +498,23 @@ uint64_t scene_signature(const ShiroSceneDesc& sd) {
 
 extern "C" {
 
+int shiro_gpu_host_alloc(size_t bytes, void** out) {
+    if (!out) return SHIRO_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (bytes == 0) return SHIRO_OK;
+    const cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return SHIRO_ERR_OUT_OF_MEMORY;
+    }
+    return SHIRO_OK;
+}
+
+void shiro_gpu_host_free(void* ptr) {
+    if (ptr) cudaFreeHost(ptr);
+}
+
 int shiro_gpu_scene_signature(const ShiroSceneDesc* scene, uint64_t* out) {
     if (!scene || !out) return SHIRO_ERR_INVALID_ARGUMENT;
     *out = scene_signature(*scene);

@@ -1392,12 +1392,14 @@ WavefrontState* wf_state(ContextImpl* ctx) {
     if (!ctx->wavefront) {
         ctx->wavefront = new WavefrontState();
         ShiroWavefrontConfig& c = ctx->wavefront->cfg;
-        c.paths_in_flight = 1u << 23;
-        c.extend_block = 128;
+        // the values the autotuner picks for a 1080p 64-spp frame: pools of
+        // 32 M paths (a pool is never larger than its request needs)
+        c.paths_in_flight = 1u << 25;
+        c.extend_block = 256;
         c.shade_block = 128;
         c.shadow_block = 128;
         c.use_graph = 1;
-        c.shade_regs = 128;
+        c.shade_regs = 96;
         c.extend_steps = 4;
         c.refill_idle = 8;
         c.concurrent_waves = 2;

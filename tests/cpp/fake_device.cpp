@@ -102,6 +102,14 @@ int shiro_gpu_scene_signature(const ShiroSceneDesc* s, uint64_t* out) {
     return SHIRO_OK;
 }
 
+int shiro_gpu_host_alloc(size_t bytes, void** out) {
+    if (!out) return SHIRO_ERR_INVALID_ARGUMENT;
+    *out = bytes ? std::malloc(bytes) : nullptr;
+    return bytes && !*out ? SHIRO_ERR_OUT_OF_MEMORY : SHIRO_OK;
+}
+
+void shiro_gpu_host_free(void* ptr) { std::free(ptr); }
+
 int shiro_gpu_upload_scene(ShiroGpuContext* ctx, const ShiroSceneDesc* scene) {
     if (!ctx || !scene) return SHIRO_ERR_INVALID_ARGUMENT;
     if (ctx->scene) oracle_scene_destroy(ctx->scene);
