@@ -111,10 +111,12 @@ def test_cancel_set_mid_frame_through_adapter(backend_lib, gpu):
     from shiro_gb300 import scenes
     from shiro_gb300.abi import FrameBuffer, MarshalledScene, render_desc
 
-    # 1920 x 1080 x 128 spp on the sphere scene: dozens of waves of 8 M paths
-    w = scenes.sphere_workload(1920, 1080, 128, 8, env_width=128, env_height=64)
+    # 1920 x 1080 x 256 spp on the sphere scene: 16 waves of the default 32 M
+    # paths; a cancel stops the render after the waves already queued (waves in
+    # flight + 1)
+    w = scenes.sphere_workload(1920, 1080, 256, 8, env_width=128, env_height=64)
     ms = MarshalledScene(w.scene)
-    req = render_desc(w.camera, w.settings, 0, 128)
+    req = render_desc(w.camera, w.settings, 0, 256)
     fb = FrameBuffer(1920, 1080)
     aov = fb.aovs()
     status, elapsed = C.c_int(0), C.c_double(0.0)

@@ -261,6 +261,9 @@ def test_cancel_flag_set_by_another_thread_mid_frame(form):
     w = scenes.sphere_workload(1920, 1080, 128, 8, env_width=128, env_height=64)
     with GpuBackend(0) as gpu:
         gpu.upload_scene(w.scene)
+        # waves of 8 M paths: dozens per frame (a cancel takes effect after the
+        # waves already queued, waves in flight + 1, so their size bounds it)
+        gpu.set_wavefront_config(paths_in_flight=1 << 23)
         render = (lambda fb, cancel: gpu.render_batch(w.scene, [(w.camera, w.settings)], cancel=cancel, outs_fb=[fb])) \
             if form == "wavefront" else (lambda fb, cancel: gpu.render(w.scene, w.camera, w.settings, cancel=cancel,
                                                                         out=fb))
