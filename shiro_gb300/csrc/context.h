@@ -26,8 +26,9 @@ struct EnvHost {
 };
 
 // Default cluster size of the binned-SAH top (shiro_gpu_set_bvh_build):
-// measured on the 1.31 M-triangle field frame, 8 gave the fewest node visits
-// (binary 69.8 -> 65.1, wide 26.2 -> 25.5 per path; 16 and up fewer gains).
+// measured on the 1.31 M-triangle field frame, clusters of 2 gave the fewest
+// node visits (wide 26.2 -> 25.0 per path against the Morton hierarchy; 8:
+// 25.5, 16 and up fewer gains), at a longer build.
 constexpr uint32_t kDefaultSahCluster = 2;
 
 struct WavefrontState;
@@ -43,7 +44,10 @@ struct ContextImpl {
     // scene
     bool hasScene = false;
     DevScene scene{};
-    std::vector<DeviceBlock> sceneBlocks;
+    std::vector<DeviceBlock> sceneBlocks;  // geometry blocks first, then shading ones
+    size_t geomBlocks = 0;                 // sceneBlocks[0, geomBlocks): BVHs, triangles, shading records
+    bool geomValid = false;                // geomSignature describes the resident geometry
+    uint64_t geomSignature = 0;
     std::vector<DevEnv> envDev;        // host copy of the device env table
     std::vector<EnvHost> envHost;      // host copy of the textures (for parameter updates)
     std::vector<int32_t> domeEnv;      // dome -> env index
@@ -85,6 +89,9 @@ struct ContextImpl {
 
     ~ContextImpl();
     void freeScene();
+    // frees what an upload derives from materials, lights and environments,
+    // keeping the geometry (BVHs, triangles, per-triangle shading records)
+    void freeShading();
     size_t deviceBytes() const;
 };
 

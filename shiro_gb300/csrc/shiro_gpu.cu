@@ -124,6 +124,8 @@ ContextImpl::~ContextImpl() {
 void ContextImpl::freeScene() {
     for (auto& b : sceneBlocks) free_block(&b);
     sceneBlocks.clear();
+    geomBlocks = 0;
+    geomValid = false;
     envDev.clear();
     envHost.clear();
     domeEnv.clear();
@@ -131,6 +133,32 @@ void ContextImpl::freeScene() {
     hasScene = false;
     scene = DevScene{};
     nodes8 = tris8 = tris2 = nullptr;
+}
+
+void ContextImpl::freeShading() {
+    for (size_t i = geomBlocks; i < sceneBlocks.size(); ++i) free_block(&sceneBlocks[i]);
+    sceneBlocks.resize(std::min(geomBlocks, sceneBlocks.size()));
+    envDev.clear();
+    envHost.clear();
+    domeEnv.clear();
+    materialsHost.clear();
+    materialCount = 0;
+    extendedMaterials = false;
+    hasScene = false;
+    DevScene& s = scene;
+    s.materials = nullptr;
+    s.bsdfRecs = nullptr;
+    s.emissive = nullptr;
+    s.emissiveCdf = nullptr;
+    s.emissiveOf = nullptr;
+    s.emissiveCount = 0;
+    s.emissiveSum = 0.0f;
+    s.distant = nullptr;
+    s.distantCount = 0;
+    s.domes = nullptr;
+    s.domeCount = 0;
+    s.envs = nullptr;
+    s.extended = 0;
 }
 
 size_t ContextImpl::deviceBytes() const {
@@ -427,6 +455,33 @@ void put(std::vector<unsigned char>& b, const T& v) {
     b.insert(b.end(), p, p + sizeof(T));
 }
 
+uint64_t hash_spans(std::vector<HashSpan> spans);
+
+// The part of the snapshot the geometry depends on: the meshes' arrays and
+// counts, each mesh's material index and the material count (they key the
+// per-triangle shading records), and the cluster size of the BVH build.
+uint64_t geometry_signature(const ShiroSceneDesc& sd, uint32_t sahCluster) {
+    std::vector<unsigned char> head;
+    put(head, sahCluster);
+    put(head, sd.material_count);
+    put(head, sd.mesh_count);
+    std::vector<HashSpan> spans;
+    for (uint32_t i = 0; i < sd.mesh_count && sd.meshes; ++i) {
+        const ShiroMeshDesc& m = sd.meshes[i];
+        const uint32_t vc = m.positions ? m.vertex_count : 0u, nc = m.normals ? m.normal_count : 0u,
+                       ic = m.indices ? m.index_count : 0u;
+        put(head, vc);
+        put(head, nc);
+        put(head, ic);
+        put(head, m.material_index);
+        spans.push_back({reinterpret_cast<const unsigned char*>(m.positions), 12ull * vc});
+        spans.push_back({reinterpret_cast<const unsigned char*>(m.normals), 12ull * nc});
+        spans.push_back({reinterpret_cast<const unsigned char*>(m.indices), 4ull * ic});
+    }
+    spans.insert(spans.begin(), HashSpan{head.data(), head.size()});
+    return hash_spans(std::move(spans));
+}
+
 uint64_t scene_signature(const ShiroSceneDesc& sd) {
     // every scalar field first (counts, materials, lights, dome frames, sizes),
     // then the large arrays
@@ -466,6 +521,12 @@ uint64_t scene_signature(const ShiroSceneDesc& sd) {
     head.insert(head.end(), reinterpret_cast<const unsigned char*>(sd.environment_bottom),
                 reinterpret_cast<const unsigned char*>(sd.environment_bottom + 3));
     spans.insert(spans.begin(), HashSpan{head.data(), head.size()});
+    return hash_spans(std::move(spans));
+}
+
+// Hashes the spans in pieces of 4 MB, on several host threads for large
+// inputs; the value does not depend on the thread count.
+uint64_t hash_spans(std::vector<HashSpan> spans) {
     constexpr size_t kPiece = 4u << 20;
     std::vector<HashSpan> pieces;
     size_t total = 0;
@@ -492,6 +553,130 @@ uint64_t scene_signature(const ShiroSceneDesc& sd) {
     uint64_t h = hash_round(0x27D4EB2F165667C5ull, total);
     for (uint64_t d : dig) h = hash_round(h, d);
     return h;
+}
+
+// What an upload derives from the materials, lights and environments
+// (everything but the geometry): emissive-triangle tables, materials and
+// their BSDF records, distant lights, domes with their importance tables.
+// The geometry (ctx->scene's BVHs, triangles, per-triangle records) is
+// resident.
+int upload_shading(ContextImpl* ctx, const ShiroSceneDesc* sd) {
+    DevScene& s = ctx->scene;
+    int rc;
+    ctx->materialsHost.assign(sd->materials, sd->materials + sd->material_count);
+    ctx->materialsHost.push_back(default_material());
+    ctx->materialCount = sd->material_count;
+    size_t ttotal = 0;  // global triangle ids: meshes in order, index_count / 3 each
+    for (uint32_t i = 0; i < sd->mesh_count; ++i) ttotal += sd->meshes[i].index_count / 3u;
+    // --- emissive triangles (BuildAccelerationScene, CpuPathTracer.cpp:482-522;
+    // TriangleArea :198-222), float running sums in mesh / primitive order ----
+    std::vector<float4> emissive;
+    std::vector<float> emissiveCdf;
+    std::vector<int32_t> emissiveOf(ttotal, -1);
+    float emissiveSum = 0.0f;
+    {
+        const ShiroMaterialDesc dflt = default_material();
+        uint32_t g = 0;
+        for (uint32_t i = 0; i < sd->mesh_count; ++i) {
+            const ShiroMeshDesc& m = sd->meshes[i];
+            const uint32_t prims = m.index_count / 3u;
+            const ShiroMaterialDesc& mat = m.material_index < sd->material_count ? sd->materials[m.material_index] : dflt;
+            const float le[3] = {std::max(mat.emission_color[0] * mat.emission_strength, 0.0f),
+                                 std::max(mat.emission_color[1] * mat.emission_strength, 0.0f),
+                                 std::max(mat.emission_color[2] * mat.emission_strength, 0.0f)};
+            const float w = std::max(0.2126f * le[0] + 0.7152f * le[1] + 0.0722f * le[2], 0.0f);
+            if (m.index_count < 3 || m.index_count % 3 != 0 || w <= 0.0f) {
+                g += prims;
+                continue;
+            }
+            for (uint32_t t = 0; t < prims; ++t, ++g) {
+                const float* p0 = m.positions + 3 * static_cast<size_t>(m.indices[3 * t]);
+                const float* p1 = m.positions + 3 * static_cast<size_t>(m.indices[3 * t + 1]);
+                const float* p2 = m.positions + 3 * static_cast<size_t>(m.indices[3 * t + 2]);
+                const float a[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+                const float b[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+                const float av[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+                const float dbl = std::sqrt(av[0] * av[0] + av[1] * av[1] + av[2] * av[2]);
+                if (dbl <= 1.0e-8f) continue;
+                const float area = dbl * 0.5f;
+                const float sel = area * w;
+                emissiveSum += sel;
+                emissiveOf[g] = static_cast<int32_t>(emissiveCdf.size());
+                float gbits;
+                std::memcpy(&gbits, &g, 4);
+                emissive.push_back(make_float4(area, sel, emissiveSum, gbits));
+                emissive.push_back(make_float4(le[0], le[1], le[2], 0.0f));
+                emissive.push_back(make_float4(av[0] / dbl, av[1] / dbl, av[2] / dbl, 0.0f));
+                emissiveCdf.push_back(emissiveSum);
+            }
+        }
+    }
+
+    s.emissiveCount = static_cast<uint32_t>(emissiveCdf.size());
+    s.emissiveSum = emissiveSum;
+    if (s.emissiveCount) {
+        if ((rc = upload(ctx, emissive, &s.emissive, "emissive triangles")) != SHIRO_OK) return rc;
+        if ((rc = upload(ctx, emissiveCdf, &s.emissiveCdf, "emissive weights")) != SHIRO_OK) return rc;
+        if ((rc = upload(ctx, emissiveOf, &s.emissiveOf, "emissive index")) != SHIRO_OK) return rc;
+    }
+    ctx->extendedMaterials = false;
+    for (uint32_t i = 0; i < sd->material_count; ++i) {
+        const ShiroMaterialDesc& m = sd->materials[i];
+        if (has_transmission(m) || hclamp(m.opacity, 0.0f, 1.0f) < 0.999f || m.emission_strength > 0.0f)
+            ctx->extendedMaterials = true;
+    }
+    s.extended = ctx->extendedMaterials ? 1u : 0u;
+    if ((rc = upload(ctx, ctx->materialsHost, &s.materials, "materials")) != SHIRO_OK) return rc;
+    s.bsdfRecs = nullptr;
+    if ((rc = build_bsdf_recs(ctx)) != SHIRO_OK) return rc;
+    std::vector<DevDistant> distant(sd->distant_light_count);
+    for (uint32_t i = 0; i < sd->distant_light_count; ++i)
+        distant[i] = DevDistant{ld3(sd->distant_lights[i].direction), ld3(sd->distant_lights[i].radiance)};
+    if ((rc = upload(ctx, distant, &s.distant, "distant lights")) != SHIRO_OK) return rc;
+    s.distantCount = sd->distant_light_count;
+
+    std::vector<DevDome> domes(sd->dome_light_count);
+    for (uint32_t i = 0; i < sd->dome_light_count; ++i) {
+        const ShiroDomeLightDesc& d = sd->dome_lights[i];
+        domes[i].radiance = ld3(d.radiance);
+        domes[i].right = ld3(d.right);
+        domes[i].up = ld3(d.up);
+        domes[i].forward = ld3(d.forward);
+        domes[i].env = -1;
+        if (d.env_pixels && d.env_width && d.env_height) {
+            EnvHost e;
+            e.w = d.env_width;
+            e.h = d.env_height;
+            e.latlong = d.layout != SHIRO_ENV_LAYOUT_ANGULAR;
+            e.rgb.assign(d.env_pixels, d.env_pixels + 3 * static_cast<size_t>(e.w) * e.h);
+            domes[i].env = static_cast<int32_t>(ctx->envHost.size());
+            ctx->envHost.push_back(std::move(e));
+        }
+        ctx->domeEnv.push_back(domes[i].env);
+    }
+    ctx->envDev.assign(ctx->envHost.size(), DevEnv{});
+    if ((rc = upload_envs(ctx)) != SHIRO_OK) return rc;
+    if ((rc = upload(ctx, ctx->envDev, &s.envs, "env table")) != SHIRO_OK) return rc;
+    if ((rc = upload(ctx, domes, &s.domes, "dome lights")) != SHIRO_OK) return rc;
+    s.domeCount = sd->dome_light_count;
+    s.envTop = ld3(sd->environment_top);
+    s.envBottom = ld3(sd->environment_bottom);
+    return SHIRO_OK;
+}
+
+int finish_upload(ContextImpl* ctx) {
+    DevScene& s = ctx->scene;
+    s.error = ctx->errorWord;
+    const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "scene upload");
+    ctx->hasScene = true;
+    ctx->stats = ShiroRenderStats{};
+    ctx->stats.bvh_nodes = s.nodes8 ? ctx->node8Count : s.nodeCount;
+    ctx->stats.triangles = s.triCount;
+    ctx->stats.bvh_depth = s.nodes8 ? ctx->bvh8Depth : ctx->bvhDepth;
+    ctx->stats.bvh_max_leaf = ctx->bvhMaxLeaf;
+    ctx->stats.device_bytes = ctx->deviceBytes();
+    return SHIRO_OK;
 }
 
 }  // namespace
@@ -640,6 +825,18 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     if (sd->mesh_count && !sd->meshes) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "null mesh array");
     if (sd->material_count && !sd->materials) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "null material array");
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    const uint64_t geom = geometry_signature(*sd, ctx->sahClusterSize);
+    if (ctx->hasScene && ctx->geomValid && ctx->geomSignature == geom) {
+        // the same geometry (a light, a material or an environment edited):
+        // the BVHs, triangles and per-triangle records stay on the device
+        ctx->freeShading();
+        const int rc = upload_shading(ctx, sd);
+        if (rc != SHIRO_OK) {
+            ctx->freeScene();
+            return rc;
+        }
+        return finish_upload(ctx);
+    }
     ctx->freeScene();
 
     // --- flatten ------------------------------------------------------------
@@ -718,50 +915,6 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
         }
     }
     if (ttotal == 0) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene has no triangles");
-
-    // --- emissive triangles (BuildAccelerationScene, CpuPathTracer.cpp:482-522;
-    // TriangleArea :198-222), float running sums in mesh / primitive order ----
-    std::vector<float4> emissive;
-    std::vector<float> emissiveCdf;
-    std::vector<int32_t> emissiveOf(ttotal, -1);
-    float emissiveSum = 0.0f;
-    {
-        const ShiroMaterialDesc dflt = default_material();
-        uint32_t g = 0;
-        for (uint32_t i = 0; i < sd->mesh_count; ++i) {
-            const ShiroMeshDesc& m = sd->meshes[i];
-            const uint32_t prims = m.index_count / 3u;
-            const ShiroMaterialDesc& mat = m.material_index < sd->material_count ? sd->materials[m.material_index] : dflt;
-            const float le[3] = {std::max(mat.emission_color[0] * mat.emission_strength, 0.0f),
-                                 std::max(mat.emission_color[1] * mat.emission_strength, 0.0f),
-                                 std::max(mat.emission_color[2] * mat.emission_strength, 0.0f)};
-            const float w = std::max(0.2126f * le[0] + 0.7152f * le[1] + 0.0722f * le[2], 0.0f);
-            if (m.index_count < 3 || m.index_count % 3 != 0 || w <= 0.0f) {
-                g += prims;
-                continue;
-            }
-            for (uint32_t t = 0; t < prims; ++t, ++g) {
-                const float* p0 = m.positions + 3 * static_cast<size_t>(m.indices[3 * t]);
-                const float* p1 = m.positions + 3 * static_cast<size_t>(m.indices[3 * t + 1]);
-                const float* p2 = m.positions + 3 * static_cast<size_t>(m.indices[3 * t + 2]);
-                const float a[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
-                const float b[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
-                const float av[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
-                const float dbl = std::sqrt(av[0] * av[0] + av[1] * av[1] + av[2] * av[2]);
-                if (dbl <= 1.0e-8f) continue;
-                const float area = dbl * 0.5f;
-                const float sel = area * w;
-                emissiveSum += sel;
-                emissiveOf[g] = static_cast<int32_t>(emissiveCdf.size());
-                float gbits;
-                std::memcpy(&gbits, &g, 4);
-                emissive.push_back(make_float4(area, sel, emissiveSum, gbits));
-                emissive.push_back(make_float4(le[0], le[1], le[2], 0.0f));
-                emissive.push_back(make_float4(av[0] / dbl, av[1] / dbl, av[2] / dbl, 0.0f));
-                emissiveCdf.push_back(emissiveSum);
-            }
-        }
-    }
 
     // --- large triangles + inflated boxes -----------------------------------
     auto area = [](const float* lo, const float* hi) {
@@ -886,78 +1039,20 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     s.nodes8 = ctx->bvhWidth == 8 ? ctx->nodes8 : nullptr;
     s.tris = s.nodes8 ? ctx->tris8 : ctx->tris2;
 
-    // --- shading data ----------------------------------------------------------
-    ctx->materialsHost.assign(sd->materials, sd->materials + sd->material_count);
-    ctx->materialsHost.push_back(default_material());
-    ctx->materialCount = sd->material_count;
+    // --- per-triangle data -----------------------------------------------------
     if ((rc = upload(ctx, triVerts, &s.triVerts, "triangle vertices")) != SHIRO_OK) return rc;
     if ((rc = upload(ctx, positions, &s.positions, "positions")) != SHIRO_OK) return rc;
     if ((rc = upload(ctx, shade, &s.shade, "triangle shading records")) != SHIRO_OK) return rc;
     k_shade_normals<<<(bout.triCount + 255) / 256, 256, 0, ctx->stream>>>(ctx->tris2, bout.triCount,
                                                                          const_cast<float4*>(s.shade));
     if (const cudaError_t e = cudaGetLastError(); e != cudaSuccess) return cuda_fail(ctx, e, "shading records");
-    s.emissiveCount = static_cast<uint32_t>(emissiveCdf.size());
-    s.emissiveSum = emissiveSum;
-    if (s.emissiveCount) {
-        if ((rc = upload(ctx, emissive, &s.emissive, "emissive triangles")) != SHIRO_OK) return rc;
-        if ((rc = upload(ctx, emissiveCdf, &s.emissiveCdf, "emissive weights")) != SHIRO_OK) return rc;
-        if ((rc = upload(ctx, emissiveOf, &s.emissiveOf, "emissive index")) != SHIRO_OK) return rc;
-    }
-    ctx->extendedMaterials = false;
-    for (uint32_t i = 0; i < sd->material_count; ++i) {
-        const ShiroMaterialDesc& m = sd->materials[i];
-        if (has_transmission(m) || hclamp(m.opacity, 0.0f, 1.0f) < 0.999f || m.emission_strength > 0.0f)
-            ctx->extendedMaterials = true;
-    }
-    s.extended = ctx->extendedMaterials ? 1u : 0u;
-    if ((rc = upload(ctx, ctx->materialsHost, &s.materials, "materials")) != SHIRO_OK) return rc;
-    s.bsdfRecs = nullptr;
-    if ((rc = build_bsdf_recs(ctx)) != SHIRO_OK) return rc;
-    std::vector<DevDistant> distant(sd->distant_light_count);
-    for (uint32_t i = 0; i < sd->distant_light_count; ++i)
-        distant[i] = DevDistant{ld3(sd->distant_lights[i].direction), ld3(sd->distant_lights[i].radiance)};
-    if ((rc = upload(ctx, distant, &s.distant, "distant lights")) != SHIRO_OK) return rc;
-    s.distantCount = sd->distant_light_count;
-
-    std::vector<DevDome> domes(sd->dome_light_count);
-    for (uint32_t i = 0; i < sd->dome_light_count; ++i) {
-        const ShiroDomeLightDesc& d = sd->dome_lights[i];
-        domes[i].radiance = ld3(d.radiance);
-        domes[i].right = ld3(d.right);
-        domes[i].up = ld3(d.up);
-        domes[i].forward = ld3(d.forward);
-        domes[i].env = -1;
-        if (d.env_pixels && d.env_width && d.env_height) {
-            EnvHost e;
-            e.w = d.env_width;
-            e.h = d.env_height;
-            e.latlong = d.layout != SHIRO_ENV_LAYOUT_ANGULAR;
-            e.rgb.assign(d.env_pixels, d.env_pixels + 3 * static_cast<size_t>(e.w) * e.h);
-            domes[i].env = static_cast<int32_t>(ctx->envHost.size());
-            ctx->envHost.push_back(std::move(e));
-        }
-        ctx->domeEnv.push_back(domes[i].env);
-    }
-    ctx->envDev.assign(ctx->envHost.size(), DevEnv{});
-    if ((rc = upload_envs(ctx)) != SHIRO_OK) return rc;
-    if ((rc = upload(ctx, ctx->envDev, &s.envs, "env table")) != SHIRO_OK) return rc;
-    if ((rc = upload(ctx, domes, &s.domes, "dome lights")) != SHIRO_OK) return rc;
-    s.domeCount = sd->dome_light_count;
-    s.envTop = ld3(sd->environment_top);
-    s.envBottom = ld3(sd->environment_bottom);
+    ctx->geomBlocks = ctx->sceneBlocks.size();  // what follows derives from materials, lights, environments
+    if ((rc = upload_shading(ctx, sd)) != SHIRO_OK) return rc;
     s.boundsLo = V3{slo[0], slo[1], slo[2]};
     s.boundsHi = V3{shi[0], shi[1], shi[2]};
-    s.error = ctx->errorWord;
-    const cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "scene upload");
-    ctx->hasScene = true;
-    ctx->stats = ShiroRenderStats{};
-    ctx->stats.bvh_nodes = s.nodes8 ? ctx->node8Count : s.nodeCount;
-    ctx->stats.triangles = s.triCount;
-    ctx->stats.bvh_depth = s.nodes8 ? ctx->bvh8Depth : ctx->bvhDepth;
-    ctx->stats.bvh_max_leaf = ctx->bvhMaxLeaf;
-    ctx->stats.device_bytes = ctx->deviceBytes();
-    return SHIRO_OK;
+    ctx->geomSignature = geom;
+    ctx->geomValid = true;
+    return finish_upload(ctx);
 }
 
 int shiro_gpu_render(ShiroGpuContext* handle, const ShiroRenderDesc* req, const volatile int* cancel, ShiroAovs* out) {
