@@ -316,7 +316,11 @@ void shiro_hdri_free(float* pixels);
 /* Uploads a scene snapshot: flattens meshes, builds the device BVH, the
  * material table and the dome-light importance tables (CDF and alias).
  * Counterpart of OptixBackend::UploadSceneData (OptixBackend.cpp:751-1026) and
- * CpuPathTracer::BuildAccelerationScene (CpuPathTracer.cpp:477-598). */
+ * CpuPathTracer::BuildAccelerationScene (CpuPathTracer.cpp:477-598).  When the
+ * geometry equals the resident scene's (mesh positions, normals, indices and
+ * material indices, the material count, the BVH build setting), the BVHs and
+ * per-triangle records are kept and only what derives from materials, lights
+ * and environments is replaced. */
 int shiro_gpu_upload_scene(ShiroGpuContext* ctx, const ShiroSceneDesc* scene);
 
 /* FrameBuffer RenderSampleBatch(const RenderRequest&)
