@@ -297,6 +297,53 @@ struct SahResult {
 
 __device__ __forceinline__ float item_centroid(const SahItem& it, int a) { return 0.5f * (it.lo[a] + it.hi[a]); }
 
+// The split plane of least SAH cost (area(left) * weight(left) + area(right)
+// * weight(right)) from a node's bins in shared memory: choice[0] = axis (-1:
+// no usable plane), choice[1] = plane.  Every thread of the block calls it;
+// the first 3 * (kSahBins - 1) threads cost one plane each.
+__device__ __forceinline__ void sah_choose(const unsigned int (&binLo)[3][kSahBins][3],
+                                           const unsigned int (&binHi)[3][kSahBins][3],
+                                           const unsigned int (&binW)[3][kSahBins], const unsigned int (&binN)[3][kSahBins],
+                                           const float (&cext)[3], float* bestCost, int* choice) {
+    const int tid = threadIdx.x;
+    if (tid < 3 * (kSahBins - 1)) {
+        const int a = tid / (kSahBins - 1), sp = tid % (kSahBins - 1);
+        float l[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, h[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        float r[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, g[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        unsigned int nl = 0, nr = 0, wl = 0, wr = 0;
+        for (int b = 0; b < kSahBins; ++b) {
+            if (binN[a][b] == 0u) continue;
+            float* bl = b <= sp ? l : r;
+            float* bh = b <= sp ? h : g;
+            for (int k = 0; k < 3; ++k) {
+                bl[k] = fminf(bl[k], ord2f(binLo[a][b][k]));
+                bh[k] = fmaxf(bh[k], ord2f(binHi[a][b][k]));
+            }
+            if (b <= sp) { wl += binW[a][b]; nl += binN[a][b]; } else { wr += binW[a][b]; nr += binN[a][b]; }
+        }
+        float cost = FLT_MAX;
+        if (cext[a] > 0.0f && nl > 0u && nr > 0u) {
+            const float al = 2.0f * ((h[0] - l[0]) * (h[1] - l[1]) + (h[1] - l[1]) * (h[2] - l[2]) + (h[2] - l[2]) * (h[0] - l[0]));
+            const float ar = 2.0f * ((g[0] - r[0]) * (g[1] - r[1]) + (g[1] - r[1]) * (g[2] - r[2]) + (g[2] - r[2]) * (g[0] - r[0]));
+            cost = al * static_cast<float>(wl) + ar * static_cast<float>(wr);
+        }
+        bestCost[tid] = cost;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int best = -1;
+        float bc = FLT_MAX;
+        for (int k = 0; k < 3 * (kSahBins - 1); ++k)
+            if (bestCost[k] < bc) {  // first of equal costs: lowest axis, lowest plane
+                bc = bestCost[k];
+                best = k;
+            }
+        choice[0] = best < 0 ? -1 : best / (kSahBins - 1);
+        choice[1] = best < 0 ? 0 : best % (kSahBins - 1);
+    }
+    __syncthreads();
+}
+
 // Block-wide exclusive scan of one value per thread (kSahBlock threads).
 __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* warpSums, uint32_t* total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -324,7 +371,8 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* warpSums, u
 
 __global__ void __launch_bounds__(kSahBlock) k_sah_split(const SahTask* __restrict__ tasks, const SahItem* __restrict__ items,
                                                         const uint32_t* __restrict__ permIn, uint32_t* __restrict__ permOut,
-                                                        SahResult* __restrict__ results, uint32_t* __restrict__ newTasks) {
+                                                        SahResult* __restrict__ results, uint32_t* __restrict__ newTasks,
+                                                        uint32_t bigMin) {
     __shared__ unsigned int cbo[6];
     __shared__ unsigned int binLo[3][kSahBins][3], binHi[3][kSahBins][3];
     __shared__ unsigned int binW[3][kSahBins], binN[3][kSahBins];
@@ -333,6 +381,7 @@ __global__ void __launch_bounds__(kSahBlock) k_sah_split(const SahTask* __restri
     __shared__ uint32_t warpSums[kSahBlock / 32];
     const SahTask t = tasks[blockIdx.x];
     const uint32_t n = t.end - t.begin;
+    if (bigMin && n >= bigMin) return;  // split by the multi-block kernels below
     const int tid = threadIdx.x;
     if (tid < 6) cbo[tid] = tid < 3 ? 0xffffffffu : 0u;
     for (int e = tid; e < 3 * kSahBins * 3; e += kSahBlock) {
@@ -388,43 +437,7 @@ __global__ void __launch_bounds__(kSahBlock) k_sah_split(const SahTask* __restri
         }
     }
     __syncthreads();
-    // SAH cost of every split plane: area(left) * weight(left) + area(right) * weight(right)
-    if (tid < 3 * (kSahBins - 1)) {
-        const int a = tid / (kSahBins - 1), sp = tid % (kSahBins - 1);
-        float l[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, h[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-        float r[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, g[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-        unsigned int nl = 0, nr = 0, wl = 0, wr = 0;
-        for (int b = 0; b < kSahBins; ++b) {
-            if (binN[a][b] == 0u) continue;
-            float* bl = b <= sp ? l : r;
-            float* bh = b <= sp ? h : g;
-            for (int k = 0; k < 3; ++k) {
-                bl[k] = fminf(bl[k], ord2f(binLo[a][b][k]));
-                bh[k] = fmaxf(bh[k], ord2f(binHi[a][b][k]));
-            }
-            if (b <= sp) { wl += binW[a][b]; nl += binN[a][b]; } else { wr += binW[a][b]; nr += binN[a][b]; }
-        }
-        float cost = FLT_MAX;
-        if (cext[a] > 0.0f && nl > 0u && nr > 0u) {
-            const float al = 2.0f * ((h[0] - l[0]) * (h[1] - l[1]) + (h[1] - l[1]) * (h[2] - l[2]) + (h[2] - l[2]) * (h[0] - l[0]));
-            const float ar = 2.0f * ((g[0] - r[0]) * (g[1] - r[1]) + (g[1] - r[1]) * (g[2] - r[2]) + (g[2] - r[2]) * (g[0] - r[0]));
-            cost = al * static_cast<float>(wl) + ar * static_cast<float>(wr);
-        }
-        bestCost[tid] = cost;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        int best = -1;
-        float bc = FLT_MAX;
-        for (int k = 0; k < 3 * (kSahBins - 1); ++k)
-            if (bestCost[k] < bc) {  // first of equal costs: lowest axis, lowest plane
-                bc = bestCost[k];
-                best = k;
-            }
-        choice[0] = best < 0 ? -1 : best / (kSahBins - 1);
-        choice[1] = best < 0 ? 0 : best % (kSahBins - 1);
-    }
-    __syncthreads();
+    sah_choose(binLo, binHi, binW, binN, cext, bestCost, choice);
     const int axis = choice[0], plane = choice[1];
     // stable partition: left side first, each side in its input order; with
     // no usable plane (all centroids in one bin) the range splits in the
@@ -460,6 +473,231 @@ __global__ void __launch_bounds__(kSahBlock) k_sah_split(const SahTask* __restri
         const uint32_t mid = t.begin + nLeft;
         results[blockIdx.x] = SahResult{mid, 0u};
         newTasks[blockIdx.x] = (nLeft > 1u ? 1u : 0u) + (n - nLeft > 1u ? 1u : 0u);
+    }
+}
+
+// ---- big tasks: one task split by many blocks --------------------------------
+// At the top levels a few tasks hold most clusters; k_sah_split gives each
+// one block.  For tasks of at least bigMin items the same split is computed
+// by chunks of kSahChunk items, one block each: centroid bounds and bins are
+// merged into per-task global arrays with min / max / integer-add atomics
+// (order-independent, so the bins and the chosen plane equal k_sah_split's),
+// and the stable partition places each chunk's items after the earlier
+// chunks' (a prefix over the chunks' left counts), so the tree is the same.
+constexpr uint32_t kSahChunk = 4096;
+
+struct SahChunk {
+    uint32_t task;         // index of the task at this level
+    uint32_t begin, end;   // item range in perm (within the task's)
+    uint32_t first;        // 1 for the task's first chunk
+};
+
+struct SahBig {
+    unsigned int cbo[6];
+    unsigned int lo[3][kSahBins][3], hi[3][kSahBins][3];
+    unsigned int w[3][kSahBins], n[3][kSahBins];
+    int axis, plane;
+    uint32_t nLeft, pad;
+};
+
+__global__ void k_big_init(SahBig* __restrict__ big, uint32_t count) {
+    SahBig& b = big[blockIdx.x];
+    for (int e = threadIdx.x; e < 3 * kSahBins * 3; e += blockDim.x) {
+        (&b.lo[0][0][0])[e] = 0xffffffffu;
+        (&b.hi[0][0][0])[e] = 0u;
+    }
+    for (int e = threadIdx.x; e < 3 * kSahBins; e += blockDim.x) {
+        (&b.w[0][0])[e] = 0u;
+        (&b.n[0][0])[e] = 0u;
+    }
+    if (threadIdx.x < 6) b.cbo[threadIdx.x] = threadIdx.x < 3 ? 0xffffffffu : 0u;
+}
+
+__global__ void __launch_bounds__(kSahBlock) k_big_bounds(const SahChunk* __restrict__ chunks, const SahItem* __restrict__ items,
+                                                          const uint32_t* __restrict__ permIn, SahBig* __restrict__ big) {
+    __shared__ unsigned int cbo[6];
+    const SahChunk c = chunks[blockIdx.x];
+    const int tid = threadIdx.x;
+    if (tid < 6) cbo[tid] = tid < 3 ? 0xffffffffu : 0u;
+    __syncthreads();
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t i = c.begin + tid; i < c.end; i += kSahBlock) {
+        const SahItem& it = items[permIn[i]];
+        for (int a = 0; a < 3; ++a) {
+            const float x = item_centroid(it, a);
+            lo[a] = fminf(lo[a], x);
+            hi[a] = fmaxf(hi[a], x);
+        }
+    }
+    for (int a = 0; a < 3; ++a) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+        if ((tid & 31) == 0) {
+            atomicMin(&cbo[a], f2ord(lo[a]));
+            atomicMax(&cbo[3 + a], f2ord(hi[a]));
+        }
+    }
+    __syncthreads();
+    if (tid < 3) atomicMin(&big[c.task].cbo[tid], cbo[tid]);
+    else if (tid < 6) atomicMax(&big[c.task].cbo[tid], cbo[tid]);
+}
+
+__device__ __forceinline__ void big_extent(const SahBig& b, float (&clo)[3], float (&cext)[3]) {
+    for (int a = 0; a < 3; ++a) {
+        clo[a] = ord2f(b.cbo[a]);
+        cext[a] = ord2f(b.cbo[3 + a]) - clo[a];
+    }
+}
+
+__global__ void __launch_bounds__(kSahBlock) k_big_bins(const SahChunk* __restrict__ chunks, const SahItem* __restrict__ items,
+                                                        const uint32_t* __restrict__ permIn, SahBig* __restrict__ big) {
+    __shared__ unsigned int binLo[3][kSahBins][3], binHi[3][kSahBins][3];
+    __shared__ unsigned int binW[3][kSahBins], binN[3][kSahBins];
+    const SahChunk c = chunks[blockIdx.x];
+    SahBig& b = big[c.task];
+    const int tid = threadIdx.x;
+    for (int e = tid; e < 3 * kSahBins * 3; e += kSahBlock) {
+        (&binLo[0][0][0])[e] = 0xffffffffu;
+        (&binHi[0][0][0])[e] = 0u;
+    }
+    for (int e = tid; e < 3 * kSahBins; e += kSahBlock) {
+        (&binW[0][0])[e] = 0u;
+        (&binN[0][0])[e] = 0u;
+    }
+    float clo[3], cext[3];
+    big_extent(b, clo, cext);
+    __syncthreads();
+    for (uint32_t i = c.begin + tid; i < c.end; i += kSahBlock) {
+        const SahItem& it = items[permIn[i]];
+        for (int a = 0; a < 3; ++a) {
+            if (!(cext[a] > 0.0f)) continue;
+            int bi = static_cast<int>(kSahBins * ((item_centroid(it, a) - clo[a]) / cext[a]));
+            bi = bi < 0 ? 0 : (bi >= kSahBins ? kSahBins - 1 : bi);
+            atomicAdd(&binW[a][bi], static_cast<unsigned int>(it.weight));
+            atomicAdd(&binN[a][bi], 1u);
+            for (int k = 0; k < 3; ++k) {
+                atomicMin(&binLo[a][bi][k], f2ord(it.lo[k]));
+                atomicMax(&binHi[a][bi][k], f2ord(it.hi[k]));
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < 3 * kSahBins; e += kSahBlock) {
+        const int a = e / kSahBins, bi = e % kSahBins;
+        if (binN[a][bi] == 0u) continue;
+        atomicAdd(&b.w[a][bi], binW[a][bi]);
+        atomicAdd(&b.n[a][bi], binN[a][bi]);
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(&b.lo[a][bi][k], binLo[a][bi][k]);
+            atomicMax(&b.hi[a][bi][k], binHi[a][bi][k]);
+        }
+    }
+}
+
+// One block per big task: its plane, with k_sah_split's choice code.
+__global__ void __launch_bounds__(64) k_big_choose(SahBig* __restrict__ big) {
+    __shared__ unsigned int binLo[3][kSahBins][3], binHi[3][kSahBins][3];
+    __shared__ unsigned int binW[3][kSahBins], binN[3][kSahBins];
+    __shared__ float bestCost[3 * (kSahBins - 1)];
+    __shared__ int choice[2];
+    SahBig& b = big[blockIdx.x];
+    for (int e = threadIdx.x; e < 3 * kSahBins * 3; e += blockDim.x) {
+        (&binLo[0][0][0])[e] = (&b.lo[0][0][0])[e];
+        (&binHi[0][0][0])[e] = (&b.hi[0][0][0])[e];
+    }
+    for (int e = threadIdx.x; e < 3 * kSahBins; e += blockDim.x) {
+        (&binW[0][0])[e] = (&b.w[0][0])[e];
+        (&binN[0][0])[e] = (&b.n[0][0])[e];
+    }
+    float clo[3], cext[3];
+    big_extent(b, clo, cext);
+    __syncthreads();
+    sah_choose(binLo, binHi, binW, binN, cext, bestCost, choice);
+    if (threadIdx.x == 0) {
+        b.axis = choice[0];
+        b.plane = choice[1];
+    }
+}
+
+__device__ __forceinline__ bool big_goes_left(const SahBig& b, const float (&clo)[3], const float (&cext)[3], uint32_t i,
+                                              uint32_t half, const SahItem& it) {
+    if (b.axis < 0) return i < half;
+    int bi = static_cast<int>(kSahBins * ((item_centroid(it, b.axis) - clo[b.axis]) / cext[b.axis]));
+    bi = bi < 0 ? 0 : (bi >= kSahBins ? kSahBins - 1 : bi);
+    return bi <= b.plane;
+}
+
+__global__ void __launch_bounds__(kSahBlock) k_big_count(const SahChunk* __restrict__ chunks, const SahTask* __restrict__ tasks,
+                                                         const SahItem* __restrict__ items,
+                                                         const uint32_t* __restrict__ permIn, const SahBig* __restrict__ big,
+                                                         uint32_t* __restrict__ chunkLeft) {
+    __shared__ uint32_t warpSums[kSahBlock / 32];
+    const SahChunk c = chunks[blockIdx.x];
+    const SahTask t = tasks[c.task];
+    const SahBig& b = big[c.task];
+    float clo[3], cext[3];
+    big_extent(b, clo, cext);
+    const uint32_t half = (t.end - t.begin) / 2u;
+    uint32_t cnt = 0;
+    for (uint32_t i = c.begin + threadIdx.x; i < c.end; i += kSahBlock)
+        cnt += big_goes_left(b, clo, cext, i - t.begin, half, items[permIn[i]]) ? 1u : 0u;
+    uint32_t tot;
+    block_scan(cnt, warpSums, &tot);
+    if (threadIdx.x == 0) chunkLeft[blockIdx.x] = tot;
+}
+
+// Per big task (one thread each): exclusive prefix of its chunks' left
+// counts (its chunks are consecutive), and its left total.
+__global__ void k_big_offsets(const SahChunk* __restrict__ chunks, uint32_t nChunks, uint32_t* __restrict__ chunkLeft,
+                              SahBig* __restrict__ big, uint32_t count) {
+    const uint32_t task = blockIdx.x * blockDim.x + threadIdx.x;
+    if (task >= count) return;
+    uint32_t acc = 0;
+    bool any = false;
+    for (uint32_t k = 0; k < nChunks; ++k) {
+        if (chunks[k].task != task) continue;
+        any = true;
+        const uint32_t v = chunkLeft[k];
+        chunkLeft[k] = acc;
+        acc += v;
+    }
+    if (any) big[task].nLeft = acc;
+}
+
+__global__ void __launch_bounds__(kSahBlock) k_big_scatter(const SahChunk* __restrict__ chunks, const SahTask* __restrict__ tasks,
+                                                           const SahItem* __restrict__ items,
+                                                           const uint32_t* __restrict__ permIn, uint32_t* __restrict__ permOut,
+                                                           const SahBig* __restrict__ big,
+                                                           const uint32_t* __restrict__ chunkLeft,
+                                                           SahResult* __restrict__ results, uint32_t* __restrict__ newTasks) {
+    __shared__ uint32_t warpSums[kSahBlock / 32];
+    const SahChunk c = chunks[blockIdx.x];
+    const SahTask t = tasks[c.task];
+    const SahBig& b = big[c.task];
+    float clo[3], cext[3];
+    big_extent(b, clo, cext);
+    const uint32_t n = t.end - t.begin, half = n / 2u, nLeft = b.nLeft;
+    const uint32_t leftBefore = chunkLeft[blockIdx.x];
+    const uint32_t rightBefore = (c.begin - t.begin) - leftBefore;
+    uint32_t leftBase = 0, rightBase = 0;
+    for (uint32_t base = c.begin; base < c.end; base += kSahBlock) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < c.end;
+        const uint32_t v = valid ? permIn[i] : 0u;
+        const bool left = valid && big_goes_left(b, clo, cext, i - t.begin, half, items[v]);
+        uint32_t totL, totR;
+        const uint32_t rl = block_scan(left ? 1u : 0u, warpSums, &totL);
+        const uint32_t rr = block_scan((valid && !left) ? 1u : 0u, warpSums, &totR);
+        if (valid)
+            permOut[left ? t.begin + leftBefore + leftBase + rl : t.begin + nLeft + rightBefore + rightBase + rr] = v;
+        leftBase += totL;
+        rightBase += totR;
+    }
+    if (c.first && threadIdx.x == 0) {
+        results[c.task] = SahResult{t.begin + nLeft, 0u};
+        newTasks[c.task] = (nLeft > 1u ? 1u : 0u) + (n - nLeft > 1u ? 1u : 0u);
     }
 }
 
@@ -675,6 +913,18 @@ static int sah_top(Scratch& sc, int m, int nInternal, int clusterSize, const uin
     uint8_t* scanTmp = nullptr;
     BVH_CHECK(sc.alloc(&scanTmp, need));
     const size_t scanBytes = need;
+    // levels of at most kBigLevelTasks tasks split their tasks of at least
+    // kBigMin items with the multi-block kernels (the top of the tree)
+    constexpr uint32_t kBigLevelTasks = 64, kBigMin = 2 * kSahChunk;
+    SahBig* big = nullptr;
+    SahChunk* dChunks = nullptr;
+    uint32_t* chunkLeft = nullptr;
+    const size_t maxChunks = clusters / kSahChunk + kBigLevelTasks + 1;
+    BVH_CHECK(sc.alloc(&big, kBigLevelTasks));
+    BVH_CHECK(sc.alloc(&dChunks, maxChunks));
+    BVH_CHECK(sc.alloc(&chunkLeft, maxChunks));
+    std::vector<SahTask> hTasks;
+    std::vector<SahChunk> hChunks;
     uint32_t count = 1, nextId = 1;
     int cur = 0, pin = 0;
     for (int level = 0; count > 0; ++level) {
@@ -682,8 +932,39 @@ static int sah_top(Scratch& sc, int m, int nInternal, int clusterSize, const uin
             err = "binned-SAH top deeper than 64 levels";
             return SHIRO_ERR_DEVICE_CHECK;
         }
-        k_sah_split<<<count, kSahBlock, 0, stream>>>(tasks[cur], items, perm[pin], perm[pin ^ 1], results, newTasks);
+        uint32_t bigMin = 0;
+        hChunks.clear();
+        if (count <= kBigLevelTasks) {
+            hTasks.resize(count);
+            BVH_CHECK(cudaMemcpyAsync(hTasks.data(), tasks[cur], count * sizeof(SahTask), cudaMemcpyDeviceToHost, stream));
+            BVH_CHECK(cudaStreamSynchronize(stream));
+            for (uint32_t t = 0; t < count; ++t) {
+                if (hTasks[t].end - hTasks[t].begin < kBigMin) continue;
+                for (uint32_t b = hTasks[t].begin; b < hTasks[t].end; b += kSahChunk)
+                    hChunks.push_back(SahChunk{t, b, std::min(b + kSahChunk, hTasks[t].end), b == hTasks[t].begin ? 1u : 0u});
+            }
+            if (!hChunks.empty()) bigMin = kBigMin;
+        }
+        k_sah_split<<<count, kSahBlock, 0, stream>>>(tasks[cur], items, perm[pin], perm[pin ^ 1], results, newTasks,
+                                                     bigMin);
         BVH_CHECK(cudaGetLastError());
+        if (bigMin) {
+            const unsigned nc = static_cast<unsigned>(hChunks.size());
+            if (nc > maxChunks) {
+                err = "binned-SAH top: chunk list overflow";
+                return SHIRO_ERR_DEVICE_CHECK;
+            }
+            BVH_CHECK(cudaMemcpyAsync(dChunks, hChunks.data(), nc * sizeof(SahChunk), cudaMemcpyHostToDevice, stream));
+            k_big_init<<<count, 128, 0, stream>>>(big, count);
+            k_big_bounds<<<nc, kSahBlock, 0, stream>>>(dChunks, items, perm[pin], big);
+            k_big_bins<<<nc, kSahBlock, 0, stream>>>(dChunks, items, perm[pin], big);
+            k_big_choose<<<count, 64, 0, stream>>>(big);
+            k_big_count<<<nc, kSahBlock, 0, stream>>>(dChunks, tasks[cur], items, perm[pin], big, chunkLeft);
+            k_big_offsets<<<blocks(count, 64), 64, 0, stream>>>(dChunks, nc, chunkLeft, big, count);
+            k_big_scatter<<<nc, kSahBlock, 0, stream>>>(dChunks, tasks[cur], items, perm[pin], perm[pin ^ 1], big, chunkLeft,
+                                                        results, newTasks);
+            BVH_CHECK(cudaGetLastError());
+        }
         size_t sb = scanBytes;
         BVH_CHECK(cub::DeviceScan::ExclusiveSum(scanTmp, sb, newTasks, taskPos, static_cast<int>(count), stream));
         uint32_t lastPos = 0, lastNew = 0;
