@@ -257,6 +257,167 @@ __global__ void k_shade_normals(const float4* __restrict__ tris, uint32_t n, flo
     *r = make_float4(ng.x, ng.y, ng.z, r->w);
 }
 
+// ---- scene flattening on the device -----------------------------------------
+// The upload ships the meshes' own arrays (positions, normals, indices, each
+// concatenated over the meshes); these kernels form what the host loop of the
+// reference's BuildAccelerationScene forms (CpuPathTracer.cpp:477-598): the
+// per-triangle records in global triangle order (meshes in order, triangles
+// in order), boxes and centroids, with the same float expressions (the
+// backend is compiled without contraction), so every value equals the host
+// formulation's.
+struct FlatMesh {
+    uint32_t vbase, vcount;  // its vertices in the concatenated positions
+    uint32_t tbase, tcount;  // its global triangle ids
+    uint32_t ibase;          // its first index in the concatenated indices
+    uint32_t nbase;          // its first normal (when hasN)
+    uint32_t recBits;        // material | kShadeNormals (shading record word)
+    uint32_t hasN;
+};
+
+// Floats as unsigned integers of the same order (min / max by integer atomics).
+__host__ __device__ __forceinline__ uint32_t flat_ord(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ __forceinline__ float flat_unord(uint32_t u) {
+    const uint32_t b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+}
+
+__device__ __forceinline__ float host_min(float a, float b) { return b < a ? b : a; }  // std::min
+__device__ __forceinline__ float host_max(float a, float b) { return a < b ? b : a; }  // std::max
+
+// Vertices as float4, and the largest coordinate magnitude over all of them.
+__global__ void k_flat_verts(const float* __restrict__ pos3, uint32_t n, float4* __restrict__ pos4,
+                             unsigned int* __restrict__ magBits) {
+    float m = 0.0f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float x = pos3[3 * static_cast<size_t>(i)], y = pos3[3 * static_cast<size_t>(i) + 1],
+                    z = pos3[3 * static_cast<size_t>(i) + 2];
+        pos4[i] = make_float4(x, y, z, 0.0f);
+        m = host_max(m, host_max(fabsf(x), host_max(fabsf(y), fabsf(z))));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = host_max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31u) == 0u) atomicMax(magBits, __float_as_uint(m));  // m >= 0: the bits order as the float
+}
+
+// Per triangle: vertex indices, shading record (material bits, vertex
+// normals; the geometric normal follows after the BVH build), (p0, e1, e2),
+// raw box; the scene box as ordered-integer min / max; the first triangle
+// with an index out of range in *badTri.
+__global__ void k_flat_tris(const FlatMesh* __restrict__ meshes, uint32_t nMesh, const float* __restrict__ pos3,
+                            const float* __restrict__ nrm3, const uint32_t* __restrict__ idx, uint32_t ttotal,
+                            uint4* __restrict__ triVerts, float4* __restrict__ shade, float4* __restrict__ allTri,
+                            float* __restrict__ boxes, unsigned int* __restrict__ sceneBox, uint32_t* __restrict__ badTri) {
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < ttotal; g += gridDim.x * blockDim.x) {
+        uint32_t a = 0, b = nMesh - 1u;  // the last mesh whose first triangle is <= g
+        while (a < b) {
+            const uint32_t mid = (a + b + 1u) >> 1;
+            if (meshes[mid].tbase <= g) a = mid; else b = mid - 1u;
+        }
+        const FlatMesh m = meshes[a];
+        const uint32_t t = g - m.tbase;
+        const uint32_t i0 = idx[m.ibase + 3 * t], i1 = idx[m.ibase + 3 * t + 1], i2 = idx[m.ibase + 3 * t + 2];
+        if (i0 >= m.vcount || i1 >= m.vcount || i2 >= m.vcount) {
+            atomicMin(badTri, g);
+            continue;
+        }
+        triVerts[g] = make_uint4(m.vbase + i0, m.vbase + i1, m.vbase + i2, a);
+        float4* rec = shade + 4 * static_cast<size_t>(g);
+        rec[0] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(m.recBits));
+        const uint32_t vi[3] = {i0, i1, i2};
+        for (int k = 0; k < 3; ++k) {
+            const float* n = m.hasN ? nrm3 + 3 * (static_cast<size_t>(m.nbase) + vi[k]) : nullptr;
+            rec[1 + k] = n ? make_float4(n[0], n[1], n[2], 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        const float* p0 = pos3 + 3 * (static_cast<size_t>(m.vbase) + i0);
+        const float* p1 = pos3 + 3 * (static_cast<size_t>(m.vbase) + i1);
+        const float* p2 = pos3 + 3 * (static_cast<size_t>(m.vbase) + i2);
+        allTri[3 * static_cast<size_t>(g)] = make_float4(p0[0], p0[1], p0[2], __uint_as_float(g));
+        allTri[3 * static_cast<size_t>(g) + 1] = make_float4(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], 0.0f);
+        allTri[3 * static_cast<size_t>(g) + 2] = make_float4(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2], 0.0f);
+        for (int k = 0; k < 3; ++k) {
+            const float l = host_min(p0[k], host_min(p1[k], p2[k]));
+            const float h = host_max(p0[k], host_max(p1[k], p2[k]));
+            boxes[6 * static_cast<size_t>(g) + k] = l;
+            boxes[6 * static_cast<size_t>(g) + 3 + k] = h;
+            lo[k] = fminf(lo[k], l);
+            hi[k] = fmaxf(hi[k], h);
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+        if ((threadIdx.x & 31u) == 0u) {
+            atomicMin(&sceneBox[k], flat_ord(lo[k]));
+            atomicMax(&sceneBox[3 + k], flat_ord(hi[k]));
+        }
+    }
+}
+
+__device__ __forceinline__ float box_area(const float* lo, const float* hi) {
+    const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+// Triangles whose box area exceeds `thresh` (candidates for the leaf under
+// the root): (area bits, global id).
+__global__ void k_large_cands(const float* __restrict__ boxes, uint32_t ttotal, float thresh, uint2* __restrict__ cand,
+                              uint32_t* __restrict__ count) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < ttotal; g += gridDim.x * blockDim.x) {
+        const float a = box_area(boxes + 6 * static_cast<size_t>(g), boxes + 6 * static_cast<size_t>(g) + 3);
+        if (a > thresh) cand[atomicAdd(count, 1u)] = make_uint2(__float_as_uint(a), g);
+    }
+}
+
+struct FlatLarge {
+    uint32_t gid[8];
+    uint32_t n;
+};
+
+// Inflated boxes; the BVH input of the other triangles in global order (the
+// large ones, at most 8, go to largeOut in global order).
+__global__ void k_flat_small(const float4* __restrict__ allTri, const float* __restrict__ boxes, uint32_t ttotal,
+                             float pad, FlatLarge large, float4* __restrict__ triData, float4* __restrict__ primBoxes,
+                             float4* __restrict__ centroids, LargeTri* __restrict__ largeOut) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < ttotal; g += gridDim.x * blockDim.x) {
+        const float* bx = boxes + 6 * static_cast<size_t>(g);
+        float lo[3], hi[3];
+        for (int k = 0; k < 3; ++k) {
+            const float e = pad + (bx[3 + k] - bx[k]) * 1.0e-5f;
+            lo[k] = bx[k] - e;
+            hi[k] = bx[3 + k] + e;
+        }
+        uint32_t rank = 0;
+        bool isLarge = false;
+        for (uint32_t k = 0; k < large.n; ++k) {
+            rank += large.gid[k] < g ? 1u : 0u;
+            isLarge |= large.gid[k] == g;
+        }
+        if (isLarge) {
+            LargeTri lt;
+            for (int k = 0; k < 3; ++k) {
+                lt.tri[k] = allTri[3 * static_cast<size_t>(g) + k];
+                lt.lo[k] = lo[k];
+                lt.hi[k] = hi[k];
+            }
+            largeOut[rank] = lt;
+            continue;
+        }
+        const size_t pos = g - rank;
+        for (int k = 0; k < 3; ++k) triData[3 * pos + k] = allTri[3 * static_cast<size_t>(g) + k];
+        primBoxes[2 * pos] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+        primBoxes[2 * pos + 1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
+        centroids[pos] = make_float4(0.5f * (bx[0] + bx[3]), 0.5f * (bx[1] + bx[4]), 0.5f * (bx[2] + bx[5]), 0.0f);
+    }
+}
+
 // (Re)computes the per-material BSDF records from the resident materials.
 int build_bsdf_recs(ContextImpl* ctx) {
     const uint32_t n = ctx->materialCount + 1u;  // + the default material
@@ -839,140 +1000,160 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     }
     ctx->freeScene();
 
-    // --- flatten ------------------------------------------------------------
-    std::vector<float4> positions;
-    std::vector<uint4> triVerts;
-    size_t vtotal = 0, ttotal = 0;
+    // --- flatten (on the device) ----------------------------------------------
+    // the meshes' own arrays go up concatenated; k_flat_* form the per-triangle
+    // data, boxes and centroids there
+    size_t vtotal = 0, ttotal = 0, itotal = 0, ntotal = 0;
+    std::vector<FlatMesh> fm(sd->mesh_count);
     for (uint32_t i = 0; i < sd->mesh_count; ++i) {
         const ShiroMeshDesc& m = sd->meshes[i];
         if ((m.vertex_count && !m.positions) || (m.index_count && !m.indices))
             return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "mesh " + std::to_string(i) + ": null array");
+        const bool hasN = m.normals && m.normal_count == m.vertex_count;
+        const uint32_t material = m.material_index < sd->material_count ? m.material_index : sd->material_count;
+        fm[i] = FlatMesh{static_cast<uint32_t>(vtotal), m.vertex_count, static_cast<uint32_t>(ttotal), m.index_count / 3u,
+                         static_cast<uint32_t>(itotal), static_cast<uint32_t>(ntotal),
+                         material | (hasN ? kShadeNormals : 0u), hasN ? 1u : 0u};
         vtotal += m.vertex_count;
         ttotal += m.index_count / 3u;
+        itotal += m.index_count;
+        if (hasN) ntotal += m.vertex_count;
     }
     if (ttotal >= (1ull << 28) || vtotal >= (1ull << 32))
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene exceeds 2^28 triangles");
     if (sd->material_count >= kShadeNormals)
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene exceeds 2^31 - 1 materials");
-    positions.reserve(vtotal);
-    triVerts.reserve(ttotal);
-    std::vector<float4> shade(kShadeRec * ttotal);
-    std::vector<float4> triData;      // small triangles: 3 per
-    std::vector<float4> primBoxes;    // 2 per
-    std::vector<float4> centroids;
-    struct Cand {
-        float area;
-        uint32_t gid;
-    };
-    std::vector<float4> allTri(3 * ttotal);
-    std::vector<float> boxes(6 * ttotal);
-    float mag = 0.0f;
-    float slo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, shi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    uint32_t gid = 0;
+    if (ttotal == 0) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene has no triangles");
+    std::vector<float> pos3(3 * vtotal), nrm3(3 * std::max<size_t>(ntotal, 1));
+    std::vector<uint32_t> idx(std::max<size_t>(itotal, 1));
     for (uint32_t i = 0; i < sd->mesh_count; ++i) {
         const ShiroMeshDesc& m = sd->meshes[i];
-        const uint32_t base = static_cast<uint32_t>(positions.size());
-        for (uint32_t v = 0; v < m.vertex_count; ++v) {
-            const float* p = m.positions + 3 * static_cast<size_t>(v);
-            positions.push_back(make_float4(p[0], p[1], p[2], 0.0f));
-            mag = std::max(mag, std::max(std::fabs(p[0]), std::max(std::fabs(p[1]), std::fabs(p[2]))));
-        }
-        const bool hasN = m.normals && m.normal_count == m.vertex_count;
-        const uint32_t material = m.material_index < sd->material_count ? m.material_index : sd->material_count;
-        float recBits;
-        const uint32_t rb = material | (hasN ? kShadeNormals : 0u);
-        std::memcpy(&recBits, &rb, 4);
-        const uint32_t tris = m.index_count / 3u;
-        for (uint32_t t = 0; t < tris; ++t, ++gid) {
-            const uint32_t a = m.indices[3 * t], b = m.indices[3 * t + 1], c = m.indices[3 * t + 2];
-            if (a >= m.vertex_count || b >= m.vertex_count || c >= m.vertex_count)
-                return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT,
-                            "mesh " + std::to_string(i) + ": index out of range at triangle " + std::to_string(t));
-            triVerts.push_back(make_uint4(base + a, base + b, base + c, i));
-            float4* rec = &shade[kShadeRec * static_cast<size_t>(gid)];
-            rec[0] = make_float4(0.0f, 0.0f, 0.0f, recBits);  // the normal is formed on the device
-            const uint32_t vi[3] = {a, b, c};
-            for (int k = 0; k < 3; ++k) {
-                const float* n = hasN ? m.normals + 3 * static_cast<size_t>(vi[k]) : nullptr;
-                rec[1 + k] = n ? make_float4(n[0], n[1], n[2], 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            }
-            const float* p0 = m.positions + 3 * static_cast<size_t>(a);
-            const float* p1 = m.positions + 3 * static_cast<size_t>(b);
-            const float* p2 = m.positions + 3 * static_cast<size_t>(c);
-            float gbits;
-            std::memcpy(&gbits, &gid, 4);
-            allTri[3 * gid] = make_float4(p0[0], p0[1], p0[2], gbits);
-            allTri[3 * gid + 1] = make_float4(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], 0.0f);
-            allTri[3 * gid + 2] = make_float4(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2], 0.0f);
-            for (int k = 0; k < 3; ++k) {
-                const float lo = std::min(p0[k], std::min(p1[k], p2[k]));
-                const float hi = std::max(p0[k], std::max(p1[k], p2[k]));
-                boxes[6 * gid + k] = lo;
-                boxes[6 * gid + 3 + k] = hi;
-                slo[k] = std::min(slo[k], lo);
-                shi[k] = std::max(shi[k], hi);
-            }
-        }
+        if (m.vertex_count) std::memcpy(&pos3[3 * static_cast<size_t>(fm[i].vbase)], m.positions, 12ull * m.vertex_count);
+        if (fm[i].hasN) std::memcpy(&nrm3[3 * static_cast<size_t>(fm[i].nbase)], m.normals, 12ull * m.vertex_count);
+        if (m.index_count) std::memcpy(&idx[fm[i].ibase], m.indices, 4ull * m.index_count);
     }
-    if (ttotal == 0) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene has no triangles");
+    struct Temps {  // device scratch of the upload
+        std::vector<void*> p;
+        ~Temps() {
+            for (void* x : p) cudaFree(x);
+        }
+    } temps;
+    auto scratch = [&](size_t bytes, auto** out) -> bool {
+        void* v = nullptr;
+        if (cudaMalloc(&v, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        temps.p.push_back(v);
+        *out = static_cast<std::remove_pointer_t<decltype(out)>>(v);
+        return true;
+    };
+    auto keep = [&](size_t bytes, auto** out) -> bool {  // geometry kept with the scene
+        DeviceBlock blk;
+        if (!ensure_block(ctx, &blk, std::max<size_t>(bytes, 16), "scene geometry")) return false;
+        ctx->sceneBlocks.push_back(blk);
+        *out = static_cast<std::remove_pointer_t<decltype(out)>>(blk.ptr);
+        return true;
+    };
+    float *dPos3 = nullptr, *dNrm3 = nullptr, *dBoxes = nullptr;
+    uint32_t *dIdx = nullptr, *dRed = nullptr;
+    FlatMesh* dMeshes = nullptr;
+    float4 *dPos4 = nullptr, *dShade = nullptr, *dAllTri = nullptr;
+    uint4* dTriVerts = nullptr;
+    if (!scratch(pos3.size() * 4, &dPos3) || !scratch(nrm3.size() * 4, &dNrm3) || !scratch(idx.size() * 4, &dIdx) ||
+        !scratch(fm.size() * sizeof(FlatMesh), &dMeshes) || !scratch(8 * 4, &dRed) ||
+        !scratch(6 * ttotal * sizeof(float), &dBoxes) || !scratch(3 * ttotal * sizeof(float4), &dAllTri) ||
+        !keep(vtotal * sizeof(float4), &dPos4) || !keep(ttotal * sizeof(uint4), &dTriVerts) ||
+        !keep(kShadeRec * ttotal * sizeof(float4), &dShade))
+        return fail(ctx, SHIRO_ERR_OUT_OF_MEMORY, "scene flattening: out of device memory");
+    const uint32_t red0[8] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u, 0u, 0xffffffffu};
+    cudaError_t ce = cudaMemcpyAsync(dPos3, pos3.data(), pos3.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(dNrm3, nrm3.data(), nrm3.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(dIdx, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (ce == cudaSuccess && !fm.empty())
+        ce = cudaMemcpyAsync(dMeshes, fm.data(), fm.size() * sizeof(FlatMesh), cudaMemcpyHostToDevice, ctx->stream);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(dRed, red0, sizeof(red0), cudaMemcpyHostToDevice, ctx->stream);
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "scene flattening");
+    const unsigned gv = static_cast<unsigned>(std::min<size_t>((vtotal + 255) / 256, 4096));
+    const unsigned gt = static_cast<unsigned>(std::min<size_t>((ttotal + 255) / 256, 8192));
+    if (vtotal) k_flat_verts<<<gv, 256, 0, ctx->stream>>>(dPos3, static_cast<uint32_t>(vtotal), dPos4, dRed + 6);
+    k_flat_tris<<<gt, 256, 0, ctx->stream>>>(dMeshes, sd->mesh_count, dPos3, dNrm3, dIdx, static_cast<uint32_t>(ttotal),
+                                            dTriVerts, dShade, dAllTri, dBoxes, dRed, dRed + 7);
+    uint32_t red[8];
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(red, dRed, sizeof(red), cudaMemcpyDeviceToHost, ctx->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "scene flattening");
+    if (red[7] != 0xffffffffu) {  // the first triangle with an index out of range
+        uint32_t i = 0;
+        while (i + 1 < sd->mesh_count && fm[i + 1].tbase <= red[7]) ++i;
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT,
+                    "mesh " + std::to_string(i) + ": index out of range at triangle " + std::to_string(red[7] - fm[i].tbase));
+    }
+    float slo[3], shi[3], mag;
+    for (int k = 0; k < 3; ++k) {
+        slo[k] = flat_unord(red[k]);
+        shi[k] = flat_unord(red[3 + k]);
+    }
+    std::memcpy(&mag, &red[6], 4);
 
-    // --- large triangles + inflated boxes -----------------------------------
+    // --- large triangles (a leaf under the root) + inflated boxes --------------
     auto area = [](const float* lo, const float* hi) {
         const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
         return 2.0f * (dx * dy + dy * dz + dz * dx);
     };
     const float sceneArea = area(slo, shi);
-    std::vector<Cand> cand;
-    for (uint32_t g = 0; g < ttotal; ++g) {
-        const float a = area(&boxes[6 * g], &boxes[6 * g + 3]);
-        if (ttotal > 16 && a > 0.05f * sceneArea) cand.push_back({a, g});
+    FlatLarge fl{};
+    if (ttotal > 16) {
+        uint2* dCand = nullptr;
+        if (!scratch(ttotal * sizeof(uint2), &dCand))
+            return fail(ctx, SHIRO_ERR_OUT_OF_MEMORY, "scene flattening: out of device memory");
+        uint32_t nc = 0;
+        ce = cudaMemsetAsync(dRed, 0, 4, ctx->stream);
+        if (ce == cudaSuccess) k_large_cands<<<gt, 256, 0, ctx->stream>>>(dBoxes, static_cast<uint32_t>(ttotal),
+                                                                             0.05f * sceneArea, dCand, dRed);
+        if (ce == cudaSuccess) ce = cudaGetLastError();
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(&nc, dRed, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+        std::vector<uint2> cand(nc);
+        if (ce == cudaSuccess && nc)
+            ce = cudaMemcpyAsync(cand.data(), dCand, nc * sizeof(uint2), cudaMemcpyDeviceToHost, ctx->stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "scene flattening");
+        auto af = [](const uint2& c) {
+            float f;
+            std::memcpy(&f, &c.x, 4);
+            return f;
+        };
+        std::sort(cand.begin(), cand.end(), [&](const uint2& x, const uint2& y) {
+            return af(x) > af(y) || (af(x) == af(y) && x.y < y.y);
+        });
+        if (cand.size() > 8) cand.resize(8);
+        for (const uint2& c : cand) fl.gid[fl.n++] = c.y;
+        std::sort(fl.gid, fl.gid + fl.n);
     }
-    std::sort(cand.begin(), cand.end(), [](const Cand& x, const Cand& y) { return x.area > y.area || (x.area == y.area && x.gid < y.gid); });
-    if (cand.size() > 8) cand.resize(8);
-    std::vector<uint8_t> isLarge(ttotal, 0);
-    for (const Cand& c : cand) isLarge[c.gid] = 1;
     const float pad = mag * 1.0e-5f + 1.0e-30f;
+    const size_t nSmall = ttotal - fl.n;
+    float4 *dTri = nullptr, *dBox = nullptr, *dCen = nullptr;
+    LargeTri* dLarge = nullptr;
+    if (!scratch(3 * nSmall * sizeof(float4), &dTri) || !scratch(2 * nSmall * sizeof(float4), &dBox) ||
+        !scratch(nSmall * sizeof(float4), &dCen) || !scratch(8 * sizeof(LargeTri), &dLarge))
+        return fail(ctx, SHIRO_ERR_OUT_OF_MEMORY, "scene flattening: out of device memory");
+    k_flat_small<<<gt, 256, 0, ctx->stream>>>(dAllTri, dBoxes, static_cast<uint32_t>(ttotal), pad, fl, dTri, dBox, dCen,
+                                             dLarge);
     BvhInput bin;
-    triData.reserve(3 * ttotal);
-    primBoxes.reserve(2 * ttotal);
-    centroids.reserve(ttotal);
-    for (uint32_t g = 0; g < ttotal; ++g) {
-        float lo[3], hi[3];
-        for (int k = 0; k < 3; ++k) {
-            const float e = pad + (boxes[6 * g + 3 + k] - boxes[6 * g + k]) * 1.0e-5f;
-            lo[k] = boxes[6 * g + k] - e;
-            hi[k] = boxes[6 * g + 3 + k] + e;
-        }
-        if (isLarge[g]) {
-            LargeTri lt;
-            for (int k = 0; k < 3; ++k) {
-                lt.tri[k] = allTri[3 * g + k];
-                lt.lo[k] = lo[k];
-                lt.hi[k] = hi[k];
-            }
-            bin.largeSlots.push_back(lt);
-            continue;
-        }
-        triData.push_back(allTri[3 * g]);
-        triData.push_back(allTri[3 * g + 1]);
-        triData.push_back(allTri[3 * g + 2]);
-        primBoxes.push_back(make_float4(lo[0], lo[1], lo[2], 0.0f));
-        primBoxes.push_back(make_float4(hi[0], hi[1], hi[2], 0.0f));
-        centroids.push_back(make_float4(0.5f * (boxes[6 * g] + boxes[6 * g + 3]), 0.5f * (boxes[6 * g + 1] + boxes[6 * g + 4]),
-                                        0.5f * (boxes[6 * g + 2] + boxes[6 * g + 5]), 0.0f));
-    }
-    std::vector<float4>().swap(allTri);
-    std::vector<float>().swap(boxes);
+    bin.largeSlots.resize(fl.n);
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess && fl.n)
+        ce = cudaMemcpyAsync(bin.largeSlots.data(), dLarge, fl.n * sizeof(LargeTri), cudaMemcpyDeviceToHost, ctx->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "scene flattening");
 
     int rc;
-    const float4 *dTri = nullptr, *dBox = nullptr, *dCen = nullptr;
-    if ((rc = upload(ctx, triData, &dTri, "triangle staging")) != SHIRO_OK) return rc;
-    if ((rc = upload(ctx, primBoxes, &dBox, "box staging")) != SHIRO_OK) return rc;
-    if ((rc = upload(ctx, centroids, &dCen, "centroid staging")) != SHIRO_OK) return rc;
     bin.triData = dTri;
     bin.primBoxes = dBox;
     bin.centroids = dCen;
-    bin.smallCount = static_cast<uint32_t>(centroids.size());
+    bin.smallCount = static_cast<uint32_t>(nSmall);
     bin.sahClusterSize = ctx->sahClusterSize;
     BvhOutput bout, bwide;
     std::string berr;
@@ -986,11 +1167,6 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
         BvhInput small = bin;
         small.maxLeaf = kWideLeaf;
         rc = build_bvh(small, ctx->stream, &bwide, berr);
-    }
-    // staging blocks are no longer needed
-    for (int k = 0; k < 3; ++k) {
-        free_block(&ctx->sceneBlocks.back());
-        ctx->sceneBlocks.pop_back();
     }
     auto drop = [](BvhOutput& b) {
         if (b.nodes) cudaFree(b.nodes);
@@ -1039,10 +1215,10 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     s.nodes8 = ctx->bvhWidth == 8 ? ctx->nodes8 : nullptr;
     s.tris = s.nodes8 ? ctx->tris8 : ctx->tris2;
 
-    // --- per-triangle data -----------------------------------------------------
-    if ((rc = upload(ctx, triVerts, &s.triVerts, "triangle vertices")) != SHIRO_OK) return rc;
-    if ((rc = upload(ctx, positions, &s.positions, "positions")) != SHIRO_OK) return rc;
-    if ((rc = upload(ctx, shade, &s.shade, "triangle shading records")) != SHIRO_OK) return rc;
+    // --- per-triangle data (formed by k_flat_tris; the geometric normals now) ---
+    s.triVerts = dTriVerts;
+    s.positions = dPos4;
+    s.shade = dShade;
     k_shade_normals<<<(bout.triCount + 255) / 256, 256, 0, ctx->stream>>>(ctx->tris2, bout.triCount,
                                                                          const_cast<float4*>(s.shade));
     if (const cudaError_t e = cudaGetLastError(); e != cudaSuccess) return cuda_fail(ctx, e, "shading records");
