@@ -87,3 +87,24 @@ def test_shading_only_upload_is_fast():
         full = min(full, time.perf_counter() - t0)
     print(f"upload: full {full:.3f} s, light edit {light:.3f} s")
     assert light < 0.35 * full, (light, full)
+
+
+def test_index_out_of_range_is_refused():
+    """The device flattening checks every vertex index before using it: a
+    mesh with an index past its vertices is refused with the mesh and
+    triangle named, and the context renders the next valid scene."""
+    from shiro_gb300 import GpuBackend, scenes
+    from shiro_gb300.backend import ShiroGpuError
+
+    w = scenes.sphere_workload(32, 24, 2, 4, env_width=64, env_height=32)
+    bad = copy.deepcopy(w.scene)
+    m = bad.meshes[0]
+    m.indices = m.indices.copy()
+    m.indices[3 * 5 + 1] = np.uint32(m.positions.shape[0] + 7)  # triangle 5 of mesh 0
+    with GpuBackend(0) as gpu:
+        with pytest.raises(ShiroGpuError) as ei:
+            gpu.upload_scene(bad)
+        assert ei.value.code == -1 and "mesh 0: index out of range at triangle 5" in str(ei.value), ei.value
+        good = gpu.render(w.scene, w.camera, w.settings)
+        ref, _ = _fresh(w.scene, w.camera, w.settings)
+        assert same(good, ref)
