@@ -22,7 +22,7 @@ struct DeviceBlock {
 struct EnvHost {
     uint32_t w = 0, h = 0;
     bool latlong = true;
-    std::vector<float> rgb;  // w * h * 3, as uploaded
+    const float* rgb = nullptr;  // w * h * 3: the caller's texels (read during the upload only)
 };
 
 // Default cluster size of the binned-SAH top (shiro_gpu_set_bvh_build):

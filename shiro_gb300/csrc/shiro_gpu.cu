@@ -449,21 +449,50 @@ int finish_env(ContextImpl* ctx, size_t k) {
     return err == cudaSuccess ? SHIRO_OK : cuda_fail(ctx, err, "env sample records");
 }
 
+__global__ void k_env_texels(const float* __restrict__ rgb, size_t n, float4* __restrict__ tex) {
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x)
+        tex[i] = make_float4(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], 0.0f);
+}
+
 int upload_envs(ContextImpl* ctx) {
-    // texels go up as (r, g, b, 0); the importance tables, the masses in
-    // texels.w and the per-texel sample records are built on the device
+    // the caller's rgb texels go up as they are and become (r, g, b, 0) on
+    // the device; the importance tables, the masses in texels.w and the
+    // per-texel sample records are built there too
+    DeviceBlock rgbStage;
+    struct Free {
+        DeviceBlock& b;
+        ContextImpl* ctx;
+        ~Free() {
+            if (b.ptr) cudaStreamSynchronize(ctx->stream);  // the conversion read it
+            free_block(&b);
+        }
+    } freeStage{rgbStage, ctx};
     for (size_t k = 0; k < ctx->envHost.size(); ++k) {
         EnvHost& e = ctx->envHost[k];
         const size_t n = static_cast<size_t>(e.w) * e.h;
-        std::vector<float4> tex(n);
-        for (size_t i = 0; i < n; ++i) tex[i] = make_float4(e.rgb[3 * i], e.rgb[3 * i + 1], e.rgb[3 * i + 2], 0.0f);
         DevEnv& d = ctx->envDev[k];
         d.w = e.w;
         d.h = e.h;
         d.latlong = e.latlong ? 1u : 0u;
         d.hasTable = (e.latlong && n > 0) ? 1u : 0u;
         int rc;
-        if ((rc = upload(ctx, tex, &d.texels, "env texels")) != SHIRO_OK) return rc;
+        DeviceBlock tb;
+        if (!ensure_block(ctx, &tb, std::max<size_t>(n, 1) * sizeof(float4), "env texels")) return SHIRO_ERR_OUT_OF_MEMORY;
+        ctx->sceneBlocks.push_back(tb);
+        d.texels = static_cast<const float4*>(tb.ptr);
+        if (n) {
+            if (rgbStage.bytes < 12 * n) {  // grown for the largest texture (a sync frees the old one)
+                if (rgbStage.ptr) cudaStreamSynchronize(ctx->stream);
+                free_block(&rgbStage);
+                if (!ensure_block(ctx, &rgbStage, 12 * n, "env texel staging")) return SHIRO_ERR_OUT_OF_MEMORY;
+            }
+            cudaError_t ce = cudaMemcpyAsync(rgbStage.ptr, e.rgb, 12 * n, cudaMemcpyHostToDevice, ctx->stream);
+            if (ce != cudaSuccess) return cuda_fail(ctx, ce, "env texels");
+            k_env_texels<<<static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 4096)), 256, 0, ctx->stream>>>(
+                static_cast<const float*>(rgbStage.ptr), n, const_cast<float4*>(d.texels));
+            if ((ce = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, ce, "env texels");
+        }
         if (d.hasTable) {
             DeviceBlock rb, cb, ab;
             if (!ensure_block(ctx, &rb, (e.h + 1u) * sizeof(float), "env row cdf") ||
@@ -478,6 +507,7 @@ int upload_envs(ContextImpl* ctx) {
             d.alias = static_cast<const uint2*>(ab.ptr);
         }
         if ((rc = finish_env(ctx, k)) != SHIRO_OK) return rc;
+        e.rgb = nullptr;  // the caller's array is not ours past the upload
     }
     return SHIRO_OK;
 }
@@ -809,7 +839,7 @@ int upload_shading(ContextImpl* ctx, const ShiroSceneDesc* sd) {
             e.w = d.env_width;
             e.h = d.env_height;
             e.latlong = d.layout != SHIRO_ENV_LAYOUT_ANGULAR;
-            e.rgb.assign(d.env_pixels, d.env_pixels + 3 * static_cast<size_t>(e.w) * e.h);
+            e.rgb = d.env_pixels;
             domes[i].env = static_cast<int32_t>(ctx->envHost.size());
             ctx->envHost.push_back(std::move(e));
         }
