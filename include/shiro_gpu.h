@@ -358,7 +358,7 @@ typedef struct ShiroWavefrontConfig {
     uint32_t shade_regs;    /* register cap of the shade stage: 128, 96 or 80 */
     uint32_t extend_steps;  /* wide-BVH nodes a lane visits between refills, 1-32 */
     uint32_t refill_idle;   /* idle lanes that make a warp refill, 1-32 */
-    uint32_t concurrent_waves; /* 1 or 2: waves in flight at once, each with its own pool of
+    uint32_t concurrent_waves; /* 1 to 4: waves in flight at once, each with its own pool of
                                   paths_in_flight paths and its own stream (2 fills one wave's
                                   stage tails with the other's work); 0 leaves the current value */
     uint32_t bin_rays;         /* 1: before each bounce after the first, the closest-hit queue is

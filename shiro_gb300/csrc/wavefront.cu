@@ -1371,7 +1371,7 @@ struct WavePool {
     std::vector<unsigned char> execKey;
 };
 
-constexpr uint32_t kMaxConcurrentWaves = 2;
+constexpr uint32_t kMaxConcurrentWaves = 4;
 
 struct WavefrontState {
     ShiroWavefrontConfig cfg{};
@@ -1379,10 +1379,11 @@ struct WavefrontState {
     DeviceBlock tables;
     int smCount = 0;
     bool tuned = false;
-    // second stream for the second wave in flight, and the events that fork
-    // it from / join it to the context's stream
-    cudaStream_t side = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
+    // streams of the waves in flight after the first, the event that forks
+    // them from the context's stream and the events that join them to it
+    cudaStream_t side[kMaxConcurrentWaves - 1] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[kMaxConcurrentWaves - 1] = {};
     DeviceBlock adjView;  // device copy of the adjoint's parameter view
 };
 
@@ -1693,8 +1694,8 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     uint32_t used = std::min<uint32_t>(static_cast<uint32_t>(pl.waves.size()), maxWaves);
     // waves in flight at once: pool k runs waves k, k + nl, ... on its own
     // stream (graphs only; the diagnostic per-stage timing runs one)
-    const uint32_t nl = (cfg.use_graph && cfg.concurrent_waves >= 2 && used >= 2) ? 2u : 1u;
-    uint32_t poolP[kMaxConcurrentWaves] = {0, 0};
+    const uint32_t nl = cfg.use_graph ? std::max(1u, std::min({cfg.concurrent_waves, used, kMaxConcurrentWaves})) : 1u;
+    uint32_t poolP[kMaxConcurrentWaves] = {};
     for (uint32_t w = 0; w < used; ++w) poolP[w % nl] = std::max(poolP[w % nl], pl.waves[w].paths);
     for (uint32_t k = 0; k < nl; ++k)
         if (!ensure_pool(ctx, &wf->pools[k], poolP[k], lightSamples)) return SHIRO_ERR_OUT_OF_MEMORY;
@@ -1711,10 +1712,14 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
         const cudaError_t ce = cudaMemcpyAsync(wf->adjView.ptr, adj, sizeof(AdjView), cudaMemcpyHostToDevice, ctx->stream);
         if (ce != cudaSuccess) return cuda_fail(ctx, ce, "adjoint view");
     }
-    if (nl > 1 && !wf->side) {
-        cudaError_t ce = cudaStreamCreateWithFlags(&wf->side, cudaStreamNonBlocking);
-        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&wf->fork, cudaEventDisableTiming);
-        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&wf->join, cudaEventDisableTiming);
+    if (nl > 1 && !wf->fork) {
+        const cudaError_t ce = cudaEventCreateWithFlags(&wf->fork, cudaEventDisableTiming);
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "wavefront side stream");
+    }
+    for (uint32_t k = 1; k < nl; ++k) {
+        if (wf->side[k - 1]) continue;
+        cudaError_t ce = cudaStreamCreateWithFlags(&wf->side[k - 1], cudaStreamNonBlocking);
+        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&wf->join[k - 1], cudaEventDisableTiming);
         if (ce != cudaSuccess) return cuda_fail(ctx, ce, "wavefront side stream");
     }
     // tables: waves, segments, requests
@@ -1835,7 +1840,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev;
-    cudaGraphExec_t exec[kMaxConcurrentWaves] = {nullptr, nullptr};
+    cudaGraphExec_t exec[kMaxConcurrentWaves] = {};
     int rc = SHIRO_OK;
     if (cfg.use_graph) {
         for (uint32_t k = 0; k < nl && rc == SHIRO_OK; ++k) {
@@ -1866,13 +1871,15 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             }
         }
     }
-    // the second wave in flight runs on the side stream, after the tables and
-    // counters written above, and the context's stream waits for it at the end
+    // the waves in flight after the first run on side streams, after the
+    // tables and counters written above, and the context's stream waits for
+    // them at the end
     if (rc == SHIRO_OK && nl > 1) {
         e = cudaEventRecord(wf->fork, st);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(wf->side, wf->fork, 0);
+        for (uint32_t k = 1; k < nl && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(wf->side[k - 1], wf->fork, 0);
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront fork");
     }
+    auto lane_stream = [&](uint32_t k) { return k == 0 ? st : wf->side[k - 1]; };
     uint64_t launches = 0;
     uint32_t launchedWaves = 0;
     // with a cancel flag, nl + 1 waves are queued at most, so the flag is read
@@ -1885,20 +1892,20 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
         }
         const uint32_t k = w % nl;
         if (exec[k]) {
-            e = cudaGraphLaunch(exec[k], k == 0 ? st : wf->side);
+            e = cudaGraphLaunch(exec[k], lane_stream(k));
         } else {
             enqueue_wave_timed(L, st, ev);
             e = cudaGetLastError();
         }
-        throttle.after_launch(exec[k] && k != 0 ? wf->side : st);
+        throttle.after_launch(exec[k] ? lane_stream(k) : st);
         launches += 3 + 6ull * L.depth + (L.binShadow ? 3ull * L.depth : 0ull) +
                 (L.binRays && L.depth > 1 ? 3ull * (L.depth - 1) : 0ull) + (adj ? 2ull + 5ull * L.depth - 1ull : 0ull);
         ++launchedWaves;
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront launch");
     }
-    if (nl > 1) {  // join (also after a failed launch: the side stream's work must be done before we return)
-        cudaEventRecord(wf->join, wf->side);
-        cudaStreamWaitEvent(st, wf->join, 0);
+    for (uint32_t k = 1; k < nl; ++k) {  // join (also after a failed launch: side work must end before we return)
+        cudaEventRecord(wf->join[k - 1], wf->side[k - 1]);
+        cudaStreamWaitEvent(st, wf->join[k - 1], 0);
     }
     cudaEventRecord(e1, st);
     e = cudaEventSynchronize(e1);
@@ -2067,7 +2074,8 @@ int wavefront_adjoint(ContextImpl* ctx, const ShiroRenderDesc& req, const AdjVie
 void wavefront_free(ContextImpl* ctx) {
     if (!ctx->wavefront) return;
     WavefrontState* wf = ctx->wavefront;
-    if (wf->side) cudaStreamSynchronize(wf->side);
+    for (cudaStream_t sd : wf->side)
+        if (sd) cudaStreamSynchronize(sd);
     for (WavePool& pool : wf->pools) {
         if (pool.exec) cudaGraphExecDestroy(pool.exec);
         for (DeviceBlock* b : {&pool.state, &pool.shadow, &pool.queues, &pool.records, &pool.adj, &pool.adjLog})
@@ -2076,8 +2084,10 @@ void wavefront_free(ContextImpl* ctx) {
     if (wf->tables.ptr) cudaFree(wf->tables.ptr);
     if (wf->adjView.ptr) cudaFree(wf->adjView.ptr);
     if (wf->fork) cudaEventDestroy(wf->fork);
-    if (wf->join) cudaEventDestroy(wf->join);
-    if (wf->side) cudaStreamDestroy(wf->side);
+    for (cudaEvent_t j : wf->join)
+        if (j) cudaEventDestroy(j);
+    for (cudaStream_t sd : wf->side)
+        if (sd) cudaStreamDestroy(sd);
     delete wf;
     ctx->wavefront = nullptr;
 }
@@ -2111,7 +2121,7 @@ int wavefront_set_config(ContextImpl* ctx, const ShiroWavefrontConfig* cfg) {
     if (cfg->extend_steps) wf->cfg.extend_steps = cfg->extend_steps;
     if (cfg->refill_idle) wf->cfg.refill_idle = cfg->refill_idle;
     if (cfg->concurrent_waves > kMaxConcurrentWaves)
-        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "concurrent_waves must be 1 or 2");
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "concurrent_waves must be 1 to 4");
     if (cfg->concurrent_waves) wf->cfg.concurrent_waves = cfg->concurrent_waves;
     if (cfg->bin_rays > 2 || cfg->bin_shadow > 2)
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "bin_rays and bin_shadow must be 1 (on), 2 (off) or 0");
@@ -2210,16 +2220,17 @@ int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefr
         c.shade_regs = regs;
         if ((rc = trial(c)) != SHIRO_OK) return rc;
     }
-    // two waves in flight (each with a pool of the chosen size or half of it)
+    // 2 to 4 waves in flight (each with a pool of the chosen size or half of it)
     if (total > best.paths_in_flight) {
         const uint32_t p1 = best.paths_in_flight;
-        for (uint32_t p : {p1, p1 / 2}) {
-            if (p < (1u << 20)) continue;
-            ShiroWavefrontConfig c = best;
-            c.concurrent_waves = 2;
-            c.paths_in_flight = p;
-            if ((rc = trial(c)) != SHIRO_OK) return rc;
-        }
+        for (uint32_t n : {2u, 3u, 4u})
+            for (uint32_t p : {p1, p1 / 2}) {
+                if (p < (1u << 20) || static_cast<uint64_t>(p) * (n - 1) >= total) continue;
+                ShiroWavefrontConfig c = best;
+                c.concurrent_waves = n;
+                c.paths_in_flight = p;
+                if ((rc = trial(c)) != SHIRO_OK) return rc;
+            }
     }
     for (uint32_t on : {1u, 2u}) {  // queue binning before the traversal stages
         ShiroWavefrontConfig c = best;

@@ -171,7 +171,9 @@ def test_two_waves_in_flight_uneven_batch(gpu, pool):
                                    dict(coop_extend=1, coop_occlude=1, bin_rays=1, bin_shadow=1, refill_idle=32),
                                    dict(extend_regs=48, occlude_regs=40), dict(extend_regs=40, occlude_regs=48),
                                    dict(occlude_refill=1), dict(occlude_refill=1, extend_steps=1, refill_idle=32),
-                                   dict(occlude_refill=1, bin_shadow=1, concurrent_waves=2, paths_in_flight=2048)])
+                                   dict(occlude_refill=1, bin_shadow=1, concurrent_waves=2, paths_in_flight=2048),
+                                   dict(concurrent_waves=3, paths_in_flight=2048),
+                                   dict(concurrent_waves=4, paths_in_flight=1024, coop_occlude=1)])
 def test_tuning_knobs_keep_frames_identical(gpu, knobs):
     """Register cap of the shade stage, the lane-refill parameters of the
     wide-BVH extend stage, the binning of the ray / occlusion queues and the
