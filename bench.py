@@ -267,11 +267,11 @@ def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 
     sphere scene: 512x512 (`size` for profiling cases), 32 spp, depth 6, L2
     loss against a seeded target, gradients for 256 x (base colour, roughness,
     metalness) and the 512x256x3 environment texels.  One gradient = one
-    forward render + one adjoint pass."""
+    forward render + one adjoint pass (which replays the forward's kept paths)."""
     import torch
 
     from shiro_gb300 import GpuBackend, scenes
-    from shiro_gb300.abi import RenderSettings
+    from shiro_gb300.abi import RENDER_KEEP_PATHS, RenderSettings
 
     scene = scenes.split_sphere_scene(parts=256, env_width=512, env_height=256, seed=4)
     st = RenderSettings(width=size, height=size, samples_per_pixel=32, max_depth=6, diffuse_depth=6, specular_depth=6,
@@ -291,7 +291,8 @@ def adjoint_bench(local: int, iters: int = 5, warmup: int = 2, bvh_width: int = 
     grads = {k: torch.zeros_like(v) for k, v in p.items()}
 
     def step():
-        img = gpu.render_device(cam, st, wavefront=True)  # the forward autograd.render runs
+        # the forward autograd.render runs (its paths kept for the adjoint)
+        img = gpu.render_device(cam, st, flags=RENDER_KEEP_PATHS, wavefront=True)
         fwd_ms = gpu.last_stats()["kernel_ms"]
         d = torch.zeros_like(img)
         d[..., :3] = 2.0 * (img[..., :3] - target) / target.numel()

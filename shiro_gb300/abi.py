@@ -30,6 +30,7 @@ BACKEND_CPU, BACKEND_GPU, BACKEND_HYBRID = 0, 1, 2
 ENV_AUTOMATIC, ENV_LATLONG, ENV_ANGULAR = 0, 1, 2
 RENDER_ENV_CDF = 0x1
 RENDER_NO_CLAMP = 0x2
+RENDER_KEEP_PATHS = 0x4
 
 F3 = C.c_float * 3
 

@@ -6,8 +6,11 @@ per-material base colour [M, 3], roughness [M], metalness [M] and the texels
 [H_env, W_env, 3] of dome light 0.  The forward renders with the batched
 wavefront form (or the plain form) after writing the parameters into the
 resident scene; the backward runs the
-adjoint path-replay kernel (shiro_gpu_adjoint), which recomputes every path
-from its QMC seed instead of storing it.
+adjoint path replay (shiro_gpu_adjoint), which follows every path again from
+its QMC seed.  When the backward replays the forward's own samples, the
+wavefront forward keeps its paths' radiance records and hit / visibility logs
+on the device (SHIRO_RENDER_KEEP_PATHS) and the backward replays them without
+running the forward stages a second time.
 
 For a loss that is non-linear in the image (an L2 loss), replaying the same
 samples in the backward pass as in the forward one correlates the upstream
@@ -20,7 +23,7 @@ from __future__ import annotations
 
 import torch
 
-from .abi import Camera, RenderSettings
+from .abi import RENDER_KEEP_PATHS, Camera, RenderSettings
 
 
 class _Render(torch.autograd.Function):
@@ -30,7 +33,8 @@ class _Render(torch.autograd.Function):
         tensors = [t.detach().contiguous().float() if t is not None else None
                    for t in (base_color, roughness, metallic, env)]
         backend.set_params(*tensors)
-        beauty = backend.render_device(camera, settings, sample_start, settings.samples_per_pixel, flags,
+        keep = RENDER_KEEP_PATHS if wavefront and (adj_start is None or adj_start == sample_start) else 0
+        beauty = backend.render_device(camera, settings, sample_start, settings.samples_per_pixel, flags | keep,
                                        wavefront=wavefront)
         ctx.backend = backend
         ctx.camera = camera

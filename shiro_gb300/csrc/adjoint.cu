@@ -334,6 +334,7 @@ AdjView base_view(ContextImpl* ctx) {
 
 int adjoint_set_params(ContextImpl* ctx, const float* base, const float* rough, const float* metal, const float* env) {
     if (!ctx->hasScene) return fail(ctx, SHIRO_ERR_NO_SCENE, "no scene uploaded");
+    ++ctx->epoch;
     if ((base || rough || metal) && ctx->materialCount) {
         k_scatter_params<<<grid(ctx->materialCount, 128), 128, 0, ctx->stream>>>(
             const_cast<Mat*>(ctx->scene.materials), ctx->materialCount, base, rough, metal);

@@ -69,6 +69,10 @@ struct ContextImpl {
     // 1: the adjoint replays paths with the wavefront stages (after each
     // wave's forward stages); 0: one thread per path (k_adjoint)
     uint32_t adjointWavefront = 1;
+    // bumped by every call that changes what a render computes (scene,
+    // parameters, BVH choice, wavefront configuration): a forward wave kept
+    // for the adjoint is replayed only while it is unchanged
+    uint64_t epoch = 0;
 
     // scratch (grown on demand, kept between calls)
     DeviceBlock pathRecords;

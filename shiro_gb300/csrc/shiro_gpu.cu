@@ -218,7 +218,8 @@ int validate_request(ContextImpl* ctx, const ShiroRenderDesc& r) {
     if (!ctx->hasScene) return fail(ctx, SHIRO_ERR_NO_SCENE, "no scene uploaded");
     const uint64_t px = static_cast<uint64_t>(r.settings.width) * r.settings.height;
     if (px > (1ull << 31)) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "frame too large");
-    if (r.flags & ~(SHIRO_RENDER_ENV_CDF | SHIRO_RENDER_NO_CLAMP)) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "unknown flags");
+    if (r.flags & ~(SHIRO_RENDER_ENV_CDF | SHIRO_RENDER_NO_CLAMP | SHIRO_RENDER_KEEP_PATHS))
+        return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "unknown flags");
     return SHIRO_OK;
 }
 
@@ -972,6 +973,7 @@ int shiro_gpu_set_bvh_width(ShiroGpuContext* ctx, uint32_t width) {
     if (!ctx || (width != 0 && width != 2 && width != 8)) return SHIRO_ERR_INVALID_ARGUMENT;
     ContextImpl& c = ctx->impl;
     c.bvhWidth = width;
+    ++c.epoch;
     c.scene.nodes8 = (width == 8 && c.hasScene) ? c.nodes8 : nullptr;
     // hit slots index the triangle array of the BVH that produced them
     if (c.hasScene) c.scene.tris = c.scene.nodes8 ? c.tris8 : c.tris2;
@@ -985,6 +987,7 @@ int shiro_gpu_set_bvh_width(ShiroGpuContext* ctx, uint32_t width) {
 int shiro_gpu_set_bvh_build(ShiroGpuContext* ctx, uint32_t sah_cluster_triangles) {
     if (!ctx || sah_cluster_triangles == 1 || sah_cluster_triangles > (1u << 16)) return SHIRO_ERR_INVALID_ARGUMENT;
     ctx->impl.sahClusterSize = sah_cluster_triangles;
+    ++ctx->impl.epoch;
     return SHIRO_OK;
 }
 
@@ -1016,6 +1019,7 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     if (sd->mesh_count && !sd->meshes) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "null mesh array");
     if (sd->material_count && !sd->materials) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "null material array");
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ++ctx->epoch;
     const uint64_t geom = geometry_signature(*sd, ctx->sahClusterSize);
     if (ctx->hasScene && ctx->geomValid && ctx->geomSignature == geom) {
         // the same geometry (a light, a material or an environment edited):
@@ -1406,6 +1410,7 @@ int shiro_gpu_get_wavefront_config(const ShiroGpuContext* ctx, ShiroWavefrontCon
 
 int shiro_gpu_set_wavefront_config(ShiroGpuContext* ctx, const ShiroWavefrontConfig* cfg) {
     if (!ctx || !cfg) return SHIRO_ERR_INVALID_ARGUMENT;
+    ++ctx->impl.epoch;
     return wavefront_set_config(&ctx->impl, cfg);
 }
 

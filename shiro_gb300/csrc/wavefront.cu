@@ -1362,16 +1362,39 @@ __global__ void __launch_bounds__(128) wf_records_out(WfView v) {
 // host side
 // ===========================================================================
 // One pool of paths in flight with its queues, and the wave graph it replays.
+// An instantiated wave graph and the launch parameters it bakes in (reused
+// while a call's parameters are byte-identical: only the tables' contents
+// differ between such calls, and the kernels read them from memory).
+struct WaveGraph {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<unsigned char> key;
+    uint64_t lastUse = 0;
+};
+
+// Graphs kept per pool: a differentiable loop alternates a forward render
+// and an adjoint (two different graphs), other callers render one kind.
+constexpr int kGraphsPerPool = 4;
+
 struct WavePool {
     DeviceBlock state, shadow, queues, records, adj, adjLog;
-    // the last instantiated wave graph and the launch parameters it bakes in
-    // (reused while a call's parameters are byte-identical: only the tables'
-    // contents differ between such calls, and the kernels read them from memory)
-    cudaGraphExec_t exec = nullptr;
-    std::vector<unsigned char> execKey;
+    WaveGraph graphs[kGraphsPerPool];
 };
 
 constexpr uint32_t kMaxConcurrentWaves = 4;
+
+// A forward render with SHIRO_RENDER_KEEP_PATHS that ran as one wave leaves
+// its path records and hit / visibility logs on pool 0; an adjoint of the
+// same request, before any other wavefront call and any change of scene,
+// parameters or configuration (ContextImpl::epoch), replays them without
+// running the forward stages again.
+struct KeptWave {
+    bool valid = false;
+    DevRequest q{};  // SHIRO_RENDER_KEEP_PATHS cleared
+    uint64_t epoch = 0;
+    uint32_t P = 0, depth = 0, lightSamples = 0;
+    const void* state = nullptr;  // pool 0's blocks when it was kept
+    const void* log = nullptr;
+};
 
 struct WavefrontState {
     ShiroWavefrontConfig cfg{};
@@ -1385,6 +1408,8 @@ struct WavefrontState {
     cudaEvent_t fork = nullptr;
     cudaEvent_t join[kMaxConcurrentWaves - 1] = {};
     DeviceBlock adjView;  // device copy of the adjoint's parameter view
+    uint64_t graphClock = 0;
+    KeptWave kept;
 };
 
 namespace {
@@ -1538,6 +1563,7 @@ struct Launch {
     uint32_t occRefill;           // lane refill in the occlusion stage
     int gBin;
     AdjWave aw;                   // aw.on: the adjoint replay follows the forward stages
+    uint32_t replayOnly;          // the adjoint replay alone, of a kept forward wave
     int gAdjShade, gAdjShadow, gAdjMiss, gAdjHits;
     bool ext;  // the scene uses transmission, opacity or emitters
 };
@@ -1618,6 +1644,10 @@ void launch_shade(const Launch& L, cudaStream_t st, uint32_t cur, uint32_t d) {
 }
 
 void enqueue_wave(const Launch& L, cudaStream_t st) {
+    if (L.replayOnly) {
+        enqueue_replay(L, st);
+        return;
+    }
     wf_begin<<<1, 32, 0, st>>>(L.v);
     wf_generate<<<L.gGen, 128, 0, st>>>(L.v);
     for (uint32_t d = 0; d < L.depth; ++d) {
@@ -1647,6 +1677,10 @@ void enqueue_wave_timed(const Launch& L, cudaStream_t st, std::vector<std::pair<
         cudaEventRecord(b, st);
         ev.push_back({stage, {a, b}});
     };
+    if (L.replayOnly) {
+        timed(4, [&] { enqueue_replay(L, st); });
+        return;
+    }
     timed(5, [&] { wf_begin<<<1, 32, 0, st>>>(L.v); });
     timed(0, [&] { wf_generate<<<L.gGen, 128, 0, st>>>(L.v); });
     for (uint32_t d = 0; d < L.depth; ++d) {
@@ -1671,11 +1705,24 @@ void enqueue_wave_timed(const Launch& L, cudaStream_t st, std::vector<std::pair<
     });
 }
 
+// True when `a` and `b` describe the same paths (SHIRO_RENDER_KEEP_PATHS aside).
+bool same_paths(DevRequest a, DevRequest b) {
+    a.flags &= ~SHIRO_RENDER_KEEP_PATHS;
+    b.flags &= ~SHIRO_RENDER_KEEP_PATHS;
+    return std::memcmp(&a, &b, sizeof(DevRequest)) == 0;
+}
+
 // Renders the requests (device AOV planes in `aovs`) with configuration
 // `cfg`.  maxWaves limits the waves run (autotuning); returns paths traced.
+// adj: run the adjoint replay after each wave's forward stages (or alone,
+// over a kept forward wave of the same request); keep: log the forward
+// stages of a one-wave render and keep its pool for such an adjoint.
 int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& cfg, const std::vector<DevRequest>& qs,
               const std::vector<AovPtrs>& aovs, const volatile int* cancel, uint32_t maxWaves, uint64_t* pathsOut,
-              double* msOut, float4* recordsOut = nullptr, const AdjView* adj = nullptr) {
+              double* msOut, float4* recordsOut = nullptr, const AdjView* adj = nullptr, bool keep = false) {
+    // every call below reuses the pools: a kept wave serves at most the call that follows it
+    const KeptWave kept = wf->kept;
+    wf->kept.valid = false;
     uint32_t lightSamples = ctx->scene.distantCount;
     uint32_t domeSamplesMax = 1;
     for (const DevRequest& q : qs) domeSamplesMax = std::max(domeSamplesMax, q.domeSamples);
@@ -1692,6 +1739,13 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
         return SHIRO_OK;
     }
     uint32_t used = std::min<uint32_t>(static_cast<uint32_t>(pl.waves.size()), maxWaves);
+    const bool oneWave = qs.size() == 1 && pl.waves.size() == 1 && used == 1;
+    bool replayOnly = adj && oneWave && kept.valid && kept.epoch == ctx->epoch && kept.P == pl.waves[0].paths &&
+                            kept.depth == pl.maxDepth && kept.lightSamples == lightSamples &&
+                            kept.state == wf->pools[0].state.ptr && kept.log == wf->pools[0].adjLog.ptr &&
+                            same_paths(kept.q, qs[0]);
+    keep = keep && !adj && !recordsOut && oneWave;
+    const bool logs = adj || keep;  // the forward stages log hits and visibility
     // waves in flight at once: pool k runs waves k, k + nl, ... on its own
     // stream (graphs only; the diagnostic per-stage timing runs one)
     const uint32_t nl = cfg.use_graph ? std::max(1u, std::min({cfg.concurrent_waves, used, kMaxConcurrentWaves})) : 1u;
@@ -1699,14 +1753,18 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     for (uint32_t w = 0; w < used; ++w) poolP[w % nl] = std::max(poolP[w % nl], pl.waves[w].paths);
     for (uint32_t k = 0; k < nl; ++k)
         if (!ensure_pool(ctx, &wf->pools[k], poolP[k], lightSamples)) return SHIRO_ERR_OUT_OF_MEMORY;
+    for (uint32_t k = 0; k < nl && logs; ++k)  // each pool's hit / visibility logs
+        if (!ensure_block(ctx, &wf->pools[k].adjLog,
+                          static_cast<size_t>(poolP[k]) * std::max(1u, pl.maxDepth) *
+                              (sizeof(float4) + sizeof(uint32_t) + sizeof(uint8_t)), "adjoint hit log"))
+            return SHIRO_ERR_OUT_OF_MEMORY;
+    // (same sizes as when the wave was kept, so nothing moved; checked all the same)
+    replayOnly = replayOnly && kept.state == wf->pools[0].state.ptr && kept.log == wf->pools[0].adjLog.ptr;
     if (adj) {  // per-slot replay state of each pool, and the parameter view on the device
         for (uint32_t k = 0; k < nl; ++k)
             if (!ensure_block(ctx, &wf->pools[k].adj,
                               static_cast<size_t>(poolP[k]) * (kAdjSlotFloat4 + kAdjLightFloat4 * std::max(1u, lightSamples)) *
-                                  sizeof(float4), "adjoint replay state") ||
-                !ensure_block(ctx, &wf->pools[k].adjLog,
-                              static_cast<size_t>(poolP[k]) * std::max(1u, pl.maxDepth) *
-                                  (sizeof(float4) + sizeof(uint32_t) + sizeof(uint8_t)), "adjoint hit log"))
+                                  sizeof(float4), "adjoint replay state"))
                 return SHIRO_ERR_OUT_OF_MEMORY;
         if (!ensure_block(ctx, &wf->adjView, sizeof(AdjView), "adjoint view")) return SHIRO_ERR_OUT_OF_MEMORY;
         const cudaError_t ce = cudaMemcpyAsync(wf->adjView.ptr, adj, sizeof(AdjView), cudaMemcpyHostToDevice, ctx->stream);
@@ -1756,7 +1814,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.extRegs = cfg.extend_regs ? cfg.extend_regs : 64;
     L.occRegs = cfg.occlude_regs ? cfg.occlude_regs : 64;
     L.occRefill = cfg.occlude_refill == 1 ? 1u : 0u;
-    L.gExt = with_extend_kernel(L.coopExt, L.extRegs, adj != nullptr,
+    L.gExt = with_extend_kernel(L.coopExt, L.extRegs, logs,
                                 [&](auto kern) { return grid_for(kern, L.bExt, wf->smCount); });
     L.shadeRegs = cfg.shade_regs;
     L.ext = ctx->extendedMaterials;
@@ -1800,18 +1858,19 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     // the forward stages' hit / visibility logs of each pool; every hit record
     // starts as a miss, so that a replay ray the forward did not trace (it
     // cannot happen when both follow the same decisions) reads a miss, never
-    // a triangle of another call's scene
+    // a triangle of another call's scene (a kept wave's logs are read as they are)
     auto add_logs = [&](WfView& v, uint32_t k) -> cudaError_t {
-        if (!adj) return cudaSuccess;
+        if (!logs) return cudaSuccess;
         const size_t n = static_cast<size_t>(poolP[k]) * std::max(1u, pl.maxDepth);
         char* b = static_cast<char*>(wf->pools[k].adjLog.ptr);
         v.hitLog = reinterpret_cast<float4*>(b);
         v.gidLog = reinterpret_cast<uint32_t*>(b + n * sizeof(float4));
         v.visLog = reinterpret_cast<uint8_t*>(b + n * (sizeof(float4) + sizeof(uint32_t)));
-        return cudaMemsetAsync(v.hitLog, 0xff, n * sizeof(float4), st);
+        return replayOnly ? cudaSuccess : cudaMemsetAsync(v.hitLog, 0xff, n * sizeof(float4), st);
     };
     if ((e = add_logs(L.v, 0)) != cudaSuccess) return cuda_fail(ctx, e, "adjoint hit log");
     L.aw = adj_wave(0);
+    L.replayOnly = replayOnly ? 1u : 0u;
     Launch lanes[kMaxConcurrentWaves];
     for (uint32_t k = 0; k < nl; ++k) {
         std::memcpy(&lanes[k], &L, sizeof(Launch));  // bytes, padding included: they key the graph cache
@@ -1829,7 +1888,8 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             std::memcpy(&lanes[k].aw, &aw, sizeof(AdjWave));
         }
         // wf_begin adds the stride to the wave index: start one stride below k
-        const uint32_t first = k - nl;
+        // (the replay alone starts at its wave, 0)
+        const uint32_t first = replayOnly ? 0u : k - nl;
         e = cudaMemsetAsync(lanes[k].v.counters, 0, 16 * sizeof(uint32_t), st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(lanes[k].v.counters + 3, &first, 4, cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "wavefront counters");
@@ -1846,14 +1906,22 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
         for (uint32_t k = 0; k < nl && rc == SHIRO_OK; ++k) {
             WavePool& pool = wf->pools[k];
             const unsigned char* key = reinterpret_cast<const unsigned char*>(&lanes[k]);
-            if (pool.exec && pool.execKey.size() == sizeof(Launch) &&
-                std::memcmp(pool.execKey.data(), key, sizeof(Launch)) == 0) {
-                exec[k] = pool.exec;
+            WaveGraph* slot = nullptr;  // the matching graph, else the least recently used slot
+            for (WaveGraph& g : pool.graphs) {
+                if (g.exec && g.key.size() == sizeof(Launch) && std::memcmp(g.key.data(), key, sizeof(Launch)) == 0) {
+                    slot = &g;
+                    break;
+                }
+                if (!slot || (slot->exec && (!g.exec || g.lastUse < slot->lastUse))) slot = &g;
+            }
+            slot->lastUse = ++wf->graphClock;
+            if (slot->exec && slot->key.size() == sizeof(Launch) && std::memcmp(slot->key.data(), key, sizeof(Launch)) == 0) {
+                exec[k] = slot->exec;
                 continue;
             }
-            if (pool.exec) cudaGraphExecDestroy(pool.exec);
-            pool.exec = nullptr;
-            pool.execKey.clear();
+            if (slot->exec) cudaGraphExecDestroy(slot->exec);
+            slot->exec = nullptr;
+            slot->key.clear();
             cudaGraph_t graph = nullptr;
             e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
@@ -1866,8 +1934,8 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
                 exec[k] = nullptr;
                 rc = cuda_fail(ctx, e, "wavefront graph");
             } else {
-                pool.exec = exec[k];
-                pool.execKey.assign(key, key + sizeof(Launch));
+                slot->exec = exec[k];
+                slot->key.assign(key, key + sizeof(Launch));
             }
         }
     }
@@ -1898,8 +1966,11 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             e = cudaGetLastError();
         }
         throttle.after_launch(exec[k] ? lane_stream(k) : st);
-        launches += 3 + 6ull * L.depth + (L.binShadow ? 3ull * L.depth : 0ull) +
-                (L.binRays && L.depth > 1 ? 3ull * (L.depth - 1) : 0ull) + (adj ? 2ull + 5ull * L.depth - 1ull : 0ull);
+        if (replayOnly)
+            launches += 2ull + 5ull * L.depth;
+        else
+            launches += 3 + 6ull * L.depth + (L.binShadow ? 3ull * L.depth : 0ull) +
+                        (L.binRays && L.depth > 1 ? 3ull * (L.depth - 1) : 0ull) + (adj ? 2ull + 5ull * L.depth - 1ull : 0ull);
         ++launchedWaves;
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront launch");
     }
@@ -1937,6 +2008,17 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     ctx->stats.kernel_ms = ms;
     ctx->stats.kernel_launches = launches;
     ctx->stats.paths = paths;
+    if (keep) {
+        KeptWave& kw = wf->kept;
+        kw.valid = true;
+        kw.q = qs[0];
+        kw.epoch = ctx->epoch;
+        kw.P = pl.waves[0].paths;
+        kw.depth = pl.maxDepth;
+        kw.lightSamples = lightSamples;
+        kw.state = wf->pools[0].state.ptr;
+        kw.log = wf->pools[0].adjLog.ptr;
+    }
     if (!ev.empty()) {
         for (int k = 0; k < 6; ++k) {
             ctx->stats.stage_ms[k] = stageMs[k];
@@ -2013,7 +2095,8 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
         ctx->stats.stage_launches[k] = 0;
     }
     uint64_t paths = 0;
-    int rc = run_waves(ctx, wf, wf->cfg, qs, aov, cancel, 0xffffffffu, &paths, nullptr);
+    const bool keep = count == 1 && (reqs[0].flags & SHIRO_RENDER_KEEP_PATHS) != 0;
+    int rc = run_waves(ctx, wf, wf->cfg, qs, aov, cancel, 0xffffffffu, &paths, nullptr, nullptr, nullptr, keep);
     if (rc == SHIRO_ERR_CANCELLED) {
         // a cancelled batch is discarded (RenderParam.cpp:791-798): cleared
         // planes, as FrameBuffer::Clear leaves them (FrameBuffer.cpp:19-24);
@@ -2077,7 +2160,8 @@ void wavefront_free(ContextImpl* ctx) {
     for (cudaStream_t sd : wf->side)
         if (sd) cudaStreamSynchronize(sd);
     for (WavePool& pool : wf->pools) {
-        if (pool.exec) cudaGraphExecDestroy(pool.exec);
+        for (WaveGraph& g : pool.graphs)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
         for (DeviceBlock* b : {&pool.state, &pool.shadow, &pool.queues, &pool.records, &pool.adj, &pool.adjLog})
             if (b->ptr) cudaFree(b->ptr);
     }
@@ -2148,6 +2232,7 @@ int wavefront_set_config(ContextImpl* ctx, const ShiroWavefrontConfig* cfg) {
 int wavefront_autotune(ContextImpl* ctx, const ShiroRenderDesc* req, ShiroWavefrontConfig* chosen) {
     int rc = validate_request(ctx, *req);
     if (rc != SHIRO_OK) return rc;
+    ++ctx->epoch;  // the configuration changes
     WavefrontState* wf = wf_state(ctx);
     std::vector<DevRequest> qs{make_request(*req)};
     const uint64_t px = static_cast<uint64_t>(req->settings.width) * req->settings.height;

@@ -42,6 +42,19 @@ def test_every_declared_symbol_is_exported(lib):
     assert set(names) <= exported
 
 
+def test_constants_match_header():
+    """Every SHIRO_ERR_* and SHIRO_RENDER_* value of the header has the same
+    value in the ctypes mirror."""
+    from shiro_gb300 import abi
+
+    text = open(os.path.join(ROOT, "include", "shiro_gpu.h")).read()
+    found = re.findall(r"^#define SHIRO_(ERR_\w+|RENDER_\w+)\s+\(?(-?(?:0x)?[0-9a-fA-F]+)u?\)?", text, flags=re.M)
+    assert len(found) >= 12
+    for name, value in found:
+        mirror = ("SHIRO_" + name) if name.startswith("ERR_") else name
+        assert getattr(abi, mirror) == int(value, 0), name
+
+
 def test_struct_sizes_match_header():
     from shiro_gb300 import abi
 

@@ -311,3 +311,70 @@ def test_wavefront_replay_equals_per_thread_replay(setup, flags, pool):
         a, b = out[True][k], out[False][k]
         assert a.abs().max() > 0, k
         torch.testing.assert_close(a, b, rtol=1e-3, atol=1e-5 * float(b.abs().max()), msg=k)
+
+
+@pytest.mark.parametrize("flags", [NO_CLAMP, 0])
+def test_kept_forward_wave_replays_alone(setup, flags):
+    """SHIRO_RENDER_KEEP_PATHS: the forward image is unchanged; an adjoint of
+    the same request right after it runs the replay stages alone (2 + 5 x
+    depth launches, + 1 for the environment gradient) and adds the gradients
+    of the full adjoint.  A kept wave serves one call; another render, another
+    sample range, new parameters or a request of several waves in between
+    leave the adjoint on its own forward stages."""
+    from shiro_gb300.abi import RENDER_KEEP_PATHS as KEEP
+
+    gpu, scene, cam, st, p = setup
+    gpu.set_params(**p)
+    gen = torch.Generator(device="cpu").manual_seed(7)
+    d = (torch.rand((st.height, st.width, 4), generator=gen) - 0.3).cuda()
+    d[..., 3] = 0.0
+    replay_only = 2 + 5 * st.max_depth + 1
+
+    def adjoint():
+        g = {k: torch.zeros_like(v) for k, v in p.items()}
+        gpu.adjoint(cam, st, d, g, flags=flags)
+        return g, gpu.last_stats()["kernel_launches"]
+
+    def close(a, b):
+        for k in p:
+            assert b[k].abs().max() > 0, k
+            torch.testing.assert_close(a[k], b[k], rtol=1e-3, atol=1e-5 * float(b[k].abs().max()), msg=k)
+
+    img = gpu.render_device(cam, st, flags=flags, wavefront=True)
+    full, n_full = adjoint()
+    assert n_full > replay_only
+    assert torch.equal(gpu.render_device(cam, st, flags=flags | KEEP, wavefront=True), img)
+    kept, n = adjoint()
+    assert n == replay_only
+    close(kept, full)
+    assert adjoint()[1] == n_full  # consumed by the first adjoint
+
+    gpu.render_device(cam, st, flags=flags | KEEP, wavefront=True)
+    gpu.render_device(cam, st, sample_start=8, flags=flags, wavefront=True)
+    assert adjoint()[1] == n_full
+    gpu.render_device(cam, st, sample_start=8, flags=flags | KEEP, wavefront=True)
+    assert adjoint()[1] == n_full
+
+    base = p["base_color"].clone()
+    base[2] = torch.tensor([0.8, 0.3, 0.1], device="cuda")
+    try:
+        gpu.render_device(cam, st, flags=flags | KEEP, wavefront=True)
+        gpu.set_params(base_color=base)
+        changed, n = adjoint()
+        assert n == n_full
+        gpu.render_device(cam, st, flags=flags | KEEP, wavefront=True)
+        kept, n = adjoint()
+        assert n == replay_only
+        close(kept, changed)
+    finally:
+        gpu.set_params(**p)
+
+    cfg = gpu.wavefront_config()
+    try:
+        gpu.set_wavefront_config(paths_in_flight=4096)
+        assert torch.equal(gpu.render_device(cam, st, flags=flags | KEEP, wavefront=True), img)
+        several, n = adjoint()
+        assert n > replay_only
+        close(several, full)
+    finally:
+        gpu.set_wavefront_config(**cfg)
