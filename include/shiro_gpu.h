@@ -64,17 +64,20 @@ extern "C" {
  * the reference (CpuPathTracer.cpp:63-64) are disabled, in the forward and
  * in the adjoint, so that the rendered estimate is smooth in the parameters. */
 #define SHIRO_RENDER_NO_CLAMP 0x2u
-/* Forward pass of the differentiable form, batched wavefront form only: when
- * the request is the call's only one and its paths fit one pool
- * (ShiroWavefrontConfig.paths_in_flight), its forward stages also log every
- * bounce's hits and light-sample visibility (21 bytes per path and bounce of
- * device memory), and the paths' radiance records and logs stay on the
- * device.  A shiro_gpu_adjoint of the same request (this flag aside) that
+/* Forward pass of the differentiable form, batched wavefront form only
+ * (shiro_gpu_render_batch; the flag of the call's first request decides):
+ * when all the call's paths fit one pool (ShiroWavefrontConfig.
+ * paths_in_flight), the forward stages also log every bounce's hits and
+ * light-sample visibility (21 bytes per path and bounce of device memory),
+ * and the paths' radiance records and logs stay on the device.  A
+ * shiro_gpu_adjoint of one of the call's requests (this flag aside) that
  * follows it, with no wavefront render, adjoint, autotuning, upload,
- * parameter, BVH or configuration change in between, replays them instead of
- * running the forward stages again; otherwise the adjoint runs them as
- * usual.  Images and gradients are the same either way.  Ignored by the
- * plain form. */
+ * parameter, BVH or configuration change in between, replays that
+ * request's paths instead of running the forward stages again; otherwise
+ * the adjoint runs them as usual.  Images and gradients are the same either
+ * way.  (A loss gradient that replays samples independent of the image's
+ * renders both sample ranges in one call, two requests, and the adjoint
+ * takes the second.)  Ignored by the plain form. */
 #define SHIRO_RENDER_KEEP_PATHS 0x4u
 
 /* ---- scene snapshot (shiro/render/Renderer.h:29-133) --------------------- */

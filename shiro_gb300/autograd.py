@@ -7,10 +7,12 @@ per-material base colour [M, 3], roughness [M], metalness [M] and the texels
 wavefront form (or the plain form) after writing the parameters into the
 resident scene; the backward runs the
 adjoint path replay (shiro_gpu_adjoint), which follows every path again from
-its QMC seed.  When the backward replays the forward's own samples, the
-wavefront forward keeps its paths' radiance records and hit / visibility logs
-on the device (SHIRO_RENDER_KEEP_PATHS) and the backward replays them without
-running the forward stages a second time.
+its QMC seed.  The wavefront forward keeps the paths the backward replays on
+the device - their radiance records and hit / visibility logs
+(SHIRO_RENDER_KEEP_PATHS) - so the backward does not run the forward stages
+a second time: its own paths when the backward replays the forward's
+samples, else the replayed sample range, rendered in the same call as a
+second request.
 
 For a loss that is non-linear in the image (an L2 loss), replaying the same
 samples in the backward pass as in the forward one correlates the upstream
@@ -33,9 +35,10 @@ class _Render(torch.autograd.Function):
         tensors = [t.detach().contiguous().float() if t is not None else None
                    for t in (base_color, roughness, metallic, env)]
         backend.set_params(*tensors)
-        keep = RENDER_KEEP_PATHS if wavefront and (adj_start is None or adj_start == sample_start) else 0
-        beauty = backend.render_device(camera, settings, sample_start, settings.samples_per_pixel, flags | keep,
-                                       wavefront=wavefront)
+        also = adj_start if wavefront and adj_start is not None and adj_start != sample_start else None
+        beauty = backend.render_device(camera, settings, sample_start, settings.samples_per_pixel,
+                                       flags | (RENDER_KEEP_PATHS if wavefront else 0), wavefront=wavefront,
+                                       also_start=also)
         ctx.backend = backend
         ctx.camera = camera
         ctx.settings = settings

@@ -408,24 +408,34 @@ class GpuBackend:
         self._params_on_device = tuple(t.detach().clone() if t is not None else o for t, o in zip(send, last))
 
     def render_device(self, camera: Camera, settings: RenderSettings, sample_start: int = 0,
-                      sample_count: Optional[int] = None, flags: int = 0, wavefront: bool = False):
-        """Renders the uploaded scene into CUDA tensors; returns beauty [H,W,4]."""
+                      sample_count: Optional[int] = None, flags: int = 0, wavefront: bool = False,
+                      also_start: Optional[int] = None):
+        """Renders the uploaded scene into CUDA tensors; returns beauty [H,W,4].
+        also_start (wavefront form): the same view's `sample_count` samples
+        from that index are rendered in the same call as a second request
+        (its image is discarded); with RENDER_KEEP_PATHS in flags both
+        requests' paths are kept for an adjoint of either."""
         import torch
 
         from .abi import Aovs
 
         count = settings.samples_per_pixel if sample_count is None else sample_count
         n = settings.width * settings.height
-        planes = [torch.empty(n * c, dtype=torch.float32, device="cuda") for c in (4, 3, 3, 1)]
-        aovs = Aovs(*[C.cast(C.c_void_p(p.data_ptr()), C.POINTER(C.c_float)) for p in planes], 1, 0)
-        req = render_desc(camera, settings, sample_start, count, flags)
+        starts = [sample_start] + ([] if also_start is None else [also_start])
+        nreq = len(starts)
+        planes = [[torch.empty(n * c, dtype=torch.float32, device="cuda") for c in (4, 3, 3, 1)] for _ in starts]
+        aovs = (Aovs * nreq)(*[Aovs(*[C.cast(C.c_void_p(p.data_ptr()), C.POINTER(C.c_float)) for p in pl], 1, 0)
+                               for pl in planes])
+        reqs = (RenderDesc * nreq)(*[render_desc(camera, settings, s, count, flags) for s in starts])
         if wavefront:
-            rc = self.lib.shiro_gpu_render_batch(self._ctx, C.byref(req), 1, None, C.byref(aovs))
+            rc = self.lib.shiro_gpu_render_batch(self._ctx, reqs, nreq, None, aovs)
+        elif nreq == 1:
+            rc = self.lib.shiro_gpu_render(self._ctx, reqs, None, aovs)
         else:
-            rc = self.lib.shiro_gpu_render(self._ctx, C.byref(req), None, C.byref(aovs))
+            raise ValueError("also_start needs the wavefront form")
         if rc != 0:
             raise self._err(rc)
-        return planes[0].view(settings.height, settings.width, 4)
+        return planes[0][0].view(settings.height, settings.width, 4)
 
     def adjoint(self, camera: Camera, settings: RenderSettings, d_beauty, grads: dict, sample_start: int = 0,
                 sample_count: Optional[int] = None, flags: int = 0):

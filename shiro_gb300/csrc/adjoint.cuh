@@ -20,6 +20,7 @@ struct AdjView {
     float* dMetal;
     float4* dEnv4;  // per texel of env0: gradient (rgb, unused), summed into the caller's 3-per-texel array after
     uint32_t distinctEval;  // evalMats differ from the scene's: track the sampling throughput too
+    uint32_t targetReq;     // wavefront replay: the wave's request whose paths are replayed
 };
 
 __device__ __forceinline__ const DevEnv& env_for_eval(const DevScene& s, const AdjView& a, int32_t env) {

@@ -1013,8 +1013,8 @@ __global__ void wa_begin(WfView v) {
     }
 }
 
-// Paths restart from their QMC seed; those whose pixel has a nonzero
-// d_beauty are queued.
+// Paths restart from their QMC seed; those of the adjoint's request (the
+// wave's request a.targetReq) whose pixel has a nonzero d_beauty are queued.
 __global__ void __launch_bounds__(128) wa_generate(WfView v, AdjWave aw) {
     const WaveDesc w = cur_wave(v);
     const AdjView& a = *aw.view;
@@ -1022,8 +1022,9 @@ __global__ void __launch_bounds__(128) wa_generate(WfView v, AdjWave aw) {
     for (uint32_t base = blockIdx.x * blockDim.x; base < w.paths; base += stride) {
         const uint32_t j = base + threadIdx.x;
         bool push = false;
-        if (j < w.paths) {
-            const WaveSeg& sg = find_seg(v, w, j, false);
+        const WaveSeg* sgp = j < w.paths ? &find_seg(v, w, j, false) : nullptr;
+        if (sgp && sgp->req == a.targetReq) {
+            const WaveSeg& sg = *sgp;
             const DevRequest& q = v.reqs[sg.req].q;
             const uint32_t local = j - sg.pathOffset;
             const uint32_t pix = sg.pixelStart + local / q.sampleCount;
@@ -1383,13 +1384,13 @@ struct WavePool {
 constexpr uint32_t kMaxConcurrentWaves = 4;
 
 // A forward render with SHIRO_RENDER_KEEP_PATHS that ran as one wave leaves
-// its path records and hit / visibility logs on pool 0; an adjoint of the
-// same request, before any other wavefront call and any change of scene,
-// parameters or configuration (ContextImpl::epoch), replays them without
-// running the forward stages again.
+// its path records and hit / visibility logs on pool 0; an adjoint of one of
+// its requests, before any other wavefront call and any change of scene,
+// parameters or configuration (ContextImpl::epoch), replays that request's
+// paths of the wave without running the forward stages again.
 struct KeptWave {
     bool valid = false;
-    DevRequest q{};  // SHIRO_RENDER_KEEP_PATHS cleared
+    std::vector<DevRequest> qs;  // the render's requests, in its order
     uint64_t epoch = 0;
     uint32_t P = 0, depth = 0, lightSamples = 0;
     const void* state = nullptr;  // pool 0's blocks when it was kept
@@ -1721,30 +1722,46 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
               const std::vector<AovPtrs>& aovs, const volatile int* cancel, uint32_t maxWaves, uint64_t* pathsOut,
               double* msOut, float4* recordsOut = nullptr, const AdjView* adj = nullptr, bool keep = false) {
     // every call below reuses the pools: a kept wave serves at most the call that follows it
-    const KeptWave kept = wf->kept;
+    KeptWave kept;
+    std::swap(kept, wf->kept);
     wf->kept.valid = false;
-    uint32_t lightSamples = ctx->scene.distantCount;
-    uint32_t domeSamplesMax = 1;
-    for (const DevRequest& q : qs) domeSamplesMax = std::max(domeSamplesMax, q.domeSamples);
-    lightSamples += ctx->scene.domeCount * domeSamplesMax;
-    if (ctx->scene.emissiveCount > 0 && ctx->scene.emissiveSum > 0.0f) lightSamples += 1;
+    // light samples per shading point, pool size and wave plan of a request list
+    uint32_t lightSamples = 0;
+    Plan pl;
+    auto plan_for = [&](const std::vector<DevRequest>& rs) {
+        lightSamples = ctx->scene.distantCount;
+        uint32_t domeSamplesMax = 1, maxSpp = 1;
+        for (const DevRequest& q : rs) {
+            domeSamplesMax = std::max(domeSamplesMax, q.domeSamples);
+            maxSpp = std::max(maxSpp, q.sampleCount);
+        }
+        lightSamples += ctx->scene.domeCount * domeSamplesMax;
+        if (ctx->scene.emissiveCount > 0 && ctx->scene.emissiveSum > 0.0f) lightSamples += 1;
+        pl = plan_waves(rs, std::max(cfg.paths_in_flight, maxSpp));
+    };
+    // an adjoint of one of the kept wave's requests replays that wave (its
+    // plan again: the configuration is unchanged while the epoch is)
+    int32_t target = -1;
+    if (adj && qs.size() == 1 && kept.valid && kept.epoch == ctx->epoch)
+        for (size_t r = 0; r < kept.qs.size() && target < 0; ++r)
+            if (same_paths(kept.qs[r], qs[0])) target = static_cast<int32_t>(r);
+    if (target >= 0) {
+        plan_for(kept.qs);
+        if (pl.waves.size() != 1 || maxWaves < 1 || pl.waves[0].paths != kept.P || pl.maxDepth != kept.depth ||
+            lightSamples != kept.lightSamples || kept.state != wf->pools[0].state.ptr || kept.log != wf->pools[0].adjLog.ptr)
+            target = -1;
+    }
+    bool replayOnly = target >= 0;
+    const std::vector<DevRequest>& rqs = replayOnly ? kept.qs : qs;  // the requests the tables describe
+    if (!replayOnly) plan_for(qs);
     if (lightSamples > kMaxLightSamples)
         return fail(ctx, SHIRO_ERR_UNSUPPORTED_SCENE, "wavefront form: more than 8 light samples per shading point");
-    uint32_t maxSpp = 1;
-    for (const DevRequest& q : qs) maxSpp = std::max(maxSpp, q.sampleCount);
-    const uint32_t P = std::max(cfg.paths_in_flight, maxSpp);
-    Plan pl = plan_waves(qs, P);
     if (pl.waves.empty()) {
         *pathsOut = 0;
         return SHIRO_OK;
     }
     uint32_t used = std::min<uint32_t>(static_cast<uint32_t>(pl.waves.size()), maxWaves);
-    const bool oneWave = qs.size() == 1 && pl.waves.size() == 1 && used == 1;
-    bool replayOnly = adj && oneWave && kept.valid && kept.epoch == ctx->epoch && kept.P == pl.waves[0].paths &&
-                            kept.depth == pl.maxDepth && kept.lightSamples == lightSamples &&
-                            kept.state == wf->pools[0].state.ptr && kept.log == wf->pools[0].adjLog.ptr &&
-                            same_paths(kept.q, qs[0]);
-    keep = keep && !adj && !recordsOut && oneWave;
+    keep = keep && !adj && !recordsOut && pl.waves.size() == 1 && used == 1;
     const bool logs = adj || keep;  // the forward stages log hits and visibility
     // waves in flight at once: pool k runs waves k, k + nl, ... on its own
     // stream (graphs only; the diagnostic per-stage timing runs one)
@@ -1760,6 +1777,8 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             return SHIRO_ERR_OUT_OF_MEMORY;
     // (same sizes as when the wave was kept, so nothing moved; checked all the same)
     replayOnly = replayOnly && kept.state == wf->pools[0].state.ptr && kept.log == wf->pools[0].adjLog.ptr;
+    if (target >= 0 && !replayOnly) return fail(ctx, SHIRO_ERR_CUDA, "kept wave moved");  // not reached: sizes are equal
+    AdjView adjCopy;  // (pageable source of an asynchronous copy: staged before the call returns)
     if (adj) {  // per-slot replay state of each pool, and the parameter view on the device
         for (uint32_t k = 0; k < nl; ++k)
             if (!ensure_block(ctx, &wf->pools[k].adj,
@@ -1767,7 +1786,9 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
                                   sizeof(float4), "adjoint replay state"))
                 return SHIRO_ERR_OUT_OF_MEMORY;
         if (!ensure_block(ctx, &wf->adjView, sizeof(AdjView), "adjoint view")) return SHIRO_ERR_OUT_OF_MEMORY;
-        const cudaError_t ce = cudaMemcpyAsync(wf->adjView.ptr, adj, sizeof(AdjView), cudaMemcpyHostToDevice, ctx->stream);
+        adjCopy = *adj;
+        adjCopy.targetReq = replayOnly ? static_cast<uint32_t>(target) : 0u;
+        const cudaError_t ce = cudaMemcpyAsync(wf->adjView.ptr, &adjCopy, sizeof(AdjView), cudaMemcpyHostToDevice, ctx->stream);
         if (ce != cudaSuccess) return cuda_fail(ctx, ce, "adjoint view");
     }
     if (nl > 1 && !wf->fork) {
@@ -1780,9 +1801,10 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
         if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&wf->join[k - 1], cudaEventDisableTiming);
         if (ce != cudaSuccess) return cuda_fail(ctx, ce, "wavefront side stream");
     }
-    // tables: waves, segments, requests
-    std::vector<WfRequest> rq(qs.size());
-    for (size_t r = 0; r < qs.size(); ++r) rq[r] = WfRequest{qs[r], aovs[r]};
+    // tables: waves, segments, requests (the replay of a kept wave writes no AOVs)
+    std::vector<WfRequest> rq(rqs.size());
+    for (size_t r = 0; r < rqs.size(); ++r)
+        rq[r] = WfRequest{rqs[r], replayOnly ? AovPtrs{nullptr, nullptr, nullptr, nullptr} : aovs[r]};
     const size_t tb = pl.waves.size() * sizeof(WaveDesc) + pl.segs.size() * sizeof(WaveSeg) + rq.size() * sizeof(WfRequest) + 256;
     if (!ensure_block(ctx, &wf->tables, tb, "wavefront tables")) return SHIRO_ERR_OUT_OF_MEMORY;
     char* t = static_cast<char*>(wf->tables.ptr);
@@ -2011,7 +2033,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     if (keep) {
         KeptWave& kw = wf->kept;
         kw.valid = true;
-        kw.q = qs[0];
+        kw.qs = qs;
         kw.epoch = ctx->epoch;
         kw.P = pl.waves[0].paths;
         kw.depth = pl.maxDepth;
@@ -2095,7 +2117,7 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
         ctx->stats.stage_launches[k] = 0;
     }
     uint64_t paths = 0;
-    const bool keep = count == 1 && (reqs[0].flags & SHIRO_RENDER_KEEP_PATHS) != 0;
+    const bool keep = count >= 1 && (reqs[0].flags & SHIRO_RENDER_KEEP_PATHS) != 0;
     int rc = run_waves(ctx, wf, wf->cfg, qs, aov, cancel, 0xffffffffu, &paths, nullptr, nullptr, nullptr, keep);
     if (rc == SHIRO_ERR_CANCELLED) {
         // a cancelled batch is discarded (RenderParam.cpp:791-798): cleared

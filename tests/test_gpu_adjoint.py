@@ -242,21 +242,28 @@ def test_adjoint_agrees_with_plain_renderer_fd(setup):
         assert abs(adj - fd) <= 0.1 * abs(fd), (name, i, adj, fd)
 
 
-def test_autograd_function(setup):
+@pytest.mark.parametrize("adj_start", [None, 8])
+def test_autograd_function(setup, adj_start):
+    """The autograd binding's gradients equal a direct adjoint of the loss
+    gradient, with the backward replaying the forward's samples (its kept
+    paths) or an independent sample range (rendered and kept by the forward
+    call as a second request)."""
     gpu, scene, cam, st, p = setup
     from shiro_gb300.autograd import render
 
     params = {k: v.clone().requires_grad_(True) for k, v in p.items()}
     target = torch.rand((st.height, st.width, 3), generator=torch.Generator().manual_seed(3)).cuda()
     img = render(gpu, cam, st, params["base_color"], params["roughness"], params["metallic"], params["env"],
-                 flags=NO_CLAMP)
+                 flags=NO_CLAMP, adjoint_sample_start=adj_start)
+    assert torch.equal(img, gpu.render_device(cam, st, flags=NO_CLAMP))
     loss = ((img[..., :3] - target) ** 2).mean()
     loss.backward()
+    assert gpu.last_stats()["kernel_launches"] == 2 + 5 * st.max_depth + 1  # the kept paths replayed
     d = torch.zeros_like(img)
     d[..., :3] = 2.0 * (img[..., :3].detach() - target) / target.numel()
     grads = {k: torch.zeros_like(v) for k, v in p.items()}
     gpu.set_params(**p)
-    gpu.adjoint(cam, st, d, grads, flags=NO_CLAMP)
+    gpu.adjoint(cam, st, d, grads, sample_start=adj_start or 0, flags=NO_CLAMP)
     for k in p:
         torch.testing.assert_close(params[k].grad, grads[k], rtol=1e-4, atol=1e-7)
 
@@ -318,9 +325,11 @@ def test_kept_forward_wave_replays_alone(setup, flags):
     """SHIRO_RENDER_KEEP_PATHS: the forward image is unchanged; an adjoint of
     the same request right after it runs the replay stages alone (2 + 5 x
     depth launches, + 1 for the environment gradient) and adds the gradients
-    of the full adjoint.  A kept wave serves one call; another render, another
-    sample range, new parameters or a request of several waves in between
-    leave the adjoint on its own forward stages."""
+    of the full adjoint; so does an adjoint of either request of a kept
+    two-request call (an image and an independent sample range, as a
+    decorrelated gradient renders them).  A kept wave serves one call;
+    another render, another sample range, new parameters or a request of
+    several waves in between leave the adjoint on its own forward stages."""
     from shiro_gb300.abi import RENDER_KEEP_PATHS as KEEP
 
     gpu, scene, cam, st, p = setup
@@ -330,9 +339,9 @@ def test_kept_forward_wave_replays_alone(setup, flags):
     d[..., 3] = 0.0
     replay_only = 2 + 5 * st.max_depth + 1
 
-    def adjoint():
+    def adjoint(start=0):
         g = {k: torch.zeros_like(v) for k, v in p.items()}
-        gpu.adjoint(cam, st, d, g, flags=flags)
+        gpu.adjoint(cam, st, d, g, sample_start=start, flags=flags)
         return g, gpu.last_stats()["kernel_launches"]
 
     def close(a, b):
@@ -348,6 +357,16 @@ def test_kept_forward_wave_replays_alone(setup, flags):
     assert n == replay_only
     close(kept, full)
     assert adjoint()[1] == n_full  # consumed by the first adjoint
+
+    full8, n = adjoint(8)
+    assert n == n_full
+    for first in (True, False):  # two requests kept: the adjoint of either replays alone
+        pair = gpu.render_device(cam, st, flags=flags | KEEP, wavefront=True, also_start=8)
+        assert torch.equal(pair, img)
+        kept, n = adjoint(0 if first else 8)
+        assert n == replay_only
+        close(kept, full if first else full8)
+        assert adjoint(8)[1] == n_full
 
     gpu.render_device(cam, st, flags=flags | KEEP, wavefront=True)
     gpu.render_device(cam, st, sample_start=8, flags=flags, wavefront=True)
