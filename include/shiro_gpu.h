@@ -397,6 +397,24 @@ typedef struct ShiroWavefrontConfig {
 } ShiroWavefrontConfig;
 int shiro_gpu_get_wavefront_config(const ShiroGpuContext* ctx, ShiroWavefrontConfig* out);
 int shiro_gpu_set_wavefront_config(ShiroGpuContext* ctx, const ShiroWavefrontConfig* cfg);
+/* Told that pixels [first_pixel, first_pixel + pixel_count) of request
+ * `request` (its index in the call) are final in that request's AOV planes. */
+typedef void (*ShiroPixelsReady)(void* user, uint32_t request, uint64_t first_pixel, uint64_t pixel_count);
+
+/* shiro_gpu_render_batch that reports finished pixel ranges while later
+ * waves still render, so that a caller can consume them (copy a frame out,
+ * say) during the render: `ready` is called on the calling thread before
+ * the call returns.  Planes the device writes in place (device planes, or
+ * page-locked host planes mapped at the same address) are reported wave by
+ * wave as each wave finishes; other host planes, and requests without
+ * samples, whole once their planes are written.  Of a call that succeeds
+ * every pixel of every request is reported exactly once, the ranges of one
+ * request in increasing order; a call that fails or is cancelled stops
+ * reporting (ranges reported before held final values; a cancelled call
+ * then clears its planes).  `ready` must not call into this context. */
+int shiro_gpu_render_batch_ready(ShiroGpuContext* ctx, const ShiroRenderDesc* requests, uint32_t count,
+                                 const volatile int* cancel, ShiroAovs* outs, ShiroPixelsReady ready, void* user);
+
 /* Times candidate configurations on `request` and keeps the fastest. */
 int shiro_gpu_autotune(ShiroGpuContext* ctx, const ShiroRenderDesc* request, ShiroWavefrontConfig* chosen);
 

@@ -32,6 +32,9 @@ RENDER_ENV_CDF = 0x1
 RENDER_NO_CLAMP = 0x2
 RENDER_KEEP_PATHS = 0x4
 
+# ShiroPixelsReady(user, request, first_pixel, pixel_count)
+PixelsReady = C.CFUNCTYPE(None, C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64)
+
 F3 = C.c_float * 3
 
 

@@ -82,6 +82,7 @@ def load_library(path: str = LIB_PATH):
         "shiro_gpu_upload_scene": ([_P, _P], C.c_int),
         "shiro_gpu_render": ([_P, _P, _P, _P], C.c_int),
         "shiro_gpu_render_batch": ([_P, _P, _U, _P, _P], C.c_int),
+        "shiro_gpu_render_batch_ready": ([_P, _P, _U, _P, _P, abi.PixelsReady, _P], C.c_int),
         "shiro_gpu_get_wavefront_config": ([_P, _P], C.c_int),
         "shiro_gpu_set_wavefront_config": ([_P, _P], C.c_int),
         "shiro_gpu_autotune": ([_P, _P, _P], C.c_int),
@@ -249,10 +250,12 @@ class GpuBackend:
 
     # -- wavefront ---------------------------------------------------------
     def render_batch(self, scene: Scene, requests: Sequence[tuple], flags: int = 0,
-                     cancel: Optional[C.c_int] = None, outs_fb: Optional[Sequence[FrameBuffer]] = None
-                     ) -> List[FrameBuffer]:
+                     cancel: Optional[C.c_int] = None, outs_fb: Optional[Sequence[FrameBuffer]] = None,
+                     ready=None) -> List[FrameBuffer]:
         """requests: (camera, settings[, sample_start[, sample_count]]);
-        outs_fb: frame buffers to fill (reused across calls), else new ones."""
+        outs_fb: frame buffers to fill (reused across calls), else new ones;
+        ready(request, first_pixel, pixel_count): told of finished pixel
+        ranges during the render (shiro_gpu_render_batch_ready)."""
         self.upload_scene(scene)
         n = len(requests)
         descs = (RenderDesc * max(1, n))()
@@ -266,7 +269,12 @@ class GpuBackend:
             fb = outs_fb[i] if outs_fb is not None else FrameBuffer(st.width, st.height)
             fbs.append(fb)
             outs[i] = fb.aovs()
-        rc = self.lib.shiro_gpu_render_batch(self._ctx, descs, n, C.byref(cancel) if cancel is not None else None, outs)
+        flag = C.byref(cancel) if cancel is not None else None
+        if ready is None:
+            rc = self.lib.shiro_gpu_render_batch(self._ctx, descs, n, flag, outs)
+        else:
+            cb = abi.PixelsReady(lambda user, r, first, count: ready(r, first, count))
+            rc = self.lib.shiro_gpu_render_batch_ready(self._ctx, descs, n, flag, outs, cb, None)
         if rc != 0:
             raise self._err(rc)
         return fbs

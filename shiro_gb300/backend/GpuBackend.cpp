@@ -7,6 +7,7 @@
 #include <cstring>
 #include <limits>
 #include <exception>
+#include <functional>
 #include <thread>
 #include <vector>
 
@@ -197,18 +198,20 @@ ShiroAovs FrameAovs(FrameBuffer& fb) {
 
 bool Cancelled(const std::atomic<bool>* c) { return c && c->load(std::memory_order_relaxed); }
 
-// Copies the staged planes (beauty 4, albedo 3, normal 3, depth 1 floats per
-// pixel, back to back) into the frame's own, on several host threads for a
-// large frame.
-void CopyOut(const float* stage, FrameBuffer& fb, size_t px) {
+// Copies pixels [first, first + count) of the staged planes (beauty 4,
+// albedo 3, normal 3, depth 1 floats per pixel, plane after plane, px pixels
+// each) into the frame's own, on several host threads for a large range.
+void CopyOut(const float* stage, FrameBuffer& fb, size_t px, size_t first, size_t count) {
     const ShiroAovs dst = FrameAovs(fb);
     struct Plane {
         const float* src;
         float* dst;
         size_t n;
     };
-    const Plane planes[4] = {{stage, dst.beauty, 4 * px}, {stage + 4 * px, dst.albedo, 3 * px},
-                             {stage + 7 * px, dst.normal, 3 * px}, {stage + 10 * px, dst.depth, px}};
+    const Plane planes[4] = {{stage + 4 * first, dst.beauty + 4 * first, 4 * count},
+                             {stage + 4 * px + 3 * first, dst.albedo + 3 * first, 3 * count},
+                             {stage + 7 * px + 3 * first, dst.normal + 3 * first, 3 * count},
+                             {stage + 10 * px + first, dst.depth + first, count}};
     const unsigned threads = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
     auto part = [&](unsigned t, unsigned of) {
         for (const Plane& p : planes) {
@@ -216,7 +219,7 @@ void CopyOut(const float* stage, FrameBuffer& fb, size_t px) {
             if (b > a) std::memcpy(p.dst + a, p.src + a, (b - a) * sizeof(float));
         }
     };
-    if (threads == 1 || 11 * px < (size_t{1} << 20)) {
+    if (threads == 1 || 11 * count < (size_t{1} << 20)) {
         part(0, 1);
         return;
     }
@@ -224,6 +227,20 @@ void CopyOut(const float* stage, FrameBuffer& fb, size_t px) {
     for (unsigned t = 1; t < threads; ++t) pool.emplace_back(part, t, threads);
     part(0, threads);
     for (std::thread& th : pool) th.join();
+}
+
+// shiro_gpu_render_batch_ready's callback of RenderSampleBatch: each finished
+// range goes from the staging into the frame while later waves render.
+struct StagedFrame {
+    const float* stage;
+    FrameBuffer* frame;
+    size_t px;
+    std::function<bool()> ready;  // the frame is sized and cleared (false: that failed)
+};
+
+void CopyFinished(void* user, uint32_t, uint64_t first, uint64_t count) {
+    StagedFrame& f = *static_cast<StagedFrame*>(user);
+    if (f.ready()) CopyOut(f.stage, *f.frame, f.px, first, count);
 }
 
 }  // namespace
@@ -306,8 +323,9 @@ render::FrameBuffer GpuBackend::RenderSampleBatch(const RenderRequest& request) 
     std::scoped_lock lock(mutex_);
     // The returned frame is sized and cleared (a 1080p one is 91 MB of fresh
     // pages) on a helper thread while the device renders into page-locked
-    // staging, which the render writes in place; the planes are then copied
-    // over on several threads.
+    // staging, which the render writes in place; each wave's pixels are
+    // copied over (on several threads) as soon as the wave has finished,
+    // while the next ones render.
     std::exception_ptr failure;  // an allocation failure reaches the caller as before
     std::thread prepare([&frame, &failure, w, h] {
         try {
@@ -317,9 +335,12 @@ render::FrameBuffer GpuBackend::RenderSampleBatch(const RenderRequest& request) 
             failure = std::current_exception();
         }
     });
-    auto prepared = [&] {
+    auto joined = [&] {
         if (prepare.joinable()) prepare.join();
-        if (failure) std::rethrow_exception(failure);
+        return !failure;
+    };
+    auto prepared = [&] {
+        if (!joined()) std::rethrow_exception(failure);
     };
     if (!EnsureRuntime(request.scene)) {
         prepared();
@@ -340,7 +361,9 @@ render::FrameBuffer GpuBackend::RenderSampleBatch(const RenderRequest& request) 
     int rc;
     {
         CancelForward cancel(request.cancel);
-        rc = shiro_gpu_render_batch(ctx_, &desc, 1, cancel.Flag(), &aovs);
+        StagedFrame staged{stage, &frame, px, joined};
+        rc = stage ? shiro_gpu_render_batch_ready(ctx_, &desc, 1, cancel.Flag(), &aovs, CopyFinished, &staged)
+                   : shiro_gpu_render_batch(ctx_, &desc, 1, cancel.Flag(), &aovs);
     }
     lastStatus_ = rc;
     prepared();
@@ -354,7 +377,6 @@ render::FrameBuffer GpuBackend::RenderSampleBatch(const RenderRequest& request) 
         frame.Clear();
         return frame;
     }
-    if (stage) CopyOut(stage, frame, px);
     return frame;
 }
 

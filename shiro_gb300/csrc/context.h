@@ -150,8 +150,10 @@ struct LaunchThrottle {
 void static_scratch_setup(ContextImpl* ctx);
 
 // wavefront.cu / adjoint.cu
+// ready (may be null): told of each request's finished pixel ranges while
+// later waves render (shiro_gpu_render_batch_ready).
 int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t count, const volatile int* cancel,
-                     ShiroAovs* outs);
+                     ShiroAovs* outs, ShiroPixelsReady ready = nullptr, void* user = nullptr);
 void wavefront_free(ContextImpl* ctx);
 // Every path of one request by the wavefront form, its record (radiance,
 // first-hit depth) written to out[path] in request path order (pixel-major,

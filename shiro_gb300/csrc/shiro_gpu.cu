@@ -1403,6 +1403,13 @@ int shiro_gpu_render_batch(ShiroGpuContext* handle, const ShiroRenderDesc* reqs,
     return wavefront_render(&handle->impl, reqs, count, cancel, outs);
 }
 
+int shiro_gpu_render_batch_ready(ShiroGpuContext* handle, const ShiroRenderDesc* reqs, uint32_t count,
+                                 const volatile int* cancel, ShiroAovs* outs, ShiroPixelsReady ready, void* user) {
+    if (!handle || !ready || (count && (!reqs || !outs))) return SHIRO_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(handle->impl.device);
+    return wavefront_render(&handle->impl, reqs, count, cancel, outs, ready, user);
+}
+
 int shiro_gpu_get_wavefront_config(const ShiroGpuContext* ctx, ShiroWavefrontConfig* out) {
     if (!ctx || !out) return SHIRO_ERR_INVALID_ARGUMENT;
     return wavefront_get_config(&ctx->impl, out);

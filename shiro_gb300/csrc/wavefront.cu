@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <functional>
 #include <vector>
 
 #include "adjoint.cuh"
@@ -1717,10 +1718,14 @@ bool same_paths(DevRequest a, DevRequest b) {
 // `cfg`.  maxWaves limits the waves run (autotuning); returns paths traced.
 // adj: run the adjoint replay after each wave's forward stages (or alone,
 // over a kept forward wave of the same request); keep: log the forward
-// stages of a one-wave render and keep its pool for such an adjoint.
+// stages of a one-wave render and keep its pool for such an adjoint;
+// waveDone: called on this thread with each wave's segments once the wave
+// has finished on the device, in wave order (not after a failure or cancel).
+using WaveDone = std::function<void(const WaveSeg* segs, uint32_t count)>;
 int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& cfg, const std::vector<DevRequest>& qs,
               const std::vector<AovPtrs>& aovs, const volatile int* cancel, uint32_t maxWaves, uint64_t* pathsOut,
-              double* msOut, float4* recordsOut = nullptr, const AdjView* adj = nullptr, bool keep = false) {
+              double* msOut, float4* recordsOut = nullptr, const AdjView* adj = nullptr, bool keep = false,
+              const WaveDone* waveDone = nullptr) {
     // every call below reuses the pools: a kept wave serves at most the call that follows it
     KeptWave kept;
     std::swap(kept, wf->kept);
@@ -1975,6 +1980,32 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     // with a cancel flag, nl + 1 waves are queued at most, so the flag is read
     // between waves that ran (a wave takes milliseconds, a launch microseconds)
     LaunchThrottle throttle(cancel, nl + 1);
+    // an event after each wave tells the caller of its finished pixels
+    struct Events {
+        std::vector<cudaEvent_t> ev;
+        ~Events() {
+            for (cudaEvent_t x : ev)
+                if (x) cudaEventDestroy(x);
+        }
+    } waveEv;
+    if (waveDone && rc == SHIRO_OK) {
+        waveEv.ev.assign(used, nullptr);
+        for (cudaEvent_t& x : waveEv.ev)
+            if (rc == SHIRO_OK && (e = cudaEventCreateWithFlags(&x, cudaEventDisableTiming)) != cudaSuccess)
+                rc = cuda_fail(ctx, e, "wave events");
+    }
+    uint32_t delivered = 0;
+    auto deliver = [&](bool wait) {  // the finished waves, in order
+        while (waveDone && rc == SHIRO_OK && delivered < launchedWaves) {
+            const cudaError_t q = wait ? cudaEventSynchronize(waveEv.ev[delivered]) : cudaEventQuery(waveEv.ev[delivered]);
+            if (q != cudaSuccess) {
+                if (q != cudaErrorNotReady) rc = cuda_fail(ctx, q, "wavefront render");
+                return;
+            }
+            const WaveDesc& wd = pl.waves[delivered++];
+            (*waveDone)(pl.segs.data() + wd.segBegin, wd.segCount);
+        }
+    };
     for (uint32_t w = 0; w < used && rc == SHIRO_OK; ++w) {
         if (!throttle.before_launch()) {
             rc = fail(ctx, SHIRO_ERR_CANCELLED, "cancelled");
@@ -1987,6 +2018,7 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
             enqueue_wave_timed(L, st, ev);
             e = cudaGetLastError();
         }
+        if (waveDone && e == cudaSuccess) e = cudaEventRecord(waveEv.ev[w], exec[k] ? lane_stream(k) : st);
         throttle.after_launch(exec[k] ? lane_stream(k) : st);
         if (replayOnly)
             launches += 2ull + 5ull * L.depth;
@@ -1995,7 +2027,9 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
                         (L.binRays && L.depth > 1 ? 3ull * (L.depth - 1) : 0ull) + (adj ? 2ull + 5ull * L.depth - 1ull : 0ull);
         ++launchedWaves;
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "wavefront launch");
+        deliver(false);
     }
+    deliver(true);
     for (uint32_t k = 1; k < nl; ++k) {  // join (also after a failed launch: side work must end before we return)
         cudaEventRecord(wf->join[k - 1], wf->side[k - 1]);
         cudaStreamWaitEvent(st, wf->join[k - 1], 0);
@@ -2066,7 +2100,7 @@ static bool device_writable_host(const void* p) {
 }
 
 int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t count, const volatile int* cancel,
-                     ShiroAovs* outs) {
+                     ShiroAovs* outs, ShiroPixelsReady ready, void* user) {
     if (!ctx->hasScene) return fail(ctx, SHIRO_ERR_NO_SCENE, "no scene uploaded");
     WavefrontState* wf = wf_state(ctx);
     std::vector<DevRequest> qs(count);
@@ -2118,7 +2152,18 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
     }
     uint64_t paths = 0;
     const bool keep = count >= 1 && (reqs[0].flags & SHIRO_RENDER_KEEP_PATHS) != 0;
-    int rc = run_waves(ctx, wf, wf->cfg, qs, aov, cancel, 0xffffffffu, &paths, nullptr, nullptr, nullptr, keep);
+    // planes the resolve stage writes in place are reported wave by wave,
+    // the others (staged, or cleared for want of samples) whole at the end
+    auto in_place = [&](uint32_t r) {
+        return (outs[r].on_device || direct[r]) && reqs[r].sample_count > 0 &&
+               static_cast<uint64_t>(reqs[r].settings.width) * reqs[r].settings.height > 0;
+    };
+    const WaveDone onWave = [&](const WaveSeg* segs, uint32_t n) {
+        for (uint32_t i = 0; i < n; ++i)
+            if (in_place(segs[i].req)) ready(user, segs[i].req, segs[i].pixelStart, segs[i].pixelCount);
+    };
+    int rc = run_waves(ctx, wf, wf->cfg, qs, aov, cancel, 0xffffffffu, &paths, nullptr, nullptr, nullptr, keep,
+                       ready ? &onWave : nullptr);
     if (rc == SHIRO_ERR_CANCELLED) {
         // a cancelled batch is discarded (RenderParam.cpp:791-798): cleared
         // planes, as FrameBuffer::Clear leaves them (FrameBuffer.cpp:19-24);
@@ -2155,6 +2200,10 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
     const cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "AOV readback");
     ctx->stats.device_bytes = ctx->deviceBytes();
+    for (uint32_t r = 0; r < count && ready; ++r) {
+        const uint64_t px = static_cast<uint64_t>(reqs[r].settings.width) * reqs[r].settings.height;
+        if (px && !in_place(r)) ready(user, r, 0, px);
+    }
     return SHIRO_OK;
 }
 

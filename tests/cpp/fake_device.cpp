@@ -133,6 +133,17 @@ int shiro_gpu_render_batch(ShiroGpuContext* ctx, const ShiroRenderDesc* reqs, ui
     return SHIRO_OK;
 }
 
+int shiro_gpu_render_batch_ready(ShiroGpuContext* ctx, const ShiroRenderDesc* reqs, uint32_t count,
+                                 const volatile int* cancel, ShiroAovs* outs, ShiroPixelsReady ready, void* user) {
+    const int rc = shiro_gpu_render_batch(ctx, reqs, count, cancel, outs);
+    if (rc != SHIRO_OK) return rc;
+    for (uint32_t r = 0; r < count; ++r) {
+        const uint64_t px = static_cast<uint64_t>(reqs[r].settings.width) * reqs[r].settings.height;
+        if (px) ready(user, r, 0, px);
+    }
+    return SHIRO_OK;
+}
+
 // The device accumulator is not part of what the Renderer calls.
 int shiro_gpu_accum_create(ShiroGpuContext*, ShiroAccumulator**) { return SHIRO_ERR_UNSUPPORTED_SCENE; }
 void shiro_gpu_accum_destroy(ShiroAccumulator*) {}

@@ -103,6 +103,58 @@ def test_page_locked_planes_written_in_place(gpu, pool):
         gpu.set_wavefront_config(**base)
 
 
+@pytest.mark.parametrize("pool", [0, 4096])
+def test_ready_ranges_cover_every_pixel_once(gpu, pool):
+    """shiro_gpu_render_batch_ready reports every pixel of every request once,
+    the ranges of a request in increasing order: page-locked planes wave by
+    wave (several ranges with a pool of 4 096 paths), pageable planes and a
+    request without samples whole after the render.  A range of page-locked
+    planes already holds its final values when it is reported, and the
+    frames equal the plain ones bit for bit."""
+    from shiro_gb300 import scenes
+    from shiro_gb300.abi import FrameBuffer
+
+    w = scenes.sphere_workload(37, 23, 6, 6, env_width=64, env_height=32)
+    w2 = scenes.sphere_workload(64, 48, 4, 8, env_width=64, env_height=32)
+    plain = gpu.render(w.scene, w.camera, w.settings)
+    plain2 = gpu.render(w.scene, w2.camera, w2.settings)
+    fbs = [FrameBuffer(37, 23, pinned=True), FrameBuffer(64, 48), FrameBuffer(64, 48, pinned=True),
+           FrameBuffer(37, 23, pinned=True)]
+    reqs = [(w.camera, w.settings), (w2.camera, w2.settings), (w2.camera, w2.settings), (w.camera, w.settings, 0, 0)]
+    refs = [plain, plain2, plain2, None]
+    seen, final_when_reported = [], []
+
+    def ready(r, first, count):
+        seen.append((r, first, count))
+        if r in (0, 2):  # page-locked planes written in place
+            got = fbs[r].beauty[first:first + count].view(np.uint32)
+            final_when_reported.append(np.array_equal(got, refs[r].beauty[first:first + count].view(np.uint32)))
+
+    base = gpu.wavefront_config()
+    if pool:
+        gpu.set_wavefront_config(paths_in_flight=pool, concurrent_waves=2)
+    try:
+        outs = gpu.render_batch(w.scene, reqs, outs_fb=fbs, ready=ready)
+    finally:
+        gpu.set_wavefront_config(**base)
+    assert final_when_reported and all(final_when_reported)
+    for r, fb in enumerate(outs):
+        pos = 0
+        for rr, first, count in seen:
+            if rr == r:
+                assert first == pos and count > 0, (r, first, pos)
+                pos += count
+        assert pos == fb.width * fb.height, r
+    count = [sum(1 for x in seen if x[0] == r) for r in range(4)]
+    assert count[1] == 1 and count[3] == 1
+    if pool:
+        assert count[0] > 1 and count[2] > 1
+    for fb, ref in zip(outs[:3], refs[:3]):
+        ok, k, n = same(ref, fb)
+        assert ok, (pool, k, n)
+    assert not outs[3].beauty.any() and np.isinf(outs[3].depth).all()
+
+
 def test_mixed_dome_samples_in_batch(gpu):
     """Requests of one batch with different dome-sample counts each use their
     own light samples."""
