@@ -6,6 +6,11 @@ on the data path: rank r renders the pixels' samples
 frame buffers are combined once at the end, host-staged (device-to-host copy,
 gather to rank 0 over a CPU process group, accumulation on the host).
 
+The differentiable form shards the same way: each rank renders and replays
+its own sample range, the whole job's image is the ranks' images weighted by
+their sample counts (`allreduce_image`), and one host-staged all-reduce of
+the gradient buffers per step sums the ranks' adjoints (`replica_gradient`).
+
 The combination is the reference's progressive accumulation
 (Renderer::FrameAccumulator, src/render/Renderer.cpp:47-110) applied to the
 ranks' frames in rank order: beauty / albedo / normal weighted by the sample
@@ -124,3 +129,60 @@ def combine(fb: FrameBuffer, sample_count: int, group=None, dst: int = 0):
         return None
     frames: List[FrameBuffer] = [_from_planes(g, fb.width, fb.height) for g in gathered]
     return accumulate(frames, [int(c.item()) for c in counts])
+
+
+def _host_allreduce(flat, group=None):
+    """Sums a flat float32 tensor over the ranks of `group` (a CPU-capable
+    process group), staged through host memory; returns it on its device."""
+    import torch.distributed as dist
+
+    host = flat.detach().to("cpu", copy=True)
+    dist.all_reduce(host, op=dist.ReduceOp.SUM, group=group)
+    return host.to(flat.device)
+
+
+def allreduce_image(beauty, sample_count: int, total: int, group=None):
+    """The whole job's image on every rank: this rank's image (the mean of
+    its `sample_count` samples) weighted by sample_count / total and summed
+    over the ranks.  Returns a tensor shaped and placed like `beauty`."""
+    w = float(sample_count) / float(total) if total else 0.0
+    return _host_allreduce((beauty.float() * w).reshape(-1), group).reshape(beauty.shape)
+
+
+def allreduce_gradients(grads: dict, group=None) -> dict:
+    """Sums every rank's gradient tensors in place: all groups in one
+    host-staged all-reduce (the one exchange of a replica step)."""
+    import torch
+
+    keys = [k for k in sorted(grads) if grads[k] is not None]
+    if not keys:
+        return grads
+    flat = torch.cat([grads[k].detach().reshape(-1).float() for k in keys])
+    flat = _host_allreduce(flat, group)
+    off = 0
+    for k in keys:
+        n = grads[k].numel()
+        grads[k].copy_(flat[off:off + n].reshape(grads[k].shape))
+        off += n
+    return grads
+
+
+def replica_gradient(backend, camera, settings, d_beauty, grads: dict, group=None, sample_start: int = 0,
+                     sample_count=None, flags: int = 0) -> dict:
+    """Adds the adjoint of the whole job's image into `grads` on every rank
+    (as one adjoint over all samples adds it): this rank replays its sample
+    range (`sample_range`) with d_beauty weighted by its share of the
+    samples, so each path carries d_beauty / total, into zeroed buffers; the
+    ranks' buffers are summed (`allreduce_gradients`) and added to `grads`."""
+    import torch
+    import torch.distributed as dist
+
+    total = settings.samples_per_pixel if sample_count is None else sample_count
+    first, count = sample_range(dist.get_rank(group), dist.get_world_size(group), sample_start, total)
+    local = {k: torch.zeros_like(v) for k, v in grads.items() if v is not None}
+    if count:
+        backend.adjoint(camera, settings, d_beauty * (float(count) / float(total)), local, first, count, flags)
+    allreduce_gradients(local, group)
+    for k, v in local.items():
+        grads[k] += v
+    return grads
