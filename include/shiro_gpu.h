@@ -335,7 +335,9 @@ void shiro_hdri_free(float* pixels);
  * geometry equals the resident scene's (mesh positions, normals, indices and
  * material indices, the material count, the BVH build setting), the BVHs and
  * per-triangle records are kept and only what derives from materials, lights
- * and environments is replaced. */
+ * and environments is replaced.  A scene without triangles is accepted and
+ * renders as the CPU tracer renders it: every ray misses (the environment,
+ * unoccluded lights). */
 int shiro_gpu_upload_scene(ShiroGpuContext* ctx, const ShiroSceneDesc* scene);
 
 /* FrameBuffer RenderSampleBatch(const RenderRequest&)

@@ -54,6 +54,7 @@ struct ContextImpl {
     std::vector<ShiroMaterialDesc> materialsHost;
     uint32_t materialCount = 0;        // user materials (the default one follows)
     bool extendedMaterials = false;    // transmission, opacity or emission present (the adjoint rejects them)
+    bool noGeometry = false;           // the scene has no triangles (the BVHs hold two that nothing hits)
     uint32_t bvhDepth = 0, bvhMaxLeaf = 0;
     const float4* nodes8 = nullptr;   // wide BVH (kept even while the binary one is selected)
     const float4* tris8 = nullptr;    // triangles in the wide BVH's leaf order

@@ -864,7 +864,7 @@ int finish_upload(ContextImpl* ctx) {
     ctx->hasScene = true;
     ctx->stats = ShiroRenderStats{};
     ctx->stats.bvh_nodes = s.nodes8 ? ctx->node8Count : s.nodeCount;
-    ctx->stats.triangles = s.triCount;
+    ctx->stats.triangles = ctx->noGeometry ? 0u : s.triCount;
     ctx->stats.bvh_depth = s.nodes8 ? ctx->bvh8Depth : ctx->bvhDepth;
     ctx->stats.bvh_max_leaf = ctx->bvhMaxLeaf;
     ctx->stats.device_bytes = ctx->deviceBytes();
@@ -1057,7 +1057,21 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene exceeds 2^28 triangles");
     if (sd->material_count >= kShadeNormals)
         return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene exceeds 2^31 - 1 materials");
-    if (ttotal == 0) return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "scene has no triangles");
+    // A scene without triangles renders its lights and environment alone, as
+    // the CPU tracer does (every ray misses).  The builders get two zero-area
+    // triangles, each collapsed onto one of two points, in a mesh after the
+    // caller's with the default material: the triangle test rejects them for
+    // every ray (det = 0), so nothing can hit or occlude.
+    const bool noGeometry = ttotal == 0;
+    static const float kPointPos[18] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 1};
+    static const uint32_t kPointIdx[6] = {0, 1, 2, 3, 4, 5};
+    if (noGeometry) {
+        fm.push_back(FlatMesh{0, 6, 0, 2, 0, 0, sd->material_count, 0});
+        vtotal = 6;
+        ttotal = 2;
+        itotal = 6;
+    }
+    ctx->noGeometry = noGeometry;
     std::vector<float> pos3(3 * vtotal), nrm3(3 * std::max<size_t>(ntotal, 1));
     std::vector<uint32_t> idx(std::max<size_t>(itotal, 1));
     for (uint32_t i = 0; i < sd->mesh_count; ++i) {
@@ -1065,6 +1079,10 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
         if (m.vertex_count) std::memcpy(&pos3[3 * static_cast<size_t>(fm[i].vbase)], m.positions, 12ull * m.vertex_count);
         if (fm[i].hasN) std::memcpy(&nrm3[3 * static_cast<size_t>(fm[i].nbase)], m.normals, 12ull * m.vertex_count);
         if (m.index_count) std::memcpy(&idx[fm[i].ibase], m.indices, 4ull * m.index_count);
+    }
+    if (noGeometry) {
+        std::memcpy(pos3.data(), kPointPos, sizeof(kPointPos));
+        std::memcpy(idx.data(), kPointIdx, sizeof(kPointIdx));
     }
     struct Temps {  // device scratch of the upload
         std::vector<void*> p;
@@ -1111,7 +1129,8 @@ int shiro_gpu_upload_scene(ShiroGpuContext* handle, const ShiroSceneDesc* sd) {
     const unsigned gv = static_cast<unsigned>(std::min<size_t>((vtotal + 255) / 256, 4096));
     const unsigned gt = static_cast<unsigned>(std::min<size_t>((ttotal + 255) / 256, 8192));
     if (vtotal) k_flat_verts<<<gv, 256, 0, ctx->stream>>>(dPos3, static_cast<uint32_t>(vtotal), dPos4, dRed + 6);
-    k_flat_tris<<<gt, 256, 0, ctx->stream>>>(dMeshes, sd->mesh_count, dPos3, dNrm3, dIdx, static_cast<uint32_t>(ttotal),
+    k_flat_tris<<<gt, 256, 0, ctx->stream>>>(dMeshes, static_cast<uint32_t>(fm.size()), dPos3, dNrm3, dIdx,
+                                            static_cast<uint32_t>(ttotal),
                                             dTriVerts, dShade, dAllTri, dBoxes, dRed, dRed + 7);
     uint32_t red[8];
     ce = cudaGetLastError();

@@ -179,9 +179,31 @@ def test_errors_are_reported(gpu):
     bad = Scene(materials=[], meshes=[Mesh(np.zeros((3, 3), np.float32), np.array([0, 1, 5], np.uint32))])
     with pytest.raises(ShiroGpuError):
         gpu.upload_scene(bad, force=True)
-    empty = Scene()
-    with pytest.raises(ShiroGpuError):
-        gpu.upload_scene(empty, force=True)
+
+
+@pytest.mark.parametrize("kind", ["no_meshes", "empty_meshes"])
+def test_scene_without_triangles_renders_the_environment(gpu, port, kind):
+    """A scene without triangles (no meshes, or meshes without indices) is
+    rendered as the CPU tracer renders it: every ray misses, so the frame is
+    the environment (and nothing occludes the lights); plain and wavefront
+    forms alike, and the scene reports no triangles."""
+    from shiro_gb300 import scenes
+    from shiro_gb300.abi import Mesh, Scene
+
+    w = scenes.sphere_workload(24, 16, 4, 4, env_width=32, env_height=16)
+    meshes = [] if kind == "no_meshes" else [Mesh(np.zeros((3, 3), np.float32), np.zeros(0, np.uint32), None, 0)]
+    sc = Scene(materials=w.scene.materials, meshes=meshes, dome_lights=w.scene.dome_lights,
+               distant_lights=w.scene.distant_lights)
+    ref = api.render(port, sc, w.camera, w.settings, 0, 4)
+    for flags in (1, 0):
+        fb = gpu.render(sc, w.camera, w.settings, 0, 4, flags=flags)
+        assert gpu.last_stats()["triangles"] == 0
+        (wave,) = gpu.render_batch(sc, [(w.camera, w.settings, 0, 4)], flags=flags)
+        assert np.array_equal(wave.beauty.view(np.uint32), fb.beauty.view(np.uint32))
+        frac, mean = frame_match(fb, ref)
+        assert frac >= MIN_MATCH and mean <= MEAN_TOL, (flags, frac, mean)
+        assert np.isinf(fb.depth).all() and not fb.albedo.any() and not fb.normal.any()
+        assert not fb.beauty[:, 3].any()
 
 
 def test_cancel(gpu):
