@@ -409,7 +409,7 @@ typedef void (*ShiroPixelsReady)(void* user, uint32_t request, uint64_t first_pi
  * the call returns.  Planes the device writes in place (device planes, or
  * page-locked host planes mapped at the same address) are reported wave by
  * wave as each wave finishes; other host planes, and requests without
- * samples, whole once their planes are written.  Of a call that succeeds
+ * samples or bounces, whole once their planes are written.  Of a call that succeeds
  * every pixel of every request is reported exactly once, the ranges of one
  * request in increasing order; a call that fails or is cancelled stops
  * reporting (ranges reported before held final values; a cancelled call

@@ -2117,7 +2117,8 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
             return fail(ctx, SHIRO_ERR_INVALID_ARGUMENT, "null AOV pointer");
         qs[r] = make_request(reqs[r]);
         const uint64_t px = static_cast<uint64_t>(reqs[r].settings.width) * reqs[r].settings.height;
-        direct[r] = !outs[r].on_device && px > 0 && reqs[r].sample_count > 0 && device_writable_host(outs[r].beauty) &&
+        direct[r] = !outs[r].on_device && px > 0 && reqs[r].sample_count > 0 && reqs[r].settings.max_depth > 0 &&
+                    device_writable_host(outs[r].beauty) &&
                     device_writable_host(outs[r].albedo) && device_writable_host(outs[r].normal) &&
                     device_writable_host(outs[r].depth);
         if (!outs[r].on_device && !direct[r]) stagingFloats += 11ull * px;
@@ -2134,8 +2135,10 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
             aov[r] = AovPtrs{b, b + 4 * px, b + 7 * px, b + 10 * px};
             off += 11 * px;
         }
-        // requests without samples get cleared planes (FrameBuffer::Clear)
-        if (reqs[r].sample_count == 0 || px == 0) {
+        // requests without samples or bounces (the waves hold no paths of
+        // them) get cleared planes (FrameBuffer::Clear), what TracePath
+        // leaves them with
+        if (reqs[r].sample_count == 0 || px == 0 || reqs[r].settings.max_depth == 0) {
             cudaMemsetAsync(aov[r].beauty, 0, px * 16, ctx->stream);
             cudaMemsetAsync(aov[r].albedo, 0, px * 12, ctx->stream);
             cudaMemsetAsync(aov[r].normal, 0, px * 12, ctx->stream);
@@ -2155,7 +2158,7 @@ int wavefront_render(ContextImpl* ctx, const ShiroRenderDesc* reqs, uint32_t cou
     // planes the resolve stage writes in place are reported wave by wave,
     // the others (staged, or cleared for want of samples) whole at the end
     auto in_place = [&](uint32_t r) {
-        return (outs[r].on_device || direct[r]) && reqs[r].sample_count > 0 &&
+        return (outs[r].on_device || direct[r]) && reqs[r].sample_count > 0 && reqs[r].settings.max_depth > 0 &&
                static_cast<uint64_t>(reqs[r].settings.width) * reqs[r].settings.height > 0;
     };
     const WaveDone onWave = [&](const WaveSeg* segs, uint32_t n) {

@@ -169,6 +169,35 @@ def test_single_pixel_and_odd_sizes(gpu, port):
         assert frac >= 0.9 and mean < 0.05
 
 
+@pytest.mark.parametrize("depths", [(0, 0, 0), (1, 1, 1), (4, 0, 4), (4, 4, 0), (3, 1, 0)])
+def test_depth_limits(gpu, port, depths):
+    """max / diffuse / specular depth limits, zero included (TracePath then
+    traces nothing and the frame is cleared): plain and wavefront forms (into
+    device staging and into page-locked planes) match the port."""
+    import dataclasses
+
+    from shiro_gb300 import scenes
+    from shiro_gb300.abi import FrameBuffer
+
+    w = scenes.sphere_workload(24, 16, 4, 4, env_width=32, env_height=16)
+    md, dd, sd = depths
+    st = dataclasses.replace(w.settings, max_depth=md, diffuse_depth=dd, specular_depth=sd)
+    ref = api.render(port, w.scene, w.camera, st, 0, 4)
+    fb = gpu.render(w.scene, w.camera, st, 0, 4, flags=1)
+    frac, mean = frame_match(fb, ref)
+    assert frac >= MIN_MATCH and mean <= MEAN_TOL, (frac, mean)
+    assert np.array_equal(np.isfinite(fb.depth), np.isfinite(ref.depth))
+    for pinned in (False, True):
+        outs = [FrameBuffer(24, 16, pinned=pinned)]
+        for p in (outs[0].beauty, outs[0].albedo, outs[0].normal, outs[0].depth):
+            p[...] = 7.0  # stale values the render must overwrite
+        (wave,) = gpu.render_batch(w.scene, [(w.camera, st, 0, 4)], flags=1, outs_fb=outs)
+        for k in ("beauty", "albedo", "normal", "depth"):
+            assert np.array_equal(getattr(wave, k).view(np.uint32), getattr(fb, k).view(np.uint32)), (pinned, k)
+    if md == 0:
+        assert not fb.beauty.any() and not fb.albedo.any() and not fb.normal.any() and np.isinf(fb.depth).all()
+
+
 def test_errors_are_reported(gpu):
     from shiro_gb300 import ShiroGpuError, scenes
     from shiro_gb300.abi import Mesh, Scene
