@@ -429,7 +429,10 @@ int shiro_gpu_autotune(ShiroGpuContext* ctx, const ShiroRenderDesc* request, Shi
  * shiro_gpu_adjoint replays every path of `request` from its QMC seed and
  * accumulates d(sum over pixels of d_beauty . beauty)/d(param) into the
  * gradient buffers (added, not overwritten).  All pointers are device
- * pointers; any may be NULL to skip that parameter group. */
+ * pointers; any may be NULL to skip that parameter group.  Scenes with
+ * emitters and opacity cut-outs are covered; a scene with a transmission
+ * weight on any material is refused (SHIRO_ERR_UNSUPPORTED_SCENE), as by
+ * shiro_gpu_render_frozen. */
 int shiro_gpu_set_params(ShiroGpuContext* ctx, const float* base_color, const float* roughness,
                          const float* metallic, const float* env_rgb);
 int shiro_gpu_adjoint(ShiroGpuContext* ctx, const ShiroRenderDesc* request, const float* d_beauty,

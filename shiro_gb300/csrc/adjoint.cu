@@ -78,6 +78,14 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
             break;
         }
         const Vertex v = make_vertex(s, ps.ro, ps.rd, h);
+        // an opacity cut-out the path passes through (no media: transmission
+        // is refused) - the hit is not shaded; a partly opaque hit that is
+        // shaded scales the throughput by 1 / opacity, the sampling one too
+        if (s.extended) {
+            if (!enter_hit(s, smp, depth, v, h.t, ps)) continue;
+            const float op = sclamp(s.materials[v.hit.material].opacity, 0.0f, 1.0f);
+            if (op < 0.999f) Ts = Ts / smax(op, 1.0e-4f);
+        }
         const Mat& me = a.evalMats[v.hit.material];
         const Mat& ms = s.materials[v.hit.material];
         // the scene's materials have their BSDF records on the device; values
@@ -87,17 +95,32 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
             return a.distinctEval ? bsdf_eval(me, v.n, v.cn, v.view, l) : bsdf_eval_rec(rec, ms, v.n, v.cn, v.view, l);
         };
         if (depth == 0) depth0 = h.t;
+        if (s.extended) {
+            // emitted radiance at this hit: no parameter scales it here, and
+            // no later BSDF value does either
+            const V3 before = ps.radiance;
+            add_emission(s, v, depth, ps);
+            if (kGrad) Lrem = Lrem - (ps.radiance - before);
+        }
         const V3 origin = shadow_origin(v);
         // light samples, in sum_direct's order
         const V3 dT = delta * ps.T;
-        const V3 direct = sum_direct<false>(s, q, [&](uint32_t k, V3* c) {
+        const uint32_t firstEmissive = s.distantCount + s.domeCount * q.domeSamples;
+        const V3 direct = sum_direct<true>(s, q, [&](uint32_t k, V3* c) {
             V3 ld, L;
             V3 Ls;  // the radiance under the sampling (scene) parameters: the clamp's scale comes from it
             float w;
+            float reach = FLT_MAX;
             int32_t envIdx = -1;
             V3 local{0.0f, 0.0f, 0.0f};
             V3 domeRad{0.0f, 0.0f, 0.0f};
-            if (k < s.distantCount) {
+            if (k >= firstEmissive) {  // the emissive-triangle sample (emission is not a parameter)
+                float lp, nl;
+                if (!emissive_geometry(s, v, smp, depth, &ld, &L, &lp, &nl, &reach)) return false;
+                Ls = L;
+                const float bp = bsdf_pdf_rec(rec, ms, v.w, v.n, v.cn, v.view, ld);
+                w = nl * power_heuristic(lp, bp) / lp;
+            } else if (k < s.distantCount) {
                 const DevDistant l = s.distant[k];
                 ld = normalize(l.direction * -1.0f);
                 const float nl = sclamp(dot(v.n, ld), 0.0f, 1.0f);
@@ -135,7 +158,7 @@ __device__ __noinline__ V3 adj_path(const DevScene& s, const DevRequest& q, cons
                 const float mis = power_heuristic(lp, bp);
                 w = nl * mis / lp;
             }
-            if (trace_occluded(s, origin, ld, FLT_MAX, ctr)) return false;
+            if (trace_occluded(s, origin, ld, reach, ctr)) return false;
             const V3 f = evalE(ld);
             const V3 raw = f * L * w;
             if (a.distinctEval) {
@@ -361,9 +384,9 @@ int adjoint_set_params(ContextImpl* ctx, const float* base, const float* rough, 
 
 int adjoint_run(ContextImpl* ctx, const ShiroRenderDesc* req, const float* dBeauty, float* dBase, float* dRough, float* dMetal,
                 float* dEnv) {
-    if (ctx->hasScene && ctx->extendedMaterials)
+    if (ctx->hasScene && ctx->transmissiveMaterials)
         return fail(ctx, SHIRO_ERR_UNSUPPORTED_SCENE,
-                    "the differentiable form covers reflecting materials only (no transmission, opacity or emission)");
+                    "the differentiable form covers reflecting, emitting and cut-out materials (no transmission)");
     int rc = validate_request(ctx, *req);
     if (rc != SHIRO_OK) return rc;
     const DevRequest q = make_request(*req);
@@ -450,9 +473,9 @@ void adjoint_free(ContextImpl* ctx) {
 
 int adjoint_render_frozen(ContextImpl* ctx, const ShiroRenderDesc* req, const float* base, const float* rough,
                           const float* metal, const float* env, float* beauty) {
-    if (ctx->hasScene && ctx->extendedMaterials)
+    if (ctx->hasScene && ctx->transmissiveMaterials)
         return fail(ctx, SHIRO_ERR_UNSUPPORTED_SCENE,
-                    "the differentiable form covers reflecting materials only (no transmission, opacity or emission)");
+                    "the differentiable form covers reflecting, emitting and cut-out materials (no transmission)");
     int rc = validate_request(ctx, *req);
     if (rc != SHIRO_OK) return rc;
     AdjointState* st = adj_state(ctx);

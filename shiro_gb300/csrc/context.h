@@ -53,7 +53,8 @@ struct ContextImpl {
     std::vector<int32_t> domeEnv;      // dome -> env index
     std::vector<ShiroMaterialDesc> materialsHost;
     uint32_t materialCount = 0;        // user materials (the default one follows)
-    bool extendedMaterials = false;    // transmission, opacity or emission present (the adjoint rejects them)
+    bool extendedMaterials = false;    // transmission, opacity or emission present
+    bool transmissiveMaterials = false;  // transmission present (the adjoint rejects it)
     bool noGeometry = false;           // the scene has no triangles (the BVHs hold two that nothing hits)
     uint32_t bvhDepth = 0, bvhMaxLeaf = 0;
     const float4* nodes8 = nullptr;   // wide BVH (kept even while the binary one is selected)

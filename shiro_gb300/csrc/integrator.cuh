@@ -242,11 +242,12 @@ __device__ __forceinline__ V3 sum_direct(const DevScene& s, const DevRequest& q,
     return out;
 }
 
-// The emissive-triangle sample (:1578-1628); its shadow ray stops short of
-// the light (*maxDist).
-template <typename Ctr>
-__device__ __forceinline__ bool light_emissive(const DevScene& s, const DevRequest& q, const Vertex& v, const Sampler& smp,
-                                               uint32_t depth, V3* dir, V3* c, float* maxDist, Ctr& ctr) {
+// The emissive-triangle sample's geometry (:1578-1616): the point picked on
+// an emitter, its direction *ld from the vertex, the emitted radiance *le,
+// the sample's solid-angle pdf *lp, the cosine *nl at the vertex and the
+// reach of its shadow ray, which stops short of the light.
+__device__ __forceinline__ bool emissive_geometry(const DevScene& s, const Vertex& v, const Sampler& smp, uint32_t depth,
+                                                  V3* ld, V3* le, float* lp, float* nl, float* maxDist) {
     if (!has_emitters(s)) return false;
     const uint32_t db = kEmissiveDimBase + depth * kEmissiveDepthStride;
     const uint32_t k = sample_emitter(s, smp.next1d(db + 0u));
@@ -265,14 +266,27 @@ __device__ __forceinline__ bool light_emissive(const DevScene& s, const DevReque
     const float d2 = dot(to, to);
     if (d2 <= 1.0e-10f) return false;
     const float dist = sqrtf(d2);
-    const V3 ld = to / dist;
-    const float nl = sclamp(dot(v.n, ld), 0.0f, 1.0f);
-    const float cosL = fabsf(dot(f4xyz(e2), ld * -1.0f));
-    if (nl <= 0.0f || cosL <= 0.0f) return false;
+    *ld = to / dist;
+    *nl = sclamp(dot(v.n, *ld), 0.0f, 1.0f);
+    const float cosL = fabsf(dot(f4xyz(e2), *ld * -1.0f));
+    if (*nl <= 0.0f || cosL <= 0.0f) return false;
     const float sel = e0.y / s.emissiveSum;
     const float areaPdf = sel / smax(e0.x, 1.0e-6f);
-    const float lp = areaPdf * d2 / smax(cosL, 1.0e-6f);
-    if (lp <= 0.0f) return false;
+    *lp = areaPdf * d2 / smax(cosL, 1.0e-6f);
+    if (*lp <= 0.0f) return false;
+    *le = f4xyz(e1);
+    *maxDist = smax(dist - 2.0f * kRayEpsilon, kRayEpsilon);
+    return true;
+}
+
+// The emissive-triangle sample (:1578-1628); its shadow ray stops short of
+// the light (*maxDist).
+template <typename Ctr>
+__device__ __forceinline__ bool light_emissive(const DevScene& s, const DevRequest& q, const Vertex& v, const Sampler& smp,
+                                               uint32_t depth, V3* dir, V3* c, float* maxDist, Ctr& ctr) {
+    V3 ld, le;
+    float lp, nl;
+    if (!emissive_geometry(s, v, smp, depth, &ld, &le, &lp, &nl, maxDist)) return false;
     const Mat& m = s.materials[v.hit.material];
     ctr.bsdf_pdf();
     ctr.bsdf_eval();
@@ -280,8 +294,7 @@ __device__ __forceinline__ bool light_emissive(const DevScene& s, const DevReque
     const float bp = bsdf_pdf_rec(rec, m, v.w, v.n, v.cn, v.view, ld);
     const float mis = power_heuristic(lp, bp);
     *dir = ld;
-    *maxDist = smax(dist - 2.0f * kRayEpsilon, kRayEpsilon);
-    *c = clamp24(q, bsdf_eval_rec(rec, m, v.n, v.cn, v.view, ld) * f4xyz(e1) * (nl * mis / lp));
+    *c = clamp24(q, bsdf_eval_rec(rec, m, v.n, v.cn, v.view, ld) * le * (nl * mis / lp));
     return true;
 }
 

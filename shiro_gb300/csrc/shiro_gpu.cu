@@ -81,32 +81,6 @@ ShiroMaterialDesc default_material() {  // PbrMaterial defaults, Renderer.h:56-1
 }
 
 inline float hclamp(float v, float lo, float hi) { return v < lo ? lo : (hi < v ? hi : v); }
-inline float hmax(float a, float b) { return a < b ? b : a; }
-
-// TransmissionSampleWeight > 0 (CpuPathTracer.cpp:1391-1403), evaluated with
-// the reference's arithmetic.
-bool has_transmission(const ShiroMaterialDesc& m) {
-    const float tr = hclamp(m.transmission, 0.0f, 1.0f);
-    const float metal = hclamp(m.metallic, 0.0f, 1.0f);
-    if (tr <= 0.0f || metal >= 0.999f) return false;
-    auto f0d = [](float ior) {
-        const float s = hmax(ior, 1.0f);
-        const float r = (s - 1.0f) / (s + 1.0f);
-        return r * r;
-    };
-    const float ca = hclamp(m.coat_affect_color * m.coat_weight, 0.0f, 1.0f);
-    float best = 0.0f;
-    for (int k = 0; k < 3; ++k) {
-        const float tint = 1.0f * (1.0f - ca) + hclamp(m.coat_color[k], 0.0f, 1.0f) * ca;
-        const float cf0 = m.coat_color[k] * (hclamp(m.coat_weight, 0.0f, 1.0f) * f0d(m.coat_ior));
-        const float uc = tint * hclamp(1.0f - cf0, 0.0f, 1.0f);
-        const float d = m.specular_color[k] * (hclamp(m.specular_weight, 0.0f, 1.0f) * f0d(m.ior));
-        const float sf0 = d * (1.0f - metal) + m.base_color[k] * metal;
-        const float ub = hclamp(1.0f - sf0, 0.0f, 1.0f);
-        best = hmax(best, hclamp(m.transmission_color[k], 0.0f, 1.0f) * uc * ub);
-    }
-    return hmax(0.0f, best) * tr * (1.0f - metal) > 0.0f;
-}
 
 }  // namespace
 
@@ -811,11 +785,17 @@ int upload_shading(ContextImpl* ctx, const ShiroSceneDesc* sd) {
         if ((rc = upload(ctx, emissiveCdf, &s.emissiveCdf, "emissive weights")) != SHIRO_OK) return rc;
         if ((rc = upload(ctx, emissiveOf, &s.emissiveOf, "emissive index")) != SHIRO_OK) return rc;
     }
+    // A transmission weight, whatever base colour and metalness make of it
+    // (they are parameters shiro_gpu_set_params may change; with a zero
+    // sample weight the extended stages give the reflecting ones' values).
     ctx->extendedMaterials = false;
+    ctx->transmissiveMaterials = false;
     for (uint32_t i = 0; i < sd->material_count; ++i) {
         const ShiroMaterialDesc& m = sd->materials[i];
-        if (has_transmission(m) || hclamp(m.opacity, 0.0f, 1.0f) < 0.999f || m.emission_strength > 0.0f)
+        const bool transmissive = hclamp(m.transmission, 0.0f, 1.0f) > 0.0f;
+        if (transmissive || hclamp(m.opacity, 0.0f, 1.0f) < 0.999f || m.emission_strength > 0.0f)
             ctx->extendedMaterials = true;
+        if (transmissive) ctx->transmissiveMaterials = true;
     }
     s.extended = ctx->extendedMaterials ? 1u : 0u;
     if ((rc = upload(ctx, ctx->materialsHost, &s.materials, "materials")) != SHIRO_OK) return rc;

@@ -1109,7 +1109,12 @@ __device__ __forceinline__ bool wa_light(const DevScene& s, const DevRequest& q,
     float w;
     int32_t envIdx = -1;
     *local = V3{0.0f, 0.0f, 0.0f};
-    if (k < s.distantCount) {
+    if (k >= s.distantCount + s.domeCount * q.domeSamples) {  // the emissive-triangle sample
+        float lp, nl, reach;
+        if (!emissive_geometry(s, vx, smp, depth, ld, &L, &lp, &nl, &reach)) return false;
+        const float bp = bsdf_pdf_rec(rec, ms, vx.w, vx.n, vx.cn, vx.view, *ld);
+        w = nl * power_heuristic(lp, bp) / lp;
+    } else if (k < s.distantCount) {
         const DevDistant l = s.distant[k];
         *ld = normalize(l.direction * -1.0f);
         const float nl = sclamp(dot(vx.n, *ld), 0.0f, 1.0f);
@@ -1196,13 +1201,27 @@ __global__ void __launch_bounds__(128) wa_shade(WfView v, DevScene s, AdjWave aw
             aw.vtx[3 * static_cast<size_t>(j) + 1] = make_float4(vx.cn.x, vx.cn.y, vx.cn.z, 0.0f);
             aw.vtx[3 * static_cast<size_t>(j) + 2] = make_float4(vx.view.x, vx.view.y, vx.view.z, 0.0f);
             const Sampler smp{id.x, id.y, id.z};
-            const uint32_t nls = light_sample_count<false>(s, q);
+            // an opacity cut-out the path passes through (the forward's decision;
+            // no media, transmission being refused): the hit is not shaded
+            const bool shaded = !s.extended || enter_hit(s, smp, depth, vx, h.t, ps);
+            if (shaded && s.extended) {
+                // radiance emitted at this hit: no BSDF value of this vertex or a
+                // later one scales it, so it leaves the radiance still to come
+                ps.radiance = V3{0.0f, 0.0f, 0.0f};
+                add_emission(s, vx, depth, ps);
+                if (ps.radiance.x != 0.0f || ps.radiance.y != 0.0f || ps.radiance.z != 0.0f) {
+                    const float4 l4 = aw.lrem[j];
+                    aw.lrem[j] = make_float4(l4.x - ps.radiance.x, l4.y - ps.radiance.y, l4.z - ps.radiance.z, 0.0f);
+                }
+            }
+            const uint32_t nls = light_sample_count<true>(s, q);
             // which samples the forward stages found taken and unoccluded at this vertex
-            const uint32_t seen = v.visLog[static_cast<size_t>(depth) * v.P + j];
+            const uint32_t seen = shaded ? v.visLog[static_cast<size_t>(depth) * v.P + j] : 0u;
             for (uint32_t k = 0; k < nls; ++k) {
-                V3 ld{0.0f, 0.0f, 0.0f}, c{0.0f, 0.0f, 0.0f}, gL{0.0f, 0.0f, 0.0f}, gE{0.0f, 0.0f, 0.0f}, local;
+                V3 ld{0.0f, 0.0f, 0.0f}, c{0.0f, 0.0f, 0.0f}, gL{0.0f, 0.0f, 0.0f}, gE{0.0f, 0.0f, 0.0f},
+                    local{0.0f, 0.0f, 0.0f};
                 bool mark = false;
-                const bool ok = wa_light(s, q, a, vx, smp, depth, k, rec, ms, &ld, &c, &gL, &gE, &local, &mark);
+                const bool ok = shaded && wa_light(s, q, a, vx, smp, depth, k, rec, ms, &ld, &c, &gL, &gE, &local, &mark);
                 const size_t e = static_cast<size_t>(k) * v.P + j;
                 v.shDir[e] = make_float4(ld.x, ld.y, ld.z, (ok && ((seen >> k) & 1u)) ? FLT_MAX : 0.0f);
                 v.shC[e] = make_float4(c.x, c.y, c.z, 0.0f);
@@ -1211,13 +1230,18 @@ __global__ void __launch_bounds__(128) wa_shade(WfView v, DevScene s, AdjWave aw
                 aw.lgrad[3 * e + 2] = make_float4(local.x, local.y, local.z, 0.0f);
             }
             v.shT[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, 0.0f);
-            // continuation (the reflecting lobes of continue_path)
-            bool alive = false, due = false;
+            // continuation (the reflecting lobes of continue_path); past a cut-out
+            // the ray goes on unchanged, with no BSDF value to differentiate
+            bool alive = false, due = false, pass = false;
             V3 next{0.0f, 0.0f, 0.0f}, f{0.0f, 0.0f, 0.0f};
             const uint32_t base = depth * kPathDimStride;
             const float rw = vx.w.diffuse + vx.w.spec + vx.w.coat;
             const float tw = rw + 0.0f;
             do {
+                if (!shaded) {
+                    pass = depth + 1u < q.maxDepth;
+                    break;
+                }
                 if (tw <= 0.0f) break;
                 const float sel = smp.next1d(base + 1u) * tw;
                 const V2 ds = smp.next2d(base + 2u);
@@ -1269,7 +1293,7 @@ __global__ void __launch_bounds__(128) wa_shade(WfView v, DevScene s, AdjWave aw
             } while (false);
             aw.cont[2 * static_cast<size_t>(j)] = make_float4(next.x, next.y, next.z, due ? 1.0f : 0.0f);
             aw.cont[2 * static_cast<size_t>(j) + 1] = make_float4(f.x, f.y, f.z, 0.0f);
-            if (due) {
+            if (due || pass) {
                 v.T[j] = make_float4(ps.T.x, ps.T.y, ps.T.z, __uint_as_float(pack_state(ps)));
                 v.ro[j] = make_float4(ps.ro.x, ps.ro.y, ps.ro.z, 0.0f);
                 v.rd[j] = make_float4(ps.rd.x, ps.rd.y, ps.rd.z, ps.prevPdf);
@@ -1295,7 +1319,7 @@ __global__ void __launch_bounds__(128, 4) wa_shadow(WfView v, DevScene s, AdjWav
         const uint32_t mat = __float_as_uint(v0.w);
         const Mat& me = a.evalMats[mat];
         const V3 dT = dl * T0;
-        const V3 direct = sum_direct<false>(s, q, [&](uint32_t k, V3* c) {
+        const V3 direct = sum_direct<true>(s, q, [&](uint32_t k, V3* c) {
             const size_t e = static_cast<size_t>(k) * v.P + j;
             const float4 d4 = v.shDir[e];
             if (d4.w == 0.0f) return false;
