@@ -1101,7 +1101,9 @@ __global__ void __launch_bounds__(256) wa_hits(WfView v, uint32_t cur, uint32_t 
 // Light sample k of a vertex with the factors of its gradient: its clamped
 // contribution c, gL = L w s (material gradient = delta T gL . df) and
 // gE = f R w s (texel gradient of dome 0's texture = delta T gE at `local`),
-// with s the clamp scale held constant.
+// with s the clamp scale held constant.  kExt: the scene has emitters or
+// cut-outs (the replay stages are compiled for each kind of scene).
+template <bool kExt>
 __device__ __forceinline__ bool wa_light(const DevScene& s, const DevRequest& q, const AdjView& a, const Vertex& vx,
                                          const Sampler& smp, uint32_t depth, uint32_t k, const float4* rec, const Mat& ms,
                                          V3* ld, V3* c, V3* gL, V3* gE, V3* local, bool* envMark) {
@@ -1109,7 +1111,7 @@ __device__ __forceinline__ bool wa_light(const DevScene& s, const DevRequest& q,
     float w;
     int32_t envIdx = -1;
     *local = V3{0.0f, 0.0f, 0.0f};
-    if (k >= s.distantCount + s.domeCount * q.domeSamples) {  // the emissive-triangle sample
+    if (kExt && k >= s.distantCount + s.domeCount * q.domeSamples) {  // the emissive-triangle sample
         float lp, nl, reach;
         if (!emissive_geometry(s, vx, smp, depth, ld, &L, &lp, &nl, &reach)) return false;
         const float bp = bsdf_pdf_rec(rec, ms, vx.w, vx.n, vx.cn, vx.view, *ld);
@@ -1159,6 +1161,7 @@ __device__ __forceinline__ bool wa_light(const DevScene& s, const DevRequest& q,
     return true;
 }
 
+template <bool kExt>
 __global__ void __launch_bounds__(128) wa_shade(WfView v, DevScene s, AdjWave aw, uint32_t cur, uint32_t depth) {
     const uint32_t count = v.counters[kHitCount];
     uint32_t* qout = cur ? v.rayQ0 : v.rayQ1;
@@ -1203,8 +1206,8 @@ __global__ void __launch_bounds__(128) wa_shade(WfView v, DevScene s, AdjWave aw
             const Sampler smp{id.x, id.y, id.z};
             // an opacity cut-out the path passes through (the forward's decision;
             // no media, transmission being refused): the hit is not shaded
-            const bool shaded = !s.extended || enter_hit(s, smp, depth, vx, h.t, ps);
-            if (shaded && s.extended) {
+            const bool shaded = !kExt || enter_hit(s, smp, depth, vx, h.t, ps);
+            if (kExt && shaded) {
                 // radiance emitted at this hit: no BSDF value of this vertex or a
                 // later one scales it, so it leaves the radiance still to come
                 ps.radiance = V3{0.0f, 0.0f, 0.0f};
@@ -1214,14 +1217,15 @@ __global__ void __launch_bounds__(128) wa_shade(WfView v, DevScene s, AdjWave aw
                     aw.lrem[j] = make_float4(l4.x - ps.radiance.x, l4.y - ps.radiance.y, l4.z - ps.radiance.z, 0.0f);
                 }
             }
-            const uint32_t nls = light_sample_count<true>(s, q);
+            const uint32_t nls = light_sample_count<kExt>(s, q);
             // which samples the forward stages found taken and unoccluded at this vertex
             const uint32_t seen = shaded ? v.visLog[static_cast<size_t>(depth) * v.P + j] : 0u;
             for (uint32_t k = 0; k < nls; ++k) {
                 V3 ld{0.0f, 0.0f, 0.0f}, c{0.0f, 0.0f, 0.0f}, gL{0.0f, 0.0f, 0.0f}, gE{0.0f, 0.0f, 0.0f},
                     local{0.0f, 0.0f, 0.0f};
                 bool mark = false;
-                const bool ok = shaded && wa_light(s, q, a, vx, smp, depth, k, rec, ms, &ld, &c, &gL, &gE, &local, &mark);
+                const bool ok =
+                    shaded && wa_light<kExt>(s, q, a, vx, smp, depth, k, rec, ms, &ld, &c, &gL, &gE, &local, &mark);
                 const size_t e = static_cast<size_t>(k) * v.P + j;
                 v.shDir[e] = make_float4(ld.x, ld.y, ld.z, (ok && ((seen >> k) & 1u)) ? FLT_MAX : 0.0f);
                 v.shC[e] = make_float4(c.x, c.y, c.z, 0.0f);
@@ -1305,6 +1309,7 @@ __global__ void __launch_bounds__(128) wa_shade(WfView v, DevScene s, AdjWave aw
 }
 
 // Gradients of a shaded vertex once its light samples' visibility is known.
+template <bool kExt>
 __global__ void __launch_bounds__(128, 4) wa_shadow(WfView v, DevScene s, AdjWave aw) {
     const uint32_t count = v.counters[kHitCount];
     const AdjView& a = *aw.view;
@@ -1319,7 +1324,7 @@ __global__ void __launch_bounds__(128, 4) wa_shadow(WfView v, DevScene s, AdjWav
         const uint32_t mat = __float_as_uint(v0.w);
         const Mat& me = a.evalMats[mat];
         const V3 dT = dl * T0;
-        const V3 direct = sum_direct<true>(s, q, [&](uint32_t k, V3* c) {
+        const V3 direct = sum_direct<kExt>(s, q, [&](uint32_t k, V3* c) {
             const size_t e = static_cast<size_t>(k) * v.P + j;
             const float4 d4 = v.shDir[e];
             if (d4.w == 0.0f) return false;
@@ -1633,9 +1638,17 @@ void enqueue_replay(const Launch& L, cudaStream_t st) {
     for (uint32_t d = 0; d < L.depth; ++d) {
         const uint32_t cur = d & 1u;
         wa_hits<<<L.gAdjHits, 256, 0, st>>>(L.v, cur, d);  // no tracing: the forward stages' hits and visibility
-        wa_shade<<<L.gAdjShade, 128, 0, st>>>(L.v, L.s, L.aw, cur, d);
+        if (L.ext) {
+            wa_shade<true><<<L.gAdjShade, 128, 0, st>>>(L.v, L.s, L.aw, cur, d);
+        } else {
+            wa_shade<false><<<L.gAdjShade, 128, 0, st>>>(L.v, L.s, L.aw, cur, d);
+        }
         wa_miss<<<L.gAdjMiss, 256, 0, st>>>(L.v, L.s, L.aw, d);
-        wa_shadow<<<L.gAdjShadow, 128, 0, st>>>(L.v, L.s, L.aw);
+        if (L.ext) {
+            wa_shadow<true><<<L.gAdjShadow, 128, 0, st>>>(L.v, L.s, L.aw);
+        } else {
+            wa_shadow<false><<<L.gAdjShadow, 128, 0, st>>>(L.v, L.s, L.aw);
+        }
         wf_end_bounce<<<1, 32, 0, st>>>(L.v, cur);
     }
 }
@@ -1877,8 +1890,8 @@ int run_waves(ContextImpl* ctx, WavefrontState* wf, const ShiroWavefrontConfig& 
     L.gOcc = with_occlude_kernel(L.coopOcc, L.occRefill, L.occRegs, [&](auto kern) { return grid_for(kern, L.bShadow, wf->smCount); });
     L.gRes = grid_for(wf_resolve, 128, wf->smCount);
     L.gBin = grid_for(wf_bin_scatter, 256, wf->smCount);
-    L.gAdjShade = grid_for(wa_shade, 128, wf->smCount);
-    L.gAdjShadow = grid_for(wa_shadow, 128, wf->smCount);
+    L.gAdjShade = L.ext ? grid_for(wa_shade<true>, 128, wf->smCount) : grid_for(wa_shade<false>, 128, wf->smCount);
+    L.gAdjShadow = L.ext ? grid_for(wa_shadow<true>, 128, wf->smCount) : grid_for(wa_shadow<false>, 128, wf->smCount);
     L.gAdjMiss = grid_for(wa_miss, 256, wf->smCount);
     L.gAdjHits = grid_for(wa_hits, 256, wf->smCount);
     L.binRays = cfg.bin_rays == 1 ? 1u : 0u;
