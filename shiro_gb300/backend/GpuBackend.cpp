@@ -223,8 +223,16 @@ void CopyOut(const float* stage, FrameBuffer& fb, size_t px, size_t first, size_
         part(0, 1);
         return;
     }
+    // (also called from the render's progress callback: nothing may throw
+    // through the library, so a part whose thread cannot start runs here)
     std::vector<std::thread> pool;
-    for (unsigned t = 1; t < threads; ++t) pool.emplace_back(part, t, threads);
+    for (unsigned t = 1; t < threads; ++t) {
+        try {
+            pool.emplace_back(part, t, threads);
+        } catch (...) {
+            part(t, threads);
+        }
+    }
     part(0, threads);
     for (std::thread& th : pool) th.join();
 }
